@@ -1,0 +1,1137 @@
+/*
+ * coffe_oracle.c -- FP64 CPU restatement of COFFE's correlation-function hot
+ * path.  TEST INFRASTRUCTURE ONLY: the checker for the GPU product, never part
+ * of it.  See coffe_oracle.h for the contract and the reference citations.
+ *
+ * Build: make -C oracle  (gcc -O2 -fopenmp -ffp-contract=off, shared library)
+ */
+#include "coffe_oracle.h"
+
+#include <complex.h>
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "gk61_table.h"
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+#define OR_SQRT_PI 1.7724538509055160272981674833411451827975494561224
+#define OR_H0 (1. / 2997.92458) /* H0 in h/Mpc, common.h:76 */
+#define OR_QAG_LIMIT 50000      /* COFFE_MAX_INTSPACE, common.h:72 */
+
+/* ======================================================================
+ * splines (GSL interp semantics: binary search, NaN outside [x0, x_{n-1}])
+ * ====================================================================== */
+
+static size_t or_bsearch(const double *x, size_t n, double v)
+{
+    size_t lo = 0, hi = n - 1;
+    while (hi > lo + 1) {
+        size_t mid = (lo + hi) / 2;
+        if (x[mid] > v)
+            hi = mid;
+        else
+            lo = mid;
+    }
+    return lo;
+}
+
+/* natural cubic spline: tridiagonal system for c_i = y''_i / 2, c_0 = c_{n-1} = 0 */
+static int cspline_coeffs(const double *x, const double *y, size_t n, double *b,
+                          double *c_int, double *d)
+{
+    double *c = (double *)calloc(n, sizeof(double));
+    size_t m = n - 2;
+    if (!c)
+        return -1;
+    if (m > 0) {
+        double *diag = (double *)malloc(sizeof(double) * m);
+        double *off = (double *)malloc(sizeof(double) * m);
+        double *rhs = (double *)malloc(sizeof(double) * m);
+        for (size_t i = 0; i < m; ++i) {
+            const double h_i = x[i + 1] - x[i];
+            const double h_ip1 = x[i + 2] - x[i + 1];
+            const double g_i = 1.0 / h_i, g_ip1 = 1.0 / h_ip1;
+            off[i] = h_ip1;
+            diag[i] = 2.0 * (h_ip1 + h_i);
+            rhs[i] = 3.0 * ((y[i + 2] - y[i + 1]) * g_ip1 - (y[i + 1] - y[i]) * g_i);
+        }
+        /* Thomas algorithm for the symmetric tridiagonal system */
+        for (size_t i = 1; i < m; ++i) {
+            const double w = off[i - 1] / diag[i - 1];
+            diag[i] -= w * off[i - 1];
+            rhs[i] -= w * rhs[i - 1];
+        }
+        c[m] = rhs[m - 1] / diag[m - 1];
+        for (size_t i = m - 1; i-- > 0;)
+            c[i + 1] = (rhs[i] - off[i] * c[i + 2]) / diag[i];
+        free(diag);
+        free(off);
+        free(rhs);
+    }
+    for (size_t i = 0; i + 1 < n; ++i) {
+        const double h = x[i + 1] - x[i];
+        const double dy = y[i + 1] - y[i];
+        b[i] = dy / h - h * (c[i + 1] + 2.0 * c[i]) / 3.0;
+        c_int[i] = c[i];
+        d[i] = (c[i + 1] - c[i]) / (3.0 * h);
+    }
+    free(c);
+    return 0;
+}
+
+/* Akima (1970) with linearly extrapolated end slopes (the non-periodic rule) */
+static int akima_coeffs(const double *x, const double *y, size_t n, double *b,
+                        double *c, double *d)
+{
+    /* m[k + 2] holds the secant slope m_k, k = -2 .. n */
+    double *mm = (double *)malloc(sizeof(double) * (n + 3));
+    double *t = (double *)malloc(sizeof(double) * n);
+    if (!mm || !t) {
+        free(mm);
+        free(t);
+        return -1;
+    }
+    double *m = mm + 2;
+    for (size_t i = 0; i + 1 < n; ++i)
+        m[i] = (y[i + 1] - y[i]) / (x[i + 1] - x[i]);
+    m[-1] = 2.0 * m[0] - m[1];
+    m[-2] = 3.0 * m[0] - 2.0 * m[1];
+    m[n - 1] = 2.0 * m[n - 2] - m[n - 3];
+    m[n] = 3.0 * m[n - 2] - 2.0 * m[n - 3];
+    for (size_t i = 0; i < n; ++i) {
+        const long k = (long)i;
+        const double w1 = fabs(m[k + 1] - m[k]);
+        const double w2 = fabs(m[k - 1] - m[k - 2]);
+        const double ne = w1 + w2;
+        if (ne == 0.0)
+            t[i] = 0.5 * (m[k - 1] + m[k]);
+        else
+            t[i] = (w1 * m[k - 1] + w2 * m[k]) / ne;
+    }
+    for (size_t i = 0; i + 1 < n; ++i) {
+        const double h = x[i + 1] - x[i];
+        b[i] = t[i];
+        c[i] = (3.0 * m[i] - 2.0 * t[i] - t[i + 1]) / h;
+        d[i] = (t[i] + t[i + 1] - 2.0 * m[i]) / (h * h);
+    }
+    free(mm);
+    free(t);
+    return 0;
+}
+
+int or_spline_coeffs(int type, const double *x, const double *y, size_t n, double *b,
+                     double *c, double *d)
+{
+    if (type == OR_CSPLINE) {
+        if (n < 3)
+            return -1;
+        return cspline_coeffs(x, y, n, b, c, d);
+    }
+    if (type == OR_AKIMA) {
+        if (n < 5)
+            return -1;
+        return akima_coeffs(x, y, n, b, c, d);
+    }
+    if (type == OR_LINEAR) {
+        if (n < 2)
+            return -1;
+        for (size_t i = 0; i + 1 < n; ++i) {
+            b[i] = (y[i + 1] - y[i]) / (x[i + 1] - x[i]);
+            c[i] = 0.0;
+            d[i] = 0.0;
+        }
+        return 0;
+    }
+    return -1;
+}
+
+int or_spline_init(or_spline_t *s, const double *x, const double *y, size_t n, int type)
+{
+    memset(s, 0, sizeof(*s));
+    if (n < 2)
+        return -1;
+    s->n = n;
+    s->type = type;
+    s->x = (double *)malloc(sizeof(double) * n);
+    s->y = (double *)malloc(sizeof(double) * n);
+    s->b = (double *)malloc(sizeof(double) * n);
+    s->c = (double *)malloc(sizeof(double) * n);
+    s->d = (double *)malloc(sizeof(double) * n);
+    if (!s->x || !s->y || !s->b || !s->c || !s->d) {
+        or_spline_free(s);
+        return -1;
+    }
+    memcpy(s->x, x, sizeof(double) * n);
+    memcpy(s->y, y, sizeof(double) * n);
+    if (or_spline_coeffs(type, x, y, n, s->b, s->c, s->d) != 0) {
+        or_spline_free(s);
+        return -1;
+    }
+    return 0;
+}
+
+double or_spline_eval(const or_spline_t *s, double v)
+{
+    if (!(v >= s->x[0] && v <= s->x[s->n - 1]))
+        return NAN;
+    const size_t i = or_bsearch(s->x, s->n, v);
+    const double dx = v - s->x[i];
+    return s->y[i] + dx * (s->b[i] + dx * (s->c[i] + s->d[i] * dx));
+}
+
+void or_spline_free(or_spline_t *s)
+{
+    free(s->x);
+    free(s->y);
+    free(s->b);
+    free(s->c);
+    free(s->d);
+    memset(s, 0, sizeof(*s));
+}
+
+int or_spline_eval_array(int type, const double *x, const double *y, size_t n,
+                         const double *xq, double *yq, size_t nq)
+{
+    or_spline_t s;
+    if (or_spline_init(&s, x, y, n, type) != 0)
+        return -1;
+    for (size_t i = 0; i < nq; ++i)
+        yq[i] = or_spline_eval(&s, xq[i]);
+    or_spline_free(&s);
+    return 0;
+}
+
+/* ======================================================================
+ * QUADPACK QAG with the 61-point Gauss-Kronrod rule
+ * ====================================================================== */
+
+static double rescale_error(double err, double result_abs, double result_asc)
+{
+    err = fabs(err);
+    if (result_asc != 0 && err != 0) {
+        const double scale = pow((200 * err / result_asc), 1.5);
+        if (scale < 1)
+            err = result_asc * scale;
+        else
+            err = result_asc;
+    }
+    if (result_abs > DBL_MIN / (50 * DBL_EPSILON)) {
+        const double min_err = 50 * DBL_EPSILON * result_abs;
+        if (min_err > err)
+            err = min_err;
+    }
+    return err;
+}
+
+double or_qk61(or_fn f, void *p, double a, double b, double *abserr, double *resabs,
+               double *resasc)
+{
+    double fv1[30], fv2[30];
+    const double center = 0.5 * (a + b);
+    const double half_length = 0.5 * (b - a);
+    const double abs_half_length = fabs(half_length);
+    const double f_center = f(center, p);
+    double result_gauss = 0;
+    double result_kronrod = f_center * OR_GK61_WGK[30];
+    double result_abs = fabs(result_kronrod);
+    for (int j = 0; j < 15; ++j) {
+        const int jtw = 2 * j + 1;
+        const double abscissa = half_length * OR_GK61_XGK[jtw];
+        const double fval1 = f(center - abscissa, p);
+        const double fval2 = f(center + abscissa, p);
+        const double fsum = fval1 + fval2;
+        fv1[jtw] = fval1;
+        fv2[jtw] = fval2;
+        result_gauss += OR_GK61_WG[j] * fsum;
+        result_kronrod += OR_GK61_WGK[jtw] * fsum;
+        result_abs += OR_GK61_WGK[jtw] * (fabs(fval1) + fabs(fval2));
+    }
+    for (int j = 0; j < 15; ++j) {
+        const int jtwm1 = 2 * j;
+        const double abscissa = half_length * OR_GK61_XGK[jtwm1];
+        const double fval1 = f(center - abscissa, p);
+        const double fval2 = f(center + abscissa, p);
+        fv1[jtwm1] = fval1;
+        fv2[jtwm1] = fval2;
+        result_kronrod += OR_GK61_WGK[jtwm1] * (fval1 + fval2);
+        result_abs += OR_GK61_WGK[jtwm1] * (fabs(fval1) + fabs(fval2));
+    }
+    const double mean = result_kronrod * 0.5;
+    double result_asc = OR_GK61_WGK[30] * fabs(f_center - mean);
+    for (int j = 0; j < 30; ++j)
+        result_asc += OR_GK61_WGK[j] * (fabs(fv1[j] - mean) + fabs(fv2[j] - mean));
+    const double err = (result_kronrod - result_gauss) * half_length;
+    result_kronrod *= half_length;
+    result_abs *= abs_half_length;
+    result_asc *= abs_half_length;
+    *resabs = result_abs;
+    *resasc = result_asc;
+    *abserr = rescale_error(err, result_abs, result_asc);
+    return result_kronrod;
+}
+
+static int subinterval_too_small(double a1, double a2, double b2)
+{
+    const double e = DBL_EPSILON, u = DBL_MIN;
+    const double tmp = (1 + 100 * e) * (fabs(a2) + 1000 * u);
+    return fabs(a1) <= tmp && fabs(b2) <= tmp;
+}
+
+static _Thread_local int or_tl_intervals = 0;
+
+int or_last_qag_intervals(void) { return or_tl_intervals; }
+
+double or_qag61(or_fn f, void *p, double a, double b, double epsabs, double epsrel,
+                size_t limit, double *abserr_out, int *status)
+{
+    double result0, abserr0, resabs0, resasc0;
+    int st = 0;
+    result0 = or_qk61(f, p, a, b, &abserr0, &resabs0, &resasc0);
+    double tolerance = fmax(epsabs, epsrel * fabs(result0));
+    const double round_off = 50 * DBL_EPSILON * resabs0;
+    or_tl_intervals = 1;
+    if (abserr0 <= round_off && abserr0 > tolerance) {
+        if (abserr_out)
+            *abserr_out = abserr0;
+        if (status)
+            *status = 2;
+        return result0;
+    } else if ((abserr0 <= tolerance && abserr0 != resasc0) || abserr0 == 0.0) {
+        if (abserr_out)
+            *abserr_out = abserr0;
+        if (status)
+            *status = 0;
+        return result0;
+    } else if (limit == 1) {
+        if (abserr_out)
+            *abserr_out = abserr0;
+        if (status)
+            *status = 1;
+        return result0;
+    }
+    size_t cap = 64;
+    double *al = (double *)malloc(sizeof(double) * cap);
+    double *bl = (double *)malloc(sizeof(double) * cap);
+    double *rl = (double *)malloc(sizeof(double) * cap);
+    double *el = (double *)malloc(sizeof(double) * cap);
+    size_t size = 1;
+    al[0] = a;
+    bl[0] = b;
+    rl[0] = result0;
+    el[0] = abserr0;
+    double area = result0, errsum = abserr0;
+    int roundoff_type1 = 0, roundoff_type2 = 0, error_type = 0;
+    size_t iteration = 1;
+    do {
+        size_t imax = 0;
+        for (size_t i = 1; i < size; ++i)
+            if (el[i] > el[imax])
+                imax = i;
+        const double a_i = al[imax], b_i = bl[imax], r_i = rl[imax], e_i = el[imax];
+        const double a1 = a_i, b1 = 0.5 * (a_i + b_i), a2 = b1, b2 = b_i;
+        double error1, error2, resabs1, resabs2, resasc1, resasc2;
+        const double area1 = or_qk61(f, p, a1, b1, &error1, &resabs1, &resasc1);
+        const double area2 = or_qk61(f, p, a2, b2, &error2, &resabs2, &resasc2);
+        const double area12 = area1 + area2;
+        const double error12 = error1 + error2;
+        errsum += (error12 - e_i);
+        area += area12 - r_i;
+        if (resasc1 != error1 && resasc2 != error2) {
+            const double delta = r_i - area12;
+            if (fabs(delta) <= 1.0e-5 * fabs(area12) && error12 >= 0.99 * e_i)
+                roundoff_type1++;
+            if (iteration >= 10 && error12 > e_i)
+                roundoff_type2++;
+        }
+        tolerance = fmax(epsabs, epsrel * fabs(area));
+        if (errsum > tolerance) {
+            if (roundoff_type1 >= 6 || roundoff_type2 >= 20)
+                error_type = 2;
+            if (subinterval_too_small(a1, a2, b2))
+                error_type = 3;
+        }
+        if (size == cap) {
+            cap *= 2;
+            al = (double *)realloc(al, sizeof(double) * cap);
+            bl = (double *)realloc(bl, sizeof(double) * cap);
+            rl = (double *)realloc(rl, sizeof(double) * cap);
+            el = (double *)realloc(el, sizeof(double) * cap);
+        }
+        al[imax] = a1;
+        bl[imax] = b1;
+        rl[imax] = area1;
+        el[imax] = error1;
+        al[size] = a2;
+        bl[size] = b2;
+        rl[size] = area2;
+        el[size] = error2;
+        size++;
+        iteration++;
+    } while (iteration < limit && !error_type && errsum > tolerance);
+    double result = 0;
+    for (size_t i = 0; i < size; ++i)
+        result += rl[i];
+    if (error_type)
+        st = error_type;
+    else if (iteration >= limit && errsum > tolerance)
+        st = 1;
+    or_tl_intervals = (int)size;
+    free(al);
+    free(bl);
+    free(rl);
+    free(el);
+    if (abserr_out)
+        *abserr_out = errsum;
+    if (status)
+        *status = st;
+    return result;
+}
+
+int or_gauss_legendre(size_t n, double *x, double *w)
+{
+    if (n == 0)
+        return -1;
+    for (size_t i = 0; i < (n + 1) / 2; ++i) {
+        double z = cos(M_PI * ((double)i + 0.75) / ((double)n + 0.5));
+        double pp = 0.0;
+        for (int it = 0; it < 100; ++it) {
+            double p1 = 1.0, p2 = 0.0;
+            for (size_t j = 1; j <= n; ++j) {
+                const double p3 = p2;
+                p2 = p1;
+                p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / (double)j;
+            }
+            pp = (double)n * (z * p1 - p2) / (z * z - 1.0);
+            const double z1 = z;
+            z = z1 - p1 / pp;
+            if (fabs(z - z1) <= 1e-16)
+                break;
+        }
+        x[i] = -z;
+        x[n - 1 - i] = z;
+        w[i] = 2.0 / ((1.0 - z * z) * pp * pp);
+        w[n - 1 - i] = w[i];
+    }
+    return 0;
+}
+
+/* ======================================================================
+ * special functions
+ * ====================================================================== */
+
+/* Lanczos approximation, g = 7, 9 terms, as twofast_lgamma (twofast.c:97-144) */
+static const double or_lanczos_coeff[8] = {
+    676.5203681218851,     -1259.1392167224028,  771.32342877765313,
+    -176.61502916214059,   12.507343278686905,   -0.13857109526572012,
+    9.9843695780195716e-6, 1.5056327351493116e-7};
+
+static double complex or_lgamma_cplx(double complex z)
+{
+    if (creal(z) < 0.5)
+        return log(M_PI) - clog(csin(M_PI * z)) - or_lgamma_cplx(1. - z);
+    double complex x = 0.99999999999980993;
+    z -= 1;
+    for (int i = 0; i < 8; ++i)
+        x += or_lanczos_coeff[i] / (z + (double)i + 1.);
+    const double complex t = z + 8 - 0.5;
+    return log(2 * M_PI) / 2. + (z + 0.5) * clog(t) - t + clog(x);
+}
+
+void or_lgamma_c(double zr, double zi, double *rr, double *ri)
+{
+    const double complex r = or_lgamma_cplx(zr + I * zi);
+    *rr = creal(r);
+    *ri = cimag(r);
+}
+
+double or_legendre(int l, double x)
+{
+    if (l == 0)
+        return 1.0;
+    if (l == 1)
+        return x;
+    double p0 = 1.0, p1 = x;
+    for (int k = 2; k <= l; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / (double)k;
+        p0 = p1;
+        p1 = p2;
+    }
+    return p1;
+}
+
+/* j_l(x): ascending series for x below l + 1 (and below 1), else upward
+   recurrence from the closed forms of j_0 and j_1 (stable for x > l). */
+double or_sph_bessel(int l, double x)
+{
+    if (x < 0)
+        return (l % 2 ? -1.0 : 1.0) * or_sph_bessel(l, -x);
+    const double thr = (l < 1 ? 1.0 : (double)l + 1.0);
+    if (x < thr) {
+        /* x^l / (2l+1)!! * sum_k (-x^2/2)^k / (k! (2l+3)(2l+5)...(2l+2k+1)) */
+        double pref = 1.0;
+        for (int k = 1; k <= l; ++k)
+            pref *= x / (2.0 * k + 1.0);
+        const double y = -0.5 * x * x;
+        double term = 1.0, sum = 1.0;
+        for (int k = 1; k < 200; ++k) {
+            term *= y / ((double)k * (2.0 * l + 2.0 * k + 1.0));
+            sum += term;
+            if (fabs(term) < 1e-17 * fabs(sum))
+                break;
+        }
+        return pref * sum;
+    }
+    const double s = sin(x), c = cos(x);
+    double j0 = s / x;
+    if (l == 0)
+        return j0;
+    double j1 = (s / x - c) / x;
+    for (int k = 1; k < l; ++k) {
+        const double j2 = (2.0 * k + 1.0) / x * j1 - j0;
+        j0 = j1;
+        j1 = j2;
+    }
+    return j1;
+}
+
+/* ======================================================================
+ * FFT: recursive mixed-radix decimation in time, any length
+ * ====================================================================== */
+
+static void fft_rec(const double *xr, const double *xi, size_t stride, size_t n,
+                    double *yr, double *yi, const double *wr, const double *wi,
+                    size_t N)
+{
+    if (n == 1) {
+        yr[0] = xr[0];
+        yi[0] = xi[0];
+        return;
+    }
+    size_t p = 0;
+    for (size_t f = 2; f * f <= n; ++f)
+        if (n % f == 0) {
+            p = f;
+            break;
+        }
+    if (p == 0)
+        p = n;
+    const size_t m = n / p;
+    for (size_t r = 0; r < p; ++r)
+        fft_rec(xr + r * stride, xi + r * stride, stride * p, m, yr + r * m, yi + r * m,
+                wr, wi, N);
+    double *tr = (double *)malloc(sizeof(double) * n);
+    double *ti = (double *)malloc(sizeof(double) * n);
+    const size_t step = N / n;
+    for (size_t k = 0; k < m; ++k) {
+        for (size_t q = 0; q < p; ++q) {
+            const size_t kk = k + q * m;
+            double sr = 0, si = 0;
+            for (size_t r = 0; r < p; ++r) {
+                const size_t e = ((r * kk) % n) * step;
+                const double ar = yr[r * m + k], ai = yi[r * m + k];
+                sr += ar * wr[e] - ai * wi[e];
+                si += ar * wi[e] + ai * wr[e];
+            }
+            tr[kk] = sr;
+            ti[kk] = si;
+        }
+    }
+    memcpy(yr, tr, sizeof(double) * n);
+    memcpy(yi, ti, sizeof(double) * n);
+    free(tr);
+    free(ti);
+}
+
+int or_fft(double *re, double *im, size_t n, int sign)
+{
+    if (n == 0)
+        return -1;
+    double *wr = (double *)malloc(sizeof(double) * n);
+    double *wi = (double *)malloc(sizeof(double) * n);
+    double *yr = (double *)malloc(sizeof(double) * n);
+    double *yi = (double *)malloc(sizeof(double) * n);
+    for (size_t j = 0; j < n; ++j) {
+        const double ang = 2.0 * M_PI * (double)j / (double)n;
+        wr[j] = cos(ang);
+        wi[j] = (sign < 0 ? -1.0 : 1.0) * sin(ang);
+    }
+    fft_rec(re, im, 1, n, yr, yi, wr, wi, n);
+    memcpy(re, yr, sizeof(double) * n);
+    memcpy(im, yi, sizeof(double) * n);
+    free(wr);
+    free(wi);
+    free(yr);
+    free(yi);
+    return 0;
+}
+
+/* ======================================================================
+ * FFTLog (twofast.c)
+ * ====================================================================== */
+
+static double twofast_window(double value, double xmin, double xmax, double xleft,
+                             double xright)
+{
+    /* twofast.c:54-90 */
+    double result;
+    if (value > xleft && value < xright && value > xmin && value < xmax)
+        result = 1.0;
+    else if (value <= xmin || value >= xmax)
+        result = 0.0;
+    else {
+        if (value <= xleft)
+            result = (value - xmin) / (xleft - xmin);
+        else
+            result = (xmax - value) / (xmax - xright);
+        result = result - sin(2 * M_PI * result) / 2. / M_PI;
+    }
+    return result;
+}
+
+double or_twofast_selectqnu(double l, double nu)
+{
+    const double n1 = 0.9, n2 = 0.9999;
+    const double qmin = fmax(n2 - 1.0 - nu, -l);
+    const double qmax = fmin(n1 + 3.0 - nu, 2.0);
+    const double qbest = (2. + n1 + n2) / 2. - nu;
+    double q = qbest;
+    if (!(qmin < q && q < qmax))
+        q = (qmin + 2. * qmax) / 3.;
+    return q;
+}
+
+/* twofast_mql (twofast.c:196-224).  The reflection branch of the Lanczos
+   log-Gamma overflows csin for |Im(pi z)| above ~710; the reference then gets
+   lnGamma = -inf and the mode's coefficient becomes exactly zero.  That
+   behaviour is kept. */
+static double complex twofast_mql(double t, double q, double l, double alpha)
+{
+    const double complex n = q - 1. - t * I;
+    const double complex unl =
+        cpow(2, n - 1.) * OR_SQRT_PI *
+        cexp(or_lgamma_cplx((1. + l + n) / 2.) - or_lgamma_cplx((2. + l - n) / 2.));
+    if (isfinite(creal(unl)) && isfinite(cimag(unl)))
+        return cpow(alpha, t * I - q) * unl;
+    return NAN;
+}
+
+int or_twofast_1bessel(double *out_x, double *out_y, size_t N, const double *in_x,
+                       const double *in_y, size_t in_len, double l, double nu,
+                       double r0, double k0, double kmin, double kmax)
+{
+    if (N < 4 || in_len < 3)
+        return -1;
+    const size_t N2 = N / 2 + 1;
+    const double qnu = or_twofast_selectqnu(l, nu);
+    const double G = log(kmax / kmin);
+    const double q = qnu + nu;
+    or_spline_t sp;
+    if (or_spline_init(&sp, in_x, in_y, in_len, OR_CSPLINE) != 0)
+        return -1;
+    /* twofast_fft_input (twofast.c:252-360) */
+    const double L = 2 * M_PI * N / log(kmax / kmin);
+    double *xmod = (double *)malloc(sizeof(double) * N);
+    double *re = (double *)malloc(sizeof(double) * N);
+    double *im = (double *)malloc(sizeof(double) * N);
+    const double xmax_w = k0 * pow(kmax / kmin, (double)(N - 1) / N);
+    const double xleft_w = exp(0.46) * kmin;
+    const double xright_w = exp(-0.46) * k0 * pow(kmax / kmin, (double)(N - 1) / N);
+    for (size_t i = 0; i < N; ++i)
+        xmod[i] = k0 * pow(kmax / kmin, (double)i / N);
+    for (size_t i = 0; i < N; ++i) {
+        const double ki = k0 * pow(kmax / kmin, (double)i / N);
+        re[i] = pow(kmax / kmin, (3. - q) * i / N) * or_spline_eval(&sp, ki) *
+                twofast_window(ki, kmin, xmax_w, xleft_w, xright_w);
+        im[i] = 0.0;
+    }
+    or_spline_free(&sp);
+    or_fft(re, im, N, -1);
+    double complex *c = (double complex *)malloc(sizeof(double complex) * N2);
+    for (size_t i = 0; i < N2; ++i) {
+        const double w = twofast_window(xmod[N2 - 2 + i], kmin, xmax_w, xleft_w, xright_w);
+        c[i] = w * conj(re[i] + I * im[i]) / L;
+    }
+    /* multiply by the Gamma-ratio kernel (twofast.c:426-446) */
+    for (size_t i = 0; i < N2; ++i)
+        c[i] = c[i] * twofast_mql(2 * M_PI * i / G, qnu, l, k0 * r0);
+    /* c2r (FFTW semantics: Hermitian extension, imaginary parts of DC and
+       Nyquist ignored), twofast.c:448-465 */
+    for (size_t i = 0; i < N2; ++i) {
+        re[i] = creal(c[i]);
+        im[i] = cimag(c[i]);
+    }
+    im[0] = 0.0;
+    if (N % 2 == 0)
+        im[N / 2] = 0.0;
+    for (size_t i = N2; i < N; ++i) {
+        re[i] = re[N - i];
+        im[i] = -im[N - i];
+    }
+    or_fft(re, im, N, +1);
+    for (size_t i = 0; i < N; ++i) {
+        out_x[i] = r0 * pow(kmax / kmin, (double)i / N);
+        const double pref =
+            k0 * k0 * k0 * pow(kmax / kmin, -((qnu + nu) * i / N)) / M_PI / pow(r0 * k0, nu) / G;
+        out_y[i] = re[i] * pref;
+    }
+    free(c);
+    free(xmod);
+    free(re);
+    free(im);
+    return 0;
+}
+
+/* ======================================================================
+ * I_l^n tables (integrals.c)
+ * ====================================================================== */
+
+static const double or_min_sep[OR_N_SMALL_R] = {
+    /* integrals.c:111-126: the sub-Mpc separations evaluated by direct quadrature */
+    1E-6,   1E-5,   1E-4,  1E-3,    2E-3,  5E-3,   7E-3,   8E-3,  9E-3,   1E-2,   1.1E-2,
+    1.2E-2, 1.25E-2, 1.3E-2, 1.35E-2, 1.5E-2, 2E-2, 2.5E-2, 3E-2,  3.5E-2, 5E-2,   7E-2,
+    8E-2,   9E-2,   1E-1,  1.1E-1,  1.2E-1, 1.25E-1, 1.3E-1, 1.35E-1, 1.5E-1, 1.75E-1, 2E-1,
+    2.5E-1, 3E-1,   3.5E-1, 4E-1,   5E-1,  6E-1,   7E-1,   8E-1,  9E-1};
+
+typedef struct {
+    const or_spline_t *pk;
+    double r;
+    int n, l;
+} or_bessel_par_t;
+
+static double bessel_integrand(double k, void *vp)
+{
+    /* integrals.c:280-325 (integer n, l) */
+    const or_bessel_par_t *p = (const or_bessel_par_t *)vp;
+    const double bf = or_sph_bessel(p->l, k * p->r) / pow(k * p->r, (double)p->n);
+    return k * k * or_spline_eval(p->pk, k) * bf;
+}
+
+static double prefactor_integrand(double k, void *vp)
+{
+    /* integrals.c:238-269 */
+    const or_bessel_par_t *p = (const or_bessel_par_t *)vp;
+    return pow(k, 2.0 + p->l - p->n) * or_spline_eval(p->pk, k);
+}
+
+static double integrate_function(or_fn func, const or_spline_t *pk, int n, int l,
+                                 double sep, double kmin, double kmax)
+{
+    /* integrals.c:333-383 */
+    or_bessel_par_t p = {pk, sep, n, l};
+    const double result = or_qag61(func, &p, kmin, kmax, 0, 1e-5, OR_QAG_LIMIT, NULL, NULL);
+    double output;
+    if (n >= l && sep > 0)
+        output = result * pow(sep, (double)(n - l));
+    else
+        output = result;
+    return output / 2. / M_PI / M_PI;
+}
+
+double or_integral_direct(const double *k, const double *pk, size_t nk, int n, int l,
+                          double r, double kmin, double kmax)
+{
+    or_spline_t sp;
+    if (or_spline_init(&sp, k, pk, nk, OR_AKIMA) != 0)
+        return NAN;
+    const double v = integrate_function(bessel_integrand, &sp, n, l, r, kmin, kmax);
+    or_spline_free(&sp);
+    return v;
+}
+
+int or_integral_table(const double *k, const double *pk, size_t nk, int n, int l,
+                      size_t N, double kmin, double kmax, int with_small_r,
+                      double *out_x, double *out_y)
+{
+    /* integrals.c:459-573 */
+    const size_t off = OR_N_SMALL_R + 1;
+    double *fx = out_x + off, *fy = out_y + off;
+    if (or_twofast_1bessel(fx, fy, N, k, pk, nk, (double)l, (double)n, 1.0, kmin, kmin,
+                           kmax) != 0)
+        return -1;
+    if (n >= l)
+        for (size_t i = 0; i < N; ++i)
+            fy[i] = fy[i] * pow(fx[i], (double)(n - l));
+    out_x[0] = 0.0;
+    for (size_t i = 1; i <= OR_N_SMALL_R; ++i)
+        out_x[i] = or_min_sep[i - 1];
+    if (!with_small_r) {
+        for (size_t i = 0; i < off; ++i)
+            out_y[i] = NAN;
+        return 0;
+    }
+    or_spline_t sp;
+    if (or_spline_init(&sp, k, pk, nk, OR_AKIMA) != 0)
+        return -1;
+    if (n >= l) {
+        const double coeff = sqrt(M_PI / 2.) / pow(2, l + 0.5) / tgamma(l + 1.5);
+        out_y[0] = integrate_function(prefactor_integrand, &sp, n, l, 0, kmin, kmax) * coeff;
+    } else {
+        out_y[0] = 0.0;
+    }
+    for (size_t i = 1; i <= OR_N_SMALL_R; ++i)
+        out_y[i] = integrate_function(bessel_integrand, &sp, n, l, out_x[i], kmin, kmax);
+    or_spline_free(&sp);
+    return 0;
+}
+
+/* ======================================================================
+ * background (background.c:301-696), flat LCDM: w = -1, wint = 1
+ * ====================================================================== */
+
+#define OR_XINT_BINS 16384
+#define OR_XINT_ZMAX 100.0
+#define OR_ODE_HMAX 2.5e-4
+
+typedef struct {
+    double om; /* Omega0_cdm + Omega0_baryon */
+    double og, ode;
+} or_bgpar_t;
+
+/* x(z) = Om/(1-Om) (1+z)^3 through the linear spline on the 16385-point grid
+   of background.c:337-412 */
+static double xint_lin(const or_bgpar_t *p, double z)
+{
+    const double dz = OR_XINT_ZMAX / OR_XINT_BINS;
+    const double ratio = p->om / (1.0 - p->om);
+    double u = z / dz;
+    size_t i = (size_t)u;
+    if (i >= OR_XINT_BINS)
+        i = OR_XINT_BINS - 1;
+    const double z0 = OR_XINT_ZMAX * (double)i / OR_XINT_BINS;
+    const double z1 = OR_XINT_ZMAX * (double)(i + 1) / OR_XINT_BINS;
+    const double x0 = ratio * (1 + z0) * (1 + z0) * (1 + z0);
+    const double x1 = ratio * (1 + z1) * (1 + z1) * (1 + z1);
+    return x0 + (z - z0) * ((x1 - x0) / (z1 - z0));
+}
+
+static void growth_rhs(const or_bgpar_t *p, double a, const double y[2], double f[2])
+{
+    /* growth_rate_ode, background.c:190-211, with w = -1 */
+    const double z = 1. / a - 1;
+    const double w = -1.0;
+    const double x = xint_lin(p, z);
+    f[0] = y[1];
+    f[1] = -3. / 2 * (1 - w / (1 + x)) * y[1] / a + 3. / 2 * x / (1 + x) * y[0] / (a * a);
+}
+
+static void growth_integrate(const or_bgpar_t *p, double a_end, double y[2])
+{
+    const double a0 = 0.05;
+    y[0] = 0.05;
+    y[1] = 1.0;
+    if (!(a_end > a0))
+        return;
+    const size_t nstep = (size_t)ceil((a_end - a0) / OR_ODE_HMAX);
+    const double h = (a_end - a0) / (double)nstep;
+    for (size_t s = 0; s < nstep; ++s) {
+        const double a = a0 + h * (double)s;
+        double k1[2], k2[2], k3[2], k4[2], t[2];
+        growth_rhs(p, a, y, k1);
+        t[0] = y[0] + 0.5 * h * k1[0];
+        t[1] = y[1] + 0.5 * h * k1[1];
+        growth_rhs(p, a + 0.5 * h, t, k2);
+        t[0] = y[0] + 0.5 * h * k2[0];
+        t[1] = y[1] + 0.5 * h * k2[1];
+        growth_rhs(p, a + 0.5 * h, t, k3);
+        t[0] = y[0] + h * k3[0];
+        t[1] = y[1] + h * k3[1];
+        growth_rhs(p, a + h, t, k4);
+        y[0] += h / 6.0 * (k1[0] + 2.0 * k2[0] + 2.0 * k3[0] + k4[0]);
+        y[1] += h / 6.0 * (k1[1] + 2.0 * k2[1] + 2.0 * k3[1] + k4[1]);
+    }
+}
+
+static double comoving_integrand(double z, void *vp)
+{
+    /* integrand_comoving, background.c:281-296 */
+    const or_bgpar_t *p = (const or_bgpar_t *)vp;
+    return 1. / sqrt(p->om * pow(1 + z, 3) + p->og * pow(1 + z, 4) + p->ode * 1.0);
+}
+
+int or_background_nodes(const or_cosmo_t *c, size_t bins, double *z, double *a,
+                        double *Hz, double *confH, double *confHp, double *D1,
+                        double *f, double *chi, double *D1_unnormalised)
+{
+    if (bins < 5)
+        return -1;
+    or_bgpar_t p;
+    p.om = c->Omega0_cdm + c->Omega0_baryon;
+    p.og = c->Omega0_gamma;
+    p.ode = c->Omega0_de;
+    double *Dtmp = (double *)malloc(sizeof(double) * bins);
+    double *ftmp = (double *)malloc(sizeof(double) * bins);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (long li = 0; li < (long)bins; ++li) {
+        const size_t i = (size_t)li;
+        const double zi = 15. * i / (double)(bins - 1);
+        const double ai = 1. / (1. + zi);
+        double y[2];
+        growth_integrate(&p, ai, y);
+        Dtmp[i] = y[0];
+        ftmp[i] = y[1] * ai / y[0];
+        const double Hi =
+            sqrt(p.om * pow(1 + zi, 3) + p.og * pow(1 + zi, 4) + p.ode * 1.0) * c->h * OR_H0;
+        if (z)
+            z[i] = zi;
+        if (a)
+            a[i] = ai;
+        if (Hz)
+            Hz[i] = Hi;
+        if (confH)
+            confH[i] = ai * Hi;
+        if (confHp)
+            confHp[i] = -(pow(1 + zi, 3) * (2 * (1 + zi) * p.og + p.om) +
+                          (1 + 3 * (-1.0)) * p.ode * 1.0) /
+                        pow(1 + zi, 2) / 2. * pow(c->h * OR_H0, 2);
+        if (chi)
+            chi[i] = or_qag61(comoving_integrand, &p, 0., zi, 0, 1e-5, OR_QAG_LIMIT, NULL,
+                              NULL) /
+                     (c->h * OR_H0);
+    }
+    for (size_t i = 0; i < bins; ++i) {
+        if (D1_unnormalised)
+            D1_unnormalised[i] = Dtmp[i];
+        if (D1)
+            D1[i] = Dtmp[i] / Dtmp[0];
+        if (f)
+            f[i] = ftmp[i];
+    }
+    free(Dtmp);
+    free(ftmp);
+    return 0;
+}
+
+/* ======================================================================
+ * multipoles of the nonintegrated den+RSD terms
+ * ====================================================================== */
+
+#define OR_MAX_INTEGRALS 32
+
+struct or_model {
+    or_spline_t chi_of_z, z_of_chi, D1, f, a, confH;
+    or_spline_t bias[4];
+    int have_bias[4];
+    int nint;
+    int int_n[OR_MAX_INTEGRALS], int_l[OR_MAX_INTEGRALS];
+    or_spline_t integral[OR_MAX_INTEGRALS];
+    double h, Omega0_m;
+    int have_bg;
+};
+
+or_model_t *or_model_new(void)
+{
+    or_model_t *m = (or_model_t *)calloc(1, sizeof(or_model_t));
+    return m;
+}
+
+void or_model_free(or_model_t *m)
+{
+    if (!m)
+        return;
+    if (m->have_bg) {
+        or_spline_free(&m->chi_of_z);
+        or_spline_free(&m->z_of_chi);
+        or_spline_free(&m->D1);
+        or_spline_free(&m->f);
+        or_spline_free(&m->a);
+        or_spline_free(&m->confH);
+    }
+    for (int i = 0; i < 4; ++i)
+        if (m->have_bias[i])
+            or_spline_free(&m->bias[i]);
+    for (int i = 0; i < m->nint; ++i)
+        or_spline_free(&m->integral[i]);
+    free(m);
+}
+
+int or_model_set_background(or_model_t *m, const double *z, const double *chi,
+                            const double *D1, const double *f, const double *a,
+                            const double *confH, size_t bins, double h, double Omega0_m)
+{
+    if (m->have_bg) {
+        or_spline_free(&m->chi_of_z);
+        or_spline_free(&m->z_of_chi);
+        or_spline_free(&m->D1);
+        or_spline_free(&m->f);
+        or_spline_free(&m->a);
+        or_spline_free(&m->confH);
+    }
+    int e = 0;
+    e |= or_spline_init(&m->chi_of_z, z, chi, bins, OR_AKIMA);
+    e |= or_spline_init(&m->z_of_chi, chi, z, bins, OR_AKIMA);
+    e |= or_spline_init(&m->D1, z, D1, bins, OR_AKIMA);
+    e |= or_spline_init(&m->f, z, f, bins, OR_AKIMA);
+    e |= or_spline_init(&m->a, z, a, bins, OR_AKIMA);
+    e |= or_spline_init(&m->confH, z, confH, bins, OR_AKIMA);
+    m->h = h;
+    m->Omega0_m = Omega0_m;
+    m->have_bg = 1;
+    return e ? -1 : 0;
+}
+
+int or_model_set_bias(or_model_t *m, int which, const double *z, const double *v, size_t n)
+{
+    if (which < 0 || which > 3)
+        return -1;
+    if (m->have_bias[which])
+        or_spline_free(&m->bias[which]);
+    m->have_bias[which] = 0;
+    if (or_spline_init(&m->bias[which], z, v, n, OR_AKIMA) != 0)
+        return -1;
+    m->have_bias[which] = 1;
+    return 0;
+}
+
+int or_model_set_integral(or_model_t *m, int n, int l, const double *x, const double *y,
+                          size_t len)
+{
+    for (int i = 0; i < m->nint; ++i)
+        if (m->int_n[i] == n && m->int_l[i] == l) {
+            or_spline_free(&m->integral[i]);
+            return or_spline_init(&m->integral[i], x, y, len, OR_AKIMA);
+        }
+    if (m->nint >= OR_MAX_INTEGRALS)
+        return -1;
+    const int i = m->nint;
+    if (or_spline_init(&m->integral[i], x, y, len, OR_AKIMA) != 0)
+        return -1;
+    m->int_n[i] = n;
+    m->int_l[i] = l;
+    m->nint++;
+    return 0;
+}
+
+static const or_spline_t *find_integral(const or_model_t *m, int n, int l)
+{
+    for (int i = 0; i < m->nint; ++i)
+        if (m->int_n[i] == n && m->int_l[i] == l)
+            return &m->integral[i];
+    return NULL;
+}
+
+static double bias_eval(const or_model_t *m, int which, double z, double dflt)
+{
+    return m->have_bias[which] ? or_spline_eval(&m->bias[which], z) : dflt;
+}
+
+/*
+ * xi(z_mean, mu, r) of the nonintegrated den-den, rsd-rsd and den-rsd terms
+ * (functions.c:89-1484; den-den 129-229, rsd-rsd 230-362, den-rsd 670-771,
+ * D1(z1) D1(z2) factor 1463-1466), full-sky branch.
+ *
+ * The coefficients are written in terms of s = 1 - cos(theta) =
+ * r^2 (1 - mu^2) / D with D = 2 chi^2 - mu^2 r^2 / 2 = 2 chi1 chi2.  This is
+ * algebraically identical to the reference's expressions in cos(theta) and
+ * chi1/r, chi2/r, but avoids their cancellation: e.g. the I04 coefficient of
+ * rsd-rsd subtracts two terms of size (chi/r)^4 ~ 1e10 to leave O(1), losing up
+ * to six digits in FP64.  The expanded I04 polynomial is
+ *   (1-mu^2)^2 (3c^2 - 10c + 19) / 4 + 4 mu^2 (1-mu^2)(c^2 - 5c - 2)
+ *   + 4 (3c^2 - 1) mu^4          (= 8 P_4(mu) at c = 1).
+ */
+double or_xi_nonintegrated(const or_model_t *m, int contrib, double z_mean, double mu,
+                           double sep)
+{
+    const double chi_mean = or_spline_eval(&m->chi_of_z, z_mean);
+    const double chi1 = chi_mean - sep * mu / 2.;
+    const double chi2 = chi_mean + sep * mu / 2.;
+    const double mu2 = mu * mu;
+    const double omm = 1.0 - mu2;
+    const double D = 2. * chi_mean * chi_mean - mu2 * sep * sep / 2.;
+    const double s = sep * sep * omm / D;
+    const double c = 1.0 - s;
+    const double z1 = or_spline_eval(&m->z_of_chi, chi1);
+    const double z2 = or_spline_eval(&m->z_of_chi, chi2);
+    const double f1 = or_spline_eval(&m->f, z1);
+    const double f2 = or_spline_eval(&m->f, z2);
+    const double b1 = bias_eval(m, 0, z1, 1.0);
+    const double b2 = bias_eval(m, 1, z2, 1.0);
+    const or_spline_t *i00 = find_integral(m, 0, 0);
+    const or_spline_t *i02 = find_integral(m, 0, 2);
+    const or_spline_t *i04 = find_integral(m, 0, 4);
+    const double I00 = or_spline_eval(i00, sep);
+    double result = 0;
+    if (contrib & OR_CONTRIB_DEN)
+        result += b1 * b2 * I00;
+    if (contrib & OR_CONTRIB_RSD) {
+        const double I02 = or_spline_eval(i02, sep);
+        const double I04 = or_spline_eval(i04, sep);
+        const double c2 = c * c;
+        const double q4 = omm * omm * (3 * c2 - 10 * c + 19) / 4. +
+                          4 * mu2 * omm * (c2 - 5 * c - 2) + 4 * (3 * c2 - 1) * mu2 * mu2;
+        result += f1 * f2 * (1 + 2 * c2) / 15 * I00 -
+                  f1 * f2 / 21. * ((1 + 11. * c2) - 9 * c * (2 - s) * omm) * I02 +
+                  f1 * f2 * q4 / 35. * I04;
+    }
+    if ((contrib & OR_CONTRIB_DEN) && (contrib & OR_CONTRIB_RSD)) {
+        const double I02 = or_spline_eval(i02, sep);
+        const double g = (2 - s) * omm / D;
+        result += (b1 * f2 / 3. + b2 * f1 / 3.) * I00 -
+                  (b1 * f2 * (2. / 3. - g * chi1 * chi1) + b2 * f1 * (2. / 3. - g * chi2 * chi2)) *
+                      I02;
+    }
+    return result * or_spline_eval(&m->D1, z1) * or_spline_eval(&m->D1, z2);
+}
+
+typedef struct {
+    const or_model_t *m;
+    int contrib, l;
+    double z_mean, sep;
+} or_mp_par_t;
+
+static double mp_integrand(double x, void *vp)
+{
+    /* multipoles_nonintegrated_integrand, signal.c:83-111 */
+    const or_mp_par_t *p = (const or_mp_par_t *)vp;
+    const double mu = 2 * x - 1;
+    const double xi = or_xi_nonintegrated(p->m, p->contrib, p->z_mean, mu, p->sep);
+    if (p->l == 0)
+        return xi;
+    return xi * or_legendre(p->l, mu);
+}
+
+double or_multipole_nonintegrated(const or_model_t *m, int contrib, double z_mean,
+                                  double sep, int l, double epsrel)
+{
+    /* coffe_integrate(NONINTEGRATED, MULTIPOLES), signal.c:521-542 */
+    if (!(contrib & (OR_CONTRIB_DEN | OR_CONTRIB_RSD)))
+        return 0.0;
+    or_mp_par_t p = {m, contrib, l, z_mean, sep};
+    const double r = or_qag61(mp_integrand, &p, 0, 1, 0, epsrel, OR_QAG_LIMIT, NULL, NULL);
+    return (2 * l + 1) * r;
+}
+
+double or_multipole_nonintegrated_gl(const or_model_t *m, int contrib, double z_mean,
+                                     double sep, int l, size_t n_mu)
+{
+    double *x = (double *)malloc(sizeof(double) * n_mu);
+    double *w = (double *)malloc(sizeof(double) * n_mu);
+    or_gauss_legendre(n_mu, x, w);
+    double s = 0;
+    for (size_t i = 0; i < n_mu; ++i)
+        s += w[i] * or_xi_nonintegrated(m, contrib, z_mean, x[i], sep) * or_legendre(l, x[i]);
+    free(x);
+    free(w);
+    return (2 * l + 1) * 0.5 * s;
+}
+
+int or_multipoles_batch(const or_model_t *m, int contrib, const double *z_mean,
+                        const double *sep, const int *l, size_t count, double epsrel,
+                        double *out, int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads <= 0)
+        nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
+#endif
+    for (long i = 0; i < (long)count; ++i)
+        out[i] = or_multipole_nonintegrated(m, contrib, z_mean[i], sep[i], l[i], epsrel);
+    (void)nthreads;
+    return 0;
+}

@@ -1,0 +1,144 @@
+/*
+ * coffe_oracle.h -- CPU restatement of the COFFE correlation-function hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU product
+ * (coffe_gb300).  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline leg may load it; the product never links, imports or calls it.
+ *
+ * Every routine restates, in FP64 and in code written for this project, the
+ * algorithm of the reference file:line cited beside it (paths relative to the
+ * COFFE source tree).  Third-party arithmetic the reference delegates to GSL 2.7
+ * (splines, QAG) and FFTW 3.3.9 (real FFTs) is restated from the published
+ * algorithms: Akima (1970) / natural cubic splines, QUADPACK's QAG with the
+ * 61-point Gauss-Kronrod rule (Piessens et al. 1983), and a mixed-radix
+ * Cooley-Tukey DFT with FFTW's unnormalised sign conventions.
+ */
+#ifndef COFFE_ORACLE_H
+#define COFFE_ORACLE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ splines */
+/* type: 0 = natural cubic (gsl_interp_cspline), 1 = Akima (gsl_interp_akima),
+   2 = linear.  Reference: common.c:524-576 (coffe_init_spline), 704-710. */
+enum { OR_CSPLINE = 0, OR_AKIMA = 1, OR_LINEAR = 2 };
+
+typedef struct {
+    size_t n;
+    int type;
+    double *x, *y, *b, *c, *d; /* y_i + b_i dx + c_i dx^2 + d_i dx^3 */
+} or_spline_t;
+
+int or_spline_init(or_spline_t *s, const double *x, const double *y, size_t n, int type);
+double or_spline_eval(const or_spline_t *s, double x);
+void or_spline_free(or_spline_t *s);
+/* convenience for ctypes: build a spline and evaluate it at nq points */
+int or_spline_eval_array(int type, const double *x, const double *y, size_t n,
+                         const double *xq, double *yq, size_t nq);
+/* per-interval coefficients (b, c, d each n-1 long) for table comparisons */
+int or_spline_coeffs(int type, const double *x, const double *y, size_t n,
+                     double *b, double *c, double *d);
+
+/* --------------------------------------------------------------- quadrature */
+typedef double (*or_fn)(double, void *);
+/* QUADPACK QAG with GK61; common.c:1004-1040 calls gsl_integration_qag with
+   epsabs = 0, epsrel = precision, limit = 50000, key GSL_INTEG_GAUSS61. */
+double or_qag61(or_fn f, void *p, double a, double b, double epsabs, double epsrel,
+                size_t limit, double *abserr, int *status);
+/* one GK61 panel; returns the Kronrod estimate and the QUADPACK error */
+double or_qk61(or_fn f, void *p, double a, double b, double *abserr,
+               double *resabs, double *resasc);
+/* n-point Gauss-Legendre nodes/weights on [-1, 1] (Newton on P_n) */
+int or_gauss_legendre(size_t n, double *x, double *w);
+
+/* ------------------------------------------------------------- special fns */
+/* complex log-Gamma, Lanczos g=7 (twofast.c:97-144) */
+void or_lgamma_c(double zr, double zi, double *rr, double *ri);
+/* spherical Bessel j_l(x), l >= 0 (replaces gsl_sf_bessel_jl, integrals.c:309) */
+double or_sph_bessel(int l, double x);
+/* Legendre P_l (replaces gsl_sf_legendre_Pl, signal.c:109) */
+double or_legendre(int l, double x);
+
+/* --------------------------------------------------------------------- FFT */
+/* in-place complex DFT of any length; sign = -1 forward, +1 backward,
+   unnormalised (FFTW convention). */
+int or_fft(double *re, double *im, size_t n, int sign);
+
+/* ------------------------------------------------------------------ FFTLog */
+double or_twofast_selectqnu(double l, double nu);              /* twofast.c:240-250 */
+int or_twofast_1bessel(double *out_x, double *out_y, size_t N, /* twofast.c:362-483 */
+                       const double *in_x, const double *in_y, size_t in_len,
+                       double l, double nu, double r0, double k0, double kmin,
+                       double kmax);
+/* Full I_l^n table as coffe_integrals_renormalizable (integrals.c:459-573):
+   out has N + 43 points: r = 0, the 42 sub-Mpc separations (QAG), then the N
+   FFTLog points, times r^(n-l) when n >= l.  with_small_r = 0 leaves the
+   first 43 y values at NaN (x values are still filled).
+   P(k) is read through an Akima spline of (k, pk) for the direct integrals
+   and a natural cubic spline for the FFTLog resampling, as the reference does. */
+#define OR_N_SMALL_R 42
+int or_integral_table(const double *k, const double *pk, size_t nk, int n, int l,
+                      size_t N, double kmin, double kmax, int with_small_r,
+                      double *out_x, double *out_y);
+/* one direct integral (1/2pi^2) int k^2 P(k) j_l(kr)/(kr)^n dk, times r^(n-l)
+   when n >= l (integrals.c:333-383), P(k) through the Akima spline */
+double or_integral_direct(const double *k, const double *pk, size_t nk, int n, int l,
+                          double r, double kmin, double kmax);
+
+/* -------------------------------------------------------------- background */
+typedef struct {
+    double Omega0_cdm, Omega0_baryon, Omega0_gamma, Omega0_de, h;
+} or_cosmo_t;
+/* Node values at z_i = 15 i / (bins - 1) (background.c:415-537, flat LCDM,
+   w0 = -1, wa = 0).  Units: H, conformal H in 1/Mpc; chi in Mpc.  D1 is
+   normalised to 1 at z = 0.  Any output pointer may be NULL. */
+int or_background_nodes(const or_cosmo_t *c, size_t bins, double *z, double *a,
+                        double *Hz, double *confH, double *confHp, double *D1,
+                        double *f, double *chi, double *D1_unnormalised);
+
+/* -------------------------------------------------------------- multipoles */
+typedef struct or_model or_model_t;
+enum { OR_CONTRIB_DEN = 1, OR_CONTRIB_RSD = 2, OR_CONTRIB_LEN = 4 };
+
+or_model_t *or_model_new(void);
+void or_model_free(or_model_t *m);
+/* background splines (Akima, common.c:524) from node arrays on one z grid */
+int or_model_set_background(or_model_t *m, const double *z, const double *chi,
+                            const double *D1, const double *f, const double *a,
+                            const double *confH, size_t bins, double h,
+                            double Omega0_m);
+/* which: 0 = galaxy_bias1, 1 = galaxy_bias2, 2 = magnification_bias1,
+   3 = magnification_bias2; Akima over (z, value) */
+int or_model_set_bias(or_model_t *m, int which, const double *z, const double *v,
+                      size_t n);
+/* an I_l^n table (x, y of length len) read through an Akima spline */
+int or_model_set_integral(or_model_t *m, int n, int l, const double *x,
+                          const double *y, size_t len);
+/* den+RSD nonintegrated correlation function xi(z_mean, mu, r)
+   (functions.c:89-1484, den 129-229, rsd 230-362, den-rsd 670-771) */
+double or_xi_nonintegrated(const or_model_t *m, int contrib, double z_mean,
+                           double mu, double sep);
+/* one multipole by adaptive GK61 QAG (signal.c:83-111, 521-542) */
+double or_multipole_nonintegrated(const or_model_t *m, int contrib, double z_mean,
+                                  double sep, int l, double epsrel);
+/* batch over count points, OpenMP-parallel like multipoles.c:88-99 */
+int or_multipoles_batch(const or_model_t *m, int contrib, const double *z_mean,
+                        const double *sep, const int *l, size_t count,
+                        double epsrel, double *out, int nthreads);
+/* same as or_multipole_nonintegrated but with a fixed n-point Gauss-Legendre
+   rule in mu instead of QAG (comparator for fixed-rule paths) */
+double or_multipole_nonintegrated_gl(const or_model_t *m, int contrib, double z_mean,
+                                     double sep, int l, size_t n_mu);
+
+/* number of QAG subdivisions taken by the last or_multipole_nonintegrated call
+   in this thread (diagnostic) */
+int or_last_qag_intervals(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,229 @@
+"""ctypes bindings of the CPU oracle (test infrastructure only).
+
+Wraps ``oracle/_build/libcoffe_oracle.so`` (built by ``make -C oracle``).  Every
+function here restates the reference algorithm cited in ``coffe_oracle.h``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+_LIB_PATH = _HERE / "_build" / "libcoffe_oracle.so"
+_lib = None
+
+CONTRIB_DEN = 1
+CONTRIB_RSD = 2
+CONTRIB_LEN = 4
+H0 = 1.0 / 2997.92458  # h/Mpc
+N_SMALL_R = 42
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def build(force: bool = False) -> Path:
+    """Compile the oracle with its Makefile (gcc + OpenMP)."""
+    if force or not _LIB_PATH.exists() or any(
+        (_HERE / f).stat().st_mtime > _LIB_PATH.stat().st_mtime
+        for f in ("coffe_oracle.c", "coffe_oracle.h", "gk61_table.h")
+    ):
+        subprocess.run(["make", "-C", str(_HERE)], check=True, capture_output=True)
+    return _LIB_PATH
+
+
+class _Cosmo(C.Structure):
+    _fields_ = [
+        ("Omega0_cdm", C.c_double),
+        ("Omega0_baryon", C.c_double),
+        ("Omega0_gamma", C.c_double),
+        ("Omega0_de", C.c_double),
+        ("h", C.c_double),
+    ]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(_LIB_PATH))
+        L.or_spline_eval_array.argtypes = [C.c_int, _dp, _dp, C.c_size_t, _dp, _dp, C.c_size_t]
+        L.or_spline_coeffs.argtypes = [C.c_int, _dp, _dp, C.c_size_t, _dp, _dp, _dp]
+        L.or_lgamma_c.argtypes = [C.c_double, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.or_sph_bessel.argtypes = [C.c_int, C.c_double]
+        L.or_sph_bessel.restype = C.c_double
+        L.or_legendre.argtypes = [C.c_int, C.c_double]
+        L.or_legendre.restype = C.c_double
+        L.or_fft.argtypes = [_dp, _dp, C.c_size_t, C.c_int]
+        L.or_twofast_selectqnu.argtypes = [C.c_double, C.c_double]
+        L.or_twofast_selectqnu.restype = C.c_double
+        L.or_twofast_1bessel.argtypes = [_dp, _dp, C.c_size_t, _dp, _dp, C.c_size_t] + [C.c_double] * 6
+        L.or_integral_table.argtypes = [_dp, _dp, C.c_size_t, C.c_int, C.c_int, C.c_size_t,
+                                        C.c_double, C.c_double, C.c_int, _dp, _dp]
+        L.or_integral_direct.argtypes = [_dp, _dp, C.c_size_t, C.c_int, C.c_int, C.c_double,
+                                         C.c_double, C.c_double]
+        L.or_integral_direct.restype = C.c_double
+        L.or_background_nodes.argtypes = [C.POINTER(_Cosmo), C.c_size_t] + [_dp] * 9
+        L.or_gauss_legendre.argtypes = [C.c_size_t, _dp, _dp]
+        L.or_model_new.restype = C.c_void_p
+        L.or_model_free.argtypes = [C.c_void_p]
+        L.or_model_set_background.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp,
+                                              C.c_size_t, C.c_double, C.c_double]
+        L.or_model_set_bias.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_size_t]
+        L.or_model_set_integral.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, C.c_size_t]
+        L.or_xi_nonintegrated.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double]
+        L.or_xi_nonintegrated.restype = C.c_double
+        L.or_multipole_nonintegrated.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double,
+                                                 C.c_int, C.c_double]
+        L.or_multipole_nonintegrated.restype = C.c_double
+        L.or_multipole_nonintegrated_gl.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double,
+                                                    C.c_int, C.c_size_t]
+        L.or_multipole_nonintegrated_gl.restype = C.c_double
+        L.or_multipoles_batch.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _ip, C.c_size_t,
+                                          C.c_double, _dp, C.c_int]
+        L.or_last_qag_intervals.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+# ----------------------------------------------------------------- primitives
+def spline_eval(kind: str, x, y, xq):
+    t = {"cspline": 0, "akima": 1, "linear": 2}[kind]
+    x, y, xq = _f64(x), _f64(y), _f64(np.atleast_1d(xq))
+    out = np.empty_like(xq)
+    if lib().or_spline_eval_array(t, x, y, len(x), xq, out, len(xq)) != 0:
+        raise ValueError("spline init failed")
+    return out
+
+
+def spline_coeffs(kind: str, x, y):
+    t = {"cspline": 0, "akima": 1, "linear": 2}[kind]
+    x, y = _f64(x), _f64(y)
+    n = len(x)
+    b, c, d = (np.zeros(n) for _ in range(3))
+    if lib().or_spline_coeffs(t, x, y, n, b, c, d) != 0:
+        raise ValueError("spline init failed")
+    return b[:-1], c[:-1], d[:-1]
+
+
+def lgamma_c(z: complex) -> complex:
+    rr, ri = C.c_double(), C.c_double()
+    lib().or_lgamma_c(z.real, z.imag, C.byref(rr), C.byref(ri))
+    return complex(rr.value, ri.value)
+
+
+def sph_bessel(l: int, x: float) -> float:
+    return lib().or_sph_bessel(int(l), float(x))
+
+
+def legendre(l: int, x: float) -> float:
+    return lib().or_legendre(int(l), float(x))
+
+
+def fft(x, sign=-1):
+    x = np.asarray(x, dtype=np.complex128)
+    re, im = _f64(x.real.copy()), _f64(x.imag.copy())
+    lib().or_fft(re, im, len(x), int(sign))
+    return re + 1j * im
+
+
+def gauss_legendre(n: int):
+    x, w = np.zeros(n), np.zeros(n)
+    lib().or_gauss_legendre(n, x, w)
+    return x, w
+
+
+def selectqnu(l: float, nu: float) -> float:
+    return lib().or_twofast_selectqnu(float(l), float(nu))
+
+
+def twofast_1bessel(k, pk, N, l, nu, r0, k0, kmin, kmax):
+    k, pk = _f64(k), _f64(pk)
+    ox, oy = np.zeros(N), np.zeros(N)
+    if lib().or_twofast_1bessel(ox, oy, N, k, pk, len(k), l, nu, r0, k0, kmin, kmax) != 0:
+        raise ValueError("twofast_1bessel failed")
+    return ox, oy
+
+
+def integral_table(k, pk, n, l, N, kmin=None, kmax=None, with_small_r=True):
+    """Full I_l^n table (N + 43 points) as coffe_integrals_renormalizable."""
+    k, pk = _f64(k), _f64(pk)
+    kmin = float(k[0] if kmin is None else kmin)
+    kmax = float(k[-1] if kmax is None else kmax)
+    ox, oy = np.zeros(N + N_SMALL_R + 1), np.zeros(N + N_SMALL_R + 1)
+    if lib().or_integral_table(k, pk, len(k), n, l, N, kmin, kmax, int(with_small_r), ox, oy) != 0:
+        raise ValueError("integral table failed")
+    return ox, oy
+
+
+def integral_direct(k, pk, n, l, r, kmin=None, kmax=None):
+    k, pk = _f64(k), _f64(pk)
+    kmin = float(k[0] if kmin is None else kmin)
+    kmax = float(k[-1] if kmax is None else kmax)
+    return lib().or_integral_direct(k, pk, len(k), n, l, float(r), kmin, kmax)
+
+
+def background_nodes(omega_m=0.3, omega_baryon=0.05, omega_gamma=9e-5, h=0.67, bins=10000):
+    """Background node arrays on z_i = 15 i/(bins-1) (flat LCDM, w = -1)."""
+    c = _Cosmo(omega_m - omega_baryon, omega_baryon, omega_gamma,
+               1.0 - (omega_m + omega_gamma), h)
+    names = ["z", "a", "Hz", "confH", "confHp", "D1", "f", "chi", "D1_unnormalised"]
+    arrs = [np.zeros(bins) for _ in names]
+    if lib().or_background_nodes(C.byref(c), bins, *arrs) != 0:
+        raise ValueError("background failed")
+    return dict(zip(names, arrs))
+
+
+class Model:
+    """Background + bias + integral splines: the inputs of the multipole integrands."""
+
+    def __init__(self, bg: dict, h: float, omega_m: float):
+        self._p = lib().or_model_new()
+        z = _f64(bg["z"])
+        lib().or_model_set_background(self._p, z, _f64(bg["chi"]), _f64(bg["D1"]),
+                                      _f64(bg["f"]), _f64(bg["a"]), _f64(bg["confH"]),
+                                      len(z), float(h), float(omega_m))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "_p", None):
+            lib().or_model_free(self._p)
+            self._p = None
+
+    def set_bias(self, which: int, z, v):
+        if lib().or_model_set_bias(self._p, which, _f64(z), _f64(v), len(z)) != 0:
+            raise ValueError("bias spline failed")
+
+    def set_integral(self, n: int, l: int, x, y):
+        x, y = _f64(x), _f64(y)
+        if lib().or_model_set_integral(self._p, n, l, x, y, len(x)) != 0:
+            raise ValueError("integral spline failed")
+
+    def xi(self, contrib, z_mean, mu, sep):
+        return lib().or_xi_nonintegrated(self._p, contrib, z_mean, mu, sep)
+
+    def multipole(self, contrib, z_mean, sep, l, epsrel=1e-5):
+        return lib().or_multipole_nonintegrated(self._p, contrib, z_mean, sep, l, epsrel)
+
+    def multipole_gl(self, contrib, z_mean, sep, l, n_mu):
+        return lib().or_multipole_nonintegrated_gl(self._p, contrib, z_mean, sep, l, n_mu)
+
+    def multipoles_batch(self, contrib, z_mean, sep, l, epsrel=1e-5, nthreads=0):
+        z_mean, sep = _f64(z_mean), _f64(sep)
+        l = np.ascontiguousarray(l, dtype=np.int32)
+        out = np.zeros(len(sep))
+        lib().or_multipoles_batch(self._p, contrib, z_mean, sep, l, len(sep), epsrel, out,
+                                  int(nthreads))
+        return out
+
+
+def last_qag_intervals() -> int:
+    return lib().or_last_qag_intervals()
