@@ -1,0 +1,418 @@
+#!/usr/bin/env python
+"""Benchmark of the batched multipole path (FFTLog I_l^n tables + den/RSD
+multipole quadrature) on GB300.
+
+Workload (one "step"): 512 seeded BBKS spectra (sigma8 ~ U[0.7,0.9],
+n_s ~ U[0.93,1.0], Gamma ~ U[0.15,0.3]) x 6 mean redshifts in [0.5, 2] x
+l = 0, 2, 4, each (spectrum, z) request carrying 20-400 separations uniform in
+[5, 250] Mpc/h: FFTLog tables of I_0^0, I_2^0, I_4^0 on N = 4096 points for
+every spectrum, then every multipole by GK61 QAG.  Metric: multipole
+evaluations per second (one evaluation = one (spectrum, z, l, r) output).
+
+Arms:
+  default           : the GPU path (mixed precision headline; FP64 path beside it)
+  --impl reference  : the reference algorithm on the host cores (the CPU oracle,
+                      a C restatement: the reference itself cannot be built here),
+                      on a bounded sample of the same workload.
+
+Prints one JSON line (rank 0).  Multi-GPU (torchrun): independent replicas,
+one batch per rank ("weak" scaling), times max-reduced over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "multipole evals/s at <=1e-4 rel err vs FP64: batched mixed vs plain FP64 on 1 GB300"
+UNIT = "evals/s"
+TERMS = ((0, 0), (0, 2), (0, 4))
+N_FFT = 4096
+# algorithmic FLOP of one multipole-quadrature node (xi + three P_l + GK61 sums,
+# FMA = 2; counted from multipoles.cu) and per (request, separation) extras
+FLOP_PER_NODE = 170
+FLOP_PER_PAIR_EXTRA = 130
+NODES = 61
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=500)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n-spectra", type=int, default=512)
+    p.add_argument("--fp64-steps", type=int, default=0, help="0: max(3, steps // 50)")
+    p.add_argument("--cpu-spectra", type=int, default=48, help="CPU baseline sample size")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-clocks", action="store_true")
+    p.add_argument("--kernel-only", choices=["mixed", "fp64"], default=None,
+                   help="run only the timed multipole kernel loop (profiling)")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int, enabled: bool = True):
+        self.device = device
+        self.enabled = enabled
+        self.proc = None
+
+    def __enter__(self):
+        if not self.enabled:
+            return self
+        self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.25)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.enabled or self.proc is None:
+            return None
+        self.tmp.flush()
+        rows = []
+        with open(self.tmp.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.tmp.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------- CPU baseline
+def cpu_eval(batch, n_spectra, nthreads):
+    """The oracle (FP64 C restatement, OpenMP) on the first n_spectra spectra."""
+    import oracle as orc
+    from coffe_gb300 import workloads
+
+    b = workloads.subset(batch, n_spectra)
+    c = b.cosmo
+    bg = orc.background_nodes(c.omega_m, c.omega_baryon, c.omega_gamma, c.h, 10000)
+    t0 = time.perf_counter()
+    out = np.zeros((len(b.sep), len(b.ls)))
+    for s in range(n_spectra):
+        m = orc.Model(bg, c.h, c.omega_m)
+        for n, l in TERMS:
+            m.set_integral(n, l, *orc.integral_table(b.k, b.pk[s], n, l, N_FFT, with_small_r=False))
+        qs = np.where(b.req_spectrum == s)[0]
+        lo, hi = int(b.req_offset[qs[0]]), int(b.req_offset[qs[-1] + 1])
+        zz = np.repeat(b.req_z_mean[qs], np.diff(b.req_offset[qs[0]: qs[-1] + 2]))
+        for j, l in enumerate(b.ls):
+            out[lo:hi, j] = m.multipoles_batch(3, zz, b.sep[lo:hi], np.full(hi - lo, l),
+                                               nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return b.n_evals, dt, out
+
+
+def reference_arm(args, rank, world):
+    from coffe_gb300 import workloads
+
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    batch = workloads.cfg3(n_spectra=max(args.n_spectra, 1))
+    # size each step's sample so that the whole run takes about 90 s of CPU time
+    t1 = None
+    for _ in range(max(args.warmup, 1)):
+        t0 = time.perf_counter()
+        cpu_eval(batch, 1, nthreads)
+        t1 = time.perf_counter() - t0
+    ns = int(max(1, min(batch.pk.shape[0], 90.0 / (max(args.steps, 1) * t1))))
+    evals = 0
+    total = 0.0
+    for _ in range(args.steps):
+        e, dt, _ = cpu_eval(batch, ns, nthreads)
+        evals += e
+        total += dt
+    v = evals / total
+    line = {
+        "metric": METRIC, "value": v, "unit": UNIT, "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded BBKS spectra)",
+        "config": {"workload": "cfg3-batched: 512 spectra x 6 z x l=0,2,4, ragged 20-400 seps",
+                   "sample_spectra_per_step": ns, "fft_n": N_FFT},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": f"{ns} of 512 spectra per step ({evals // args.steps} evals)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------- GPU
+def rel_err_vs(ref, got, batch):
+    """max |got - ref| / max(|ref|, 1e-3 max_r |ref|) per (request, l)"""
+    floor = np.zeros_like(ref)
+    offs = batch.req_offset
+    for q in range(len(batch.req_spectrum)):
+        lo, hi = int(offs[q]), int(offs[q + 1])
+        if hi > lo:
+            floor[lo:hi] = 1e-3 * np.abs(ref[lo:hi]).max(axis=0)
+    return float(np.max(np.abs(got - ref) / np.maximum(np.abs(ref), np.maximum(floor, 1e-300))))
+
+
+def measure_gemm_peak(torch, dtype, n=8192, reps=5):
+    a = torch.randn(n, n, device="cuda", dtype=dtype)
+    b = torch.randn(n, n, device="cuda", dtype=dtype)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(reps):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = max(best, 2 * n ** 3 / (s.elapsed_time(e) * 1e-3))
+    del a, b
+    return best / 1e12
+
+
+def ours(args, rank, world, local_rank):
+    import torch
+
+    from coffe_gb300 import Context, workloads
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    batch = workloads.cfg3(n_spectra=args.n_spectra, seed=workloads.CFG3_SEED + rank)
+    c = batch.cosmo
+    n_sep = len(batch.sep)
+    n_evals = batch.n_evals
+    ctx = Context(local_rank)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.background_init(c.omega_m, c.omega_baryon, c.omega_gamma, c.h, 10000)
+    pk_d = torch.from_numpy(batch.pk).to(dev)
+    rs_d = torch.from_numpy(batch.req_spectrum).to(dev)
+    rz_d = torch.from_numpy(batch.req_z_mean).to(dev)
+    ro_d = torch.from_numpy(batch.req_offset).to(dev)
+    sep_d = torch.from_numpy(batch.sep).to(dev)
+    outs = {p: torch.empty((n_sep, len(batch.ls)), dtype=torch.float64, device=dev)
+            for p in ("mixed", "fp64")}
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    def step(prec):
+        ctx.integrals_init_device(batch.k, pk_d, TERMS, N=N_FFT, precision=prec, sync=False)
+        ctx.multipoles_async(rs_d, rz_d, ro_d, sep_d, n_sep, batch.ls, outs[prec], precision=prec)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # build the per-grid tables once (synchronous), then warm up
+    for prec in ("mixed", "fp64"):
+        ctx.integrals_init_device(batch.k, pk_d, TERMS, N=N_FFT, precision=prec, sync=True)
+    for _ in range(max(args.warmup, 0)):
+        step("mixed")
+    ctx.synchronize()
+
+    def timed(prec, k):
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+        barrier()
+        l0 = ctx.launch_count()
+        w0 = time.perf_counter()
+        for i in range(k):
+            flush.zero_()  # evict the previous step's tables and inputs from L2
+            starts[i].record(stream)
+            step(prec)
+            ends[i].record(stream)
+        barrier()
+        wall = time.perf_counter() - w0
+        ctx.synchronize()
+        dev_s = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) * 1e-3
+        return dev_s, wall, ctx.launch_count() - l0
+
+    if args.kernel_only:
+        # profiling aid: only the multipole kernel of one precision, tables built once
+        prec = args.kernel_only
+        ctx.integrals_init_device(batch.k, pk_d, TERMS, N=N_FFT, precision=prec, sync=True)
+        for _ in range(args.steps):
+            ctx.multipoles_async(rs_d, rz_d, ro_d, sep_d, n_sep, batch.ls, outs[prec], precision=prec)
+        ctx.synchronize()
+        return
+
+    with ClockSampler(local_rank, enabled=not args.no_clocks and rank == 0) as clk:
+        dev_mixed, wall_mixed, launches = timed("mixed", args.steps)
+    clocks = clk.summary()
+    k64 = args.fp64_steps or max(3, args.steps // 50)
+    for _ in range(2):
+        step("fp64")
+    ctx.synchronize()
+    dev_fp64, wall_fp64, _ = timed("fp64", k64)
+
+    # accuracy of the mixed path against the FP64 path on the full batch (the
+    # FP64 path itself matches the CPU oracle to 1e-10 in the parity tests)
+    step("mixed")
+    step("fp64")
+    ctx.synchronize()
+    err = rel_err_vs(outs["fp64"].cpu().numpy(), outs["mixed"].cpu().numpy(), batch)
+
+    # dominant kernel: the mixed multipole kernel alone, CUDA events on our stream
+    ctx.integrals_init_device(batch.k, pk_d, TERMS, N=N_FFT, precision="mixed", sync=True)
+    nk_rep = 20
+    s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    s_ev.record(stream)
+    for _ in range(nk_rep):
+        ctx.multipoles_async(rs_d, rz_d, ro_d, sep_d, n_sep, batch.ls, outs["mixed"],
+                             precision="mixed")
+    e_ev.record(stream)
+    e_ev.synchronize()
+    kern_s = s_ev.elapsed_time(e_ev) * 1e-3 / nk_rep
+    flop_launch = n_sep * (NODES * FLOP_PER_NODE + FLOP_PER_PAIR_EXTRA)
+
+    # end to end through the public API with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+        h_pk, h_rs, h_rz = pin(batch.pk), pin(batch.req_spectrum), pin(batch.req_z_mean)
+        h_ro, h_sep = pin(batch.req_offset), pin(batch.sep)
+        ctx.set_stream(None)
+        ctx.integrals_init(batch.k, h_pk, TERMS, N=N_FFT, precision="mixed", small_r=False)
+        ctx.multipoles(h_rs, h_rz, h_ro, h_sep, batch.ls, precision="mixed")
+        ke = max(3, min(args.steps, 20))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            ctx.integrals_init(batch.k, h_pk, TERMS, N=N_FFT, precision="mixed", small_r=False)
+            res = ctx.multipoles(h_rs, h_rz, h_ro, h_sep, batch.ls, precision="mixed")
+        barrier()
+        te = time.perf_counter() - t0
+        h2d = h_pk.nbytes + h_rs.nbytes + h_rz.nbytes + h_ro.nbytes + h_sep.nbytes
+        e2e = {"value": n_evals * ke / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(res.nbytes), "steps": ke,
+               "ms_per_step": 1e3 * te / ke}
+        ctx.set_stream(stream.cuda_stream)
+
+    # reduce over ranks (max time)
+    times = torch.tensor([dev_mixed, dev_fp64, kern_s], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+    dev_mixed, dev_fp64, kern_s = times.tolist()
+    if e2e is not None and world > 1:
+        t = torch.tensor([e2e["ms_per_step"]], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e["ms_per_step"] = float(t.item())
+        e2e["value"] = n_evals * world / (e2e["ms_per_step"] * 1e-3)
+    if rank != 0:
+        ctx.close()
+        return
+
+    value = n_evals * args.steps * world / dev_mixed
+    fp64_value = n_evals * k64 * world / dev_fp64
+    sgemm = measure_gemm_peak(torch, torch.float32)
+    achieved = flop_launch / kern_s / 1e12
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except OSError:
+        pass
+    cpu = None
+    if not args.no_cpu:
+        nthreads = os.cpu_count() or 1
+        ce, cdt, cout = cpu_eval(batch, args.cpu_spectra, nthreads)
+        sub_err = rel_err_vs(cout, outs["fp64"].cpu().numpy()[: cout.shape[0]],
+                             workloads.subset(batch, args.cpu_spectra))
+        cpu = {"value": ce / cdt, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": f"first {args.cpu_spectra} of {args.n_spectra} spectra, all their "
+                         f"requests ({ce} evals, {cdt:.1f} s)",
+               "gpu_fp64_vs_cpu_max_rel_err": sub_err}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dev_mixed / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded BBKS spectra, seed 20261203 + rank)",
+        "config": {"workload": "cfg3-batched: 512 spectra x 6 z_mean x l=0,2,4, ragged 20-400 "
+                               "separations in [5,250] Mpc/h, FFTLog N=4096",
+                   "n_spectra": args.n_spectra, "requests": len(batch.req_spectrum),
+                   "separations": n_sep, "evals_per_step": n_evals,
+                   "l2": "flushed between timed steps (256 MiB write outside the events)",
+                   "parallelism": f"replicas x{world}"},
+        "fp64": {"value": fp64_value, "unit": UNIT, "steps": k64,
+                 "ms_per_step": 1e3 * dev_fp64 / k64},
+        "mixed_over_fp64": value / fp64_value,
+        "max_rel_err_mixed_vs_fp64": err,
+        "gpu_launches": int(launches),
+        "roofline": {"kernel": "multipoles_kernel<float> (mixed multipole quadrature)",
+                     "bound": "fp32", "achieved": achieved,
+                     "peak": sgemm, "unit": "TFLOP/s", "frac": achieved / sgemm,
+                     "peak_source": "measured cuBLAS SGEMM 8192^3 (FP32 CUDA cores, TF32 off) "
+                                    "in this run; the kernel is FP32-pipe bound, neither HBM "
+                                    "nor tensor",
+                     "flop_per_launch": flop_launch, "launch_ms": kern_s * 1e3,
+                     "traffic": None,
+                     "hbm_peak_gbs": peaks.get("hbm_gbs")},
+        "clocks": clocks,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    import torch
+
+    torch.backends.cuda.matmul.allow_tf32 = False
+    if world > 1:
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    try:
+        ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,386 @@
+"""Python host API over the C ABI: a context object and a ``Coffe`` class that
+mirrors the reference's Python wrapper (python/coffe/coffe.pyx) for the
+correlation-function hot path.
+
+Units follow the reference: k in 1/Mpc, P(k) in Mpc^3, separations in Mpc.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Iterable, List, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib
+from ._lib import CoffeGpuError, Cosmology
+
+# the default full-sky integrals of coffe_integrals_init (integrals.c:599-608)
+DEFAULT_TERMS: Tuple[Tuple[int, int], ...] = (
+    (0, 0), (0, 2), (0, 4), (1, 1), (1, 3), (2, 0), (2, 2), (3, 1),
+)
+DEN_RSD_TERMS: Tuple[Tuple[int, int], ...] = ((0, 0), (0, 2), (0, 4))
+COFFE_H0 = 1.0 / 2997.92458  # h/Mpc (common.h:76)
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _lptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _precision(p) -> int:
+    if p in (0, "fp64", "double", "float64"):
+        return _lib.FP64
+    if p in (1, "mixed", "fp32"):
+        return _lib.MIXED
+    raise ValueError(f"unknown precision {p!r} (use 'fp64' or 'mixed')")
+
+
+class Context:
+    """One ``coffe_gpu_ctx_t``: device buffers, a stream and the cached tables."""
+
+    def __init__(self, device: int = 0):
+        self._L = _lib.load()
+        self._ctx = C.c_void_p()
+        st = self._L.coffe_gpu_ctx_create(int(device), C.byref(self._ctx))
+        if st != 0:
+            raise CoffeGpuError(st, "coffe_gpu_ctx_create", "no usable CUDA device")
+        self.device = device
+        self.N = None
+        self.terms: Tuple[Tuple[int, int], ...] = ()
+        self.n_spectra = 0
+        self.precision = None
+
+    # -------------------------------------------------------------- plumbing
+    def _check(self, st: int, what: str):
+        if st != 0:
+            detail = self._L.coffe_gpu_last_error(self._ctx)
+            raise CoffeGpuError(st, what, detail.decode() if detail else "")
+
+    def close(self):
+        if getattr(self, "_ctx", None) and self._ctx.value:
+            self._L.coffe_gpu_ctx_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> int:
+        return self._ctx.value
+
+    def synchronize(self):
+        self._check(self._L.coffe_gpu_synchronize(self._ctx), "synchronize")
+
+    def set_stream(self, stream_ptr: int | None):
+        self._check(self._L.coffe_gpu_set_stream(self._ctx, C.c_void_p(stream_ptr or 0)),
+                    "set_stream")
+
+    def launch_count(self) -> int:
+        return int(self._L.coffe_gpu_launch_count(self._ctx))
+
+    # ------------------------------------------------------------ background
+    def background_init(self, omega_m=0.3, omega_baryon=0.05, omega_gamma=9e-5, h=0.67,
+                        bins=10000):
+        c = Cosmology(omega_m - omega_baryon, omega_baryon, omega_gamma,
+                      1.0 - (omega_m + omega_gamma), h, int(bins))
+        self._check(self._L.coffe_gpu_background_init(self._ctx, C.byref(c)), "background_init")
+        self.bins = int(bins)
+
+    def background_set(self, z, chi, D1, f, a, conformal_Hz, omega_m, h):
+        arrs = [_f64(x) for x in (z, chi, D1, f, a, conformal_Hz)]
+        n = len(arrs[0])
+        if any(len(x) != n for x in arrs):
+            raise ValueError("background arrays must have equal lengths")
+        self._check(self._L.coffe_gpu_background_set(self._ctx, *map(_dptr, arrs), n,
+                                                     float(omega_m), float(h)), "background_set")
+        self.bins = n
+
+    def background(self, with_H: bool = True) -> dict:
+        n = self.bins
+        names = ["z", "chi", "D1", "f", "a", "Hz", "conformal_Hz", "conformal_Hz_prime"]
+        arrs = {k: np.zeros(n) for k in names}
+        ptrs = [_dptr(arrs[k]) for k in names]
+        if not with_H:
+            ptrs[5] = None
+            ptrs[7] = None
+        self._check(self._L.coffe_gpu_background_get(self._ctx, *ptrs), "background_get")
+        return arrs
+
+    def set_bias(self, which: int, z, value):
+        z, v = _f64(z), _f64(value)
+        self._check(self._L.coffe_gpu_set_bias(self._ctx, int(which), _dptr(z), _dptr(v), len(z)),
+                    "set_bias")
+
+    # ------------------------------------------------------------- integrals
+    def integrals_init(self, k, pk, terms: Sequence[Tuple[int, int]] = DEFAULT_TERMS,
+                       N: int = 4096, precision="fp64", small_r: bool = True):
+        """FFTLog tables of I_l^n for each spectrum row of ``pk`` (shape (S, nk))."""
+        k = _f64(k)
+        pk = _f64(np.atleast_2d(pk))
+        if pk.shape[1] != len(k):
+            raise ValueError("pk must have shape (n_spectra, len(k))")
+        n = np.ascontiguousarray([t[0] for t in terms], dtype=np.int32)
+        l = np.ascontiguousarray([t[1] for t in terms], dtype=np.int32)
+        prec = _precision(precision)
+        flags = _lib.SMALL_R if small_r else 0
+        self._check(self._L.coffe_gpu_integrals_init(self._ctx, _dptr(k), _dptr(pk), pk.shape[0],
+                                                     len(k), _iptr(n), _iptr(l), len(terms),
+                                                     int(N), prec, flags), "integrals_init")
+        self.N = int(N)
+        self.terms = tuple((int(a), int(b)) for a, b in terms)
+        self.n_spectra = pk.shape[0]
+        self.precision = prec
+
+    def table_len(self) -> int:
+        return int(self._L.coffe_gpu_integral_table_len(self.N))
+
+    def _term(self, n: int, l: int) -> int:
+        try:
+            return self.terms.index((n, l))
+        except ValueError:
+            raise ValueError(f"Cannot find integral with n = {n}, l = {l}") from None
+
+    def integral_table(self, spectrum: int, n: int, l: int):
+        m = self.table_len()
+        x, y = np.zeros(m), np.zeros(m)
+        self._check(self._L.coffe_gpu_integral_get(self._ctx, int(spectrum), self._term(n, l),
+                                                   _dptr(x), _dptr(y)), "integral_get")
+        return x, y
+
+    def integral_eval(self, spectrum: int, n: int, l: int, r):
+        r = _f64(np.atleast_1d(r))
+        out = np.zeros(len(r))
+        self._check(self._L.coffe_gpu_integral_eval(self._ctx, int(spectrum), self._term(n, l),
+                                                    _dptr(r), len(r), _dptr(out)), "integral_eval")
+        return out
+
+    # ------------------------------------------------------------ multipoles
+    def multipoles(self, req_spectrum, req_z_mean, req_offset, sep, ls=(0, 2, 4),
+                   contrib=_lib.DEN | _lib.RSD, precision="fp64", epsrel=1e-5) -> np.ndarray:
+        """Batched multipoles; returns an array of shape (len(sep), len(ls))."""
+        rs = np.ascontiguousarray(req_spectrum, dtype=np.int32)
+        rz = _f64(req_z_mean)
+        ro = np.ascontiguousarray(req_offset, dtype=np.int64)
+        sp = _f64(sep)
+        la = np.ascontiguousarray(ls, dtype=np.int32)
+        if len(ro) != len(rs) + 1 or len(rz) != len(rs):
+            raise ValueError("req_offset needs len(req_spectrum) + 1 entries")
+        out = np.zeros((max(len(sp), 1), len(la)))
+        self._check(self._L.coffe_gpu_multipoles(self._ctx, int(contrib), _precision(precision),
+                                                 float(epsrel), len(rs), _iptr(rs), _dptr(rz),
+                                                 _lptr(ro), _dptr(sp), len(la), _iptr(la),
+                                                 _dptr(out), 0), "multipoles")
+        return out[: len(sp)]
+
+    def integrals_init_device(self, k, pk_dev, terms=DEN_RSD_TERMS, N: int = 4096,
+                              precision="fp64", small_r: bool = False, sync: bool = True):
+        """Like :meth:`integrals_init` with P(k) already on the device (a CUDA
+        float64 tensor of shape (S, nk)); ``sync=False`` only enqueues."""
+        k = _f64(k)
+        S, nk = int(pk_dev.shape[0]), int(pk_dev.shape[1])
+        if nk != len(k):
+            raise ValueError("pk must have shape (n_spectra, len(k))")
+        n = np.ascontiguousarray([t[0] for t in terms], dtype=np.int32)
+        l = np.ascontiguousarray([t[1] for t in terms], dtype=np.int32)
+        flags = _lib.PK_DEVICE | (_lib.SMALL_R if small_r else 0) | (0 if sync else _lib.ASYNC)
+        pk_ptr = C.cast(C.c_void_p(pk_dev.data_ptr()), C.POINTER(C.c_double))
+        self._check(self._L.coffe_gpu_integrals_init(self._ctx, _dptr(k), pk_ptr, S, nk, _iptr(n),
+                                                     _iptr(l), len(terms), int(N),
+                                                     _precision(precision), flags),
+                    "integrals_init")
+        self.N = int(N)
+        self.terms = tuple((int(a), int(b)) for a, b in terms)
+        self.n_spectra = S
+        self.precision = _precision(precision)
+
+    def multipoles_async(self, req_spectrum, req_z_mean, req_offset, sep, n_sep: int, ls, out,
+                         contrib=_lib.DEN | _lib.RSD, precision="fp64", epsrel=1e-5):
+        """Enqueue-only multipoles on device tensors; ``ls`` is a host sequence.
+        Errors surface at :meth:`synchronize`."""
+        P = lambda t, ty: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ty))
+        la = np.ascontiguousarray(ls, dtype=np.int32)
+        self._check(self._L.coffe_gpu_multipoles_async(
+            self._ctx, int(contrib), _precision(precision), float(epsrel),
+            int(req_spectrum.numel()), int(n_sep), P(req_spectrum, C.c_int),
+            P(req_z_mean, C.c_double), P(req_offset, C.c_int64), P(sep, C.c_double), len(la),
+            _iptr(la), P(out, C.c_double)), "multipoles_async")
+
+    def multipoles_device(self, req_spectrum, req_z_mean, req_offset, sep, ls, out,
+                          contrib=_lib.DEN | _lib.RSD, precision="fp64", epsrel=1e-5):
+        """Same as :meth:`multipoles` with CUDA tensors (int32, float64, int64,
+        float64, int32, float64 out of shape (len(sep), len(ls))); no copies."""
+        P = lambda t, ty: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ty))
+        self._check(self._L.coffe_gpu_multipoles(
+            self._ctx, int(contrib), _precision(precision), float(epsrel), int(req_spectrum.numel()),
+            P(req_spectrum, C.c_int), P(req_z_mean, C.c_double), P(req_offset, C.c_int64),
+            P(sep, C.c_double), int(ls.numel()), P(ls, C.c_int), P(out, C.c_double), 1),
+            "multipoles")
+
+
+# ---------------------------------------------------------------- Coffe mirror
+@dataclass
+class Multipoles:
+    """One multipole value (python/coffe/representation.py's Multipoles record)."""
+
+    z: float
+    r: float
+    l: int
+    value: float
+
+    def to_dict(self):
+        return {"z": self.z, "r": self.r, "l": self.l, "value": self.value}
+
+
+def _check_parameter(name, value, kind, lo, hi):
+    """Range/type check with the reference's semantics (coffe.pyx:86-110)."""
+    if not isinstance(value, kind) or isinstance(value, bool) and kind is not bool:
+        raise TypeError(f"Expected {kind}, got {type(value)} for {name}")
+    if not (lo <= value <= hi):
+        raise ValueError(f"Value {value} of {name} outside of interval [{lo}, {hi}]")
+
+
+class Coffe:
+    """Mirror of ``coffe.Coffe`` (coffe.pyx:237-3585) for the hot path: the
+    FFTLog integrals, density/RSD multipoles, with lazy initialisation and
+    caching like the reference (background -> power spectrum -> integrals ->
+    multipoles), computed on the GPU through the C ABI.
+    """
+
+    def __init__(self, *, omega_m=0.3, omega_baryon=0.05, omega_gamma=9e-5, h=0.67,
+                 sep=None, l=(0, 2, 4), z_mean=(1.0,), has_density=True, has_rsd=False,
+                 integrals_fftlog_sampling=4096, background_bins=10000,
+                 integration_1d_prec=1e-5, precision="fp64", device=0):
+        self._ctx = Context(device)
+        self.omega_m = float(omega_m)
+        self.omega_baryon = float(omega_baryon)
+        self.omega_gamma = float(omega_gamma)
+        self.h = float(h)
+        # default separations of coffe_parse_default_parameters (parser.c:836-838)
+        self.sep = np.linspace(5, 305, 100, endpoint=False) if sep is None else np.asarray(sep, float)
+        self.l = list(l)
+        self.z_mean = list(z_mean)
+        self.has_density = bool(has_density)
+        self.has_rsd = bool(has_rsd)
+        self.integrals_fftlog_sampling = int(integrals_fftlog_sampling)
+        self.background_bins = int(background_bins)
+        self.integration_1d_prec = float(integration_1d_prec)
+        self.precision = precision
+        self._k = None
+        self._pk = None
+        self._bg_ready = False
+        self._int_ready = False
+        self._bias = {}
+
+    # ------------------------------------------------------------ parameters
+    def set_power_spectrum_linear(self, k: Iterable[float], pk: Iterable[float], z: float = 0):
+        """k in 1/Mpc, P(k) in Mpc^3 (coffe.pyx:2929-2996); kmin/kmax = k[0], k[-1]."""
+        k = np.asarray(k, dtype=float)
+        pk = np.asarray(pk, dtype=float)
+        if not np.allclose(k, np.sort(k)):
+            raise ValueError("The input k array must be sorted")
+        if len(k) != len(pk):
+            raise ValueError("The input arrays have mismatching lengths")
+        self._k, self._pk = k, pk
+        self._int_ready = False
+
+    def set_galaxy_bias1(self, z, value):
+        self._set_bias(0, z, value)
+
+    def set_galaxy_bias2(self, z, value):
+        self._set_bias(1, z, value)
+
+    def _set_bias(self, which, z, value):
+        z = np.asarray(z, float)
+        if np.any(z < 0) or np.any(z > 15):
+            raise ValueError("bias redshifts must be in [0, 15]")
+        self._bias[which] = (z, np.asarray(value, float))
+        if self._bg_ready:
+            self._ctx.set_bias(which, *self._bias[which])
+
+    # ------------------------------------------------------------------ init
+    def _background_init(self):
+        self._ctx.background_init(self.omega_m, self.omega_baryon, self.omega_gamma, self.h,
+                                  self.background_bins)
+        for which, (z, v) in self._bias.items():
+            self._ctx.set_bias(which, z, v)
+        self._bg_ready = True
+
+    def _integrals_init(self):
+        if self._k is None:
+            raise ValueError("no power spectrum: call set_power_spectrum_linear first")
+        self._ctx.integrals_init(self._k, self._pk[None, :], DEFAULT_TERMS,
+                                 N=self.integrals_fftlog_sampling, precision=self.precision,
+                                 small_r=True)
+        self._int_ready = True
+
+    def _ensure(self):
+        if not self._bg_ready:
+            self._background_init()
+        if not self._int_ready:
+            self._integrals_init()
+
+    @property
+    def _contrib(self) -> int:
+        c = (_lib.DEN if self.has_density else 0) | (_lib.RSD if self.has_rsd else 0)
+        if c == 0:
+            raise ValueError("no contributions selected (has_density / has_rsd)")
+        return c
+
+    # --------------------------------------------------------------- outputs
+    def integral(self, *, r: float, n: int, l: int) -> float:
+        """I_l^n(r) (times r^(n-l) when n > l), coffe.pyx:1657-1713."""
+        _check_parameter("r", r, (int, float), 0, 25000)
+        _check_parameter("n", n, int, -2, 4)
+        _check_parameter("l", l, int, 0, 4)
+        self._ensure()
+        return float(self._ctx.integral_eval(0, n, l, [float(r)])[0])
+
+    def compute_multipole(self, *, z: float, r: float, l: int) -> float:
+        """One multipole at (z_mean, r, l) (coffe.pyx:3232-3300)."""
+        _check_parameter("z", z, (int, float), 0, 15)
+        _check_parameter("r", r, (int, float), 0, 1500)
+        _check_parameter("l", l, int, 0, 10)
+        self._ensure()
+        out = self._ctx.multipoles([0], [float(z)], [0, 1], [float(r)], [l], self._contrib,
+                                   self.precision, self.integration_1d_prec)
+        return float(out[0, 0])
+
+    def compute_multipoles_bulk(self) -> List[Multipoles]:
+        """All (z_mean, l, sep) points in the reference's order: z outer, l,
+        then separation (multipoles.c:76-86)."""
+        self._ensure()
+        nz, ns = len(self.z_mean), len(self.sep)
+        offs = np.arange(nz + 1, dtype=np.int64) * ns
+        sep = np.tile(self.sep, nz)
+        vals = self._ctx.multipoles(np.zeros(nz, np.int32), self.z_mean, offs, sep, self.l,
+                                    self._contrib, self.precision, self.integration_1d_prec)
+        res = []
+        for iz, zm in enumerate(self.z_mean):
+            for il, ll in enumerate(self.l):
+                for js, r in enumerate(self.sep):
+                    res.append(Multipoles(z=zm, r=float(r), l=ll, value=float(vals[iz * ns + js, il])))
+        return res
+
+    def close(self):
+        self._ctx.close()

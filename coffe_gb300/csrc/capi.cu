@@ -1,0 +1,411 @@
+// C ABI entry points (include/coffe_gpu.h): argument checks, host<->device
+// staging, error mapping.  The numerical work lives in the other .cu files.
+#include <string.h>
+
+#include <vector>
+
+#include "ctx.cuh"
+
+void cg_set_error(coffe_gpu_ctx *ctx, const char *fmt, ...)
+{
+    if (!ctx) return;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(ctx->last_error, sizeof(ctx->last_error), fmt, ap);
+    va_end(ap);
+}
+
+int cg_ensure(coffe_gpu_ctx *ctx, DevBuf &b, size_t bytes)
+{
+    if (b.bytes >= bytes && b.p) return COFFE_GPU_OK;
+    if (b.p) {
+        // the stream may still use the old buffer
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(b.p);
+    }
+    b.p = nullptr;
+    b.bytes = 0;
+    if (bytes == 0) return COFFE_GPU_OK;
+    if (cudaMalloc(&b.p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        cg_set_error(ctx, "cudaMalloc of %zu bytes failed", bytes);
+        return COFFE_GPU_ENOMEM;
+    }
+    b.bytes = bytes;
+    return COFFE_GPU_OK;
+}
+
+void cg_release(DevBuf &b)
+{
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+int cg_after_launch(coffe_gpu_ctx *ctx, const char *what)
+{
+    ctx->launches++;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        cg_set_error(ctx, "launch of %s failed: %s", what, cudaGetErrorString(e));
+        return COFFE_GPU_ECUDA;
+    }
+    return COFFE_GPU_OK;
+}
+
+int cg_check_device_errors(coffe_gpu_ctx *ctx, const char *where)
+{
+    CG_CUDA(ctx, cudaMemcpyAsync(ctx->h_err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const int bits = *ctx->h_err;
+    if (!bits) return COFFE_GPU_OK;
+    CG_CUDA(ctx, cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    *ctx->h_err = 0;
+    if (bits & CG_ERR_NONFINITE) {
+        cg_set_error(ctx, "%s: non-finite value produced (device flags 0x%x)", where, bits);
+        return COFFE_GPU_ENONFINITE;
+    }
+    if (bits & CG_ERR_QAG_LIMIT) {
+        cg_set_error(ctx, "%s: adaptive quadrature exhausted its subintervals", where);
+        return COFFE_GPU_ELIMIT;
+    }
+    if (bits & CG_ERR_TIMEOUT) {
+        cg_set_error(ctx, "%s: a bounded device wait timed out", where);
+        return COFFE_GPU_ETIMEOUT;
+    }
+    cg_set_error(ctx, "%s: device error flags 0x%x", where, bits);
+    return COFFE_GPU_EINVAL;
+}
+
+extern "C" {
+
+const char *coffe_gpu_strerror(int status)
+{
+    switch (status) {
+    case COFFE_GPU_OK: return "success";
+    case COFFE_GPU_EINVAL: return "invalid argument";
+    case COFFE_GPU_ECUDA: return "CUDA runtime error";
+    case COFFE_GPU_ENOMEM: return "device out of memory";
+    case COFFE_GPU_ENONFINITE: return "non-finite value in a result";
+    case COFFE_GPU_ESTATE: return "missing prerequisite (background or integrals)";
+    case COFFE_GPU_ELIMIT: return "adaptive quadrature subinterval limit reached";
+    case COFFE_GPU_ETIMEOUT: return "device-side wait timed out";
+    default: return "unknown status";
+    }
+}
+
+int coffe_gpu_ctx_create(int device, coffe_gpu_ctx_t **out)
+{
+    if (!out) return COFFE_GPU_EINVAL;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+        cudaGetLastError();
+        return COFFE_GPU_ECUDA;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return COFFE_GPU_ECUDA;
+    coffe_gpu_ctx *ctx = new coffe_gpu_ctx();
+    ctx->device = device;
+    if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_err, sizeof(int)) != cudaSuccess) {
+        coffe_gpu_ctx_destroy(ctx);
+        return COFFE_GPU_ECUDA;
+    }
+    ctx->stream = ctx->own_stream;
+    *ctx->h_err = 0;
+    if (cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        coffe_gpu_ctx_destroy(ctx);
+        return COFFE_GPU_ECUDA;
+    }
+    *out = ctx;
+    return COFFE_GPU_OK;
+}
+
+int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
+{
+    if (!ctx) return COFFE_GPU_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (int i = 0; i < BG_NFN; ++i) spline_free(ctx->bg[i]);
+    for (int i = 0; i < 4; ++i) {
+        spline_free(ctx->bias[i]);
+        cg_release(ctx->bias_nodes[i]);
+    }
+    DevBuf *bufs[] = {&ctx->bg_nodes, &ctx->tab_x,  &ctx->tab_x32, &ctx->tab_y,  &ctx->pk,
+                      &ctx->kgrid,    &ctx->csc,    &ctx->csfac,   &ctx->samp_idx, &ctx->samp_dx,
+                      &ctx->qfac,     &ctx->modec,  &ctx->postf,   &ctx->twid,   &ctx->twid32,
+                      &ctx->spec,     &ctx->req_buf, &ctx->term_meta};
+    for (DevBuf *b : bufs) cg_release(*b);
+    if (ctx->d_err) cudaFree(ctx->d_err);
+    if (ctx->h_err) cudaFreeHost(ctx->h_err);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return COFFE_GPU_OK;
+}
+
+const char *coffe_gpu_last_error(const coffe_gpu_ctx_t *ctx)
+{
+    return ctx ? ctx->last_error : "no context";
+}
+
+int coffe_gpu_synchronize(coffe_gpu_ctx_t *ctx)
+{
+    if (!ctx) return COFFE_GPU_EINVAL;
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return cg_check_device_errors(ctx, "synchronize");
+}
+
+int coffe_gpu_set_stream(coffe_gpu_ctx_t *ctx, void *stream)
+{
+    if (!ctx) return COFFE_GPU_EINVAL;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return COFFE_GPU_OK;
+}
+
+long long coffe_gpu_launch_count(const coffe_gpu_ctx_t *ctx) { return ctx ? ctx->launches : -1; }
+
+int coffe_gpu_background_init(coffe_gpu_ctx_t *ctx, const coffe_gpu_cosmology_t *c)
+{
+    if (!ctx || !c) return COFFE_GPU_EINVAL;
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int st = bg_init_device(ctx, c);
+    if (st) return st;
+    return cg_check_device_errors(ctx, "background_init");
+}
+
+int coffe_gpu_background_set(coffe_gpu_ctx_t *ctx, const double *z, const double *chi,
+                             const double *D1, const double *f, const double *a,
+                             const double *conformal_Hz, size_t bins, double Omega0_m, double h)
+{
+    if (!ctx || !z || !chi || !D1 || !f || !a || !conformal_Hz) return COFFE_GPU_EINVAL;
+    if (bins < 5 || bins > (1u << 24)) {
+        cg_set_error(ctx, "background_set: bins must be in [5, 2^24]");
+        return COFFE_GPU_EINVAL;
+    }
+    for (size_t i = 1; i < bins; ++i)
+        if (!(z[i] > z[i - 1]) || !(chi[i] > chi[i - 1])) {
+            cg_set_error(ctx, "background_set: z and chi must be strictly increasing");
+            return COFFE_GPU_EINVAL;
+        }
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    int st = cg_ensure(ctx, ctx->bg_nodes, sizeof(double) * 8 * bins);
+    if (st) return st;
+    double *d = (double *)ctx->bg_nodes.p;
+    const double *src[6] = {z, chi, D1, f, a, conformal_Hz};
+    const int row[6] = {0, 1, 2, 3, 4, 5};
+    for (int i = 0; i < 6; ++i)
+        CG_CUDA(ctx, cudaMemcpyAsync(d + row[i] * bins, src[i], sizeof(double) * bins,
+                                     cudaMemcpyHostToDevice, ctx->stream));
+    ctx->bg_bins = (int)bins;
+    ctx->Omega0_m = Omega0_m;
+    ctx->h = h;
+    ctx->bg_has_H = false;
+    st = bg_build_splines(ctx);
+    if (st) return st;
+    return cg_check_device_errors(ctx, "background_set");
+}
+
+int coffe_gpu_background_get(coffe_gpu_ctx_t *ctx, double *z, double *chi, double *D1, double *f,
+                             double *a, double *Hz, double *conformal_Hz,
+                             double *conformal_Hz_prime)
+{
+    if (!ctx) return COFFE_GPU_EINVAL;
+    if (ctx->bg_bins <= 0) {
+        cg_set_error(ctx, "background_get: no background");
+        return COFFE_GPU_ESTATE;
+    }
+    if ((Hz || conformal_Hz_prime) && !ctx->bg_has_H) {
+        cg_set_error(ctx, "background_get: H and H' exist only after background_init");
+        return COFFE_GPU_ESTATE;
+    }
+    const size_t bins = (size_t)ctx->bg_bins;
+    const double *d = (const double *)ctx->bg_nodes.p;
+    double *dst[8] = {z, chi, D1, f, a, conformal_Hz, Hz, conformal_Hz_prime};
+    for (int i = 0; i < 8; ++i)
+        if (dst[i])
+            CG_CUDA(ctx, cudaMemcpyAsync(dst[i], d + i * bins, sizeof(double) * bins,
+                                         cudaMemcpyDeviceToHost, ctx->stream));
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return COFFE_GPU_OK;
+}
+
+int coffe_gpu_set_bias(coffe_gpu_ctx_t *ctx, int which, const double *z, const double *value,
+                       size_t n)
+{
+    if (!ctx || which < 0 || which > 3) return COFFE_GPU_EINVAL;
+    if (!z || !value || n < 5 || n > (1u << 24)) {
+        cg_set_error(ctx, "set_bias: need at least 5 (z, value) samples");
+        return COFFE_GPU_EINVAL;
+    }
+    for (size_t i = 1; i < n; ++i)
+        if (!(z[i] > z[i - 1])) {
+            cg_set_error(ctx, "set_bias: z must be strictly increasing");
+            return COFFE_GPU_EINVAL;
+        }
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    int st = cg_ensure(ctx, ctx->bias_nodes[which], sizeof(double) * 2 * n);
+    if (st) return st;
+    double *d = (double *)ctx->bias_nodes[which].p;
+    CG_CUDA(ctx, cudaMemcpyAsync(d, z, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CG_CUDA(ctx, cudaMemcpyAsync(d + n, value, sizeof(double) * n, cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    ctx->bias_set[which] = false;
+    st = spline_build(ctx, ctx->bias[which], d, d + n, (int)n);
+    if (st) return st;
+    ctx->bias_set[which] = true;
+    return cg_check_device_errors(ctx, "set_bias");
+}
+
+size_t coffe_gpu_integral_table_len(size_t N) { return N + CG_N_SMALL_R + 1; }
+
+int coffe_gpu_integrals_init(coffe_gpu_ctx_t *ctx, const double *k, const double *pk,
+                             int n_spectra, size_t nk, const int *n, const int *l, int n_terms,
+                             size_t N, int precision, unsigned flags)
+{
+    if (!ctx) return COFFE_GPU_EINVAL;
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int st = integrals_build(ctx, k, pk, n_spectra, nk, n, l, n_terms, N, precision, flags);
+    if (st) {
+        ctx->int_ready = false;
+        return st;
+    }
+    if (flags & COFFE_GPU_ASYNC) return COFFE_GPU_OK;
+    const int st2 = cg_check_device_errors(ctx, "integrals_init");
+    if (st2) ctx->int_ready = false;
+    return st2;
+}
+
+int coffe_gpu_integral_get(coffe_gpu_ctx_t *ctx, int spectrum, int term, double *x, double *y)
+{
+    if (!ctx) return COFFE_GPU_EINVAL;
+    if (!ctx->int_ready) {
+        cg_set_error(ctx, "integral_get: integrals not initialised");
+        return COFFE_GPU_ESTATE;
+    }
+    if (spectrum < 0 || spectrum >= ctx->n_spectra || term < 0 || term >= ctx->n_terms) {
+        cg_set_error(ctx, "integral_get: (spectrum %d, term %d) out of range", spectrum, term);
+        return COFFE_GPU_EINVAL;
+    }
+    const size_t len = ctx->N + CG_N_SMALL_R + 1;
+    const size_t off = ((size_t)spectrum * ctx->n_terms + term) * len;
+    if (x)
+        CG_CUDA(ctx, cudaMemcpyAsync(x, ctx->tab_x.p, sizeof(double) * len, cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+    if (y) {
+        if (ctx->int_precision == COFFE_GPU_MIXED) {
+            std::vector<float> tmp(len);
+            CG_CUDA(ctx, cudaMemcpyAsync(tmp.data(), (const float *)ctx->tab_y.p + off,
+                                         sizeof(float) * len, cudaMemcpyDeviceToHost, ctx->stream));
+            CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            for (size_t i = 0; i < len; ++i) y[i] = tmp[i];
+        } else {
+            CG_CUDA(ctx, cudaMemcpyAsync(y, (const double *)ctx->tab_y.p + off,
+                                         sizeof(double) * len, cudaMemcpyDeviceToHost, ctx->stream));
+        }
+    }
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return COFFE_GPU_OK;
+}
+
+int coffe_gpu_integral_eval(coffe_gpu_ctx_t *ctx, int spectrum, int term, const double *r,
+                            size_t nq, double *out)
+{
+    if (!ctx || (nq && (!r || !out))) return COFFE_GPU_EINVAL;
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int st = integrals_eval(ctx, spectrum, term, r, nq, out);
+    if (st) return st;
+    return cg_check_device_errors(ctx, "integral_eval");
+}
+
+int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, double epsrel,
+                         int n_req, const int *req_spectrum, const double *req_z_mean,
+                         const int64_t *req_offset, const double *sep, int n_l, const int *l,
+                         double *out, int arrays_on_device)
+{
+    if (!ctx || !req_spectrum || !req_z_mean || !req_offset || !l || n_req < 1 || n_l < 1)
+        return COFFE_GPU_EINVAL;
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (arrays_on_device) {
+        int ls[64];
+        if (n_l > 64) return COFFE_GPU_EINVAL;
+        CG_CUDA(ctx, cudaMemcpyAsync(ls, l, sizeof(int) * n_l, cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+        CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        int64_t total = 0;
+        CG_CUDA(ctx, cudaMemcpyAsync(&total, req_offset + n_req, sizeof(int64_t),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+        CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        const int st = multipoles_run(ctx, contrib, precision, epsrel, n_req, req_spectrum,
+                                      req_z_mean, req_offset, sep, n_l, ls, out, total);
+        if (st) return st;
+        return cg_check_device_errors(ctx, "multipoles");
+    }
+    // host arrays: validate, stage, run, copy back
+    if (req_offset[0] != 0) {
+        cg_set_error(ctx, "multipoles: req_offset[0] must be 0");
+        return COFFE_GPU_EINVAL;
+    }
+    for (int q = 0; q < n_req; ++q) {
+        if (req_offset[q + 1] < req_offset[q]) {
+            cg_set_error(ctx, "multipoles: req_offset must be non-decreasing");
+            return COFFE_GPU_EINVAL;
+        }
+        if (req_spectrum[q] < 0 || req_spectrum[q] >= ctx->n_spectra) {
+            cg_set_error(ctx, "multipoles: request %d names spectrum %d of %d", q, req_spectrum[q],
+                         ctx->n_spectra);
+            return COFFE_GPU_EINVAL;
+        }
+        if (!(req_z_mean[q] >= 0)) {
+            cg_set_error(ctx, "multipoles: request %d has a bad mean redshift", q);
+            return COFFE_GPU_EINVAL;
+        }
+    }
+    const int64_t total = req_offset[n_req];
+    if (total > 0 && (!sep || !out)) return COFFE_GPU_EINVAL;
+    for (int64_t i = 0; i < total; ++i)
+        if (!(sep[i] > 0)) {
+            cg_set_error(ctx, "multipoles: separations must be positive");
+            return COFFE_GPU_EINVAL;
+        }
+    const size_t b_spec = sizeof(int) * n_req, b_z = sizeof(double) * n_req,
+                 b_off = sizeof(int64_t) * (n_req + 1), b_sep = sizeof(double) * total,
+                 b_out = sizeof(double) * total * n_l;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t bytes = al(b_spec) + al(b_z) + al(b_off) + al(b_sep) + al(b_out);
+    int st = cg_ensure(ctx, ctx->req_buf, bytes);
+    if (st) return st;
+    char *base = (char *)ctx->req_buf.p;
+    int *d_spec = (int *)base;
+    double *d_z = (double *)(base + al(b_spec));
+    int64_t *d_off = (int64_t *)(base + al(b_spec) + al(b_z));
+    double *d_sep = (double *)(base + al(b_spec) + al(b_z) + al(b_off));
+    double *d_out = (double *)(base + al(b_spec) + al(b_z) + al(b_off) + al(b_sep));
+    CG_CUDA(ctx, cudaMemcpyAsync(d_spec, req_spectrum, b_spec, cudaMemcpyHostToDevice, ctx->stream));
+    CG_CUDA(ctx, cudaMemcpyAsync(d_z, req_z_mean, b_z, cudaMemcpyHostToDevice, ctx->stream));
+    CG_CUDA(ctx, cudaMemcpyAsync(d_off, req_offset, b_off, cudaMemcpyHostToDevice, ctx->stream));
+    if (total > 0)
+        CG_CUDA(ctx, cudaMemcpyAsync(d_sep, sep, b_sep, cudaMemcpyHostToDevice, ctx->stream));
+    st = multipoles_run(ctx, contrib, precision, epsrel, n_req, d_spec, d_z, d_off, d_sep, n_l, l,
+                        d_out, total);
+    if (st) return st;
+    if (total > 0)
+        CG_CUDA(ctx, cudaMemcpyAsync(out, d_out, b_out, cudaMemcpyDeviceToHost, ctx->stream));
+    return cg_check_device_errors(ctx, "multipoles");
+}
+
+int coffe_gpu_multipoles_async(coffe_gpu_ctx_t *ctx, int contrib, int precision, double epsrel,
+                               int n_req, int64_t n_sep, const int *req_spectrum,
+                               const double *req_z_mean, const int64_t *req_offset,
+                               const double *sep, int n_l, const int *l, double *out)
+{
+    if (!ctx || !req_spectrum || !req_z_mean || !req_offset || !l || n_req < 1 || n_l < 1 ||
+        n_sep < 0 || (n_sep > 0 && (!sep || !out)))
+        return COFFE_GPU_EINVAL;
+    return multipoles_run(ctx, contrib, precision, epsrel, n_req, req_spectrum, req_z_mean,
+                          req_offset, sep, n_l, l, out, n_sep);
+}
+
+} // extern "C"

@@ -1,0 +1,96 @@
+// Host-side context of the C ABI (include/coffe_gpu.h): device buffers, the
+// stream, error state and the cached per-grid tables.
+#pragma once
+
+#include <stdarg.h>
+#include <stdio.h>
+
+#include <vector>
+
+#include "spline.cuh"
+
+#define CG_MAX_TERMS 64
+#define CG_N_SMALL_R 42
+
+// Device buffer that only grows.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+enum cg_bg_fn { BG_CHI_OF_Z = 0, BG_Z_OF_CHI, BG_D1, BG_F, BG_A, BG_CONFH, BG_NFN };
+
+struct coffe_gpu_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    int *d_err = nullptr;   // device error bits (cg_err_bits)
+    int *h_err = nullptr;   // pinned mirror
+    long long launches = 0; // kernels launched through this context
+    int sm_count = 0;
+    char last_error[512] = {0};
+
+    // ---- background
+    int bg_bins = 0;
+    bool bg_ready = false, bg_has_H = false;
+    double Omega0_m = 0.3, h = 0.67;
+    DevBuf bg_nodes; // bins * 8 doubles: z, chi, D1, f, a, confH, H, confHp
+    SplineBuf bg[BG_NFN];
+    SplineBuf bias[4];
+    bool bias_set[4] = {false, false, false, false};
+    DevBuf bias_nodes[4];
+
+    // ---- integral tables
+    bool int_ready = false;
+    int n_spectra = 0, n_terms = 0, int_precision = 0;
+    size_t N = 0, nk = 0;
+    double kmin = 0, kmax = 0;
+    int term_n[CG_MAX_TERMS], term_l[CG_MAX_TERMS], term_q[CG_MAX_TERMS];
+    int n_q = 0;
+    double qvals[CG_MAX_TERMS];
+    DevBuf tab_x;     // (N + 43) doubles, shared by all tables
+    DevBuf tab_x32;   // same in float
+    DevBuf tab_y;     // n_spectra * n_terms * (N + 43), double or float
+    DevBuf pk;        // n_spectra * nk doubles (input spectra)
+    DevBuf kgrid;     // nk doubles
+    DevBuf csc;       // n_spectra * nk doubles: natural-spline c coefficients
+    DevBuf csfac;     // 2 * nk doubles: Thomas factors of the shared k grid
+    DevBuf samp_idx;  // N ints: input interval of each FFT node
+    DevBuf samp_dx;   // N doubles: offset of each FFT node in its interval
+    DevBuf qfac;      // n_q * N doubles: (kmax/kmin)^((3-q) i/N) W(k_i)
+    DevBuf modec;     // n_terms * (N/2+1) double2: W_mode/L * M_{q,l}(t)
+    DevBuf postf;     // n_terms * N doubles: prefactor * r^(n-l)
+    DevBuf twid;      // N/2+1 double2 twiddles exp(-2 pi i j / N)
+    DevBuf twid32;    // float2 copy
+    DevBuf spec;      // n_spectra * n_q * (N/2+1) double2 forward half spectra
+    // cache key of the per-grid tables
+    size_t grid_N = 0, grid_nk = 0;
+    double grid_kmin = 0, grid_kmax = 0;
+    std::vector<double> grid_k;
+    std::vector<int> grid_terms;
+
+    DevBuf term_meta; // per-term metadata of the integral tables
+
+    // ---- multipole request staging (host-pointer calls)
+    DevBuf req_buf;
+};
+
+void cg_set_error(coffe_gpu_ctx *ctx, const char *fmt, ...);
+int cg_ensure(coffe_gpu_ctx *ctx, DevBuf &b, size_t bytes);
+void cg_release(DevBuf &b);
+// Reads and clears the device error bits; maps them to a status.
+int cg_check_device_errors(coffe_gpu_ctx *ctx, const char *where);
+// Checks the last launch; counts it.
+int cg_after_launch(coffe_gpu_ctx *ctx, const char *what);
+
+// module entry points (host code)
+int bg_init_device(coffe_gpu_ctx *ctx, const coffe_gpu_cosmology_t *c);
+int bg_build_splines(coffe_gpu_ctx *ctx);
+int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n_spectra,
+                    size_t nk, const int *n, const int *l, int n_terms, size_t N, int precision,
+                    unsigned flags);
+int integrals_eval(coffe_gpu_ctx *ctx, int spectrum, int term, const double *r, size_t nq,
+                   double *out);
+int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, int n_req,
+                   const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
+                   const double *sep, int n_l, const int *l, double *out, long long total);

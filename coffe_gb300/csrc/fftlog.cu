@@ -1,0 +1,825 @@
+// Batched FFTLog Bessel integrals I_l^n(r) on the device.
+//
+// Restates twofast_1bessel (twofast.c:362-483) and the table assembly of
+// coffe_integrals_renormalizable (integrals.c:459-573) for many spectra:
+//   1. P(k) is resampled on the FFT grid k_i = kmin (kmax/kmin)^(i/N) through
+//      the natural cubic spline of the input table (twofast.c:399-401), biased
+//      by (kmax/kmin)^((3-q) i/N) and tapered (twofast.c:275-290);
+//   2. real FFT, conjugate, Fourier-mode taper / L (twofast.c:292-355);
+//   3. per (n, l): multiply by the Gamma-ratio kernel M_{q,l}(t)
+//      (twofast_mql, twofast.c:196-224), inverse real FFT (FFTW c2r,
+//      unnormalised), times the prefactor (twofast.c:419-422) and r^(n-l).
+// Everything that does not depend on the spectrum (sampling positions,
+// biases, tapers, M_{q,l}, prefactors, twiddles) is a per-grid table built
+// once; a spectrum costs one forward FFT per distinct q and one inverse FFT
+// per term.  One CTA holds one transform in shared memory (radix-2, in place).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "cplx.cuh"
+#include "ctx.cuh"
+#include "qag.cuh"
+
+namespace {
+
+// the 42 sub-Mpc separations evaluated by direct quadrature (integrals.c:111-126)
+const double h_min_sep[CG_N_SMALL_R] = {
+    1E-6,   1E-5,    1E-4,   1E-3,    2E-3,   5E-3,   7E-3,   8E-3,    9E-3,   1E-2,    1.1E-2,
+    1.2E-2, 1.25E-2, 1.3E-2, 1.35E-2, 1.5E-2, 2E-2,   2.5E-2, 3E-2,    3.5E-2, 5E-2,    7E-2,
+    8E-2,   9E-2,    1E-1,   1.1E-1,  1.2E-1, 1.25E-1, 1.3E-1, 1.35E-1, 1.5E-1, 1.75E-1, 2E-1,
+    2.5E-1, 3E-1,    3.5E-1, 4E-1,    5E-1,   6E-1,   7E-1,   8E-1,    9E-1};
+
+// twofast_selectqnu (twofast.c:240-250)
+double select_qnu(double l, double nu)
+{
+    const double n1 = 0.9, n2 = 0.9999;
+    const double qmin = std::max(n2 - 1.0 - nu, -l);
+    const double qmax = std::min(n1 + 3.0 - nu, 2.0);
+    const double qbest = (2. + n1 + n2) / 2. - nu;
+    double q = qbest;
+    if (!(qmin < q && q < qmax)) q = (qmin + 2. * qmax) / 3.;
+    return q;
+}
+
+__device__ __forceinline__ double twofast_window(double value, double xmin, double xmax,
+                                                 double xleft, double xright)
+{
+    double result;
+    if (value > xleft && value < xright && value > xmin && value < xmax)
+        result = 1.0;
+    else if (value <= xmin || value >= xmax)
+        result = 0.0;
+    else {
+        if (value <= xleft)
+            result = (value - xmin) / (xleft - xmin);
+        else
+            result = (xmax - value) / (xmax - xright);
+        result = result - sin(2 * CG_PI * result) / 2. / CG_PI;
+    }
+    return result;
+}
+
+struct GridPar {
+    double kmin, kmax, k0, r0;
+    int N, nk;
+};
+
+// --------------------------------------------------------------- per grid
+
+// Thomas factors of the natural-spline system on the shared k grid (one thread).
+__global__ void csfac_kernel(const double *__restrict__ x, int nk, double *__restrict__ fac)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const int m = nk - 2;
+    double *diag = fac, *w = fac + nk;
+    for (int i = 0; i < m; ++i) {
+        const double h_i = x[i + 1] - x[i];
+        const double h_ip1 = x[i + 2] - x[i + 1];
+        diag[i] = 2.0 * (h_ip1 + h_i);
+    }
+    w[0] = 0.0;
+    for (int i = 1; i < m; ++i) {
+        const double off = x[i + 1] - x[i];
+        w[i] = off / diag[i - 1];
+        diag[i] -= w[i] * off;
+    }
+}
+
+// FFT node -> (input interval, offset); windowed bias per distinct q
+__global__ void sampling_kernel(GridPar g, const double *__restrict__ kx, int *__restrict__ idx,
+                                double *__restrict__ dxs, int n_q, const double *__restrict__ qv,
+                                double *__restrict__ qfac, double *__restrict__ modew,
+                                double *__restrict__ tab_x, float *__restrict__ tab_x32)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = g.N;
+    const double ratio = g.kmax / g.kmin;
+    const double xmax_w = g.k0 * pow(ratio, (double)(N - 1) / N);
+    const double xleft_w = exp(0.46) * g.kmin;
+    const double xright_w = exp(-0.46) * g.k0 * pow(ratio, (double)(N - 1) / N);
+    if (i < N) {
+        const double ki = g.k0 * pow(ratio, (double)i / N);
+        int lo = 0, hi = g.nk - 1;
+        while (hi > lo + 1) {
+            const int mid = (lo + hi) / 2;
+            if (kx[mid] > ki)
+                hi = mid;
+            else
+                lo = mid;
+        }
+        const bool inside = ki >= kx[0] && ki <= kx[g.nk - 1];
+        idx[i] = inside ? lo : -1;
+        dxs[i] = ki - kx[lo];
+        const double w = twofast_window(ki, g.kmin, xmax_w, xleft_w, xright_w);
+        for (int q = 0; q < n_q; ++q) qfac[(size_t)q * N + i] = pow(ratio, (3. - qv[q]) * i / N) * w;
+        const double ri = g.r0 * pow(ratio, (double)i / N);
+        tab_x[CG_N_SMALL_R + 1 + i] = ri;
+        tab_x32[CG_N_SMALL_R + 1 + i] = (float)ri;
+    }
+    const int M = N / 2;
+    if (i <= M) {
+        // Fourier-mode taper at x_mod[N2 - 2 + i] (twofast.c:298-355), over L
+        const double L = 2 * CG_PI * N / log(ratio);
+        const double xm = g.k0 * pow(ratio, (double)(M - 1 + i) / N);
+        modew[i] = twofast_window(xm, g.kmin, xmax_w, xleft_w, xright_w) / L;
+    }
+}
+
+// Gamma-ratio kernel M_{q,l}(t_m) of every term (FP64, twofast_mql) and the
+// output prefactor times r^(n-l) (twofast.c:419-422, integrals.c:514-523)
+__global__ void term_tables_kernel(GridPar g, int n_terms, const double *__restrict__ tq,
+                                   const double *__restrict__ tl, const double *__restrict__ tn,
+                                   double2 *__restrict__ mcoef, double *__restrict__ postf,
+                                   int *err)
+{
+    const int N = g.N, M = N / 2;
+    const int t = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_terms) return;
+    const double qnu = tq[t], l = tl[t], nu = tn[t];
+    const double G = log(g.kmax / g.kmin);
+    if (i <= M) {
+        const double tt = 2 * CG_PI * i / G;
+        const cplx n = cx(qnu - 1., -tt);
+        cplx lg1, lg2;
+        const bool ok1 = cx_lgamma_lanczos(cx((1. + l + n.re) / 2., n.im / 2.), &lg1);
+        const bool ok2 = cx_lgamma_lanczos(cx((2. + l - n.re) / 2., -n.im / 2.), &lg2);
+        double2 out = make_double2(0.0, 0.0);
+        if (!ok2) {
+            cg_flag(err, CG_ERR_NONFINITE);
+        } else if (ok1) {
+            const cplx unl = cx_rpow(2.0, cx(n.re - 1., n.im)) * (CG_SQRT_PI * cx_exp(lg1 - lg2));
+            if (!(isfinite(unl.re) && isfinite(unl.im))) {
+                cg_flag(err, CG_ERR_NONFINITE);
+            } else {
+                const cplx m = cx_rpow(g.k0 * g.r0, cx(-qnu, tt)) * unl;
+                out = make_double2(m.re, m.im);
+            }
+        }
+        // ok1 == false: the reflection overflowed, lnGamma = -inf, M = 0
+        mcoef[(size_t)t * (M + 1) + i] = out;
+    }
+    if (i < N) {
+        const double ratio = g.kmax / g.kmin;
+        double p = g.k0 * g.k0 * g.k0 * pow(ratio, -((qnu + nu) * i / N)) / CG_PI /
+                   pow(g.r0 * g.k0, nu) / G;
+        if (nu >= l) p *= pow(g.r0 * pow(ratio, (double)i / N), nu - l);
+        postf[(size_t)t * N + i] = p;
+    }
+}
+
+__global__ void twiddle_kernel(int N, double2 *__restrict__ tw, float2 *__restrict__ tw32)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j > N / 2) return;
+    double s, c;
+    sincospi(2.0 * (double)j / (double)N, &s, &c);
+    tw[j] = make_double2(c, -s);
+    tw32[j] = make_float2((float)c, (float)-s);
+}
+
+// ------------------------------------------------------------ per spectrum
+
+// natural cubic spline coefficients c_i (= y''/2) of each spectrum (one thread
+// per spectrum; forward elimination and back substitution with the grid's
+// Thomas factors, in the order of gsl's tridiagonal solve)
+__global__ void cspline_c_kernel(const double *__restrict__ x, const double *__restrict__ pk,
+                                 const double *__restrict__ fac, int nk, int n_spectra,
+                                 double *__restrict__ cc)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_spectra) return;
+    const double *y = pk + (size_t)s * nk;
+    double *c = cc + (size_t)s * nk;
+    const double *diag = fac, *w = fac + nk;
+    const int m = nk - 2;
+    // forward sweep (rhs stored in c[1..m])
+    double prev = 0.0;
+    for (int i = 0; i < m; ++i) {
+        const double g_i = 1.0 / (x[i + 1] - x[i]);
+        const double g_ip1 = 1.0 / (x[i + 2] - x[i + 1]);
+        double r = 3.0 * ((y[i + 2] - y[i + 1]) * g_ip1 - (y[i + 1] - y[i]) * g_i);
+        if (i > 0) r -= w[i] * prev;
+        c[i + 1] = r;
+        prev = r;
+    }
+    c[0] = 0.0;
+    c[nk - 1] = 0.0;
+    double next = c[m] / diag[m - 1];
+    c[m] = next;
+    for (int i = m - 2; i >= 0; --i) {
+        const double off = x[i + 2] - x[i + 1];
+        next = (c[i + 1] - off * next) / diag[i];
+        c[i + 1] = next;
+    }
+}
+
+template <typename T> struct V2;
+template <> struct V2<double> { typedef double2 t; };
+template <> struct V2<float> { typedef float2 t; };
+
+template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b)
+{
+    T2 r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+
+// In-place radix-2 DIT FFT of M = 2^logM points already in bit-reversed
+// order; tw[j] = exp(-2 pi i j / (2M)), so the M-point twiddle w_M^e is
+// tw[2e].  sign = -1 forward, +1 backward (conjugate twiddles).
+template <typename T2>
+__device__ void smem_fft(T2 *buf, int logM, const T2 *__restrict__ tw, int sign)
+{
+    const int M = 1 << logM;
+    for (int s = 1; s <= logM; ++s) {
+        const int half = 1 << (s - 1);
+        const int stride = M >> (s - 1); // index step in tw (2 * M / (2 half))
+        for (int b = threadIdx.x; b < M / 2; b += blockDim.x) {
+            const int pos = b & (half - 1);
+            const int i0 = ((b >> (s - 1)) << s) + pos;
+            const int i1 = i0 + half;
+            T2 w = tw[pos * stride];
+            if (sign > 0) w.y = -w.y;
+            const T2 u = buf[i0];
+            const T2 t = cmul(w, buf[i1]);
+            buf[i0].x = u.x + t.x;
+            buf[i0].y = u.y + t.y;
+            buf[i1].x = u.x - t.x;
+            buf[i1].y = u.y - t.y;
+        }
+        __syncthreads();
+    }
+}
+
+// Forward half: sample, bias, FFT, conjugate, mode taper.  Grid (spectrum, q).
+template <typename T>
+__global__ void fftlog_forward_kernel(GridPar g, const double *__restrict__ kx,
+                                      const double *__restrict__ pk,
+                                      const double *__restrict__ cc, const int *__restrict__ idx,
+                                      const double *__restrict__ dxs,
+                                      const double *__restrict__ qfac,
+                                      const double *__restrict__ modew,
+                                      const typename V2<T>::t *__restrict__ tw, int n_q,
+                                      typename V2<T>::t *__restrict__ spec, int *err)
+{
+    typedef typename V2<T>::t T2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T2 *buf = reinterpret_cast<T2 *>(smem_raw);
+    const int s = blockIdx.x, qi = blockIdx.y;
+    const int N = g.N, M = N / 2;
+    const int logM = 31 - __clz(M);
+    const double *y = pk + (size_t)s * g.nk;
+    const double *c = cc + (size_t)s * g.nk;
+    bool bad = false;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const int j = idx[i];
+        T v;
+        if (j < 0) {
+            v = cg_nan<T>();
+        } else {
+            const T h = (T)(kx[j + 1] - kx[j]);
+            const T y0 = (T)y[j], y1 = (T)y[j + 1], c0 = (T)c[j], c1 = (T)c[j + 1];
+            const T b = (y1 - y0) / h - h * (c1 + T(2) * c0) / T(3);
+            const T d = (c1 - c0) / (T(3) * h);
+            const T dx = (T)dxs[i];
+            const T p = y0 + dx * (b + dx * (c0 + d * dx));
+            v = p * (T)qfac[(size_t)qi * N + i];
+        }
+        if (!isfinite(v)) bad = true;
+        const int jj = __brev((unsigned)(i >> 1)) >> (32 - logM);
+        if (i & 1)
+            buf[jj].y = v;
+        else
+            buf[jj].x = v;
+    }
+    if (bad) cg_flag(err, CG_ERR_NONFINITE);
+    __syncthreads();
+    smem_fft<T2>(buf, logM, tw, -1);
+    // unpack the real FFT: Y_k = (Z_k + conj Z_{M-k})/2 - i w^k (Z_k - conj Z_{M-k})/2
+    T2 *out = spec + ((size_t)s * n_q + qi) * (M + 1);
+    for (int k = threadIdx.x; k <= M; k += blockDim.x) {
+        const T2 zk = buf[k & (M - 1)];
+        const T2 zm = buf[(M - k) & (M - 1)];
+        const T ex = T(0.5) * (zk.x + zm.x), ey = T(0.5) * (zk.y - zm.y);
+        const T ox = T(0.5) * (zk.y + zm.y), oy = T(-0.5) * (zk.x - zm.x);
+        const T2 w = tw[k];
+        const T yx = ex + (w.x * ox - w.y * oy);
+        const T yy = ey + (w.x * oy + w.y * ox);
+        const T mw = (T)modew[k];
+        T2 o;
+        o.x = mw * yx;
+        o.y = -mw * yy; // conjugate
+        out[k] = o;
+    }
+}
+
+// Inverse half: multiply by M_{q,l}, c2r, prefactor.  Grid (spectrum, term).
+template <typename T, typename TO>
+__global__ void fftlog_inverse_kernel(GridPar g, const typename V2<T>::t *__restrict__ spec,
+                                      const int *__restrict__ term_q, int n_q, int n_terms,
+                                      const double2 *__restrict__ mcoef,
+                                      const double *__restrict__ postf,
+                                      const typename V2<T>::t *__restrict__ tw,
+                                      TO *__restrict__ tab, int *err)
+{
+    typedef typename V2<T>::t T2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T2 *buf = reinterpret_cast<T2 *>(smem_raw);
+    const int s = blockIdx.x, t = blockIdx.y;
+    const int N = g.N, M = N / 2;
+    const int logM = 31 - __clz(M);
+    const T2 *in = spec + ((size_t)s * n_q + term_q[t]) * (M + 1);
+    const double2 *mc = mcoef + (size_t)t * (M + 1);
+    // X_k = S_k M_k with Im X_0 = Im X_M = 0 (FFTW c2r ignores them)
+    for (int k = threadIdx.x; k < M; k += blockDim.x) {
+        const int km = M - k;
+        const double2 ma = mc[k], mb = mc[km];
+        const T2 sa = in[k], sb = in[km];
+        T2 xa, xb;
+        xa.x = sa.x * (T)ma.x - sa.y * (T)ma.y;
+        xa.y = sa.x * (T)ma.y + sa.y * (T)ma.x;
+        xb.x = sb.x * (T)mb.x - sb.y * (T)mb.y;
+        xb.y = sb.x * (T)mb.y + sb.y * (T)mb.x;
+        if (k == 0) {
+            xa.y = T(0);
+            xb.y = T(0);
+        }
+        // Fe = X_k + conj X_{M-k};  Fo = (X_k - conj X_{M-k}) conj(w^k);  Z = Fe + i Fo
+        const T fex = xa.x + xb.x, fey = xa.y - xb.y;
+        const T dx = xa.x - xb.x, dy = xa.y + xb.y;
+        const T2 w = tw[k];
+        const T fox = dx * w.x + dy * w.y;
+        const T foy = dy * w.x - dx * w.y;
+        T2 z;
+        z.x = fex - foy;
+        z.y = fey + fox;
+        const int jj = __brev((unsigned)k) >> (32 - logM);
+        buf[jj] = z;
+    }
+    __syncthreads();
+    smem_fft<T2>(buf, logM, tw, +1);
+    const size_t len = (size_t)N + CG_N_SMALL_R + 1;
+    TO *o = tab + ((size_t)s * n_terms + t) * len + CG_N_SMALL_R + 1;
+    const double *pf = postf + (size_t)t * N;
+    bool bad = false;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const T2 z = buf[i >> 1];
+        const T v = (i & 1) ? z.y : z.x;
+        const TO r = (TO)((double)v * pf[i]);
+        if (!isfinite((double)r)) bad = true;
+        o[i] = r;
+    }
+    if (bad) cg_flag(err, CG_ERR_NONFINITE);
+}
+
+// ------------------------------------------------- r = 0 and sub-Mpc points
+
+// j_l(x): ascending series below max(1, l + 1), upward recurrence above
+__device__ double sph_bessel(int l, double x)
+{
+    const double thr = (l < 1 ? 1.0 : (double)l + 1.0);
+    if (x < thr) {
+        double pref = 1.0;
+        for (int k = 1; k <= l; ++k) pref *= x / (2.0 * k + 1.0);
+        const double yy = -0.5 * x * x;
+        double term = 1.0, sum = 1.0;
+        for (int k = 1; k < 200; ++k) {
+            term *= yy / ((double)k * (2.0 * l + 2.0 * k + 1.0));
+            sum += term;
+            if (fabs(term) < 1e-17 * fabs(sum)) break;
+        }
+        return pref * sum;
+    }
+    double sn, cs;
+    sincos(x, &sn, &cs);
+    double j0 = sn / x;
+    if (l == 0) return j0;
+    double j1 = (sn / x - cs) / x;
+    for (int k = 1; k < l; ++k) {
+        const double j2 = (2.0 * k + 1.0) / x * j1 - j0;
+        j0 = j1;
+        j1 = j2;
+    }
+    return j1;
+}
+
+// Akima spline of the input P(k) (power_spectrum_norm, interp_method default)
+struct PkAkima {
+    const double *x, *y;
+    int n;
+    __device__ double operator()(double k) const
+    {
+        if (!(k >= x[0] && k <= x[n - 1])) return cg_nan<double>();
+        int lo = 0, hi = n - 1;
+        while (hi > lo + 1) {
+            const int mid = (lo + hi) / 2;
+            if (x[mid] > k)
+                hi = mid;
+            else
+                lo = mid;
+        }
+        return akima_eval_at<double>(x, y, n, lo, k);
+    }
+};
+
+// k^2 P(k) j_l(k r) / (k r)^n  (integrals.c:280-325)
+struct BesselIntegrand {
+    PkAkima pk;
+    double r;
+    int n, l;
+    __device__ double operator()(double k) const
+    {
+        const double bf = sph_bessel(l, k * r) / pow(k * r, (double)n);
+        return k * k * pk(k) * bf;
+    }
+};
+
+// k^(2+l-n) P(k)  (integrals.c:238-269)
+struct PrefactorIntegrand {
+    PkAkima pk;
+    int n, l;
+    __device__ double operator()(double k) const { return pow(k, 2.0 + l - n) * pk(k); }
+};
+
+#define SR_WARPS 4
+#define SR_CAP 256
+
+// One warp per (spectrum, term, point j): j = 0 is r = 0, j = 1..42 the
+// sub-Mpc separations (integrals.c:524-562), GK61 QAG with epsrel 1e-5.
+template <typename TO>
+__global__ void __launch_bounds__(32 * SR_WARPS)
+    small_r_kernel(const double *__restrict__ kx, const double *__restrict__ pk, int nk,
+                   int n_spectra, int n_terms, const int *__restrict__ tn,
+                   const int *__restrict__ tl, const double *__restrict__ tab_x, size_t len,
+                   TO *__restrict__ tab, int *err)
+{
+    __shared__ double sa[SR_WARPS][SR_CAP], sb[SR_WARPS][SR_CAP], sr[SR_WARPS][SR_CAP],
+        se[SR_WARPS][SR_CAP];
+    const int w = threadIdx.x >> 5;
+    const long item = (long)blockIdx.x * SR_WARPS + w;
+    const long total = (long)n_spectra * n_terms * (CG_N_SMALL_R + 1);
+    if (item >= total) return;
+    const int j = (int)(item % (CG_N_SMALL_R + 1));
+    const long st_ = item / (CG_N_SMALL_R + 1);
+    const int t = (int)(st_ % n_terms);
+    const int s = (int)(st_ / n_terms);
+    const int n = tn[t], l = tl[t];
+    PkAkima P{kx, pk + (size_t)s * nk, nk};
+    QagStore<double> store{sa[w], sb[w], sr[w], se[w], SR_CAP};
+    int status = 0;
+    double v;
+    const double kmin = kx[0], kmax = kx[nk - 1];
+    if (j == 0) {
+        if (n >= l) {
+            PrefactorIntegrand f{P, n, l};
+            const double res = qag61_warp<double>(f, kmin, kmax, 0.0, 1e-5, store, 50000, &status);
+            const double coeff = sqrt(CG_PI / 2.) / pow(2.0, l + 0.5) / tgamma(l + 1.5);
+            v = res / 2. / CG_PI / CG_PI * coeff;
+        } else {
+            v = 0.0;
+        }
+    } else {
+        const double r = tab_x[j];
+        BesselIntegrand f{P, r, n, l};
+        double res = qag61_warp<double>(f, kmin, kmax, 0.0, 1e-5, store, 50000, &status);
+        if (n >= l) res = res * pow(r, (double)(n - l));
+        v = res / 2. / CG_PI / CG_PI;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (status == 1) cg_flag(err, CG_ERR_QAG_LIMIT);
+        if (!isfinite(v)) cg_flag(err, CG_ERR_NONFINITE);
+        tab[((size_t)s * n_terms + t) * len + j] = (TO)v;
+    }
+}
+
+template <typename TO> __global__ void fill_nan_kernel(TO *tab, size_t len, long count)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count * (CG_N_SMALL_R + 1)) return;
+    const long tb = i / (CG_N_SMALL_R + 1), j = i % (CG_N_SMALL_R + 1);
+    tab[tb * len + j] = (TO)cg_nan<double>();
+}
+
+__global__ void table_eval_kernel(const double *__restrict__ x, const double *__restrict__ y,
+                                  int n, const double *__restrict__ r, int nq,
+                                  double *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    const double v = r[i];
+    if (!(v >= x[0] && v <= x[n - 1])) {
+        out[i] = cg_nan<double>();
+        return;
+    }
+    int lo = 0, hi = n - 1;
+    while (hi > lo + 1) {
+        const int mid = (lo + hi) / 2;
+        if (x[mid] > v)
+            hi = mid;
+        else
+            lo = mid;
+    }
+    out[i] = akima_eval_at<double>(x, y, n, lo, v);
+}
+
+__global__ void table_f32_to_f64_kernel(const float *__restrict__ in, double *__restrict__ out,
+                                        size_t n)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (double)in[i];
+}
+
+bool same_grid(const coffe_gpu_ctx *ctx, const double *k, size_t nk, size_t N,
+               const std::vector<int> &terms)
+{
+    if (ctx->grid_N != N || ctx->grid_nk != nk || ctx->grid_terms != terms) return false;
+    if (ctx->grid_k.size() != nk) return false;
+    return std::memcmp(ctx->grid_k.data(), k, sizeof(double) * nk) == 0;
+}
+
+} // namespace
+
+int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n_spectra,
+                    size_t nk, const int *n, const int *l, int n_terms, size_t N, int precision,
+                    unsigned flags)
+{
+    if (!k || !pk || !n || !l || n_spectra < 1 || n_terms < 1 || n_terms > CG_MAX_TERMS) {
+        cg_set_error(ctx, "integrals: bad arguments (n_spectra=%d, n_terms=%d)", n_spectra,
+                     n_terms);
+        return COFFE_GPU_EINVAL;
+    }
+    if (N < 64 || N > 16384 || (N & (N - 1))) {
+        cg_set_error(ctx, "integrals: N must be a power of two in [64, 16384] (got %zu)", N);
+        return COFFE_GPU_EINVAL;
+    }
+    if (nk < 5 || nk > (1u << 22)) {
+        cg_set_error(ctx, "integrals: need 5 <= nk <= 2^22 k samples (got %zu)", nk);
+        return COFFE_GPU_EINVAL;
+    }
+    if (precision != COFFE_GPU_FP64 && precision != COFFE_GPU_MIXED) {
+        cg_set_error(ctx, "integrals: unknown precision %d", precision);
+        return COFFE_GPU_EINVAL;
+    }
+    for (size_t i = 0; i < nk; ++i)
+        if (!(k[i] > 0) || (i > 0 && !(k[i] > k[i - 1]))) {
+            cg_set_error(ctx, "integrals: k must be positive and strictly increasing");
+            return COFFE_GPU_EINVAL;
+        }
+    for (int t = 0; t < n_terms; ++t)
+        if (l[t] < 0 || l[t] > 16 || n[t] < -4 || n[t] > 16) {
+            cg_set_error(ctx, "integrals: unsupported term (n=%d, l=%d)", n[t], l[t]);
+            return COFFE_GPU_EINVAL;
+        }
+    const bool mixed = precision == COFFE_GPU_MIXED;
+    const int M = (int)N / 2;
+    const size_t len = N + CG_N_SMALL_R + 1;
+    int st;
+    ctx->int_ready = false;
+
+    // distinct total biases q + nu
+    std::vector<double> qvals;
+    std::vector<int> term_q(n_terms);
+    std::vector<double> tq(n_terms), tl(n_terms), tn(n_terms);
+    for (int t = 0; t < n_terms; ++t) {
+        const double qnu = select_qnu((double)l[t], (double)n[t]);
+        const double qt = qnu + n[t];
+        int qi = -1;
+        for (size_t j = 0; j < qvals.size(); ++j)
+            if (qvals[j] == qt) qi = (int)j;
+        if (qi < 0) {
+            qi = (int)qvals.size();
+            qvals.push_back(qt);
+        }
+        term_q[t] = qi;
+        tq[t] = qnu;
+        tl[t] = l[t];
+        tn[t] = n[t];
+        ctx->term_n[t] = n[t];
+        ctx->term_l[t] = l[t];
+        ctx->term_q[t] = qi;
+    }
+    const int n_q = (int)qvals.size();
+    std::vector<int> terms_key;
+    for (int t = 0; t < n_terms; ++t) {
+        terms_key.push_back(n[t]);
+        terms_key.push_back(l[t]);
+    }
+
+    GridPar g{k[0], k[nk - 1], k[0], 1.0, (int)N, (int)nk};
+    const bool grid_cached = same_grid(ctx, k, nk, N, terms_key);
+    // device buffers
+    const bool pk_on_device = (flags & COFFE_GPU_PK_DEVICE) != 0;
+    if (!pk_on_device && (st = cg_ensure(ctx, ctx->pk, sizeof(double) * nk * n_spectra))) return st;
+    if ((st = cg_ensure(ctx, ctx->csc, sizeof(double) * nk * n_spectra))) return st;
+    if ((st = cg_ensure(ctx, ctx->spec, (mixed ? sizeof(float2) : sizeof(double2)) * (M + 1) *
+                                            (size_t)n_spectra * n_q)))
+        return st;
+    if ((st = cg_ensure(ctx, ctx->tab_y, (mixed ? sizeof(float) : sizeof(double)) * len *
+                                             (size_t)n_spectra * n_terms)))
+        return st;
+    if (!grid_cached) {
+        if ((st = cg_ensure(ctx, ctx->kgrid, sizeof(double) * nk))) return st;
+        if ((st = cg_ensure(ctx, ctx->csfac, sizeof(double) * 2 * nk))) return st;
+        if ((st = cg_ensure(ctx, ctx->samp_idx, sizeof(int) * N))) return st;
+        if ((st = cg_ensure(ctx, ctx->samp_dx, sizeof(double) * N))) return st;
+        if ((st = cg_ensure(ctx, ctx->qfac, sizeof(double) * N * n_q))) return st;
+        if ((st = cg_ensure(ctx, ctx->modec, sizeof(double2) * (M + 1) * n_terms + sizeof(double) * (M + 1)))) return st;
+        if ((st = cg_ensure(ctx, ctx->postf, sizeof(double) * N * n_terms))) return st;
+        if ((st = cg_ensure(ctx, ctx->twid, sizeof(double2) * (M + 1)))) return st;
+        if ((st = cg_ensure(ctx, ctx->twid32, sizeof(float2) * (M + 1)))) return st;
+        if ((st = cg_ensure(ctx, ctx->tab_x, sizeof(double) * len))) return st;
+        if ((st = cg_ensure(ctx, ctx->tab_x32, sizeof(float) * len))) return st;
+    }
+    // term metadata (small, staged through the request buffer)
+    struct TermMeta {
+        double q[CG_MAX_TERMS], l[CG_MAX_TERMS], n[CG_MAX_TERMS], qv[CG_MAX_TERMS];
+        int tq[CG_MAX_TERMS], tn[CG_MAX_TERMS], tl[CG_MAX_TERMS];
+    } meta;
+    for (int t = 0; t < n_terms; ++t) {
+        meta.q[t] = tq[t];
+        meta.l[t] = tl[t];
+        meta.n[t] = tn[t];
+        meta.tq[t] = term_q[t];
+        meta.tn[t] = n[t];
+        meta.tl[t] = l[t];
+    }
+    for (int q = 0; q < n_q; ++q) meta.qv[q] = qvals[q];
+    if ((st = cg_ensure(ctx, ctx->term_meta, sizeof(TermMeta)))) return st;
+    TermMeta *d_meta = (TermMeta *)ctx->term_meta.p;
+    if (!grid_cached)
+        CG_CUDA(ctx, cudaMemcpyAsync(d_meta, &meta, sizeof(TermMeta), cudaMemcpyHostToDevice,
+                                     ctx->stream));
+    const double *d_pk = pk_on_device ? pk : (const double *)ctx->pk.p;
+    if (!pk_on_device)
+        CG_CUDA(ctx, cudaMemcpyAsync(ctx->pk.p, pk, sizeof(double) * nk * n_spectra,
+                                     cudaMemcpyHostToDevice, ctx->stream));
+
+    double2 *mcoef = (double2 *)ctx->modec.p;
+    double *modew = (double *)((char *)ctx->modec.p + sizeof(double2) * (M + 1) * n_terms);
+    if (!grid_cached) {
+        CG_CUDA(ctx, cudaMemcpyAsync(ctx->kgrid.p, k, sizeof(double) * nk, cudaMemcpyHostToDevice,
+                                     ctx->stream));
+        double hx[CG_N_SMALL_R + 1];
+        hx[0] = 0.0;
+        for (int i = 0; i < CG_N_SMALL_R; ++i) hx[i + 1] = h_min_sep[i];
+        float hx32[CG_N_SMALL_R + 1];
+        for (int i = 0; i <= CG_N_SMALL_R; ++i) hx32[i] = (float)hx[i];
+        CG_CUDA(ctx, cudaMemcpyAsync(ctx->tab_x.p, hx, sizeof(hx), cudaMemcpyHostToDevice,
+                                     ctx->stream));
+        CG_CUDA(ctx, cudaMemcpyAsync(ctx->tab_x32.p, hx32, sizeof(hx32), cudaMemcpyHostToDevice,
+                                     ctx->stream));
+        csfac_kernel<<<1, 1, 0, ctx->stream>>>((const double *)ctx->kgrid.p, (int)nk,
+                                               (double *)ctx->csfac.p);
+        if ((st = cg_after_launch(ctx, "csfac_kernel"))) return st;
+        const int tb = 256;
+        sampling_kernel<<<((int)N + tb) / tb, tb, 0, ctx->stream>>>(
+            g, (const double *)ctx->kgrid.p, (int *)ctx->samp_idx.p, (double *)ctx->samp_dx.p, n_q,
+            d_meta->qv, (double *)ctx->qfac.p, modew, (double *)ctx->tab_x.p,
+            (float *)ctx->tab_x32.p);
+        if ((st = cg_after_launch(ctx, "sampling_kernel"))) return st;
+        dim3 tg(((int)N + tb - 1) / tb + 1, n_terms);
+        term_tables_kernel<<<tg, tb, 0, ctx->stream>>>(g, n_terms, d_meta->q, d_meta->l,
+                                                        d_meta->n, mcoef, (double *)ctx->postf.p,
+                                                        ctx->d_err);
+        if ((st = cg_after_launch(ctx, "term_tables_kernel"))) return st;
+        twiddle_kernel<<<(M + 1 + tb - 1) / tb, tb, 0, ctx->stream>>>(
+            (int)N, (double2 *)ctx->twid.p, (float2 *)ctx->twid32.p);
+        if ((st = cg_after_launch(ctx, "twiddle_kernel"))) return st;
+        if ((st = cg_check_device_errors(ctx, "FFTLog coefficient tables"))) return st;
+        ctx->grid_N = N;
+        ctx->grid_nk = nk;
+        ctx->grid_k.assign(k, k + nk);
+        ctx->grid_terms = terms_key;
+    }
+    // per spectrum: natural-spline coefficients, forward FFTs, inverse FFTs
+    cspline_c_kernel<<<(n_spectra + 63) / 64, 64, 0, ctx->stream>>>(
+        (const double *)ctx->kgrid.p, d_pk, (const double *)ctx->csfac.p,
+        (int)nk, n_spectra, (double *)ctx->csc.p);
+    if ((st = cg_after_launch(ctx, "cspline_c_kernel"))) return st;
+    const int fft_threads = 512;
+    const size_t smem = (mixed ? sizeof(float2) : sizeof(double2)) * M;
+    dim3 gf(n_spectra, n_q), gi(n_spectra, n_terms);
+    if (mixed) {
+        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_forward_kernel<float>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_kernel<float, float>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        fftlog_forward_kernel<float><<<gf, fft_threads, smem, ctx->stream>>>(
+            g, (const double *)ctx->kgrid.p, d_pk, (const double *)ctx->csc.p,
+            (const int *)ctx->samp_idx.p, (const double *)ctx->samp_dx.p,
+            (const double *)ctx->qfac.p, modew, (const float2 *)ctx->twid32.p, n_q,
+            (float2 *)ctx->spec.p, ctx->d_err);
+        if ((st = cg_after_launch(ctx, "fftlog_forward_kernel<float>"))) return st;
+        fftlog_inverse_kernel<float, float><<<gi, fft_threads, smem, ctx->stream>>>(
+            g, (const float2 *)ctx->spec.p, d_meta->tq, n_q, n_terms, mcoef,
+            (const double *)ctx->postf.p, (const float2 *)ctx->twid32.p, (float *)ctx->tab_y.p,
+            ctx->d_err);
+        if ((st = cg_after_launch(ctx, "fftlog_inverse_kernel<float>"))) return st;
+    } else {
+        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_forward_kernel<double>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_kernel<double, double>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        fftlog_forward_kernel<double><<<gf, fft_threads, smem, ctx->stream>>>(
+            g, (const double *)ctx->kgrid.p, d_pk, (const double *)ctx->csc.p,
+            (const int *)ctx->samp_idx.p, (const double *)ctx->samp_dx.p,
+            (const double *)ctx->qfac.p, modew, (const double2 *)ctx->twid.p, n_q,
+            (double2 *)ctx->spec.p, ctx->d_err);
+        if ((st = cg_after_launch(ctx, "fftlog_forward_kernel<double>"))) return st;
+        fftlog_inverse_kernel<double, double><<<gi, fft_threads, smem, ctx->stream>>>(
+            g, (const double2 *)ctx->spec.p, d_meta->tq, n_q, n_terms, mcoef,
+            (const double *)ctx->postf.p, (const double2 *)ctx->twid.p, (double *)ctx->tab_y.p,
+            ctx->d_err);
+        if ((st = cg_after_launch(ctx, "fftlog_inverse_kernel<double>"))) return st;
+    }
+    // r = 0 and sub-Mpc entries
+    const long tables = (long)n_spectra * n_terms;
+    if (flags & COFFE_GPU_SMALL_R) {
+        const long items = tables * (CG_N_SMALL_R + 1);
+        const int blocks = (int)((items + SR_WARPS - 1) / SR_WARPS);
+        if (mixed)
+            small_r_kernel<float><<<blocks, 32 * SR_WARPS, 0, ctx->stream>>>(
+                (const double *)ctx->kgrid.p, d_pk, (int)nk, n_spectra,
+                n_terms, d_meta->tn, d_meta->tl, (const double *)ctx->tab_x.p, len,
+                (float *)ctx->tab_y.p, ctx->d_err);
+        else
+            small_r_kernel<double><<<blocks, 32 * SR_WARPS, 0, ctx->stream>>>(
+                (const double *)ctx->kgrid.p, d_pk, (int)nk, n_spectra,
+                n_terms, d_meta->tn, d_meta->tl, (const double *)ctx->tab_x.p, len,
+                (double *)ctx->tab_y.p, ctx->d_err);
+        if ((st = cg_after_launch(ctx, "small_r_kernel"))) return st;
+    } else {
+        const long items = tables * (CG_N_SMALL_R + 1);
+        if (mixed)
+            fill_nan_kernel<float><<<(int)((items + 255) / 256), 256, 0, ctx->stream>>>(
+                (float *)ctx->tab_y.p, len, tables);
+        else
+            fill_nan_kernel<double><<<(int)((items + 255) / 256), 256, 0, ctx->stream>>>(
+                (double *)ctx->tab_y.p, len, tables);
+        if ((st = cg_after_launch(ctx, "fill_nan_kernel"))) return st;
+    }
+    ctx->n_spectra = n_spectra;
+    ctx->n_terms = n_terms;
+    ctx->n_q = n_q;
+    ctx->N = N;
+    ctx->nk = nk;
+    ctx->kmin = k[0];
+    ctx->kmax = k[nk - 1];
+    ctx->int_precision = precision;
+    ctx->int_ready = true;
+    return COFFE_GPU_OK;
+}
+
+// Evaluates table (spectrum, term) with the Akima spline at host separations.
+int integrals_eval(coffe_gpu_ctx *ctx, int spectrum, int term, const double *r, size_t nq,
+                   double *out)
+{
+    if (!ctx->int_ready) {
+        cg_set_error(ctx, "integrals not initialised");
+        return COFFE_GPU_ESTATE;
+    }
+    if (spectrum < 0 || spectrum >= ctx->n_spectra || term < 0 || term >= ctx->n_terms) {
+        cg_set_error(ctx, "integral (spectrum %d, term %d) out of range", spectrum, term);
+        return COFFE_GPU_EINVAL;
+    }
+    if (nq == 0) return COFFE_GPU_OK;
+    const size_t len = ctx->N + CG_N_SMALL_R + 1;
+    int st;
+    DevBuf tmp;
+    const size_t bytes = sizeof(double) * (len + 2 * nq);
+    if (cudaMalloc(&tmp.p, bytes) != cudaSuccess) {
+        cg_set_error(ctx, "cudaMalloc of %zu bytes failed", bytes);
+        return COFFE_GPU_ENOMEM;
+    }
+    double *y = (double *)tmp.p, *dr = y + len, *dout = dr + nq;
+    const size_t off = ((size_t)spectrum * ctx->n_terms + term) * len;
+    if (ctx->int_precision == COFFE_GPU_MIXED) {
+        table_f32_to_f64_kernel<<<(int)((len + 255) / 256), 256, 0, ctx->stream>>>(
+            (const float *)ctx->tab_y.p + off, y, len);
+        if ((st = cg_after_launch(ctx, "table_f32_to_f64_kernel"))) {
+            cudaFree(tmp.p);
+            return st;
+        }
+    } else {
+        cudaMemcpyAsync(y, (const double *)ctx->tab_y.p + off, sizeof(double) * len,
+                        cudaMemcpyDeviceToDevice, ctx->stream);
+    }
+    cudaMemcpyAsync(dr, r, sizeof(double) * nq, cudaMemcpyHostToDevice, ctx->stream);
+    table_eval_kernel<<<(int)((nq + 255) / 256), 256, 0, ctx->stream>>>(
+        (const double *)ctx->tab_x.p, y, (int)len, dr, (int)nq, dout);
+    st = cg_after_launch(ctx, "table_eval_kernel");
+    if (!st) {
+        cudaError_t e = cudaMemcpyAsync(out, dout, sizeof(double) * nq, cudaMemcpyDeviceToHost,
+                                        ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) {
+            cg_set_error(ctx, "integral_eval copy: %s", cudaGetErrorString(e));
+            st = COFFE_GPU_ECUDA;
+        }
+    }
+    cudaFree(tmp.p);
+    return st;
+}

@@ -1,0 +1,200 @@
+/*
+ * coffe_gpu.h -- C ABI of the GB300 (sm_103a) implementation of COFFE's
+ * correlation-function hot path.
+ *
+ * Plain C types only (pointers, sizes, doubles, ints): no CUDA, C++ or torch
+ * types cross this boundary, so the reference's C drivers (integrals.c,
+ * multipoles.c, covariance.c), its Cython wrapper (python/coffe/coffe.pxd) or
+ * any ctypes/cffi caller can bind it directly.
+ *
+ * Conventions shared by every entry point:
+ *  - Return value: COFFE_GPU_OK (0) or a negative coffe_gpu_status.  Nothing
+ *    here calls exit(); the reference's fatal exits (e.g. twofast.c:82-88,
+ *    functions.c:1470-1483) become error returns.
+ *  - Units follow the reference internals: k in 1/Mpc, P(k) in Mpc^3,
+ *    separations and comoving distances in Mpc.
+ *  - A context owns the device buffers and one CUDA stream; calls on one
+ *    context are stream-ordered and must not be made from two host threads at
+ *    once.  Separate contexts are independent.
+ *  - Array arguments are host pointers unless a *_device flag says otherwise.
+ */
+#ifndef COFFE_GPU_H
+#define COFFE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct coffe_gpu_ctx coffe_gpu_ctx_t;
+
+enum coffe_gpu_status {
+    COFFE_GPU_OK = 0,
+    COFFE_GPU_EINVAL = -1,     /* bad argument (size, range, NULL pointer) */
+    COFFE_GPU_ECUDA = -2,      /* a CUDA runtime call failed */
+    COFFE_GPU_ENOMEM = -3,     /* device allocation failed */
+    COFFE_GPU_ENONFINITE = -4, /* a kernel produced NaN/Inf (reference would exit) */
+    COFFE_GPU_ESTATE = -5,     /* a prerequisite (background, integrals) is missing */
+    COFFE_GPU_ELIMIT = -6,     /* adaptive quadrature ran out of subintervals */
+    COFFE_GPU_ETIMEOUT = -7    /* a bounded device-side wait gave up */
+};
+
+/* Precision of a computation. */
+enum coffe_gpu_precision {
+    COFFE_GPU_FP64 = 0, /* plain FP64 everywhere: the parity path */
+    COFFE_GPU_MIXED = 1 /* FP32 FFT/spline/integrand arithmetic with compensated
+                           sums; FP64 Gamma-ratio coefficients and background */
+};
+
+/* Contributions to the 2-point function (the den, rsd, len flags of
+   coffe_parameters_t.correlation_contrib, common.h). */
+enum coffe_gpu_contrib {
+    COFFE_GPU_DEN = 1,
+    COFFE_GPU_RSD = 2,
+    COFFE_GPU_LEN = 4
+};
+
+/* ----------------------------------------------------------------- context */
+
+/* Creates a context on CUDA device `device`.  No reference counterpart: the
+   reference keeps its state in coffe_parameters_t / coffe_background_t. */
+int coffe_gpu_ctx_create(int device, coffe_gpu_ctx_t **ctx);
+int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx);
+/* Human-readable text of a status code (static storage). */
+const char *coffe_gpu_strerror(int status);
+/* Text of the last error recorded on this context (static to the context). */
+const char *coffe_gpu_last_error(const coffe_gpu_ctx_t *ctx);
+/* Blocks until all work queued on the context's stream has finished. */
+int coffe_gpu_synchronize(coffe_gpu_ctx_t *ctx);
+/* Makes the context enqueue on an external cudaStream_t (passed as void*);
+   NULL restores the context's own stream. */
+int coffe_gpu_set_stream(coffe_gpu_ctx_t *ctx, void *stream);
+
+/* -------------------------------------------------------------- background */
+
+/* Flat LCDM cosmology (w0 = -1, wa = 0), the fields of coffe_parameters_t that
+   coffe_background_init reads (background.c:301-537). */
+typedef struct {
+    double Omega0_cdm;
+    double Omega0_baryon;
+    double Omega0_gamma;
+    double Omega0_de;
+    double h;
+    int bins; /* background_bins; nodes at z_i = 15 i / (bins - 1) */
+} coffe_gpu_cosmology_t;
+
+/* Replaces coffe_background_init (background.c:301-696) for flat LCDM: the
+   node values of chi(z) (GK61 QAG of 1/E, FP64), D1 and f (growth ODE, FP64)
+   and a, H, conformal H, its derivative are computed on the device and splined
+   (Akima, as interp_method's default, parser.c:807). */
+int coffe_gpu_background_init(coffe_gpu_ctx_t *ctx, const coffe_gpu_cosmology_t *c);
+
+/* Alternative to coffe_gpu_background_init for callers that already own a
+   background (e.g. a coffe_background_t built by the reference): node arrays
+   on one strictly increasing z grid; chi in Mpc, conformal H in 1/Mpc.
+   `Omega0_m` and `h` are the cosmology's (lensing prefactors). */
+int coffe_gpu_background_set(coffe_gpu_ctx_t *ctx, const double *z, const double *chi,
+                             const double *D1, const double *f, const double *a,
+                             const double *conformal_Hz, size_t bins, double Omega0_m,
+                             double h);
+
+/* Copies the background nodes to host arrays of length `bins` (any may be
+   NULL).  Hz and conformal_Hz_prime are only available after _init. */
+int coffe_gpu_background_get(coffe_gpu_ctx_t *ctx, double *z, double *chi, double *D1,
+                             double *f, double *a, double *Hz, double *conformal_Hz,
+                             double *conformal_Hz_prime);
+
+/* Bias of a population as an Akima spline of (z, value) (galaxy_bias1/2,
+   magnification_bias1/2 of coffe_parameters_t; parser.c:36-51 sets constant
+   defaults b = 1, s = 0, which is also what an unset bias means here).
+   which: 0 = galaxy_bias1, 1 = galaxy_bias2, 2 = magnification_bias1,
+   3 = magnification_bias2.  n >= 5 (Akima's minimum). */
+int coffe_gpu_set_bias(coffe_gpu_ctx_t *ctx, int which, const double *z,
+                       const double *value, size_t n);
+
+/* --------------------------------------------------------------- integrals */
+
+/* Number of points of one I_l^n table for an FFT size N: r = 0, the 42
+   sub-Mpc separations of integrals.c:111-126, then the N FFTLog points. */
+size_t coffe_gpu_integral_table_len(size_t N);
+
+/* Replaces coffe_integrals_init (integrals.c:580-770) for a batch of power
+   spectra.  For each spectrum s (P(k) sampled at the shared grid k[0..nk-1],
+   pk[s*nk + i]) and each term t (integer n[t], l[t]) builds the table of
+   I_l^n(r) = 1/(2 pi^2) int dk k^2 P(k) j_l(kr)/(kr)^n (times r^(n-l) when
+   n >= l) with the FFTLog of twofast_1bessel (twofast.c:362-483) on N points
+   (N a power of two, 64 <= N <= 16384), kmin = k[0], kmax = k[nk-1]
+   (set_power_spectrum_linear, coffe.pyx:2929-2996).
+   flags: bit 0 (COFFE_GPU_SMALL_R) also fills the r = 0 value and the 42
+   sub-Mpc points by GK61 QAG (integrals.c:524-562); without it those 43
+   entries are NaN and tables serve lookups at r >= the third FFT node
+   (1.01 Mpc at the default grids).
+   precision: COFFE_GPU_FP64 or COFFE_GPU_MIXED (FP32 FFT, FP64 Gamma-ratio
+   coefficients).  Tables stay on the device for coffe_gpu_multipoles. */
+#define COFFE_GPU_SMALL_R 1
+/* flags bit 1: `pk` is a device pointer (n_spectra * nk doubles). */
+#define COFFE_GPU_PK_DEVICE 2
+/* flags bit 2: enqueue only -- no host synchronisation; device-side errors are
+   reported by the next coffe_gpu_synchronize.  The grid arguments (k, n, l,
+   N) must be those of the previous call so that no per-grid table is rebuilt
+   (otherwise the call synchronises once to build them). */
+#define COFFE_GPU_ASYNC 4
+int coffe_gpu_integrals_init(coffe_gpu_ctx_t *ctx, const double *k, const double *pk,
+                             int n_spectra, size_t nk, const int *n, const int *l,
+                             int n_terms, size_t N, int precision, unsigned flags);
+
+/* Copies table (spectrum, term) out: x and y of coffe_gpu_integral_table_len(N)
+   points (the arrays coffe_integrals_init hands to coffe_init_spline,
+   integrals.c:652-658). */
+int coffe_gpu_integral_get(coffe_gpu_ctx_t *ctx, int spectrum, int term, double *x,
+                           double *y);
+
+/* Evaluates table (spectrum, term) at nq separations through the same Akima
+   spline the reference builds (coffe_interp_spline, common.c:704-710; the
+   lookup Coffe.integral does, coffe.pyx:1657-1713). */
+int coffe_gpu_integral_eval(coffe_gpu_ctx_t *ctx, int spectrum, int term, const double *r,
+                            size_t nq, double *out);
+
+/* -------------------------------------------------------------- multipoles */
+
+/* Replaces coffe_multipoles_init (multipoles.c:48-136) for many spectra,
+   mean redshifts and uneven separation lists in one launch.
+   Request q (0 <= q < n_req) uses spectrum req_spectrum[q] of the last
+   coffe_gpu_integrals_init, mean redshift req_z_mean[q] and the separations
+   sep[req_offset[q] .. req_offset[q+1]-1] (req_offset has n_req+1 entries,
+   req_offset[0] = 0).  For every separation and every multipole l[0..n_l-1]
+   the output is
+     out[(req_offset[q] + j) * n_l + i] = (2l+1) int_0^1 dx xi(mu=2x-1) P_l(mu)
+   of the nonintegrated den/rsd terms selected by `contrib` (signal.c:83-111,
+   521-542; functions.c:89-771), by adaptive GK61 QAG with relative tolerance
+   `epsrel` (integration_1d_prec, default 1e-5, parser.c:769).
+   The integrals (0,0), (0,2) and (0,4) must be among the terms.
+   precision: COFFE_GPU_FP64 follows the reference in FP64; COFFE_GPU_MIXED
+   evaluates the integrand in FP32 with compensated FP32 sums.
+   All arrays are host pointers unless arrays_on_device != 0, in which case
+   every array (including out) is a device pointer. */
+int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, double epsrel,
+                         int n_req, const int *req_spectrum, const double *req_z_mean,
+                         const int64_t *req_offset, const double *sep, int n_l,
+                         const int *l, double *out, int arrays_on_device);
+
+/* Stream-ordered variant of coffe_gpu_multipoles for device-resident
+   requests: every array except `l` (host, n_l entries) is a device pointer,
+   n_sep = req_offset[n_req] is passed by the caller, and nothing synchronises
+   the host; device-side errors surface at the next coffe_gpu_synchronize.
+   The host-side argument checks of coffe_gpu_multipoles are the caller's. */
+int coffe_gpu_multipoles_async(coffe_gpu_ctx_t *ctx, int contrib, int precision,
+                               double epsrel, int n_req, int64_t n_sep,
+                               const int *req_spectrum, const double *req_z_mean,
+                               const int64_t *req_offset, const double *sep, int n_l,
+                               const int *l, double *out);
+
+/* Kernel launches issued by this context since creation (for accounting). */
+long long coffe_gpu_launch_count(const coffe_gpu_ctx_t *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* COFFE_GPU_H */

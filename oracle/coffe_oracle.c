@@ -787,7 +787,7 @@ int or_integral_table(const double *k, const double *pk, size_t nk, int n, int l
 
 #define OR_XINT_BINS 16384
 #define OR_XINT_ZMAX 100.0
-#define OR_ODE_HMAX 2.5e-4
+#define OR_ODE_HMAX 1e-3
 
 typedef struct {
     double om; /* Omega0_cdm + Omega0_baryon */

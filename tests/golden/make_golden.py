@@ -1,0 +1,47 @@
+"""Extract the golden vectors the oracle is pinned to from the reference's own
+test fixtures (tests/benchmarks/*.dat and PkL_CLASS.dat of JCGoran/coffe).
+
+Run once where the reference tree is available:
+    python tests/golden/make_golden.py /path/to/coffe
+It writes golden.npz next to this script.  The integral tables (10001 rows
+each) are thinned to the rows the reference's Python test checks
+(1.5 < r < 20000 Mpc, tests/test_coffe.py:196-233), every 8th row; all other
+files are copied whole except the background (every 4th of its 10001 rows).  The values are the reference's published outputs,
+not recomputed.
+"""
+import sys
+from pathlib import Path
+
+import numpy as np
+
+H = 0.67
+COFFE_H0 = 1.0 / 2997.92458
+
+
+def main(ref: Path):
+    bench = ref / "tests" / "benchmarks"
+    out = {}
+    out["pk_class"] = np.loadtxt(ref / "PkL_CLASS.dat")
+    out["background"] = np.loadtxt(bench / "benchmark_background.dat")[::4]
+    for i in range(8):
+        d = np.loadtxt(bench / f"benchmark_integral{i}.dat")
+        r = d[:, 0] / (COFFE_H0 * H)
+        keep = np.where((r > 1.5) & (r < 20000))[0][::8]
+        out[f"integral{i}"] = d[keep]
+        with open(bench / f"benchmark_integral{i}.dat") as fh:
+            out[f"integral{i}_header"] = np.array(fh.readline().strip())
+    for name in ("den", "rsd", "std", "len", "std_len", "flatsky_lensing_lensing",
+                 "flatsky_density_lensing"):
+        for l in (0, 2, 4):
+            out[f"{name}_multipoles{l}"] = np.loadtxt(bench / f"benchmark_{name}_multipoles{l}.dat")
+    for a in (0, 2, 4):
+        for b in (0, 2, 4):
+            out[f"multipoles_covariance_{a}{b}"] = np.loadtxt(
+                bench / f"benchmark_multipoles_covariance_{a}{b}.dat")
+    dst = Path(__file__).resolve().parent / "golden.npz"
+    np.savez_compressed(dst, **out)
+    print(dst, dst.stat().st_size, "bytes")
+
+
+if __name__ == "__main__":
+    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))

@@ -1,0 +1,318 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle on the same
+seeded inputs, and against the reference's golden vectors.
+
+Tolerances (stated per test):
+  * FP64 path: 1e-10 relative (the benchmark spec), with a floor of 1e-3 of the largest
+    |value| of the same multipole / 1e-8 of the local table envelope so that
+    zero crossings do not turn rounding into infinite relative error;
+  * mixed path: 1e-4 relative with the same floors;
+  * golden vectors: the reference's own tolerances (integrals rtol 1e-4,
+    multipoles rtol 5e-4, np.isclose semantics).
+"""
+import numpy as np
+import pytest
+
+from conftest import COFFE_H0, H
+
+pytestmark = pytest.mark.gpu
+
+TERMS8 = [(0, 0), (0, 2), (0, 4), (1, 1), (1, 3), (2, 0), (2, 2), (3, 1)]
+
+
+def rel_floor(got, ref, floor):
+    return np.max(np.abs(got - ref) / np.maximum(np.abs(ref), floor))
+
+
+def local_envelope(y, half=64):
+    a = np.abs(y)
+    out = np.empty_like(a)
+    for i in range(len(a)):
+        out[i] = a[max(0, i - half): i + half + 1].max()
+    return out
+
+
+def table_err(gy, oy, mask):
+    env = local_envelope(oy)
+    return np.max((np.abs(gy - oy) / np.maximum(np.abs(oy), 1e-8 * env))[mask])
+
+
+@pytest.fixture(scope="module")
+def w():
+    from coffe_gb300 import workloads
+
+    return workloads
+
+
+@pytest.fixture(scope="module")
+def cfg1(w):
+    return w.cfg1()
+
+
+@pytest.fixture(scope="module")
+def bg031(oracle):
+    return oracle.background_nodes(0.31, 0.05, 9e-5, H, 10000)
+
+
+def oracle_model(oracle, bg, k, pk, N, omega_m=0.31, small_r=False):
+    m = oracle.Model(bg, H, omega_m)
+    for n, l in [(0, 0), (0, 2), (0, 4)]:
+        x, y = oracle.integral_table(k, pk, n, l, N, with_small_r=small_r)
+        m.set_integral(n, l, x, y)
+    return m
+
+
+# ----------------------------------------------------------------- background
+def test_background_init_matches_oracle(gpu_ctx, bg031):
+    gpu_ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+    g = gpu_ctx.background()
+    pairs = {"z": "z", "chi": "chi", "D1": "D1", "f": "f", "a": "a", "Hz": "Hz",
+             "conformal_Hz": "confH", "conformal_Hz_prime": "confHp"}
+    for gk, ok in pairs.items():
+        err = rel_floor(g[gk], bg031[ok], 1e-300)
+        assert err < 1e-12, (gk, err)
+
+
+def test_background_set_roundtrip(gpu_ctx, bg031):
+    gpu_ctx.background_set(bg031["z"], bg031["chi"], bg031["D1"], bg031["f"], bg031["a"],
+                           bg031["confH"], 0.31, H)
+    g = gpu_ctx.background(with_H=False)
+    assert np.array_equal(g["chi"], bg031["chi"]) and np.array_equal(g["f"], bg031["f"])
+
+
+# ------------------------------------------------------------------ integrals
+def test_integral_tables_fp64_match_oracle(gpu_ctx, oracle, cfg1):
+    k, pk = cfg1["k"], cfg1["pk"]
+    N = 4096
+    gpu_ctx.integrals_init(k, pk[None, :], TERMS8, N=N, precision="fp64", small_r=True)
+    for n, l in TERMS8:
+        gx, gy = gpu_ctx.integral_table(0, n, l)
+        ox, oy = oracle.integral_table(k, pk, n, l, N, with_small_r=True)
+        assert rel_floor(gx, ox, 1e-300) < 1e-14
+        fft = np.zeros(len(ox), bool)
+        fft[43:] = True
+        mask = fft & (ox >= 1.0) & (ox <= 1e4)
+        e_fft = table_err(gy, oy, mask)
+        e_small = rel_floor(gy[:43], oy[:43], 1e-8 * np.abs(oy[:43]).max())
+        assert e_fft < 1e-10, ((n, l), e_fft)
+        assert e_small < 1e-9, ((n, l), e_small)
+
+
+def test_integral_tables_mixed_close_to_oracle(gpu_ctx, oracle, cfg1):
+    k, pk = cfg1["k"], cfg1["pk"]
+    N = 4096
+    gpu_ctx.integrals_init(k, pk[None, :], [(0, 0), (0, 2), (0, 4)], N=N, precision="mixed",
+                           small_r=False)
+    for n, l in [(0, 0), (0, 2), (0, 4)]:
+        gx, gy = gpu_ctx.integral_table(0, n, l)
+        ox, oy = oracle.integral_table(k, pk, n, l, N, with_small_r=False)
+        mask = (ox >= 5 / H) & (ox <= 300 / H)
+        mask[:43] = False
+        assert np.isnan(gy[:43]).all()  # not requested
+        e = table_err(gy, oy, mask)
+        assert e < 1e-4, ((n, l), e)
+
+
+def test_all_bessel_integrals_2e14_fp64(gpu_ctx, oracle, w):
+    """l = 0..4, n = -1..4 on 2^14 points, including the pairs whose Gamma-ratio
+    reflection overflows at high frequency (kept as the reference computes them)."""
+    c = w.cfg2()
+    k, pk, N = c["k"], c["pk"], c["N"]
+    gpu_ctx.integrals_init(k, pk[None, :], c["terms"], N=N, precision="fp64", small_r=False)
+    worst = 0.0
+    for n, l in c["terms"]:
+        gx, gy = gpu_ctx.integral_table(0, n, l)
+        ox, oy = oracle.integral_table(k, pk, n, l, N, with_small_r=False)
+        mask = (ox >= 1.0) & (ox <= 1e4)
+        mask[:43] = False
+        e = table_err(gy, oy, mask)
+        worst = max(worst, e)
+        assert e < 1e-10, ((n, l), e)
+    print("worst FP64 table error (2^14, 30 terms):", worst)
+
+
+def test_integrals_golden_through_gpu(gpu_ctx, golden, class_pk):
+    k, pk = class_pk
+    gpu_ctx.integrals_init(k, pk[None, :], TERMS8, N=16384, precision="fp64", small_r=True)
+    for i, (n, l) in enumerate(TERMS8):
+        d = golden[f"integral{i}"]
+        r = d[:, 0] / (COFFE_H0 * H)
+        val = gpu_ctx.integral_eval(0, n, l, r)
+        if n > l:
+            val = val * (COFFE_H0 * H) ** (n - l)
+        assert np.isclose(d[:, 1], val, rtol=1e-4).all(), (n, l)
+
+
+# ----------------------------------------------------------------- multipoles
+def _run_batch(ctx, b, precision):
+    return ctx.multipoles(b.req_spectrum, b.req_z_mean, b.req_offset, b.sep, b.ls,
+                          precision=precision)
+
+
+def _oracle_batch(oracle, bg, b, N):
+    out = np.zeros((len(b.sep), len(b.ls)))
+    for s in range(b.pk.shape[0]):
+        m = oracle_model(oracle, bg, b.k, b.pk[s], N)
+        for q in np.where(b.req_spectrum == s)[0]:
+            lo, hi = b.req_offset[q], b.req_offset[q + 1]
+            for j, l in enumerate(b.ls):
+                z = np.full(hi - lo, b.req_z_mean[q])
+                out[lo:hi, j] = m.multipoles_batch(3, z, b.sep[lo:hi], np.full(hi - lo, l))
+    return out
+
+
+def _per_l_floor(ref, b, frac):
+    """floor = frac * max |ref| over the request's separations, per l"""
+    fl = np.zeros_like(ref)
+    for q in range(len(b.req_spectrum)):
+        lo, hi = b.req_offset[q], b.req_offset[q + 1]
+        if hi > lo:
+            fl[lo:hi] = frac * np.abs(ref[lo:hi]).max(axis=0)
+    return np.maximum(fl, 1e-300)
+
+
+@pytest.fixture(scope="module")
+def small_batch(w):
+    return w.subset(w.cfg3(n_spectra=6), 6)
+
+
+@pytest.fixture(scope="module")
+def small_batch_ref(oracle, bg031, small_batch):
+    return _oracle_batch(oracle, bg031, small_batch, 4096)
+
+
+def test_multipoles_cfg1_fp64(gpu_ctx, oracle, bg031, cfg1):
+    k, pk = cfg1["k"], cfg1["pk"]
+    gpu_ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+    gpu_ctx.integrals_init(k, pk[None, :], [(0, 0), (0, 2), (0, 4)], N=4096, precision="fp64",
+                           small_r=False)
+    sep = cfg1["sep"]
+    got = gpu_ctx.multipoles([0], [1.0], [0, len(sep)], sep, (0, 2, 4), precision="fp64")
+    m = oracle_model(oracle, bg031, k, pk, 4096)
+    for j, l in enumerate((0, 2, 4)):
+        ref = m.multipoles_batch(3, np.ones(len(sep)), sep, np.full(len(sep), l))
+        e = rel_floor(got[:, j], ref, 1e-3 * np.abs(ref).max())
+        assert e < 1e-10, (l, e)
+
+
+def test_multipoles_batch_fp64(gpu_ctx, small_batch, small_batch_ref):
+    b = small_batch
+    gpu_ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+    gpu_ctx.integrals_init(b.k, b.pk, [(0, 0), (0, 2), (0, 4)], N=4096, precision="fp64",
+                           small_r=False)
+    got = _run_batch(gpu_ctx, b, "fp64")
+    e = np.max(np.abs(got - small_batch_ref) /
+               np.maximum(np.abs(small_batch_ref), _per_l_floor(small_batch_ref, b, 1e-3)))
+    print("fp64 max rel error:", e)
+    assert e < 1e-10, e
+
+
+def test_multipoles_batch_mixed(gpu_ctx, small_batch, small_batch_ref):
+    b = small_batch
+    gpu_ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+    gpu_ctx.integrals_init(b.k, b.pk, [(0, 0), (0, 2), (0, 4)], N=4096, precision="mixed",
+                           small_r=False)
+    got = _run_batch(gpu_ctx, b, "mixed")
+    e = np.max(np.abs(got - small_batch_ref) /
+               np.maximum(np.abs(small_batch_ref), _per_l_floor(small_batch_ref, b, 1e-3)))
+    print("mixed max rel error:", e)
+    assert e < 1e-4, e
+
+
+def test_multipoles_golden_through_gpu(gpu_ctx, golden, class_pk, ref_bg):
+    k, pk = class_pk
+    gpu_ctx.background_init(0.3, 0.05, 9e-5, H, 10000)
+    gpu_ctx.integrals_init(k, pk[None, :], [(0, 0), (0, 2), (0, 4)], N=16384, precision="fp64",
+                           small_r=True)
+    for name, mask in [("den", 1), ("rsd", 2), ("std", 3)]:
+        d0 = golden[f"{name}_multipoles0"]
+        sep = d0[:, 0] / H
+        got = gpu_ctx.multipoles([0], [1.0], [0, len(sep)], sep, (0, 2, 4), contrib=mask)
+        for j, l in enumerate((0, 2, 4)):
+            d = golden[f"{name}_multipoles{l}"]
+            assert np.allclose(got[:, j], d[:, 1], rtol=5e-4), (name, l)
+
+
+def test_multipoles_sub_mpc_uses_small_r_table(gpu_ctx, oracle, bg031, cfg1):
+    k, pk = cfg1["k"], cfg1["pk"]
+    gpu_ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+    gpu_ctx.integrals_init(k, pk[None, :], [(0, 0), (0, 2), (0, 4)], N=4096, precision="fp64",
+                           small_r=True)
+    sep = np.array([0.05, 0.3, 0.95, 1.004, 2.0])
+    got = gpu_ctx.multipoles([0], [1.2], [0, len(sep)], sep, (0, 2, 4))
+    m = oracle_model(oracle, bg031, k, pk, 4096, small_r=True)
+    for j, l in enumerate((0, 2, 4)):
+        ref = m.multipoles_batch(3, np.full(len(sep), 1.2), sep, np.full(len(sep), l))
+        assert rel_floor(got[:, j], ref, 1e-3 * np.abs(ref).max()) < 1e-10, l
+
+
+def test_ragged_and_empty_requests(gpu_ctx, oracle, bg031, cfg1):
+    k, pk = cfg1["k"], cfg1["pk"]
+    gpu_ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+    gpu_ctx.integrals_init(k, np.stack([pk, 1.3 * pk]), [(0, 0), (0, 2), (0, 4)], N=4096,
+                           precision="fp64", small_r=False)
+    # request 0 empty, request 1 one separation, request 2 three, request 3 empty
+    offs = [0, 0, 1, 4, 4]
+    sep = np.array([50.0, 10.0, 60.0, 150.0])
+    got = gpu_ctx.multipoles([0, 1, 0, 1], [1.0, 0.7, 1.5, 2.0], offs, sep, (2, 0))
+    m0 = oracle_model(oracle, bg031, k, pk, 4096)
+    m1 = oracle_model(oracle, bg031, k, 1.3 * pk, 4096)
+    ref = np.array([[m1.multipole(3, 0.7, 50.0, 2), m1.multipole(3, 0.7, 50.0, 0)]] +
+                   [[m0.multipole(3, 1.5, r, 2), m0.multipole(3, 1.5, r, 0)] for r in sep[1:]])
+    assert rel_floor(got, ref, 1e-300) < 1e-10
+
+
+# ----------------------------------------------------------------- API mirror
+def test_coffe_mirror_against_golden(golden, class_pk):
+    from coffe_gb300.api import Coffe
+
+    k, pk = class_pk
+    c = Coffe(omega_m=0.3, sep=golden["std_multipoles0"][:, 0] / H, l=[0, 2, 4], z_mean=[1.0],
+              has_density=True, has_rsd=True, integrals_fftlog_sampling=16384)
+    c.set_power_spectrum_linear(k, pk)
+    res = c.compute_multipoles_bulk()
+    assert [(r.z, r.l) for r in res[:6]] == [(1.0, 0)] * 5 + [(1.0, 2)]
+    for l in (0, 2, 4):
+        vals = np.array([r.value for r in res if r.l == l])
+        assert np.allclose(vals, golden[f"std_multipoles{l}"][:, 1], rtol=5e-4)
+    d = golden["integral1"]
+    r = float(d[10, 0] / (COFFE_H0 * H))
+    assert np.isclose(c.integral(r=r, n=0, l=2), d[10, 1], rtol=1e-4)
+    v = c.compute_multipole(z=1.0, r=float(golden["std_multipoles2"][2, 0] / H), l=2)
+    assert np.isclose(v, golden["std_multipoles2"][2, 1], rtol=5e-4)
+    with pytest.raises(ValueError):
+        c.integral(r=-1.0, n=0, l=0)
+    with pytest.raises(ValueError):
+        c.integral(r=1.0, n=0, l=7)
+    c.close()
+
+
+# --------------------------------------------------------------- error paths
+def test_error_statuses(w, cfg1):
+    from coffe_gb300._lib import CoffeGpuError
+    from coffe_gb300.api import Context
+
+    k, pk = cfg1["k"], cfg1["pk"]
+    with Context(0) as ctx:
+        with pytest.raises(CoffeGpuError) as e:  # multipoles before anything
+            ctx.multipoles([0], [1.0], [0, 1], [10.0])
+        assert e.value.status == -5
+        with pytest.raises(CoffeGpuError) as e:  # N not a power of two
+            ctx.integrals_init(k, pk[None, :], [(0, 0)], N=1000)
+        assert e.value.status == -1
+        with pytest.raises(CoffeGpuError) as e:  # k not increasing
+            ctx.integrals_init(k[::-1].copy(), pk[None, :], [(0, 0)], N=1024)
+        assert e.value.status == -1
+        bad = pk.copy()
+        bad[100] = np.nan
+        with pytest.raises(CoffeGpuError) as e:  # NaN P(k): the reference would exit
+            ctx.integrals_init(k, bad[None, :], [(0, 0)], N=1024)
+        assert e.value.status == -4
+        ctx.background_init(0.31, 0.05, 9e-5, H, 2000)
+        ctx.integrals_init(k, pk[None, :], [(0, 0), (0, 2), (0, 4)], N=1024)
+        with pytest.raises(CoffeGpuError) as e:  # spectrum index out of range
+            ctx.multipoles([3], [1.0], [0, 1], [10.0])
+        assert e.value.status == -1
+        with pytest.raises(CoffeGpuError) as e:  # precision mismatch with the tables
+            ctx.multipoles([0], [1.0], [0, 1], [10.0], precision="mixed")
+        assert e.value.status == -1
+        assert ctx.launch_count() > 0

@@ -1,0 +1,108 @@
+"""The CPU oracle pinned against the reference's own golden test vectors
+(tests/benchmarks/*.dat of the reference, extracted to tests/golden/golden.npz).
+Tolerances are the reference's: background np.isclose (tests/test_coffe.py:
+143-194), integrals rtol 1e-4 (test_coffe.py:196-233), multipoles rtol 5e-4
+(test_coffe.py:270-303)."""
+import numpy as np
+import pytest
+
+from conftest import COFFE_H0, H
+
+TERMS = [(0, 0), (0, 2), (0, 4), (1, 1), (1, 3), (2, 0), (2, 2), (3, 1)]
+
+
+def test_background_matches_golden(golden, ref_bg):
+    d = golden["background"]
+    idx = np.arange(0, 10000, 4)  # the fixture keeps every 4th node
+    assert np.allclose(ref_bg["z"][idx], d[:, 0], rtol=1e-9)
+    assert np.isclose(ref_bg["a"][idx], d[:, 1]).all()
+    assert np.isclose(ref_bg["Hz"][idx] / H, d[:, 2]).all()
+    assert np.isclose(ref_bg["confH"][idx] / H, d[:, 3]).all()
+    assert np.isclose(ref_bg["confHp"][idx] / H ** 2, d[:, 4]).all()
+    assert np.isclose(ref_bg["D1"][idx], d[:, 5] / d[0, 5]).all()
+    assert np.isclose(ref_bg["f"][idx], d[:, 6]).all()
+    assert np.isclose(ref_bg["chi"][idx], d[:, 7] / H).all()
+
+
+@pytest.mark.parametrize("index", range(8))
+def test_integrals_match_golden(golden, oracle, class_pk, index):
+    n, l = TERMS[index]
+    hdr = str(golden[f"integral{index}_header"])
+    assert f"n = {n}, l = {l}" in hdr
+    k, pk = class_pk
+    x, y = oracle.integral_table(k, pk, n, l, 10000)  # bessel_bins default (parser.c:990)
+    d = golden[f"integral{index}"]
+    r = d[:, 0] / (COFFE_H0 * H)
+    val = oracle.spline_eval("akima", x, y, r)
+    if n > l:
+        val = val * (COFFE_H0 * H) ** (n - l)
+    assert np.isclose(d[:, 1], val, rtol=1e-4).all()
+
+
+@pytest.mark.parametrize("name,mask", [("den", 1), ("rsd", 2), ("std", 3)])
+def test_multipoles_match_golden(golden, oracle, class_pk, ref_bg, name, mask):
+    k, pk = class_pk
+    m = oracle.Model(ref_bg, H, 0.3)
+    for n, l in [(0, 0), (0, 2), (0, 4)]:
+        x, y = oracle.integral_table(k, pk, n, l, 10000)
+        m.set_integral(n, l, x, y)
+    for l in (0, 2, 4):
+        d = golden[f"{name}_multipoles{l}"]
+        vals = np.array([m.multipole(mask, 1.0, r / H, l) for r in d[:, 0]])
+        assert np.allclose(vals, d[:, 1], rtol=5e-4)
+
+
+def test_oracle_fft_matches_numpy(oracle):
+    rng = np.random.default_rng(0)
+    for n in (16, 64, 100, 10000):
+        x = rng.normal(size=n) + 1j * rng.normal(size=n)
+        assert np.allclose(oracle.fft(x, -1), np.fft.fft(x), atol=1e-10 * n)
+        assert np.allclose(oracle.fft(x, +1), np.fft.ifft(x) * n, atol=1e-10 * n)
+
+
+def test_oracle_special_functions(oracle):
+    from scipy.special import loggamma, spherical_jn, eval_legendre
+
+    for z in [0.7 + 0.3j, 2.5 - 40j, 1.3 + 300j, 0.475 + 100j]:
+        g = oracle.lgamma_c(z)
+        ref = loggamma(z)
+        # lnGamma is defined up to 2 pi i in the imaginary part
+        assert abs(g.real - ref.real) < 1e-9 * max(1, abs(ref.real))
+        assert abs(np.exp(1j * (g.imag - ref.imag)) - 1) < 1e-8
+    for l in range(5):
+        for x in [1e-4, 0.3, 1.0, 2.7, 5.0, 30.0, 300.0]:
+            assert abs(oracle.sph_bessel(l, x) - spherical_jn(l, x)) < 1e-12 * max(1e-30, 1)
+        for mu in [-1, -0.3, 0.0, 0.8, 1.0]:
+            assert abs(oracle.legendre(l, mu) - eval_legendre(l, mu)) < 1e-14
+
+
+def test_oracle_gk61_nodes():
+    """The generated GK61 rule matches the published outermost QUADPACK node and
+    integrates polynomials up to degree 91 exactly."""
+    import importlib.util
+    from pathlib import Path
+
+    src = (Path(__file__).resolve().parent.parent / "oracle" / "gk61_table.h").read_text()
+    vals = [float(t.strip().rstrip(",")) for t in src.split("{")[1].split("}")[0].split()
+            if t.strip().rstrip(",")]
+    assert abs(vals[0] - 0.999484410050490637571325895705811) < 1e-16
+
+
+def test_oracle_qag_known_integrals(oracle):
+    from scipy.special import spherical_jn
+
+    lib = oracle.lib()
+    # integral of a smooth and of an oscillatory function via the direct
+    # Bessel integral: int k^2 P j_0(kr) with P = exp(-k^2) has a closed form
+    k = np.linspace(1e-6, 12, 4000)
+    pk = np.exp(-k ** 2)
+    r = 0.7
+    val = oracle.integral_direct(k, pk, 0, 0, r) * 2 * np.pi ** 2
+    exact = np.sqrt(np.pi) / 4 * np.exp(-r ** 2 / 4)
+    assert abs(val - exact) < 1e-6 * exact
+
+
+def test_gauss_legendre(oracle):
+    x, w = oracle.gauss_legendre(128)
+    xr, wr = np.polynomial.legendre.leggauss(128)
+    assert np.allclose(x, xr, atol=1e-14) and np.allclose(w, wr, atol=1e-14)
