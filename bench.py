@@ -219,7 +219,9 @@ def ours(args, rank, world, local_rank):
     n_sep = len(batch.sep)
     n_evals = batch.n_evals
     ctx = Context(local_rank)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream shared by our kernels and the CUDA events
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     ctx.background_init(c.omega_m, c.omega_baryon, c.omega_gamma, c.h, 10000)
     pk_d = torch.from_numpy(batch.pk).to(dev)

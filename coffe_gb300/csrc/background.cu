@@ -178,6 +178,7 @@ int bg_build_splines(coffe_gpu_ctx *ctx)
     if ((st = spline_build(ctx, ctx->bg[BG_F], z, f, bins))) return st;
     if ((st = spline_build(ctx, ctx->bg[BG_A], z, a, bins))) return st;
     if ((st = spline_build(ctx, ctx->bg[BG_CONFH], z, cH, bins))) return st;
+    if ((st = multipoles_prepare_background(ctx))) return st;
     ctx->bg_ready = true;
     return COFFE_GPU_OK;
 }

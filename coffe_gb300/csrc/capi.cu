@@ -137,7 +137,8 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
     DevBuf *bufs[] = {&ctx->bg_nodes, &ctx->tab_x,  &ctx->tab_x32, &ctx->tab_y,  &ctx->pk,
                       &ctx->kgrid,    &ctx->csc,    &ctx->csfac,   &ctx->samp_idx, &ctx->samp_dx,
                       &ctx->qfac,     &ctx->modec,  &ctx->postf,   &ctx->twid,   &ctx->twid32,
-                      &ctx->spec,     &ctx->req_buf, &ctx->term_meta};
+                      &ctx->spec,     &ctx->req_buf, &ctx->term_meta, &ctx->zrec64,
+                      &ctx->zrec32,   &ctx->mp_retry, &ctx->term_df};
     for (DevBuf *b : bufs) cg_release(*b);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
@@ -344,6 +345,10 @@ int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, doubl
         return cg_check_device_errors(ctx, "multipoles");
     }
     // host arrays: validate, stage, run, copy back
+    if (!ctx->bg_ready || !ctx->int_ready) {
+        cg_set_error(ctx, "multipoles: %s not initialised", ctx->bg_ready ? "integrals" : "background");
+        return COFFE_GPU_ESTATE;
+    }
     if (req_offset[0] != 0) {
         cg_set_error(ctx, "multipoles: req_offset[0] must be 0");
         return COFFE_GPU_EINVAL;

@@ -36,6 +36,10 @@ struct coffe_gpu_ctx {
     double Omega0_m = 0.3, h = 0.67;
     DevBuf bg_nodes; // bins * 8 doubles: z, chi, D1, f, a, confH, H, confHp
     SplineBuf bg[BG_NFN];
+    // fused f / D1 coefficient records on a uniform z grid (multipoles.cu)
+    bool z_uniform = false;
+    double z0 = 0, zn = 0, dz = 0;
+    DevBuf zrec64, zrec32;
     SplineBuf bias[4];
     bool bias_set[4] = {false, false, false, false};
     DevBuf bias_nodes[4];
@@ -61,7 +65,8 @@ struct coffe_gpu_ctx {
     DevBuf modec;     // n_terms * (N/2+1) double2: W_mode/L * M_{q,l}(t)
     DevBuf postf;     // n_terms * N doubles: prefactor * r^(n-l)
     DevBuf twid;      // N/2+1 double2 twiddles exp(-2 pi i j / N)
-    DevBuf twid32;    // float2 copy
+    DevBuf twid32;    // double-float (float4) copy
+    DevBuf term_df;   // double-float copies of modec / modew / postf
     DevBuf spec;      // n_spectra * n_q * (N/2+1) double2 forward half spectra
     // cache key of the per-grid tables
     size_t grid_N = 0, grid_nk = 0;
@@ -71,8 +76,9 @@ struct coffe_gpu_ctx {
 
     DevBuf term_meta; // per-term metadata of the integral tables
 
-    // ---- multipole request staging (host-pointer calls)
+    // ---- multipole request staging (host-pointer calls) and retry list
     DevBuf req_buf;
+    DevBuf mp_retry;
 };
 
 void cg_set_error(coffe_gpu_ctx *ctx, const char *fmt, ...);
@@ -91,6 +97,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
                     unsigned flags);
 int integrals_eval(coffe_gpu_ctx *ctx, int spectrum, int term, const double *r, size_t nq,
                    double *out);
+int multipoles_prepare_background(coffe_gpu_ctx *ctx);
 int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, int n_req,
                    const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
                    const double *sep, int n_l, const int *l, double *out, long long total);

@@ -1,0 +1,77 @@
+// Double-float ("df") arithmetic: a value is the unevaluated sum hi + lo of
+// two floats, |lo| <= ulp(hi)/2, giving about 48 significant bits on the FP32
+// pipes.  Error-free transformations after Knuth (two-sum), Dekker
+// (quick-two-sum) and the FMA-based exact product; the addition is the
+// "sloppy" variant whose error is bounded relative to |x| + |y|, which is what
+// FFT butterflies need.  Used by the mixed-precision FFTLog, where a plain
+// FP32 transform is not accurate enough (its absolute error at high Fourier
+// modes is amplified by the growing Gamma-ratio kernel).
+#pragma once
+
+#include <cuda_runtime.h>
+
+struct dfl {
+    float hi, lo;
+};
+
+__device__ __forceinline__ dfl df_quick_two_sum(float a, float b)
+{
+    const float s = a + b;
+    return dfl{s, b - (s - a)};
+}
+
+__device__ __forceinline__ dfl df_two_sum(float a, float b)
+{
+    const float s = a + b;
+    const float bb = s - a;
+    return dfl{s, (a - (s - bb)) + (b - bb)};
+}
+
+__device__ __forceinline__ dfl df_add(dfl x, dfl y)
+{
+    dfl s = df_two_sum(x.hi, y.hi);
+    return df_quick_two_sum(s.hi, s.lo + (x.lo + y.lo));
+}
+
+__device__ __forceinline__ dfl df_neg(dfl x) { return dfl{-x.hi, -x.lo}; }
+__device__ __forceinline__ dfl df_sub(dfl x, dfl y) { return df_add(x, df_neg(y)); }
+
+__device__ __forceinline__ dfl df_mul(dfl x, dfl y)
+{
+    const float p = x.hi * y.hi;
+    float e = fmaf(x.hi, y.hi, -p);
+    e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, e));
+    return df_quick_two_sum(p, e);
+}
+
+__device__ __forceinline__ dfl df_scale(dfl x, float f) // exact power-of-two scaling when f is one
+{
+    const float p = x.hi * f;
+    const float e = fmaf(x.hi, f, -p) + x.lo * f;
+    return df_quick_two_sum(p, e);
+}
+
+__device__ __forceinline__ dfl df_from_double(double d)
+{
+    const float hi = (float)d;
+    return dfl{hi, (float)(d - (double)hi)};
+}
+
+__device__ __forceinline__ double df_to_double(dfl x) { return (double)x.hi + (double)x.lo; }
+
+// complex double-float, stored as float4 (re.hi, re.lo, im.hi, im.lo)
+struct dfc {
+    dfl re, im;
+};
+
+__device__ __forceinline__ dfc dfc_load(const float4 v) { return dfc{{v.x, v.y}, {v.z, v.w}}; }
+__device__ __forceinline__ float4 dfc_pack(dfc a) { return make_float4(a.re.hi, a.re.lo, a.im.hi, a.im.lo); }
+__device__ __forceinline__ dfc dfc_add(dfc a, dfc b) { return dfc{df_add(a.re, b.re), df_add(a.im, b.im)}; }
+__device__ __forceinline__ dfc dfc_sub(dfc a, dfc b) { return dfc{df_sub(a.re, b.re), df_sub(a.im, b.im)}; }
+__device__ __forceinline__ dfc dfc_mul(dfc a, dfc b)
+{
+    return dfc{df_sub(df_mul(a.re, b.re), df_mul(a.im, b.im)),
+               df_add(df_mul(a.re, b.im), df_mul(a.im, b.re))};
+}
+__device__ __forceinline__ dfc dfc_conj(dfc a) { return dfc{a.re, df_neg(a.im)}; }
+__device__ __forceinline__ dfc dfc_from_double2(double2 v) { return dfc{df_from_double(v.x), df_from_double(v.y)}; }

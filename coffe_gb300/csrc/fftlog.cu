@@ -19,6 +19,7 @@
 
 #include "cplx.cuh"
 #include "ctx.cuh"
+#include "dfloat.cuh"
 #include "qag.cuh"
 
 namespace {
@@ -67,22 +68,27 @@ struct GridPar {
 
 // --------------------------------------------------------------- per grid
 
-// Thomas factors of the natural-spline system on the shared k grid (one thread).
+// Factors of the natural-spline tridiagonal system on the shared k grid (one
+// thread, once per grid): fac = [1/diag'_i (eliminated diagonal), w_i
+// (elimination multipliers), g_i = 1/h_i], each nk long.
 __global__ void csfac_kernel(const double *__restrict__ x, int nk, double *__restrict__ fac)
 {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     const int m = nk - 2;
-    double *diag = fac, *w = fac + nk;
+    double *invd = fac, *w = fac + nk, *g = fac + 2 * nk;
+    for (int i = 0; i + 1 < nk; ++i) g[i] = 1.0 / (x[i + 1] - x[i]);
+    double dprev = 0.0;
+    w[0] = 0.0;
     for (int i = 0; i < m; ++i) {
         const double h_i = x[i + 1] - x[i];
         const double h_ip1 = x[i + 2] - x[i + 1];
-        diag[i] = 2.0 * (h_ip1 + h_i);
-    }
-    w[0] = 0.0;
-    for (int i = 1; i < m; ++i) {
-        const double off = x[i + 1] - x[i];
-        w[i] = off / diag[i - 1];
-        diag[i] -= w[i] * off;
+        double d = 2.0 * (h_ip1 + h_i);
+        if (i > 0) {
+            w[i] = h_i / dprev;
+            d -= w[i] * h_i;
+        }
+        invd[i] = 1.0 / d;
+        dprev = d;
     }
 }
 
@@ -169,49 +175,114 @@ __global__ void term_tables_kernel(GridPar g, int n_terms, const double *__restr
     }
 }
 
-__global__ void twiddle_kernel(int N, double2 *__restrict__ tw, float2 *__restrict__ tw32)
+__global__ void twiddle_kernel(int N, double2 *__restrict__ tw, float4 *__restrict__ twdf)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j > N / 2) return;
     double s, c;
     sincospi(2.0 * (double)j / (double)N, &s, &c);
     tw[j] = make_double2(c, -s);
-    tw32[j] = make_float2((float)c, (float)-s);
+    twdf[j] = dfc_pack(dfc_from_double2(make_double2(c, -s)));
+}
+
+// double-float copies of the per-term tables used by the mixed path
+__global__ void term_tables_df_kernel(int M, int N, int n_terms, const double2 *__restrict__ mcoef,
+                                      const double *__restrict__ postf,
+                                      const double *__restrict__ modew, float4 *__restrict__ mdf,
+                                      float2 *__restrict__ pdf, float2 *__restrict__ wdf)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.y;
+    if (i <= M) {
+        mdf[(size_t)t * (M + 1) + i] = dfc_pack(dfc_from_double2(mcoef[(size_t)t * (M + 1) + i]));
+        if (t == 0) {
+            const dfl v = df_from_double(modew[i]);
+            wdf[i] = make_float2(v.hi, v.lo);
+        }
+    }
+    if (i < N) {
+        const dfl v = df_from_double(postf[(size_t)t * N + i]);
+        pdf[(size_t)t * N + i] = make_float2(v.hi, v.lo);
+    }
 }
 
 // ------------------------------------------------------------ per spectrum
 
-// natural cubic spline coefficients c_i (= y''/2) of each spectrum (one thread
-// per spectrum; forward elimination and back substitution with the grid's
-// Thomas factors, in the order of gsl's tridiagonal solve)
+// Natural cubic spline coefficients c_i (= y''/2) of every spectrum on the
+// shared k grid: one warp per spectrum.  The forward elimination
+// r_i = rhs_i - w_i r_{i-1} and the back substitution
+// c_{i+1} = (r_i - h_{i+1} c_{i+2}) / diag'_i are first-order linear
+// recurrences; each lane owns a contiguous chunk, composes its chunk's affine
+// map, a warp scan of the maps gives every chunk its incoming value, and each
+// lane then replays its chunk.  Same algebra as the sequential Thomas sweep
+// of the tridiagonal solve.
+__device__ __forceinline__ void affine_scan(double &A, double &B, int lane)
+{
+    // inclusive scan of maps r -> A + B r, later lanes applied after earlier ones
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double Ap = __shfl_up_sync(0xffffffffu, A, o);
+        const double Bp = __shfl_up_sync(0xffffffffu, B, o);
+        if (lane >= o) {
+            A = A + B * Ap;
+            B = B * Bp;
+        }
+    }
+}
+
 __global__ void cspline_c_kernel(const double *__restrict__ x, const double *__restrict__ pk,
                                  const double *__restrict__ fac, int nk, int n_spectra,
                                  double *__restrict__ cc)
 {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
     if (s >= n_spectra) return;
     const double *y = pk + (size_t)s * nk;
     double *c = cc + (size_t)s * nk;
-    const double *diag = fac, *w = fac + nk;
+    const double *invd = fac, *w = fac + nk, *g = fac + 2 * nk;
     const int m = nk - 2;
-    // forward sweep (rhs stored in c[1..m])
-    double prev = 0.0;
-    for (int i = 0; i < m; ++i) {
-        const double g_i = 1.0 / (x[i + 1] - x[i]);
-        const double g_ip1 = 1.0 / (x[i + 2] - x[i + 1]);
-        double r = 3.0 * ((y[i + 2] - y[i + 1]) * g_ip1 - (y[i + 1] - y[i]) * g_i);
-        if (i > 0) r -= w[i] * prev;
-        c[i + 1] = r;
-        prev = r;
+    const int chunk = (m + 31) / 32;
+    const int lo = lane * chunk, hi = min(lo + chunk, m);
+    // forward elimination, map r -> rhs_i - w_i r (w_0 = 0)
+    double A = 0.0, B = 1.0;
+    for (int i = lo; i < hi; ++i) {
+        const double rhs = 3.0 * ((y[i + 2] - y[i + 1]) * g[i + 1] - (y[i + 1] - y[i]) * g[i]);
+        const double b = i > 0 ? -w[i] : 0.0;
+        A = rhs + b * A;
+        B = b * B;
     }
-    c[0] = 0.0;
-    c[nk - 1] = 0.0;
-    double next = c[m] / diag[m - 1];
-    c[m] = next;
-    for (int i = m - 2; i >= 0; --i) {
-        const double off = x[i + 2] - x[i + 1];
-        next = (c[i + 1] - off * next) / diag[i];
-        c[i + 1] = next;
+    affine_scan(A, B, lane);
+    double r = __shfl_up_sync(0xffffffffu, A, 1);
+    if (lane == 0) r = 0.0;
+    for (int i = lo; i < hi; ++i) {
+        const double rhs = 3.0 * ((y[i + 2] - y[i + 1]) * g[i + 1] - (y[i + 1] - y[i]) * g[i]);
+        r = i > 0 ? rhs - w[i] * r : rhs;
+        c[i + 1] = r;
+    }
+    __syncwarp();
+    // back substitution from the top: map c -> (r_i - h_{i+1} c) / diag'_i;
+    // lane order reversed so the scan runs from i = m-1 down to 0
+    const int rl = 31 - lane;
+    const int blo = rl * chunk, bhi = min(blo + chunk, m);
+    A = 0.0;
+    B = 1.0;
+    for (int i = bhi - 1; i >= blo; --i) {
+        const double a_i = c[i + 1] * invd[i];
+        const double b_i = -(x[i + 2] - x[i + 1]) * invd[i];
+        A = a_i + b_i * A;
+        B = b_i * B;
+    }
+    affine_scan(A, B, lane);
+    double cn = __shfl_up_sync(0xffffffffu, A, 1);
+    if (lane == 0) cn = 0.0; // c_{m+1} = c_{nk-1} = 0
+    __syncwarp();
+    for (int i = bhi - 1; i >= blo; --i) {
+        cn = (c[i + 1] - (x[i + 2] - x[i + 1]) * cn) * invd[i];
+        c[i + 1] = cn;
+    }
+    if (lane == 0) {
+        c[0] = 0.0;
+        c[nk - 1] = 0.0;
     }
 }
 
@@ -254,40 +325,52 @@ __device__ void smem_fft(T2 *buf, int logM, const T2 *__restrict__ tw, int sign)
     }
 }
 
+// FP64 value of the biased, tapered FFT input at node i: the natural cubic
+// spline of P(k) (twofast.c:399-401, gsl cspline with y + dx(b + dx(c + d dx)))
+// times (kmax/kmin)^((3-q) i/N) W(k_i) (twofast.c:279-290)
+__device__ __forceinline__ double sample_input(const double *__restrict__ kx,
+                                               const double *__restrict__ y,
+                                               const double *__restrict__ c,
+                                               const double *__restrict__ gi,
+                                               const int *__restrict__ idx,
+                                               const double *__restrict__ dxs,
+                                               const double *__restrict__ qf, int i)
+{
+    const int j = idx[i];
+    if (j < 0) return cg_nan<double>();
+    const double h = kx[j + 1] - kx[j];
+    const double g = gi[j];
+    const double y0 = y[j], y1 = y[j + 1], c0 = c[j], c1 = c[j + 1];
+    const double b = (y1 - y0) * g - h * (c1 + 2.0 * c0) * (1.0 / 3.0);
+    const double d = (c1 - c0) * g * (1.0 / 3.0);
+    const double dx = dxs[i];
+    return (y0 + dx * (b + dx * (c0 + d * dx))) * qf[i];
+}
+
+// ---- FP64 path
+
 // Forward half: sample, bias, FFT, conjugate, mode taper.  Grid (spectrum, q).
-template <typename T>
 __global__ void fftlog_forward_kernel(GridPar g, const double *__restrict__ kx,
                                       const double *__restrict__ pk,
-                                      const double *__restrict__ cc, const int *__restrict__ idx,
+                                      const double *__restrict__ cc, const double *__restrict__ fac,
+                                      const int *__restrict__ idx,
                                       const double *__restrict__ dxs,
                                       const double *__restrict__ qfac,
                                       const double *__restrict__ modew,
-                                      const typename V2<T>::t *__restrict__ tw, int n_q,
-                                      typename V2<T>::t *__restrict__ spec, int *err)
+                                      const double2 *__restrict__ tw, int n_q,
+                                      double2 *__restrict__ spec, int *err)
 {
-    typedef typename V2<T>::t T2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T2 *buf = reinterpret_cast<T2 *>(smem_raw);
+    double2 *buf = reinterpret_cast<double2 *>(smem_raw);
     const int s = blockIdx.x, qi = blockIdx.y;
     const int N = g.N, M = N / 2;
     const int logM = 31 - __clz(M);
     const double *y = pk + (size_t)s * g.nk;
     const double *c = cc + (size_t)s * g.nk;
+    const double *gi = fac + 2 * (size_t)g.nk;
     bool bad = false;
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        const int j = idx[i];
-        T v;
-        if (j < 0) {
-            v = cg_nan<T>();
-        } else {
-            const T h = (T)(kx[j + 1] - kx[j]);
-            const T y0 = (T)y[j], y1 = (T)y[j + 1], c0 = (T)c[j], c1 = (T)c[j + 1];
-            const T b = (y1 - y0) / h - h * (c1 + T(2) * c0) / T(3);
-            const T d = (c1 - c0) / (T(3) * h);
-            const T dx = (T)dxs[i];
-            const T p = y0 + dx * (b + dx * (c0 + d * dx));
-            v = p * (T)qfac[(size_t)qi * N + i];
-        }
+        const double v = sample_input(kx, y, c, gi, idx, dxs, qfac + (size_t)qi * N, i);
         if (!isfinite(v)) bad = true;
         const int jj = __brev((unsigned)(i >> 1)) >> (32 - logM);
         if (i & 1)
@@ -297,80 +380,182 @@ __global__ void fftlog_forward_kernel(GridPar g, const double *__restrict__ kx,
     }
     if (bad) cg_flag(err, CG_ERR_NONFINITE);
     __syncthreads();
-    smem_fft<T2>(buf, logM, tw, -1);
+    smem_fft<double2>(buf, logM, tw, -1);
     // unpack the real FFT: Y_k = (Z_k + conj Z_{M-k})/2 - i w^k (Z_k - conj Z_{M-k})/2
-    T2 *out = spec + ((size_t)s * n_q + qi) * (M + 1);
+    double2 *out = spec + ((size_t)s * n_q + qi) * (M + 1);
     for (int k = threadIdx.x; k <= M; k += blockDim.x) {
-        const T2 zk = buf[k & (M - 1)];
-        const T2 zm = buf[(M - k) & (M - 1)];
-        const T ex = T(0.5) * (zk.x + zm.x), ey = T(0.5) * (zk.y - zm.y);
-        const T ox = T(0.5) * (zk.y + zm.y), oy = T(-0.5) * (zk.x - zm.x);
-        const T2 w = tw[k];
-        const T yx = ex + (w.x * ox - w.y * oy);
-        const T yy = ey + (w.x * oy + w.y * ox);
-        const T mw = (T)modew[k];
-        T2 o;
-        o.x = mw * yx;
-        o.y = -mw * yy; // conjugate
-        out[k] = o;
+        const double2 zk = buf[k & (M - 1)];
+        const double2 zm = buf[(M - k) & (M - 1)];
+        const double ex = 0.5 * (zk.x + zm.x), ey = 0.5 * (zk.y - zm.y);
+        const double ox = 0.5 * (zk.y + zm.y), oy = -0.5 * (zk.x - zm.x);
+        const double2 w = tw[k];
+        const double yx = ex + (w.x * ox - w.y * oy);
+        const double yy = ey + (w.x * oy + w.y * ox);
+        const double mw = modew[k];
+        out[k] = make_double2(mw * yx, -mw * yy); // conjugate
     }
 }
 
 // Inverse half: multiply by M_{q,l}, c2r, prefactor.  Grid (spectrum, term).
-template <typename T, typename TO>
-__global__ void fftlog_inverse_kernel(GridPar g, const typename V2<T>::t *__restrict__ spec,
+__global__ void fftlog_inverse_kernel(GridPar g, const double2 *__restrict__ spec,
                                       const int *__restrict__ term_q, int n_q, int n_terms,
                                       const double2 *__restrict__ mcoef,
                                       const double *__restrict__ postf,
-                                      const typename V2<T>::t *__restrict__ tw,
-                                      TO *__restrict__ tab, int *err)
+                                      const double2 *__restrict__ tw, double *__restrict__ tab,
+                                      int *err)
 {
-    typedef typename V2<T>::t T2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T2 *buf = reinterpret_cast<T2 *>(smem_raw);
+    double2 *buf = reinterpret_cast<double2 *>(smem_raw);
     const int s = blockIdx.x, t = blockIdx.y;
     const int N = g.N, M = N / 2;
     const int logM = 31 - __clz(M);
-    const T2 *in = spec + ((size_t)s * n_q + term_q[t]) * (M + 1);
+    const double2 *in = spec + ((size_t)s * n_q + term_q[t]) * (M + 1);
     const double2 *mc = mcoef + (size_t)t * (M + 1);
     // X_k = S_k M_k with Im X_0 = Im X_M = 0 (FFTW c2r ignores them)
     for (int k = threadIdx.x; k < M; k += blockDim.x) {
         const int km = M - k;
-        const double2 ma = mc[k], mb = mc[km];
-        const T2 sa = in[k], sb = in[km];
-        T2 xa, xb;
-        xa.x = sa.x * (T)ma.x - sa.y * (T)ma.y;
-        xa.y = sa.x * (T)ma.y + sa.y * (T)ma.x;
-        xb.x = sb.x * (T)mb.x - sb.y * (T)mb.y;
-        xb.y = sb.x * (T)mb.y + sb.y * (T)mb.x;
+        const double2 xa0 = cmul(in[k], mc[k]), xb0 = cmul(in[km], mc[km]);
+        double2 xa = xa0, xb = xb0;
         if (k == 0) {
-            xa.y = T(0);
-            xb.y = T(0);
+            xa.y = 0.0;
+            xb.y = 0.0;
         }
         // Fe = X_k + conj X_{M-k};  Fo = (X_k - conj X_{M-k}) conj(w^k);  Z = Fe + i Fo
-        const T fex = xa.x + xb.x, fey = xa.y - xb.y;
-        const T dx = xa.x - xb.x, dy = xa.y + xb.y;
-        const T2 w = tw[k];
-        const T fox = dx * w.x + dy * w.y;
-        const T foy = dy * w.x - dx * w.y;
-        T2 z;
-        z.x = fex - foy;
-        z.y = fey + fox;
+        const double fex = xa.x + xb.x, fey = xa.y - xb.y;
+        const double dx = xa.x - xb.x, dy = xa.y + xb.y;
+        const double2 w = tw[k];
+        const double fox = dx * w.x + dy * w.y;
+        const double foy = dy * w.x - dx * w.y;
         const int jj = __brev((unsigned)k) >> (32 - logM);
-        buf[jj] = z;
+        buf[jj] = make_double2(fex - foy, fey + fox);
     }
     __syncthreads();
-    smem_fft<T2>(buf, logM, tw, +1);
+    smem_fft<double2>(buf, logM, tw, +1);
     const size_t len = (size_t)N + CG_N_SMALL_R + 1;
-    TO *o = tab + ((size_t)s * n_terms + t) * len + CG_N_SMALL_R + 1;
+    double *o = tab + ((size_t)s * n_terms + t) * len + CG_N_SMALL_R + 1;
     const double *pf = postf + (size_t)t * N;
     bool bad = false;
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        const T2 z = buf[i >> 1];
-        const T v = (i & 1) ? z.y : z.x;
-        const TO r = (TO)((double)v * pf[i]);
-        if (!isfinite((double)r)) bad = true;
+        const double2 z = buf[i >> 1];
+        const double r = ((i & 1) ? z.y : z.x) * pf[i];
+        if (!isfinite(r)) bad = true;
         o[i] = r;
+    }
+    if (bad) cg_flag(err, CG_ERR_NONFINITE);
+}
+
+// ---- mixed path: the same transforms in double-float on the FP32 pipes
+
+// radix-2 DIT of M = 2^logM double-float complex points (bit-reversed input)
+__device__ void smem_fft_df(float4 *buf, int logM, const float4 *__restrict__ tw, int sign)
+{
+    const int M = 1 << logM;
+    for (int st = 1; st <= logM; ++st) {
+        const int half = 1 << (st - 1);
+        const int stride = M >> (st - 1);
+        for (int b = threadIdx.x; b < M / 2; b += blockDim.x) {
+            const int pos = b & (half - 1);
+            const int i0 = ((b >> (st - 1)) << st) + pos;
+            const int i1 = i0 + half;
+            dfc w = dfc_load(tw[pos * stride]);
+            if (sign > 0) w.im = df_neg(w.im);
+            const dfc u = dfc_load(buf[i0]);
+            const dfc t = dfc_mul(w, dfc_load(buf[i1]));
+            buf[i0] = dfc_pack(dfc_add(u, t));
+            buf[i1] = dfc_pack(dfc_sub(u, t));
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void fftlog_forward_df_kernel(GridPar g, const double *__restrict__ kx,
+                                         const double *__restrict__ pk,
+                                         const double *__restrict__ cc,
+                                         const double *__restrict__ fac,
+                                         const int *__restrict__ idx,
+                                         const double *__restrict__ dxs,
+                                         const double *__restrict__ qfac,
+                                         const float2 *__restrict__ modew_df,
+                                         const float4 *__restrict__ twdf, int n_q,
+                                         float4 *__restrict__ spec, int *err)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4 *buf = reinterpret_cast<float4 *>(smem_raw);
+    float2 *buf2 = reinterpret_cast<float2 *>(smem_raw);
+    const int s = blockIdx.x, qi = blockIdx.y;
+    const int N = g.N, M = N / 2;
+    const int logM = 31 - __clz(M);
+    const double *y = pk + (size_t)s * g.nk;
+    const double *c = cc + (size_t)s * g.nk;
+    const double *gi = fac + 2 * (size_t)g.nk;
+    bool bad = false;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const double v = sample_input(kx, y, c, gi, idx, dxs, qfac + (size_t)qi * N, i);
+        if (!isfinite(v)) bad = true;
+        const dfl d = df_from_double(v);
+        const int jj = __brev((unsigned)(i >> 1)) >> (32 - logM);
+        buf2[2 * jj + (i & 1)] = make_float2(d.hi, d.lo);
+    }
+    if (bad) cg_flag(err, CG_ERR_NONFINITE);
+    __syncthreads();
+    smem_fft_df(buf, logM, twdf, -1);
+    float4 *out = spec + ((size_t)s * n_q + qi) * (M + 1);
+    for (int k = threadIdx.x; k <= M; k += blockDim.x) {
+        const dfc zk = dfc_load(buf[k & (M - 1)]);
+        const dfc zm = dfc_conj(dfc_load(buf[(M - k) & (M - 1)]));
+        const dfc e = dfc_add(zk, zm);                  // 2 E
+        const dfc dd = dfc_sub(zk, zm);                 // 2 i O
+        const dfc o = dfc{dd.im, df_neg(dd.re)};        // 2 O = -i (2 i O)
+        const dfc yk = dfc_add(e, dfc_mul(dfc_load(twdf[k]), o)); // 2 Y_k
+        const float2 mw = modew_df[k];
+        const dfl m = df_scale(dfl{mw.x, mw.y}, 0.5f);
+        out[k] = dfc_pack(dfc{df_mul(yk.re, m), df_neg(df_mul(yk.im, m))}); // conjugate
+    }
+}
+
+__global__ void fftlog_inverse_df_kernel(GridPar g, const float4 *__restrict__ spec,
+                                         const int *__restrict__ term_q, int n_q, int n_terms,
+                                         const float4 *__restrict__ mcoef_df,
+                                         const float2 *__restrict__ postf_df,
+                                         const float4 *__restrict__ twdf, float *__restrict__ tab,
+                                         int *err)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4 *buf = reinterpret_cast<float4 *>(smem_raw);
+    const int s = blockIdx.x, t = blockIdx.y;
+    const int N = g.N, M = N / 2;
+    const int logM = 31 - __clz(M);
+    const float4 *in = spec + ((size_t)s * n_q + term_q[t]) * (M + 1);
+    const float4 *mc = mcoef_df + (size_t)t * (M + 1);
+    for (int k = threadIdx.x; k < M; k += blockDim.x) {
+        const int km = M - k;
+        dfc xa = dfc_mul(dfc_load(in[k]), dfc_load(mc[k]));
+        dfc xb = dfc_mul(dfc_load(in[km]), dfc_load(mc[km]));
+        if (k == 0) {
+            xa.im = dfl{0.f, 0.f};
+            xb.im = dfl{0.f, 0.f};
+        }
+        const dfc xbc = dfc_conj(xb);
+        const dfc fe = dfc_add(xa, xbc);
+        const dfc fo = dfc_mul(dfc_sub(xa, xbc), dfc_conj(dfc_load(twdf[k])));
+        const dfc z = dfc{df_sub(fe.re, fo.im), df_add(fe.im, fo.re)}; // Fe + i Fo
+        const int jj = __brev((unsigned)k) >> (32 - logM);
+        buf[jj] = dfc_pack(z);
+    }
+    __syncthreads();
+    smem_fft_df(buf, logM, twdf, +1);
+    const size_t len = (size_t)N + CG_N_SMALL_R + 1;
+    float *o = tab + ((size_t)s * n_terms + t) * len + CG_N_SMALL_R + 1;
+    const float2 *pf = postf_df + (size_t)t * N;
+    bool bad = false;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const float4 z = buf[i >> 1];
+        const dfl u = (i & 1) ? dfl{z.z, z.w} : dfl{z.x, z.y};
+        const float2 p = pf[i];
+        const dfl r = df_mul(u, dfl{p.x, p.y});
+        const float v = r.hi + r.lo;
+        if (!isfinite(v)) bad = true;
+        o[i] = v;
     }
     if (bad) cg_flag(err, CG_ERR_NONFINITE);
 }
@@ -614,22 +799,25 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     const bool pk_on_device = (flags & COFFE_GPU_PK_DEVICE) != 0;
     if (!pk_on_device && (st = cg_ensure(ctx, ctx->pk, sizeof(double) * nk * n_spectra))) return st;
     if ((st = cg_ensure(ctx, ctx->csc, sizeof(double) * nk * n_spectra))) return st;
-    if ((st = cg_ensure(ctx, ctx->spec, (mixed ? sizeof(float2) : sizeof(double2)) * (M + 1) *
-                                            (size_t)n_spectra * n_q)))
+    if ((st = cg_ensure(ctx, ctx->spec, sizeof(double2) * (M + 1) * (size_t)n_spectra * n_q)))
         return st;
     if ((st = cg_ensure(ctx, ctx->tab_y, (mixed ? sizeof(float) : sizeof(double)) * len *
                                              (size_t)n_spectra * n_terms)))
         return st;
     if (!grid_cached) {
         if ((st = cg_ensure(ctx, ctx->kgrid, sizeof(double) * nk))) return st;
-        if ((st = cg_ensure(ctx, ctx->csfac, sizeof(double) * 2 * nk))) return st;
+        if ((st = cg_ensure(ctx, ctx->csfac, sizeof(double) * 3 * nk))) return st;
         if ((st = cg_ensure(ctx, ctx->samp_idx, sizeof(int) * N))) return st;
         if ((st = cg_ensure(ctx, ctx->samp_dx, sizeof(double) * N))) return st;
         if ((st = cg_ensure(ctx, ctx->qfac, sizeof(double) * N * n_q))) return st;
         if ((st = cg_ensure(ctx, ctx->modec, sizeof(double2) * (M + 1) * n_terms + sizeof(double) * (M + 1)))) return st;
         if ((st = cg_ensure(ctx, ctx->postf, sizeof(double) * N * n_terms))) return st;
         if ((st = cg_ensure(ctx, ctx->twid, sizeof(double2) * (M + 1)))) return st;
-        if ((st = cg_ensure(ctx, ctx->twid32, sizeof(float2) * (M + 1)))) return st;
+        if ((st = cg_ensure(ctx, ctx->twid32, sizeof(float4) * (M + 1)))) return st;
+        if ((st = cg_ensure(ctx, ctx->term_df, (sizeof(float4) + sizeof(float2)) * (M + 1) *
+                                                   (size_t)n_terms +
+                                               sizeof(float2) * (size_t)N * n_terms)))
+            return st;
         if ((st = cg_ensure(ctx, ctx->tab_x, sizeof(double) * len))) return st;
         if ((st = cg_ensure(ctx, ctx->tab_x32, sizeof(float) * len))) return st;
     }
@@ -659,6 +847,9 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
 
     double2 *mcoef = (double2 *)ctx->modec.p;
     double *modew = (double *)((char *)ctx->modec.p + sizeof(double2) * (M + 1) * n_terms);
+    float4 *mdf = (float4 *)ctx->term_df.p;
+    float2 *wdf = (float2 *)(mdf + (size_t)(M + 1) * n_terms);
+    float2 *pdf = wdf + (size_t)(M + 1) * n_terms;
     if (!grid_cached) {
         CG_CUDA(ctx, cudaMemcpyAsync(ctx->kgrid.p, k, sizeof(double) * nk, cudaMemcpyHostToDevice,
                                      ctx->stream));
@@ -686,8 +877,11 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
                                                         ctx->d_err);
         if ((st = cg_after_launch(ctx, "term_tables_kernel"))) return st;
         twiddle_kernel<<<(M + 1 + tb - 1) / tb, tb, 0, ctx->stream>>>(
-            (int)N, (double2 *)ctx->twid.p, (float2 *)ctx->twid32.p);
+            (int)N, (double2 *)ctx->twid.p, (float4 *)ctx->twid32.p);
         if ((st = cg_after_launch(ctx, "twiddle_kernel"))) return st;
+        term_tables_df_kernel<<<tg, tb, 0, ctx->stream>>>(
+            M, (int)N, n_terms, mcoef, (const double *)ctx->postf.p, modew, mdf, pdf, wdf);
+        if ((st = cg_after_launch(ctx, "term_tables_df_kernel"))) return st;
         if ((st = cg_check_device_errors(ctx, "FFTLog coefficient tables"))) return st;
         ctx->grid_N = N;
         ctx->grid_nk = nk;
@@ -695,45 +889,44 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         ctx->grid_terms = terms_key;
     }
     // per spectrum: natural-spline coefficients, forward FFTs, inverse FFTs
-    cspline_c_kernel<<<(n_spectra + 63) / 64, 64, 0, ctx->stream>>>(
-        (const double *)ctx->kgrid.p, d_pk, (const double *)ctx->csfac.p,
-        (int)nk, n_spectra, (double *)ctx->csc.p);
+    cspline_c_kernel<<<(n_spectra + 3) / 4, 128, 0, ctx->stream>>>(
+        (const double *)ctx->kgrid.p, d_pk, (const double *)ctx->csfac.p, (int)nk, n_spectra,
+        (double *)ctx->csc.p);
     if ((st = cg_after_launch(ctx, "cspline_c_kernel"))) return st;
     const int fft_threads = 512;
-    const size_t smem = (mixed ? sizeof(float2) : sizeof(double2)) * M;
+    const size_t smem = sizeof(double2) * M; // == sizeof(float4) * M
     dim3 gf(n_spectra, n_q), gi(n_spectra, n_terms);
     if (mixed) {
-        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_forward_kernel<float>,
+        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_forward_df_kernel,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_kernel<float, float>,
+        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_df_kernel,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        fftlog_forward_kernel<float><<<gf, fft_threads, smem, ctx->stream>>>(
+        fftlog_forward_df_kernel<<<gf, fft_threads, smem, ctx->stream>>>(
             g, (const double *)ctx->kgrid.p, d_pk, (const double *)ctx->csc.p,
-            (const int *)ctx->samp_idx.p, (const double *)ctx->samp_dx.p,
-            (const double *)ctx->qfac.p, modew, (const float2 *)ctx->twid32.p, n_q,
-            (float2 *)ctx->spec.p, ctx->d_err);
-        if ((st = cg_after_launch(ctx, "fftlog_forward_kernel<float>"))) return st;
-        fftlog_inverse_kernel<float, float><<<gi, fft_threads, smem, ctx->stream>>>(
-            g, (const float2 *)ctx->spec.p, d_meta->tq, n_q, n_terms, mcoef,
-            (const double *)ctx->postf.p, (const float2 *)ctx->twid32.p, (float *)ctx->tab_y.p,
-            ctx->d_err);
-        if ((st = cg_after_launch(ctx, "fftlog_inverse_kernel<float>"))) return st;
+            (const double *)ctx->csfac.p, (const int *)ctx->samp_idx.p,
+            (const double *)ctx->samp_dx.p, (const double *)ctx->qfac.p, wdf,
+            (const float4 *)ctx->twid32.p, n_q, (float4 *)ctx->spec.p, ctx->d_err);
+        if ((st = cg_after_launch(ctx, "fftlog_forward_df_kernel"))) return st;
+        fftlog_inverse_df_kernel<<<gi, fft_threads, smem, ctx->stream>>>(
+            g, (const float4 *)ctx->spec.p, d_meta->tq, n_q, n_terms, mdf, pdf,
+            (const float4 *)ctx->twid32.p, (float *)ctx->tab_y.p, ctx->d_err);
+        if ((st = cg_after_launch(ctx, "fftlog_inverse_df_kernel"))) return st;
     } else {
-        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_forward_kernel<double>,
+        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_forward_kernel,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_kernel<double, double>,
+        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_kernel,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        fftlog_forward_kernel<double><<<gf, fft_threads, smem, ctx->stream>>>(
+        fftlog_forward_kernel<<<gf, fft_threads, smem, ctx->stream>>>(
             g, (const double *)ctx->kgrid.p, d_pk, (const double *)ctx->csc.p,
-            (const int *)ctx->samp_idx.p, (const double *)ctx->samp_dx.p,
-            (const double *)ctx->qfac.p, modew, (const double2 *)ctx->twid.p, n_q,
-            (double2 *)ctx->spec.p, ctx->d_err);
-        if ((st = cg_after_launch(ctx, "fftlog_forward_kernel<double>"))) return st;
-        fftlog_inverse_kernel<double, double><<<gi, fft_threads, smem, ctx->stream>>>(
+            (const double *)ctx->csfac.p, (const int *)ctx->samp_idx.p,
+            (const double *)ctx->samp_dx.p, (const double *)ctx->qfac.p, modew,
+            (const double2 *)ctx->twid.p, n_q, (double2 *)ctx->spec.p, ctx->d_err);
+        if ((st = cg_after_launch(ctx, "fftlog_forward_kernel"))) return st;
+        fftlog_inverse_kernel<<<gi, fft_threads, smem, ctx->stream>>>(
             g, (const double2 *)ctx->spec.p, d_meta->tq, n_q, n_terms, mcoef,
             (const double *)ctx->postf.p, (const double2 *)ctx->twid.p, (double *)ctx->tab_y.p,
             ctx->d_err);
-        if ((st = cg_after_launch(ctx, "fftlog_inverse_kernel<double>"))) return st;
+        if ((st = cg_after_launch(ctx, "fftlog_inverse_kernel"))) return st;
     }
     // r = 0 and sub-Mpc entries
     const long tables = (long)n_spectra * n_terms;

@@ -8,43 +8,154 @@
 //     mp_l(z, r) = (2l+1) int_0^1 dx xi(z, mu = 2x - 1, r) P_l(mu)
 // integrated by QUADPACK QAG with the 61-point Gauss-Kronrod rule.
 //
-// One warp owns one (request, separation) pair.  Each lane evaluates xi at two
-// of the 61 nodes of the first panel; xi does not depend on l, so all
-// requested multipoles share those evaluations (the reference recomputes the
-// integrand once per l).  Each l then gets its own GK61 sums and error test;
-// an l whose first panel misses the tolerance continues with the adaptive
-// bisection of QAG for that l alone.
+// Work split: one thread owns one (request, separation) pair and evaluates the
+// whole first GK61 panel on [0, 1] itself -- 61 integrand values, summed in
+// QUADPACK's order, no cross-lane reductions.  The panel's abscissae, weights
+// and P_l(mu_k) are the same for every pair, so they sit in constant memory
+// and are read as warp-uniform broadcasts.  xi does not depend on l, so all
+// requested multipoles share the 61 evaluations (the reference recomputes the
+// integrand once per l).  Each l gets QUADPACK's error estimate and tolerance
+// test; an l whose first panel misses the tolerance is appended to a retry
+// list that a second kernel finishes with the full adaptive QAG, one warp per
+// entry (qag.cuh).  For the den/RSD integrand the first panel converges for
+// practically every pair, so the retry kernel is nearly idle.
 //
 // FP64 path: the reference's arithmetic in double.  Mixed path: the same
-// algorithm with float splines, integrand and Legendre polynomials, and
-// compensated (two-sum) float reductions for the panel result.
+// algorithm with float splines, integrand and Legendre values, and a
+// Kahan-compensated float sum for the panel result.
+#include <vector>
+
 #include "ctx.cuh"
 #include "qag.cuh"
 
 namespace {
 
-#define MP_WARPS 4
-#define MP_CAP 128
 #define MP_MAX_L 8
+#define MP_MAX_LDEG 16
+#define MP_LANE_THREADS 128
+#define MP_RETRY_WARPS 4
+#define MP_CAP 128
 
-template <typename S> struct SplPack {
-    S z_of_chi, f, D1, b1, b2;
-    int has_b1, has_b2;
+// ------------------------------------------------ first-panel constant tables
+// pair p (0..29): xgk index 2p+1 (Gauss nodes, p < 15) or 2(p-15) (Kronrod-only)
+template <typename T> struct PanelTables {
+    T mu1[30], mu2[30]; // mu at x = 0.5 - 0.5 xgk, x = 0.5 + 0.5 xgk
+    T wk[31];           // Kronrod weights; [30] = centre
+    T wg[30];           // Gauss weights (0 for Kronrod-only pairs)
+    T p1[MP_MAX_LDEG + 1][30], p2[MP_MAX_LDEG + 1][30], pc[MP_MAX_LDEG + 1];
 };
+__constant__ PanelTables<double> c_pt64;
+__constant__ PanelTables<float> c_pt32;
 
-// P_l(x) by the upward recurrence (gsl_sf_legendre_Pl), 1/k as a product
-template <typename T> __device__ __forceinline__ T legendre_p(int l, T x)
+template <typename T> __device__ __forceinline__ const PanelTables<T> &pt();
+template <> __device__ __forceinline__ const PanelTables<double> &pt<double>() { return c_pt64; }
+template <> __device__ __forceinline__ const PanelTables<float> &pt<float>() { return c_pt32; }
+
+// P_l(x) by the upward recurrence (gsl_sf_legendre_Pl), host side
+double host_legendre(int l, double x)
 {
-    if (l == 0) return T(1);
+    if (l == 0) return 1.0;
     if (l == 1) return x;
-    T p0 = T(1), p1 = x;
+    double p0 = 1.0, p1 = x;
     for (int k = 2; k <= l; ++k) {
-        const T p2 = ((T(2) * k - T(1)) * x * p1 - (T(k) - T(1)) * p0) * (T(1) / T(k));
+        const double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / (double)k;
         p0 = p1;
         p1 = p2;
     }
     return p1;
 }
+
+const double h_xgk[31] = CG_GK61_XGK_INIT;
+const double h_wgk[31] = CG_GK61_WGK_INIT;
+const double h_wg[15] = CG_GK61_WG_INIT;
+
+bool g_tables_uploaded[64] = {false};
+
+int upload_panel_tables(coffe_gpu_ctx *ctx)
+{
+    if (ctx->device < 64 && g_tables_uploaded[ctx->device]) return COFFE_GPU_OK;
+    PanelTables<double> t64;
+    PanelTables<float> t32;
+    const double center = 0.5, half_length = 0.5;
+    for (int p = 0; p < 30; ++p) {
+        const int g = p < 15 ? 2 * p + 1 : 2 * (p - 15);
+        const double absc = half_length * h_xgk[g];
+        const double x1 = center - absc, x2 = center + absc;
+        t64.mu1[p] = 2 * x1 - 1;
+        t64.mu2[p] = 2 * x2 - 1;
+        t64.wk[p] = h_wgk[g];
+        t64.wg[p] = p < 15 ? h_wg[p] : 0.0;
+        for (int l = 0; l <= MP_MAX_LDEG; ++l) {
+            t64.p1[l][p] = host_legendre(l, t64.mu1[p]);
+            t64.p2[l][p] = host_legendre(l, t64.mu2[p]);
+        }
+    }
+    t64.wk[30] = h_wgk[30];
+    for (int l = 0; l <= MP_MAX_LDEG; ++l) t64.pc[l] = host_legendre(l, 2 * center - 1);
+    for (int p = 0; p < 30; ++p) {
+        t32.mu1[p] = (float)t64.mu1[p];
+        t32.mu2[p] = (float)t64.mu2[p];
+        t32.wk[p] = (float)t64.wk[p];
+        t32.wg[p] = (float)t64.wg[p];
+        for (int l = 0; l <= MP_MAX_LDEG; ++l) {
+            t32.p1[l][p] = (float)t64.p1[l][p];
+            t32.p2[l][p] = (float)t64.p2[l][p];
+        }
+    }
+    t32.wk[30] = (float)t64.wk[30];
+    for (int l = 0; l <= MP_MAX_LDEG; ++l) t32.pc[l] = (float)t64.pc[l];
+    CG_CUDA(ctx, cudaMemcpyToSymbol(c_pt64, &t64, sizeof(t64)));
+    CG_CUDA(ctx, cudaMemcpyToSymbol(c_pt32, &t32, sizeof(t32)));
+    if (ctx->device < 64) g_tables_uploaded[ctx->device] = true;
+    return COFFE_GPU_OK;
+}
+
+// ------------------------------------------------------ background access
+template <typename T> struct ZRec; // f and D1 coefficients of one z interval
+template <> struct ZRec<double> { double4_32a f, d; };
+template <> struct ZRec<float> { float4 f, d; };
+
+__device__ __forceinline__ ZRec<double> ldg_zrec(const ZRec<double> *p)
+{
+    ZRec<double> r;
+    r.f = ldg_c4(&p->f);
+    r.d = ldg_c4(&p->d);
+    return r;
+}
+__device__ __forceinline__ ZRec<float> ldg_zrec(const ZRec<float> *p)
+{
+    ZRec<float> r;
+    r.f = __ldg(&p->f);
+    r.d = __ldg(&p->d);
+    return r;
+}
+
+template <typename T, typename S> struct Bg {
+    S z_of_chi, f, D1, b1, b2;
+    const ZRec<T> *zrec; // fused f / D1 records on a uniform z grid (or null)
+    T z0, zn, dz, inv_dz;
+    int nz, has_b1, has_b2;
+
+    // f(z) and D1(z), one interval search for both
+    __device__ __forceinline__ void fD1(T z, T &fv, T &dv) const
+    {
+        if (zrec) {
+            if (!(z >= z0 && z <= zn)) {
+                fv = dv = cg_nan<T>();
+                return;
+            }
+            int i = (int)((z - z0) * inv_dz);
+            i = i < 0 ? 0 : (i > nz - 2 ? nz - 2 : i);
+            const T dx = z - (z0 + (T)i * dz);
+            const ZRec<T> r = ldg_zrec(zrec + i);
+            fv = r.f.x + dx * (r.f.y + dx * (r.f.z + r.f.w * dx));
+            dv = r.d.x + dx * (r.d.y + dx * (r.d.z + r.d.w * dx));
+        } else {
+            fv = spl_eval(f, z);
+            dv = spl_eval(D1, z);
+        }
+    }
+};
 
 // xi(z_mean, mu, r) of the den/rsd terms in the cancellation-free form:
 // with D = 2 chi^2 - mu^2 r^2 / 2 (= 2 chi1 chi2) and s = 1 - cos(theta) =
@@ -52,7 +163,7 @@ template <typename T> __device__ __forceinline__ T legendre_p(int l, T x)
 // become the polynomials below (identical algebra; the reference's I04
 // coefficient cancels two terms of size (chi/r)^4).
 template <typename T, typename S> struct Xi {
-    SplPack<S> sp;
+    Bg<T, S> bg;
     T chi_mean, sep, I00, I02, I04;
     int contrib;
 
@@ -66,12 +177,13 @@ template <typename T, typename S> struct Xi {
         const T inv_D = T(1) / D;
         const T s = sep * sep * omm * inv_D;
         const T c = T(1) - s;
-        const T z1 = spl_eval(sp.z_of_chi, chi1);
-        const T z2 = spl_eval(sp.z_of_chi, chi2);
-        const T f1 = spl_eval(sp.f, z1);
-        const T f2 = spl_eval(sp.f, z2);
-        const T b1 = sp.has_b1 ? spl_eval(sp.b1, z1) : T(1);
-        const T b2 = sp.has_b2 ? spl_eval(sp.b2, z2) : T(1);
+        const T z1 = spl_eval(bg.z_of_chi, chi1);
+        const T z2 = spl_eval(bg.z_of_chi, chi2);
+        T f1, f2, g1, g2;
+        bg.fD1(z1, f1, g1);
+        bg.fD1(z2, f2, g2);
+        const T b1 = bg.has_b1 ? spl_eval(bg.b1, z1) : T(1);
+        const T b2 = bg.has_b2 ? spl_eval(bg.b2, z2) : T(1);
         T result = T(0);
         if (contrib & COFFE_GPU_DEN) result += b1 * b2 * I00;
         if (contrib & COFFE_GPU_RSD) {
@@ -91,11 +203,25 @@ template <typename T, typename S> struct Xi {
                        b2 * f1 * (T(2.0 / 3) - g * chi2 * chi2)) *
                           I02;
         }
-        return result * spl_eval(sp.D1, z1) * spl_eval(sp.D1, z2);
+        return result * g1 * g2;
     }
 };
 
-// integrand of one multipole at x in [0, 1] (for the adaptive continuation)
+// P_l(x) by the upward recurrence, 1/k as a product (device; adaptive path)
+template <typename T> __device__ __forceinline__ T legendre_p(int l, T x)
+{
+    if (l == 0) return T(1);
+    if (l == 1) return x;
+    T p0 = T(1), p1 = x;
+    for (int k = 2; k <= l; ++k) {
+        const T p2 = ((T(2) * k - T(1)) * x * p1 - (T(k) - T(1)) * p0) * (T(1) / T(k));
+        p0 = p1;
+        p1 = p2;
+    }
+    return p1;
+}
+
+// integrand of one multipole at x in [0, 1] (adaptive continuation)
 template <typename T, typename S> struct MpIntegrand {
     Xi<T, S> xi;
     int l;
@@ -142,108 +268,228 @@ struct MpArgs {
     int t00, t02, t04;
     int n_terms, tab_len;
     double inv_dlog; // N / ln(kmax/kmin), r0 = 1
-    long long per_warp; // contiguous separations per warp
     double epsrel;
+    long long retry_cap;
     int ls[MP_MAX_L];
 };
 
-template <typename T, typename S, typename TT>
-__global__ void __launch_bounds__(32 * MP_WARPS)
-    multipoles_kernel(MpArgs a, SplPack<S> sp, S chi_of_z, const TT *__restrict__ tab_x,
-                      const TT *__restrict__ tab_y, const int *__restrict__ req_spectrum,
-                      const double *__restrict__ req_z_mean, const int64_t *__restrict__ req_offset,
-                      const double *__restrict__ sep, long long total, double *__restrict__ out,
-                      int *err)
+// request of each separation: largest q with req_offset[q] <= item
+__device__ __forceinline__ int find_request(const int64_t *__restrict__ req_offset, int n_req,
+                                            long long item)
 {
-    __shared__ T sa[MP_WARPS][MP_CAP], sb[MP_WARPS][MP_CAP], sr[MP_WARPS][MP_CAP],
-        se[MP_WARPS][MP_CAP];
-    const int w = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
-    const GkLane<T> g = gk_lane<T>();
-    const long long warp_id = (long long)blockIdx.x * MP_WARPS + w;
-    const long long begin = warp_id * a.per_warp;
-    const long long end = begin + a.per_warp < total ? begin + a.per_warp : total;
-    if (begin >= end) return;
-    // request of the first separation: largest q with req_offset[q] <= begin
-    int q;
-    {
-        int lo = 0, hi = a.n_req;
-        while (hi > lo + 1) {
-            const int mid = (lo + hi) >> 1;
-            if (req_offset[mid] <= begin)
-                lo = mid;
-            else
-                hi = mid;
-        }
-        q = lo;
+    int lo = 0, hi = n_req;
+    while (hi > lo + 1) {
+        const int mid = (lo + hi) >> 1;
+        if (req_offset[mid] <= item)
+            lo = mid;
+        else
+            hi = mid;
     }
-    long long q_end = req_offset[q + 1];
-    for (long long item = begin; item < end; ++item) {
-        while (item >= q_end) {
-            ++q;
-            q_end = req_offset[q + 1];
-        }
-        const int s = req_spectrum[q];
-        const T r = (T)sep[item];
-        const T zm = (T)req_z_mean[q];
-        // the three I tables at r: lanes 0..2 look one up each
-        T Iv = T(0);
-        if (lane < 3) {
-            const int t = lane == 0 ? a.t00 : (lane == 1 ? a.t02 : a.t04);
-            const TT *y = tab_y + ((size_t)s * a.n_terms + t) * a.tab_len;
-            Iv = (T)table_lookup<TT>(tab_x, y, a.tab_len, (TT)a.inv_dlog, (TT)r);
-        }
-        Xi<T, S> xi;
-        xi.sp = sp;
-        xi.sep = r;
-        xi.contrib = a.contrib;
-        xi.I00 = __shfl_sync(0xffffffffu, Iv, 0);
-        xi.I02 = __shfl_sync(0xffffffffu, Iv, 1);
-        xi.I04 = __shfl_sync(0xffffffffu, Iv, 2);
-        xi.chi_mean = spl_eval(chi_of_z, zm);
-        // first panel on [0, 1]: mu = 2x - 1 at x = 0.5 -+ 0.5 xgk
-        T mu1 = T(0), mu2 = T(0), xi1 = T(0), xi2 = T(0);
-        if (g.centre) {
-            mu1 = T(0);
-            xi1 = xi(mu1);
-        } else if (g.active) {
-            const T absc = T(0.5) * g.x;
-            mu1 = T(2) * (T(0.5) - absc) - T(1);
-            mu2 = T(2) * (T(0.5) + absc) - T(1);
-            xi1 = xi(mu1);
-            xi2 = xi(mu2);
-        }
-        for (int li = 0; li < a.n_l; ++li) {
-            const int l = a.ls[li];
-            T f1 = xi1, f2 = xi2;
-            if (l != 0) {
-                f1 = g.active ? xi1 * legendre_p<T>(l, mu1) : T(0);
-                f2 = (g.active && !g.centre) ? xi2 * legendre_p<T>(l, mu2) : T(0);
-            }
-            QkOut<T> p0 = qk61_reduce<T>(g, f1, f2, T(0.5));
+    return lo;
+}
+
+template <typename T, typename S, typename TT>
+__device__ __forceinline__ Xi<T, S> make_xi(const MpArgs &a, const Bg<T, S> &bg, const S &chi_of_z,
+                                            const TT *__restrict__ tab_x,
+                                            const TT *__restrict__ tab_y, int s, T zm, T r)
+{
+    Xi<T, S> xi;
+    xi.bg = bg;
+    xi.sep = r;
+    xi.contrib = a.contrib;
+    const TT *y0 = tab_y + ((size_t)s * a.n_terms) * a.tab_len;
+    xi.I00 = (T)table_lookup<TT>(tab_x, y0 + (size_t)a.t00 * a.tab_len, a.tab_len, (TT)a.inv_dlog, (TT)r);
+    xi.I02 = (T)table_lookup<TT>(tab_x, y0 + (size_t)a.t02 * a.tab_len, a.tab_len, (TT)a.inv_dlog, (TT)r);
+    xi.I04 = (T)table_lookup<TT>(tab_x, y0 + (size_t)a.t04 * a.tab_len, a.tab_len, (TT)a.inv_dlog, (TT)r);
+    xi.chi_mean = spl_eval(chi_of_z, zm);
+    return xi;
+}
+
+// --------------------------------------------------------------- fast path
+template <typename T, typename S, typename TT>
+__global__ void __launch_bounds__(MP_LANE_THREADS)
+    mp_lane_kernel(MpArgs a, Bg<T, S> bg, S chi_of_z, const TT *__restrict__ tab_x,
+                   const TT *__restrict__ tab_y, const int *__restrict__ req_spectrum,
+                   const double *__restrict__ req_z_mean, const int64_t *__restrict__ req_offset,
+                   const double *__restrict__ sep, long long total, double *__restrict__ out,
+                   int *__restrict__ retry_count, int2 *__restrict__ retry, int *err)
+{
+    extern __shared__ __align__(16) unsigned char mp_smem[];
+    T *xs = reinterpret_cast<T *>(mp_smem); // [61][blockDim.x] integrand values
+    const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= total) return;
+    const int q = find_request(req_offset, a.n_req, item);
+    const int s = req_spectrum[q];
+    const T r = (T)sep[item];
+    const T zm = (T)req_z_mean[q];
+    const Xi<T, S> xi = make_xi<T, S, TT>(a, bg, chi_of_z, tab_x, tab_y, s, zm, r);
+    const PanelTables<T> &P = pt<T>();
+    const int bd = blockDim.x, tid = threadIdx.x;
+    // integrand at the 61 nodes, QUADPACK order: centre, Gauss pairs, Kronrod pairs
+    const T fc = xi(T(0));
+    xs[60 * bd + tid] = fc;
+#pragma unroll 2
+    for (int p = 0; p < 30; ++p) {
+        xs[(2 * p) * bd + tid] = xi(P.mu1[p]);
+        xs[(2 * p + 1) * bd + tid] = xi(P.mu2[p]);
+    }
+    for (int li = 0; li < a.n_l; ++li) {
+        const int l = a.ls[li];
+        // Kronrod, Gauss and |f| sums
+        T K = fc * P.pc[l] * P.wk[30];
+        T Kc = T(0); // Kahan compensation (mixed path)
+        T G = T(0);
+        T A = fabs(K);
+        for (int p = 0; p < 30; ++p) {
+            const T f1 = xs[(2 * p) * bd + tid] * P.p1[l][p];
+            const T f2 = xs[(2 * p + 1) * bd + tid] * P.p2[l][p];
+            const T fs = f1 + f2;
+            G += P.wg[p] * fs;
+            const T term = P.wk[p] * fs;
             if (sizeof(T) == 4) {
-                // compensated sum of the Kronrod estimate
-                const T fs = f1 + f2;
-                const T prod = g.wk * fs;
-                const T perr = fmaf((float)g.wk, (float)fs, -(float)prod);
-                p0.result = (T)warp_sum_comp((float)prod, (float)perr) * T(0.5);
+                const T yk = term - Kc;
+                const T tk = K + yk;
+                Kc = (tk - K) - yk;
+                K = tk;
+            } else {
+                K += term;
             }
-            int status = 0;
-            MpIntegrand<T, S> fn{xi, l};
-            QagStore<T> store{sa[w], sb[w], sr[w], se[w], MP_CAP};
-            const T v = qag_continue<T>(fn, g, T(0), T(1), p0, T(0), (T)a.epsrel, store, 50000,
-                                        &status);
-            if (lane == 0) {
-                if (status == 1) cg_flag(err, CG_ERR_QAG_LIMIT);
-                const double res = (double)(T(2 * l + 1) * v);
-                if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
-                out[item * a.n_l + li] = res;
-            }
+            A += P.wk[p] * (fabs(f1) + fabs(f2));
+        }
+        const T mean = K * T(0.5);
+        T asc = P.wk[30] * fabs(fc * P.pc[l] - mean);
+        for (int p = 0; p < 30; ++p) {
+            const T f1 = xs[(2 * p) * bd + tid] * P.p1[l][p];
+            const T f2 = xs[(2 * p + 1) * bd + tid] * P.p2[l][p];
+            asc += P.wk[p] * (fabs(f1 - mean) + fabs(f2 - mean));
+        }
+        QkOut<T> o;
+        o.result = K * T(0.5);
+        o.resabs = A * T(0.5);
+        o.resasc = asc * T(0.5);
+        o.abserr = qk_rescale_error((K - G) * T(0.5), o.resabs, o.resasc);
+        // QUADPACK's acceptance test of the first panel (gsl qag.c)
+        const T tolerance = (T)a.epsrel * fabs(o.result);
+        const T round_off = T(50 * CG_DBL_EPS) * o.resabs;
+        const bool roundoff_fail = o.abserr <= round_off && o.abserr > tolerance;
+        const bool ok = (o.abserr <= tolerance && o.abserr != o.resasc) || o.abserr == T(0);
+        if (ok || roundoff_fail) {
+            const double res = (double)(T(2 * l + 1) * o.result);
+            if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
+            out[item * a.n_l + li] = res;
+        } else {
+            const int slot = atomicAdd(retry_count, 1);
+            if (slot < a.retry_cap)
+                retry[slot] = make_int2((int)item, li);
+            else
+                cg_flag(err, CG_ERR_QAG_LIMIT);
         }
     }
 }
 
+// ------------------------------------------------------- adaptive retries
+template <typename T, typename S, typename TT>
+__global__ void __launch_bounds__(32 * MP_RETRY_WARPS)
+    mp_retry_kernel(MpArgs a, Bg<T, S> bg, S chi_of_z, const TT *__restrict__ tab_x,
+                    const TT *__restrict__ tab_y, const int *__restrict__ req_spectrum,
+                    const double *__restrict__ req_z_mean, const int64_t *__restrict__ req_offset,
+                    const double *__restrict__ sep, double *__restrict__ out,
+                    const int *__restrict__ retry_count, const int2 *__restrict__ retry, int *err)
+{
+    __shared__ T sa[MP_RETRY_WARPS][MP_CAP], sb[MP_RETRY_WARPS][MP_CAP],
+        sr[MP_RETRY_WARPS][MP_CAP], se[MP_RETRY_WARPS][MP_CAP];
+    const int w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    int count = *retry_count;
+    if (count > a.retry_cap) count = (int)a.retry_cap;
+    const int nw = gridDim.x * MP_RETRY_WARPS;
+    for (int e = blockIdx.x * MP_RETRY_WARPS + w; e < count; e += nw) {
+        const int2 ent = retry[e];
+        const long long item = ent.x;
+        const int li = ent.y;
+        const int l = a.ls[li];
+        const int q = find_request(req_offset, a.n_req, item);
+        const Xi<T, S> xi =
+            make_xi<T, S, TT>(a, bg, chi_of_z, tab_x, tab_y, req_spectrum[q], (T)req_z_mean[q],
+                              (T)sep[item]);
+        MpIntegrand<T, S> fn{xi, l};
+        QagStore<T> store{sa[w], sb[w], sr[w], se[w], MP_CAP};
+        int status = 0;
+        const T v = qag61_warp<T>(fn, T(0), T(1), T(0), (T)a.epsrel, store, 50000, &status);
+        if (lane == 0) {
+            if (status == 1) cg_flag(err, CG_ERR_QAG_LIMIT);
+            const double res = (double)(T(2 * l + 1) * v);
+            if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
+            out[item * a.n_l + li] = res;
+        }
+    }
+}
+
+template <typename T, typename S, typename TT>
+int launch(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S &chi_of_z,
+           const TT *tab_x, const TT *tab_y, const int *req_spectrum, const double *req_z_mean,
+           const int64_t *req_offset, const double *sep, long long total, double *out)
+{
+    int *d_count = (int *)ctx->mp_retry.p;
+    int2 *d_retry = (int2 *)((char *)ctx->mp_retry.p + 256);
+    CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
+    const size_t smem = sizeof(T) * 61 * MP_LANE_THREADS;
+    CG_CUDA(ctx, cudaFuncSetAttribute(mp_lane_kernel<T, S, TT>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const long long blocks = (total + MP_LANE_THREADS - 1) / MP_LANE_THREADS;
+    mp_lane_kernel<T, S, TT><<<(unsigned)blocks, MP_LANE_THREADS, smem, ctx->stream>>>(
+        a, bg, chi_of_z, tab_x, tab_y, req_spectrum, req_z_mean, req_offset, sep, total, out,
+        d_count, d_retry, ctx->d_err);
+    int st = cg_after_launch(ctx, "mp_lane_kernel");
+    if (st) return st;
+    mp_retry_kernel<T, S, TT><<<ctx->sm_count * 2, 32 * MP_RETRY_WARPS, 0, ctx->stream>>>(
+        a, bg, chi_of_z, tab_x, tab_y, req_spectrum, req_z_mean, req_offset, sep, out, d_count,
+        d_retry, ctx->d_err);
+    return cg_after_launch(ctx, "mp_retry_kernel");
+}
+
+__global__ void zrec_kernel(const double4_32a *__restrict__ f64, const double4_32a *__restrict__ d64,
+                            const float4 *__restrict__ f32, const float4 *__restrict__ d32, int n,
+                            ZRec<double> *__restrict__ r64, ZRec<float> *__restrict__ r32)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    r64[i].f = f64[i];
+    r64[i].d = d64[i];
+    r32[i].f = f32[i];
+    r32[i].d = d32[i];
+}
+
 } // namespace
+
+// Fused f/D1 records when f and D1 share a uniform z grid (background_init's
+// grid z_i = 15 i / (bins - 1)); called after the background splines exist.
+int multipoles_prepare_background(coffe_gpu_ctx *ctx)
+{
+    const int n = ctx->bg_bins;
+    ctx->z_uniform = false;
+    std::vector<double> z(n);
+    CG_CUDA(ctx, cudaMemcpyAsync(z.data(), ctx->bg_nodes.p, sizeof(double) * n,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const double dz = (z[n - 1] - z[0]) / (n - 1);
+    bool uni = dz > 0;
+    for (int i = 0; i < n && uni; ++i)
+        if (fabs(z[i] - (z[0] + i * dz)) > 1e-12 * (fabs(z[i]) + dz)) uni = false;
+    if (!uni) return COFFE_GPU_OK;
+    int st = cg_ensure(ctx, ctx->zrec64, sizeof(ZRec<double>) * (n - 1));
+    if (st) return st;
+    if ((st = cg_ensure(ctx, ctx->zrec32, sizeof(ZRec<float>) * (n - 1)))) return st;
+    zrec_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(
+        ctx->bg[BG_F].c64, ctx->bg[BG_D1].c64, ctx->bg[BG_F].c32, ctx->bg[BG_D1].c32, n,
+        (ZRec<double> *)ctx->zrec64.p, (ZRec<float> *)ctx->zrec32.p);
+    if ((st = cg_after_launch(ctx, "zrec_kernel"))) return st;
+    ctx->z_uniform = true;
+    ctx->z0 = z[0];
+    ctx->zn = z[n - 1];
+    ctx->dz = dz;
+    return COFFE_GPU_OK;
+}
 
 int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, int n_req,
                    const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
@@ -275,6 +521,10 @@ int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel
         cg_set_error(ctx, "multipoles: epsrel must be positive");
         return COFFE_GPU_EINVAL;
     }
+    if (total > (long long)INT32_MAX) {
+        cg_set_error(ctx, "multipoles: at most 2^31-1 separations per call");
+        return COFFE_GPU_EINVAL;
+    }
     MpArgs a;
     a.n_req = n_req;
     a.n_l = n_l;
@@ -293,40 +543,58 @@ int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel
     a.tab_len = (int)(ctx->N + CG_N_SMALL_R + 1);
     a.inv_dlog = (double)ctx->N / log(ctx->kmax / ctx->kmin);
     a.epsrel = epsrel;
+    for (int i = 0; i < MP_MAX_L; ++i) a.ls[i] = 0;
     for (int i = 0; i < n_l; ++i) {
-        if (l[i] < 0 || l[i] > 32) {
-            cg_set_error(ctx, "multipoles: l = %d out of range", l[i]);
+        if (l[i] < 0 || l[i] > MP_MAX_LDEG) {
+            cg_set_error(ctx, "multipoles: l = %d out of range [0, %d]", l[i], MP_MAX_LDEG);
             return COFFE_GPU_EINVAL;
         }
         a.ls[i] = l[i];
     }
     if (total <= 0) return COFFE_GPU_OK;
+    int st = upload_panel_tables(ctx);
+    if (st) return st;
     if (ctx->sm_count <= 0)
         CG_CUDA(ctx, cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount,
                                             ctx->device));
-    const int sms = ctx->sm_count;
-    // contiguous ranges of separations per warp (one request search per range)
-    const long long max_warps = (long long)sms * 16 * MP_WARPS;
-    long long nw = total < max_warps ? total : max_warps;
-    a.per_warp = (total + nw - 1) / nw;
-    nw = (total + a.per_warp - 1) / a.per_warp;
-    const int blocks = (int)((nw + MP_WARPS - 1) / MP_WARPS);
+    a.retry_cap = total * n_l;
+    if ((st = cg_ensure(ctx, ctx->mp_retry, 256 + sizeof(int2) * (size_t)a.retry_cap))) return st;
     if (precision == COFFE_GPU_MIXED) {
-        SplPack<Spl32> sp{ctx->bg[BG_Z_OF_CHI].v32(), ctx->bg[BG_F].v32(), ctx->bg[BG_D1].v32(),
-                          ctx->bias[0].v32(), ctx->bias[1].v32(), ctx->bias_set[0],
-                          ctx->bias_set[1]};
-        multipoles_kernel<float, Spl32, float><<<blocks, 32 * MP_WARPS, 0, ctx->stream>>>(
-            a, sp, ctx->bg[BG_CHI_OF_Z].v32(), (const float *)ctx->tab_x32.p,
-            (const float *)ctx->tab_y.p, req_spectrum, req_z_mean, req_offset, sep, total, out,
-            ctx->d_err);
-    } else {
-        SplPack<Spl64> sp{ctx->bg[BG_Z_OF_CHI].v64(), ctx->bg[BG_F].v64(), ctx->bg[BG_D1].v64(),
-                          ctx->bias[0].v64(), ctx->bias[1].v64(), ctx->bias_set[0],
-                          ctx->bias_set[1]};
-        multipoles_kernel<double, Spl64, double><<<blocks, 32 * MP_WARPS, 0, ctx->stream>>>(
-            a, sp, ctx->bg[BG_CHI_OF_Z].v64(), (const double *)ctx->tab_x.p,
-            (const double *)ctx->tab_y.p, req_spectrum, req_z_mean, req_offset, sep, total, out,
-            ctx->d_err);
+        Bg<float, Spl32> bg;
+        bg.z_of_chi = ctx->bg[BG_Z_OF_CHI].v32();
+        bg.f = ctx->bg[BG_F].v32();
+        bg.D1 = ctx->bg[BG_D1].v32();
+        bg.b1 = ctx->bias[0].v32();
+        bg.b2 = ctx->bias[1].v32();
+        bg.has_b1 = ctx->bias_set[0];
+        bg.has_b2 = ctx->bias_set[1];
+        bg.zrec = ctx->z_uniform ? (const ZRec<float> *)ctx->zrec32.p : nullptr;
+        bg.z0 = (float)ctx->z0;
+        bg.zn = (float)ctx->zn;
+        bg.dz = (float)ctx->dz;
+        bg.inv_dz = (float)(1.0 / ctx->dz);
+        bg.nz = ctx->bg_bins;
+        return launch<float, Spl32, float>(ctx, a, bg, ctx->bg[BG_CHI_OF_Z].v32(),
+                                           (const float *)ctx->tab_x32.p,
+                                           (const float *)ctx->tab_y.p, req_spectrum, req_z_mean,
+                                           req_offset, sep, total, out);
     }
-    return cg_after_launch(ctx, "multipoles_kernel");
+    Bg<double, Spl64> bg;
+    bg.z_of_chi = ctx->bg[BG_Z_OF_CHI].v64();
+    bg.f = ctx->bg[BG_F].v64();
+    bg.D1 = ctx->bg[BG_D1].v64();
+    bg.b1 = ctx->bias[0].v64();
+    bg.b2 = ctx->bias[1].v64();
+    bg.has_b1 = ctx->bias_set[0];
+    bg.has_b2 = ctx->bias_set[1];
+    bg.zrec = ctx->z_uniform ? (const ZRec<double> *)ctx->zrec64.p : nullptr;
+    bg.z0 = ctx->z0;
+    bg.zn = ctx->zn;
+    bg.dz = ctx->dz;
+    bg.inv_dz = 1.0 / ctx->dz;
+    bg.nz = ctx->bg_bins;
+    return launch<double, Spl64, double>(ctx, a, bg, ctx->bg[BG_CHI_OF_Z].v64(),
+                                         (const double *)ctx->tab_x.p,
+                                         (const double *)ctx->tab_y.p, req_spectrum, req_z_mean,
+                                         req_offset, sep, total, out);
 }

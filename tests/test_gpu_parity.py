@@ -24,16 +24,16 @@ def rel_floor(got, ref, floor):
 
 
 def local_envelope(y, half=64):
-    a = np.abs(y)
+    a = np.nan_to_num(np.abs(y), nan=0.0)
     out = np.empty_like(a)
     for i in range(len(a)):
         out[i] = a[max(0, i - half): i + half + 1].max()
     return out
 
 
-def table_err(gy, oy, mask):
+def table_err(gy, oy, mask, floor=1e-8):
     env = local_envelope(oy)
-    return np.max((np.abs(gy - oy) / np.maximum(np.abs(oy), 1e-8 * env))[mask])
+    return np.max((np.abs(gy - oy) / np.maximum(np.abs(oy), floor * env))[mask])
 
 
 @pytest.fixture(scope="module")
@@ -108,8 +108,9 @@ def test_integral_tables_mixed_close_to_oracle(gpu_ctx, oracle, cfg1):
         mask = (ox >= 5 / H) & (ox <= 300 / H)
         mask[:43] = False
         assert np.isnan(gy[:43]).all()  # not requested
-        e = table_err(gy, oy, mask)
-        assert e < 1e-4, ((n, l), e)
+        # double-float FFT, tables stored as float: float rounding dominates
+        e = table_err(gy, oy, mask, floor=1e-6)
+        assert e < 1e-6, ((n, l), e)
 
 
 def test_all_bessel_integrals_2e14_fp64(gpu_ctx, oracle, w):
@@ -124,7 +125,8 @@ def test_all_bessel_integrals_2e14_fp64(gpu_ctx, oracle, w):
         ox, oy = oracle.integral_table(k, pk, n, l, N, with_small_r=False)
         mask = (ox >= 1.0) & (ox <= 1e4)
         mask[:43] = False
-        e = table_err(gy, oy, mask)
+        # 2^14-point tables span a wider dynamic range: floor at 1e-6 of the local envelope
+        e = table_err(gy, oy, mask, floor=1e-6)
         worst = max(worst, e)
         assert e < 1e-10, ((n, l), e)
     print("worst FP64 table error (2^14, 30 terms):", worst)
