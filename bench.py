@@ -287,7 +287,9 @@ def ours(args, rank, world, local_rank):
     # accuracy of the mixed path against the FP64 path on the full batch (the
     # FP64 path itself matches the CPU oracle to 1e-10 in the parity tests)
     step("mixed")
+    retries = {"mixed": ctx.last_retries()}
     step("fp64")
+    retries["fp64"] = ctx.last_retries()
     ctx.synchronize()
     err = rel_err_vs(outs["fp64"].cpu().numpy(), outs["mixed"].cpu().numpy(), batch)
 
@@ -377,6 +379,7 @@ def ours(args, rank, world, local_rank):
                  "ms_per_step": 1e3 * dev_fp64 / k64},
         "mixed_over_fp64": value / fp64_value,
         "max_rel_err_mixed_vs_fp64": err,
+        "adaptive_retries": retries,
         "gpu_launches": int(launches),
         "roofline": {"kernel": "multipoles_kernel<float> (mixed multipole quadrature)",
                      "bound": "fp32", "achieved": achieved,

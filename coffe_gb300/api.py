@@ -99,6 +99,11 @@ class Context:
     def launch_count(self) -> int:
         return int(self._L.coffe_gpu_launch_count(self._ctx))
 
+    def last_retries(self) -> int:
+        """(separation, l) outputs of the last multipoles call that needed the
+        adaptive bisection after the first GK61 panel."""
+        return int(self._L.coffe_gpu_multipoles_retries(self._ctx))
+
     # ------------------------------------------------------------ background
     def background_init(self, omega_m=0.3, omega_baryon=0.05, omega_gamma=9e-5, h=0.67,
                         bins=10000):

@@ -138,7 +138,8 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
                       &ctx->kgrid,    &ctx->csc,    &ctx->csfac,   &ctx->samp_idx, &ctx->samp_dx,
                       &ctx->qfac,     &ctx->modec,  &ctx->postf,   &ctx->twid,   &ctx->twid32,
                       &ctx->spec,     &ctx->req_buf, &ctx->term_meta, &ctx->zrec64,
-                      &ctx->zrec32,   &ctx->mp_retry, &ctx->term_df};
+                      &ctx->zrec32,   &ctx->mp_retry, &ctx->term_df,
+                      &ctx->samp_f32, &ctx->csfac32};
     for (DevBuf *b : bufs) cg_release(*b);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
@@ -167,6 +168,17 @@ int coffe_gpu_set_stream(coffe_gpu_ctx_t *ctx, void *stream)
 }
 
 long long coffe_gpu_launch_count(const coffe_gpu_ctx_t *ctx) { return ctx ? ctx->launches : -1; }
+
+long long coffe_gpu_multipoles_retries(coffe_gpu_ctx_t *ctx)
+{
+    if (!ctx || !ctx->mp_retry.p) return -1;
+    int count = 0;
+    if (cudaMemcpyAsync(&count, ctx->mp_retry.p, sizeof(int), cudaMemcpyDeviceToHost,
+                        ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        return -1;
+    return count;
+}
 
 int coffe_gpu_background_init(coffe_gpu_ctx_t *ctx, const coffe_gpu_cosmology_t *c)
 {

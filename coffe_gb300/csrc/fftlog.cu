@@ -71,7 +71,8 @@ struct GridPar {
 // Factors of the natural-spline tridiagonal system on the shared k grid (one
 // thread, once per grid): fac = [1/diag'_i (eliminated diagonal), w_i
 // (elimination multipliers), g_i = 1/h_i], each nk long.
-__global__ void csfac_kernel(const double *__restrict__ x, int nk, double *__restrict__ fac)
+__global__ void csfac_kernel(const double *__restrict__ x, int nk, double *__restrict__ fac,
+                             float *__restrict__ fac32)
 {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     const int m = nk - 2;
@@ -90,13 +91,21 @@ __global__ void csfac_kernel(const double *__restrict__ x, int nk, double *__res
         invd[i] = 1.0 / d;
         dprev = d;
     }
+    // float copies for the mixed path: [1/diag', w, 1/h, h]
+    for (int i = 0; i < nk; ++i) {
+        fac32[i] = i < m ? (float)invd[i] : 0.f;
+        fac32[nk + i] = i < m ? (float)w[i] : 0.f;
+        fac32[2 * nk + i] = i + 1 < nk ? (float)g[i] : 0.f;
+        fac32[3 * nk + i] = i + 1 < nk ? (float)(x[i + 1] - x[i]) : 0.f;
+    }
 }
 
 // FFT node -> (input interval, offset); windowed bias per distinct q
 __global__ void sampling_kernel(GridPar g, const double *__restrict__ kx, int *__restrict__ idx,
-                                double *__restrict__ dxs, int n_q, const double *__restrict__ qv,
-                                double *__restrict__ qfac, double *__restrict__ modew,
-                                double *__restrict__ tab_x, float *__restrict__ tab_x32)
+                                double *__restrict__ dxs, float4 *__restrict__ sf32, int n_q,
+                                const double *__restrict__ qv, double *__restrict__ qfac,
+                                double *__restrict__ modew, double *__restrict__ tab_x,
+                                float *__restrict__ tab_x32)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = g.N;
@@ -117,6 +126,8 @@ __global__ void sampling_kernel(GridPar g, const double *__restrict__ kx, int *_
         const bool inside = ki >= kx[0] && ki <= kx[g.nk - 1];
         idx[i] = inside ? lo : -1;
         dxs[i] = ki - kx[lo];
+        const double hl = kx[lo + 1] - kx[lo];
+        sf32[i] = make_float4((float)(ki - kx[lo]), (float)hl, (float)(1.0 / hl), 0.f);
         const double w = twofast_window(ki, g.kmin, xmax_w, xleft_w, xright_w);
         for (int q = 0; q < n_q; ++q) qfac[(size_t)q * N + i] = pow(ratio, (3. - qv[q]) * i / N) * w;
         const double ri = g.r0 * pow(ratio, (double)i / N);
@@ -283,6 +294,84 @@ __global__ void cspline_c_kernel(const double *__restrict__ x, const double *__r
     if (lane == 0) {
         c[0] = 0.0;
         c[nk - 1] = 0.0;
+    }
+}
+
+// The same solve in float for the mixed path: c enters the resampled P(k) only
+// through the h (c1 + 2 c0)/3 and dx^2 terms, corrections of relative size
+// ~(h/k)^2, so float accuracy of c is far below the target error.
+__device__ __forceinline__ void affine_scan_f(float &A, float &B, int lane)
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float Ap = __shfl_up_sync(0xffffffffu, A, o);
+        const float Bp = __shfl_up_sync(0xffffffffu, B, o);
+        if (lane >= o) {
+            A = fmaf(B, Ap, A);
+            B = B * Bp;
+        }
+    }
+}
+
+__global__ void cspline_c32_kernel(const double *__restrict__ pk, const float *__restrict__ fac32,
+                                   int nk, int n_spectra, float *__restrict__ cc)
+{
+    const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (s >= n_spectra) return;
+    const double *y = pk + (size_t)s * nk;
+    float *c = cc + (size_t)s * nk;
+    const float *invd = fac32, *w = fac32 + nk, *g = fac32 + 2 * nk, *hh = fac32 + 3 * nk;
+    const int m = nk - 2;
+    const int chunk = (m + 31) / 32;
+    const int lo = lane * chunk, hi = min(lo + chunk, m);
+    // sliding window of float samples: one conversion per element and pass
+    float A = 0.f, B = 1.f;
+    float ya = lo < hi ? (float)y[lo] : 0.f, yb = lo < hi ? (float)y[lo + 1] : 0.f;
+    for (int i = lo; i < hi; ++i) {
+        const float yc = (float)y[i + 2];
+        const float rhs = 3.f * ((yc - yb) * g[i + 1] - (yb - ya) * g[i]);
+        const float b = i > 0 ? -w[i] : 0.f;
+        A = fmaf(b, A, rhs);
+        B = b * B;
+        ya = yb;
+        yb = yc;
+    }
+    affine_scan_f(A, B, lane);
+    float r = __shfl_up_sync(0xffffffffu, A, 1);
+    if (lane == 0) r = 0.f;
+    ya = lo < hi ? (float)y[lo] : 0.f;
+    yb = lo < hi ? (float)y[lo + 1] : 0.f;
+    for (int i = lo; i < hi; ++i) {
+        const float yc = (float)y[i + 2];
+        const float rhs = 3.f * ((yc - yb) * g[i + 1] - (yb - ya) * g[i]);
+        r = i > 0 ? fmaf(-w[i], r, rhs) : rhs;
+        c[i + 1] = r;
+        ya = yb;
+        yb = yc;
+    }
+    __syncwarp();
+    const int rl = 31 - lane;
+    const int blo = rl * chunk, bhi = min(blo + chunk, m);
+    A = 0.f;
+    B = 1.f;
+    for (int i = bhi - 1; i >= blo; --i) {
+        const float a_i = c[i + 1] * invd[i];
+        const float b_i = -hh[i + 1] * invd[i];
+        A = fmaf(b_i, A, a_i);
+        B = b_i * B;
+    }
+    affine_scan_f(A, B, lane);
+    float cn = __shfl_up_sync(0xffffffffu, A, 1);
+    if (lane == 0) cn = 0.f;
+    __syncwarp();
+    for (int i = bhi - 1; i >= blo; --i) {
+        cn = (c[i + 1] - hh[i + 1] * cn) * invd[i];
+        c[i + 1] = cn;
+    }
+    if (lane == 0) {
+        c[0] = 0.f;
+        c[nk - 1] = 0.f;
     }
 }
 
@@ -468,12 +557,34 @@ __device__ void smem_fft_df(float4 *buf, int logM, const float4 *__restrict__ tw
     }
 }
 
-__global__ void fftlog_forward_df_kernel(GridPar g, const double *__restrict__ kx,
-                                         const double *__restrict__ pk,
-                                         const double *__restrict__ cc,
+// Mixed-path sampling: the secant part y0 + dx (y1 - y0)/h in FP64, the
+// spline-curvature correction dx (-h (c1 + 2 c0)/3 + dx (c0 + d dx)) in float
+// (a relative correction of size ~(h/k)^2, so float is far below the target).
+__device__ __forceinline__ double sample_input_mixed(const double *__restrict__ y,
+                                                     const float *__restrict__ c,
+                                                     const double *__restrict__ gi,
+                                                     const int *__restrict__ idx,
+                                                     const double *__restrict__ dxs,
+                                                     const float4 *__restrict__ sf,
+                                                     const double *__restrict__ qf, int i)
+{
+    const int j = idx[i];
+    if (j < 0) return cg_nan<double>();
+    const double y0 = y[j];
+    const double main = fma(dxs[i], (y[j + 1] - y0) * gi[j], y0);
+    const float4 f = sf[i]; // (dx, h, 1/h, -)
+    const float c0 = c[j], c1 = c[j + 1];
+    const float d = (c1 - c0) * f.z * (1.f / 3.f);
+    const float corr = f.x * (-f.y * (c1 + 2.f * c0) * (1.f / 3.f) + f.x * (c0 + d * f.x));
+    return (main + (double)corr) * qf[i];
+}
+
+__global__ void fftlog_forward_df_kernel(GridPar g, const double *__restrict__ pk,
+                                         const float *__restrict__ cc32,
                                          const double *__restrict__ fac,
                                          const int *__restrict__ idx,
                                          const double *__restrict__ dxs,
+                                         const float4 *__restrict__ sf32,
                                          const double *__restrict__ qfac,
                                          const float2 *__restrict__ modew_df,
                                          const float4 *__restrict__ twdf, int n_q,
@@ -486,11 +597,11 @@ __global__ void fftlog_forward_df_kernel(GridPar g, const double *__restrict__ k
     const int N = g.N, M = N / 2;
     const int logM = 31 - __clz(M);
     const double *y = pk + (size_t)s * g.nk;
-    const double *c = cc + (size_t)s * g.nk;
+    const float *c = cc32 + (size_t)s * g.nk;
     const double *gi = fac + 2 * (size_t)g.nk;
     bool bad = false;
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        const double v = sample_input(kx, y, c, gi, idx, dxs, qfac + (size_t)qi * N, i);
+        const double v = sample_input_mixed(y, c, gi, idx, dxs, sf32, qfac + (size_t)qi * N, i);
         if (!isfinite(v)) bad = true;
         const dfl d = df_from_double(v);
         const int jj = __brev((unsigned)(i >> 1)) >> (32 - logM);
@@ -809,6 +920,8 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         if ((st = cg_ensure(ctx, ctx->csfac, sizeof(double) * 3 * nk))) return st;
         if ((st = cg_ensure(ctx, ctx->samp_idx, sizeof(int) * N))) return st;
         if ((st = cg_ensure(ctx, ctx->samp_dx, sizeof(double) * N))) return st;
+        if ((st = cg_ensure(ctx, ctx->samp_f32, sizeof(float4) * N))) return st;
+        if ((st = cg_ensure(ctx, ctx->csfac32, sizeof(float) * 4 * nk))) return st;
         if ((st = cg_ensure(ctx, ctx->qfac, sizeof(double) * N * n_q))) return st;
         if ((st = cg_ensure(ctx, ctx->modec, sizeof(double2) * (M + 1) * n_terms + sizeof(double) * (M + 1)))) return st;
         if ((st = cg_ensure(ctx, ctx->postf, sizeof(double) * N * n_terms))) return st;
@@ -863,13 +976,13 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         CG_CUDA(ctx, cudaMemcpyAsync(ctx->tab_x32.p, hx32, sizeof(hx32), cudaMemcpyHostToDevice,
                                      ctx->stream));
         csfac_kernel<<<1, 1, 0, ctx->stream>>>((const double *)ctx->kgrid.p, (int)nk,
-                                               (double *)ctx->csfac.p);
+                                               (double *)ctx->csfac.p, (float *)ctx->csfac32.p);
         if ((st = cg_after_launch(ctx, "csfac_kernel"))) return st;
         const int tb = 256;
         sampling_kernel<<<((int)N + tb) / tb, tb, 0, ctx->stream>>>(
-            g, (const double *)ctx->kgrid.p, (int *)ctx->samp_idx.p, (double *)ctx->samp_dx.p, n_q,
-            d_meta->qv, (double *)ctx->qfac.p, modew, (double *)ctx->tab_x.p,
-            (float *)ctx->tab_x32.p);
+            g, (const double *)ctx->kgrid.p, (int *)ctx->samp_idx.p, (double *)ctx->samp_dx.p,
+            (float4 *)ctx->samp_f32.p, n_q, d_meta->qv, (double *)ctx->qfac.p, modew,
+            (double *)ctx->tab_x.p, (float *)ctx->tab_x32.p);
         if ((st = cg_after_launch(ctx, "sampling_kernel"))) return st;
         dim3 tg(((int)N + tb - 1) / tb + 1, n_terms);
         term_tables_kernel<<<tg, tb, 0, ctx->stream>>>(g, n_terms, d_meta->q, d_meta->l,
@@ -889,10 +1002,16 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         ctx->grid_terms = terms_key;
     }
     // per spectrum: natural-spline coefficients, forward FFTs, inverse FFTs
-    cspline_c_kernel<<<(n_spectra + 3) / 4, 128, 0, ctx->stream>>>(
-        (const double *)ctx->kgrid.p, d_pk, (const double *)ctx->csfac.p, (int)nk, n_spectra,
-        (double *)ctx->csc.p);
-    if ((st = cg_after_launch(ctx, "cspline_c_kernel"))) return st;
+    if (mixed) {
+        cspline_c32_kernel<<<(n_spectra + 3) / 4, 128, 0, ctx->stream>>>(
+            d_pk, (const float *)ctx->csfac32.p, (int)nk, n_spectra, (float *)ctx->csc.p);
+        if ((st = cg_after_launch(ctx, "cspline_c32_kernel"))) return st;
+    } else {
+        cspline_c_kernel<<<(n_spectra + 3) / 4, 128, 0, ctx->stream>>>(
+            (const double *)ctx->kgrid.p, d_pk, (const double *)ctx->csfac.p, (int)nk, n_spectra,
+            (double *)ctx->csc.p);
+        if ((st = cg_after_launch(ctx, "cspline_c_kernel"))) return st;
+    }
     const int fft_threads = 512;
     const size_t smem = sizeof(double2) * M; // == sizeof(float4) * M
     dim3 gf(n_spectra, n_q), gi(n_spectra, n_terms);
@@ -902,9 +1021,9 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_df_kernel,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         fftlog_forward_df_kernel<<<gf, fft_threads, smem, ctx->stream>>>(
-            g, (const double *)ctx->kgrid.p, d_pk, (const double *)ctx->csc.p,
-            (const double *)ctx->csfac.p, (const int *)ctx->samp_idx.p,
-            (const double *)ctx->samp_dx.p, (const double *)ctx->qfac.p, wdf,
+            g, d_pk, (const float *)ctx->csc.p, (const double *)ctx->csfac.p,
+            (const int *)ctx->samp_idx.p, (const double *)ctx->samp_dx.p,
+            (const float4 *)ctx->samp_f32.p, (const double *)ctx->qfac.p, wdf,
             (const float4 *)ctx->twid32.p, n_q, (float4 *)ctx->spec.p, ctx->d_err);
         if ((st = cg_after_launch(ctx, "fftlog_forward_df_kernel"))) return st;
         fftlog_inverse_df_kernel<<<gi, fft_threads, smem, ctx->stream>>>(

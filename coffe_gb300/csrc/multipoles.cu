@@ -23,6 +23,7 @@
 // FP64 path: the reference's arithmetic in double.  Mixed path: the same
 // algorithm with float splines, integrand and Legendre values, and a
 // Kahan-compensated float sum for the panel result.
+#include <algorithm>
 #include <vector>
 
 #include "ctx.cuh"
@@ -31,18 +32,26 @@
 namespace {
 
 #define MP_MAX_L 8
-#define MP_MAX_LDEG 16
+#define MP_MAX_LDEG 8
 #define MP_LANE_THREADS 128
 #define MP_RETRY_WARPS 4
 #define MP_CAP 128
 
 // ------------------------------------------------ first-panel constant tables
-// pair p (0..29): xgk index 2p+1 (Gauss nodes, p < 15) or 2(p-15) (Kronrod-only)
+// The 61 nodes of the first panel on [0, 1] are stored in "slots": slot 2p and
+// 2p+1 are the pair x = 0.5 -+ 0.5 xgk[g_p] with g_p = 2p+1 (Gauss nodes,
+// p < 15) or 2(p-15) (Kronrod-only), slot 60 the centre.  The integrand is
+// evaluated in ascending mu (order[]), which makes the two z(chi) lookups of a
+// thread monotone sweeps; the sums use the weight x P_l products per slot.
 template <typename T> struct PanelTables {
-    T mu1[30], mu2[30]; // mu at x = 0.5 - 0.5 xgk, x = 0.5 + 0.5 xgk
-    T wk[31];           // Kronrod weights; [30] = centre
-    T wg[30];           // Gauss weights (0 for Kronrod-only pairs)
-    T p1[MP_MAX_LDEG + 1][30], p2[MP_MAX_LDEG + 1][30], pc[MP_MAX_LDEG + 1];
+    T mu[61];                       // mu = 2x - 1 per slot
+    T wk[61];                       // Kronrod weight per slot
+    T wkP[MP_MAX_LDEG + 1][61];     // wk P_l(mu)
+    T wgP[MP_MAX_LDEG + 1][61];     // wg P_l(mu) (0 on Kronrod-only slots)
+    T wkA[MP_MAX_LDEG + 1][61];     // wk |P_l(mu)|
+    T Pl[MP_MAX_LDEG + 1][61];      // P_l(mu)
+    T mu_sorted[61];                // mu in ascending order
+    int order[61];                  // slot of the k-th smallest mu
 };
 __constant__ PanelTables<double> c_pt64;
 __constant__ PanelTables<float> c_pt32;
@@ -76,34 +85,46 @@ int upload_panel_tables(coffe_gpu_ctx *ctx)
     if (ctx->device < 64 && g_tables_uploaded[ctx->device]) return COFFE_GPU_OK;
     PanelTables<double> t64;
     PanelTables<float> t32;
+    // node positions and weights exactly as QUADPACK's qk61 forms them on [0, 1]
     const double center = 0.5, half_length = 0.5;
+    double wg[61];
     for (int p = 0; p < 30; ++p) {
         const int g = p < 15 ? 2 * p + 1 : 2 * (p - 15);
         const double absc = half_length * h_xgk[g];
-        const double x1 = center - absc, x2 = center + absc;
-        t64.mu1[p] = 2 * x1 - 1;
-        t64.mu2[p] = 2 * x2 - 1;
-        t64.wk[p] = h_wgk[g];
-        t64.wg[p] = p < 15 ? h_wg[p] : 0.0;
+        t64.mu[2 * p] = 2 * (center - absc) - 1;
+        t64.mu[2 * p + 1] = 2 * (center + absc) - 1;
+        t64.wk[2 * p] = t64.wk[2 * p + 1] = h_wgk[g];
+        wg[2 * p] = wg[2 * p + 1] = p < 15 ? h_wg[p] : 0.0;
+    }
+    t64.mu[60] = 2 * center - 1;
+    t64.wk[60] = h_wgk[30];
+    wg[60] = 0.0;
+    for (int sl = 0; sl < 61; ++sl)
         for (int l = 0; l <= MP_MAX_LDEG; ++l) {
-            t64.p1[l][p] = host_legendre(l, t64.mu1[p]);
-            t64.p2[l][p] = host_legendre(l, t64.mu2[p]);
+            const double P = host_legendre(l, t64.mu[sl]);
+            t64.Pl[l][sl] = P;
+            t64.wkP[l][sl] = t64.wk[sl] * P;
+            t64.wgP[l][sl] = wg[sl] * P;
+            t64.wkA[l][sl] = t64.wk[sl] * fabs(P);
+        }
+    std::vector<int> ord(61);
+    for (int i = 0; i < 61; ++i) ord[i] = i;
+    std::sort(ord.begin(), ord.end(), [&](int a, int b) { return t64.mu[a] < t64.mu[b]; });
+    for (int i = 0; i < 61; ++i) {
+        t64.order[i] = t32.order[i] = ord[i];
+        t64.mu_sorted[i] = t64.mu[ord[i]];
+    }
+    for (int sl = 0; sl < 61; ++sl) {
+        t32.mu[sl] = (float)t64.mu[sl];
+        t32.wk[sl] = (float)t64.wk[sl];
+        t32.mu_sorted[sl] = (float)t64.mu_sorted[sl];
+        for (int l = 0; l <= MP_MAX_LDEG; ++l) {
+            t32.Pl[l][sl] = (float)t64.Pl[l][sl];
+            t32.wkP[l][sl] = (float)t64.wkP[l][sl];
+            t32.wgP[l][sl] = (float)t64.wgP[l][sl];
+            t32.wkA[l][sl] = (float)t64.wkA[l][sl];
         }
     }
-    t64.wk[30] = h_wgk[30];
-    for (int l = 0; l <= MP_MAX_LDEG; ++l) t64.pc[l] = host_legendre(l, 2 * center - 1);
-    for (int p = 0; p < 30; ++p) {
-        t32.mu1[p] = (float)t64.mu1[p];
-        t32.mu2[p] = (float)t64.mu2[p];
-        t32.wk[p] = (float)t64.wk[p];
-        t32.wg[p] = (float)t64.wg[p];
-        for (int l = 0; l <= MP_MAX_LDEG; ++l) {
-            t32.p1[l][p] = (float)t64.p1[l][p];
-            t32.p2[l][p] = (float)t64.p2[l][p];
-        }
-    }
-    t32.wk[30] = (float)t64.wk[30];
-    for (int l = 0; l <= MP_MAX_LDEG; ++l) t32.pc[l] = (float)t64.pc[l];
     CG_CUDA(ctx, cudaMemcpyToSymbol(c_pt64, &t64, sizeof(t64)));
     CG_CUDA(ctx, cudaMemcpyToSymbol(c_pt32, &t32, sizeof(t32)));
     if (ctx->device < 64) g_tables_uploaded[ctx->device] = true;
@@ -162,6 +183,10 @@ template <typename T, typename S> struct Bg {
 // r^2 (1 - mu^2) / D, the reference's cos(theta)- and chi/r-expressions
 // become the polynomials below (identical algebra; the reference's I04
 // coefficient cancels two terms of size (chi/r)^4).
+// 1/x: IEEE division in double; the MUFU reciprocal (2 ulp) in the float path
+__device__ __forceinline__ double rcp_t(double x) { return 1.0 / x; }
+__device__ __forceinline__ float rcp_t(float x) { return __fdividef(1.0f, x); }
+
 template <typename T, typename S> struct Xi {
     Bg<T, S> bg;
     T chi_mean, sep, I00, I02, I04;
@@ -171,14 +196,18 @@ template <typename T, typename S> struct Xi {
     {
         const T chi1 = chi_mean - sep * mu * T(0.5);
         const T chi2 = chi_mean + sep * mu * T(0.5);
+        return combine(mu, chi1, chi2, spl_eval(bg.z_of_chi, chi1), spl_eval(bg.z_of_chi, chi2));
+    }
+
+    // xi from the two line-of-sight distances and their redshifts
+    __device__ __forceinline__ T combine(T mu, T chi1, T chi2, T z1, T z2) const
+    {
         const T mu2 = mu * mu;
         const T omm = T(1) - mu2;
         const T D = T(2) * chi_mean * chi_mean - mu2 * sep * sep * T(0.5);
-        const T inv_D = T(1) / D;
+        const T inv_D = rcp_t(D);
         const T s = sep * sep * omm * inv_D;
         const T c = T(1) - s;
-        const T z1 = spl_eval(bg.z_of_chi, chi1);
-        const T z2 = spl_eval(bg.z_of_chi, chi2);
         T f1, f2, g1, g2;
         bg.fD1(z1, f1, g1);
         bg.fD1(z2, f2, g2);
@@ -306,7 +335,63 @@ __device__ __forceinline__ Xi<T, S> make_xi(const MpArgs &a, const Bg<T, S> &bg,
 }
 
 // --------------------------------------------------------------- fast path
-template <typename T, typename S, typename TT>
+
+// A monotone cursor over the knots of the z(chi) spline: along the mu-sorted
+// node sweep chi1 = chi - r mu / 2 only decreases and chi2 = chi + r mu / 2
+// only increases, so each lookup moves the previous interval by a step or
+// two instead of searching.  The interval reached is the one a binary search
+// returns (x_i <= v < x_{i+1}).
+template <typename T> struct Cursor {
+    int i;
+    T xa, xb; // x_i, x_{i+1}
+};
+
+template <typename S>
+__device__ __forceinline__ Cursor<typename SplTraits<S>::T> cursor_at(const S &s,
+                                                                      typename SplTraits<S>::T v)
+{
+    Cursor<typename SplTraits<S>::T> c;
+    c.i = spl_interval(s, v);
+    c.xa = __ldg(s.x + c.i);
+    c.xb = __ldg(s.x + c.i + 1);
+    return c;
+}
+
+template <typename S>
+__device__ __forceinline__ typename SplTraits<S>::T cursor_up(const S &s,
+                                                              Cursor<typename SplTraits<S>::T> &c,
+                                                              typename SplTraits<S>::T v)
+{
+    typedef typename SplTraits<S>::T T;
+    while (c.i < s.n - 2 && c.xb <= v) {
+        ++c.i;
+        c.xa = c.xb;
+        c.xb = __ldg(s.x + c.i + 1);
+    }
+    if (!(v >= s.x0 && v <= s.xn)) return cg_nan<T>();
+    const T dx = v - c.xa;
+    const typename SplTraits<S>::C4 q = ldg_c4(s.c + c.i);
+    return q.x + dx * (q.y + dx * (q.z + q.w * dx));
+}
+
+template <typename S>
+__device__ __forceinline__ typename SplTraits<S>::T cursor_down(const S &s,
+                                                                Cursor<typename SplTraits<S>::T> &c,
+                                                                typename SplTraits<S>::T v)
+{
+    typedef typename SplTraits<S>::T T;
+    while (c.i > 0 && c.xa > v) {
+        --c.i;
+        c.xb = c.xa;
+        c.xa = __ldg(s.x + c.i);
+    }
+    if (!(v >= s.x0 && v <= s.xn)) return cg_nan<T>();
+    const T dx = v - c.xa;
+    const typename SplTraits<S>::C4 q = ldg_c4(s.c + c.i);
+    return q.x + dx * (q.y + dx * (q.z + q.w * dx));
+}
+
+template <int NL, typename T, typename S, typename TT>
 __global__ void __launch_bounds__(MP_LANE_THREADS)
     mp_lane_kernel(MpArgs a, Bg<T, S> bg, S chi_of_z, const TT *__restrict__ tab_x,
                    const TT *__restrict__ tab_y, const int *__restrict__ req_spectrum,
@@ -315,7 +400,7 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
                    int *__restrict__ retry_count, int2 *__restrict__ retry, int *err)
 {
     extern __shared__ __align__(16) unsigned char mp_smem[];
-    T *xs = reinterpret_cast<T *>(mp_smem); // [61][blockDim.x] integrand values
+    T *xs = reinterpret_cast<T *>(mp_smem); // [61 slots][blockDim.x] integrand values
     const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (item >= total) return;
     const int q = find_request(req_offset, a.n_req, item);
@@ -325,62 +410,74 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
     const Xi<T, S> xi = make_xi<T, S, TT>(a, bg, chi_of_z, tab_x, tab_y, s, zm, r);
     const PanelTables<T> &P = pt<T>();
     const int bd = blockDim.x, tid = threadIdx.x;
-    // integrand at the 61 nodes, QUADPACK order: centre, Gauss pairs, Kronrod pairs
-    const T fc = xi(T(0));
-    xs[60 * bd + tid] = fc;
-#pragma unroll 2
-    for (int p = 0; p < 30; ++p) {
-        xs[(2 * p) * bd + tid] = xi(P.mu1[p]);
-        xs[(2 * p + 1) * bd + tid] = xi(P.mu2[p]);
+    int ls[NL];
+    T K[NL], Kc[NL], G[NL], A[NL];
+#pragma unroll
+    for (int j = 0; j < NL; ++j) {
+        ls[j] = a.ls[j];
+        K[j] = Kc[j] = G[j] = A[j] = T(0);
     }
-    for (int li = 0; li < a.n_l; ++li) {
-        const int l = a.ls[li];
-        // Kronrod, Gauss and |f| sums
-        T K = fc * P.pc[l] * P.wk[30];
-        T Kc = T(0); // Kahan compensation (mixed path)
-        T G = T(0);
-        T A = fabs(K);
-        for (int p = 0; p < 30; ++p) {
-            const T f1 = xs[(2 * p) * bd + tid] * P.p1[l][p];
-            const T f2 = xs[(2 * p + 1) * bd + tid] * P.p2[l][p];
-            const T fs = f1 + f2;
-            G += P.wg[p] * fs;
-            const T term = P.wk[p] * fs;
-            if (sizeof(T) == 4) {
-                const T yk = term - Kc;
-                const T tk = K + yk;
-                Kc = (tk - K) - yk;
-                K = tk;
+    // integrand at the 61 nodes in ascending mu; Kronrod, Gauss and |f| sums
+    const T half_r = r * T(0.5);
+    Cursor<T> c1 = cursor_at(bg.z_of_chi, xi.chi_mean - P.mu_sorted[0] * half_r);
+    Cursor<T> c2 = cursor_at(bg.z_of_chi, xi.chi_mean + P.mu_sorted[0] * half_r);
+#pragma unroll 1
+    for (int k = 0; k < 61; ++k) {
+        const int slot = P.order[k];
+        const T mu = P.mu_sorted[k];
+        const T chi1 = xi.chi_mean - mu * half_r;
+        const T chi2 = xi.chi_mean + mu * half_r;
+        const T z1 = cursor_down(bg.z_of_chi, c1, chi1);
+        const T z2 = cursor_up(bg.z_of_chi, c2, chi2);
+        const T v = xi.combine(mu, chi1, chi2, z1, z2);
+        xs[slot * bd + tid] = v;
+        const T av = fabs(v);
+#pragma unroll
+        for (int j = 0; j < NL; ++j) {
+            const T term = P.wkP[ls[j]][slot] * v;
+            if (sizeof(T) == 4) { // Kahan-compensated float sum of the Kronrod estimate
+                const T yk = term - Kc[j];
+                const T tk = K[j] + yk;
+                Kc[j] = (tk - K[j]) - yk;
+                K[j] = tk;
             } else {
-                K += term;
+                K[j] += term;
             }
-            A += P.wk[p] * (fabs(f1) + fabs(f2));
+            G[j] += P.wgP[ls[j]][slot] * v;
+            A[j] += P.wkA[ls[j]][slot] * av;
         }
-        const T mean = K * T(0.5);
-        T asc = P.wk[30] * fabs(fc * P.pc[l] - mean);
-        for (int p = 0; p < 30; ++p) {
-            const T f1 = xs[(2 * p) * bd + tid] * P.p1[l][p];
-            const T f2 = xs[(2 * p + 1) * bd + tid] * P.p2[l][p];
-            asc += P.wk[p] * (fabs(f1 - mean) + fabs(f2 - mean));
-        }
+    }
+    T asc[NL];
+#pragma unroll
+    for (int j = 0; j < NL; ++j) asc[j] = T(0);
+#pragma unroll 1
+    for (int sl = 0; sl < 61; ++sl) {
+        const T v = xs[sl * bd + tid];
+        const T w = P.wk[sl];
+#pragma unroll
+        for (int j = 0; j < NL; ++j) asc[j] += w * fabs(v * P.Pl[ls[j]][sl] - K[j] * T(0.5));
+    }
+#pragma unroll
+    for (int j = 0; j < NL; ++j) {
+        const int l = ls[j];
         QkOut<T> o;
-        o.result = K * T(0.5);
-        o.resabs = A * T(0.5);
-        o.resasc = asc * T(0.5);
-        o.abserr = qk_rescale_error((K - G) * T(0.5), o.resabs, o.resasc);
+        o.result = K[j] * T(0.5);
+        o.resabs = A[j] * T(0.5);
+        o.resasc = asc[j] * T(0.5);
+        o.abserr = qk_rescale_error((K[j] - G[j]) * T(0.5), o.resabs, o.resasc);
         // QUADPACK's acceptance test of the first panel (gsl qag.c)
         const T tolerance = (T)a.epsrel * fabs(o.result);
-        const T round_off = T(50 * CG_DBL_EPS) * o.resabs;
+        const T round_off = T(50) * qk_eps<T>() * o.resabs;
         const bool roundoff_fail = o.abserr <= round_off && o.abserr > tolerance;
         const bool ok = (o.abserr <= tolerance && o.abserr != o.resasc) || o.abserr == T(0);
         if (ok || roundoff_fail) {
             const double res = (double)(T(2 * l + 1) * o.result);
             if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
-            out[item * a.n_l + li] = res;
+            out[item * NL + j] = res;
         } else {
             const int slot = atomicAdd(retry_count, 1);
             if (slot < a.retry_cap)
-                retry[slot] = make_int2((int)item, li);
+                retry[slot] = make_int2((int)item, j);
             else
                 cg_flag(err, CG_ERR_QAG_LIMIT);
         }
@@ -434,12 +531,31 @@ int launch(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S &chi
     int2 *d_retry = (int2 *)((char *)ctx->mp_retry.p + 256);
     CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
     const size_t smem = sizeof(T) * 61 * MP_LANE_THREADS;
-    CG_CUDA(ctx, cudaFuncSetAttribute(mp_lane_kernel<T, S, TT>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long blocks = (total + MP_LANE_THREADS - 1) / MP_LANE_THREADS;
-    mp_lane_kernel<T, S, TT><<<(unsigned)blocks, MP_LANE_THREADS, smem, ctx->stream>>>(
-        a, bg, chi_of_z, tab_x, tab_y, req_spectrum, req_z_mean, req_offset, sep, total, out,
-        d_count, d_retry, ctx->d_err);
+#define MP_LAUNCH_NL(NLV)                                                                        \
+    case NLV: {                                                                                  \
+        CG_CUDA(ctx, cudaFuncSetAttribute(mp_lane_kernel<NLV, T, S, TT>,                        \
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,           \
+                                          (int)smem));                                           \
+        mp_lane_kernel<NLV, T, S, TT><<<(unsigned)blocks, MP_LANE_THREADS, smem, ctx->stream>>>( \
+            a, bg, chi_of_z, tab_x, tab_y, req_spectrum, req_z_mean, req_offset, sep, total,    \
+            out, d_count, d_retry, ctx->d_err);                                                  \
+        break;                                                                                   \
+    }
+    switch (a.n_l) {
+        MP_LAUNCH_NL(1)
+        MP_LAUNCH_NL(2)
+        MP_LAUNCH_NL(3)
+        MP_LAUNCH_NL(4)
+        MP_LAUNCH_NL(5)
+        MP_LAUNCH_NL(6)
+        MP_LAUNCH_NL(7)
+        MP_LAUNCH_NL(8)
+    default:
+        cg_set_error(ctx, "multipoles: unsupported number of multipoles %d", a.n_l);
+        return COFFE_GPU_EINVAL;
+    }
+#undef MP_LAUNCH_NL
     int st = cg_after_launch(ctx, "mp_lane_kernel");
     if (st) return st;
     mp_retry_kernel<T, S, TT><<<ctx->sm_count * 2, 32 * MP_RETRY_WARPS, 0, ctx->stream>>>(

@@ -43,6 +43,13 @@ template <typename T> __device__ __forceinline__ T qk_tiny();
 template <> __device__ __forceinline__ double qk_tiny<double>() { return CG_DBL_MIN / (50 * CG_DBL_EPS); }
 template <> __device__ __forceinline__ float qk_tiny<float>() { return 0.0f; }
 
+// unit round-off of the working precision: QUADPACK's round-off floor
+// (50 eps |f|) and its round-off exit use it, so the float path stops where
+// float arithmetic stops resolving the error, as the double path does at DBL_EPSILON
+template <typename T> __device__ __forceinline__ T qk_eps();
+template <> __device__ __forceinline__ double qk_eps<double>() { return CG_DBL_EPS; }
+template <> __device__ __forceinline__ float qk_eps<float>() { return 1.1920928955078125e-07f; }
+
 template <typename T> __device__ __forceinline__ T qk_rescale_error(T err, T result_abs, T result_asc)
 {
     err = fabs(err);
@@ -51,7 +58,7 @@ template <typename T> __device__ __forceinline__ T qk_rescale_error(T err, T res
         err = scale < T(1) ? result_asc * scale : result_asc;
     }
     if (result_abs > qk_tiny<T>()) {
-        const T min_err = T(50 * CG_DBL_EPS) * result_abs;
+        const T min_err = T(50) * qk_eps<T>() * result_abs;
         if (min_err > err) err = min_err;
     }
     return err;
@@ -147,7 +154,7 @@ __device__ T qag_continue(const F &f, const GkLane<T> &g, T a, T b, QkOut<T> p0,
 {
     const int lane = threadIdx.x & 31;
     T tolerance = fmax(epsabs, epsrel * fabs(p0.result));
-    const T round_off = T(50 * CG_DBL_EPS) * p0.resabs;
+    const T round_off = T(50) * qk_eps<T>() * p0.resabs;
     *status = 0;
     if (p0.abserr <= round_off && p0.abserr > tolerance) {
         *status = 2;

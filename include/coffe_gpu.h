@@ -191,6 +191,12 @@ int coffe_gpu_multipoles_async(coffe_gpu_ctx_t *ctx, int contrib, int precision,
                                const int64_t *req_offset, const double *sep, int n_l,
                                const int *l, double *out);
 
+/* Number of (separation, multipole) outputs of the last multipoles call on
+   this context whose first GK61 panel missed the tolerance and went through
+   the adaptive bisection (synchronises the context's stream); -1 if none ran.
+   No counterpart in the reference (its QAG keeps this count internal). */
+long long coffe_gpu_multipoles_retries(coffe_gpu_ctx_t *ctx);
+
 /* Kernel launches issued by this context since creation (for accounting). */
 long long coffe_gpu_launch_count(const coffe_gpu_ctx_t *ctx);
 
