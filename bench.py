@@ -58,8 +58,10 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-clocks", action="store_true")
-    p.add_argument("--kernel-only", choices=["mixed", "fp64"], default=None,
-                   help="run only the timed multipole kernel loop (profiling)")
+    p.add_argument("--kernel-only", choices=["mixed", "fp64", "tables-mixed", "tables-fp64"],
+                   default=None,
+                   help="profiling aid: run only the multipole kernel (mixed/fp64) or only the "
+                        "FFTLog tables (tables-*) `steps` times")
     return p.parse_args()
 
 
@@ -267,11 +269,15 @@ def ours(args, rank, world, local_rank):
         return dev_s, wall, ctx.launch_count() - l0
 
     if args.kernel_only:
-        # profiling aid: only the multipole kernel of one precision, tables built once
-        prec = args.kernel_only
+        # profiling aid: only one stage of one precision
+        prec = args.kernel_only.split("-")[-1]
         ctx.integrals_init_device(batch.k, pk_d, TERMS, N=N_FFT, precision=prec, sync=True)
         for _ in range(args.steps):
-            ctx.multipoles_async(rs_d, rz_d, ro_d, sep_d, n_sep, batch.ls, outs[prec], precision=prec)
+            if args.kernel_only.startswith("tables"):
+                ctx.integrals_init_device(batch.k, pk_d, TERMS, N=N_FFT, precision=prec, sync=False)
+            else:
+                ctx.multipoles_async(rs_d, rz_d, ro_d, sep_d, n_sep, batch.ls, outs[prec],
+                                     precision=prec)
         ctx.synchronize()
         return
 

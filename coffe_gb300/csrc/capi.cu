@@ -139,7 +139,7 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
                       &ctx->qfac,     &ctx->modec,  &ctx->postf,   &ctx->twid,   &ctx->twid32,
                       &ctx->spec,     &ctx->req_buf, &ctx->term_meta, &ctx->zrec64,
                       &ctx->zrec32,   &ctx->mp_retry, &ctx->term_df,
-                      &ctx->samp_f32, &ctx->csfac32};
+                      &ctx->samp_f32, &ctx->csfac32, &ctx->mp_nodes};
     for (DevBuf *b : bufs) cg_release(*b);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->h_err) cudaFreeHost(ctx->h_err);

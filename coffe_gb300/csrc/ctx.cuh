@@ -81,6 +81,9 @@ struct coffe_gpu_ctx {
     // ---- multipole request staging (host-pointer calls) and retry list
     DevBuf req_buf;
     DevBuf mp_retry;
+    DevBuf mp_nodes; // first-panel node table of the last multipole list
+    int mp_nodes_nl = 0, mp_nodes_prec = -1;
+    int mp_nodes_ls[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 void cg_set_error(coffe_gpu_ctx *ctx, const char *fmt, ...);

@@ -53,13 +53,6 @@ template <typename T> struct PanelTables {
     T mu_sorted[61];                // mu in ascending order
     int order[61];                  // slot of the k-th smallest mu
 };
-__constant__ PanelTables<double> c_pt64;
-__constant__ PanelTables<float> c_pt32;
-
-template <typename T> __device__ __forceinline__ const PanelTables<T> &pt();
-template <> __device__ __forceinline__ const PanelTables<double> &pt<double>() { return c_pt64; }
-template <> __device__ __forceinline__ const PanelTables<float> &pt<float>() { return c_pt32; }
-
 // P_l(x) by the upward recurrence (gsl_sf_legendre_Pl), host side
 double host_legendre(int l, double x)
 {
@@ -78,13 +71,12 @@ const double h_xgk[31] = CG_GK61_XGK_INIT;
 const double h_wgk[31] = CG_GK61_WGK_INIT;
 const double h_wg[15] = CG_GK61_WG_INIT;
 
-bool g_tables_uploaded[64] = {false};
-
-int upload_panel_tables(coffe_gpu_ctx *ctx)
+// first-panel tables in FP64, built once on the host
+const PanelTables<double> &panel_tables()
 {
-    if (ctx->device < 64 && g_tables_uploaded[ctx->device]) return COFFE_GPU_OK;
-    PanelTables<double> t64;
-    PanelTables<float> t32;
+    static PanelTables<double> t64;
+    static bool built = false;
+    if (built) return t64;
     // node positions and weights exactly as QUADPACK's qk61 forms them on [0, 1]
     const double center = 0.5, half_length = 0.5;
     double wg[61];
@@ -111,24 +103,36 @@ int upload_panel_tables(coffe_gpu_ctx *ctx)
     for (int i = 0; i < 61; ++i) ord[i] = i;
     std::sort(ord.begin(), ord.end(), [&](int a, int b) { return t64.mu[a] < t64.mu[b]; });
     for (int i = 0; i < 61; ++i) {
-        t64.order[i] = t32.order[i] = ord[i];
+        t64.order[i] = ord[i];
         t64.mu_sorted[i] = t64.mu[ord[i]];
     }
-    for (int sl = 0; sl < 61; ++sl) {
-        t32.mu[sl] = (float)t64.mu[sl];
-        t32.wk[sl] = (float)t64.wk[sl];
-        t32.mu_sorted[sl] = (float)t64.mu_sorted[sl];
-        for (int l = 0; l <= MP_MAX_LDEG; ++l) {
-            t32.Pl[l][sl] = (float)t64.Pl[l][sl];
-            t32.wkP[l][sl] = (float)t64.wkP[l][sl];
-            t32.wgP[l][sl] = (float)t64.wgP[l][sl];
-            t32.wkA[l][sl] = (float)t64.wkA[l][sl];
+    built = true;
+    return t64;
+}
+
+// The node table of one launch (layout NodeLayout<NL>), in T, for multipoles ls[0..NL)
+template <typename T>
+void build_node_table(int NL, const int *ls, std::vector<T> &out)
+{
+    const PanelTables<double> &P = panel_tables();
+    const int R1 = ((2 + 3 * NL) + 3) / 4 * 4, R2 = ((1 + NL) + 3) / 4 * 4;
+    out.assign((size_t)61 * (R1 + R2), T(0));
+    for (int k = 0; k < 61; ++k) {
+        const int sl = P.order[k];
+        T *r = out.data() + (size_t)k * R1;
+        r[0] = (T)P.mu_sorted[k];
+        r[1] = (T)sl;
+        for (int j = 0; j < NL; ++j) {
+            r[2 + j] = (T)P.wkP[ls[j]][sl];
+            r[2 + NL + j] = (T)P.wgP[ls[j]][sl];
+            r[2 + 2 * NL + j] = (T)P.wkA[ls[j]][sl];
         }
     }
-    CG_CUDA(ctx, cudaMemcpyToSymbol(c_pt64, &t64, sizeof(t64)));
-    CG_CUDA(ctx, cudaMemcpyToSymbol(c_pt32, &t32, sizeof(t32)));
-    if (ctx->device < 64) g_tables_uploaded[ctx->device] = true;
-    return COFFE_GPU_OK;
+    for (int sl = 0; sl < 61; ++sl) {
+        T *r = out.data() + (size_t)61 * R1 + (size_t)sl * R2;
+        r[0] = (T)P.wk[sl];
+        for (int j = 0; j < NL; ++j) r[1 + j] = (T)P.Pl[ls[j]][sl];
+    }
 }
 
 // ------------------------------------------------------ background access
@@ -340,7 +344,8 @@ __device__ __forceinline__ Xi<T, S> make_xi(const MpArgs &a, const Bg<T, S> &bg,
 // node sweep chi1 = chi - r mu / 2 only decreases and chi2 = chi + r mu / 2
 // only increases, so each lookup moves the previous interval by a step or
 // two instead of searching.  The interval reached is the one a binary search
-// returns (x_i <= v < x_{i+1}).
+// returns (x_i <= v < x_{i+1}).  Range checks are done once per pair by the
+// caller (the sweep stays inside [chi - r mu_max / 2, chi + r mu_max / 2]).
 template <typename T> struct Cursor {
     int i;
     T xa, xb; // x_i, x_{i+1}
@@ -368,7 +373,6 @@ __device__ __forceinline__ typename SplTraits<S>::T cursor_up(const S &s,
         c.xa = c.xb;
         c.xb = __ldg(s.x + c.i + 1);
     }
-    if (!(v >= s.x0 && v <= s.xn)) return cg_nan<T>();
     const T dx = v - c.xa;
     const typename SplTraits<S>::C4 q = ldg_c4(s.c + c.i);
     return q.x + dx * (q.y + dx * (q.z + q.w * dx));
@@ -385,10 +389,41 @@ __device__ __forceinline__ typename SplTraits<S>::T cursor_down(const S &s,
         c.xb = c.xa;
         c.xa = __ldg(s.x + c.i);
     }
-    if (!(v >= s.x0 && v <= s.xn)) return cg_nan<T>();
     const T dx = v - c.xa;
     const typename SplTraits<S>::C4 q = ldg_c4(s.c + c.i);
     return q.x + dx * (q.y + dx * (q.z + q.w * dx));
+}
+
+// Per-launch node table for the requested multipoles (NL of them), staged in
+// shared memory so every node reads its constants as broadcast vector loads:
+//   pass-1 record k (ascending mu): mu, slot, wk P_l, wg P_l, wk |P_l| per l;
+//   pass-2 record per slot: wk, P_l per l.
+template <int NL> struct NodeLayout {
+    static constexpr int R1 = ((2 + 3 * NL) + 3) / 4 * 4;
+    static constexpr int R2 = ((1 + NL) + 3) / 4 * 4;
+    static constexpr int COUNT = 61 * (R1 + R2);
+};
+
+template <typename T, int R> __device__ __forceinline__ void lds_rec(const T *p, T (&r)[R]);
+template <int R> __device__ __forceinline__ void lds_rec(const float *p, float (&r)[R])
+{
+#pragma unroll
+    for (int i = 0; i < R / 4; ++i) {
+        const float4 v = reinterpret_cast<const float4 *>(p)[i];
+        r[4 * i] = v.x;
+        r[4 * i + 1] = v.y;
+        r[4 * i + 2] = v.z;
+        r[4 * i + 3] = v.w;
+    }
+}
+template <int R> __device__ __forceinline__ void lds_rec(const double *p, double (&r)[R])
+{
+#pragma unroll
+    for (int i = 0; i < R / 2; ++i) {
+        const double2 v = reinterpret_cast<const double2 *>(p)[i];
+        r[2 * i] = v.x;
+        r[2 * i + 1] = v.y;
+    }
 }
 
 template <int NL, typename T, typename S, typename TT>
@@ -396,11 +431,17 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
     mp_lane_kernel(MpArgs a, Bg<T, S> bg, S chi_of_z, const TT *__restrict__ tab_x,
                    const TT *__restrict__ tab_y, const int *__restrict__ req_spectrum,
                    const double *__restrict__ req_z_mean, const int64_t *__restrict__ req_offset,
-                   const double *__restrict__ sep, long long total, double *__restrict__ out,
+                   const double *__restrict__ sep, long long total,
+                   const T *__restrict__ nodes, double *__restrict__ out,
                    int *__restrict__ retry_count, int2 *__restrict__ retry, int *err)
 {
+    typedef NodeLayout<NL> LY;
     extern __shared__ __align__(16) unsigned char mp_smem[];
-    T *xs = reinterpret_cast<T *>(mp_smem); // [61 slots][blockDim.x] integrand values
+    T *tab1 = reinterpret_cast<T *>(mp_smem);  // [61][R1]
+    T *tab2 = tab1 + 61 * LY::R1;               // [61][R2]
+    T *xs = tab2 + 61 * LY::R2;                 // [61 slots][blockDim.x] integrand values
+    for (int i = threadIdx.x; i < LY::COUNT; i += blockDim.x) tab1[i] = nodes[i];
+    __syncthreads();
     const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (item >= total) return;
     const int q = find_request(req_offset, a.n_req, item);
@@ -408,58 +449,66 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
     const T r = (T)sep[item];
     const T zm = (T)req_z_mean[q];
     const Xi<T, S> xi = make_xi<T, S, TT>(a, bg, chi_of_z, tab_x, tab_y, s, zm, r);
-    const PanelTables<T> &P = pt<T>();
     const int bd = blockDim.x, tid = threadIdx.x;
-    int ls[NL];
     T K[NL], Kc[NL], G[NL], A[NL];
 #pragma unroll
-    for (int j = 0; j < NL; ++j) {
-        ls[j] = a.ls[j];
-        K[j] = Kc[j] = G[j] = A[j] = T(0);
-    }
-    // integrand at the 61 nodes in ascending mu; Kronrod, Gauss and |f| sums
+    for (int j = 0; j < NL; ++j) K[j] = Kc[j] = G[j] = A[j] = T(0);
     const T half_r = r * T(0.5);
-    Cursor<T> c1 = cursor_at(bg.z_of_chi, xi.chi_mean - P.mu_sorted[0] * half_r);
-    Cursor<T> c2 = cursor_at(bg.z_of_chi, xi.chi_mean + P.mu_sorted[0] * half_r);
+    // the sweep covers chi -+ r mu_max / 2: outside the chi knots every node of
+    // the reference's integrand is NaN, so the whole pair is
+    const T mu0 = tab1[0];
+    const T span = fabs(mu0) * half_r;
+    const bool inside = (xi.chi_mean - span >= bg.z_of_chi.x0) && (xi.chi_mean + span <= bg.z_of_chi.xn);
+    bool finite = inside && isfinite(xi.I00) && isfinite(xi.I02) && isfinite(xi.I04);
+    if (inside) {
+        Cursor<T> c1 = cursor_at(bg.z_of_chi, xi.chi_mean - mu0 * half_r);
+        Cursor<T> c2 = cursor_at(bg.z_of_chi, xi.chi_mean + mu0 * half_r);
+        // integrand at the 61 nodes in ascending mu; Kronrod, Gauss and |f| sums
 #pragma unroll 1
-    for (int k = 0; k < 61; ++k) {
-        const int slot = P.order[k];
-        const T mu = P.mu_sorted[k];
-        const T chi1 = xi.chi_mean - mu * half_r;
-        const T chi2 = xi.chi_mean + mu * half_r;
-        const T z1 = cursor_down(bg.z_of_chi, c1, chi1);
-        const T z2 = cursor_up(bg.z_of_chi, c2, chi2);
-        const T v = xi.combine(mu, chi1, chi2, z1, z2);
-        xs[slot * bd + tid] = v;
-        const T av = fabs(v);
+        for (int k = 0; k < 61; ++k) {
+            T rec[LY::R1];
+            lds_rec<LY::R1>(tab1 + k * LY::R1, rec);
+            const T mu = rec[0];
+            const int slot = (int)rec[1];
+            const T chi1 = xi.chi_mean - mu * half_r;
+            const T chi2 = xi.chi_mean + mu * half_r;
+            const T z1 = cursor_down(bg.z_of_chi, c1, chi1);
+            const T z2 = cursor_up(bg.z_of_chi, c2, chi2);
+            const T v = xi.combine(mu, chi1, chi2, z1, z2);
+            xs[slot * bd + tid] = v;
+            const T av = fabs(v);
 #pragma unroll
-        for (int j = 0; j < NL; ++j) {
-            const T term = P.wkP[ls[j]][slot] * v;
-            if (sizeof(T) == 4) { // Kahan-compensated float sum of the Kronrod estimate
-                const T yk = term - Kc[j];
-                const T tk = K[j] + yk;
-                Kc[j] = (tk - K[j]) - yk;
-                K[j] = tk;
-            } else {
-                K[j] += term;
+            for (int j = 0; j < NL; ++j) {
+                const T term = rec[2 + j] * v;
+                if (sizeof(T) == 4) { // Kahan-compensated float sum of the Kronrod estimate
+                    const T yk = term - Kc[j];
+                    const T tk = K[j] + yk;
+                    Kc[j] = (tk - K[j]) - yk;
+                    K[j] = tk;
+                } else {
+                    K[j] += term;
+                }
+                G[j] += rec[2 + NL + j] * v;
+                A[j] += rec[2 + 2 * NL + j] * av;
             }
-            G[j] += P.wgP[ls[j]][slot] * v;
-            A[j] += P.wkA[ls[j]][slot] * av;
         }
     }
     T asc[NL];
 #pragma unroll
     for (int j = 0; j < NL; ++j) asc[j] = T(0);
+    if (inside) {
 #pragma unroll 1
-    for (int sl = 0; sl < 61; ++sl) {
-        const T v = xs[sl * bd + tid];
-        const T w = P.wk[sl];
+        for (int sl = 0; sl < 61; ++sl) {
+            T rec[LY::R2];
+            lds_rec<LY::R2>(tab2 + sl * LY::R2, rec);
+            const T v = xs[sl * bd + tid];
 #pragma unroll
-        for (int j = 0; j < NL; ++j) asc[j] += w * fabs(v * P.Pl[ls[j]][sl] - K[j] * T(0.5));
+            for (int j = 0; j < NL; ++j) asc[j] += rec[0] * fabs(v * rec[1 + j] - K[j] * T(0.5));
+        }
     }
 #pragma unroll
     for (int j = 0; j < NL; ++j) {
-        const int l = ls[j];
+        const int l = a.ls[j];
         QkOut<T> o;
         o.result = K[j] * T(0.5);
         o.resabs = A[j] * T(0.5);
@@ -470,7 +519,10 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
         const T round_off = T(50) * qk_eps<T>() * o.resabs;
         const bool roundoff_fail = o.abserr <= round_off && o.abserr > tolerance;
         const bool ok = (o.abserr <= tolerance && o.abserr != o.resasc) || o.abserr == T(0);
-        if (ok || roundoff_fail) {
+        if (!finite) {
+            cg_flag(err, CG_ERR_NONFINITE);
+            out[item * NL + j] = cg_nan<double>();
+        } else if (ok || roundoff_fail) {
             const double res = (double)(T(2 * l + 1) * o.result);
             if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
             out[item * NL + j] = res;
@@ -530,16 +582,33 @@ int launch(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S &chi
     int *d_count = (int *)ctx->mp_retry.p;
     int2 *d_retry = (int2 *)((char *)ctx->mp_retry.p + 256);
     CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
-    const size_t smem = sizeof(T) * 61 * MP_LANE_THREADS;
+    // node table of these multipoles (rebuilt only when the l list or precision changes)
+    const int prec_tag = sizeof(T) == 8 ? COFFE_GPU_FP64 : COFFE_GPU_MIXED;
+    bool same = ctx->mp_nodes_nl == a.n_l && ctx->mp_nodes_prec == prec_tag;
+    for (int j = 0; same && j < a.n_l; ++j) same = ctx->mp_nodes_ls[j] == a.ls[j];
+    if (!same) {
+        std::vector<T> tab;
+        build_node_table<T>(a.n_l, a.ls, tab);
+        int st0 = cg_ensure(ctx, ctx->mp_nodes, sizeof(T) * tab.size());
+        if (st0) return st0;
+        CG_CUDA(ctx, cudaMemcpyAsync(ctx->mp_nodes.p, tab.data(), sizeof(T) * tab.size(),
+                                     cudaMemcpyHostToDevice, ctx->stream));
+        CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream)); // tab is a host temporary
+        ctx->mp_nodes_nl = a.n_l;
+        ctx->mp_nodes_prec = prec_tag;
+        for (int j = 0; j < a.n_l; ++j) ctx->mp_nodes_ls[j] = a.ls[j];
+    }
+    const T *d_nodes = (const T *)ctx->mp_nodes.p;
     const long long blocks = (total + MP_LANE_THREADS - 1) / MP_LANE_THREADS;
 #define MP_LAUNCH_NL(NLV)                                                                        \
     case NLV: {                                                                                  \
+        const size_t smem = sizeof(T) * (NodeLayout<NLV>::COUNT + 61 * MP_LANE_THREADS);         \
         CG_CUDA(ctx, cudaFuncSetAttribute(mp_lane_kernel<NLV, T, S, TT>,                        \
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,           \
                                           (int)smem));                                           \
         mp_lane_kernel<NLV, T, S, TT><<<(unsigned)blocks, MP_LANE_THREADS, smem, ctx->stream>>>( \
             a, bg, chi_of_z, tab_x, tab_y, req_spectrum, req_z_mean, req_offset, sep, total,    \
-            out, d_count, d_retry, ctx->d_err);                                                  \
+            d_nodes, out, d_count, d_retry, ctx->d_err);                                         \
         break;                                                                                   \
     }
     switch (a.n_l) {
@@ -668,8 +737,7 @@ int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel
         a.ls[i] = l[i];
     }
     if (total <= 0) return COFFE_GPU_OK;
-    int st = upload_panel_tables(ctx);
-    if (st) return st;
+    int st;
     if (ctx->sm_count <= 0)
         CG_CUDA(ctx, cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount,
                                             ctx->device));

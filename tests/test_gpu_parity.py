@@ -108,9 +108,10 @@ def test_integral_tables_mixed_close_to_oracle(gpu_ctx, oracle, cfg1):
         mask = (ox >= 5 / H) & (ox <= 300 / H)
         mask[:43] = False
         assert np.isnan(gy[:43]).all()  # not requested
-        # double-float FFT, tables stored as float: float rounding dominates
+        # double-float FFT, tables stored as float; the float spline-curvature
+        # correction of the resampled P(k) adds ~1e-6 near the zero crossings
         e = table_err(gy, oy, mask, floor=1e-6)
-        assert e < 1e-6, ((n, l), e)
+        assert e < 1e-5, ((n, l), e)
 
 
 def test_all_bessel_integrals_2e14_fp64(gpu_ctx, oracle, w):
