@@ -29,6 +29,7 @@ LEN = 4
 SMALL_R = 1
 PK_DEVICE = 2
 ASYNC = 4
+NOALLOC_MAX_OUTPUTS = 1048576
 
 # every symbol include/coffe_gpu.h declares
 EXPORTS = (
@@ -48,6 +49,7 @@ EXPORTS = (
     "coffe_gpu_integral_eval",
     "coffe_gpu_multipoles",
     "coffe_gpu_multipoles_async",
+    "coffe_gpu_multipoles_noalloc",
     "coffe_gpu_multipoles_retries",
     "coffe_gpu_launch_count",
 )
@@ -115,6 +117,8 @@ def load(build_if_missing: bool = True):
                                        _dp, C.c_int, _ip, _dp, C.c_int]
     L.coffe_gpu_multipoles_async.argtypes = [_p, C.c_int, C.c_int, C.c_double, C.c_int,
                                              C.c_int64, _ip, _dp, _lp, _dp, C.c_int, _ip, _dp]
+    L.coffe_gpu_multipoles_noalloc.argtypes = [_p, C.c_int, C.c_int, C.c_double, C.c_int,
+                                               C.c_int64, _ip, _dp, _lp, _dp, C.c_int, _ip, _dp]
     L.coffe_gpu_multipoles_retries.argtypes = [_p]
     L.coffe_gpu_multipoles_retries.restype = C.c_longlong
     L.coffe_gpu_launch_count.argtypes = [_p]

@@ -231,6 +231,23 @@ class Context:
             P(req_z_mean, C.c_double), P(req_offset, C.c_int64), P(sep, C.c_double), len(la),
             _iptr(la), P(out, C.c_double)), "multipoles_async")
 
+    def multipoles_noalloc(self, req_spectrum, req_z_mean, req_offset, sep, n_sep: int, ls, out,
+                           contrib=_lib.DEN | _lib.RSD, precision="fp64", epsrel=1e-5):
+        """:meth:`multipoles_async` without any device allocation by the library:
+        scratch comes from a fixed array of the library (at most
+        ``NOALLOC_MAX_OUTPUTS`` = n_sep * len(ls) outputs per call).  For callers
+        whose device memory is all pooled up front, or who cannot have
+        cudaMalloc/cudaFree stall the device mid-run.  Calls on one device share
+        that array: serialise them (one stream).  Make the first call on a device
+        before any stream capture; it resolves the array's address."""
+        P = lambda t, ty: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ty))
+        la = np.ascontiguousarray(ls, dtype=np.int32)
+        self._check(self._L.coffe_gpu_multipoles_noalloc(
+            self._ctx, int(contrib), _precision(precision), float(epsrel),
+            int(req_spectrum.numel()), int(n_sep), P(req_spectrum, C.c_int),
+            P(req_z_mean, C.c_double), P(req_offset, C.c_int64), P(sep, C.c_double), len(la),
+            _iptr(la), P(out, C.c_double)), "multipoles_noalloc")
+
     def multipoles_device(self, req_spectrum, req_z_mean, req_offset, sep, ls, out,
                           contrib=_lib.DEN | _lib.RSD, precision="fp64", epsrel=1e-5):
         """Same as :meth:`multipoles` with CUDA tensors (int32, float64, int64,

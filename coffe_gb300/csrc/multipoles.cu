@@ -24,6 +24,7 @@
 // algorithm with float splines, integrand and Legendre values, and a
 // Kahan-compensated float sum for the panel result.
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "ctx.cuh"
@@ -781,4 +782,294 @@ int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel
                                          (const double *)ctx->tab_x.p,
                                          (const double *)ctx->tab_y.p, req_spectrum, req_z_mean,
                                          req_offset, sep, total, out);
+}
+
+// ============================================================================
+// coffe_gpu_multipoles_noalloc: the multipole kernels above with every byte of
+// their scratch taken from one fixed array in the library's device memory.
+//
+// Some callers cannot let the library allocate while they run: a process that
+// hands all device memory to a pool at start-up (PyTorch's caching allocator, a
+// service reserving its HBM) could see a growing buffer fail mid-run, and
+// cudaMalloc/cudaFree synchronise the whole device, stalling every other
+// stream.  multipoles_run grows its retry list and node table on demand; this
+// variant never calls cudaMalloc, cudaFree or any allocating routine.
+//
+// Scratch layout (noalloc_scratch, 256-byte aligned):
+//   [0, 256)                    retry counter (int) -- must start at zero, so
+//                               every call clears it on its stream first;
+//   [256, 256 + 20480)          first-panel node table, rewritten every call
+//                               by mp_node_table_kernel;
+//   [20736, + 8 * max outputs)  retry list, one int2 per (separation, l).
+// One array serves every call on a device, so calls whose work overlaps in
+// time race on it; callers serialise them (one stream does).
+// ============================================================================
+namespace {
+
+#define MP_NOALLOC_NODE_BYTES 20480
+#define MP_NOALLOC_LIST_OFFSET (256 + MP_NOALLOC_NODE_BYTES)
+#define MP_NOALLOC_BYTES \
+    (MP_NOALLOC_LIST_OFFSET + sizeof(int2) * (size_t)COFFE_GPU_NOALLOC_MAX_OUTPUTS)
+#define MP_NOALLOC_MAX_DEVICES 64
+static_assert(sizeof(double) * NodeLayout<MP_MAX_L>::COUNT <= MP_NOALLOC_NODE_BYTES,
+              "node table of the largest multipole list must fit the scratch slot");
+static_assert(MP_NOALLOC_LIST_OFFSET % 256 == 0, "retry list alignment");
+
+static __device__ __align__(256) unsigned char noalloc_scratch[MP_NOALLOC_BYTES];
+
+// device address of noalloc_scratch per device, resolved once per device
+std::mutex noalloc_mutex;
+unsigned char *noalloc_addr[MP_NOALLOC_MAX_DEVICES];
+
+// Looks up (first call on the device) or returns the scratch address for
+// ctx->device, which the caller has made current.
+int noalloc_scratch_address(coffe_gpu_ctx *ctx, unsigned char **addr)
+{
+    if (ctx->device < 0 || ctx->device >= MP_NOALLOC_MAX_DEVICES) {
+        cg_set_error(ctx, "multipoles_noalloc: device %d beyond the %d supported", ctx->device,
+                     MP_NOALLOC_MAX_DEVICES);
+        return COFFE_GPU_EINVAL;
+    }
+    std::lock_guard<std::mutex> lock(noalloc_mutex);
+    if (!noalloc_addr[ctx->device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cg_set_error(ctx, "multipoles_noalloc: cannot resolve the scratch array on device %d: %s",
+                         ctx->device, cudaGetErrorString(e));
+            return COFFE_GPU_ECUDA;
+        }
+        noalloc_addr[ctx->device] = (unsigned char *)p;
+    }
+    *addr = noalloc_addr[ctx->device];
+    return COFFE_GPU_OK;
+}
+
+// P_l(x) by the upward recurrence, as host_legendre forms it
+__device__ double node_legendre(int l, double x)
+{
+    if (l == 0) return 1.0;
+    if (l == 1) return x;
+    double p0 = 1.0, p1 = x;
+    for (int k = 2; k <= l; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / (double)k;
+        p0 = p1;
+        p1 = p2;
+    }
+    return p1;
+}
+
+// The node table of build_node_table (layout NodeLayout<a.n_l>), computed on
+// the device so that no host staging buffer is needed: thread sl owns slot sl,
+// finds its rank in ascending mu and writes its pass-1 and pass-2 records.
+template <typename T> __global__ void __launch_bounds__(64) mp_node_table_kernel(MpArgs a, T *out)
+{
+    __shared__ double mus[64];
+    const int sl = threadIdx.x;
+    double mu = 0.0, wk = 0.0, wg = 0.0;
+    if (sl < 60) { // slots 2p, 2p+1: x = 0.5 -+ 0.5 xgk[g_p]
+        const int p = sl >> 1;
+        const int g = p < 15 ? 2 * p + 1 : 2 * (p - 15);
+        const double absc = 0.5 * cg_gk_xgk[g];
+        mu = (sl & 1) ? 2.0 * (0.5 + absc) - 1.0 : 2.0 * (0.5 - absc) - 1.0;
+        wk = cg_gk_wgk[g];
+        wg = p < 15 ? cg_gk_wg[p] : 0.0;
+    } else if (sl == 60) { // centre
+        wk = cg_gk_wgk[30];
+    }
+    mus[sl] = sl < 61 ? mu : 2.0;
+    __syncthreads();
+    if (sl >= 61) return;
+    int rank = 0;
+    for (int i = 0; i < 61; ++i) rank += (mus[i] < mu) || (mus[i] == mu && i < sl);
+    const int NL = a.n_l;
+    const int R1 = ((2 + 3 * NL) + 3) / 4 * 4, R2 = ((1 + NL) + 3) / 4 * 4;
+    T *r1 = out + (size_t)rank * R1;
+    T *r2 = out + (size_t)61 * R1 + (size_t)sl * R2;
+    for (int i = 0; i < R1; ++i) r1[i] = T(0);
+    for (int i = 0; i < R2; ++i) r2[i] = T(0);
+    r1[0] = (T)mu;
+    r1[1] = (T)sl;
+    r2[0] = (T)wk;
+    for (int j = 0; j < NL; ++j) {
+        const double P = node_legendre(a.ls[j], mu);
+        r1[2 + j] = (T)(wk * P);
+        r1[2 + NL + j] = (T)(wg * P);
+        r1[2 + 2 * NL + j] = (T)(wk * fabs(P));
+        r2[1 + j] = (T)P;
+    }
+}
+
+// Background views of the context for the multipole kernels.
+template <typename T, typename S> Bg<T, S> noalloc_bg(const coffe_gpu_ctx *ctx);
+template <> Bg<float, Spl32> noalloc_bg<float, Spl32>(const coffe_gpu_ctx *ctx)
+{
+    Bg<float, Spl32> bg;
+    bg.z_of_chi = ctx->bg[BG_Z_OF_CHI].v32();
+    bg.f = ctx->bg[BG_F].v32();
+    bg.D1 = ctx->bg[BG_D1].v32();
+    bg.b1 = ctx->bias[0].v32();
+    bg.b2 = ctx->bias[1].v32();
+    bg.has_b1 = ctx->bias_set[0];
+    bg.has_b2 = ctx->bias_set[1];
+    bg.zrec = ctx->z_uniform ? (const ZRec<float> *)ctx->zrec32.p : nullptr;
+    bg.z0 = (float)ctx->z0;
+    bg.zn = (float)ctx->zn;
+    bg.dz = (float)ctx->dz;
+    bg.inv_dz = (float)(1.0 / ctx->dz);
+    bg.nz = ctx->bg_bins;
+    return bg;
+}
+template <> Bg<double, Spl64> noalloc_bg<double, Spl64>(const coffe_gpu_ctx *ctx)
+{
+    Bg<double, Spl64> bg;
+    bg.z_of_chi = ctx->bg[BG_Z_OF_CHI].v64();
+    bg.f = ctx->bg[BG_F].v64();
+    bg.D1 = ctx->bg[BG_D1].v64();
+    bg.b1 = ctx->bias[0].v64();
+    bg.b2 = ctx->bias[1].v64();
+    bg.has_b1 = ctx->bias_set[0];
+    bg.has_b2 = ctx->bias_set[1];
+    bg.zrec = ctx->z_uniform ? (const ZRec<double> *)ctx->zrec64.p : nullptr;
+    bg.z0 = ctx->z0;
+    bg.zn = ctx->zn;
+    bg.dz = ctx->dz;
+    bg.inv_dz = 1.0 / ctx->dz;
+    bg.nz = ctx->bg_bins;
+    return bg;
+}
+
+// The launches of `launch` with the counter, node table and retry list in the
+// fixed scratch.
+template <typename T, typename S, typename TT>
+int launch_noalloc(coffe_gpu_ctx *ctx, const MpArgs &a, const S &chi_of_z, const TT *tab_x,
+                   const TT *tab_y, const int *req_spectrum, const double *req_z_mean,
+                   const int64_t *req_offset, const double *sep, long long total, double *out,
+                   unsigned char *scratch)
+{
+    const Bg<T, S> bg = noalloc_bg<T, S>(ctx);
+    int *d_count = (int *)scratch;
+    T *d_nodes = (T *)(scratch + 256);
+    int2 *d_retry = (int2 *)(scratch + MP_NOALLOC_LIST_OFFSET);
+    CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
+    mp_node_table_kernel<T><<<1, 64, 0, ctx->stream>>>(a, d_nodes);
+    int st = cg_after_launch(ctx, "mp_node_table_kernel");
+    if (st) return st;
+    const long long blocks = (total + MP_LANE_THREADS - 1) / MP_LANE_THREADS;
+#define MP_NOALLOC_NL(NLV)                                                                       \
+    case NLV: {                                                                                  \
+        const size_t smem = sizeof(T) * (NodeLayout<NLV>::COUNT + 61 * MP_LANE_THREADS);         \
+        CG_CUDA(ctx, cudaFuncSetAttribute(mp_lane_kernel<NLV, T, S, TT>,                        \
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,           \
+                                          (int)smem));                                           \
+        mp_lane_kernel<NLV, T, S, TT><<<(unsigned)blocks, MP_LANE_THREADS, smem, ctx->stream>>>( \
+            a, bg, chi_of_z, tab_x, tab_y, req_spectrum, req_z_mean, req_offset, sep, total,    \
+            d_nodes, out, d_count, d_retry, ctx->d_err);                                         \
+        break;                                                                                   \
+    }
+    switch (a.n_l) {
+        MP_NOALLOC_NL(1)
+        MP_NOALLOC_NL(2)
+        MP_NOALLOC_NL(3)
+        MP_NOALLOC_NL(4)
+        MP_NOALLOC_NL(5)
+        MP_NOALLOC_NL(6)
+        MP_NOALLOC_NL(7)
+        MP_NOALLOC_NL(8)
+    default:
+        cg_set_error(ctx, "multipoles_noalloc: unsupported number of multipoles %d", a.n_l);
+        return COFFE_GPU_EINVAL;
+    }
+#undef MP_NOALLOC_NL
+    if ((st = cg_after_launch(ctx, "mp_lane_kernel"))) return st;
+    mp_retry_kernel<T, S, TT><<<ctx->sm_count * 2, 32 * MP_RETRY_WARPS, 0, ctx->stream>>>(
+        a, bg, chi_of_z, tab_x, tab_y, req_spectrum, req_z_mean, req_offset, sep, out, d_count,
+        d_retry, ctx->d_err);
+    return cg_after_launch(ctx, "mp_retry_kernel");
+}
+
+} // namespace
+
+extern "C" int coffe_gpu_multipoles_noalloc(coffe_gpu_ctx_t *ctx, int contrib, int precision,
+                                            double epsrel, int n_req, int64_t n_sep,
+                                            const int *req_spectrum, const double *req_z_mean,
+                                            const int64_t *req_offset, const double *sep, int n_l,
+                                            const int *l, double *out)
+{
+    if (!ctx || !req_spectrum || !req_z_mean || !req_offset || !l || n_req < 1 || n_sep < 0 ||
+        (n_sep > 0 && (!sep || !out)))
+        return COFFE_GPU_EINVAL;
+    if (!ctx->bg_ready || !ctx->int_ready) {
+        cg_set_error(ctx, "multipoles_noalloc: %s not initialised",
+                     ctx->bg_ready ? "integrals" : "background");
+        return COFFE_GPU_ESTATE;
+    }
+    if (n_l < 1 || n_l > MP_MAX_L) {
+        cg_set_error(ctx, "multipoles_noalloc: need 1 <= n_l <= %d", MP_MAX_L);
+        return COFFE_GPU_EINVAL;
+    }
+    if ((long long)n_sep * n_l > (long long)COFFE_GPU_NOALLOC_MAX_OUTPUTS) {
+        cg_set_error(ctx,
+                     "multipoles_noalloc: %lld separations x %d multipoles = %lld outputs exceed "
+                     "the fixed scratch limit of %d outputs per call; split the requests",
+                     (long long)n_sep, n_l, (long long)n_sep * n_l, COFFE_GPU_NOALLOC_MAX_OUTPUTS);
+        return COFFE_GPU_EINVAL;
+    }
+    if (precision != ctx->int_precision) {
+        cg_set_error(ctx, "multipoles_noalloc: precision %d differs from the integrals' (%d)",
+                     precision, ctx->int_precision);
+        return COFFE_GPU_EINVAL;
+    }
+    if (!(contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD)) || (contrib & ~7)) {
+        cg_set_error(ctx, "multipoles_noalloc: contrib must select den and/or rsd");
+        return COFFE_GPU_EINVAL;
+    }
+    if (!(epsrel > 0)) {
+        cg_set_error(ctx, "multipoles_noalloc: epsrel must be positive");
+        return COFFE_GPU_EINVAL;
+    }
+    MpArgs a;
+    a.n_req = n_req;
+    a.n_l = n_l;
+    a.contrib = contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD);
+    a.t00 = a.t02 = a.t04 = -1;
+    for (int t = 0; t < ctx->n_terms; ++t) {
+        if (ctx->term_n[t] == 0 && ctx->term_l[t] == 0) a.t00 = t;
+        if (ctx->term_n[t] == 0 && ctx->term_l[t] == 2) a.t02 = t;
+        if (ctx->term_n[t] == 0 && ctx->term_l[t] == 4) a.t04 = t;
+    }
+    if (a.t00 < 0 || a.t02 < 0 || a.t04 < 0) {
+        cg_set_error(ctx, "multipoles_noalloc: integrals (0,0), (0,2), (0,4) are required");
+        return COFFE_GPU_ESTATE;
+    }
+    a.n_terms = ctx->n_terms;
+    a.tab_len = (int)(ctx->N + CG_N_SMALL_R + 1);
+    a.inv_dlog = (double)ctx->N / log(ctx->kmax / ctx->kmin);
+    a.epsrel = epsrel;
+    for (int i = 0; i < MP_MAX_L; ++i) a.ls[i] = 0;
+    for (int i = 0; i < n_l; ++i) {
+        if (l[i] < 0 || l[i] > MP_MAX_LDEG) {
+            cg_set_error(ctx, "multipoles_noalloc: l = %d out of range [0, %d]", l[i], MP_MAX_LDEG);
+            return COFFE_GPU_EINVAL;
+        }
+        a.ls[i] = l[i];
+    }
+    a.retry_cap = (long long)n_sep * n_l;
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    unsigned char *scratch = nullptr;
+    int st = noalloc_scratch_address(ctx, &scratch);
+    if (st) return st;
+    if (n_sep == 0) return COFFE_GPU_OK;
+    if (ctx->sm_count <= 0)
+        CG_CUDA(ctx, cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount,
+                                            ctx->device));
+    if (precision == COFFE_GPU_MIXED)
+        return launch_noalloc<float, Spl32, float>(
+            ctx, a, ctx->bg[BG_CHI_OF_Z].v32(), (const float *)ctx->tab_x32.p,
+            (const float *)ctx->tab_y.p, req_spectrum, req_z_mean, req_offset, sep, n_sep, out,
+            scratch);
+    return launch_noalloc<double, Spl64, double>(
+        ctx, a, ctx->bg[BG_CHI_OF_Z].v64(), (const double *)ctx->tab_x.p,
+        (const double *)ctx->tab_y.p, req_spectrum, req_z_mean, req_offset, sep, n_sep, out,
+        scratch);
 }

@@ -191,6 +191,37 @@ int coffe_gpu_multipoles_async(coffe_gpu_ctx_t *ctx, int contrib, int precision,
                                const int64_t *req_offset, const double *sep, int n_l,
                                const int *l, double *out);
 
+/* No counterpart in the reference (its multipoles allocate freely on the host).
+   Same computation, arguments and results as coffe_gpu_multipoles_async, for
+   callers that must not have the library allocate device memory during the call:
+   a process whose device memory is all handed to a pool at start-up (PyTorch's
+   caching allocator, a service that reserves its HBM up front) could see a
+   growing scratch buffer fail halfway through a run, and cudaMalloc/cudaFree
+   synchronise the whole device, stalling every other stream of a process that
+   shares the GPU.  The other multipole entry points grow their scratch (retry
+   list, node table) on demand; this one takes it from one fixed array in the
+   library's own device memory (8 MiB + 20 KiB) and never calls cudaMalloc,
+   cudaFree or any other allocating routine.
+   - Limit: n_sep * n_l <= COFFE_GPU_NOALLOC_MAX_OUTPUTS per call; larger calls
+     return COFFE_GPU_EINVAL with the reason in coffe_gpu_last_error (split the
+     requests into several calls).
+   - Set-up: the first call on each device looks up the array's device address
+     (with that device current) and may trigger the driver's lazy loading of the
+     library's kernels; make that first call before any stream capture.
+   - Concurrency: every call on one device uses the same array, so two calls on
+     the same device whose work can overlap (different streams, contexts or host
+     threads) race and corrupt each other's results; serialise them, e.g. on one
+     stream.
+   - Arrays as for coffe_gpu_multipoles_async (device pointers, `l` on the host);
+     device-side errors surface at the next coffe_gpu_synchronize, and
+     coffe_gpu_multipoles_retries does not count these calls. */
+#define COFFE_GPU_NOALLOC_MAX_OUTPUTS 1048576
+int coffe_gpu_multipoles_noalloc(coffe_gpu_ctx_t *ctx, int contrib, int precision,
+                                 double epsrel, int n_req, int64_t n_sep,
+                                 const int *req_spectrum, const double *req_z_mean,
+                                 const int64_t *req_offset, const double *sep, int n_l,
+                                 const int *l, double *out);
+
 /* Number of (separation, multipole) outputs of the last multipoles call on
    this context whose first GK61 panel missed the tolerance and went through
    the adaptive bisection (synchronises the context's stream); -1 if none ran.
