@@ -44,6 +44,10 @@ N_FFT = 4096
 FLOP_PER_NODE = 170
 FLOP_PER_PAIR_EXTRA = 130
 NODES = 61
+# DRAM bytes (read + write) per (request, separation) of the mixed multipole
+# kernel, from an ncu capture of the first 256 spectra of this batch (324,864
+# pairs, 5.90 MB read, 0 B written); traffic grows with the number of pairs
+DRAM_BYTES_PER_PAIR = 5.897728e6 / 324864
 
 
 def parse():
@@ -387,14 +391,16 @@ def ours(args, rank, world, local_rank):
         "max_rel_err_mixed_vs_fp64": err,
         "adaptive_retries": retries,
         "gpu_launches": int(launches),
-        "roofline": {"kernel": "multipoles_kernel<float> (mixed multipole quadrature)",
+        "roofline": {"kernel": "mp_lane_kernel<3, float> (mixed multipole quadrature)",
                      "bound": "fp32", "achieved": achieved,
                      "peak": sgemm, "unit": "TFLOP/s", "frac": achieved / sgemm,
                      "peak_source": "measured cuBLAS SGEMM 8192^3 (FP32 CUDA cores, TF32 off) "
                                     "in this run; the kernel is FP32-pipe bound, neither HBM "
                                     "nor tensor",
                      "flop_per_launch": flop_launch, "launch_ms": kern_s * 1e3,
-                     "traffic": None,
+                     "traffic": n_sep * DRAM_BYTES_PER_PAIR,
+                     "traffic_unit": "bytes per launch (ncu dram read+write of a 256-spectrum "
+                                     "capture, scaled by pairs)",
                      "hbm_peak_gbs": peaks.get("hbm_gbs")},
         "clocks": clocks,
         "e2e": e2e,
