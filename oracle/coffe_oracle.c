@@ -1135,3 +1135,269 @@ int or_multipoles_batch(const or_model_t *m, int contrib, const double *z_mean,
     (void)nthreads;
     return 0;
 }
+
+/* ------------------------------------------------------------------ lensing
+ * Full-sky lensing terms of the linear-P(k), non-divergent path
+ * (flatsky_local_nonlocal = flatsky_nonlocal = only_cross_correlations = 0,
+ * the reference's defaults, parser.c:801, 1018-1022).
+ *
+ * Geometry as functions.c:1498-1509 and 3473-3481: chi_{1,2} = chi(z_mean) -+
+ * sep mu / 2, lambda_i = chi_i x_i.  cos(theta) is formed as 1 - s with
+ * s = sep^2 (1 - mu^2) / (2 chi1 chi2) (the same quantity as the reference's
+ * ratio, without its cancellation), 1 - cos^2 = s (2 - s), and the squared
+ * distances as r21 = (lambda2 - chi1)^2 + 2 chi1 lambda2 s etc., which equal
+ * the reference's lambda2^2 + chi1^2 - 2 chi1 lambda2 cos(theta).
+ */
+typedef struct {
+    double chi_mean, chi1, chi2, s, ct, one_m_ct2;
+} or_lens_geom_t;
+
+static or_lens_geom_t lens_geom(const or_model_t *m, double z_mean, double mu, double sep)
+{
+    or_lens_geom_t g;
+    g.chi_mean = or_spline_eval(&m->chi_of_z, z_mean);
+    g.chi1 = g.chi_mean - sep * mu / 2.;
+    g.chi2 = g.chi_mean + sep * mu / 2.;
+    g.s = sep * sep * (1 - mu * mu) / (2. * g.chi_mean * g.chi_mean - mu * mu * sep * sep / 2.);
+    g.ct = 1 - g.s;
+    g.one_m_ct2 = g.s * (2 - g.s);
+    return g;
+}
+
+/* den-len + len-den (functions.c:1557-2052) and rsd-len + len-rsd
+   (functions.c:2053-2483) single-integrated xi at (mu, x), without the
+   (2l+1) P_l(mu) of the multipole integrand (signal.c:141-186) */
+double or_xi_single_integrated(const or_model_t *m, int contrib, double z_mean, double mu,
+                               double sep, double x)
+{
+    if (!(contrib & OR_CONTRIB_LEN) || !(contrib & (OR_CONTRIB_DEN | OR_CONTRIB_RSD)))
+        return 0.0;
+    const or_lens_geom_t g = lens_geom(m, z_mean, mu, sep);
+    const double chi1 = g.chi1, chi2 = g.chi2, ct = g.ct, omc2 = g.one_m_ct2;
+    const double lambda1 = chi1 * x, lambda2 = chi2 * x;
+    double r21 = (lambda2 - chi1) * (lambda2 - chi1) + 2 * chi1 * lambda2 * g.s;
+    double r22 = (lambda1 - chi2) * (lambda1 - chi2) + 2 * chi2 * lambda1 * g.s;
+    if (r21 < 0) r21 = 0;
+    if (r22 < 0) r22 = 0;
+    const double z1c = or_spline_eval(&m->z_of_chi, chi1);
+    const double z2c = or_spline_eval(&m->z_of_chi, chi2);
+    const double z1 = or_spline_eval(&m->z_of_chi, lambda1);
+    const double z2 = or_spline_eval(&m->z_of_chi, lambda2);
+    const double s1 = bias_eval(m, 2, z1c, 0.0), s2 = bias_eval(m, 3, z2c, 0.0);
+    const double pref = pow(OR_H0 * m->h, 2);
+    const double Om = m->Omega0_m;
+    /* the "2" side: the lensing convergence along the line of sight to chi2,
+       correlated with the local term at chi1 (and the mirror "1" side) */
+    const double D1z1 = or_spline_eval(&m->D1, z1), D1z2 = or_spline_eval(&m->D1, z2);
+    const double az1 = or_spline_eval(&m->a, z1), az2 = or_spline_eval(&m->a, z2);
+    const double D1z1c = or_spline_eval(&m->D1, z1c), D1z2c = or_spline_eval(&m->D1, z2c);
+    const double sr21 = sqrt(r21), sr22 = sqrt(r22);
+    const or_spline_t *i00 = find_integral(m, 0, 0), *i02 = find_integral(m, 0, 2),
+                      *i04 = find_integral(m, 0, 4), *i11 = find_integral(m, 1, 1);
+    double result = 0;
+    if (contrib & OR_CONTRIB_DEN) {
+        const double b1 = bias_eval(m, 0, z1c, 1.0), b2 = bias_eval(m, 1, z2c, 1.0);
+        /* functions.c:1620-1719 (both nonzero), 1720-1876, 1877-1974, 1975-2050 */
+        double t1, t2;
+        if (r21 != 0.0)
+            t1 = chi2 * (2 * chi1 * ct * or_spline_eval(i11, sr21) -
+                         chi1 * chi1 * lambda2 * omc2 * or_spline_eval(i02, sr21) / r21);
+        else
+            t1 = chi2 * 2 * chi1 * or_spline_eval(i11, 0.0);
+        if (r22 != 0.0)
+            t2 = chi1 * (2 * chi2 * ct * or_spline_eval(i11, sr22) -
+                         chi2 * chi2 * lambda1 * omc2 * or_spline_eval(i02, sr22) / r22);
+        else
+            t2 = chi1 * 2 * chi2 * or_spline_eval(i11, 0.0);
+        result += pref * (-3 * Om / 2. *
+                          (b1 * (2 - 5 * s2) * D1z1c * (1 - x) * D1z2 / az2 * t1 +
+                           b2 * (2 - 5 * s1) * D1z2c * (1 - x) * D1z1 / az1 * t2));
+    }
+    if (contrib & OR_CONTRIB_RSD) {
+        const double f1c = or_spline_eval(&m->f, z1c), f2c = or_spline_eval(&m->f, z2c);
+        const double c2m1 = 2 * ct * ct - 1; /* cos(2 theta) */
+        /* I00/I02 part of one side (functions.c:2174-2183) */
+#define OR_RL_A(ch, la, sr, r2)                                                                \
+    ((la - 6 * ch * ct + 3 * la * c2m1) * or_spline_eval(i00, sr) / 15. -                     \
+     (6 * ch * ch * ch * ct - ch * ch * la * (9 * ct * ct + 11) +                             \
+      ch * la * la * ct * (3 * c2m1 + 19) - 2 * la * la * la * (3 * c2m1 + 1)) *              \
+         or_spline_eval(i02, sr) / (r2) / 21.)
+        /* I04 part of one side (functions.c:2298-2306) */
+#define OR_RL_B(ch, la, sr, r2)                                                                \
+    (-(-4 * pow(ch, 5) * ct - pow(ch, 3) * pow(la, 2) * ct * (c2m1 + 7) +                      \
+       pow(ch, 2) * pow(la, 3) * (pow(ct, 4) + 12 * ct * ct - 21) -                            \
+       3 * ch * pow(la, 4) * ct * (c2m1 - 5) - pow(la, 5) * (3 * c2m1 + 1) +                   \
+       12 * pow(ch, 4) * la) *                                                                 \
+     or_spline_eval(i04, sr) / (r2) / (r2) / 35.)
+        const double w2 = chi2 * f1c * (2 - 5 * s2) * D1z1c * D1z2 / az2; /* side at chi2 */
+        const double w1 = chi1 * f2c * (2 - 5 * s1) * D1z2c * D1z1 / az1; /* side at chi1 */
+        const double c = pref * 3 * Om / 2.;
+        if (r21 != 0 && r22 != 0) {
+            /* functions.c:2060-2391 */
+            result += c * (w2 * (1 - x) * OR_RL_A(chi1, lambda2, sr21, r21) +
+                           w1 * (1 - x) * OR_RL_A(chi2, lambda1, sr22, r22));
+            if (fabs(mu) < 0.999)
+                result += c * (w2 * (1 - x) * OR_RL_B(chi1, lambda2, sr21, r21) +
+                               w1 * (1 - x) * OR_RL_B(chi2, lambda1, sr22, r22));
+            else
+                result += c * (w2 * (1 - x) * 4. * (lambda2 + chi1) * or_spline_eval(i04, sr21) / 35. +
+                               w1 * (1 - x) * 4. * (lambda1 + chi2) * or_spline_eval(i04, sr22) / 35.);
+        } else if (r21 == 0 && r22 != 0) {
+            /* functions.c:2392-2426 */
+            result += c * (w2 * (1 - chi1 / chi2) * (-2 * chi1 * or_spline_eval(i00, 0.0) / 15.) +
+                           w1 * (1 - x) *
+                               (OR_RL_A(chi2, lambda1, sr22, r22) + OR_RL_B(chi2, lambda1, sr22, r22)));
+        } else if (r21 != 0 && r22 == 0) {
+            /* functions.c:2427-2462 */
+            result += c * (w2 * (1 - x) *
+                               (OR_RL_A(chi1, lambda2, sr21, r21) + OR_RL_B(chi1, lambda2, sr21, r21)) +
+                           w1 * (1 - chi2 / chi1) * (-2 * chi2 * or_spline_eval(i00, 0.0) / 15.));
+        } else {
+            /* functions.c:2463-2481 */
+            result += c * (w2 * (1 - chi1 / chi2) * (-2 * chi1 * or_spline_eval(i00, 0.0) / 15.) +
+                           w1 * (1 - chi2 / chi1) * (-2 * chi2 * or_spline_eval(i00, 0.0) / 15.));
+        }
+#undef OR_RL_A
+#undef OR_RL_B
+    }
+    return result;
+}
+
+/* len-len double-integrated xi at (mu, x1, x2) (functions.c:3460-3836 and the
+   (H0 h)^4 factor of 3988-3990) */
+double or_xi_double_integrated(const or_model_t *m, int contrib, double z_mean, double mu,
+                               double sep, double x1, double x2)
+{
+    if (!(contrib & OR_CONTRIB_LEN))
+        return 0.0;
+    const or_lens_geom_t g = lens_geom(m, z_mean, mu, sep);
+    const double chi1 = g.chi1, chi2 = g.chi2, ct = g.ct, omc2 = g.one_m_ct2;
+    const double lambda1 = chi1 * x1, lambda2 = chi2 * x2;
+    double r2 = (lambda1 - lambda2) * (lambda1 - lambda2) + 2 * lambda1 * lambda2 * g.s;
+    if (r2 < 0) r2 = 0;
+    const double z1c = or_spline_eval(&m->z_of_chi, chi1);
+    const double z2c = or_spline_eval(&m->z_of_chi, chi2);
+    const double z1 = or_spline_eval(&m->z_of_chi, lambda1);
+    const double z2 = or_spline_eval(&m->z_of_chi, lambda2);
+    const double s1 = bias_eval(m, 2, z1c, 0.0), s2 = bias_eval(m, 3, z2c, 0.0);
+    const double Om = m->Omega0_m;
+    const double pre = 9. * Om * Om * (2 - 5 * s1) * (2 - 5 * s2) / 4. * chi1 * chi2 *
+                       or_spline_eval(&m->D1, z1) * or_spline_eval(&m->D1, z2) /
+                       or_spline_eval(&m->a, z1) / or_spline_eval(&m->a, z2) * (1 - x1) * (1 - x2);
+    const double ll = lambda1 * lambda2;
+    double result;
+    if (r2 > 1e-20) {
+        const double r = sqrt(r2);
+        const double c2m = -omc2; /* cos^2 - 1 */
+        result = pre * (2 * c2m * ll * or_spline_eval(find_integral(m, 0, 0), r) / 5. +
+                        4 * ct * or_spline_eval(find_integral(m, 2, 0), r) / 3. +
+                        4 * ct * (r2 + 6 * ct * ll) * or_spline_eval(find_integral(m, 1, 1), r) / 15. +
+                        2 * c2m * ll * (2 * r2 + 3 * ct * ll) *
+                            or_spline_eval(find_integral(m, 0, 2), r) / 7. / r2 +
+                        2 * ct * (2 * r2 * r2 + 12 * ct * r2 * ll + 15 * c2m * ll * ll) *
+                            or_spline_eval(find_integral(m, 1, 3), r) / 15. / r2 +
+                        c2m * ll * (6 * r2 * r2 + 30 * ct * r2 * ll + 35 * c2m * ll * ll) *
+                            or_spline_eval(find_integral(m, 0, 4), r) / 35. / r2 / r2);
+    } else {
+        /* functions.c:3801-3833 */
+        result = pre * (4. + 24. * ll * or_spline_eval(find_integral(m, 1, 1), 0.0) / 15.);
+    }
+    return result * pow(OR_H0 * m->h, 4);
+}
+
+/* Lensing multipoles with Gauss-Legendre product rules on the unit cube of
+   signal.c:141-237 (mu = 2 v - 1): n_mu nodes in v and, per x line, n_x nodes
+   split into two panels of n_x / 2 at the point where the integrand's
+   separation argument is smallest (x* = lambda1 / chi2 for the inner len-len
+   line, x* = min(chi1, chi2) cos(theta) / max(chi1, chi2) for the single
+   integral), where its narrow peak sits; GL nodes cluster at panel ends, so
+   the peak is resolved at no extra cost.  n_x odd or 0 panels fall back to
+   one panel.  out[j] = (2 l_j + 1) * integral (signal.c:659-668, 742-751);
+   nothing is added for the nonintegrated terms. */
+typedef struct {
+    size_t n;
+    const double *xf, *wf; /* n-point rule on [-1, 1] */
+    const double *xh, *wh; /* n/2-point rule on [-1, 1] */
+} or_line_rule_t;
+
+static double lens_line(double x0, double x1_, double xs, const or_line_rule_t *R, int which,
+                        const or_model_t *m, int contrib, double z_mean, double mu, double sep,
+                        double xa)
+{
+    /* integrates over [x0, x1_]: two panels [x0, xs], [xs, x1_] of n/2 GL nodes
+       when xs is inside and n even, else one panel of n nodes */
+    double acc = 0.0;
+    const size_t n = R->n;
+    const int split = (n % 2 == 0) && xs > x0 && xs < x1_;
+    const size_t np = split ? n / 2 : n;
+    const double *gx = split ? R->xh : R->xf, *gw = split ? R->wh : R->wf;
+    const double lo[2] = {x0, xs}, hi[2] = {xs, x1_};
+    for (int p = 0; p < (split ? 2 : 1); ++p) {
+        const double a = split ? lo[p] : x0, b = split ? hi[p] : x1_;
+        const double c = 0.5 * (a + b), h = 0.5 * (b - a);
+        double part = 0.0;
+        for (size_t i = 0; i < np; ++i) {
+            const double x = c + h * gx[i];
+            part += gw[i] * (which == 1 ? or_xi_single_integrated(m, contrib, z_mean, mu, sep, x)
+                                        : or_xi_double_integrated(m, contrib, z_mean, mu, sep, xa, x));
+        }
+        acc += h * part;
+    }
+    return acc;
+}
+
+int or_multipoles_lensing_gl(const or_model_t *m, int contrib, double z_mean, double sep,
+                             int n_l, const int *ls, size_t n_mu, size_t n_x, double *out)
+{
+    double *xm = (double *)malloc(sizeof(double) * n_mu), *wm = (double *)malloc(sizeof(double) * n_mu);
+    double *xf = (double *)malloc(sizeof(double) * n_x), *wf = (double *)malloc(sizeof(double) * n_x);
+    double *xh = (double *)malloc(sizeof(double) * n_x), *wh = (double *)malloc(sizeof(double) * n_x);
+    if (!xm || !wm || !xf || !wf || !xh || !wh) {
+        free(xm); free(wm); free(xf); free(wf); free(xh); free(wh);
+        return -1;
+    }
+    or_gauss_legendre(n_mu, xm, wm);
+    or_gauss_legendre(n_x, xf, wf);
+    if (n_x >= 2) or_gauss_legendre(n_x / 2, xh, wh);
+    for (int j = 0; j < n_l; ++j) out[j] = 0.0;
+    const int single = (contrib & OR_CONTRIB_LEN) && (contrib & (OR_CONTRIB_DEN | OR_CONTRIB_RSD));
+    const int dbl = (contrib & OR_CONTRIB_LEN) != 0;
+    const or_line_rule_t R = {n_x, xf, wf, xh, wh};
+    for (size_t i = 0; i < n_mu; ++i) {
+        const double mu = xm[i], wmu = 0.5 * wm[i]; /* dv = dmu / 2 */
+        const or_lens_geom_t g = lens_geom(m, z_mean, mu, sep);
+        double acc = 0.0;
+        if (single) {
+            const double xs = fmin(g.chi1, g.chi2) * g.ct / fmax(g.chi1, g.chi2);
+            acc += lens_line(0, 1, xs, &R, 1, m, contrib, z_mean, mu, sep, 0);
+        }
+        if (dbl)
+            for (size_t a = 0; a < n_x; ++a) {
+                const double x1 = 0.5 * (xf[a] + 1.0);
+                const double xs = x1 * g.chi1 / g.chi2;
+                acc += 0.5 * wf[a] * lens_line(0, 1, xs, &R, 2, m, contrib, z_mean, mu, sep, x1);
+            }
+        for (int j = 0; j < n_l; ++j) out[j] += wmu * acc * or_legendre(ls[j], mu);
+    }
+    for (int j = 0; j < n_l; ++j) out[j] *= (2 * ls[j] + 1);
+    free(xm); free(wm); free(xf); free(wf); free(xh); free(wh);
+    return 0;
+}
+
+/* many (z_mean, sep) points, OpenMP over points; out[p * n_l + j] */
+int or_multipoles_lensing_batch(const or_model_t *m, int contrib, const double *z_mean,
+                                const double *sep, size_t count, int n_l, const int *ls,
+                                size_t n_mu, size_t n_x, double *out, int nthreads)
+{
+    int bad = 0;
+#ifdef _OPENMP
+    if (nthreads <= 0)
+        nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(| : bad)
+#endif
+    for (long p = 0; p < (long)count; ++p)
+        bad |= or_multipoles_lensing_gl(m, contrib, z_mean[p], sep[p], n_l, ls, n_mu, n_x,
+                                        out + (size_t)p * n_l) != 0;
+    (void)nthreads;
+    return bad ? -1 : 0;
+}

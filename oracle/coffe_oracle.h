@@ -134,6 +134,23 @@ int or_multipoles_batch(const or_model_t *m, int contrib, const double *z_mean,
 double or_multipole_nonintegrated_gl(const or_model_t *m, int contrib, double z_mean,
                                      double sep, int l, size_t n_mu);
 
+/* ----------------------------------------------------------------- lensing */
+/* den-len + rsd-len single-integrated xi at (mu, x) (functions.c:1486-2483,
+   full sky, linear P(k), no renormalisation) */
+double or_xi_single_integrated(const or_model_t *m, int contrib, double z_mean, double mu,
+                               double sep, double x);
+/* len-len double-integrated xi at (mu, x1, x2) (functions.c:3460-3836) */
+double or_xi_double_integrated(const or_model_t *m, int contrib, double z_mean, double mu,
+                               double sep, double x1, double x2);
+/* lensing multipoles (single + double integrated terms selected by contrib)
+   with product Gauss-Legendre rules: n_mu x n_x (single), n_mu x n_x x n_x
+   (double); out[j] for l = ls[j] */
+int or_multipoles_lensing_gl(const or_model_t *m, int contrib, double z_mean, double sep,
+                             int n_l, const int *ls, size_t n_mu, size_t n_x, double *out);
+int or_multipoles_lensing_batch(const or_model_t *m, int contrib, const double *z_mean,
+                                const double *sep, size_t count, int n_l, const int *ls,
+                                size_t n_mu, size_t n_x, double *out, int nthreads);
+
 /* number of QAG subdivisions taken by the last or_multipole_nonintegrated call
    in this thread (diagnostic) */
 int or_last_qag_intervals(void);

@@ -86,6 +86,13 @@ def lib():
         L.or_multipoles_batch.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _ip, C.c_size_t,
                                           C.c_double, _dp, C.c_int]
         L.or_last_qag_intervals.restype = C.c_int
+        L.or_xi_single_integrated.argtypes = [C.c_void_p, C.c_int] + [C.c_double] * 4
+        L.or_xi_single_integrated.restype = C.c_double
+        L.or_xi_double_integrated.argtypes = [C.c_void_p, C.c_int] + [C.c_double] * 5
+        L.or_xi_double_integrated.restype = C.c_double
+        L.or_multipoles_lensing_batch.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_size_t,
+                                                  C.c_int, _ip, C.c_size_t, C.c_size_t, _dp,
+                                                  C.c_int]
         _lib = L
     return _lib
 
@@ -222,6 +229,25 @@ class Model:
         out = np.zeros(len(sep))
         lib().or_multipoles_batch(self._p, contrib, z_mean, sep, l, len(sep), epsrel, out,
                                   int(nthreads))
+        return out
+
+
+    def xi_single(self, contrib, z_mean, mu, sep, x):
+        return lib().or_xi_single_integrated(self._p, contrib, z_mean, mu, sep, x)
+
+    def xi_double(self, contrib, z_mean, mu, sep, x1, x2):
+        return lib().or_xi_double_integrated(self._p, contrib, z_mean, mu, sep, x1, x2)
+
+    def multipoles_lensing(self, contrib, z_mean, sep, ls, n_mu, n_x, nthreads=0):
+        """Lensing multipoles (single + double integrated terms) with product
+        Gauss-Legendre rules; returns (len(sep), len(ls))."""
+        sep = _f64(np.atleast_1d(sep))
+        z = _f64(np.broadcast_to(np.asarray(z_mean, dtype=np.float64), sep.shape))
+        la = np.ascontiguousarray(ls, dtype=np.int32)
+        out = np.zeros((len(sep), len(la)))
+        if lib().or_multipoles_lensing_batch(self._p, contrib, z, sep, len(sep), len(la), la,
+                                             int(n_mu), int(n_x), out, int(nthreads)) != 0:
+            raise MemoryError("lensing multipoles failed")
         return out
 
 
