@@ -48,6 +48,7 @@ EXPORTS = (
     "coffe_gpu_integral_get",
     "coffe_gpu_integral_eval",
     "coffe_gpu_multipoles",
+    "coffe_gpu_set_lensing_rule",
     "coffe_gpu_multipoles_async",
     "coffe_gpu_multipoles_noalloc",
     "coffe_gpu_multipoles_retries",
@@ -117,6 +118,7 @@ def load(build_if_missing: bool = True):
                                        _dp, C.c_int, _ip, _dp, C.c_int]
     L.coffe_gpu_multipoles_async.argtypes = [_p, C.c_int, C.c_int, C.c_double, C.c_int,
                                              C.c_int64, _ip, _dp, _lp, _dp, C.c_int, _ip, _dp]
+    L.coffe_gpu_set_lensing_rule.argtypes = [_p, C.c_int, C.c_int]
     L.coffe_gpu_multipoles_noalloc.argtypes = [_p, C.c_int, C.c_int, C.c_double, C.c_int,
                                                C.c_int64, _ip, _dp, _lp, _dp, C.c_int, _ip, _dp]
     L.coffe_gpu_multipoles_retries.argtypes = [_p]

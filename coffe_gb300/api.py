@@ -219,6 +219,12 @@ class Context:
         self.n_spectra = S
         self.precision = _precision(precision)
 
+    def set_lensing_rule(self, n_mu: int = 128, n_x: int = 256):
+        """Gauss-Legendre rule of the lensing terms: n_mu nodes in mu, n_x per x
+        line (split in two panels at the line's integrand peak)."""
+        self._check(self._L.coffe_gpu_set_lensing_rule(self._ctx, int(n_mu), int(n_x)),
+                    "set_lensing_rule")
+
     def multipoles_async(self, req_spectrum, req_z_mean, req_offset, sep, n_sep: int, ls, out,
                          contrib=_lib.DEN | _lib.RSD, precision="fp64", epsrel=1e-5):
         """Enqueue-only multipoles on device tensors; ``ls`` is a host sequence.

@@ -139,7 +139,8 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
                       &ctx->qfac,     &ctx->modec,  &ctx->postf,   &ctx->twid,   &ctx->twid32,
                       &ctx->spec,     &ctx->req_buf, &ctx->term_meta, &ctx->zrec64,
                       &ctx->zrec32,   &ctx->mp_retry, &ctx->term_df,
-                      &ctx->samp_f32, &ctx->csfac32, &ctx->mp_nodes};
+                      &ctx->samp_f32, &ctx->csfac32, &ctx->mp_nodes,
+                      &ctx->lens_rule, &ctx->lens_rec, &ctx->lens_part};
     for (DevBuf *b : bufs) cg_release(*b);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
@@ -411,6 +412,18 @@ int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, doubl
     if (total > 0)
         CG_CUDA(ctx, cudaMemcpyAsync(out, d_out, b_out, cudaMemcpyDeviceToHost, ctx->stream));
     return cg_check_device_errors(ctx, "multipoles");
+}
+
+int coffe_gpu_set_lensing_rule(coffe_gpu_ctx_t *ctx, int n_mu, int n_x)
+{
+    if (!ctx) return COFFE_GPU_EINVAL;
+    if (n_mu < 2 || n_mu > 4096 || n_x < 2 || n_x > 4096) {
+        cg_set_error(ctx, "set_lensing_rule: need 2 <= n_mu, n_x <= 4096 (got %d, %d)", n_mu, n_x);
+        return COFFE_GPU_EINVAL;
+    }
+    ctx->lens_n_mu = n_mu;
+    ctx->lens_n_x = n_x;
+    return COFFE_GPU_OK;
 }
 
 int coffe_gpu_multipoles_async(coffe_gpu_ctx_t *ctx, int contrib, int precision, double epsrel,

@@ -49,6 +49,7 @@ struct coffe_gpu_ctx {
     int n_spectra = 0, n_terms = 0, int_precision = 0;
     size_t N = 0, nk = 0;
     double kmin = 0, kmax = 0;
+    bool int_small_r = false; // r = 0 and sub-Mpc entries filled
     int term_n[CG_MAX_TERMS], term_l[CG_MAX_TERMS], term_q[CG_MAX_TERMS];
     int n_q = 0;
     double qvals[CG_MAX_TERMS];
@@ -84,6 +85,13 @@ struct coffe_gpu_ctx {
     DevBuf mp_nodes; // first-panel node table of the last multipole list
     int mp_nodes_nl = 0, mp_nodes_prec = -1;
     int mp_nodes_ls[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+
+    // ---- lensing terms (lensing.cu)
+    int lens_n_mu = 128, lens_n_x = 256; // Gauss-Legendre rule sizes
+    DevBuf lens_rule;                    // the rule's nodes and weights
+    int lens_rule_mu = 0, lens_rule_x = 0;
+    DevBuf lens_rec;  // Akima records of the six lensing tables
+    DevBuf lens_part; // per (pair, mu) partial integrals
 };
 
 void cg_set_error(coffe_gpu_ctx *ctx, const char *fmt, ...);
@@ -106,3 +114,6 @@ int multipoles_prepare_background(coffe_gpu_ctx *ctx);
 int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, int n_req,
                    const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
                    const double *sep, int n_l, const int *l, double *out, long long total);
+int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,
+                const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
+                const double *sep, int n_l, const int *l, double *out, long long total);

@@ -1081,6 +1081,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     ctx->kmin = k[0];
     ctx->kmax = k[nk - 1];
     ctx->int_precision = precision;
+    ctx->int_small_r = (flags & COFFE_GPU_SMALL_R) != 0;
     ctx->int_ready = true;
     return COFFE_GPU_OK;
 }

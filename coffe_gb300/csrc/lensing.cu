@@ -1,0 +1,605 @@
+// Lensing contributions to the multipoles of a ragged batch of
+// (spectrum, mean redshift, separation list) requests: the single-integrated
+// density/RSD x lensing terms and the double-integrated lensing-lensing term
+// of the full-sky correlation function, projected on Legendre multipoles.
+//
+// Restates coffe_integrate(SINGLE_INTEGRATED / DOUBLE_INTEGRATED, MULTIPOLES)
+// (signal.c:607-671, 704-754) with the integrands of signal.c:141-237,
+// functions_single_integrated (functions.c:1486-2483) and
+// functions_double_integrated (functions.c:3460-3836): linear P(k), full sky,
+// no renormalisation.  The reference integrates the unit cube (v, x) or
+// (v, x1, x2), mu = 2v - 1, with Cuhre (common.c:1096-1110); here the cube is
+// integrated with fixed Gauss-Legendre product rules: n_mu nodes in v and,
+// per x line, n_x nodes split into two panels of n_x / 2 at the point of the
+// line where the integrand's separation argument is smallest (its narrow
+// peak): x* = lambda1 / chi2 on an x2 line of len-len, x* = min(chi1, chi2)
+// cos(theta) / max(chi1, chi2) on the single-integrated line.
+//
+// Work split (one launch each, per chunk of pairs):
+//   lens_double_kernel  one CTA per (pair, mu node): threads own x1 lines and
+//                       sweep their x2 line; one partial per (pair, mu);
+//   lens_single_kernel  one warp per (pair, mu node), FP64 on both paths (the
+//                       RSD-lensing coefficients cancel terms of size chi^5);
+//   lens_reduce_kernel  per (pair, l): the mu weights and P_l(mu), summed in a
+//                       fixed order, added to the nonintegrated multipole.
+// The six I_l^n tables the integrands read are evaluated through Akima
+// records {y, b, c, d} built once per call and interleaved per interval, so a
+// node's six lookups share one interval search and one 192-byte (FP64) or
+// 96-byte (float) block.
+#include <math.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "ctx.cuh"
+
+namespace {
+
+#define LENS_THREADS 128
+#define LENS_NT 6
+enum { L00 = 0, L02, L04, L11, L13, L20 };
+
+struct LensArgs {
+    int n_req, n_l, n_mu, n_x, nh, contrib;
+    int tab_len, n_terms;
+    int term[LENS_NT];
+    double inv_dlog; // N / ln(kmax/kmin), r0 = 1
+    double Om, pref2, pref4;
+    int has_b1, has_b2, has_s1, has_s2;
+    long long pair0, n_items;
+    int ls[8];
+};
+
+struct LensBg64 {
+    Spl64 chi_of_z, z_of_chi, D1, f, a, b1, b2, s1, s2;
+};
+template <typename S> struct LensBgT {
+    S z_of_chi, D1, a;
+};
+
+template <typename TT> struct Rec4;
+template <> struct Rec4<double> { typedef double4_32a type; };
+template <> struct Rec4<float> { typedef float4 type; };
+
+__device__ __forceinline__ int lens_find_request(const int64_t *__restrict__ req_offset, int n_req,
+                                                 long long item)
+{
+    int lo = 0, hi = n_req;
+    while (hi > lo + 1) {
+        const int mid = (lo + hi) >> 1;
+        if (req_offset[mid] <= item)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// rec[(s * (len - 1) + i) * 6 + t]: Akima record of interval i of table
+// (spectrum s, lensing term t), from the raw table knots (spline.cuh's
+// akima_interval: the coefficients the reference's Akima spline holds)
+template <typename TT>
+__global__ void lens_records_kernel(LensArgs a, const TT *__restrict__ tab_x,
+                                    const TT *__restrict__ tab_y, int n_spectra,
+                                    typename Rec4<TT>::type *__restrict__ rec)
+{
+    const int len = a.tab_len, ni = len - 1;
+    const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= (long long)n_spectra * ni * LENS_NT) return;
+    const int t = (int)(item % LENS_NT);
+    const long long si = item / LENS_NT;
+    const int i = (int)(si % ni);
+    const int s = (int)(si / ni);
+    const TT *y = tab_y + ((size_t)s * a.n_terms + a.term[t]) * len;
+    TT b, c, d;
+    akima_interval<TT>(tab_x, y, len, i, b, c, d);
+    typename Rec4<TT>::type r;
+    r.x = y[i];
+    r.y = b;
+    r.z = c;
+    r.w = d;
+    rec[item] = r;
+}
+
+// interval of r in the table knots as a binary search returns it (an O(1)
+// guess on the log-spaced part, then a local correction); -1 outside
+template <typename TT>
+__device__ __forceinline__ int lens_interval(const TT *__restrict__ x, int n, TT inv_dlog, TT r)
+{
+    if (!(r >= x[0] && r <= x[n - 1])) return -1;
+    const int first = CG_N_SMALL_R + 1;
+    int i;
+    if (r >= __ldg(x + first)) {
+        i = first + (int)(log(r) * inv_dlog);
+        if (i > n - 2) i = n - 2;
+        if (i < first) i = first;
+        while (i > 0 && __ldg(x + i) > r) --i;
+        while (i < n - 2 && __ldg(x + i + 1) <= r) ++i;
+    } else {
+        int lo = 0, hi = first;
+        while (hi > lo + 1) {
+            const int mid = (lo + hi) / 2;
+            if (__ldg(x + mid) > r)
+                hi = mid;
+            else
+                lo = mid;
+        }
+        i = lo;
+    }
+    return i;
+}
+
+// the six lensing tables at r (NaN outside the tables)
+template <typename T, typename TT>
+__device__ __forceinline__ void lens_tables(const typename Rec4<TT>::type *__restrict__ recs,
+                                            const TT *__restrict__ x, int n, TT inv_dlog, T r,
+                                            T (&v)[LENS_NT])
+{
+    const int i = lens_interval<TT>(x, n, inv_dlog, (TT)r);
+    if (i < 0) {
+#pragma unroll
+        for (int t = 0; t < LENS_NT; ++t) v[t] = cg_nan<T>();
+        return;
+    }
+    const T dx = r - (T)__ldg(x + i);
+    const typename Rec4<TT>::type *p = recs + (size_t)i * LENS_NT;
+#pragma unroll
+    for (int t = 0; t < LENS_NT; ++t) {
+        const typename Rec4<TT>::type c = ldg_c4(p + t);
+        v[t] = (T)c.x + dx * ((T)c.y + dx * ((T)c.z + (T)c.w * dx));
+    }
+}
+
+// the value at r = 0 (first knot) of table t
+template <typename TT>
+__device__ __forceinline__ TT lens_at_zero(const typename Rec4<TT>::type *__restrict__ recs, int t)
+{
+    return ldg_c4(recs + t).x;
+}
+
+// Geometry of one (pair, mu node), functions.c:1498-1509 / 3473-3481, with
+// cos(theta) = 1 - s, s = sep^2 (1 - mu^2) / (2 chi1 chi2) (no cancellation)
+struct LensGeom {
+    double chi1, chi2, s, ct, omc2, z1c, z2c;
+};
+__device__ __forceinline__ LensGeom lens_geom(const LensBg64 &g, double z_mean, double mu,
+                                              double sep)
+{
+    LensGeom o;
+    const double chi_mean = spl_eval(g.chi_of_z, z_mean);
+    o.chi1 = chi_mean - sep * mu / 2.;
+    o.chi2 = chi_mean + sep * mu / 2.;
+    o.s = sep * sep * (1 - mu * mu) / (2. * chi_mean * chi_mean - mu * mu * sep * sep / 2.);
+    o.ct = 1 - o.s;
+    o.omc2 = o.s * (2 - o.s);
+    o.z1c = spl_eval(g.z_of_chi, o.chi1);
+    o.z2c = spl_eval(g.z_of_chi, o.chi2);
+    return o;
+}
+
+// float sums with Kahan compensation, double sums plain
+template <typename T> struct Acc {
+    T s = T(0), c = T(0);
+    __device__ __forceinline__ void add(T v)
+    {
+        if (sizeof(T) == 4) {
+            const T y = v - c;
+            const T t = s + y;
+            c = (t - s) - y;
+            s = t;
+        } else {
+            s += v;
+        }
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+template <typename T, typename S, typename TT>
+__global__ void __launch_bounds__(LENS_THREADS)
+    lens_double_kernel(LensArgs a, LensBg64 g64, LensBgT<S> gT, const TT *__restrict__ tab_x,
+                       const typename Rec4<TT>::type *__restrict__ rec,
+                       const int *__restrict__ req_spectrum, const double *__restrict__ req_z_mean,
+                       const int64_t *__restrict__ req_offset, const double *__restrict__ sep,
+                       const double *__restrict__ rule, double *__restrict__ part, int *err)
+{
+    __shared__ double red[LENS_THREADS / 32];
+    const long long item = blockIdx.x;
+    const long long pair = a.pair0 + item / a.n_mu;
+    const int im = (int)(item % a.n_mu);
+    const int q = lens_find_request(req_offset, a.n_req, pair);
+    const int s = req_spectrum[q];
+    const double *xf = rule + 2 * a.n_mu, *wf = xf + a.n_x, *xh = wf + a.n_x, *wh = xh + a.nh;
+    const double mu = rule[im];
+    const LensGeom G = lens_geom(g64, req_z_mean[q], mu, sep[pair]);
+    const double s1 = a.has_s1 ? spl_eval(g64.s1, G.z1c) : 0.0;
+    const double s2 = a.has_s2 ? spl_eval(g64.s2, G.z2c) : 0.0;
+    const double pre = 9. * a.Om * a.Om * (2 - 5 * s1) * (2 - 5 * s2) / 4. * G.chi1 * G.chi2 * a.pref4;
+    const typename Rec4<TT>::type *recs = rec + (size_t)s * (a.tab_len - 1) * LENS_NT;
+    const T chi1 = (T)G.chi1, chi2 = (T)G.chi2, ss = (T)G.s, ct = (T)G.ct, c2m = (T)(-G.omc2);
+    const T i11_0 = (T)lens_at_zero<TT>(recs, L11);
+    const TT inv_dlog = (TT)a.inv_dlog;
+    Acc<T> acc;
+    for (int ia = threadIdx.x; ia < a.n_x; ia += blockDim.x) {
+        const double x1d = 0.5 * (xf[ia] + 1.0);
+        const T x1 = (T)x1d;
+        const T l1 = chi1 * x1;
+        const T z1 = spl_eval(gT.z_of_chi, l1);
+        const T g1 = spl_eval(gT.D1, z1) / spl_eval(gT.a, z1) * (T(1) - x1);
+        const double xs = x1d * G.chi1 / G.chi2;
+        const bool split = a.nh > 0 && xs > 0 && xs < 1;
+        T line = T(0);
+        for (int p = 0; p < (split ? 2 : 1); ++p) {
+            const double lo = (split && p) ? xs : 0.0, hi = (split && !p) ? xs : 1.0;
+            const double c = 0.5 * (lo + hi), hw = 0.5 * (hi - lo);
+            const int np = split ? a.nh : a.n_x;
+            const double *gx = split ? xh : xf, *gw = split ? wh : wf;
+            Acc<T> pa;
+            for (int k = 0; k < np; ++k) {
+                const T x2 = (T)(c + hw * gx[k]);
+                const T l2 = chi2 * x2;
+                const T z2 = spl_eval(gT.z_of_chi, l2);
+                const T g2 = spl_eval(gT.D1, z2) / spl_eval(gT.a, z2) * (T(1) - x2);
+                const T ll = l1 * l2;
+                const T dl = l1 - l2;
+                const T r2 = dl * dl + T(2) * ll * ss;
+                T v;
+                if (r2 > T(1e-20)) {
+                    T I[LENS_NT];
+                    lens_tables<T, TT>(recs, tab_x, a.tab_len, inv_dlog, sqrt(r2), I);
+                    // functions.c:3695-3775
+                    v = T(2) * c2m * ll * I[L00] / T(5) + T(4) * ct * I[L20] / T(3) +
+                        T(4) * ct * (r2 + T(6) * ct * ll) * I[L11] / T(15) +
+                        T(2) * c2m * ll * (T(2) * r2 + T(3) * ct * ll) * I[L02] / T(7) / r2 +
+                        T(2) * ct * (T(2) * r2 * r2 + T(12) * ct * r2 * ll + T(15) * c2m * ll * ll) *
+                            I[L13] / T(15) / r2 +
+                        c2m * ll * (T(6) * r2 * r2 + T(30) * ct * r2 * ll + T(35) * c2m * ll * ll) *
+                            I[L04] / T(35) / r2 / r2;
+                } else {
+                    // functions.c:3801-3833
+                    v = T(4) + T(24) * ll * i11_0 / T(15);
+                }
+                pa.add((T)gw[k] * g2 * v);
+            }
+            line += (T)hw * (T)pa.value();
+        }
+        acc.add((T)(0.5 * wf[ia]) * g1 * line);
+    }
+    double tot = warp_sum(acc.value());
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = tot;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        const double res = pre * t;
+        if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
+        part[item] = res;
+    }
+}
+
+// den-len + rsd-len at (mu, x) in FP64 (functions.c:1557-2483), per side:
+// "2" = lensing to chi2 correlated with the local term at chi1, "1" = mirror
+template <typename TT>
+__device__ double lens_single_xi(const LensArgs &a, const LensBg64 &g,
+                                 const typename Rec4<TT>::type *__restrict__ recs,
+                                 const TT *__restrict__ tab_x, const LensGeom &G, double x,
+                                 double b1, double b2, double s1, double s2, double f1c,
+                                 double f2c, double D1z1c, double D1z2c, double mu)
+{
+    const double chi1 = G.chi1, chi2 = G.chi2, ct = G.ct, omc2 = G.omc2;
+    const double lambda1 = chi1 * x, lambda2 = chi2 * x;
+    double r21 = (lambda2 - chi1) * (lambda2 - chi1) + 2 * chi1 * lambda2 * G.s;
+    double r22 = (lambda1 - chi2) * (lambda1 - chi2) + 2 * chi2 * lambda1 * G.s;
+    if (r21 < 0) r21 = 0;
+    if (r22 < 0) r22 = 0;
+    const double z1 = spl_eval(g.z_of_chi, lambda1), z2 = spl_eval(g.z_of_chi, lambda2);
+    const double D1z1 = spl_eval(g.D1, z1), D1z2 = spl_eval(g.D1, z2);
+    const double az1 = spl_eval(g.a, z1), az2 = spl_eval(g.a, z2);
+    const TT inv_dlog = (TT)a.inv_dlog;
+    double I1[LENS_NT], I2[LENS_NT];
+    lens_tables<double, TT>(recs, tab_x, a.tab_len, inv_dlog, sqrt(r21), I1);
+    lens_tables<double, TT>(recs, tab_x, a.tab_len, inv_dlog, sqrt(r22), I2);
+    const double I00_0 = (double)lens_at_zero<TT>(recs, L00);
+    const double I11_0 = (double)lens_at_zero<TT>(recs, L11);
+    double result = 0;
+    if (a.contrib & COFFE_GPU_DEN) {
+        double t1, t2;
+        if (r21 != 0.0)
+            t1 = chi2 * (2 * chi1 * ct * I1[L11] - chi1 * chi1 * lambda2 * omc2 * I1[L02] / r21);
+        else
+            t1 = chi2 * 2 * chi1 * I11_0;
+        if (r22 != 0.0)
+            t2 = chi1 * (2 * chi2 * ct * I2[L11] - chi2 * chi2 * lambda1 * omc2 * I2[L02] / r22);
+        else
+            t2 = chi1 * 2 * chi2 * I11_0;
+        result += a.pref2 * (-3 * a.Om / 2. *
+                             (b1 * (2 - 5 * s2) * D1z1c * (1 - x) * D1z2 / az2 * t1 +
+                              b2 * (2 - 5 * s1) * D1z2c * (1 - x) * D1z1 / az1 * t2));
+    }
+    if (a.contrib & COFFE_GPU_RSD) {
+        const double c2m1 = 2 * ct * ct - 1;
+        // I00/I02 part (functions.c:2174-2183) and I04 part (2298-2306) of one
+        // side.  The polynomials multiplying I02 / r^2 and I04 / r^4 vanish like
+        // r^2 and r^4; written, as in the reference, in chi, lambda and
+        // cos(theta) they cancel up to ~10 digits, so they are expanded in
+        // d = chi - lambda and s = 1 - cos(theta) (the same polynomials), where
+        // every term has the size of the result.
+        const double ss = G.s;
+        auto Q = [&](double ch, double d) {
+            return d * d * d * (8 - 24 * ss + 12 * ss * ss) +
+                   ch * d * d * (-2 + 38 * ss - 18 * ss * ss - 6 * ss * ss * ss) +
+                   ch * ch * d * ss * (-22 + 9 * ss + 12 * ss * ss) +
+                   ch * ch * ch * ss * (2 - 3 * ss - 6 * ss * ss);
+        };
+        auto P = [&](double ch, double d) {
+            const double d2 = d * d, d3 = d2 * d, d4 = d2 * d2, d5 = d4 * d;
+            const double ch2 = ch * ch, ch3 = ch2 * ch, ch4 = ch2 * ch2, ch5 = ch4 * ch;
+            const double s2 = ss * ss, s3 = s2 * ss;
+            return d5 * (4 - 12 * ss + 6 * s2) + ch * d4 * (-8 + 60 * ss - 48 * s2 + 6 * s3) +
+                   ch2 * d3 * ss * (-92 + 114 * ss - 20 * s2 - s3) +
+                   ch3 * d2 * ss * (48 - 120 * ss + 26 * s2 + 3 * s3) +
+                   ch4 * d * s2 * (60 - 16 * ss - 3 * s2) + ch5 * s2 * (-12 + 4 * ss + s2);
+        };
+        auto A = [&](double ch, double la, const double *I, double r2) {
+            return (la - 6 * ch * ct + 3 * la * c2m1) * I[L00] / 15. -
+                   Q(ch, ch - la) * I[L02] / r2 / 21.;
+        };
+        auto B = [&](double ch, double la, const double *I, double r2) {
+            return -P(ch, ch - la) * I[L04] / r2 / r2 / 35.;
+        };
+        const double w2 = chi2 * f1c * (2 - 5 * s2) * D1z1c * D1z2 / az2;
+        const double w1 = chi1 * f2c * (2 - 5 * s1) * D1z2c * D1z1 / az1;
+        const double c = a.pref2 * 3 * a.Om / 2.;
+        if (r21 != 0 && r22 != 0) {
+            result += c * (w2 * (1 - x) * A(chi1, lambda2, I1, r21) +
+                           w1 * (1 - x) * A(chi2, lambda1, I2, r22));
+            if (fabs(mu) < 0.999)
+                result += c * (w2 * (1 - x) * B(chi1, lambda2, I1, r21) +
+                               w1 * (1 - x) * B(chi2, lambda1, I2, r22));
+            else
+                result += c * (w2 * (1 - x) * 4. * (lambda2 + chi1) * I1[L04] / 35. +
+                               w1 * (1 - x) * 4. * (lambda1 + chi2) * I2[L04] / 35.);
+        } else if (r21 == 0 && r22 != 0) {
+            result += c * (w2 * (1 - chi1 / chi2) * (-2 * chi1 * I00_0 / 15.) +
+                           w1 * (1 - x) * (A(chi2, lambda1, I2, r22) + B(chi2, lambda1, I2, r22)));
+        } else if (r21 != 0 && r22 == 0) {
+            result += c * (w2 * (1 - x) * (A(chi1, lambda2, I1, r21) + B(chi1, lambda2, I1, r21)) +
+                           w1 * (1 - chi2 / chi1) * (-2 * chi2 * I00_0 / 15.));
+        } else {
+            result += c * (w2 * (1 - chi1 / chi2) * (-2 * chi1 * I00_0 / 15.) +
+                           w1 * (1 - chi2 / chi1) * (-2 * chi2 * I00_0 / 15.));
+        }
+    }
+    return result;
+}
+
+template <typename TT>
+__global__ void __launch_bounds__(LENS_THREADS)
+    lens_single_kernel(LensArgs a, LensBg64 g, const TT *__restrict__ tab_x,
+                       const typename Rec4<TT>::type *__restrict__ rec,
+                       const int *__restrict__ req_spectrum, const double *__restrict__ req_z_mean,
+                       const int64_t *__restrict__ req_offset, const double *__restrict__ sep,
+                       const double *__restrict__ rule, double *__restrict__ part, int *err)
+{
+    const long long item = (long long)blockIdx.x * (LENS_THREADS / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (item >= a.n_items) return;
+    const long long pair = a.pair0 + item / a.n_mu;
+    const int im = (int)(item % a.n_mu);
+    const int q = lens_find_request(req_offset, a.n_req, pair);
+    const int s = req_spectrum[q];
+    const double *xf = rule + 2 * a.n_mu, *wf = xf + a.n_x, *xh = wf + a.n_x, *wh = xh + a.nh;
+    const double mu = rule[im];
+    const LensGeom G = lens_geom(g, req_z_mean[q], mu, sep[pair]);
+    const double b1 = a.has_b1 ? spl_eval(g.b1, G.z1c) : 1.0;
+    const double b2 = a.has_b2 ? spl_eval(g.b2, G.z2c) : 1.0;
+    const double s1 = a.has_s1 ? spl_eval(g.s1, G.z1c) : 0.0;
+    const double s2 = a.has_s2 ? spl_eval(g.s2, G.z2c) : 0.0;
+    const double f1c = spl_eval(g.f, G.z1c), f2c = spl_eval(g.f, G.z2c);
+    const double D1z1c = spl_eval(g.D1, G.z1c), D1z2c = spl_eval(g.D1, G.z2c);
+    const typename Rec4<TT>::type *recs = rec + (size_t)s * (a.tab_len - 1) * LENS_NT;
+    const double xs = fmin(G.chi1, G.chi2) * G.ct / fmax(G.chi1, G.chi2);
+    const bool split = a.nh > 0 && xs > 0 && xs < 1;
+    double sum = 0;
+    for (int p = 0; p < (split ? 2 : 1); ++p) {
+        const double lo = (split && p) ? xs : 0.0, hi = (split && !p) ? xs : 1.0;
+        const double c = 0.5 * (lo + hi), hw = 0.5 * (hi - lo);
+        const int np = split ? a.nh : a.n_x;
+        const double *gx = split ? xh : xf, *gw = split ? wh : wf;
+        double ps = 0;
+        for (int k = lane; k < np; k += 32)
+            ps += gw[k] * lens_single_xi<TT>(a, g, recs, tab_x, G, c + hw * gx[k], b1, b2, s1, s2,
+                                             f1c, f2c, D1z1c, D1z2c, mu);
+        sum += hw * warp_sum(ps);
+    }
+    if (lane == 0) {
+        if (!isfinite(sum)) cg_flag(err, CG_ERR_NONFINITE);
+        part[item] = sum;
+    }
+}
+
+__device__ __forceinline__ double lens_legendre(int l, double x)
+{
+    if (l == 0) return 1.0;
+    if (l == 1) return x;
+    double p0 = 1.0, p1 = x;
+    for (int k = 2; k <= l; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / (double)k;
+        p0 = p1;
+        p1 = p2;
+    }
+    return p1;
+}
+
+// out[pair][j] += (2l+1) sum_mu (w_mu / 2) P_l(mu) (single + double partials)
+__global__ void lens_reduce_kernel(LensArgs a, const double *__restrict__ rule,
+                                   const double *__restrict__ part_d,
+                                   const double *__restrict__ part_s, long long n_pairs,
+                                   double *__restrict__ out, int *err)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_pairs * a.n_l) return;
+    const long long pl = t / a.n_l;
+    const int j = (int)(t % a.n_l);
+    const int l = a.ls[j];
+    double sum = 0;
+    for (int im = 0; im < a.n_mu; ++im) {
+        double v = 0;
+        if (part_d) v += part_d[pl * a.n_mu + im];
+        if (part_s) v += part_s[pl * a.n_mu + im];
+        sum += 0.5 * rule[a.n_mu + im] * v * lens_legendre(l, rule[im]);
+    }
+    const double res = (2 * l + 1) * sum;
+    if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
+    out[(a.pair0 + pl) * a.n_l + j] += res;
+}
+
+// n-point Gauss-Legendre nodes and weights on [-1, 1] (Newton on P_n from the
+// Tricomi initial guesses), nodes ascending
+void gauss_legendre(int n, double *x, double *w)
+{
+    for (int i = 0; i < (n + 1) / 2; ++i) {
+        double z = cos(CG_PI * (i + 0.75) / (n + 0.5));
+        double dp = 0.0;
+        for (int it = 0; it < 100; ++it) {
+            double p1 = 1.0, p2 = 0.0;
+            for (int j = 1; j <= n; ++j) {
+                const double p3 = p2;
+                p2 = p1;
+                p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+            }
+            dp = n * (z * p1 - p2) / (z * z - 1.0);
+            const double z1 = z;
+            z = z1 - p1 / dp;
+            if (fabs(z - z1) <= 1e-15) break;
+        }
+        x[i] = -z;
+        x[n - 1 - i] = z;
+        w[i] = w[n - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+}
+
+template <typename T, typename S, typename TT>
+int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const LensBgT<S> &gT,
+                   const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
+                   const double *sep, double *out, long long total)
+{
+    typedef typename Rec4<TT>::type R;
+    int st;
+    const TT *tab_x = (const TT *)(sizeof(TT) == 8 ? ctx->tab_x.p : ctx->tab_x32.p);
+    const long long n_rec = (long long)ctx->n_spectra * (a.tab_len - 1) * LENS_NT;
+    if ((st = cg_ensure(ctx, ctx->lens_rec, sizeof(R) * (size_t)n_rec))) return st;
+    R *rec = (R *)ctx->lens_rec.p;
+    lens_records_kernel<TT><<<(unsigned)((n_rec + 255) / 256), 256, 0, ctx->stream>>>(
+        a, tab_x, (const TT *)ctx->tab_y.p, ctx->n_spectra, rec);
+    if ((st = cg_after_launch(ctx, "lens_records_kernel"))) return st;
+    const bool single = (a.contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD)) != 0;
+    // pairs per chunk: partials of at most 2^22 (pair, mu) items per kind
+    const long long chunk = std::max(1LL, std::min(total, (1LL << 22) / a.n_mu));
+    if ((st = cg_ensure(ctx, ctx->lens_part, sizeof(double) * 2 * (size_t)(chunk * a.n_mu))))
+        return st;
+    double *part_d = (double *)ctx->lens_part.p;
+    double *part_s = part_d + chunk * a.n_mu;
+    const double *rule = (const double *)ctx->lens_rule.p;
+    for (long long p0 = 0; p0 < total; p0 += chunk) {
+        const long long np = std::min(chunk, total - p0);
+        a.pair0 = p0;
+        a.n_items = np * a.n_mu;
+        lens_double_kernel<T, S, TT><<<(unsigned)a.n_items, LENS_THREADS, 0, ctx->stream>>>(
+            a, g64, gT, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule, part_d,
+            ctx->d_err);
+        if ((st = cg_after_launch(ctx, "lens_double_kernel"))) return st;
+        if (single) {
+            const long long blocks = (a.n_items + LENS_THREADS / 32 - 1) / (LENS_THREADS / 32);
+            lens_single_kernel<TT><<<(unsigned)blocks, LENS_THREADS, 0, ctx->stream>>>(
+                a, g64, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule, part_s,
+                ctx->d_err);
+            if ((st = cg_after_launch(ctx, "lens_single_kernel"))) return st;
+        }
+        const long long nt = np * a.n_l;
+        lens_reduce_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, ctx->stream>>>(
+            a, rule, part_d, single ? part_s : nullptr, np, out, ctx->d_err);
+        if ((st = cg_after_launch(ctx, "lens_reduce_kernel"))) return st;
+    }
+    return COFFE_GPU_OK;
+}
+
+} // namespace
+
+// Adds the lensing terms (contrib & COFFE_GPU_LEN) to out; the arguments are
+// those multipoles_run has validated, all arrays on the device.
+int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,
+                const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
+                const double *sep, int n_l, const int *l, double *out, long long total)
+{
+    if (!(contrib & COFFE_GPU_LEN) || total <= 0) return COFFE_GPU_OK;
+    if (!ctx->int_small_r) {
+        cg_set_error(ctx, "multipoles: lensing needs the r = 0 and sub-Mpc table entries "
+                          "(integrals_init with COFFE_GPU_SMALL_R)");
+        return COFFE_GPU_ESTATE;
+    }
+    LensArgs a;
+    const int want[LENS_NT][2] = {{0, 0}, {0, 2}, {0, 4}, {1, 1}, {1, 3}, {2, 0}};
+    for (int t = 0; t < LENS_NT; ++t) {
+        a.term[t] = -1;
+        for (int k = 0; k < ctx->n_terms; ++k)
+            if (ctx->term_n[k] == want[t][0] && ctx->term_l[k] == want[t][1]) a.term[t] = k;
+        if (a.term[t] < 0) {
+            cg_set_error(ctx, "multipoles: lensing needs the integral (n=%d, l=%d)", want[t][0],
+                         want[t][1]);
+            return COFFE_GPU_ESTATE;
+        }
+    }
+    a.n_req = n_req;
+    a.n_l = n_l;
+    a.n_mu = ctx->lens_n_mu;
+    a.n_x = ctx->lens_n_x;
+    a.nh = (a.n_x % 2 == 0) ? a.n_x / 2 : 0;
+    a.contrib = contrib;
+    a.tab_len = (int)(ctx->N + CG_N_SMALL_R + 1);
+    a.n_terms = ctx->n_terms;
+    a.inv_dlog = (double)ctx->N / log(ctx->kmax / ctx->kmin);
+    a.Om = ctx->Omega0_m;
+    a.pref2 = pow(CG_H0 * ctx->h, 2);
+    a.pref4 = pow(CG_H0 * ctx->h, 4);
+    a.has_b1 = ctx->bias_set[0];
+    a.has_b2 = ctx->bias_set[1];
+    a.has_s1 = ctx->bias_set[2];
+    a.has_s2 = ctx->bias_set[3];
+    a.pair0 = 0;
+    a.n_items = 0;
+    for (int i = 0; i < 8; ++i) a.ls[i] = i < n_l ? l[i] : 0;
+    int st;
+    // the Gauss-Legendre rule: mu[n_mu], w_mu[n_mu], x[n_x], w_x[n_x], x_h[nh], w_h[nh]
+    if (ctx->lens_rule_mu != a.n_mu || ctx->lens_rule_x != a.n_x) {
+        std::vector<double> r(2 * (size_t)a.n_mu + 2 * (size_t)a.n_x + 2 * (size_t)a.nh);
+        gauss_legendre(a.n_mu, r.data(), r.data() + a.n_mu);
+        gauss_legendre(a.n_x, r.data() + 2 * a.n_mu, r.data() + 2 * a.n_mu + a.n_x);
+        if (a.nh)
+            gauss_legendre(a.nh, r.data() + 2 * a.n_mu + 2 * a.n_x,
+                           r.data() + 2 * a.n_mu + 2 * a.n_x + a.nh);
+        if ((st = cg_ensure(ctx, ctx->lens_rule, sizeof(double) * r.size()))) return st;
+        CG_CUDA(ctx, cudaMemcpyAsync(ctx->lens_rule.p, r.data(), sizeof(double) * r.size(),
+                                     cudaMemcpyHostToDevice, ctx->stream));
+        CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream)); // r is a host temporary
+        ctx->lens_rule_mu = a.n_mu;
+        ctx->lens_rule_x = a.n_x;
+    }
+    LensBg64 g64;
+    g64.chi_of_z = ctx->bg[BG_CHI_OF_Z].v64();
+    g64.z_of_chi = ctx->bg[BG_Z_OF_CHI].v64();
+    g64.D1 = ctx->bg[BG_D1].v64();
+    g64.f = ctx->bg[BG_F].v64();
+    g64.a = ctx->bg[BG_A].v64();
+    g64.b1 = ctx->bias[0].v64();
+    g64.b2 = ctx->bias[1].v64();
+    g64.s1 = ctx->bias[2].v64();
+    g64.s2 = ctx->bias[3].v64();
+    if (precision == COFFE_GPU_MIXED) {
+        LensBgT<Spl32> gT{ctx->bg[BG_Z_OF_CHI].v32(), ctx->bg[BG_D1].v32(), ctx->bg[BG_A].v32()};
+        return lensing_launch<float, Spl32, float>(ctx, a, g64, gT, req_spectrum, req_z_mean,
+                                                   req_offset, sep, out, total);
+    }
+    LensBgT<Spl64> gT{ctx->bg[BG_Z_OF_CHI].v64(), ctx->bg[BG_D1].v64(), ctx->bg[BG_A].v64()};
+    return lensing_launch<double, Spl64, double>(ctx, a, g64, gT, req_spectrum, req_z_mean,
+                                                 req_offset, sep, out, total);
+}

@@ -677,6 +677,11 @@ int multipoles_prepare_background(coffe_gpu_ctx *ctx)
     return COFFE_GPU_OK;
 }
 
+static int multipoles_nonintegrated(coffe_gpu_ctx *ctx, const MpArgs &a, int precision,
+                                    const int *req_spectrum, const double *req_z_mean,
+                                    const int64_t *req_offset, const double *sep, double *out,
+                                    long long total);
+
 int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, int n_req,
                    const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
                    const double *sep, int n_l, const int *l, double *out, long long total)
@@ -699,8 +704,8 @@ int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel
                      ctx->int_precision);
         return COFFE_GPU_EINVAL;
     }
-    if (!(contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD)) || (contrib & ~7)) {
-        cg_set_error(ctx, "multipoles: contrib must select den and/or rsd");
+    if (!(contrib & 7) || (contrib & ~7)) {
+        cg_set_error(ctx, "multipoles: contrib must select den, rsd and/or len");
         return COFFE_GPU_EINVAL;
     }
     if (!(epsrel > 0)) {
@@ -742,8 +747,27 @@ int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel
     if (ctx->sm_count <= 0)
         CG_CUDA(ctx, cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount,
                                             ctx->device));
+    if (!(contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD))) {
+        // lensing only: no nonintegrated terms (signal.c:472-520 returns 0)
+        CG_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(double) * (size_t)total * n_l, ctx->stream));
+        return lensing_run(ctx, contrib, precision, n_req, req_spectrum, req_z_mean, req_offset,
+                           sep, n_l, l, out, total);
+    }
     a.retry_cap = total * n_l;
     if ((st = cg_ensure(ctx, ctx->mp_retry, 256 + sizeof(int2) * (size_t)a.retry_cap))) return st;
+    if ((st = multipoles_nonintegrated(ctx, a, precision, req_spectrum, req_z_mean, req_offset,
+                                       sep, out, total)))
+        return st;
+    return lensing_run(ctx, contrib, precision, n_req, req_spectrum, req_z_mean, req_offset, sep,
+                       n_l, l, out, total);
+}
+
+// the den/rsd nonintegrated multipoles of a validated call
+static int multipoles_nonintegrated(coffe_gpu_ctx *ctx, const MpArgs &a, int precision,
+                                    const int *req_spectrum, const double *req_z_mean,
+                                    const int64_t *req_offset, const double *sep, double *out,
+                                    long long total)
+{
     if (precision == COFFE_GPU_MIXED) {
         Bg<float, Spl32> bg;
         bg.z_of_chi = ctx->bg[BG_Z_OF_CHI].v32();
@@ -1020,8 +1044,9 @@ extern "C" int coffe_gpu_multipoles_noalloc(coffe_gpu_ctx_t *ctx, int contrib, i
                      precision, ctx->int_precision);
         return COFFE_GPU_EINVAL;
     }
-    if (!(contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD)) || (contrib & ~7)) {
-        cg_set_error(ctx, "multipoles_noalloc: contrib must select den and/or rsd");
+    if (!(contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD)) || (contrib & ~3)) {
+        cg_set_error(ctx, "multipoles_noalloc: contrib must select den and/or rsd (the lensing "
+                          "terms need per-call buffers)");
         return COFFE_GPU_EINVAL;
     }
     if (!(epsrel > 0)) {

@@ -71,6 +71,20 @@ def cfg2():
     return dict(cosmo=c, k=k, pk=pk, terms=terms, N=16384, r_out=r_out)
 
 
+LENS_TERMS = ((0, 0), (0, 2), (0, 4), (1, 1), (1, 3), (2, 0))
+
+
+def cfg4():
+    """den+RSD+lensing multipoles l = 0,2,4,6 at z = 1.5 (delta z 0.2), 200
+    separations 20-300 Mpc/h, lensing by Gauss-Legendre 128 mu x 256 chi."""
+    c = Cosmo()
+    kh = k_grid_h(4096)
+    k, pk = to_internal(kh, bbks_pk(kh), c.h)
+    sep = np.linspace(20, 300, 200) / c.h
+    return dict(cosmo=c, k=k, pk=pk, z_mean=1.5, deltaz=0.2, sep=sep, ls=(0, 2, 4, 6),
+                terms=LENS_TERMS, rule=(128, 256))
+
+
 @dataclass
 class Batch:
     k: np.ndarray

@@ -171,14 +171,32 @@ int coffe_gpu_integral_eval(coffe_gpu_ctx_t *ctx, int spectrum, int term, const 
    521-542; functions.c:89-771), by adaptive GK61 QAG with relative tolerance
    `epsrel` (integration_1d_prec, default 1e-5, parser.c:769).
    The integrals (0,0), (0,2) and (0,4) must be among the terms.
+   With COFFE_GPU_LEN in `contrib` the full-sky lensing terms are added, as
+   coffe_multipoles_init adds the single- and double-integrated parts
+   (multipoles.c:100-130): den/rsd x lensing if den or rsd is selected
+   (functions.c:1486-2483) and lensing-lensing (functions.c:3460-3836), by the
+   Gauss-Legendre rule of coffe_gpu_set_lensing_rule.  They also need the
+   integrals (1,1), (1,3), (2,0) and tables built with COFFE_GPU_SMALL_R.
    precision: COFFE_GPU_FP64 follows the reference in FP64; COFFE_GPU_MIXED
-   evaluates the integrand in FP32 with compensated FP32 sums.
+   evaluates the integrand in FP32 with compensated FP32 sums (the
+   single-integrated lensing terms stay FP64: their RSD-lensing coefficients
+   cancel terms of size chi^5).
    All arrays are host pointers unless arrays_on_device != 0, in which case
    every array (including out) is a device pointer. */
 int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, double epsrel,
                          int n_req, const int *req_spectrum, const double *req_z_mean,
                          const int64_t *req_offset, const double *sep, int n_l,
                          const int *l, double *out, int arrays_on_device);
+
+/* Quadrature rule of the lensing terms (contrib & COFFE_GPU_LEN), which
+   replaces the reference's Cuhre cubature of the unit cube (common.c:1074-1110,
+   integration_bins evaluations at most): n_mu Gauss-Legendre nodes in
+   v (mu = 2v - 1) and n_x nodes per x line, split into two panels of n_x / 2 at
+   the line's integrand peak (n_x even).  The single-integrated den/rsd-lensing
+   terms (functions.c:1486-2483) use n_mu x n_x nodes, lensing-lensing
+   (functions.c:3460-3836) n_mu x n_x x n_x.  Defaults 128 and 256;
+   2 <= n_mu, n_x <= 4096. */
+int coffe_gpu_set_lensing_rule(coffe_gpu_ctx_t *ctx, int n_mu, int n_x);
 
 /* Stream-ordered variant of coffe_gpu_multipoles for device-resident
    requests: every array except `l` (host, n_l entries) is a device pointer,

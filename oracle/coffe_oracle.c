@@ -1216,19 +1216,29 @@ double or_xi_single_integrated(const or_model_t *m, int contrib, double z_mean, 
     if (contrib & OR_CONTRIB_RSD) {
         const double f1c = or_spline_eval(&m->f, z1c), f2c = or_spline_eval(&m->f, z2c);
         const double c2m1 = 2 * ct * ct - 1; /* cos(2 theta) */
-        /* I00/I02 part of one side (functions.c:2174-2183) */
+        /* I00/I02 part (functions.c:2174-2183) and I04 part (2298-2306) of one
+           side.  The reference's polynomials in (chi, lambda, cos theta) that
+           multiply I02 / r^2 and I04 / r^4 vanish like r^2 and r^4 and lose up
+           to ~10 digits to cancellation; they are expanded here in d = chi -
+           lambda and s = 1 - cos(theta) (identical polynomials), where every
+           term is of the size of the result. */
+#define OR_RL_Q(ch, d, ss)                                                                     \
+    ((d) * (d) * (d) * (8 - 24 * (ss) + 12 * (ss) * (ss)) +                                    \
+     (ch) * (d) * (d) * (-2 + 38 * (ss) - 18 * (ss) * (ss) - 6 * (ss) * (ss) * (ss)) +         \
+     (ch) * (ch) * (d) * (ss) * (-22 + 9 * (ss) + 12 * (ss) * (ss)) +                          \
+     (ch) * (ch) * (ch) * (ss) * (2 - 3 * (ss) - 6 * (ss) * (ss)))
+#define OR_RL_P(ch, d, ss)                                                                     \
+    (pow(d, 5) * (4 - 12 * (ss) + 6 * (ss) * (ss)) +                                           \
+     (ch) * pow(d, 4) * (-8 + 60 * (ss) - 48 * (ss) * (ss) + 6 * pow(ss, 3)) +                 \
+     pow(ch, 2) * pow(d, 3) * (ss) * (-92 + 114 * (ss) - 20 * (ss) * (ss) - pow(ss, 3)) +     \
+     pow(ch, 3) * pow(d, 2) * (ss) * (48 - 120 * (ss) + 26 * (ss) * (ss) + 3 * pow(ss, 3)) +  \
+     pow(ch, 4) * (d) * (ss) * (ss) * (60 - 16 * (ss) - 3 * (ss) * (ss)) +                     \
+     pow(ch, 5) * (ss) * (ss) * (-12 + 4 * (ss) + (ss) * (ss)))
 #define OR_RL_A(ch, la, sr, r2)                                                                \
     ((la - 6 * ch * ct + 3 * la * c2m1) * or_spline_eval(i00, sr) / 15. -                     \
-     (6 * ch * ch * ch * ct - ch * ch * la * (9 * ct * ct + 11) +                             \
-      ch * la * la * ct * (3 * c2m1 + 19) - 2 * la * la * la * (3 * c2m1 + 1)) *              \
-         or_spline_eval(i02, sr) / (r2) / 21.)
-        /* I04 part of one side (functions.c:2298-2306) */
+     OR_RL_Q(ch, (ch) - (la), g.s) * or_spline_eval(i02, sr) / (r2) / 21.)
 #define OR_RL_B(ch, la, sr, r2)                                                                \
-    (-(-4 * pow(ch, 5) * ct - pow(ch, 3) * pow(la, 2) * ct * (c2m1 + 7) +                      \
-       pow(ch, 2) * pow(la, 3) * (pow(ct, 4) + 12 * ct * ct - 21) -                            \
-       3 * ch * pow(la, 4) * ct * (c2m1 - 5) - pow(la, 5) * (3 * c2m1 + 1) +                   \
-       12 * pow(ch, 4) * la) *                                                                 \
-     or_spline_eval(i04, sr) / (r2) / (r2) / 35.)
+    (-OR_RL_P(ch, (ch) - (la), g.s) * or_spline_eval(i04, sr) / (r2) / (r2) / 35.)
         const double w2 = chi2 * f1c * (2 - 5 * s2) * D1z1c * D1z2 / az2; /* side at chi2 */
         const double w1 = chi1 * f2c * (2 - 5 * s1) * D1z2c * D1z1 / az1; /* side at chi1 */
         const double c = pref * 3 * Om / 2.;
@@ -1259,6 +1269,8 @@ double or_xi_single_integrated(const or_model_t *m, int contrib, double z_mean, 
         }
 #undef OR_RL_A
 #undef OR_RL_B
+#undef OR_RL_P
+#undef OR_RL_Q
     }
     return result;
 }

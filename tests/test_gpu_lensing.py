@@ -1,0 +1,130 @@
+"""GPU parity of the lensing terms (single-integrated den/rsd x lensing and the
+double-integrated lensing-lensing term) through the C ABI, against the CPU
+oracle with the same split Gauss-Legendre rule, and against the reference's
+golden multipoles.
+
+Tolerances: FP64 1e-10 relative, mixed 1e-4 relative, both with a floor of
+1e-3 of the largest |value| of the same multipole over the separations;
+golden values at the oracle's own golden-test tolerances.
+"""
+import numpy as np
+import pytest
+
+from conftest import H
+
+pytestmark = pytest.mark.gpu
+
+LENS_TERMS = [(0, 0), (0, 2), (0, 4), (1, 1), (1, 3), (2, 0)]
+DEN, RSD, LEN = 1, 2, 4
+
+
+def _rel(got, ref):
+    floor = 1e-3 * np.abs(ref).max(axis=0, keepdims=True)
+    return np.max(np.abs(got - ref) / np.maximum(np.abs(ref), floor))
+
+
+@pytest.fixture(scope="module")
+def lens_setup(oracle):
+    from coffe_gb300 import workloads
+
+    c = workloads.cfg1()
+    k, pk = c["k"], c["pk"]
+    bg = oracle.background_nodes(0.31, 0.05, 9e-5, H, 10000)
+    m = oracle.Model(bg, H, 0.31)
+    for n, l in LENS_TERMS:
+        x, y = oracle.integral_table(k, pk, n, l, 4096, with_small_r=True)
+        m.set_integral(n, l, x, y)
+    return k, pk, m
+
+
+def _gpu(ctx, k, pk, precision, sep, z, ls, contrib, rule):
+    ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+    ctx.integrals_init(k, pk[None, :], LENS_TERMS, N=4096, precision=precision, small_r=True)
+    ctx.set_lensing_rule(*rule)
+    return ctx.multipoles([0], [z], [0, len(sep)], sep, ls, contrib=contrib, precision=precision)
+
+
+@pytest.mark.parametrize("contrib", [LEN, DEN | LEN, RSD | LEN, DEN | RSD | LEN])
+def test_lensing_fp64_matches_oracle(gpu_ctx, lens_setup, contrib):
+    k, pk, m = lens_setup
+    sep = np.array([20.0, 55.0, 120.0, 300.0]) / H
+    ls = (0, 2, 4, 6)
+    rule = (16, 32)
+    got = _gpu(gpu_ctx, k, pk, "fp64", sep, 1.5, ls, contrib, rule)
+    ref = m.multipoles_lensing(contrib, 1.5, sep, ls, *rule)
+    if contrib & (DEN | RSD):
+        for j, l in enumerate(ls):
+            ref[:, j] += [m.multipole(contrib & 3, 1.5, r, l) for r in sep]
+    e = _rel(got, ref)
+    print("contrib", contrib, "fp64 max rel error", e)
+    assert e < 1e-10, e
+
+
+def test_lensing_mixed_close_to_oracle(gpu_ctx, lens_setup):
+    k, pk, m = lens_setup
+    sep = np.array([20.0, 55.0, 120.0, 300.0]) / H
+    ls = (0, 2, 4, 6)
+    rule = (16, 32)
+    got = _gpu(gpu_ctx, k, pk, "mixed", sep, 1.5, ls, DEN | RSD | LEN, rule)
+    ref = m.multipoles_lensing(DEN | RSD | LEN, 1.5, sep, ls, *rule)
+    for j, l in enumerate(ls):
+        ref[:, j] += [m.multipole(3, 1.5, r, l) for r in sep]
+    e = _rel(got, ref)
+    print("mixed max rel error", e)
+    assert e < 1e-4, e
+    # the lensing-lensing part alone (FP32 integrand, compensated sums)
+    got = _gpu(gpu_ctx, k, pk, "mixed", sep, 1.5, ls, LEN, rule)
+    ref = m.multipoles_lensing(LEN, 1.5, sep, ls, *rule)
+    e = _rel(got, ref)
+    print("mixed len-len max rel error", e)
+    assert e < 1e-4, e
+
+
+def test_lensing_full_rule_matches_oracle(gpu_ctx, lens_setup):
+    """The 128 mu x 256 x rule at two separations (8.4M len-len nodes each)."""
+    k, pk, m = lens_setup
+    sep = np.array([30.0, 200.0]) / H
+    ls = (0, 2, 4, 6)
+    for prec, tol in (("fp64", 1e-10), ("mixed", 1e-4)):
+        got = _gpu(gpu_ctx, k, pk, prec, sep, 1.5, ls, LEN | DEN | RSD, (128, 256))
+        ref = m.multipoles_lensing(LEN | DEN | RSD, 1.5, sep, ls, 128, 256)
+        for j, l in enumerate(ls):
+            ref[:, j] += [m.multipole(3, 1.5, r, l) for r in sep]
+        e = _rel(got, ref)
+        print(prec, "128x256 max rel error", e)
+        assert e < tol, (prec, e)
+
+
+def test_lensing_golden_through_gpu(gpu_ctx, golden, class_pk):
+    """The reference's len and std_len golden multipoles (z = 1, PkL_CLASS),
+    with the tolerances of the oracle's golden tests."""
+    k, pk = class_pk
+    gpu_ctx.background_init(0.3, 0.05, 9e-5, H, 10000)
+    gpu_ctx.integrals_init(k, pk[None, :], LENS_TERMS, N=8192, precision="fp64", small_r=True)
+    gpu_ctx.set_lensing_rule(128, 256)
+    sep = golden["len_multipoles0"][:, 0] / H
+    got = gpu_ctx.multipoles([0], [1.0], [0, len(sep)], sep, (0, 2, 4), contrib=LEN)
+    far = sep * H >= 100
+    for j, l in enumerate((0, 2, 4)):
+        ref = golden[f"len_multipoles{l}"][:, 1]
+        assert np.allclose(got[far, j], ref[far], rtol=2e-3), (l, got[:, j] / ref - 1)
+    got = gpu_ctx.multipoles([0], [1.0], [0, len(sep)], sep, (0, 2, 4), contrib=DEN | RSD | LEN)
+    for j, l in enumerate((0, 2, 4)):
+        ref = golden[f"std_len_multipoles{l}"][:, 1]
+        tol = 5e-4 if l < 4 else 2e-3
+        assert np.allclose(got[:, j], ref, rtol=tol), (l, got[:, j] / ref - 1)
+
+
+def test_lensing_needs_small_r_and_terms(gpu_ctx, lens_setup):
+    from coffe_gb300.api import CoffeGpuError
+
+    k, pk, _ = lens_setup
+    gpu_ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+    gpu_ctx.integrals_init(k, pk[None, :], LENS_TERMS, N=4096, precision="fp64", small_r=False)
+    with pytest.raises(CoffeGpuError) as ei:
+        gpu_ctx.multipoles([0], [1.0], [0, 1], [50.0], (0,), contrib=LEN)
+    assert ei.value.status == -5
+    gpu_ctx.integrals_init(k, pk[None, :], [(0, 0), (0, 2), (0, 4)], N=4096, precision="fp64")
+    with pytest.raises(CoffeGpuError) as ei:
+        gpu_ctx.multipoles([0], [1.0], [0, 1], [50.0], (0,), contrib=LEN)
+    assert ei.value.status == -5
