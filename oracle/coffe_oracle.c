@@ -1413,3 +1413,418 @@ int or_multipoles_lensing_batch(const or_model_t *m, int contrib, const double *
     (void)nthreads;
     return bad ? -1 : 0;
 }
+
+/* --------------------------------------------------------------- covariance
+ * Flat-sky Gaussian covariance of the multipoles (covariance.c:477-1103) with
+ * the double-Bessel integrals by 2D FFTLog (covariance.c:357-470,
+ * twobessel.c:16-122, utils.c:179-258) or by direct quadrature
+ * (covariance.c:305-341).
+ */
+
+/* (l1 l2 l3; 0 0 0)^2 by the closed form for even J = l1 + l2 + l3 (zero for
+   odd J or when the triangle condition fails) */
+static double w3j0_sq(int l1, int l2, int l3)
+{
+    const int J = l1 + l2 + l3;
+    if (J % 2 || l3 < abs(l1 - l2) || l3 > l1 + l2)
+        return 0.0;
+    const int g = J / 2;
+    /* log of [(J-2l1)! (J-2l2)! (J-2l3)! / (J+1)!] [g! / ((g-l1)! (g-l2)! (g-l3)!)]^2 */
+    const double lr = lgamma(J - 2. * l1 + 1) + lgamma(J - 2. * l2 + 1) + lgamma(J - 2. * l3 + 1) -
+                      lgamma(J + 2.) +
+                      2 * (lgamma(g + 1.) - lgamma(g - l1 + 1.) - lgamma(g - l2 + 1.) -
+                           lgamma(g - l3 + 1.));
+    return exp(lr);
+}
+
+/* int_{-1}^{1} P_n P_m P_a P_b dmu = 2 sum_L (2L+1) (n m L;000)^2 (a b L;000)^2
+   (coffe_legendre_integral, common.c:1370-1394) */
+double or_legendre_integral(int n, int m, int a, int b)
+{
+    if ((n + m + a + b) % 2 != 0)
+        return 0;
+    const int lo = abs(n - m) > abs(a - b) ? abs(n - m) : abs(a - b);
+    const int hi = n + m < a + b ? n + m : a + b;
+    double r = 0;
+    for (int L = lo; L <= hi; ++L)
+        r += (2. * L + 1) * w3j0_sq(n, m, L) * w3j0_sq(a, b, L);
+    return 2 * r;
+}
+
+/* g_l(eta) = exp(z ln 2 + lnGamma((l + z)/2) - lnGamma((3 + l - z)/2)),
+   z = nu + i eta (utils.c:212-221) */
+static void twob_gl(double l, double nu, double eta, double *gr, double *gi)
+{
+    double a_r, a_i, b_r, b_i;
+    or_lgamma_c((l + nu) / 2., eta / 2., &a_r, &a_i);
+    or_lgamma_c((3. + l - nu) / 2., -eta / 2., &b_r, &b_i);
+    const double er = nu * log(2.) + a_r - b_r, ei = eta * log(2.) + a_i - b_i;
+    *gr = exp(er) * cos(ei);
+    *gi = exp(er) * sin(ei);
+}
+
+static double twob_window(long t, long ncut)
+{
+    return (double)t / ncut - 1. / (2. * M_PI) * sin(2. * t * M_PI / ncut);
+}
+
+/* 2D FFTLog (two_sph_bessel, twobessel.c:16-122; C branch) of a kernel that
+   is diagonal in (k1, k2): fk1k2[i][j] = diag[i] delta_ij on the log grid k.
+   out[a * N + b] = result(r1[a], r2[b]), r[i] = 1 / k[N - 1 - i]. */
+int or_twobessel_diag(const double *k, const double *diag, size_t N, double l1, double l2,
+                      double nu1, double nu2, double c_window_width, double *r, double *out)
+{
+    if (N % 2)
+        return -1;
+    const long hN = (long)N / 2;
+    const double dlnk = log(k[1] / k[0]);
+    for (size_t i = 0; i < N; ++i)
+        r[i] = 1. / k[N - 1 - i];
+    const double kr = k[0] * r[0];
+    /* forward r2c 2D of the diagonal: out[m][n] = F[(m + n) mod N] */
+    double *Fr = (double *)malloc(sizeof(double) * N), *Fi = (double *)malloc(sizeof(double) * N);
+    double *Xr = (double *)malloc(sizeof(double) * N * (hN + 1));
+    double *Xi = (double *)malloc(sizeof(double) * N * (hN + 1));
+    if (!Fr || !Fi || !Xr || !Xi) {
+        free(Fr); free(Fi); free(Xr); free(Xi);
+        return -1;
+    }
+    for (size_t i = 0; i < N; ++i) {
+        Fr[i] = diag[i] / pow(k[i], nu1) / pow(k[i], nu2);
+        Fi[i] = 0;
+    }
+    or_fft(Fr, Fi, N, -1);
+    /* windows (c_window_2d, utils.c:235-258) */
+    const long nc1 = (long)(hN * c_window_width), nc2 = (long)(hN * c_window_width);
+    /* per-row and per-column factors (k0 r0)^(-+ i eta) g_l */
+    for (long m = 0; m < (long)N; ++m) {
+        const long mm = m <= hN ? m : (long)N - m;
+        const double eta_m = 2 * M_PI / dlnk / N * mm;
+        double g1r, g1i;
+        twob_gl(l1, nu1, eta_m, &g1r, &g1i);
+        /* (kr)^(-i eta) = exp(-i eta ln kr) */
+        double pr = cos(-eta_m * log(kr)), pi_ = sin(-eta_m * log(kr));
+        if (m > hN) { /* conj of the m <= N/2 factor */
+            pi_ = -pi_;
+            g1i = -g1i;
+        }
+        const double R_r = pr * g1r - pi_ * g1i, R_i = pr * g1i + pi_ * g1r;
+        double wr = 1.0;
+        if (m <= hN && hN - m <= nc1) wr = twob_window(hN - m, nc1);
+        if (m >= hN + 1 && m - hN - 1 <= nc1) wr = twob_window(m - hN - 1, nc1);
+        for (long n = 0; n <= hN; ++n) {
+            const double eta_n = 2 * M_PI / dlnk / N * n;
+            double g2r, g2i;
+            twob_gl(l2, nu2, eta_n, &g2r, &g2i);
+            const double qr = cos(-eta_n * log(kr)), qi = sin(-eta_n * log(kr));
+            const double C_r = qr * g2r - qi * g2i, C_i = qr * g2i + qi * g2r;
+            double wc = 1.0;
+            if (hN - n <= nc2) wc = twob_window(hN - n, nc2);
+            const long f = (m + n) % (long)N;
+            double vr = Fr[f] * wc * wr, vi = Fi[f] * wc * wr;
+            /* times C * R, then conjugated */
+            const double fr = C_r * R_r - C_i * R_i, fi = C_r * R_i + C_i * R_r;
+            const double tr = vr * fr - vi * fi, ti = vr * fi + vi * fr;
+            Xr[m * (hN + 1) + n] = tr;
+            Xi[m * (hN + 1) + n] = -ti;
+        }
+    }
+    free(Fr);
+    free(Fi);
+    /* c2r 2D: inverse c2c along m for every n, then c2r along n per row */
+    int bad = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(| : bad)
+#endif
+    for (long n = 0; n <= hN; ++n) {
+        double *cr = (double *)malloc(sizeof(double) * N), *ci = (double *)malloc(sizeof(double) * N);
+        if (!cr || !ci) { free(cr); free(ci); bad |= 1; continue; }
+        for (size_t m = 0; m < N; ++m) {
+            cr[m] = Xr[m * (hN + 1) + n];
+            ci[m] = Xi[m * (hN + 1) + n];
+        }
+        or_fft(cr, ci, N, +1);
+        for (size_t m = 0; m < N; ++m) {
+            Xr[m * (hN + 1) + n] = cr[m];
+            Xi[m * (hN + 1) + n] = ci[m];
+        }
+        free(cr);
+        free(ci);
+    }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(| : bad)
+#endif
+    for (long a = 0; a < (long)N; ++a) {
+        double *cr = (double *)malloc(sizeof(double) * N), *ci = (double *)malloc(sizeof(double) * N);
+        if (!cr || !ci) { free(cr); free(ci); bad |= 1; continue; }
+        /* Hermitian completion along n; c2r ignores Im of the n = 0, N/2 terms */
+        for (long n = 0; n <= hN; ++n) {
+            cr[n] = Xr[a * (hN + 1) + n];
+            ci[n] = (n == 0 || n == hN) ? 0.0 : Xi[a * (hN + 1) + n];
+        }
+        for (long n = hN + 1; n < (long)N; ++n) {
+            cr[n] = cr[N - n];
+            ci[n] = -ci[N - n];
+        }
+        or_fft(cr, ci, N, +1);
+        for (size_t b = 0; b < N; ++b)
+            out[a * N + b] = cr[b] * M_PI / (16. * N * N * pow(r[b], nu2) * pow(r[a], nu1));
+        free(cr);
+        free(ci);
+    }
+    free(Xr);
+    free(Xi);
+    return bad ? -1 : 0;
+}
+
+/* Bicubic interpolation on a rectilinear grid as gsl_interp2d_bicubic builds
+   it (covariance.c:445-464 via coffe_init_spline2d, common.c:579-613): partial
+   derivatives zx, zy, zxy at the knots from natural cubic splines (zx along x
+   per y row, zy along y per x column, zxy along y of zx), then the bicubic
+   Hermite patch of each cell.  z[j * nx + i] = f(x_i, y_j). */
+typedef struct {
+    size_t nx, ny;
+    const double *x, *y, *z;
+    double *zx, *zy, *zxy;
+} or_bicubic_t;
+
+static double cspline_node_deriv(const or_spline_t *s, size_t i)
+{
+    /* derivative of the natural cubic spline at knot i (gsl_spline_eval_deriv) */
+    if (i + 1 < s->n)
+        return s->b[i];
+    const size_t j = s->n - 2;
+    const double h = s->x[j + 1] - s->x[j];
+    return s->b[j] + 2 * s->c[j] * h + 3 * s->d[j] * h * h;
+}
+
+static int bicubic_init(or_bicubic_t *B, const double *x, const double *y, const double *z,
+                        size_t nx, size_t ny)
+{
+    B->nx = nx; B->ny = ny; B->x = x; B->y = y; B->z = z;
+    B->zx = (double *)malloc(sizeof(double) * nx * ny);
+    B->zy = (double *)malloc(sizeof(double) * nx * ny);
+    B->zxy = (double *)malloc(sizeof(double) * nx * ny);
+    if (!B->zx || !B->zy || !B->zxy)
+        return -1;
+    int bad = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(| : bad)
+#endif
+    for (long j = 0; j < (long)ny; ++j) {
+        or_spline_t s;
+        if (or_spline_init(&s, x, z + j * nx, nx, OR_CSPLINE)) { bad |= 1; continue; }
+        for (size_t i = 0; i < nx; ++i) B->zx[j * nx + i] = cspline_node_deriv(&s, i);
+        or_spline_free(&s);
+    }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(| : bad)
+#endif
+    for (long i = 0; i < (long)nx; ++i) {
+        double *col = (double *)malloc(sizeof(double) * ny), *colx = (double *)malloc(sizeof(double) * ny);
+        if (!col || !colx) { free(col); free(colx); bad |= 1; continue; }
+        for (size_t j = 0; j < ny; ++j) {
+            col[j] = z[j * nx + i];
+            colx[j] = B->zx[j * nx + i];
+        }
+        or_spline_t s, sx;
+        if (or_spline_init(&s, y, col, ny, OR_CSPLINE) || or_spline_init(&sx, y, colx, ny, OR_CSPLINE)) {
+            bad |= 1;
+        } else {
+            for (size_t j = 0; j < ny; ++j) {
+                B->zy[j * nx + i] = cspline_node_deriv(&s, j);
+                B->zxy[j * nx + i] = cspline_node_deriv(&sx, j);
+            }
+            or_spline_free(&s);
+            or_spline_free(&sx);
+        }
+        free(col);
+        free(colx);
+    }
+    return bad ? -1 : 0;
+}
+
+static void bicubic_free(or_bicubic_t *B)
+{
+    free(B->zx); free(B->zy); free(B->zxy);
+}
+
+static size_t grid_index(const double *x, size_t n, double v)
+{
+    /* x_i <= v < x_{i+1} (last interval for v == x_{n-1}) */
+    size_t lo = 0, hi = n - 1;
+    while (hi > lo + 1) {
+        const size_t mid = (lo + hi) / 2;
+        if (x[mid] > v) hi = mid; else lo = mid;
+    }
+    return lo;
+}
+
+static double bicubic_eval(const or_bicubic_t *B, double xv, double yv)
+{
+    if (!(xv >= B->x[0] && xv <= B->x[B->nx - 1] && yv >= B->y[0] && yv <= B->y[B->ny - 1]))
+        return NAN;
+    const size_t i = grid_index(B->x, B->nx, xv), j = grid_index(B->y, B->ny, yv);
+    const double dx = B->x[i + 1] - B->x[i], dy = B->y[j + 1] - B->y[j];
+    const double t = (xv - B->x[i]) / dx, u = (yv - B->y[j]) / dy;
+    /* cubic Hermite basis: value at 0 / 1, slope at 0 / 1 */
+    const double ht[2] = {(2 * t - 3) * t * t + 1, (3 - 2 * t) * t * t};
+    const double gt[2] = {((t - 2) * t + 1) * t, (t - 1) * t * t};
+    const double hu[2] = {(2 * u - 3) * u * u + 1, (3 - 2 * u) * u * u};
+    const double gu[2] = {((u - 2) * u + 1) * u, (u - 1) * u * u};
+    double v = 0;
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b) {
+            const size_t q = (j + b) * B->nx + (i + a);
+            v += B->z[q] * ht[a] * hu[b] + B->zx[q] * dx * gt[a] * hu[b] +
+                 B->zy[q] * dy * ht[a] * gu[b] + B->zxy[q] * dx * dy * gt[a] * gu[b];
+        }
+    return v;
+}
+
+/* covariance_integrate_fftlog (covariance.c:357-470): the 2D FFTLog of
+   diag(k^3 P(k)^power / dlnk) on N log-spaced k in [kmin, kmax), resampled by
+   bicubic interpolation at the separations: out[nsep * n + m] = value at
+   (sep[m], sep[n]).  P(k) through the Akima spline of (k, pk). */
+int or_covariance_fftlog(const double *k, const double *pk, size_t nk, int power, int l1, int l2,
+                         size_t N, const double *sep, size_t nsep, double kmin, double kmax,
+                         double *out)
+{
+    or_spline_t P;
+    if (or_spline_init(&P, k, pk, nk, OR_AKIMA))
+        return -1;
+    const double step = log(kmax / kmin) / N;
+    double *ks = (double *)malloc(sizeof(double) * N), *dg = (double *)malloc(sizeof(double) * N);
+    double *r = (double *)malloc(sizeof(double) * N), *res = (double *)malloc(sizeof(double) * N * N);
+    double *zt = (double *)malloc(sizeof(double) * N * N);
+    int st = -1;
+    if (ks && dg && r && res && zt) {
+        for (size_t i = 0; i < N; ++i) {
+            ks[i] = kmin * pow(kmax / kmin, (double)i / N);
+            dg[i] = pow(ks[i], 3) * pow(or_spline_eval(&P, ks[i]), power) / step;
+        }
+        st = or_twobessel_diag(ks, dg, N, l1, l2, 1.01, 1.01, 0.25, r, res);
+        if (!st) {
+            /* z(x = r1[a], y = r2[b]) at zt[b * N + a] (covariance.c:432-437) */
+            for (size_t a = 0; a < N; ++a)
+                for (size_t b = 0; b < N; ++b) zt[b * N + a] = res[a * N + b];
+            or_bicubic_t B;
+            st = bicubic_init(&B, r, r, zt, N, N);
+            if (!st)
+                for (size_t m = 0; m < nsep; ++m)
+                    for (size_t n = 0; n < nsep; ++n)
+                        out[nsep * n + m] = bicubic_eval(&B, sep[m], sep[n]);
+            bicubic_free(&B);
+        }
+    }
+    free(ks); free(dg); free(r); free(res); free(zt);
+    or_spline_free(&P);
+    return st;
+}
+
+/* direct double-Bessel integral (covariance_integral, covariance.c:305-341,
+   no window): 2/pi int_kmin^kmax k^2 P(k)^power j_l1(k r1) j_l2(k r2) dk */
+typedef struct {
+    const or_spline_t *P;
+    int power, l1, l2;
+    double r1, r2;
+} or_cov_par_t;
+
+static double cov_integrand(double kk, void *vp)
+{
+    const or_cov_par_t *p = (const or_cov_par_t *)vp;
+    return kk * kk * pow(or_spline_eval(p->P, kk), p->power) * or_sph_bessel(p->l1, kk * p->r1) *
+           or_sph_bessel(p->l2, kk * p->r2);
+}
+
+double or_covariance_integral(const double *k, const double *pk, size_t nk, int power, double r1,
+                              double r2, int l1, int l2, double kmin, double kmax, double epsrel,
+                              int power_of_spline)
+{
+    /* the reference's integrand reads an Akima spline of the node values
+       P^power (temp_spectrum_pk2, covariance.c:609-628); power_of_spline != 0
+       uses the power of the spline of P instead, as the FFTLog path samples it
+       (covariance.c:397-402) */
+    or_spline_t P;
+    double *pp = (double *)malloc(sizeof(double) * nk);
+    if (!pp)
+        return NAN;
+    for (size_t i = 0; i < nk; ++i) pp[i] = power_of_spline ? pk[i] : pow(pk[i], power);
+    const int bad = or_spline_init(&P, k, pp, nk, OR_AKIMA);
+    free(pp);
+    if (bad)
+        return NAN;
+    or_cov_par_t p = {&P, power_of_spline ? power : 1, l1, l2, r1, r2};
+    double err;
+    int status;
+    const double v = or_qag61(cov_integrand, &p, kmin, kmax, 0, epsrel, 50000, &err, &status);
+    or_spline_free(&P);
+    return 2 * v / M_PI;
+}
+
+static double cov_coeff(double b1, double b2, double f, int ell)
+{
+    /* covariance_coefficient, covariance.c:40-57 */
+    switch (ell) {
+    case 0: return b1 * b2 + (b1 + b2) * f / 3 + f * f / 5.;
+    case 2: return 2 * (b1 + b2) * f / 3. + 4 * f * f / 7.;
+    case 4: return 8 * f * f / 35.;
+    default: return 0;
+    }
+}
+
+static int isign(int m) { return abs(m) % 2 == 0 ? 1 : -1; }
+
+/* Multipole covariance (covariance.c:786-1059) for one population (all four
+   covariance_pop = 1, the defaults, parser.c:945-948), no window, linear P(k):
+   ipk / ipk2 hold the double-Bessel integrals I[l1][l2](r1 = sep[m],
+   r2 = sep[n]) at [(i * nl + j) * nsep * nsep + nsep * n + m] for ALL (i, j)
+   already multiplied by (2l1+1)(2l2+1) 2/pi^2 and (2l1+1)(2l2+1)/pi^2
+   (covariance.c:752-763, transposes 773-784).  out in (z, l1, r1, l2, r2)
+   order (covariance.c:1046-1059). */
+int or_covariance_multipoles(const or_model_t *mdl, int contrib, size_t nz, const double *z_mean,
+                             const double *deltaz, const double *fsky, const double *density,
+                             const double *pixelsize, size_t nl, const int *ls, size_t nsep,
+                             const double *sep, const double *ipk, const double *ipk2,
+                             double *out)
+{
+    size_t idx = 0;
+    for (size_t zk = 0; zk < nz; ++zk) {
+        const double z = z_mean[zk];
+        const double c1 = or_spline_eval(&mdl->chi_of_z, z - deltaz[zk]);
+        const double c2 = or_spline_eval(&mdl->chi_of_z, z + deltaz[zk]);
+        const double V = 4 * M_PI * fsky[zk] * (pow(c2, 3) - pow(c1, 3)) / 3.;
+        const double b = (contrib & OR_CONTRIB_DEN) ? bias_eval(mdl, 0, z, 1.0) : 0.0;
+        const double f = (contrib & OR_CONTRIB_RSD) ? or_spline_eval(&mdl->f, z) : 0.0;
+        const double D1 = or_spline_eval(&mdl->D1, z);
+        const double n1 = density[zk], n2 = density[zk];
+        for (size_t i = 0; i < nl; ++i)
+            for (size_t m = 0; m < nsep; ++m)
+                for (size_t j = 0; j < nl; ++j)
+                    for (size_t n = 0; n < nsep; ++n) {
+                        const int l1 = ls[i], l2 = ls[j];
+                        double cosmic = 0;
+                        for (int a = 0; a <= 4; a += 2)
+                            for (int bb = 0; bb <= 4; bb += 2)
+                                cosmic += (cov_coeff(b, b, f, a) * cov_coeff(b, b, f, bb) +
+                                           isign(bb) * cov_coeff(b, b, f, a) * cov_coeff(b, b, f, bb)) *
+                                          or_legendre_integral(l1, l2, a, bb);
+                        cosmic /= 4.;
+                        double mixed = 0;
+                        for (int a = 0; a <= 4; a += 2)
+                            mixed += (cov_coeff(b, b, f, a) / n2 + cov_coeff(b, b, f, a) / n1 +
+                                      cov_coeff(b, b, f, a) / n2 + cov_coeff(b, b, f, a) / n1) *
+                                     or_legendre_integral(l1, l2, a, 0);
+                        mixed /= 8.;
+                        const double pois = (l1 == l2 && m == n)
+                                                ? (2 * l1 + 1) / 4. / M_PI * (1 + isign(l2)) /
+                                                      sep[n] / sep[m] / pixelsize[zk] / n1 / n2 / V
+                                                : 0.0;
+                        const size_t q = (i * nl + j) * nsep * nsep + nsep * n + m;
+                        const double cm = isign((l2 - l1) / 2) * isign(l1 + l2) * D1 * D1 * ipk[q] * mixed / V;
+                        const double cc = isign((l2 - l1) / 2) * D1 * D1 * D1 * D1 * ipk2[q] * cosmic / V;
+                        out[idx++] = pois + cm + cc;
+                    }
+    }
+    return 0;
+}

@@ -151,6 +151,28 @@ int or_multipoles_lensing_batch(const or_model_t *m, int contrib, const double *
                                 const double *sep, size_t count, int n_l, const int *ls,
                                 size_t n_mu, size_t n_x, double *out, int nthreads);
 
+/* -------------------------------------------------------------- covariance */
+/* int P_n P_m P_a P_b dmu over [-1, 1] (common.c:1370-1394) */
+double or_legendre_integral(int n, int m, int a, int b);
+/* 2D FFTLog (twobessel.c:16-122) of a kernel diagonal in (k1, k2);
+   out[a * N + b] at (r[a], r[b]), r[i] = 1 / k[N - 1 - i] */
+int or_twobessel_diag(const double *k, const double *diag, size_t N, double l1, double l2,
+                      double nu1, double nu2, double c_window_width, double *r, double *out);
+/* covariance_integrate_fftlog (covariance.c:357-470); out[nsep * n + m] */
+int or_covariance_fftlog(const double *k, const double *pk, size_t nk, int power, int l1, int l2,
+                         size_t N, const double *sep, size_t nsep, double kmin, double kmax,
+                         double *out);
+/* covariance_integral without window (covariance.c:305-341) */
+double or_covariance_integral(const double *k, const double *pk, size_t nk, int power, double r1,
+                              double r2, int l1, int l2, double kmin, double kmax, double epsrel,
+                              int power_of_spline);
+/* multipole covariance assembly (covariance.c:786-1059), one population */
+int or_covariance_multipoles(const or_model_t *mdl, int contrib, size_t nz, const double *z_mean,
+                             const double *deltaz, const double *fsky, const double *density,
+                             const double *pixelsize, size_t nl, const int *ls, size_t nsep,
+                             const double *sep, const double *ipk, const double *ipk2,
+                             double *out);
+
 /* number of QAG subdivisions taken by the last or_multipole_nonintegrated call
    in this thread (diagnostic) */
 int or_last_qag_intervals(void);

@@ -90,6 +90,19 @@ def lib():
         L.or_xi_single_integrated.restype = C.c_double
         L.or_xi_double_integrated.argtypes = [C.c_void_p, C.c_int] + [C.c_double] * 5
         L.or_xi_double_integrated.restype = C.c_double
+        L.or_legendre_integral.argtypes = [C.c_int] * 4
+        L.or_legendre_integral.restype = C.c_double
+        L.or_twobessel_diag.argtypes = [_dp, _dp, C.c_size_t] + [C.c_double] * 5 + [_dp, _dp]
+        L.or_covariance_fftlog.argtypes = [_dp, _dp, C.c_size_t, C.c_int, C.c_int, C.c_int,
+                                           C.c_size_t, _dp, C.c_size_t, C.c_double, C.c_double,
+                                           _dp]
+        L.or_covariance_integral.argtypes = [_dp, _dp, C.c_size_t, C.c_int, C.c_double,
+                                             C.c_double, C.c_int, C.c_int, C.c_double,
+                                             C.c_double, C.c_double, C.c_int]
+        L.or_covariance_integral.restype = C.c_double
+        L.or_covariance_multipoles.argtypes = [C.c_void_p, C.c_int, C.c_size_t, _dp, _dp, _dp,
+                                               _dp, _dp, C.c_size_t, _ip, C.c_size_t, _dp, _dp,
+                                               _dp, _dp]
         L.or_multipoles_lensing_batch.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_size_t,
                                                   C.c_int, _ip, C.c_size_t, C.c_size_t, _dp,
                                                   C.c_int]
@@ -249,6 +262,63 @@ class Model:
                                              int(n_mu), int(n_x), out, int(nthreads)) != 0:
             raise MemoryError("lensing multipoles failed")
         return out
+
+
+    def covariance_multipoles(self, contrib, z_mean, deltaz, fsky, density, pixelsize, ls, sep,
+                              ipk, ipk2):
+        """Multipole covariance (z, l1, r1, l2, r2) from the double-Bessel
+        integrals ipk / ipk2 of shape (nl, nl, nsep(n), nsep(m))."""
+        z = _f64(np.atleast_1d(z_mean))
+        nz = len(z)
+        arr = [_f64(np.broadcast_to(np.asarray(a, dtype=np.float64), z.shape))
+               for a in (deltaz, fsky, density, pixelsize)]
+        la = np.ascontiguousarray(ls, dtype=np.int32)
+        sep = _f64(sep)
+        nl, ns = len(la), len(sep)
+        out = np.zeros(nz * nl * ns * nl * ns)
+        lib().or_covariance_multipoles(self._p, contrib, nz, z, *arr, nl, la, ns, sep,
+                                       _f64(ipk).ravel(), _f64(ipk2).ravel(), out)
+        return out.reshape(nz, nl, ns, nl, ns)
+
+
+def legendre_integral(n, m, a, b) -> float:
+    return lib().or_legendre_integral(n, m, a, b)
+
+
+def twobessel_diag(k, diag, l1, l2, nu1=1.01, nu2=1.01, c_window_width=0.25):
+    """2D FFTLog of a diagonal kernel; returns (r, out[a, b] at (r[a], r[b]))."""
+    k, diag = _f64(k), _f64(diag)
+    N = len(k)
+    r = np.zeros(N)
+    out = np.zeros((N, N))
+    if lib().or_twobessel_diag(k, diag, N, l1, l2, nu1, nu2, c_window_width, r, out) != 0:
+        raise ValueError("twobessel failed")
+    return r, out
+
+
+def covariance_fftlog(k, pk, power, l1, l2, N, sep, kmin=None, kmax=None):
+    """covariance_integrate_fftlog: array [n, m] at (sep[m], sep[n])."""
+    k, pk, sep = _f64(k), _f64(pk), _f64(sep)
+    kmin = float(k[0] if kmin is None else kmin)
+    kmax = float(k[-1] if kmax is None else kmax)
+    out = np.zeros((len(sep), len(sep)))
+    if lib().or_covariance_fftlog(k, pk, len(k), int(power), int(l1), int(l2), int(N), sep,
+                                  len(sep), kmin, kmax, out) != 0:
+        raise ValueError("covariance fftlog failed")
+    return out
+
+
+def covariance_integral(k, pk, power, r1, r2, l1, l2, kmin=None, kmax=None, epsrel=1e-5,
+                        power_of_spline=False):
+    """2/pi int k^2 P^power j_l1(k r1) j_l2(k r2) dk by QAG; P^power as the
+    reference's direct method splines it (Akima of the node values P^power),
+    or as the FFTLog path samples it (power of the Akima spline of P)."""
+    k, pk = _f64(k), _f64(pk)
+    kmin = float(k[0] if kmin is None else kmin)
+    kmax = float(k[-1] if kmax is None else kmax)
+    return lib().or_covariance_integral(k, pk, len(k), int(power), float(r1), float(r2), int(l1),
+                                        int(l2), kmin, kmax, float(epsrel),
+                                        int(bool(power_of_spline)))
 
 
 def last_qag_intervals() -> int:
