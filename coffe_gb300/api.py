@@ -254,6 +254,36 @@ class Context:
             P(req_z_mean, C.c_double), P(req_offset, C.c_int64), P(sep, C.c_double), len(la),
             _iptr(la), P(out, C.c_double)), "multipoles_noalloc")
 
+    # ------------------------------------------------------------ covariance
+    def covariance_integrals(self, k, pk, N, jobs, sep) -> np.ndarray:
+        """2D-FFTLog double-Bessel integrals for jobs (power, l1, l2); returns
+        (len(jobs), len(sep), len(sep)) with [q, n, m] at (r1 = sep[m], r2 = sep[n])."""
+        k, pk, sep = _f64(k), _f64(pk), _f64(sep)
+        p = np.ascontiguousarray([j[0] for j in jobs], dtype=np.int32)
+        a = np.ascontiguousarray([j[1] for j in jobs], dtype=np.int32)
+        b = np.ascontiguousarray([j[2] for j in jobs], dtype=np.int32)
+        out = np.zeros((len(jobs), len(sep), len(sep)))
+        self._check(self._L.coffe_gpu_covariance_integrals(
+            self._ctx, _dptr(k), _dptr(pk), len(k), int(N), len(jobs), _iptr(p), _iptr(a),
+            _iptr(b), _dptr(sep), len(sep), _dptr(out)), "covariance_integrals")
+        return out
+
+    def covariance_multipoles(self, k, pk, N, z_mean, deltaz, fsky, density1, density2,
+                              pixelsize, ls, sep, contrib=_lib.DEN | _lib.RSD) -> np.ndarray:
+        """Multipole covariance, shape (n_z, n_l, n_sep, n_l, n_sep) in the
+        reference's (z, l1, r1, l2, r2) order."""
+        k, pk, sep = _f64(k), _f64(pk), _f64(sep)
+        z = _f64(np.atleast_1d(z_mean))
+        per_z = [_f64(np.broadcast_to(np.asarray(v, dtype=np.float64), z.shape))
+                 for v in (deltaz, fsky, density1, density2, pixelsize)]
+        la = np.ascontiguousarray(ls, dtype=np.int32)
+        out = np.zeros((len(z), len(la), len(sep), len(la), len(sep)))
+        self._check(self._L.coffe_gpu_covariance_multipoles(
+            self._ctx, int(contrib), _dptr(k), _dptr(pk), len(k), int(N), len(z), _dptr(z),
+            *map(_dptr, per_z), len(la), _iptr(la), len(sep), _dptr(sep), _dptr(out)),
+            "covariance_multipoles")
+        return out
+
     def multipoles_device(self, req_spectrum, req_z_mean, req_offset, sep, ls, out,
                           contrib=_lib.DEN | _lib.RSD, precision="fp64", epsrel=1e-5):
         """Same as :meth:`multipoles` with CUDA tensors (int32, float64, int64,

@@ -92,6 +92,11 @@ struct coffe_gpu_ctx {
     int lens_rule_mu = 0, lens_rule_x = 0;
     DevBuf lens_rec;  // Akima records of the six lensing tables
     DevBuf lens_part; // per (pair, mu) partial integrals
+
+    // ---- covariance (covariance.cu)
+    SplineBuf cov_pk; // Akima spline of the covariance's P(k)
+    DevBuf cov_buf;   // FFTLog work arrays
+    DevBuf cov_out;   // integrals, assembly inputs and outputs
 };
 
 void cg_set_error(coffe_gpu_ctx *ctx, const char *fmt, ...);

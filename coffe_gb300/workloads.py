@@ -85,6 +85,27 @@ def cfg4():
                 terms=LENS_TERMS, rule=(128, 256))
 
 
+def cfg5(chi_of_z=None):
+    """Flat-sky Gaussian covariance of the l = 0,2,4 multipoles: 5 redshift bins
+    (z = 0.5..2.0, delta z 0.1), each of volume 1 (Gpc/h)^3, n = 1e-3 (h/Mpc)^3,
+    128 x 128 separations 20-300 Mpc/h, 2D FFTLog on 2^11 x 2^11 points.
+    chi_of_z (Mpc) fixes fsky from the volume; without it fsky is None."""
+    c = Cosmo()
+    kh = k_grid_h(4096)
+    k, pk = to_internal(kh, bbks_pk(kh), c.h)
+    z = np.linspace(0.5, 2.0, 5)
+    dz = np.full(5, 0.1)
+    sep = np.linspace(20, 300, 128) / c.h
+    fsky = None
+    if chi_of_z is not None:
+        vol = 1e9 / c.h ** 3  # (Gpc/h)^3 in Mpc^3
+        shell = 4 * np.pi * (chi_of_z(z + dz) ** 3 - chi_of_z(z - dz) ** 3) / 3
+        fsky = vol / shell
+    return dict(cosmo=c, k=k, pk=pk, z_mean=z, deltaz=dz, fsky=fsky,
+                density=np.full(5, 1e-3 * c.h ** 3), pixelsize=np.full(5, sep[1] - sep[0]),
+                sep=sep, ls=(0, 2, 4), N=2048)
+
+
 @dataclass
 class Batch:
     k: np.ndarray

@@ -246,6 +246,41 @@ int coffe_gpu_multipoles_noalloc(coffe_gpu_ctx_t *ctx, int contrib, int precisio
    No counterpart in the reference (its QAG keeps this count internal). */
 long long coffe_gpu_multipoles_retries(coffe_gpu_ctx_t *ctx);
 
+/* -------------------------------------------------------------- covariance */
+
+/* The double-Bessel integrals of the multipole covariance by 2D FFTLog, as
+   covariance_integrate_fftlog computes them (covariance.c:357-470 with
+   two_sph_bessel, twobessel.c:16-122; nu = 1.01, window 0.25): for each job q
+   the 2D FFTLog of diag(k^3 P(k)^power[q] / dlnk) on N log-spaced k in
+   [k[0], k[nk-1]) with multipoles l1[q], l2[q], resampled bicubically at the
+   separations:
+     out[q * n_sep^2 + n_sep * n + m] = value at (r1 = sep[m], r2 = sep[n])
+   (unscaled; coffe_covariance_init multiplies by (2l1+1)(2l2+1) 2/pi^2 or
+   /pi^2).  P(k) through the Akima spline of (k, pk); N a power of two in
+   [64, 8192]; separations inside [1/k(N-1), 1/k[0]].  Host arrays. */
+int coffe_gpu_covariance_integrals(coffe_gpu_ctx_t *ctx, const double *k, const double *pk,
+                                   size_t nk, size_t N, int n_jobs, const int *power,
+                                   const int *l1, const int *l2, const double *sep, int n_sep,
+                                   double *out);
+
+/* Replaces coffe_covariance_init (covariance.c:477-1103) for the multipole
+   covariance with covariance_integration_method = fftlog, one population
+   (covariance_pop1..4 = 1, the defaults), no window, linear P(k): the Poisson,
+   mixed and cosmic-variance terms for every redshift bin (z_mean, deltaz, fsky,
+   number densities density1/2, pixelsize), multipoles l[0..n_l-1] and
+   separations, in the reference's output order
+     out[(((z * n_l + i1) * n_sep + m) * n_l + i2) * n_sep + n]
+   = cov(z, l1 = l[i1], r1 = sep[m], l2 = l[i2], r2 = sep[n]) (covariance.c:
+   1046-1059).  Background from coffe_gpu_background_init/_set, galaxy bias 1
+   from coffe_gpu_set_bias (default 1).  contrib: den and/or rsd (bias or
+   growth rate zero otherwise, covariance.c:845-861).  Host arrays. */
+int coffe_gpu_covariance_multipoles(coffe_gpu_ctx_t *ctx, int contrib, const double *k,
+                                    const double *pk, size_t nk, size_t N, int n_z,
+                                    const double *z_mean, const double *deltaz,
+                                    const double *fsky, const double *density1,
+                                    const double *density2, const double *pixelsize, int n_l,
+                                    const int *l, int n_sep, const double *sep, double *out);
+
 /* Kernel launches issued by this context since creation (for accounting). */
 long long coffe_gpu_launch_count(const coffe_gpu_ctx_t *ctx);
 

@@ -1783,8 +1783,8 @@ static int isign(int m) { return abs(m) % 2 == 0 ? 1 : -1; }
    (covariance.c:752-763, transposes 773-784).  out in (z, l1, r1, l2, r2)
    order (covariance.c:1046-1059). */
 int or_covariance_multipoles(const or_model_t *mdl, int contrib, size_t nz, const double *z_mean,
-                             const double *deltaz, const double *fsky, const double *density,
-                             const double *pixelsize, size_t nl, const int *ls, size_t nsep,
+                             const double *deltaz, const double *fsky, const double *density1,
+                             const double *density2, const double *pixelsize, size_t nl, const int *ls, size_t nsep,
                              const double *sep, const double *ipk, const double *ipk2,
                              double *out)
 {
@@ -1797,7 +1797,7 @@ int or_covariance_multipoles(const or_model_t *mdl, int contrib, size_t nz, cons
         const double b = (contrib & OR_CONTRIB_DEN) ? bias_eval(mdl, 0, z, 1.0) : 0.0;
         const double f = (contrib & OR_CONTRIB_RSD) ? or_spline_eval(&mdl->f, z) : 0.0;
         const double D1 = or_spline_eval(&mdl->D1, z);
-        const double n1 = density[zk], n2 = density[zk];
+        const double n1 = density1[zk], n2 = density2[zk];
         for (size_t i = 0; i < nl; ++i)
             for (size_t m = 0; m < nsep; ++m)
                 for (size_t j = 0; j < nl; ++j)

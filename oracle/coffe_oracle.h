@@ -168,8 +168,8 @@ double or_covariance_integral(const double *k, const double *pk, size_t nk, int 
                               int power_of_spline);
 /* multipole covariance assembly (covariance.c:786-1059), one population */
 int or_covariance_multipoles(const or_model_t *mdl, int contrib, size_t nz, const double *z_mean,
-                             const double *deltaz, const double *fsky, const double *density,
-                             const double *pixelsize, size_t nl, const int *ls, size_t nsep,
+                             const double *deltaz, const double *fsky, const double *density1,
+                             const double *density2, const double *pixelsize, size_t nl, const int *ls, size_t nsep,
                              const double *sep, const double *ipk, const double *ipk2,
                              double *out);
 

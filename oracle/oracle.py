@@ -101,8 +101,8 @@ def lib():
                                              C.c_double, C.c_double, C.c_int]
         L.or_covariance_integral.restype = C.c_double
         L.or_covariance_multipoles.argtypes = [C.c_void_p, C.c_int, C.c_size_t, _dp, _dp, _dp,
-                                               _dp, _dp, C.c_size_t, _ip, C.c_size_t, _dp, _dp,
-                                               _dp, _dp]
+                                               _dp, _dp, _dp, C.c_size_t, _ip, C.c_size_t, _dp,
+                                               _dp, _dp, _dp]
         L.or_multipoles_lensing_batch.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_size_t,
                                                   C.c_int, _ip, C.c_size_t, C.c_size_t, _dp,
                                                   C.c_int]
@@ -265,13 +265,14 @@ class Model:
 
 
     def covariance_multipoles(self, contrib, z_mean, deltaz, fsky, density, pixelsize, ls, sep,
-                              ipk, ipk2):
+                              ipk, ipk2, density2=None):
         """Multipole covariance (z, l1, r1, l2, r2) from the double-Bessel
         integrals ipk / ipk2 of shape (nl, nl, nsep(n), nsep(m))."""
         z = _f64(np.atleast_1d(z_mean))
         nz = len(z)
         arr = [_f64(np.broadcast_to(np.asarray(a, dtype=np.float64), z.shape))
-               for a in (deltaz, fsky, density, pixelsize)]
+               for a in (deltaz, fsky, density, density if density2 is None else density2,
+                         pixelsize)]
         la = np.ascontiguousarray(ls, dtype=np.int32)
         sep = _f64(sep)
         nl, ns = len(la), len(sep)
