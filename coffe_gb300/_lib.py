@@ -52,6 +52,8 @@ EXPORTS = (
     "coffe_gpu_multipoles_async",
     "coffe_gpu_multipoles_noalloc",
     "coffe_gpu_multipoles_retries",
+    "coffe_gpu_multipoles_scaled",
+    "coffe_gpu_multipoles_adjoint",
     "coffe_gpu_covariance_integrals",
     "coffe_gpu_covariance_multipoles",
     "coffe_gpu_launch_count",
@@ -123,6 +125,10 @@ def load(build_if_missing: bool = True):
     L.coffe_gpu_set_lensing_rule.argtypes = [_p, C.c_int, C.c_int]
     L.coffe_gpu_multipoles_noalloc.argtypes = [_p, C.c_int, C.c_int, C.c_double, C.c_int,
                                                C.c_int64, _ip, _dp, _lp, _dp, C.c_int, _ip, _dp]
+    L.coffe_gpu_multipoles_scaled.argtypes = [_p, C.c_int, C.c_int, C.c_int64, _ip, _dp, _lp, _dp,
+                                              C.c_int, _ip, _dp, _dp, _dp]
+    L.coffe_gpu_multipoles_adjoint.argtypes = [_p, C.c_int, C.c_int, C.c_int64, _ip, _dp, _lp,
+                                               _dp, C.c_int, _ip, _dp, _dp, _dp, _dp, _dp, _dp]
     L.coffe_gpu_covariance_integrals.argtypes = [_p, _dp, _dp, C.c_size_t, C.c_size_t, C.c_int,
                                                  _ip, _ip, _ip, _dp, C.c_int, _dp]
     L.coffe_gpu_covariance_multipoles.argtypes = [_p, C.c_int, _dp, _dp, C.c_size_t, C.c_size_t,

@@ -219,6 +219,31 @@ class Context:
         self.n_spectra = S
         self.precision = _precision(precision)
 
+    def multipoles_scaled(self, req_spectrum, req_z_mean, req_offset, sep, n_sep: int, ls, out,
+                          bias_scale=None, growth_scale=None, contrib=_lib.DEN | _lib.RSD):
+        """Differentiable form of the den/rsd multipoles on CUDA tensors (first
+        GK61 panel), with optional per-request bias / growth-rate scales."""
+        P = lambda t, ty: None if t is None else C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ty))
+        la = np.ascontiguousarray(ls, dtype=np.int32)
+        self._check(self._L.coffe_gpu_multipoles_scaled(
+            self._ctx, int(contrib), int(req_spectrum.numel()), int(n_sep),
+            P(req_spectrum, C.c_int), P(req_z_mean, C.c_double), P(req_offset, C.c_int64),
+            P(sep, C.c_double), len(la), _iptr(la), P(bias_scale, C.c_double),
+            P(growth_scale, C.c_double), P(out, C.c_double)), "multipoles_scaled")
+
+    def multipoles_adjoint(self, req_spectrum, req_z_mean, req_offset, sep, n_sep: int, ls,
+                           grad_out, grad_pk, grad_bias=None, grad_growth=None, bias_scale=None,
+                           growth_scale=None, contrib=_lib.DEN | _lib.RSD):
+        """Reverse-mode derivative of :meth:`multipoles_scaled` (CUDA tensors)."""
+        P = lambda t, ty: None if t is None else C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ty))
+        la = np.ascontiguousarray(ls, dtype=np.int32)
+        self._check(self._L.coffe_gpu_multipoles_adjoint(
+            self._ctx, int(contrib), int(req_spectrum.numel()), int(n_sep),
+            P(req_spectrum, C.c_int), P(req_z_mean, C.c_double), P(req_offset, C.c_int64),
+            P(sep, C.c_double), len(la), _iptr(la), P(bias_scale, C.c_double),
+            P(growth_scale, C.c_double), P(grad_out, C.c_double), P(grad_pk, C.c_double),
+            P(grad_bias, C.c_double), P(grad_growth, C.c_double)), "multipoles_adjoint")
+
     def set_lensing_rule(self, n_mu: int = 128, n_x: int = 256):
         """Gauss-Legendre rule of the lensing terms: n_mu nodes in mu, n_x per x
         line (split in two panels at the line's integrand peak)."""

@@ -1,0 +1,78 @@
+"""PyTorch autograd surface of the den/RSD multipoles: derivatives with respect
+to the input power spectra and to per-request galaxy-bias and growth-rate
+scales, computed by the library's adjoint kernels (no counterpart in the
+reference, which has no derivatives).
+
+    mp = multipoles(ctx, k, pk, req_spectrum, req_z_mean, req_offset, sep, ls,
+                    bias_scale, growth_scale)
+    mp.backward(g)   # pk.grad, bias_scale.grad, growth_scale.grad
+
+``pk`` is a CUDA float64 tensor (n_spectra, nk) on the k grid ``k`` (1/Mpc);
+the request tensors follow :meth:`Context.multipoles_async`.  The value is the
+first-GK61-panel multipole (coffe_gpu_multipoles_scaled), equal to the
+adaptive result wherever the first panel meets the tolerance.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+from .api import DEN_RSD_TERMS, Context
+
+
+class _Spec:
+    def __init__(self, engine: Context, k, req, ls, contrib, N):
+        self.engine, self.k, self.req, self.ls, self.contrib, self.N = engine, k, req, ls, contrib, N
+
+
+class MultipolesFunction(torch.autograd.Function):
+    """(pk, bias_scale, growth_scale) -> multipoles (n_sep, n_l)."""
+
+    @staticmethod
+    def forward(fctx, pk, bias_scale, growth_scale, spec: _Spec):
+        e = spec.engine
+        rs, rz, ro, sep = spec.req
+        torch.cuda.synchronize()
+        e.integrals_init_device(spec.k, pk.detach().contiguous(), DEN_RSD_TERMS, N=spec.N,
+                                precision="fp64", small_r=False, sync=True)
+        out = torch.empty((sep.numel(), len(spec.ls)), dtype=torch.float64, device=pk.device)
+        e.multipoles_scaled(rs, rz, ro, sep, sep.numel(), spec.ls, out,
+                            bias_scale=bias_scale.detach().contiguous(),
+                            growth_scale=growth_scale.detach().contiguous(),
+                            contrib=spec.contrib)
+        fctx.spec = spec
+        fctx.save_for_backward(pk, bias_scale, growth_scale)
+        return out
+
+    @staticmethod
+    def backward(fctx, grad_out):
+        pk, bias_scale, growth_scale = fctx.saved_tensors
+        spec = fctx.spec
+        e = spec.engine
+        rs, rz, ro, sep = spec.req
+        torch.cuda.synchronize()
+        # the tables of this forward's spectra (another forward may have run since)
+        e.integrals_init_device(spec.k, pk.detach().contiguous(), DEN_RSD_TERMS, N=spec.N,
+                                precision="fp64", small_r=False, sync=True)
+        g_pk = torch.empty_like(pk, dtype=torch.float64)
+        g_b = torch.empty_like(bias_scale, dtype=torch.float64)
+        g_f = torch.empty_like(growth_scale, dtype=torch.float64)
+        e.multipoles_adjoint(rs, rz, ro, sep, sep.numel(), spec.ls,
+                             grad_out.detach().to(torch.float64).contiguous(), g_pk, g_b, g_f,
+                             bias_scale=bias_scale.detach().contiguous(),
+                             growth_scale=growth_scale.detach().contiguous(),
+                             contrib=spec.contrib)
+        return g_pk, g_b, g_f, None
+
+
+def multipoles(engine: Context, k, pk, req_spectrum, req_z_mean, req_offset, sep, ls=(0, 2, 4),
+               bias_scale=None, growth_scale=None, contrib=_lib.DEN | _lib.RSD, N: int = 4096):
+    """Differentiable batched den/RSD multipoles, shape (len(sep), len(ls))."""
+    n_req = req_spectrum.numel()
+    dev = pk.device
+    if bias_scale is None:
+        bias_scale = torch.ones(n_req, dtype=torch.float64, device=dev)
+    if growth_scale is None:
+        growth_scale = torch.ones(n_req, dtype=torch.float64, device=dev)
+    spec = _Spec(engine, k, (req_spectrum, req_z_mean, req_offset, sep), tuple(ls), contrib, N)
+    return MultipolesFunction.apply(pk, bias_scale, growth_scale, spec)

@@ -70,6 +70,11 @@ int cg_check_device_errors(coffe_gpu_ctx *ctx, const char *where)
         cg_set_error(ctx, "%s: adaptive quadrature exhausted its subintervals", where);
         return COFFE_GPU_ELIMIT;
     }
+    if (bits & CG_ERR_BOUNDS) {
+        cg_set_error(ctx, "%s: an input was outside the supported range (device flags 0x%x)", where,
+                     bits);
+        return COFFE_GPU_EINVAL;
+    }
     if (bits & CG_ERR_TIMEOUT) {
         cg_set_error(ctx, "%s: a bounded device wait timed out", where);
         return COFFE_GPU_ETIMEOUT;
@@ -141,7 +146,7 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
                       &ctx->zrec32,   &ctx->mp_retry, &ctx->term_df,
                       &ctx->samp_f32, &ctx->csfac32, &ctx->mp_nodes,
                       &ctx->lens_rule, &ctx->lens_rec, &ctx->lens_part,
-                      &ctx->cov_buf,  &ctx->cov_out};
+                      &ctx->cov_buf,  &ctx->cov_out, &ctx->adj_buf};
     spline_free(ctx->cov_pk);
     for (DevBuf *b : bufs) cg_release(*b);
     if (ctx->d_err) cudaFree(ctx->d_err);
@@ -414,6 +419,43 @@ int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, doubl
     if (total > 0)
         CG_CUDA(ctx, cudaMemcpyAsync(out, d_out, b_out, cudaMemcpyDeviceToHost, ctx->stream));
     return cg_check_device_errors(ctx, "multipoles");
+}
+
+int coffe_gpu_multipoles_scaled(coffe_gpu_ctx_t *ctx, int contrib, int n_req, int64_t n_sep,
+                                const int *req_spectrum, const double *req_z_mean,
+                                const int64_t *req_offset, const double *sep, int n_l,
+                                const int *l, const double *bias_scale,
+                                const double *growth_scale, double *out)
+{
+    if (!ctx || !req_spectrum || !req_z_mean || !req_offset || !l || n_sep < 0 ||
+        (n_sep > 0 && (!sep || !out)))
+        return COFFE_GPU_EINVAL;
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int st = multipoles_adjoint_run(ctx, contrib, n_req, req_spectrum, req_z_mean,
+                                          req_offset, sep, n_sep, n_l, l, bias_scale,
+                                          growth_scale, nullptr, out, nullptr, nullptr, nullptr);
+    if (st) return st;
+    return cg_check_device_errors(ctx, "multipoles_scaled");
+}
+
+int coffe_gpu_multipoles_adjoint(coffe_gpu_ctx_t *ctx, int contrib, int n_req, int64_t n_sep,
+                                 const int *req_spectrum, const double *req_z_mean,
+                                 const int64_t *req_offset, const double *sep, int n_l,
+                                 const int *l, const double *bias_scale,
+                                 const double *growth_scale, const double *grad_out,
+                                 double *grad_pk, double *grad_bias_scale,
+                                 double *grad_growth_scale)
+{
+    if (!ctx || !req_spectrum || !req_z_mean || !req_offset || !l || n_sep < 0 ||
+        (n_sep > 0 && (!sep || !grad_out)) || !grad_pk)
+        return COFFE_GPU_EINVAL;
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int st = multipoles_adjoint_run(ctx, contrib, n_req, req_spectrum, req_z_mean,
+                                          req_offset, sep, n_sep, n_l, l, bias_scale,
+                                          growth_scale, grad_out, nullptr, grad_pk,
+                                          grad_bias_scale, grad_growth_scale);
+    if (st) return st;
+    return cg_check_device_errors(ctx, "multipoles_adjoint");
 }
 
 int coffe_gpu_set_lensing_rule(coffe_gpu_ctx_t *ctx, int n_mu, int n_x)

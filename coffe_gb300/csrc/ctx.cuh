@@ -97,6 +97,9 @@ struct coffe_gpu_ctx {
     SplineBuf cov_pk; // Akima spline of the covariance's P(k)
     DevBuf cov_buf;   // FFTLog work arrays
     DevBuf cov_out;   // integrals, assembly inputs and outputs
+
+    // ---- multipole adjoint (adjoint.cu)
+    DevBuf adj_buf; // table, spectrum and resampling cotangents
 };
 
 void cg_set_error(coffe_gpu_ctx *ctx, const char *fmt, ...);
@@ -119,6 +122,11 @@ int multipoles_prepare_background(coffe_gpu_ctx *ctx);
 int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, int n_req,
                    const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
                    const double *sep, int n_l, const int *l, double *out, long long total);
+int multipoles_adjoint_run(coffe_gpu_ctx *ctx, int contrib, int n_req, const int *req_spectrum,
+                           const double *req_z_mean, const int64_t *req_offset, const double *sep,
+                           long long total, int n_l, const int *l, const double *bias_scale,
+                           const double *growth_scale, const double *grad_out, double *value_out,
+                           double *grad_pk, double *grad_bias, double *grad_growth);
 int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,
                 const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
                 const double *sep, int n_l, const int *l, double *out, long long total);

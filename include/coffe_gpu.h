@@ -246,6 +246,39 @@ int coffe_gpu_multipoles_noalloc(coffe_gpu_ctx_t *ctx, int contrib, int precisio
    No counterpart in the reference (its QAG keeps this count internal). */
 long long coffe_gpu_multipoles_retries(coffe_gpu_ctx_t *ctx);
 
+/* ------------------------------------------------------------- derivatives */
+
+/* No counterpart in the reference (which has no derivatives): the den/rsd
+   multipoles as a differentiable function of the spectra and of a galaxy-bias
+   and a growth-rate scale per request (b -> bias_scale[q] b, f ->
+   growth_scale[q] f; NULL means 1), evaluated on the first GK61 panel of the
+   multipole quadrature -- the value coffe_gpu_multipoles returns wherever that
+   panel meets the tolerance, which on the benchmark batches is all but ~1 in
+   10^6 outputs.  Tables from the last coffe_gpu_integrals_init (FP64, with the
+   integrals (0,0), (0,2), (0,4)); separations >= the third FFTLog node above
+   1 Mpc (the Akima stencil must stay on the FFTLog part of the tables).
+   Every array is a device pointer except `l` (host, n_l entries); out as
+   coffe_gpu_multipoles: out[(req_offset[q] + j) * n_l + i]. */
+int coffe_gpu_multipoles_scaled(coffe_gpu_ctx_t *ctx, int contrib, int n_req, int64_t n_sep,
+                                const int *req_spectrum, const double *req_z_mean,
+                                const int64_t *req_offset, const double *sep, int n_l,
+                                const int *l, const double *bias_scale,
+                                const double *growth_scale, double *out);
+
+/* Reverse-mode derivative of coffe_gpu_multipoles_scaled: given grad_out (same
+   layout as out), writes grad_pk[s * nk + i] = sum grad_out * d out / d P_s(k_i)
+   for every spectrum of the last coffe_gpu_integrals_init (through the
+   natural-spline resampling, the FFTLog transform and the Akima interpolation
+   of the tables, twofast.c:362-483), and, when not NULL, grad_bias_scale[q] and
+   grad_growth_scale[q].  Device pointers except `l`. */
+int coffe_gpu_multipoles_adjoint(coffe_gpu_ctx_t *ctx, int contrib, int n_req, int64_t n_sep,
+                                 const int *req_spectrum, const double *req_z_mean,
+                                 const int64_t *req_offset, const double *sep, int n_l,
+                                 const int *l, const double *bias_scale,
+                                 const double *growth_scale, const double *grad_out,
+                                 double *grad_pk, double *grad_bias_scale,
+                                 double *grad_growth_scale);
+
 /* -------------------------------------------------------------- covariance */
 
 /* The double-Bessel integrals of the multipole covariance by 2D FFTLog, as
