@@ -277,6 +277,8 @@ int coffe_gpu_set_bias(coffe_gpu_ctx_t *ctx, int which, const double *z, const d
     st = spline_build(ctx, ctx->bias[which], d, d + n, (int)n);
     if (st) return st;
     ctx->bias_set[which] = true;
+    ctx->bias_host[which].assign(z, z + n);
+    ctx->bias_host[which].insert(ctx->bias_host[which].end(), value, value + n);
     return cg_check_device_errors(ctx, "set_bias");
 }
 

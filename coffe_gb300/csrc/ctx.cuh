@@ -42,6 +42,7 @@ struct coffe_gpu_ctx {
     DevBuf zrec64, zrec32;
     SplineBuf bias[4];
     bool bias_set[4] = {false, false, false, false};
+    std::vector<double> bias_host[4]; // (z, value) samples as set, for symmetry checks
     DevBuf bias_nodes[4];
 
     // ---- integral tables
@@ -83,7 +84,7 @@ struct coffe_gpu_ctx {
     DevBuf req_buf;
     DevBuf mp_retry;
     DevBuf mp_nodes; // first-panel node table of the last multipole list
-    int mp_nodes_nl = 0, mp_nodes_prec = -1;
+    int mp_nodes_nl = 0, mp_nodes_prec = -1, mp_nodes_mirror = -1;
     int mp_nodes_ls[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
     // ---- lensing terms (lensing.cu)

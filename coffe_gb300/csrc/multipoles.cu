@@ -113,10 +113,32 @@ const PanelTables<double> &panel_tables()
 
 // The node table of one launch (layout NodeLayout<NL>), in T, for multipoles ls[0..NL)
 template <typename T>
-void build_node_table(int NL, const int *ls, std::vector<T> &out)
+void build_node_table(int NL, const int *ls, std::vector<T> &out, bool mirror = false)
 {
     const PanelTables<double> &P = panel_tables();
     const int R1 = ((2 + 3 * NL) + 3) / 4 * 4, R2 = ((1 + NL) + 3) / 4 * 4;
+    if (mirror) {
+        // rows: mu >= 0 ascending (the centre, then the 30 positive nodes); the
+        // value slot of pair p (slots 2p, 2p+1) is p, of the centre 30
+        out.assign((size_t)31 * (R1 + R2), T(0));
+        for (int k = 0; k < 31; ++k) {
+            const int sl = P.order[30 + k];
+            const double mult = sl == 60 ? 1.0 : 2.0;
+            const int pidx = sl == 60 ? 30 : sl >> 1;
+            T *r = out.data() + (size_t)k * R1;
+            r[0] = (T)P.mu_sorted[30 + k];
+            r[1] = (T)pidx;
+            for (int j = 0; j < NL; ++j) {
+                r[2 + j] = (T)(mult * P.wkP[ls[j]][sl]);
+                r[2 + NL + j] = (T)(mult * P.wgP[ls[j]][sl]);
+                r[2 + 2 * NL + j] = (T)(mult * P.wkA[ls[j]][sl]);
+            }
+            T *r2 = out.data() + (size_t)31 * R1 + (size_t)pidx * R2;
+            r2[0] = (T)(mult * P.wk[sl]);
+            for (int j = 0; j < NL; ++j) r2[1 + j] = (T)P.Pl[ls[j]][sl];
+        }
+        return;
+    }
     out.assign((size_t)61 * (R1 + R2), T(0));
     for (int k = 0; k < 61; ++k) {
         const int sl = P.order[k];
@@ -399,10 +421,15 @@ __device__ __forceinline__ typename SplTraits<S>::T cursor_down(const S &s,
 // shared memory so every node reads its constants as broadcast vector loads:
 //   pass-1 record k (ascending mu): mu, slot, wk P_l, wg P_l, wk |P_l| per l;
 //   pass-2 record per slot: wk, P_l per l.
-template <int NL> struct NodeLayout {
+// With MIRROR the integrand is even in mu (equal tracers, even multipoles:
+// functions.c's xi swaps chi1 <-> chi2 under mu -> -mu), so only the 31 nodes
+// with mu >= 0 are evaluated; the weights of the 30 nodes off the centre are
+// doubled (the Kronrod, Gauss, |f| and resasc sums are unchanged).
+template <int NL, bool MIRROR = false> struct NodeLayout {
     static constexpr int R1 = ((2 + 3 * NL) + 3) / 4 * 4;
     static constexpr int R2 = ((1 + NL) + 3) / 4 * 4;
-    static constexpr int COUNT = 61 * (R1 + R2);
+    static constexpr int ROWS = MIRROR ? 31 : 61;
+    static constexpr int COUNT = ROWS * (R1 + R2);
 };
 
 template <typename T, int R> __device__ __forceinline__ void lds_rec(const T *p, T (&r)[R]);
@@ -427,7 +454,7 @@ template <int R> __device__ __forceinline__ void lds_rec(const double *p, double
     }
 }
 
-template <int NL, typename T, typename S, typename TT>
+template <int NL, typename T, typename S, typename TT, bool MIRROR = false>
 __global__ void __launch_bounds__(MP_LANE_THREADS)
     mp_lane_kernel(MpArgs a, Bg<T, S> bg, S chi_of_z, const TT *__restrict__ tab_x,
                    const TT *__restrict__ tab_y, const int *__restrict__ req_spectrum,
@@ -436,11 +463,11 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
                    const T *__restrict__ nodes, double *__restrict__ out,
                    int *__restrict__ retry_count, int2 *__restrict__ retry, int *err)
 {
-    typedef NodeLayout<NL> LY;
+    typedef NodeLayout<NL, MIRROR> LY;
     extern __shared__ __align__(16) unsigned char mp_smem[];
-    T *tab1 = reinterpret_cast<T *>(mp_smem);  // [61][R1]
-    T *tab2 = tab1 + 61 * LY::R1;               // [61][R2]
-    T *xs = tab2 + 61 * LY::R2;                 // [61 slots][blockDim.x] integrand values
+    T *tab1 = reinterpret_cast<T *>(mp_smem);  // [ROWS][R1]
+    T *tab2 = tab1 + LY::ROWS * LY::R1;         // [ROWS][R2]
+    T *xs = tab2 + LY::ROWS * LY::R2;           // [ROWS slots][blockDim.x] integrand values
     for (int i = threadIdx.x; i < LY::COUNT; i += blockDim.x) tab1[i] = nodes[i];
     __syncthreads();
     const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -457,8 +484,8 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
     const T half_r = r * T(0.5);
     // the sweep covers chi -+ r mu_max / 2: outside the chi knots every node of
     // the reference's integrand is NaN, so the whole pair is
-    const T mu0 = tab1[0];
-    const T span = fabs(mu0) * half_r;
+    const T mu0 = tab1[0]; // first node of the sweep
+    const T span = fabs(tab1[(LY::ROWS - 1) * LY::R1]) * half_r; // largest |mu|
     const bool inside = (xi.chi_mean - span >= bg.z_of_chi.x0) && (xi.chi_mean + span <= bg.z_of_chi.xn);
     bool finite = inside && isfinite(xi.I00) && isfinite(xi.I02) && isfinite(xi.I04);
     if (inside) {
@@ -466,7 +493,7 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
         Cursor<T> c2 = cursor_at(bg.z_of_chi, xi.chi_mean + mu0 * half_r);
         // integrand at the 61 nodes in ascending mu; Kronrod, Gauss and |f| sums
 #pragma unroll 1
-        for (int k = 0; k < 61; ++k) {
+        for (int k = 0; k < LY::ROWS; ++k) {
             T rec[LY::R1];
             lds_rec<LY::R1>(tab1 + k * LY::R1, rec);
             const T mu = rec[0];
@@ -499,7 +526,7 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
     for (int j = 0; j < NL; ++j) asc[j] = T(0);
     if (inside) {
 #pragma unroll 1
-        for (int sl = 0; sl < 61; ++sl) {
+        for (int sl = 0; sl < LY::ROWS; ++sl) {
             T rec[LY::R2];
             lds_rec<LY::R2>(tab2 + sl * LY::R2, rec);
             const T v = xs[sl * bd + tid];
@@ -583,13 +610,20 @@ int launch(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S &chi
     int *d_count = (int *)ctx->mp_retry.p;
     int2 *d_retry = (int2 *)((char *)ctx->mp_retry.p + 256);
     CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
-    // node table of these multipoles (rebuilt only when the l list or precision changes)
+    // xi is even in mu when both tracers share one galaxy bias (or density is
+    // off); then even multipoles need only the nodes with mu >= 0
+    bool mirror = !(a.contrib & COFFE_GPU_DEN) || (!ctx->bias_set[0] && !ctx->bias_set[1]) ||
+                  (ctx->bias_set[0] && ctx->bias_set[1] && ctx->bias_host[0] == ctx->bias_host[1]);
+    for (int j = 0; j < a.n_l; ++j) mirror = mirror && (a.ls[j] % 2 == 0);
+    // node table of these multipoles (rebuilt only when the l list, precision
+    // or layout changes)
     const int prec_tag = sizeof(T) == 8 ? COFFE_GPU_FP64 : COFFE_GPU_MIXED;
-    bool same = ctx->mp_nodes_nl == a.n_l && ctx->mp_nodes_prec == prec_tag;
+    bool same = ctx->mp_nodes_nl == a.n_l && ctx->mp_nodes_prec == prec_tag &&
+                ctx->mp_nodes_mirror == (int)mirror;
     for (int j = 0; same && j < a.n_l; ++j) same = ctx->mp_nodes_ls[j] == a.ls[j];
     if (!same) {
         std::vector<T> tab;
-        build_node_table<T>(a.n_l, a.ls, tab);
+        build_node_table<T>(a.n_l, a.ls, tab, mirror);
         int st0 = cg_ensure(ctx, ctx->mp_nodes, sizeof(T) * tab.size());
         if (st0) return st0;
         CG_CUDA(ctx, cudaMemcpyAsync(ctx->mp_nodes.p, tab.data(), sizeof(T) * tab.size(),
@@ -597,21 +631,30 @@ int launch(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S &chi
         CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream)); // tab is a host temporary
         ctx->mp_nodes_nl = a.n_l;
         ctx->mp_nodes_prec = prec_tag;
+        ctx->mp_nodes_mirror = (int)mirror;
         for (int j = 0; j < a.n_l; ++j) ctx->mp_nodes_ls[j] = a.ls[j];
     }
     const T *d_nodes = (const T *)ctx->mp_nodes.p;
     const long long blocks = (total + MP_LANE_THREADS - 1) / MP_LANE_THREADS;
-#define MP_LAUNCH_NL(NLV)                                                                        \
-    case NLV: {                                                                                  \
-        const size_t smem = sizeof(T) * (NodeLayout<NLV>::COUNT + 61 * MP_LANE_THREADS);         \
-        CG_CUDA(ctx, cudaFuncSetAttribute(mp_lane_kernel<NLV, T, S, TT>,                        \
+#define MP_LAUNCH_MIR(NLV, MIR)                                                                  \
+    {                                                                                            \
+        const size_t smem = sizeof(T) * (NodeLayout<NLV, MIR>::COUNT +                           \
+                                         NodeLayout<NLV, MIR>::ROWS * MP_LANE_THREADS);          \
+        CG_CUDA(ctx, cudaFuncSetAttribute(mp_lane_kernel<NLV, T, S, TT, MIR>,                   \
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,           \
                                           (int)smem));                                           \
-        mp_lane_kernel<NLV, T, S, TT><<<(unsigned)blocks, MP_LANE_THREADS, smem, ctx->stream>>>( \
-            a, bg, chi_of_z, tab_x, tab_y, req_spectrum, req_z_mean, req_offset, sep, total,    \
-            d_nodes, out, d_count, d_retry, ctx->d_err);                                         \
-        break;                                                                                   \
+        mp_lane_kernel<NLV, T, S, TT, MIR>                                                       \
+            <<<(unsigned)blocks, MP_LANE_THREADS, smem, ctx->stream>>>(                          \
+                a, bg, chi_of_z, tab_x, tab_y, req_spectrum, req_z_mean, req_offset, sep, total, \
+                d_nodes, out, d_count, d_retry, ctx->d_err);                                     \
     }
+#define MP_LAUNCH_NL(NLV)                                                                        \
+    case NLV:                                                                                    \
+        if (mirror)                                                                              \
+            MP_LAUNCH_MIR(NLV, true)                                                             \
+        else                                                                                     \
+            MP_LAUNCH_MIR(NLV, false)                                                            \
+        break;
     switch (a.n_l) {
         MP_LAUNCH_NL(1)
         MP_LAUNCH_NL(2)
@@ -626,6 +669,7 @@ int launch(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S &chi
         return COFFE_GPU_EINVAL;
     }
 #undef MP_LAUNCH_NL
+#undef MP_LAUNCH_MIR
     int st = cg_after_launch(ctx, "mp_lane_kernel");
     if (st) return st;
     mp_retry_kernel<T, S, TT><<<ctx->sm_count * 2, 32 * MP_RETRY_WARPS, 0, ctx->stream>>>(
