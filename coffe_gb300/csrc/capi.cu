@@ -146,7 +146,7 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
                       &ctx->zrec32,   &ctx->mp_retry, &ctx->term_df,
                       &ctx->samp_f32, &ctx->csfac32, &ctx->mp_nodes,
                       &ctx->lens_rule, &ctx->lens_rec, &ctx->lens_part,
-                      &ctx->cov_buf,  &ctx->cov_out, &ctx->adj_buf};
+                      &ctx->cov_buf,  &ctx->cov_out, &ctx->adj_buf, &ctx->csband};
     spline_free(ctx->cov_pk);
     for (DevBuf *b : bufs) cg_release(*b);
     if (ctx->d_err) cudaFree(ctx->d_err);

@@ -65,6 +65,7 @@ struct coffe_gpu_ctx {
     DevBuf samp_dx;   // N doubles: offset of each FFT node in its interval
     DevBuf samp_f32;  // N float4 (dx, h, 1/h, -) for the mixed path
     DevBuf csfac32;   // 4 * nk floats: spline factors for the mixed path
+    DevBuf csband;    // (nk - 2) x 25 floats: band of the inverse spline matrix
     DevBuf qfac;      // n_q * N doubles: (kmax/kmin)^((3-q) i/N) W(k_i)
     DevBuf modec;     // n_terms * (N/2+1) double2: W_mode/L * M_{q,l}(t)
     DevBuf postf;     // n_terms * N doubles: prefactor * r^(n-l)

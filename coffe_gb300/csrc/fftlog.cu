@@ -298,81 +298,79 @@ __global__ void cspline_c_kernel(const double *__restrict__ x, const double *__r
     }
 }
 
-// The same solve in float for the mixed path: c enters the resampled P(k) only
-// through the h (c1 + 2 c0)/3 and dx^2 terms, corrections of relative size
-// ~(h/k)^2, so float accuracy of c is far below the target error.
-__device__ __forceinline__ void affine_scan_f(float &A, float &B, int lane)
+// The mixed path's c: rows of the inverse of the natural-spline matrix decay
+// like 0.27^|i - j| (2 - sqrt(3) on a uniform grid), so
+//   c_{i+1} = sum_{|d| <= CS_BAND} Ainv[i][i + d] rhs_{i+d}
+// with the band precomputed once per k grid (float; truncation 0.27^13 ~ 4e-8
+// of the diagonal, the float resolution of c).  c enters the resampled P(k)
+// only through the h (c1 + 2 c0)/3 and dx^2 terms, corrections of relative size
+// ~(h/k)^2.  One thread per (spectrum, knot), rhs staged in shared memory.
+#define CS_BAND 12
+#define CS_TILE 256
+__global__ void __launch_bounds__(CS_TILE)
+    cspline_band_kernel(const double *__restrict__ pk, const float *__restrict__ band,
+                        const float *__restrict__ fac32, int nk, float *__restrict__ cc)
 {
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const float Ap = __shfl_up_sync(0xffffffffu, A, o);
-        const float Bp = __shfl_up_sync(0xffffffffu, B, o);
-        if (lane >= o) {
-            A = fmaf(B, Ap, A);
-            B = B * Bp;
+    __shared__ float rhs_s[CS_TILE + 2 * CS_BAND];
+    const int s = blockIdx.y;
+    const int i0 = blockIdx.x * CS_TILE;
+    const int m = nk - 2;
+    const double *y = pk + (size_t)s * nk;
+    const float *g = fac32 + 2 * nk;
+    for (int t = threadIdx.x; t < CS_TILE + 2 * CS_BAND; t += blockDim.x) {
+        const int i = i0 - CS_BAND + t;
+        float v = 0.f;
+        if (i >= 0 && i < m) {
+            const float ya = (float)y[i], yb = (float)y[i + 1], yc = (float)y[i + 2];
+            v = 3.f * ((yc - yb) * g[i + 1] - (yb - ya) * g[i]);
         }
+        rhs_s[t] = v;
+    }
+    __syncthreads();
+    float *c = cc + (size_t)s * nk;
+    const int i = i0 + threadIdx.x;
+    if (i < m) {
+        const float *b = band + (size_t)i * (2 * CS_BAND + 1);
+        float acc = 0.f;
+#pragma unroll
+        for (int d = 0; d <= 2 * CS_BAND; ++d) acc = fmaf(__ldg(b + d), rhs_s[threadIdx.x + d], acc);
+        c[i + 1] = acc;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        c[0] = 0.f;
+        c[nk - 1] = 0.f;
     }
 }
 
-__global__ void cspline_c32_kernel(const double *__restrict__ pk, const float *__restrict__ fac32,
-                                   int nk, int n_spectra, float *__restrict__ cc)
+// Band of the inverse natural-spline matrix (rows of A^-1 = columns, A
+// symmetric), each from a tridiagonal solve on a window of 3 CS_BAND knots
+// around the row (the window's edge changes the kept entries by 0.27^24 of
+// the diagonal; windows touching the grid ends use the true boundary).
+void cspline_band_host(const std::vector<double> &x, std::vector<float> &band)
 {
-    const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (s >= n_spectra) return;
-    const double *y = pk + (size_t)s * nk;
-    float *c = cc + (size_t)s * nk;
-    const float *invd = fac32, *w = fac32 + nk, *g = fac32 + 2 * nk, *hh = fac32 + 3 * nk;
-    const int m = nk - 2;
-    const int chunk = (m + 31) / 32;
-    const int lo = lane * chunk, hi = min(lo + chunk, m);
-    // sliding window of float samples: one conversion per element and pass
-    float A = 0.f, B = 1.f;
-    float ya = lo < hi ? (float)y[lo] : 0.f, yb = lo < hi ? (float)y[lo + 1] : 0.f;
-    for (int i = lo; i < hi; ++i) {
-        const float yc = (float)y[i + 2];
-        const float rhs = 3.f * ((yc - yb) * g[i + 1] - (yb - ya) * g[i]);
-        const float b = i > 0 ? -w[i] : 0.f;
-        A = fmaf(b, A, rhs);
-        B = b * B;
-        ya = yb;
-        yb = yc;
-    }
-    affine_scan_f(A, B, lane);
-    float r = __shfl_up_sync(0xffffffffu, A, 1);
-    if (lane == 0) r = 0.f;
-    ya = lo < hi ? (float)y[lo] : 0.f;
-    yb = lo < hi ? (float)y[lo + 1] : 0.f;
-    for (int i = lo; i < hi; ++i) {
-        const float yc = (float)y[i + 2];
-        const float rhs = 3.f * ((yc - yb) * g[i + 1] - (yb - ya) * g[i]);
-        r = i > 0 ? fmaf(-w[i], r, rhs) : rhs;
-        c[i + 1] = r;
-        ya = yb;
-        yb = yc;
-    }
-    __syncwarp();
-    const int rl = 31 - lane;
-    const int blo = rl * chunk, bhi = min(blo + chunk, m);
-    A = 0.f;
-    B = 1.f;
-    for (int i = bhi - 1; i >= blo; --i) {
-        const float a_i = c[i + 1] * invd[i];
-        const float b_i = -hh[i + 1] * invd[i];
-        A = fmaf(b_i, A, a_i);
-        B = b_i * B;
-    }
-    affine_scan_f(A, B, lane);
-    float cn = __shfl_up_sync(0xffffffffu, A, 1);
-    if (lane == 0) cn = 0.f;
-    __syncwarp();
-    for (int i = bhi - 1; i >= blo; --i) {
-        cn = (c[i + 1] - hh[i + 1] * cn) * invd[i];
-        c[i + 1] = cn;
-    }
-    if (lane == 0) {
-        c[0] = 0.f;
-        c[nk - 1] = 0.f;
+    const int nk = (int)x.size(), m = nk - 2, W = 3 * CS_BAND, B = 2 * CS_BAND + 1;
+    band.assign((size_t)m * B, 0.f);
+    std::vector<double> dg(2 * W + 1), up(2 * W + 1), rhs(2 * W + 1);
+    for (int j = 0; j < m; ++j) {
+        const int lo = std::max(0, j - W), hi = std::min(m, j + W + 1), n = hi - lo;
+        // rows i = lo..hi-1 (unknown c_{i+1}): diag 2 (h_i + h_{i+1}), coupling h_{i+1}
+        for (int r = 0; r < n; ++r) {
+            const int i = lo + r;
+            dg[r] = 2.0 * ((x[i + 1] - x[i]) + (x[i + 2] - x[i + 1]));
+            up[r] = x[i + 2] - x[i + 1];
+            rhs[r] = i == j ? 1.0 : 0.0;
+        }
+        for (int r = 1; r < n; ++r) {
+            const double w = up[r - 1] / dg[r - 1];
+            dg[r] -= w * up[r - 1];
+            rhs[r] -= w * rhs[r - 1];
+        }
+        rhs[n - 1] /= dg[n - 1];
+        for (int r = n - 2; r >= 0; --r) rhs[r] = (rhs[r] - up[r] * rhs[r + 1]) / dg[r];
+        for (int d = -CS_BAND; d <= CS_BAND; ++d) {
+            const int i = j + d;
+            if (i >= lo && i < hi) band[(size_t)j * B + d + CS_BAND] = (float)rhs[i - lo];
+        }
     }
 }
 
@@ -944,6 +942,14 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         csfac_kernel<<<1, 1, 0, ctx->stream>>>((const double *)ctx->kgrid.p, (int)nk,
                                                (double *)ctx->csfac.p, (float *)ctx->csfac32.p);
         if ((st = cg_after_launch(ctx, "csfac_kernel"))) return st;
+        {
+            std::vector<float> band;
+            cspline_band_host(std::vector<double>(k, k + nk), band);
+            if ((st = cg_ensure(ctx, ctx->csband, sizeof(float) * band.size()))) return st;
+            CG_CUDA(ctx, cudaMemcpyAsync(ctx->csband.p, band.data(), sizeof(float) * band.size(),
+                                         cudaMemcpyHostToDevice, ctx->stream));
+            CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream)); // band is a host temporary
+        }
         const int tb = 256;
         sampling_kernel<<<((int)N + tb) / tb, tb, 0, ctx->stream>>>(
             g, (const double *)ctx->kgrid.p, (int *)ctx->samp_idx.p, (double *)ctx->samp_dx.p,
@@ -969,9 +975,11 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     }
     // per spectrum: natural-spline coefficients, forward FFTs, inverse FFTs
     if (mixed) {
-        cspline_c32_kernel<<<(n_spectra + 3) / 4, 128, 0, ctx->stream>>>(
-            d_pk, (const float *)ctx->csfac32.p, (int)nk, n_spectra, (float *)ctx->csc.p);
-        if ((st = cg_after_launch(ctx, "cspline_c32_kernel"))) return st;
+        cspline_band_kernel<<<dim3(((int)nk - 2 + CS_TILE - 1) / CS_TILE, n_spectra), CS_TILE, 0,
+                              ctx->stream>>>(d_pk, (const float *)ctx->csband.p,
+                                             (const float *)ctx->csfac32.p, (int)nk,
+                                             (float *)ctx->csc.p);
+        if ((st = cg_after_launch(ctx, "cspline_band_kernel"))) return st;
     } else {
         cspline_c_kernel<<<(n_spectra + 3) / 4, 128, 0, ctx->stream>>>(
             (const double *)ctx->kgrid.p, d_pk, (const double *)ctx->csfac.p, (int)nk, n_spectra,
