@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--cpu-spectra", type=int, default=48, help="CPU baseline sample size")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the lensing / covariance / gradient workload timings")
     p.add_argument("--no-clocks", action="store_true")
     p.add_argument("--kernel-only", choices=["mixed", "fp64", "tables-mixed", "tables-fp64"],
                    default=None,
@@ -213,6 +215,98 @@ def measure_gemm_peak(torch, dtype, n=8192, reps=5):
     return best / 1e12
 
 
+def extras(torch, ctx, stream):
+    """Device timings of the other workloads of the path (one GB300, CUDA events
+    on the library's stream): den+RSD+lensing multipoles (128 mu x 256 x rule),
+    the 2D-FFTLog multipole covariance and the multipole gradient."""
+    from coffe_gb300 import workloads
+
+    out = {}
+
+    def ev_time(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(reps):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            fn()
+            e.record(stream)
+            e.synchronize()
+            t = s.elapsed_time(e)
+            best = t if best is None else min(best, t)
+        return best
+
+    # lensing: l = 0,2,4,6 at z = 1.5, 200 separations
+    c4 = workloads.cfg4()
+    co = c4["cosmo"]
+    ctx.background_init(co.omega_m, co.omega_baryon, co.omega_gamma, co.h, 10000)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    sep = torch.tensor(c4["sep"], device=dev)
+    rs = torch.zeros(1, dtype=torch.int32, device=dev)
+    rz = torch.tensor([c4["z_mean"]], dtype=torch.float64, device=dev)
+    ro = torch.tensor([0, len(c4["sep"])], dtype=torch.int64, device=dev)
+    res = {}
+    for prec, reps in (("mixed", 3), ("fp64", 1)):
+        ctx.integrals_init(c4["k"], c4["pk"][None, :], c4["terms"], N=N_FFT, precision=prec,
+                           small_r=True)
+        ctx.set_lensing_rule(*c4["rule"])
+        o = torch.empty((len(c4["sep"]), 4), dtype=torch.float64, device=dev)
+        ms = ev_time(lambda: ctx.multipoles_async(rs, rz, ro, sep, len(c4["sep"]), c4["ls"], o,
+                                                  contrib=7, precision=prec), reps)
+        ctx.synchronize()
+        res[prec] = (ms, o.cpu().numpy())
+    fl = 1e-3 * np.abs(res["fp64"][1]).max(0)
+    fl[3] = 1e-3 * np.abs(res["fp64"][1]).max()  # l = 6: see the lensing tests
+    err = float(np.max(np.abs(res["mixed"][1] - res["fp64"][1]) /
+                       np.maximum(np.abs(res["fp64"][1]), fl)))
+    n4 = len(c4["sep"]) * 4
+    out["lensing_cfg4"] = {
+        "workload": "den+RSD+lensing multipoles l=0,2,4,6, z=1.5, 200 separations 20-300 "
+                    "Mpc/h, Gauss-Legendre 128 mu x 256 x (split), FFTLog N=4096",
+        "mixed_ms": res["mixed"][0], "fp64_ms": res["fp64"][0],
+        "mixed_evals_per_s": n4 / (res["mixed"][0] * 1e-3),
+        "fp64_evals_per_s": n4 / (res["fp64"][0] * 1e-3),
+        "lensing_nodes_per_s_mixed": len(c4["sep"]) * 128 * 256 * 256 / (res["mixed"][0] * 1e-3),
+        "max_rel_err_mixed_vs_fp64": err}
+    # covariance: 5 z bins x l = 0,2,4 x 128 x 128 separations, 2D FFTLog 2^11
+    ctx.background_init(co.omega_m, co.omega_baryon, co.omega_gamma, co.h, 10000)
+    bg = ctx.background(with_H=False)
+    c5 = workloads.cfg5(lambda z: np.interp(z, bg["z"], bg["chi"]))
+    cov_call = lambda: ctx.covariance_multipoles(
+        c5["k"], c5["pk"], c5["N"], c5["z_mean"], c5["deltaz"], c5["fsky"], c5["density"],
+        c5["density"], c5["pixelsize"], c5["ls"], c5["sep"])
+    cov_call()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        cov = cov_call()
+    cov_ms = (time.perf_counter() - t0) / 3 * 1e3
+    out["covariance_cfg5"] = {
+        "workload": "multipole covariance l=0,2,4, 5 z bins of 1 (Gpc/h)^3, n=1e-3 (h/Mpc)^3, "
+                    "128 x 128 separations 20-300 Mpc/h, 2D FFTLog 2^11 x 2^11, FP64",
+        "ms_per_call": cov_ms, "outputs": int(cov.size),
+        "note": "host API wall time (host arrays in, covariance out), 12 2D transforms"}
+    # gradient of the config-1 multipoles with respect to P(k), bias and growth scales
+    c1 = workloads.cfg1()
+    ctx.background_init(co.omega_m, co.omega_baryon, co.omega_gamma, co.h, 10000)
+    pk1 = torch.tensor(c1["pk"][None, :], device=dev)
+    sep1 = torch.tensor(c1["sep"], device=dev)
+    ro1 = torch.tensor([0, len(c1["sep"])], dtype=torch.int64, device=dev)
+    rz1 = torch.tensor([1.0], dtype=torch.float64, device=dev)
+    ctx.integrals_init_device(c1["k"], pk1, TERMS, N=N_FFT, precision="fp64")
+    G = torch.ones((len(c1["sep"]), 3), dtype=torch.float64, device=dev)
+    gpk = torch.empty_like(pk1)
+    gb = torch.empty(1, dtype=torch.float64, device=dev)
+    gf = torch.empty(1, dtype=torch.float64, device=dev)
+    grad_ms = ev_time(lambda: ctx.multipoles_adjoint(rs, rz1, ro1, sep1, len(c1["sep"]),
+                                                     (0, 2, 4), G, gpk, gb, gf), 3)
+    out["gradient_cfg1"] = {
+        "workload": "d(multipoles)/d(P(k), bias scale, growth scale), den+RSD l=0,2,4, z=1, "
+                    "100 separations, 4096 k nodes, FP64 adjoint",
+        "ms_per_call": grad_ms}
+    return out
+
+
 def ours(args, rank, world, local_rank):
     import torch
 
@@ -323,15 +417,16 @@ def ours(args, rank, world, local_rank):
         pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
         h_pk, h_rs, h_rz = pin(batch.pk), pin(batch.req_spectrum), pin(batch.req_z_mean)
         h_ro, h_sep = pin(batch.req_offset), pin(batch.sep)
+        h_out = pin(np.zeros((len(batch.sep), len(batch.ls))))
         ctx.set_stream(None)
         ctx.integrals_init(batch.k, h_pk, TERMS, N=N_FFT, precision="mixed", small_r=False)
-        ctx.multipoles(h_rs, h_rz, h_ro, h_sep, batch.ls, precision="mixed")
+        ctx.multipoles(h_rs, h_rz, h_ro, h_sep, batch.ls, precision="mixed", out=h_out)
         ke = max(3, min(args.steps, 20))
         barrier()
         t0 = time.perf_counter()
         for _ in range(ke):
             ctx.integrals_init(batch.k, h_pk, TERMS, N=N_FFT, precision="mixed", small_r=False)
-            res = ctx.multipoles(h_rs, h_rz, h_ro, h_sep, batch.ls, precision="mixed")
+            res = ctx.multipoles(h_rs, h_rz, h_ro, h_sep, batch.ls, precision="mixed", out=h_out)
         barrier()
         te = time.perf_counter() - t0
         h2d = h_pk.nbytes + h_rs.nbytes + h_rz.nbytes + h_ro.nbytes + h_sep.nbytes
@@ -374,6 +469,9 @@ def ours(args, rank, world, local_rank):
                "sample": f"first {args.cpu_spectra} of {args.n_spectra} spectra, all their "
                          f"requests ({ce} evals, {cdt:.1f} s)",
                "gpu_fp64_vs_cpu_max_rel_err": sub_err}
+    extra = None
+    if not args.no_extras:
+        extra = extras(torch, ctx, stream)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_mixed / args.steps,
@@ -405,6 +503,7 @@ def ours(args, rank, world, local_rank):
         "clocks": clocks,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "extras": extra,
     }
     print(json.dumps(line), flush=True)
     ctx.close()

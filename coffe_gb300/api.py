@@ -182,8 +182,11 @@ class Context:
 
     # ------------------------------------------------------------ multipoles
     def multipoles(self, req_spectrum, req_z_mean, req_offset, sep, ls=(0, 2, 4),
-                   contrib=_lib.DEN | _lib.RSD, precision="fp64", epsrel=1e-5) -> np.ndarray:
-        """Batched multipoles; returns an array of shape (len(sep), len(ls))."""
+                   contrib=_lib.DEN | _lib.RSD, precision="fp64", epsrel=1e-5,
+                   out=None) -> np.ndarray:
+        """Batched multipoles; returns an array of shape (len(sep), len(ls)).
+        ``out``: optional C-contiguous float64 array of that shape to fill (page-locked
+        host memory makes the device-to-host copy run at full link speed)."""
         rs = np.ascontiguousarray(req_spectrum, dtype=np.int32)
         rz = _f64(req_z_mean)
         ro = np.ascontiguousarray(req_offset, dtype=np.int64)
@@ -191,7 +194,11 @@ class Context:
         la = np.ascontiguousarray(ls, dtype=np.int32)
         if len(ro) != len(rs) + 1 or len(rz) != len(rs):
             raise ValueError("req_offset needs len(req_spectrum) + 1 entries")
-        out = np.zeros((max(len(sp), 1), len(la)))
+        if out is None:
+            out = np.zeros((max(len(sp), 1), len(la)))
+        elif (out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"] or
+              out.shape[0] < max(len(sp), 1) or out.shape[1] != len(la)):
+            raise ValueError("out must be a C-contiguous float64 array of shape (len(sep), len(ls))")
         self._check(self._L.coffe_gpu_multipoles(self._ctx, int(contrib), _precision(precision),
                                                  float(epsrel), len(rs), _iptr(rs), _dptr(rz),
                                                  _lptr(ro), _dptr(sp), len(la), _iptr(la),
