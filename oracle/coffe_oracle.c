@@ -1828,3 +1828,108 @@ int or_covariance_multipoles(const or_model_t *mdl, int contrib, size_t nz, cons
     }
     return 0;
 }
+
+/* ---------------------------------------------------------------- flat sky
+ * Half-integer tables I^{n/2}_{l/2} (integrals.c:189-207, the HALF_INTEGER
+ * state) and the flat-sky lensing multipoles (functions.c:4020-4253 with the
+ * 2 pi^2 of signal.c:619-630, 708-734).  Half-integer tables are stored in the
+ * model under the keys (OR_HALF_KEY + n, OR_HALF_KEY + l).
+ */
+#define OR_HALF_KEY 10000
+
+/* FFTLog table of I^{n_num/2}_{l_num/2} on N points, times r^(n-l) when
+   n >= l (integrals.c:459-523); the r = 0 and sub-Mpc entries are NaN */
+int or_integral_table_half(const double *k, const double *pk, size_t nk, int n_num, int l_num,
+                           size_t N, double kmin, double kmax, double *out_x, double *out_y)
+{
+    const size_t off = OR_N_SMALL_R + 1;
+    const double n = n_num / 2., l = l_num / 2.;
+    double *fx = out_x + off, *fy = out_y + off;
+    if (or_twofast_1bessel(fx, fy, N, k, pk, nk, l, n, 1.0, kmin, kmin, kmax) != 0)
+        return -1;
+    if (n >= l)
+        for (size_t i = 0; i < N; ++i)
+            fy[i] = fy[i] * pow(fx[i], n - l);
+    out_x[0] = 0.0;
+    for (size_t i = 1; i <= OR_N_SMALL_R; ++i)
+        out_x[i] = or_min_sep[i - 1];
+    for (size_t i = 0; i < off; ++i)
+        out_y[i] = NAN;
+    return 0;
+}
+
+static double or_fact(int n)
+{
+    double r = 1;
+    for (int i = 2; i <= n; ++i) r *= i;
+    return r;
+}
+
+static double or_choose(int n, int k)
+{
+    return or_fact(n) / or_fact(k) / or_fact(n - k);
+}
+
+/* flat-sky density-lensing multipole (functions.c:4136-4253), even l, times
+   2 pi^2 (signal.c:619-630); needs the half-integer tables
+   ((l - 2k + 3)/2, (l - 2k + 1)/2), k = 0..l/2 */
+double or_flatsky_density_lensing(const or_model_t *m, double z_mean, double sep, int l)
+{
+    if (l % 2)
+        return 0.0;
+    const double s1 = bias_eval(m, 2, z_mean, 0.0), s2 = bias_eval(m, 3, z_mean, 0.0);
+    const double b1 = bias_eval(m, 0, z_mean, 1.0), b2 = bias_eval(m, 1, z_mean, 1.0);
+    double result = 0;
+    for (int k = 0; k <= l / 2; ++k) {
+        const or_spline_t *tab = find_integral(m, OR_HALF_KEY + l - 2 * k + 3, OR_HALF_KEY + l - 2 * k + 1);
+        if (!tab)
+            return NAN;
+        result += pow(-1, k) / pow(2, k) * or_choose(l, k) * or_choose(2 * l - 2 * k, l) *
+                  or_fact(l / 2 - k) * or_spline_eval(tab, sep);
+    }
+    const double D1 = or_spline_eval(&m->D1, z_mean);
+    result *= -3 * m->Omega0_m / M_PI / 8 * (2 * l + 1) * D1 * D1 * (1 + z_mean) * sep *
+              ((2 - 5 * s1) * b2 + (2 - 5 * s2) * b1) * pow(2, 1 - l / 2);
+    return 2 * M_PI * M_PI * result / sqrt(2 * M_PI) * pow(OR_H0 * m->h, 2);
+}
+
+typedef struct {
+    const or_model_t *m;
+    double z_mean, sep;
+    int l;
+} or_flat_par_t;
+
+/* functions_flatsky_lensing_lensing_multipoles (functions.c:4020-4132) */
+static double flat_ll_integrand(double x, void *vp)
+{
+    const or_flat_par_t *p = (const or_flat_par_t *)vp;
+    const or_model_t *m = p->m;
+    const int l = p->l;
+    const double chi_mean = or_spline_eval(&m->chi_of_z, p->z_mean);
+    const double lambda = chi_mean * x;
+    const double s1 = bias_eval(m, 2, p->z_mean, 0.0), s2 = bias_eval(m, 3, p->z_mean, 0.0);
+    const double zl = or_spline_eval(&m->z_of_chi, lambda);
+    const double D1 = or_spline_eval(&m->D1, zl);
+    double result = (2 * l + 1) * or_fact(l) / pow(2, l) / pow(or_fact(l / 2), 2) * 9 *
+                    m->Omega0_m * m->Omega0_m * (2 - 5 * s1) * (2 - 5 * s2) * pow(chi_mean, 3) /
+                    8. / M_PI * or_spline_eval(find_integral(m, 1, l), x * p->sep) * D1 * D1 *
+                    (1 + zl) * (1 + zl) * pow(x * (1 - x), 2);
+    if (l > 0)
+        return result * x * p->sep * pow(OR_H0 * m->h, 4);
+    return result * pow(OR_H0 * m->h, 4);
+}
+
+/* flat-sky lensing-lensing multipole, even l: 2 pi^2 times the QAG integral
+   over x in [0, 1] (signal.c:708-734); needs the integer tables I^1_l with
+   their r = 0 and sub-Mpc entries */
+double or_flatsky_lensing_lensing(const or_model_t *m, double z_mean, double sep, int l,
+                                  double epsrel)
+{
+    if (l % 2 || !find_integral(m, 1, l))
+        return l % 2 ? 0.0 : NAN;
+    or_flat_par_t p = {m, z_mean, sep, l};
+    double err;
+    int status;
+    const double v = or_qag61(flat_ll_integrand, &p, 0, 1, 0, epsrel, 50000, &err, &status);
+    return 2 * M_PI * M_PI * v;
+}

@@ -173,6 +173,17 @@ int or_covariance_multipoles(const or_model_t *mdl, int contrib, size_t nz, cons
                              const double *sep, const double *ipk, const double *ipk2,
                              double *out);
 
+/* ---------------------------------------------------------------- flat sky */
+/* half-integer table I^{n_num/2}_{l_num/2} (FFT part; small-r entries NaN);
+   stored in a model with or_model_set_integral(m, 10000 + n_num, 10000 + l_num, ...) */
+int or_integral_table_half(const double *k, const double *pk, size_t nk, int n_num, int l_num,
+                           size_t N, double kmin, double kmax, double *out_x, double *out_y);
+/* flat-sky density-lensing multipole (functions.c:4136-4253) x 2 pi^2 */
+double or_flatsky_density_lensing(const or_model_t *m, double z_mean, double sep, int l);
+/* flat-sky lensing-lensing multipole (functions.c:4020-4132) by QAG x 2 pi^2 */
+double or_flatsky_lensing_lensing(const or_model_t *m, double z_mean, double sep, int l,
+                                  double epsrel);
+
 /* number of QAG subdivisions taken by the last or_multipole_nonintegrated call
    in this thread (diagnostic) */
 int or_last_qag_intervals(void);

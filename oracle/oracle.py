@@ -90,6 +90,13 @@ def lib():
         L.or_xi_single_integrated.restype = C.c_double
         L.or_xi_double_integrated.argtypes = [C.c_void_p, C.c_int] + [C.c_double] * 5
         L.or_xi_double_integrated.restype = C.c_double
+        L.or_integral_table_half.argtypes = [_dp, _dp, C.c_size_t, C.c_int, C.c_int, C.c_size_t,
+                                             C.c_double, C.c_double, _dp, _dp]
+        L.or_flatsky_density_lensing.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int]
+        L.or_flatsky_density_lensing.restype = C.c_double
+        L.or_flatsky_lensing_lensing.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int,
+                                                 C.c_double]
+        L.or_flatsky_lensing_lensing.restype = C.c_double
         L.or_legendre_integral.argtypes = [C.c_int] * 4
         L.or_legendre_integral.restype = C.c_double
         L.or_twobessel_diag.argtypes = [_dp, _dp, C.c_size_t] + [C.c_double] * 5 + [_dp, _dp]
@@ -245,6 +252,16 @@ class Model:
         return out
 
 
+    def set_integral_half(self, n_num: int, l_num: int, x, y):
+        """a half-integer table I^{n_num/2}_{l_num/2}"""
+        self.set_integral(10000 + n_num, 10000 + l_num, x, y)
+
+    def flatsky_density_lensing(self, z_mean, sep, l):
+        return lib().or_flatsky_density_lensing(self._p, z_mean, sep, l)
+
+    def flatsky_lensing_lensing(self, z_mean, sep, l, epsrel=1e-5):
+        return lib().or_flatsky_lensing_lensing(self._p, z_mean, sep, l, epsrel)
+
     def xi_single(self, contrib, z_mean, mu, sep, x):
         return lib().or_xi_single_integrated(self._p, contrib, z_mean, mu, sep, x)
 
@@ -280,6 +297,19 @@ class Model:
         lib().or_covariance_multipoles(self._p, contrib, nz, z, *arr, nl, la, ns, sep,
                                        _f64(ipk).ravel(), _f64(ipk2).ravel(), out)
         return out.reshape(nz, nl, ns, nl, ns)
+
+
+def integral_table_half(k, pk, n_num, l_num, N, kmin=None, kmax=None):
+    """FFTLog table of I^{n_num/2}_{l_num/2} (small-r entries NaN)."""
+    k, pk = _f64(k), _f64(pk)
+    kmin = float(k[0] if kmin is None else kmin)
+    kmax = float(k[-1] if kmax is None else kmax)
+    n_out = N + 43
+    x, y = np.zeros(n_out), np.zeros(n_out)
+    if lib().or_integral_table_half(k, pk, len(k), int(n_num), int(l_num), int(N), kmin, kmax,
+                                    x, y) != 0:
+        raise ValueError("half-integer table failed")
+    return x, y
 
 
 def legendre_integral(n, m, a, b) -> float:

@@ -158,3 +158,26 @@ def test_density_rsd_lensing_multipoles_match_golden(golden, lens_model):
         ref = golden[f"std_len_multipoles{l}"][:, 1]
         tol = 5e-4 if l < 4 else 2e-3
         assert np.allclose(std + lens[:, j], ref, rtol=tol), (l, (std + lens[:, j]) / ref - 1)
+
+
+def test_flatsky_lensing_multipoles_match_golden(golden, oracle, class_pk, ref_bg):
+    """Flat-sky lensing-lensing (functions.c:4020-4132, QAG over x) and
+    density-lensing (functions.c:4136-4253, closed sums over the half-integer
+    tables I^{(l-2k+3)/2}_{(l-2k+1)/2}) against the golden files at the
+    reference's rtol 5e-4 (test_coffe.py:328-380)."""
+    k, pk = class_pk
+    m = oracle.Model(ref_bg, H, 0.3)
+    N = 8192
+    for l in (0, 2, 4):
+        x, y = oracle.integral_table(k, pk, 1, l, N, with_small_r=True)
+        m.set_integral(1, l, x, y)
+        for kk in range(l // 2 + 1):
+            nn, ll = l - 2 * kk + 3, l - 2 * kk + 1
+            x, y = oracle.integral_table_half(k, pk, nn, ll, N)
+            m.set_integral_half(nn, ll, x, y)
+    for name, fn in (("flatsky_lensing_lensing", m.flatsky_lensing_lensing),
+                     ("flatsky_density_lensing", m.flatsky_density_lensing)):
+        for l in (0, 2, 4):
+            d = golden[f"{name}_multipoles{l}"]
+            v = np.array([fn(1.0, r / H, l) for r in d[:, 0]])
+            assert np.allclose(v, d[:, 1], rtol=5e-4), (name, l, v / d[:, 1] - 1)
