@@ -26,6 +26,7 @@ MIXED = 1
 DEN = 1
 RSD = 2
 LEN = 4
+ONLY_CROSS = 8
 SMALL_R = 1
 PK_DEVICE = 2
 ASYNC = 4
@@ -45,9 +46,11 @@ EXPORTS = (
     "coffe_gpu_set_bias",
     "coffe_gpu_integral_table_len",
     "coffe_gpu_integrals_init",
+    "coffe_gpu_integrals_init_ex",
     "coffe_gpu_integral_get",
     "coffe_gpu_integral_eval",
     "coffe_gpu_multipoles",
+    "coffe_gpu_set_flatsky",
     "coffe_gpu_set_lensing_rule",
     "coffe_gpu_multipoles_async",
     "coffe_gpu_multipoles_noalloc",
@@ -116,6 +119,9 @@ def load(build_if_missing: bool = True):
     L.coffe_gpu_integral_table_len.restype = C.c_size_t
     L.coffe_gpu_integrals_init.argtypes = [_p, _dp, _dp, C.c_int, C.c_size_t, _ip, _ip, C.c_int,
                                            C.c_size_t, C.c_int, C.c_uint]
+    L.coffe_gpu_integrals_init_ex.argtypes = [_p, _dp, _dp, C.c_int, C.c_size_t, _ip, _ip, _ip,
+                                              C.c_int, C.c_size_t, C.c_int, C.c_uint]
+    L.coffe_gpu_set_flatsky.argtypes = [_p, C.c_int, C.c_int]
     L.coffe_gpu_integral_get.argtypes = [_p, C.c_int, C.c_int, _dp, _dp]
     L.coffe_gpu_integral_eval.argtypes = [_p, C.c_int, C.c_int, _dp, C.c_size_t, _dp]
     L.coffe_gpu_multipoles.argtypes = [_p, C.c_int, C.c_int, C.c_double, C.c_int, _ip, _dp, _lp,

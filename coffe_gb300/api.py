@@ -145,17 +145,27 @@ class Context:
         pk = _f64(np.atleast_2d(pk))
         if pk.shape[1] != len(k):
             raise ValueError("pk must have shape (n_spectra, len(k))")
+        # a term is (n, l) or (n, l, half): half = 1 makes n, l numerators of n/2, l/2
         n = np.ascontiguousarray([t[0] for t in terms], dtype=np.int32)
         l = np.ascontiguousarray([t[1] for t in terms], dtype=np.int32)
+        half = np.ascontiguousarray([t[2] if len(t) > 2 else 0 for t in terms], dtype=np.int32)
         prec = _precision(precision)
         flags = _lib.SMALL_R if small_r else 0
-        self._check(self._L.coffe_gpu_integrals_init(self._ctx, _dptr(k), _dptr(pk), pk.shape[0],
-                                                     len(k), _iptr(n), _iptr(l), len(terms),
-                                                     int(N), prec, flags), "integrals_init")
+        self._check(self._L.coffe_gpu_integrals_init_ex(self._ctx, _dptr(k), _dptr(pk),
+                                                        pk.shape[0], len(k), _iptr(n), _iptr(l),
+                                                        _iptr(half), len(terms), int(N), prec,
+                                                        flags), "integrals_init")
         self.N = int(N)
-        self.terms = tuple((int(a), int(b)) for a, b in terms)
+        self.terms = tuple((int(t[0]), int(t[1])) + ((1,) if len(t) > 2 and t[2] else ())
+                           for t in terms)
         self.n_spectra = pk.shape[0]
         self.precision = prec
+
+    def set_flatsky(self, local_nonlocal: bool = False, nonlocal_: bool = False):
+        """Flat-sky forms of density-lensing (local_nonlocal) and lensing-lensing
+        (nonlocal_) in the multipoles, as the reference's flatsky flags."""
+        self._check(self._L.coffe_gpu_set_flatsky(self._ctx, int(bool(local_nonlocal)),
+                                                  int(bool(nonlocal_))), "set_flatsky")
 
     def table_len(self) -> int:
         return int(self._L.coffe_gpu_integral_table_len(self.N))

@@ -454,9 +454,7 @@ int multipoles_adjoint_run(coffe_gpu_ctx *ctx, int contrib, int n_req, const int
     a.has_b2 = ctx->bias_set[1];
     const int want[3] = {0, 2, 4};
     for (int t = 0; t < 3; ++t) {
-        a.t[t] = -1;
-        for (int k = 0; k < ctx->n_terms; ++k)
-            if (ctx->term_n[k] == 0 && ctx->term_l[k] == want[t]) a.t[t] = k;
+        a.t[t] = cg_find_term(ctx, 0, want[t]);
         if (a.t[t] < 0) {
             cg_set_error(ctx, "multipoles adjoint: integrals (0,0), (0,2), (0,4) are required");
             return COFFE_GPU_ESTATE;

@@ -288,9 +288,19 @@ int coffe_gpu_integrals_init(coffe_gpu_ctx_t *ctx, const double *k, const double
                              int n_spectra, size_t nk, const int *n, const int *l, int n_terms,
                              size_t N, int precision, unsigned flags)
 {
+    return coffe_gpu_integrals_init_ex(ctx, k, pk, n_spectra, nk, n, l, nullptr, n_terms, N,
+                                       precision, flags);
+}
+
+int coffe_gpu_integrals_init_ex(coffe_gpu_ctx_t *ctx, const double *k, const double *pk,
+                                int n_spectra, size_t nk, const int *n, const int *l,
+                                const int *half, int n_terms, size_t N, int precision,
+                                unsigned flags)
+{
     if (!ctx) return COFFE_GPU_EINVAL;
     CG_CUDA(ctx, cudaSetDevice(ctx->device));
-    const int st = integrals_build(ctx, k, pk, n_spectra, nk, n, l, n_terms, N, precision, flags);
+    const int st = integrals_build(ctx, k, pk, n_spectra, nk, n, l, half, n_terms, N, precision,
+                                   flags);
     if (st) {
         ctx->int_ready = false;
         return st;
@@ -458,6 +468,14 @@ int coffe_gpu_multipoles_adjoint(coffe_gpu_ctx_t *ctx, int contrib, int n_req, i
                                           grad_bias_scale, grad_growth_scale);
     if (st) return st;
     return cg_check_device_errors(ctx, "multipoles_adjoint");
+}
+
+int coffe_gpu_set_flatsky(coffe_gpu_ctx_t *ctx, int local_nonlocal, int nonlocal)
+{
+    if (!ctx) return COFFE_GPU_EINVAL;
+    ctx->flat_local_nonlocal = local_nonlocal != 0;
+    ctx->flat_nonlocal = nonlocal != 0;
+    return COFFE_GPU_OK;
 }
 
 int coffe_gpu_set_lensing_rule(coffe_gpu_ctx_t *ctx, int n_mu, int n_x)

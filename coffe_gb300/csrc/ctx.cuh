@@ -52,6 +52,7 @@ struct coffe_gpu_ctx {
     double kmin = 0, kmax = 0;
     bool int_small_r = false; // r = 0 and sub-Mpc entries filled
     int term_n[CG_MAX_TERMS], term_l[CG_MAX_TERMS], term_q[CG_MAX_TERMS];
+    int term_half[CG_MAX_TERMS]; // 1: (n, l) are numerators of n/2, l/2
     int n_q = 0;
     double qvals[CG_MAX_TERMS];
     DevBuf tab_x;     // (N + 43) doubles, shared by all tables
@@ -88,6 +89,10 @@ struct coffe_gpu_ctx {
     int mp_nodes_nl = 0, mp_nodes_prec = -1, mp_nodes_mirror = -1;
     int mp_nodes_ls[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
+    // ---- flat-sky lensing and cross-correlation switches (lensing.cu)
+    int flat_local_nonlocal = 0; // den-lensing in the flat-sky limit
+    int flat_nonlocal = 0;       // lensing-lensing in the flat-sky limit
+
     // ---- lensing terms (lensing.cu)
     int lens_n_mu = 128, lens_n_x = 256; // Gauss-Legendre rule sizes
     DevBuf lens_rule;                    // the rule's nodes and weights
@@ -105,6 +110,13 @@ struct coffe_gpu_ctx {
 };
 
 void cg_set_error(coffe_gpu_ctx *ctx, const char *fmt, ...);
+// index of the table I^n_l (half: numerators of half-integers) or -1
+inline int cg_find_term(const coffe_gpu_ctx *ctx, int n, int l, int half = 0)
+{
+    for (int t = 0; t < ctx->n_terms; ++t)
+        if (ctx->term_n[t] == n && ctx->term_l[t] == l && ctx->term_half[t] == half) return t;
+    return -1;
+}
 int cg_ensure(coffe_gpu_ctx *ctx, DevBuf &b, size_t bytes);
 void cg_release(DevBuf &b);
 // Reads and clears the device error bits; maps them to a status.
@@ -116,8 +128,8 @@ int cg_after_launch(coffe_gpu_ctx *ctx, const char *what);
 int bg_init_device(coffe_gpu_ctx *ctx, const coffe_gpu_cosmology_t *c);
 int bg_build_splines(coffe_gpu_ctx *ctx);
 int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n_spectra,
-                    size_t nk, const int *n, const int *l, int n_terms, size_t N, int precision,
-                    unsigned flags);
+                    size_t nk, const int *n, const int *l, const int *half, int n_terms, size_t N,
+                    int precision, unsigned flags);
 int integrals_eval(coffe_gpu_ctx *ctx, int spectrum, int term, const double *r, size_t nq,
                    double *out);
 int multipoles_prepare_background(coffe_gpu_ctx *ctx);
@@ -129,6 +141,6 @@ int multipoles_adjoint_run(coffe_gpu_ctx *ctx, int contrib, int n_req, const int
                            long long total, int n_l, const int *l, const double *bias_scale,
                            const double *growth_scale, const double *grad_out, double *value_out,
                            double *grad_pk, double *grad_bias, double *grad_growth);
-int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,
+int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, int n_req,
                 const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
                 const double *sep, int n_l, const int *l, double *out, long long total);

@@ -727,6 +727,10 @@ __global__ void __launch_bounds__(32 * SR_WARPS)
     const int t = (int)(st_ % n_terms);
     const int s = (int)(st_ / n_terms);
     const int n = tn[t], l = tl[t];
+    if (l < 0) { // half-integer table: the r = 0 and sub-Mpc entries stay NaN
+        if ((threadIdx.x & 31) == 0) tab[((size_t)s * n_terms + t) * len + j] = cg_nan<TO>();
+        return;
+    }
     PkAkima P{kx, pk + (size_t)s * nk, nk};
     QagStore<double> store{sa[w], sb[w], sr[w], se[w], SR_CAP};
     int status = 0;
@@ -803,8 +807,8 @@ bool same_grid(const coffe_gpu_ctx *ctx, const double *k, size_t nk, size_t N,
 } // namespace
 
 int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n_spectra,
-                    size_t nk, const int *n, const int *l, int n_terms, size_t N, int precision,
-                    unsigned flags)
+                    size_t nk, const int *n, const int *l, const int *half, int n_terms, size_t N,
+                    int precision, unsigned flags)
 {
     if (!k || !pk || !n || !l || n_spectra < 1 || n_terms < 1 || n_terms > CG_MAX_TERMS) {
         cg_set_error(ctx, "integrals: bad arguments (n_spectra=%d, n_terms=%d)", n_spectra,
@@ -828,11 +832,19 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
             cg_set_error(ctx, "integrals: k must be positive and strictly increasing");
             return COFFE_GPU_EINVAL;
         }
-    for (int t = 0; t < n_terms; ++t)
-        if (l[t] < 0 || l[t] > 16 || n[t] < -4 || n[t] > 16) {
-            cg_set_error(ctx, "integrals: unsupported term (n=%d, l=%d)", n[t], l[t]);
+    for (int t = 0; t < n_terms; ++t) {
+        const int hf = half ? half[t] : 0;
+        if (hf != 0 && hf != 1) {
+            cg_set_error(ctx, "integrals: half[%d] must be 0 or 1", t);
             return COFFE_GPU_EINVAL;
         }
+        const int lmax = hf ? 33 : 16, nmin = hf ? -8 : -4, nmax = hf ? 33 : 16;
+        if (l[t] < 0 || l[t] > lmax || n[t] < nmin || n[t] > nmax) {
+            cg_set_error(ctx, "integrals: unsupported term (n=%d, l=%d%s)", n[t], l[t],
+                         hf ? ", half-integer numerators" : "");
+            return COFFE_GPU_EINVAL;
+        }
+    }
     const bool mixed = precision == COFFE_GPU_MIXED;
     const int M = (int)N / 2;
     const size_t len = N + CG_N_SMALL_R + 1;
@@ -844,8 +856,11 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     std::vector<int> term_q(n_terms);
     std::vector<double> tq(n_terms), tl(n_terms), tn(n_terms);
     for (int t = 0; t < n_terms; ++t) {
-        const double qnu = select_qnu((double)l[t], (double)n[t]);
-        const double qt = qnu + n[t];
+        // half-integer terms (integrals.c:189-207): n, l are numerators of n/2, l/2
+        const int hf = half ? half[t] : 0;
+        const double lt = hf ? l[t] / 2.0 : (double)l[t], nt = hf ? n[t] / 2.0 : (double)n[t];
+        const double qnu = select_qnu(lt, nt);
+        const double qt = qnu + nt;
         int qi = -1;
         for (size_t j = 0; j < qvals.size(); ++j)
             if (qvals[j] == qt) qi = (int)j;
@@ -855,10 +870,11 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         }
         term_q[t] = qi;
         tq[t] = qnu;
-        tl[t] = l[t];
-        tn[t] = n[t];
+        tl[t] = lt;
+        tn[t] = nt;
         ctx->term_n[t] = n[t];
         ctx->term_l[t] = l[t];
+        ctx->term_half[t] = hf;
         ctx->term_q[t] = qi;
     }
     const int n_q = (int)qvals.size();
@@ -866,6 +882,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     for (int t = 0; t < n_terms; ++t) {
         terms_key.push_back(n[t]);
         terms_key.push_back(l[t]);
+        terms_key.push_back(half ? half[t] : 0);
     }
 
     GridPar g{k[0], k[nk - 1], k[0], 1.0, (int)N, (int)nk};
@@ -909,7 +926,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         meta.n[t] = tn[t];
         meta.tq[t] = term_q[t];
         meta.tn[t] = n[t];
-        meta.tl[t] = l[t];
+        meta.tl[t] = (half && half[t]) ? -1 : l[t]; // -1: no sub-Mpc QAG entries
     }
     for (int q = 0; q < n_q; ++q) meta.qv[q] = qvals[q];
     if ((st = cg_ensure(ctx, ctx->term_meta, sizeof(TermMeta)))) return st;

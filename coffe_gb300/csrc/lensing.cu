@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "ctx.cuh"
+#include "qag.cuh"
 
 namespace {
 
@@ -478,10 +479,139 @@ void gauss_legendre(int n, double *x, double *w)
     }
 }
 
+
+// ------------------------------------------------------------------ flat sky
+#define FLAT_MAX_L 8
+#define FLAT_WARPS 4
+#define FLAT_CAP 128
+
+struct FlatArgs {
+    int n_req, n_l, tab_len, n_terms;
+    double inv_dlog, Om, pref2, pref4, epsrel;
+    int has_b1, has_b2, has_s1, has_s2;
+    int ls[FLAT_MAX_L];
+    int dl_term[FLAT_MAX_L][5];   // half-integer table of each k in the den-lensing sum
+    double dl_coef[FLAT_MAX_L][5]; // (-1)^k 2^-k C(l,k) C(2l-2k,l) (l/2-k)!
+    int ll_term[FLAT_MAX_L];      // integer table (1, l) of lensing-lensing
+    double ll_coef[FLAT_MAX_L];   // (2l+1) l! / 2^l / ((l/2)!)^2
+};
+
+// Akima value of table t of spectrum s at r (NaN outside)
+template <typename TT>
+__device__ __forceinline__ double flat_table(const FlatArgs &a, const TT *__restrict__ tab_x,
+                                             const TT *__restrict__ tab_y, int s, int t, double r)
+{
+    const TT *y = tab_y + ((size_t)s * a.n_terms + t) * a.tab_len;
+    const int i = lens_interval<TT>(tab_x, a.tab_len, (TT)a.inv_dlog, (TT)r);
+    if (i < 0) return cg_nan<double>();
+    return (double)akima_eval_at<TT>(tab_x, y, a.tab_len, i, (TT)r);
+}
+
+// flat-sky density-lensing multipole (functions.c:4136-4253) times 2 pi^2
+// (signal.c:619-630), added to out; one thread per (pair, l)
+template <typename TT>
+__global__ void flat_denlen_kernel(FlatArgs a, LensBg64 g, const TT *__restrict__ tab_x,
+                                   const TT *__restrict__ tab_y, const int *__restrict__ req_spectrum,
+                                   const double *__restrict__ req_z_mean,
+                                   const int64_t *__restrict__ req_offset,
+                                   const double *__restrict__ sep, long long total,
+                                   double *__restrict__ out, int *err)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total * a.n_l) return;
+    const long long item = t / a.n_l;
+    const int j = (int)(t % a.n_l), l = a.ls[j];
+    if (l % 2) return; // odd multipoles are zero (functions.c:4244-4247)
+    const int q = lens_find_request(req_offset, a.n_req, item);
+    const int s = req_spectrum[q];
+    const double z = req_z_mean[q], r = sep[item];
+    const double s1 = a.has_s1 ? spl_eval(g.s1, z) : 0.0, s2 = a.has_s2 ? spl_eval(g.s2, z) : 0.0;
+    const double b1 = a.has_b1 ? spl_eval(g.b1, z) : 1.0, b2 = a.has_b2 ? spl_eval(g.b2, z) : 1.0;
+    double result = 0;
+    for (int k = 0; k <= l / 2; ++k)
+        result += a.dl_coef[j][k] * flat_table<TT>(a, tab_x, tab_y, s, a.dl_term[j][k], r);
+    const double D1 = spl_eval(g.D1, z);
+    result *= -3 * a.Om / CG_PI / 8 * (2 * l + 1) * D1 * D1 * (1 + z) * r *
+              ((2 - 5 * s1) * b2 + (2 - 5 * s2) * b1) * pow(2.0, 1 - l / 2);
+    const double v = 2 * CG_PI * CG_PI * result / sqrt(2 * CG_PI) * a.pref2;
+    if (!isfinite(v)) cg_flag(err, CG_ERR_NONFINITE);
+    out[item * a.n_l + j] += v;
+}
+
+// functions_flatsky_lensing_lensing_multipoles (functions.c:4020-4132) at x
+template <typename TT> struct FlatLL {
+    const FlatArgs *a;
+    const LensBg64 *g;
+    const TT *tab_x, *tab_y;
+    int s, j, l;
+    double z, r, chi_mean, pre;
+    __device__ __forceinline__ double operator()(double x) const
+    {
+        const double lambda = chi_mean * x;
+        const double zl = spl_eval(g->z_of_chi, lambda);
+        const double D1 = spl_eval(g->D1, zl);
+        const double v = pre * flat_table<TT>(*a, tab_x, tab_y, s, a->ll_term[j], x * r) * D1 * D1 *
+                         (1 + zl) * (1 + zl) * (x * (1 - x)) * (x * (1 - x));
+        return l > 0 ? v * x * r * a->pref4 : v * a->pref4;
+    }
+};
+
+// flat-sky lensing-lensing multipole: 2 pi^2 times the QAG integral over x in
+// [0, 1] (signal.c:708-734), added to out; one warp per (pair, even l)
+template <typename TT>
+__global__ void __launch_bounds__(32 * FLAT_WARPS)
+    flat_lenlen_kernel(FlatArgs a, LensBg64 g, const TT *__restrict__ tab_x,
+                       const TT *__restrict__ tab_y, const int *__restrict__ req_spectrum,
+                       const double *__restrict__ req_z_mean, const int64_t *__restrict__ req_offset,
+                       const double *__restrict__ sep, long long total, double *__restrict__ out,
+                       int *err)
+{
+    __shared__ double sa[FLAT_WARPS][FLAT_CAP], sb[FLAT_WARPS][FLAT_CAP], sr[FLAT_WARPS][FLAT_CAP],
+        se[FLAT_WARPS][FLAT_CAP];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long t = (long long)blockIdx.x * FLAT_WARPS + w;
+    if (t >= total * a.n_l) return;
+    const long long item = t / a.n_l;
+    const int j = (int)(t % a.n_l), l = a.ls[j];
+    if (l % 2) return;
+    const int q = lens_find_request(req_offset, a.n_req, item);
+    FlatLL<TT> f;
+    f.a = &a;
+    f.g = &g;
+    f.tab_x = tab_x;
+    f.tab_y = tab_y;
+    f.s = req_spectrum[q];
+    f.j = j;
+    f.l = l;
+    f.z = req_z_mean[q];
+    f.r = sep[item];
+    f.chi_mean = spl_eval(g.chi_of_z, f.z);
+    const double s1 = a.has_s1 ? spl_eval(g.s1, f.z) : 0.0, s2 = a.has_s2 ? spl_eval(g.s2, f.z) : 0.0;
+    f.pre = a.ll_coef[j] * 9 * a.Om * a.Om * (2 - 5 * s1) * (2 - 5 * s2) * pow(f.chi_mean, 3) / 8. /
+            CG_PI;
+    QagStore<double> store{sa[w], sb[w], sr[w], se[w], FLAT_CAP};
+    int status = 0;
+    const double v = qag61_warp<double>(f, 0.0, 1.0, 0.0, a.epsrel, store, 50000, &status);
+    if (lane == 0) {
+        if (status == 1) cg_flag(err, CG_ERR_QAG_LIMIT);
+        const double res = 2 * CG_PI * CG_PI * v;
+        if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
+        out[item * a.n_l + j] += res;
+    }
+}
+
+double host_fact(int n)
+{
+    double r = 1;
+    for (int i = 2; i <= n; ++i) r *= i;
+    return r;
+}
+
 template <typename T, typename S, typename TT>
 int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const LensBgT<S> &gT,
                    const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
-                   const double *sep, double *out, long long total)
+                   const double *sep, double *out, long long total, bool do_single,
+                   bool do_double)
 {
     typedef typename Rec4<TT>::type R;
     int st;
@@ -492,7 +622,7 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
     lens_records_kernel<TT><<<(unsigned)((n_rec + 255) / 256), 256, 0, ctx->stream>>>(
         a, tab_x, (const TT *)ctx->tab_y.p, ctx->n_spectra, rec);
     if ((st = cg_after_launch(ctx, "lens_records_kernel"))) return st;
-    const bool single = (a.contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD)) != 0;
+    const bool single = do_single;
     // pairs per chunk: partials of at most 2^22 (pair, mu) items per kind
     const long long chunk = std::max(1LL, std::min(total, (1LL << 22) / a.n_mu));
     if ((st = cg_ensure(ctx, ctx->lens_part, sizeof(double) * 2 * (size_t)(chunk * a.n_mu))))
@@ -504,10 +634,12 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
         const long long np = std::min(chunk, total - p0);
         a.pair0 = p0;
         a.n_items = np * a.n_mu;
-        lens_double_kernel<T, S, TT><<<(unsigned)a.n_items, LENS_THREADS, 0, ctx->stream>>>(
-            a, g64, gT, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule, part_d,
-            ctx->d_err);
-        if ((st = cg_after_launch(ctx, "lens_double_kernel"))) return st;
+        if (do_double) {
+            lens_double_kernel<T, S, TT><<<(unsigned)a.n_items, LENS_THREADS, 0, ctx->stream>>>(
+                a, g64, gT, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule, part_d,
+                ctx->d_err);
+            if ((st = cg_after_launch(ctx, "lens_double_kernel"))) return st;
+        }
         if (single) {
             const long long blocks = (a.n_items + LENS_THREADS / 32 - 1) / (LENS_THREADS / 32);
             lens_single_kernel<TT><<<(unsigned)blocks, LENS_THREADS, 0, ctx->stream>>>(
@@ -517,7 +649,7 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
         }
         const long long nt = np * a.n_l;
         lens_reduce_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, ctx->stream>>>(
-            a, rule, part_d, single ? part_s : nullptr, np, out, ctx->d_err);
+            a, rule, do_double ? part_d : nullptr, single ? part_s : nullptr, np, out, ctx->d_err);
         if ((st = cg_after_launch(ctx, "lens_reduce_kernel"))) return st;
     }
     return COFFE_GPU_OK;
@@ -527,11 +659,125 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
 
 // Adds the lensing terms (contrib & COFFE_GPU_LEN) to out; the arguments are
 // those multipoles_run has validated, all arrays on the device.
-int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,
+// flat-sky lensing terms (ctx->flat_local_nonlocal / flat_nonlocal)
+static int flatsky_run(coffe_gpu_ctx *ctx, bool denlen, bool lenlen, double epsrel, int n_req,
+                       const int *req_spectrum, const double *req_z_mean,
+                       const int64_t *req_offset, const double *sep, int n_l, const int *l,
+                       double *out, long long total)
+{
+    FlatArgs f;
+    f.n_req = n_req;
+    f.n_l = n_l;
+    f.tab_len = (int)(ctx->N + CG_N_SMALL_R + 1);
+    f.n_terms = ctx->n_terms;
+    f.inv_dlog = (double)ctx->N / log(ctx->kmax / ctx->kmin);
+    f.Om = ctx->Omega0_m;
+    f.pref2 = pow(CG_H0 * ctx->h, 2);
+    f.pref4 = pow(CG_H0 * ctx->h, 4);
+    f.epsrel = epsrel;
+    f.has_b1 = ctx->bias_set[0];
+    f.has_b2 = ctx->bias_set[1];
+    f.has_s1 = ctx->bias_set[2];
+    f.has_s2 = ctx->bias_set[3];
+    for (int j = 0; j < FLAT_MAX_L; ++j) {
+        f.ls[j] = j < n_l ? l[j] : 1;
+        f.ll_term[j] = -1;
+        f.ll_coef[j] = 0;
+        for (int k = 0; k < 5; ++k) {
+            f.dl_term[j][k] = -1;
+            f.dl_coef[j][k] = 0;
+        }
+    }
+    for (int j = 0; j < n_l; ++j) {
+        const int L = l[j];
+        if (L % 2) continue;
+        if (denlen) {
+            if (L / 2 + 1 > 5) {
+                cg_set_error(ctx, "multipoles: flat-sky density-lensing supports l <= 8");
+                return COFFE_GPU_EINVAL;
+            }
+            for (int k = 0; k <= L / 2; ++k) {
+                const int t = cg_find_term(ctx, L - 2 * k + 3, L - 2 * k + 1, 1);
+                if (t < 0) {
+                    cg_set_error(ctx, "multipoles: flat-sky density-lensing needs the half-integer "
+                                      "integral (%d/2, %d/2)", L - 2 * k + 3, L - 2 * k + 1);
+                    return COFFE_GPU_ESTATE;
+                }
+                f.dl_term[j][k] = t;
+                f.dl_coef[j][k] = pow(-1, k) / pow(2, k) * host_fact(L) / host_fact(k) /
+                                  host_fact(L - k) * host_fact(2 * L - 2 * k) / host_fact(L) /
+                                  host_fact(L - 2 * k) * host_fact(L / 2 - k);
+            }
+        }
+        if (lenlen) {
+            const int t = cg_find_term(ctx, 1, L);
+            if (t < 0 || !ctx->int_small_r) {
+                cg_set_error(ctx, "multipoles: flat-sky lensing-lensing needs the integral (1, %d) "
+                                  "with its r = 0 and sub-Mpc entries (COFFE_GPU_SMALL_R)", L);
+                return COFFE_GPU_ESTATE;
+            }
+            f.ll_term[j] = t;
+            f.ll_coef[j] = (2 * L + 1) * host_fact(L) / pow(2, L) / pow(host_fact(L / 2), 2);
+        }
+    }
+    LensBg64 g;
+    g.chi_of_z = ctx->bg[BG_CHI_OF_Z].v64();
+    g.z_of_chi = ctx->bg[BG_Z_OF_CHI].v64();
+    g.D1 = ctx->bg[BG_D1].v64();
+    g.f = ctx->bg[BG_F].v64();
+    g.a = ctx->bg[BG_A].v64();
+    g.b1 = ctx->bias[0].v64();
+    g.b2 = ctx->bias[1].v64();
+    g.s1 = ctx->bias[2].v64();
+    g.s2 = ctx->bias[3].v64();
+    const long long items = total * n_l;
+    int st;
+    const bool mixed = ctx->int_precision == COFFE_GPU_MIXED;
+    if (denlen) {
+        const unsigned blocks = (unsigned)((items + 127) / 128);
+        if (mixed)
+            flat_denlen_kernel<float><<<blocks, 128, 0, ctx->stream>>>(
+                f, g, (const float *)ctx->tab_x32.p, (const float *)ctx->tab_y.p, req_spectrum,
+                req_z_mean, req_offset, sep, total, out, ctx->d_err);
+        else
+            flat_denlen_kernel<double><<<blocks, 128, 0, ctx->stream>>>(
+                f, g, (const double *)ctx->tab_x.p, (const double *)ctx->tab_y.p, req_spectrum,
+                req_z_mean, req_offset, sep, total, out, ctx->d_err);
+        if ((st = cg_after_launch(ctx, "flat_denlen_kernel"))) return st;
+    }
+    if (lenlen) {
+        const unsigned blocks = (unsigned)((items + FLAT_WARPS - 1) / FLAT_WARPS);
+        if (mixed)
+            flat_lenlen_kernel<float><<<blocks, 32 * FLAT_WARPS, 0, ctx->stream>>>(
+                f, g, (const float *)ctx->tab_x32.p, (const float *)ctx->tab_y.p, req_spectrum,
+                req_z_mean, req_offset, sep, total, out, ctx->d_err);
+        else
+            flat_lenlen_kernel<double><<<blocks, 32 * FLAT_WARPS, 0, ctx->stream>>>(
+                f, g, (const double *)ctx->tab_x.p, (const double *)ctx->tab_y.p, req_spectrum,
+                req_z_mean, req_offset, sep, total, out, ctx->d_err);
+        if ((st = cg_after_launch(ctx, "flat_lenlen_kernel"))) return st;
+    }
+    return COFFE_GPU_OK;
+}
+
+int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, int n_req,
                 const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
                 const double *sep, int n_l, const int *l, double *out, long long total)
 {
     if (!(contrib & COFFE_GPU_LEN) || total <= 0) return COFFE_GPU_OK;
+    // which forms of the single- and double-integrated terms (signal.c:607-754)
+    const bool only_cross = (contrib & COFFE_GPU_ONLY_CROSS) != 0;
+    const bool want_single = (contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD)) != 0;
+    const bool single_full = want_single && !ctx->flat_local_nonlocal;
+    const bool single_flat = want_single && ctx->flat_local_nonlocal && (contrib & COFFE_GPU_DEN);
+    const bool double_full = !only_cross && !ctx->flat_nonlocal;
+    const bool double_flat = !only_cross && ctx->flat_nonlocal;
+    int st;
+    if (single_flat || double_flat)
+        if ((st = flatsky_run(ctx, single_flat, double_flat, epsrel, n_req, req_spectrum,
+                              req_z_mean, req_offset, sep, n_l, l, out, total)))
+            return st;
+    if (!single_full && !double_full) return COFFE_GPU_OK;
     if (!ctx->int_small_r) {
         cg_set_error(ctx, "multipoles: lensing needs the r = 0 and sub-Mpc table entries "
                           "(integrals_init with COFFE_GPU_SMALL_R)");
@@ -540,9 +786,7 @@ int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,
     LensArgs a;
     const int want[LENS_NT][2] = {{0, 0}, {0, 2}, {0, 4}, {1, 1}, {1, 3}, {2, 0}};
     for (int t = 0; t < LENS_NT; ++t) {
-        a.term[t] = -1;
-        for (int k = 0; k < ctx->n_terms; ++k)
-            if (ctx->term_n[k] == want[t][0] && ctx->term_l[k] == want[t][1]) a.term[t] = k;
+        a.term[t] = cg_find_term(ctx, want[t][0], want[t][1]);
         if (a.term[t] < 0) {
             cg_set_error(ctx, "multipoles: lensing needs the integral (n=%d, l=%d)", want[t][0],
                          want[t][1]);
@@ -554,7 +798,7 @@ int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,
     a.n_mu = ctx->lens_n_mu;
     a.n_x = ctx->lens_n_x;
     a.nh = (a.n_x % 2 == 0) ? a.n_x / 2 : 0;
-    a.contrib = contrib;
+    a.contrib = contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD | COFFE_GPU_LEN);
     a.tab_len = (int)(ctx->N + CG_N_SMALL_R + 1);
     a.n_terms = ctx->n_terms;
     a.inv_dlog = (double)ctx->N / log(ctx->kmax / ctx->kmin);
@@ -568,7 +812,6 @@ int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,
     a.pair0 = 0;
     a.n_items = 0;
     for (int i = 0; i < 8; ++i) a.ls[i] = i < n_l ? l[i] : 0;
-    int st;
     // the Gauss-Legendre rule: mu[n_mu], w_mu[n_mu], x[n_x], w_x[n_x], x_h[nh], w_h[nh]
     if (ctx->lens_rule_mu != a.n_mu || ctx->lens_rule_x != a.n_x) {
         std::vector<double> r(2 * (size_t)a.n_mu + 2 * (size_t)a.n_x + 2 * (size_t)a.nh);
@@ -597,9 +840,11 @@ int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,
     if (precision == COFFE_GPU_MIXED) {
         LensBgT<Spl32> gT{ctx->bg[BG_Z_OF_CHI].v32(), ctx->bg[BG_D1].v32(), ctx->bg[BG_A].v32()};
         return lensing_launch<float, Spl32, float>(ctx, a, g64, gT, req_spectrum, req_z_mean,
-                                                   req_offset, sep, out, total);
+                                                   req_offset, sep, out, total, single_full,
+                                                   double_full);
     }
     LensBgT<Spl64> gT{ctx->bg[BG_Z_OF_CHI].v64(), ctx->bg[BG_D1].v64(), ctx->bg[BG_A].v64()};
     return lensing_launch<double, Spl64, double>(ctx, a, g64, gT, req_spectrum, req_z_mean,
-                                                 req_offset, sep, out, total);
+                                                 req_offset, sep, out, total, single_full,
+                                                 double_full);
 }

@@ -241,8 +241,9 @@ template <typename T, typename S> struct Xi {
         const T b1 = bg.has_b1 ? spl_eval(bg.b1, z1) : T(1);
         const T b2 = bg.has_b2 ? spl_eval(bg.b2, z2) : T(1);
         T result = T(0);
-        if (contrib & COFFE_GPU_DEN) result += b1 * b2 * I00;
-        if (contrib & COFFE_GPU_RSD) {
+        const bool autos = !(contrib & COFFE_GPU_ONLY_CROSS); // functions.c:129-133, 230-234
+        if ((contrib & COFFE_GPU_DEN) && autos) result += b1 * b2 * I00;
+        if ((contrib & COFFE_GPU_RSD) && autos) {
             const T c2 = c * c;
             const T q4 = omm * omm * (T(3) * c2 - T(10) * c + T(19)) * T(0.25) +
                          T(4) * mu2 * omm * (c2 - T(5) * c - T(2)) +
@@ -748,8 +749,8 @@ int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel
                      ctx->int_precision);
         return COFFE_GPU_EINVAL;
     }
-    if (!(contrib & 7) || (contrib & ~7)) {
-        cg_set_error(ctx, "multipoles: contrib must select den, rsd and/or len");
+    if (!(contrib & 7) || (contrib & ~15)) {
+        cg_set_error(ctx, "multipoles: contrib must select den, rsd and/or len (+ only-cross)");
         return COFFE_GPU_EINVAL;
     }
     if (!(epsrel > 0)) {
@@ -763,13 +764,10 @@ int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel
     MpArgs a;
     a.n_req = n_req;
     a.n_l = n_l;
-    a.contrib = contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD);
-    a.t00 = a.t02 = a.t04 = -1;
-    for (int t = 0; t < ctx->n_terms; ++t) {
-        if (ctx->term_n[t] == 0 && ctx->term_l[t] == 0) a.t00 = t;
-        if (ctx->term_n[t] == 0 && ctx->term_l[t] == 2) a.t02 = t;
-        if (ctx->term_n[t] == 0 && ctx->term_l[t] == 4) a.t04 = t;
-    }
+    a.contrib = contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD | COFFE_GPU_ONLY_CROSS);
+    a.t00 = cg_find_term(ctx, 0, 0);
+    a.t02 = cg_find_term(ctx, 0, 2);
+    a.t04 = cg_find_term(ctx, 0, 4);
     if (a.t00 < 0 || a.t02 < 0 || a.t04 < 0) {
         cg_set_error(ctx, "multipoles: integrals (0,0), (0,2), (0,4) are required");
         return COFFE_GPU_ESTATE;
@@ -794,16 +792,16 @@ int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel
     if (!(contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD))) {
         // lensing only: no nonintegrated terms (signal.c:472-520 returns 0)
         CG_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(double) * (size_t)total * n_l, ctx->stream));
-        return lensing_run(ctx, contrib, precision, n_req, req_spectrum, req_z_mean, req_offset,
-                           sep, n_l, l, out, total);
+        return lensing_run(ctx, contrib, precision, epsrel, n_req, req_spectrum, req_z_mean,
+                           req_offset, sep, n_l, l, out, total);
     }
     a.retry_cap = total * n_l;
     if ((st = cg_ensure(ctx, ctx->mp_retry, 256 + sizeof(int2) * (size_t)a.retry_cap))) return st;
     if ((st = multipoles_nonintegrated(ctx, a, precision, req_spectrum, req_z_mean, req_offset,
                                        sep, out, total)))
         return st;
-    return lensing_run(ctx, contrib, precision, n_req, req_spectrum, req_z_mean, req_offset, sep,
-                       n_l, l, out, total);
+    return lensing_run(ctx, contrib, precision, epsrel, n_req, req_spectrum, req_z_mean,
+                       req_offset, sep, n_l, l, out, total);
 }
 
 // the den/rsd nonintegrated multipoles of a validated call
@@ -1101,12 +1099,9 @@ extern "C" int coffe_gpu_multipoles_noalloc(coffe_gpu_ctx_t *ctx, int contrib, i
     a.n_req = n_req;
     a.n_l = n_l;
     a.contrib = contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD);
-    a.t00 = a.t02 = a.t04 = -1;
-    for (int t = 0; t < ctx->n_terms; ++t) {
-        if (ctx->term_n[t] == 0 && ctx->term_l[t] == 0) a.t00 = t;
-        if (ctx->term_n[t] == 0 && ctx->term_l[t] == 2) a.t02 = t;
-        if (ctx->term_n[t] == 0 && ctx->term_l[t] == 4) a.t04 = t;
-    }
+    a.t00 = cg_find_term(ctx, 0, 0);
+    a.t02 = cg_find_term(ctx, 0, 2);
+    a.t04 = cg_find_term(ctx, 0, 4);
     if (a.t00 < 0 || a.t02 < 0 || a.t04 < 0) {
         cg_set_error(ctx, "multipoles_noalloc: integrals (0,0), (0,2), (0,4) are required");
         return COFFE_GPU_ESTATE;

@@ -145,6 +145,17 @@ int coffe_gpu_integrals_init(coffe_gpu_ctx_t *ctx, const double *k, const double
                              int n_spectra, size_t nk, const int *n, const int *l,
                              int n_terms, size_t N, int precision, unsigned flags);
 
+/* coffe_gpu_integrals_init with half-integer terms (the HALF_INTEGER state of
+   coffe_integral_t, integrals.c:189-207): where half[t] = 1, n[t] and l[t] are
+   the numerators of n/2 and l/2 (e.g. (3, 1) is I^{3/2}_{1/2}, as the flat-sky
+   density-lensing multipoles read them, functions.c:4209-4228).  Their r = 0
+   and sub-Mpc entries are not computed (NaN) even with COFFE_GPU_SMALL_R; the
+   FFTLog part serves r >= the third FFT node.  half may be NULL (all integer). */
+int coffe_gpu_integrals_init_ex(coffe_gpu_ctx_t *ctx, const double *k, const double *pk,
+                                int n_spectra, size_t nk, const int *n, const int *l,
+                                const int *half, int n_terms, size_t N, int precision,
+                                unsigned flags);
+
 /* Copies table (spectrum, term) out: x and y of coffe_gpu_integral_table_len(N)
    points (the arrays coffe_integrals_init hands to coffe_init_spline,
    integrals.c:652-658). */
@@ -187,6 +198,21 @@ int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, doubl
                          int n_req, const int *req_spectrum, const double *req_z_mean,
                          const int64_t *req_offset, const double *sep, int n_l,
                          const int *l, double *out, int arrays_on_device);
+
+/* Contribution bit: only the cross-correlations of the selected terms
+   (only_cross_correlations, functions.c:129-362, 3516-3519): den-den, rsd-rsd
+   and lensing-lensing are dropped, den-rsd and the den/rsd-lensing terms kept. */
+#define COFFE_GPU_ONLY_CROSS 8
+
+/* Flat-sky forms of the lensing terms, as the flatsky_local_nonlocal and
+   flatsky_nonlocal flags select them in coffe_integrate (signal.c:607-671,
+   704-754): local_nonlocal != 0 replaces the single-integrated den/rsd-lensing
+   terms by the flat-sky density-lensing multipoles (closed sums over the
+   half-integer tables ((l-2k+3)/2, (l-2k+1)/2), functions.c:4136-4253; RSD-
+   lensing vanishes in that limit); nonlocal != 0 replaces lensing-lensing by
+   its flat-sky multipoles (even l; a QAG integral over the line of sight of the
+   integer tables (1, l), functions.c:4020-4132).  Default: both off. */
+int coffe_gpu_set_flatsky(coffe_gpu_ctx_t *ctx, int local_nonlocal, int nonlocal);
 
 /* Quadrature rule of the lensing terms (contrib & COFFE_GPU_LEN), which
    replaces the reference's Cuhre cubature of the unit cube (common.c:1074-1110,

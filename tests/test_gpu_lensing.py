@@ -138,3 +138,69 @@ def test_lensing_needs_small_r_and_terms(gpu_ctx, lens_setup):
     with pytest.raises(CoffeGpuError) as ei:
         gpu_ctx.multipoles([0], [1.0], [0, 1], [50.0], (0,), contrib=LEN)
     assert ei.value.status == -5
+
+
+# ------------------------------------------------------------------- flat sky
+FLAT_TERMS = [(0, 0), (0, 2), (0, 4), (1, 0), (1, 2), (1, 4), (3, 1, 1), (5, 3, 1), (7, 5, 1)]
+ONLY_CROSS = 8
+
+
+@pytest.fixture(scope="module")
+def flat_setup(oracle):
+    from coffe_gb300 import workloads
+
+    c = workloads.cfg1()
+    k, pk = c["k"], c["pk"]
+    bg = oracle.background_nodes(0.31, 0.05, 9e-5, H, 10000)
+    m = oracle.Model(bg, H, 0.31)
+    for t in FLAT_TERMS:
+        if len(t) == 3:
+            x, y = oracle.integral_table_half(k, pk, t[0], t[1], 4096)
+            m.set_integral_half(t[0], t[1], x, y)
+        else:
+            x, y = oracle.integral_table(k, pk, t[0], t[1], 4096, with_small_r=True)
+            m.set_integral(t[0], t[1], x, y)
+    return k, pk, m
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("mixed", 1e-4)])
+def test_flatsky_lensing_matches_oracle(gpu_ctx, flat_setup, prec, tol):
+    """den + flat-sky density-lensing + flat-sky lensing-lensing (l = 0, 2, 4)."""
+    k, pk, m = flat_setup
+    sep = np.array([20.0, 55.0, 120.0, 300.0]) / H
+    ls = (0, 2, 4)
+    gpu_ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+    gpu_ctx.integrals_init(k, pk[None, :], FLAT_TERMS, N=4096, precision=prec, small_r=True)
+    gpu_ctx.set_flatsky(True, True)
+    try:
+        got = gpu_ctx.multipoles([0], [1.5], [0, len(sep)], sep, ls, contrib=DEN | LEN,
+                                 precision=prec)
+    finally:
+        gpu_ctx.set_flatsky(False, False)
+    ref = np.array([[m.multipole(DEN, 1.5, r, l) + m.flatsky_density_lensing(1.5, r, l) +
+                     m.flatsky_lensing_lensing(1.5, r, l) for l in ls] for r in sep])
+    e = _rel(got, ref)
+    print(prec, "flat-sky max rel error", e)
+    assert e < tol, e
+
+
+def test_flatsky_golden_through_gpu(gpu_ctx, golden, class_pk):
+    """The reference's flat-sky golden multipoles (test_coffe.py:328-380): lensing-
+    lensing alone, and density-lensing with only cross-correlations."""
+    k, pk = class_pk
+    gpu_ctx.background_init(0.3, 0.05, 9e-5, H, 10000)
+    gpu_ctx.integrals_init(k, pk[None, :], FLAT_TERMS, N=8192, precision="fp64", small_r=True)
+    sep = golden["flatsky_lensing_lensing_multipoles0"][:, 0] / H
+    try:
+        gpu_ctx.set_flatsky(False, True)
+        ll = gpu_ctx.multipoles([0], [1.0], [0, len(sep)], sep, (0, 2, 4), contrib=LEN)
+        gpu_ctx.set_flatsky(True, True)
+        dl = gpu_ctx.multipoles([0], [1.0], [0, len(sep)], sep, (0, 2, 4),
+                                contrib=DEN | LEN | ONLY_CROSS)
+    finally:
+        gpu_ctx.set_flatsky(False, False)
+    for j, l in enumerate((0, 2, 4)):
+        assert np.allclose(ll[:, j], golden[f"flatsky_lensing_lensing_multipoles{l}"][:, 1],
+                           rtol=5e-4), (l, ll[:, j])
+        assert np.allclose(dl[:, j], golden[f"flatsky_density_lensing_multipoles{l}"][:, 1],
+                           rtol=5e-4), (l, dl[:, j])
