@@ -417,9 +417,18 @@ def ours(args, rank, world, local_rank):
     dev_fp64, wall_fp64, _ = timed("fp64", k64)
 
     # accuracy of the mixed path against the FP64 path on the full batch (the
-    # FP64 path itself matches the CPU oracle to 1e-10 in the parity tests)
+    # FP64 path itself matches the CPU oracle to 1e-10 in the parity tests);
+    # the replayed graph must give the direct launch's output bit for bit
+    graph_equal = None
+    if "mixed" in graphs:
+        graphs["mixed"][0].replay()
+        ctx.synchronize()
+        replayed = outs["mixed"].clone()
     step("mixed")
     retries = {"mixed": ctx.last_retries()}
+    if "mixed" in graphs:
+        ctx.synchronize()
+        graph_equal = bool(torch.equal(replayed, outs["mixed"]))
     step("fp64")
     retries["fp64"] = ctx.last_retries()
     ctx.synchronize()
@@ -510,7 +519,7 @@ def ours(args, rank, world, local_rank):
                    "n_spectra": args.n_spectra, "requests": len(batch.req_spectrum),
                    "separations": n_sep, "evals_per_step": n_evals,
                    "l2": "flushed between timed steps (256 MiB write outside the events)",
-                   "cuda_graph": bool(graphs),
+                   "cuda_graph": bool(graphs), "graph_output_equals_direct": graph_equal,
                    "parallelism": f"replicas x{world}"},
         "fp64": {"value": fp64_value, "unit": UNIT, "steps": k64,
                  "ms_per_step": 1e3 * dev_fp64 / k64},

@@ -144,11 +144,13 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
                       &ctx->qfac,     &ctx->modec,  &ctx->postf,   &ctx->twid,   &ctx->twid32,
                       &ctx->spec,     &ctx->req_buf, &ctx->term_meta, &ctx->zrec64,
                       &ctx->zrec32,   &ctx->mp_retry, &ctx->term_df,
-                      &ctx->samp_f32, &ctx->csfac32, &ctx->mp_nodes,
+                      &ctx->samp_f32, &ctx->csfac32,
                       &ctx->lens_rule, &ctx->lens_rec, &ctx->lens_part,
-                      &ctx->cov_buf,  &ctx->cov_out, &ctx->adj_buf, &ctx->csband};
+                      &ctx->cov_buf,  &ctx->cov_out, &ctx->adj_buf, &ctx->csband,
+                      &ctx->samp_tdf, &ctx->qfac_df, &ctx->pk_df};
     spline_free(ctx->cov_pk);
     for (DevBuf *b : bufs) cg_release(*b);
+    for (auto &slot : ctx->mp_node_slots) cg_release(slot.buf);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);

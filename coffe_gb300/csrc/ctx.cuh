@@ -67,6 +67,9 @@ struct coffe_gpu_ctx {
     DevBuf samp_f32;  // N float4 (dx, h, 1/h, -) for the mixed path
     DevBuf csfac32;   // 4 * nk floats: spline factors for the mixed path
     DevBuf csband;    // (nk - 2) x 25 floats: band of the inverse spline matrix
+    DevBuf samp_tdf;  // N float2: double-float dx / h of each FFT node (mixed path)
+    DevBuf qfac_df;   // n_q * N float2: double-float windowed bias (mixed path)
+    DevBuf pk_df;     // n_spectra * nk float2: double-float input spectra (mixed path)
     DevBuf qfac;      // n_q * N doubles: (kmax/kmin)^((3-q) i/N) W(k_i)
     DevBuf modec;     // n_terms * (N/2+1) double2: W_mode/L * M_{q,l}(t)
     DevBuf postf;     // n_terms * N doubles: prefactor * r^(n-l)
@@ -85,9 +88,18 @@ struct coffe_gpu_ctx {
     // ---- multipole request staging (host-pointer calls) and retry list
     DevBuf req_buf;
     DevBuf mp_retry;
-    DevBuf mp_nodes; // first-panel node table of the last multipole list
-    int mp_nodes_nl = 0, mp_nodes_prec = -1, mp_nodes_mirror = -1;
-    int mp_nodes_ls[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // first-panel node tables, one per (multipole list, precision, layout):
+    // each is written once and never overwritten while fewer than
+    // CG_NODE_SLOTS distinct tables are in use, so a captured launch that
+    // reads one stays valid when calls of another precision run in between
+    struct NodeSlot {
+        DevBuf buf;
+        int nl = 0, prec = -1, mirror = -1;
+        int ls[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    };
+    static constexpr int CG_NODE_SLOTS = 8;
+    NodeSlot mp_node_slots[CG_NODE_SLOTS];
+    int mp_node_next = 0;
 
     // ---- flat-sky lensing and cross-correlation switches (lensing.cu)
     int flat_local_nonlocal = 0; // den-lensing in the flat-sky limit

@@ -106,7 +106,8 @@ __global__ void sampling_kernel(GridPar g, const double *__restrict__ kx, int *_
                                 double *__restrict__ dxs, float4 *__restrict__ sf32, int n_q,
                                 const double *__restrict__ qv, double *__restrict__ qfac,
                                 double *__restrict__ modew, double *__restrict__ tab_x,
-                                float *__restrict__ tab_x32)
+                                float *__restrict__ tab_x32, float2 *__restrict__ tdf,
+                                float2 *__restrict__ qfac_df)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = g.N;
@@ -129,8 +130,15 @@ __global__ void sampling_kernel(GridPar g, const double *__restrict__ kx, int *_
         dxs[i] = ki - kx[lo];
         const double hl = kx[lo + 1] - kx[lo];
         sf32[i] = make_float4((float)(ki - kx[lo]), (float)hl, (float)(1.0 / hl), 0.f);
+        const dfl t = df_from_double((ki - kx[lo]) / hl); // mixed path: position in the interval
+        tdf[i] = make_float2(t.hi, t.lo);
         const double w = twofast_window(ki, g.kmin, xmax_w, xleft_w, xright_w);
-        for (int q = 0; q < n_q; ++q) qfac[(size_t)q * N + i] = pow(ratio, (3. - qv[q]) * i / N) * w;
+        for (int q = 0; q < n_q; ++q) {
+            const double qf = pow(ratio, (3. - qv[q]) * i / N) * w;
+            qfac[(size_t)q * N + i] = qf;
+            const dfl qd = df_from_double(qf);
+            qfac_df[(size_t)q * N + i] = make_float2(qd.hi, qd.lo);
+        }
         const double ri = g.r0 * pow(ratio, (double)i / N);
         tab_x[CG_N_SMALL_R + 1 + i] = ri;
         tab_x32[CG_N_SMALL_R + 1 + i] = (float)ri;
@@ -308,20 +316,27 @@ __global__ void cspline_c_kernel(const double *__restrict__ x, const double *__r
 #define CS_BAND 12
 #define CS_TILE 256
 __global__ void __launch_bounds__(CS_TILE)
-    cspline_band_kernel(const double *__restrict__ pk, const float *__restrict__ band,
+    cspline_band_kernel(const float2 *__restrict__ pkdf, const float *__restrict__ band,
                         const float *__restrict__ fac32, int nk, float *__restrict__ cc)
 {
+    __shared__ float y_s[CS_TILE + 2 * CS_BAND + 2];
     __shared__ float rhs_s[CS_TILE + 2 * CS_BAND];
     const int s = blockIdx.y;
     const int i0 = blockIdx.x * CS_TILE;
     const int m = nk - 2;
-    const double *y = pk + (size_t)s * nk;
+    const float2 *y = pkdf + (size_t)s * nk;
     const float *g = fac32 + 2 * nk;
+    // the float (high) parts of the samples this tile reads, once each
+    for (int t = threadIdx.x; t < CS_TILE + 2 * CS_BAND + 2; t += blockDim.x) {
+        const int i = i0 - CS_BAND + t;
+        y_s[t] = (i >= 0 && i < nk) ? y[i].x : 0.f;
+    }
+    __syncthreads();
     for (int t = threadIdx.x; t < CS_TILE + 2 * CS_BAND; t += blockDim.x) {
         const int i = i0 - CS_BAND + t;
         float v = 0.f;
         if (i >= 0 && i < m) {
-            const float ya = (float)y[i], yb = (float)y[i + 1], yc = (float)y[i + 2];
+            const float ya = y_s[t], yb = y_s[t + 1], yc = y_s[t + 2];
             v = 3.f * ((yc - yb) * g[i + 1] - (yb - ya) * g[i]);
         }
         rhs_s[t] = v;
@@ -521,35 +536,46 @@ __device__ void smem_fft_df(float4 *buf, int logM, const float4 *__restrict__ tw
     }
 }
 
-// Mixed-path sampling: the secant part y0 + dx (y1 - y0)/h in FP64, the
-// spline-curvature correction dx (-h (c1 + 2 c0)/3 + dx (c0 + d dx)) in float
-// (a relative correction of size ~(h/k)^2, so float is far below the target).
-__device__ __forceinline__ double sample_input_mixed(const double *__restrict__ y,
-                                                     const float *__restrict__ c,
-                                                     const double *__restrict__ gi,
-                                                     const int *__restrict__ idx,
-                                                     const double *__restrict__ dxs,
-                                                     const float4 *__restrict__ sf,
-                                                     const double *__restrict__ qf, int i)
+// The input spectra as double-float pairs, one conversion per sample: the
+// mixed path's only FP64 work per spectrum (the FP64 pipe is ~1/64 of FP32).
+__global__ void pk_split_kernel(const double *__restrict__ pk, long long count,
+                                float2 *__restrict__ out)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const dfl d = df_from_double(pk[i]);
+    out[i] = make_float2(d.hi, d.lo);
+}
+
+// Mixed-path sampling in double-float: the secant part y0 + t (y1 - y0),
+// t = dx / h, plus the spline-curvature correction dx (-h (c1 + 2 c0)/3 +
+// dx (c0 + d dx)) in float (a relative correction of size ~(h/k)^2, so float
+// is far below the target), times the windowed bias.
+__device__ __forceinline__ dfl sample_input_df(const float2 *__restrict__ y,
+                                               const float *__restrict__ c,
+                                               const int *__restrict__ idx,
+                                               const float2 *__restrict__ tdf,
+                                               const float4 *__restrict__ sf,
+                                               const float2 *__restrict__ qf, int i)
 {
     const int j = idx[i];
-    if (j < 0) return cg_nan<double>();
-    const double y0 = y[j];
-    const double main = fma(dxs[i], (y[j + 1] - y0) * gi[j], y0);
+    if (j < 0) return dfl{cg_nan<float>(), 0.f};
+    const float2 a = y[j], b = y[j + 1], t = tdf[i], q = qf[i];
+    const dfl y0{a.x, a.y};
+    const dfl secant = df_add(y0, df_mul(dfl{t.x, t.y}, df_sub(dfl{b.x, b.y}, y0)));
     const float4 f = sf[i]; // (dx, h, 1/h, -)
     const float c0 = c[j], c1 = c[j + 1];
     const float d = (c1 - c0) * f.z * (1.f / 3.f);
     const float corr = f.x * (-f.y * (c1 + 2.f * c0) * (1.f / 3.f) + f.x * (c0 + d * f.x));
-    return (main + (double)corr) * qf[i];
+    return df_mul(df_add(secant, dfl{corr, 0.f}), dfl{q.x, q.y});
 }
 
-__global__ void fftlog_forward_df_kernel(GridPar g, const double *__restrict__ pk,
+__global__ void fftlog_forward_df_kernel(GridPar g, const float2 *__restrict__ pkdf,
                                          const float *__restrict__ cc32,
-                                         const double *__restrict__ fac,
                                          const int *__restrict__ idx,
-                                         const double *__restrict__ dxs,
+                                         const float2 *__restrict__ tdf,
                                          const float4 *__restrict__ sf32,
-                                         const double *__restrict__ qfac,
+                                         const float2 *__restrict__ qfac_df,
                                          const float2 *__restrict__ modew_df,
                                          const float4 *__restrict__ twdf, int n_q,
                                          float4 *__restrict__ spec, int *err)
@@ -560,14 +586,12 @@ __global__ void fftlog_forward_df_kernel(GridPar g, const double *__restrict__ p
     const int s = blockIdx.x, qi = blockIdx.y;
     const int N = g.N, M = N / 2;
     const int logM = 31 - __clz(M);
-    const double *y = pk + (size_t)s * g.nk;
+    const float2 *y = pkdf + (size_t)s * g.nk;
     const float *c = cc32 + (size_t)s * g.nk;
-    const double *gi = fac + 2 * (size_t)g.nk;
     bool bad = false;
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        const double v = sample_input_mixed(y, c, gi, idx, dxs, sf32, qfac + (size_t)qi * N, i);
-        if (!isfinite(v)) bad = true;
-        const dfl d = df_from_double(v);
+        const dfl d = sample_input_df(y, c, idx, tdf, sf32, qfac_df + (size_t)qi * N, i);
+        if (!isfinite(d.hi)) bad = true;
         const int jj = __brev((unsigned)(i >> 1)) >> (32 - logM);
         buf2[2 * jj + (i & 1)] = make_float2(d.hi, d.lo);
     }
@@ -903,6 +927,8 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         if ((st = cg_ensure(ctx, ctx->samp_dx, sizeof(double) * N))) return st;
         if ((st = cg_ensure(ctx, ctx->samp_f32, sizeof(float4) * N))) return st;
         if ((st = cg_ensure(ctx, ctx->csfac32, sizeof(float) * 4 * nk))) return st;
+        if ((st = cg_ensure(ctx, ctx->samp_tdf, sizeof(float2) * N))) return st;
+        if ((st = cg_ensure(ctx, ctx->qfac_df, sizeof(float2) * N * n_q))) return st;
         if ((st = cg_ensure(ctx, ctx->qfac, sizeof(double) * N * n_q))) return st;
         if ((st = cg_ensure(ctx, ctx->modec, sizeof(double2) * (M + 1) * n_terms + sizeof(double) * (M + 1)))) return st;
         if ((st = cg_ensure(ctx, ctx->postf, sizeof(double) * N * n_terms))) return st;
@@ -971,7 +997,8 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         sampling_kernel<<<((int)N + tb) / tb, tb, 0, ctx->stream>>>(
             g, (const double *)ctx->kgrid.p, (int *)ctx->samp_idx.p, (double *)ctx->samp_dx.p,
             (float4 *)ctx->samp_f32.p, n_q, d_meta->qv, (double *)ctx->qfac.p, modew,
-            (double *)ctx->tab_x.p, (float *)ctx->tab_x32.p);
+            (double *)ctx->tab_x.p, (float *)ctx->tab_x32.p, (float2 *)ctx->samp_tdf.p,
+            (float2 *)ctx->qfac_df.p);
         if ((st = cg_after_launch(ctx, "sampling_kernel"))) return st;
         dim3 tg(((int)N + tb - 1) / tb + 1, n_terms);
         term_tables_kernel<<<tg, tb, 0, ctx->stream>>>(g, n_terms, d_meta->q, d_meta->l,
@@ -992,8 +1019,14 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     }
     // per spectrum: natural-spline coefficients, forward FFTs, inverse FFTs
     if (mixed) {
+        if ((st = cg_ensure(ctx, ctx->pk_df, sizeof(float2) * nk * n_spectra))) return st;
+        const long long cnt = (long long)nk * n_spectra;
+        pk_split_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, ctx->stream>>>(
+            d_pk, cnt, (float2 *)ctx->pk_df.p);
+        if ((st = cg_after_launch(ctx, "pk_split_kernel"))) return st;
         cspline_band_kernel<<<dim3(((int)nk - 2 + CS_TILE - 1) / CS_TILE, n_spectra), CS_TILE, 0,
-                              ctx->stream>>>(d_pk, (const float *)ctx->csband.p,
+                              ctx->stream>>>((const float2 *)ctx->pk_df.p,
+                                             (const float *)ctx->csband.p,
                                              (const float *)ctx->csfac32.p, (int)nk,
                                              (float *)ctx->csc.p);
         if ((st = cg_after_launch(ctx, "cspline_band_kernel"))) return st;
@@ -1012,9 +1045,9 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_df_kernel,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         fftlog_forward_df_kernel<<<gf, fft_threads, smem, ctx->stream>>>(
-            g, d_pk, (const float *)ctx->csc.p, (const double *)ctx->csfac.p,
-            (const int *)ctx->samp_idx.p, (const double *)ctx->samp_dx.p,
-            (const float4 *)ctx->samp_f32.p, (const double *)ctx->qfac.p, wdf,
+            g, (const float2 *)ctx->pk_df.p, (const float *)ctx->csc.p,
+            (const int *)ctx->samp_idx.p, (const float2 *)ctx->samp_tdf.p,
+            (const float4 *)ctx->samp_f32.p, (const float2 *)ctx->qfac_df.p, wdf,
             (const float4 *)ctx->twid32.p, n_q, (float4 *)ctx->spec.p, ctx->d_err);
         if ((st = cg_after_launch(ctx, "fftlog_forward_df_kernel"))) return st;
         fftlog_inverse_df_kernel<<<gi, fft_threads, smem, ctx->stream>>>(

@@ -616,26 +616,35 @@ int launch(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S &chi
     bool mirror = !(a.contrib & COFFE_GPU_DEN) || (!ctx->bias_set[0] && !ctx->bias_set[1]) ||
                   (ctx->bias_set[0] && ctx->bias_set[1] && ctx->bias_host[0] == ctx->bias_host[1]);
     for (int j = 0; j < a.n_l; ++j) mirror = mirror && (a.ls[j] % 2 == 0);
-    // node table of these multipoles (rebuilt only when the l list, precision
-    // or layout changes)
+    // node table of these multipoles: one cached table per (l list,
+    // precision, layout), built on first use
     const int prec_tag = sizeof(T) == 8 ? COFFE_GPU_FP64 : COFFE_GPU_MIXED;
-    bool same = ctx->mp_nodes_nl == a.n_l && ctx->mp_nodes_prec == prec_tag &&
-                ctx->mp_nodes_mirror == (int)mirror;
-    for (int j = 0; same && j < a.n_l; ++j) same = ctx->mp_nodes_ls[j] == a.ls[j];
-    if (!same) {
+    coffe_gpu_ctx::NodeSlot *slot = nullptr;
+    for (auto &sl : ctx->mp_node_slots) {
+        bool same = sl.buf.p && sl.nl == a.n_l && sl.prec == prec_tag && sl.mirror == (int)mirror;
+        for (int j = 0; same && j < a.n_l; ++j) same = sl.ls[j] == a.ls[j];
+        if (same) {
+            slot = &sl;
+            break;
+        }
+    }
+    if (!slot) {
+        slot = &ctx->mp_node_slots[ctx->mp_node_next];
+        ctx->mp_node_next = (ctx->mp_node_next + 1) % coffe_gpu_ctx::CG_NODE_SLOTS;
         std::vector<T> tab;
         build_node_table<T>(a.n_l, a.ls, tab, mirror);
-        int st0 = cg_ensure(ctx, ctx->mp_nodes, sizeof(T) * tab.size());
+        slot->nl = 0; // invalid until the upload below has finished
+        int st0 = cg_ensure(ctx, slot->buf, sizeof(T) * tab.size());
         if (st0) return st0;
-        CG_CUDA(ctx, cudaMemcpyAsync(ctx->mp_nodes.p, tab.data(), sizeof(T) * tab.size(),
+        CG_CUDA(ctx, cudaMemcpyAsync(slot->buf.p, tab.data(), sizeof(T) * tab.size(),
                                      cudaMemcpyHostToDevice, ctx->stream));
         CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream)); // tab is a host temporary
-        ctx->mp_nodes_nl = a.n_l;
-        ctx->mp_nodes_prec = prec_tag;
-        ctx->mp_nodes_mirror = (int)mirror;
-        for (int j = 0; j < a.n_l; ++j) ctx->mp_nodes_ls[j] = a.ls[j];
+        slot->nl = a.n_l;
+        slot->prec = prec_tag;
+        slot->mirror = (int)mirror;
+        for (int j = 0; j < a.n_l; ++j) slot->ls[j] = a.ls[j];
     }
-    const T *d_nodes = (const T *)ctx->mp_nodes.p;
+    const T *d_nodes = (const T *)slot->buf.p;
     const long long blocks = (total + MP_LANE_THREADS - 1) / MP_LANE_THREADS;
 #define MP_LAUNCH_MIR(NLV, MIR)                                                                  \
     {                                                                                            \
