@@ -66,7 +66,7 @@ struct coffe_gpu_ctx {
     DevBuf samp_dx;   // N doubles: offset of each FFT node in its interval
     DevBuf samp_f32;  // N float4 (dx, h, 1/h, -) for the mixed path
     DevBuf csfac32;   // 4 * nk floats: spline factors for the mixed path
-    DevBuf csband;    // (nk - 2) x 25 floats: band of the inverse spline matrix
+    DevBuf csband;    // 25 x (nk - 2) floats: band of the inverse spline matrix, by diagonal
     DevBuf samp_tdf;  // N float2: double-float dx / h of each FFT node (mixed path)
     DevBuf qfac_df;   // n_q * N float2: double-float windowed bias (mixed path)
     DevBuf pk_df;     // n_spectra * nk float2: double-float input spectra (mixed path)

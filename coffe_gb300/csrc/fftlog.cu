@@ -312,48 +312,69 @@ __global__ void cspline_c_kernel(const double *__restrict__ x, const double *__r
 // with the band precomputed once per k grid (float; truncation 0.27^13 ~ 4e-8
 // of the diagonal, the float resolution of c).  c enters the resampled P(k)
 // only through the h (c1 + 2 c0)/3 and dx^2 terms, corrections of relative size
-// ~(h/k)^2.  One thread per (spectrum, knot), rhs staged in shared memory.
+// ~(h/k)^2.  One thread per knot for CS_SPB spectra, rhs staged in shared
+// memory, the band stored by diagonal so that its loads coalesce.
 #define CS_BAND 12
 #define CS_TILE 256
+#define CS_SPB 8 // spectra per block: each thread keeps its band row in registers
+#define CS_HALO (CS_TILE + 2 * CS_BAND + 2)
+// One pass per (tile of knots, group of CS_SPB spectra): reads the FP64
+// spectra once, writes them as double-float pairs for the FFT input
+// (integer split, no FP64 work) and the float spline coefficients.
 __global__ void __launch_bounds__(CS_TILE)
-    cspline_band_kernel(const float2 *__restrict__ pkdf, const float *__restrict__ band,
-                        const float *__restrict__ fac32, int nk, float *__restrict__ cc)
+    cspline_band_kernel(const double *__restrict__ pk, const float *__restrict__ band_t,
+                        const float *__restrict__ fac32, int nk, int n_spectra,
+                        float2 *__restrict__ pkdf, float *__restrict__ cc)
 {
-    __shared__ float y_s[CS_TILE + 2 * CS_BAND + 2];
-    __shared__ float rhs_s[CS_TILE + 2 * CS_BAND];
-    const int s = blockIdx.y;
+    __shared__ float y_s[CS_SPB][CS_HALO];
+    __shared__ float rhs_s[CS_SPB][CS_TILE + 2 * CS_BAND];
     const int i0 = blockIdx.x * CS_TILE;
+    const int s0 = blockIdx.y * CS_SPB;
+    const int ns = min(CS_SPB, n_spectra - s0);
     const int m = nk - 2;
-    const float2 *y = pkdf + (size_t)s * nk;
+    const bool last_tile = blockIdx.x == gridDim.x - 1;
     const float *g = fac32 + 2 * nk;
-    // the float (high) parts of the samples this tile reads, once each
-    for (int t = threadIdx.x; t < CS_TILE + 2 * CS_BAND + 2; t += blockDim.x) {
-        const int i = i0 - CS_BAND + t;
-        y_s[t] = (i >= 0 && i < nk) ? y[i].x : 0.f;
+    for (int t = threadIdx.x; t < CS_SPB * CS_HALO; t += blockDim.x) {
+        const int q = t / CS_HALO, r = t - q * CS_HALO;
+        const int i = i0 - CS_BAND + r;
+        float h = 0.f;
+        if (q < ns && i >= 0 && i < nk) {
+            const size_t at = (size_t)(s0 + q) * nk + i;
+            const dfl d = df_from_double_bits(pk[at]);
+            h = d.hi;
+            // each knot's pair is written by the tile that owns it (the last
+            // tile also owns the two knots past the final spline row)
+            if (i >= i0 && (i < i0 + CS_TILE || last_tile)) pkdf[at] = make_float2(d.hi, d.lo);
+        }
+        y_s[q][r] = h;
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < CS_TILE + 2 * CS_BAND; t += blockDim.x) {
-        const int i = i0 - CS_BAND + t;
+    for (int t = threadIdx.x; t < CS_SPB * (CS_TILE + 2 * CS_BAND); t += blockDim.x) {
+        const int q = t / (CS_TILE + 2 * CS_BAND), r = t - q * (CS_TILE + 2 * CS_BAND);
+        const int i = i0 - CS_BAND + r;
         float v = 0.f;
         if (i >= 0 && i < m) {
-            const float ya = y_s[t], yb = y_s[t + 1], yc = y_s[t + 2];
+            const float ya = y_s[q][r], yb = y_s[q][r + 1], yc = y_s[q][r + 2];
             v = 3.f * ((yc - yb) * g[i + 1] - (yb - ya) * g[i]);
         }
-        rhs_s[t] = v;
+        rhs_s[q][r] = v;
     }
     __syncthreads();
-    float *c = cc + (size_t)s * nk;
     const int i = i0 + threadIdx.x;
     if (i < m) {
-        const float *b = band + (size_t)i * (2 * CS_BAND + 1);
-        float acc = 0.f;
+        float bw[2 * CS_BAND + 1];
 #pragma unroll
-        for (int d = 0; d <= 2 * CS_BAND; ++d) acc = fmaf(__ldg(b + d), rhs_s[threadIdx.x + d], acc);
-        c[i + 1] = acc;
+        for (int d = 0; d <= 2 * CS_BAND; ++d) bw[d] = __ldg(band_t + (size_t)d * m + i);
+        for (int q = 0; q < ns; ++q) {
+            float acc = 0.f;
+#pragma unroll
+            for (int d = 0; d <= 2 * CS_BAND; ++d) acc = fmaf(bw[d], rhs_s[q][threadIdx.x + d], acc);
+            cc[(size_t)(s0 + q) * nk + i + 1] = acc;
+        }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        c[0] = 0.f;
-        c[nk - 1] = 0.f;
+    if (blockIdx.x == 0 && threadIdx.x < ns) {
+        cc[(size_t)(s0 + threadIdx.x) * nk] = 0.f;
+        cc[(size_t)(s0 + threadIdx.x) * nk + nk - 1] = 0.f;
     }
 }
 
@@ -384,7 +405,7 @@ void cspline_band_host(const std::vector<double> &x, std::vector<float> &band)
         for (int r = n - 2; r >= 0; --r) rhs[r] = (rhs[r] - up[r] * rhs[r + 1]) / dg[r];
         for (int d = -CS_BAND; d <= CS_BAND; ++d) {
             const int i = j + d;
-            if (i >= lo && i < hi) band[(size_t)j * B + d + CS_BAND] = (float)rhs[i - lo];
+            if (i >= lo && i < hi) band[(size_t)(d + CS_BAND) * m + j] = (float)rhs[i - lo];
         }
     }
 }
@@ -514,37 +535,60 @@ __global__ void fftlog_inverse_kernel(GridPar g, const double2 *__restrict__ spe
 
 // ---- mixed path: the same transforms in double-float on the FP32 pipes
 
-// radix-2 DIT of M = 2^logM double-float complex points (bit-reversed input)
+// DIT FFT of M = 2^logM double-float complex points (bit-reversed input):
+// pairs of radix-2 stages fused into radix-4 butterflies in registers (three
+// twiddle products per four points instead of four, half the shared-memory
+// passes), after one twiddle-free radix-2 stage when logM is odd.
+// tw[j] = exp(-2 pi i j / (2M)), j <= M; sign = -1 forward, +1 backward.
 __device__ void smem_fft_df(float4 *buf, int logM, const float4 *__restrict__ tw, int sign)
 {
     const int M = 1 << logM;
-    for (int st = 1; st <= logM; ++st) {
-        const int half = 1 << (st - 1);
-        const int stride = M >> (st - 1);
+    int st = 1;
+    if (logM & 1) {
         for (int b = threadIdx.x; b < M / 2; b += blockDim.x) {
+            const dfc u = dfc_load(buf[2 * b]), v = dfc_load(buf[2 * b + 1]);
+            buf[2 * b] = dfc_pack(dfc_add(u, v));
+            buf[2 * b + 1] = dfc_pack(dfc_sub(u, v));
+        }
+        __syncthreads();
+        st = 2;
+    }
+    for (; st < logM; st += 2) {
+        // radix-2 stages st and st + 1: points i0 + {0, 1, 2, 3} half of a
+        // block of 4 half; W = w_{4 half}^pos, twiddles W^2, W, W^3
+        const int half = 1 << (st - 1);
+        const int step = M >> st; // tw index of w_{4 half}
+        for (int b = threadIdx.x; b < M / 4; b += blockDim.x) {
             const int pos = b & (half - 1);
-            const int i0 = ((b >> (st - 1)) << st) + pos;
-            const int i1 = i0 + half;
-            dfc w = dfc_load(tw[pos * stride]);
-            if (sign > 0) w.im = df_neg(w.im);
-            const dfc u = dfc_load(buf[i0]);
-            const dfc t = dfc_mul(w, dfc_load(buf[i1]));
-            buf[i0] = dfc_pack(dfc_add(u, t));
-            buf[i1] = dfc_pack(dfc_sub(u, t));
+            const int i0 = ((b >> (st - 1)) << (st + 1)) + pos;
+            const dfc x0 = dfc_load(buf[i0]);
+            dfc x1 = dfc_load(buf[i0 + half]);
+            dfc x2 = dfc_load(buf[i0 + 2 * half]);
+            dfc x3 = dfc_load(buf[i0 + 3 * half]);
+            if (half > 1) { // pos = 0 when half = 1: all twiddles are one
+                const int j = pos * step, j3 = 3 * j;
+                dfc w1 = dfc_load(tw[2 * j]), w2 = dfc_load(tw[j]);
+                dfc w3 = j3 <= M ? dfc_load(tw[j3]) : dfc_neg(dfc_load(tw[j3 - M]));
+                if (sign > 0) {
+                    w1 = dfc_conj(w1);
+                    w2 = dfc_conj(w2);
+                    w3 = dfc_conj(w3);
+                }
+                x1 = dfc_mul(x1, w1);
+                x2 = dfc_mul(x2, w2);
+                x3 = dfc_mul(x3, w3);
+            }
+            const dfc t0 = dfc_add(x0, x1), t1 = dfc_sub(x0, x1);
+            const dfc t2 = dfc_add(x2, x3), t3 = dfc_sub(x2, x3);
+            // w_{4 half}^half = -i forward, +i backward
+            const dfc r = sign < 0 ? dfc{t3.im, df_neg(t3.re)} : dfc{df_neg(t3.im), t3.re};
+            buf[i0] = dfc_pack(dfc_add(t0, t2));
+            buf[i0 + half] = dfc_pack(dfc_add(t1, r));
+            buf[i0 + 2 * half] = dfc_pack(dfc_sub(t0, t2));
+            buf[i0 + 3 * half] = dfc_pack(dfc_sub(t1, r));
         }
         __syncthreads();
     }
-}
-
-// The input spectra as double-float pairs, one conversion per sample: the
-// mixed path's only FP64 work per spectrum (the FP64 pipe is ~1/64 of FP32).
-__global__ void pk_split_kernel(const double *__restrict__ pk, long long count,
-                                float2 *__restrict__ out)
-{
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
-    const dfl d = df_from_double(pk[i]);
-    out[i] = make_float2(d.hi, d.lo);
 }
 
 // Mixed-path sampling in double-float: the secant part y0 + t (y1 - y0),
@@ -612,6 +656,16 @@ __global__ void fftlog_forward_df_kernel(GridPar g, const float2 *__restrict__ p
     }
 }
 
+// the half-length complex input of a real inverse transform:
+// Fe + i Fo, Fe = X_k + conj(X_{M-k}), Fo = (X_k - conj(X_{M-k})) conj(w_k)
+__device__ __forceinline__ dfc c2r_pre(dfc xa, dfc xb, float4 w)
+{
+    const dfc xbc = dfc_conj(xb);
+    const dfc fe = dfc_add(xa, xbc);
+    const dfc fo = dfc_mul(dfc_sub(xa, xbc), dfc_conj(dfc_load(w)));
+    return dfc{df_sub(fe.re, fo.im), df_add(fe.im, fo.re)};
+}
+
 __global__ void fftlog_inverse_df_kernel(GridPar g, const float4 *__restrict__ spec,
                                          const int *__restrict__ term_q, int n_q, int n_terms,
                                          const float4 *__restrict__ mcoef_df,
@@ -626,7 +680,9 @@ __global__ void fftlog_inverse_df_kernel(GridPar g, const float4 *__restrict__ s
     const int logM = 31 - __clz(M);
     const float4 *in = spec + ((size_t)s * n_q + term_q[t]) * (M + 1);
     const float4 *mc = mcoef_df + (size_t)t * (M + 1);
-    for (int k = threadIdx.x; k < M; k += blockDim.x) {
+    // z_k = Fe_k + i Fo_k from X_k and conj(X_{M-k}), X = spectrum x kernel;
+    // one thread makes z_k and z_{M-k} from the same two products
+    for (int k = threadIdx.x; k <= M / 2; k += blockDim.x) {
         const int km = M - k;
         dfc xa = dfc_mul(dfc_load(in[k]), dfc_load(mc[k]));
         dfc xb = dfc_mul(dfc_load(in[km]), dfc_load(mc[km]));
@@ -634,12 +690,9 @@ __global__ void fftlog_inverse_df_kernel(GridPar g, const float4 *__restrict__ s
             xa.im = dfl{0.f, 0.f};
             xb.im = dfl{0.f, 0.f};
         }
-        const dfc xbc = dfc_conj(xb);
-        const dfc fe = dfc_add(xa, xbc);
-        const dfc fo = dfc_mul(dfc_sub(xa, xbc), dfc_conj(dfc_load(twdf[k])));
-        const dfc z = dfc{df_sub(fe.re, fo.im), df_add(fe.im, fo.re)}; // Fe + i Fo
-        const int jj = __brev((unsigned)k) >> (32 - logM);
-        buf[jj] = dfc_pack(z);
+        buf[__brev((unsigned)k) >> (32 - logM)] = dfc_pack(c2r_pre(xa, xb, twdf[k]));
+        if (k > 0 && k < M / 2)
+            buf[__brev((unsigned)km) >> (32 - logM)] = dfc_pack(c2r_pre(xb, xa, twdf[km]));
     }
     __syncthreads();
     smem_fft_df(buf, logM, twdf, +1);
@@ -1020,15 +1073,11 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     // per spectrum: natural-spline coefficients, forward FFTs, inverse FFTs
     if (mixed) {
         if ((st = cg_ensure(ctx, ctx->pk_df, sizeof(float2) * nk * n_spectra))) return st;
-        const long long cnt = (long long)nk * n_spectra;
-        pk_split_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, ctx->stream>>>(
-            d_pk, cnt, (float2 *)ctx->pk_df.p);
-        if ((st = cg_after_launch(ctx, "pk_split_kernel"))) return st;
-        cspline_band_kernel<<<dim3(((int)nk - 2 + CS_TILE - 1) / CS_TILE, n_spectra), CS_TILE, 0,
-                              ctx->stream>>>((const float2 *)ctx->pk_df.p,
-                                             (const float *)ctx->csband.p,
-                                             (const float *)ctx->csfac32.p, (int)nk,
-                                             (float *)ctx->csc.p);
+        cspline_band_kernel<<<dim3(((int)nk - 2 + CS_TILE - 1) / CS_TILE,
+                                   (n_spectra + CS_SPB - 1) / CS_SPB),
+                              CS_TILE, 0, ctx->stream>>>(
+            d_pk, (const float *)ctx->csband.p, (const float *)ctx->csfac32.p, (int)nk, n_spectra,
+            (float2 *)ctx->pk_df.p, (float *)ctx->csc.p);
         if ((st = cg_after_launch(ctx, "cspline_band_kernel"))) return st;
     } else {
         cspline_c_kernel<<<(n_spectra + 3) / 4, 128, 0, ctx->stream>>>(
