@@ -40,6 +40,10 @@ struct coffe_gpu_ctx {
     bool z_uniform = false;
     double z0 = 0, zn = 0, dz = 0;
     DevBuf zrec64, zrec32;
+    // mixed path: D1 and f D1 on a uniform chi grid (linear cells, two guard cells)
+    DevBuf chitab32;
+    int chi_cells = 0;
+    double chi_lo = 0, chi_hi = 0;
     SplineBuf bias[4];
     bool bias_set[4] = {false, false, false, false};
     std::vector<double> bias_host[4]; // (z, value) samples as set, for symmetry checks

@@ -111,6 +111,37 @@ const PanelTables<double> &panel_tables()
     return t64;
 }
 
+// The node table of mp_fast_kernel (layout FastLayout<NL>, float): the mirror
+// rule's rows mu >= 0 ascending with the mu-only RSD coefficients
+void build_node_table_fast(int NL, const int *ls, std::vector<float> &out)
+{
+    const PanelTables<double> &P = panel_tables();
+    const int R1 = ((8 + 3 * NL) + 3) / 4 * 4, R2 = ((1 + NL) + 3) / 4 * 4;
+    out.assign((size_t)31 * (R1 + R2), 0.f);
+    for (int k = 0; k < 31; ++k) {
+        const int sl = P.order[30 + k];
+        const double mult = sl == 60 ? 1.0 : 2.0;
+        const double mu = P.mu_sorted[30 + k], mu2 = mu * mu, omm = 1.0 - mu2;
+        float *r = out.data() + (size_t)k * R1;
+        r[0] = (float)mu;
+        r[1] = (float)mu2;
+        r[2] = (float)omm;
+        r[3] = (float)(0.75 * omm * omm + 4.0 * mu2 * omm + 12.0 * mu2 * mu2);  // a2
+        r[4] = (float)(-2.5 * omm * omm - 20.0 * mu2 * omm);                   // a1
+        r[5] = (float)(4.75 * omm * omm - 8.0 * mu2 * omm - 4.0 * mu2 * mu2);  // a0
+        r[6] = (float)(11.0 - 9.0 * omm);                                      // b2
+        r[7] = (float)(9.0 * omm);                                             // -b1
+        for (int j = 0; j < NL; ++j) {
+            r[8 + j] = (float)(mult * P.wkP[ls[j]][sl]);
+            r[8 + NL + j] = (float)(mult * P.wgP[ls[j]][sl]);
+            r[8 + 2 * NL + j] = (float)(mult * P.wkA[ls[j]][sl]);
+        }
+        float *r2 = out.data() + (size_t)31 * R1 + (size_t)k * R2;
+        r2[0] = (float)(mult * P.wk[sl]);
+        for (int j = 0; j < NL; ++j) r2[1 + j] = (float)P.Pl[ls[j]][sl];
+    }
+}
+
 // The node table of one launch (layout NodeLayout<NL>), in T, for multipoles ls[0..NL)
 template <typename T>
 void build_node_table(int NL, const int *ls, std::vector<T> &out, bool mirror = false)
@@ -455,6 +486,46 @@ template <int R> __device__ __forceinline__ void lds_rec(const double *p, double
     }
 }
 
+// First-panel results of one separation: QUADPACK's acceptance test of the
+// 61-point panel (gsl qag.c) per multipole; accepted values are written,
+// the others queued for the adaptive continuation.
+template <int NL, typename T>
+__device__ __forceinline__ void first_panel_out(const MpArgs &a, long long item, bool finite,
+                                                const T (&K)[NL], const T (&G)[NL],
+                                                const T (&A)[NL], const T (&asc)[NL],
+                                                double *__restrict__ out,
+                                                int *__restrict__ retry_count,
+                                                int2 *__restrict__ retry, int *err)
+{
+#pragma unroll
+    for (int j = 0; j < NL; ++j) {
+        const int l = a.ls[j];
+        QkOut<T> o;
+        o.result = K[j] * T(0.5);
+        o.resabs = A[j] * T(0.5);
+        o.resasc = asc[j] * T(0.5);
+        o.abserr = qk_rescale_error((K[j] - G[j]) * T(0.5), o.resabs, o.resasc);
+        const T tolerance = (T)a.epsrel * fabs(o.result);
+        const T round_off = T(50) * qk_eps<T>() * o.resabs;
+        const bool roundoff_fail = o.abserr <= round_off && o.abserr > tolerance;
+        const bool ok = (o.abserr <= tolerance && o.abserr != o.resasc) || o.abserr == T(0);
+        if (!finite) {
+            cg_flag(err, CG_ERR_NONFINITE);
+            out[item * NL + j] = cg_nan<double>();
+        } else if (ok || roundoff_fail) {
+            const double res = (double)(T(2 * l + 1) * o.result);
+            if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
+            out[item * NL + j] = res;
+        } else {
+            const int slot = atomicAdd(retry_count, 1);
+            if (slot < a.retry_cap)
+                retry[slot] = make_int2((int)item, j);
+            else
+                cg_flag(err, CG_ERR_QAG_LIMIT);
+        }
+    }
+}
+
 template <int NL, typename T, typename S, typename TT, bool MIRROR = false>
 __global__ void __launch_bounds__(MP_LANE_THREADS)
     mp_lane_kernel(MpArgs a, Bg<T, S> bg, S chi_of_z, const TT *__restrict__ tab_x,
@@ -535,34 +606,166 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
             for (int j = 0; j < NL; ++j) asc[j] += rec[0] * fabs(v * rec[1 + j] - K[j] * T(0.5));
         }
     }
+    first_panel_out<NL, T>(a, item, finite, K, G, A, asc, out, retry_count, retry, err);
+}
+
+// ------------------------------------------- mixed path, equal unit biases
+//
+// The same first panel for the common case of the mixed path: unit galaxy
+// biases (so equal tracers and, with even multipoles, the 31-node mirror
+// rule), density and/or RSD without the only-cross switch.  Two changes
+// against mp_lane_kernel, both exact rearrangements up to float rounding:
+//  * background: D1 and f D1 read from one uniform-chi table of linear cells
+//    (16384 cells over the background's chi range: interpolation error
+//    ~h^2 y''/8, about 1e-8 relative), instead of z(chi) and then f(z), D1(z);
+//  * integrand: with G = D1 and F = f D1 at both ends, xi g1 g2 becomes
+//      G1 G2 I00 + F1 F2 R(c) + (G1 F2 + F1 G2)(I00 - 2 I02)/3
+//      + g I02 (G1 F2 chi1^2 + F1 G2 chi2^2),       g = (2 - s)(1 - mu^2)/D,
+//    R(c) = (1 + 2c^2) I00/15 - (b2 c^2 + b1 c + 1) I02/21
+//           + (a2 c^2 + a1 c + a0) I04/35,
+//    where the mu-only coefficients a_i, b_i of the RSD polynomials (functions.c
+//    :129-134 as rewritten for Xi::combine) sit in the node table.
+#define MP_CHI_CELLS 16384
+
+// Uniform-chi cells: u = (chi - chi_lo)/h - 1/2 in [-1/2, cells - 1/2];
+// record 1 + round(u) holds (G, dG, F, dF) at the cell centre (record 0 and
+// cells + 1 are guards), t = u - round(u) in [-1/2, 1/2].
+struct ChiTab {
+    const float4 *rec;
+    float inv_h, off, umax;
+};
+
+__device__ __forceinline__ void chi_cell(const ChiTab &ct, float chi, float &G, float &F)
+{
+    const float big = 12582912.f; // 1.5 * 2^23: round-to-nearest integer for |u| < 2^22
+    const float u = fminf(fmaxf(fmaf(chi, ct.inv_h, ct.off), -1.f), ct.umax);
+    const float rb = __fadd_rn(u, big);
+    const float t = __fadd_rn(u, -__fadd_rn(rb, -big));
+    const float4 c = __ldg(ct.rec + 1 + (__float_as_int(rb) - 0x4B400000));
+    G = fmaf(t, c.y, c.x);
+    F = fmaf(t, c.w, c.z);
+}
+
+// node table of mp_fast_kernel, rows mu >= 0 ascending:
+//   row k: mu, mu^2, 1 - mu^2, a2, a1, a0, b2, -b1, wk P_l (NL), wg P_l (NL), wk |P_l| (NL)
+//   then per row: wk, P_l (NL)
+template <int NL> struct FastLayout {
+    static constexpr int R1 = ((8 + 3 * NL) + 3) / 4 * 4;
+    static constexpr int R2 = ((1 + NL) + 3) / 4 * 4;
+    static constexpr int ROWS = 31;
+    static constexpr int COUNT = ROWS * (R1 + R2);
+};
+
+template <int NL, int CONTRIB>
+__global__ void __launch_bounds__(MP_LANE_THREADS)
+    mp_fast_kernel(MpArgs a, ChiTab ct, float chi_lo, float chi_hi, Spl32 chi_of_z,
+                   const float *__restrict__ tab_x, const float *__restrict__ tab_y,
+                   const int *__restrict__ req_spectrum, const double *__restrict__ req_z_mean,
+                   const int64_t *__restrict__ req_offset, const double *__restrict__ sep,
+                   long long total, const float *__restrict__ nodes, double *__restrict__ out,
+                   int *__restrict__ retry_count, int2 *__restrict__ retry, int *err)
+{
+    typedef FastLayout<NL> LY;
+    extern __shared__ __align__(16) unsigned char mp_smem[];
+    float *tab1 = reinterpret_cast<float *>(mp_smem); // [ROWS][R1]
+    float *tab2 = tab1 + LY::ROWS * LY::R1;           // [ROWS][R2]
+    float *xs = tab2 + LY::ROWS * LY::R2;             // [ROWS][blockDim.x] integrand values
+    for (int i = threadIdx.x; i < LY::COUNT; i += blockDim.x) tab1[i] = nodes[i];
+    __syncthreads();
+    const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= total) return;
+    const int q = find_request(req_offset, a.n_req, item);
+    const int s = req_spectrum[q];
+    const float r = (float)sep[item];
+    const float chim = spl_eval(chi_of_z, (float)req_z_mean[q]);
+    const float *y0 = tab_y + ((size_t)s * a.n_terms) * a.tab_len;
+    const float idl = (float)a.inv_dlog;
+    const float I00 = table_lookup<float>(tab_x, y0 + (size_t)a.t00 * a.tab_len, a.tab_len, idl, r);
+    const float I02 = table_lookup<float>(tab_x, y0 + (size_t)a.t02 * a.tab_len, a.tab_len, idl, r);
+    const float I04 = table_lookup<float>(tab_x, y0 + (size_t)a.t04 * a.tab_len, a.tab_len, idl, r);
+    const int bd = blockDim.x, tid = threadIdx.x;
+    float K[NL], Kc[NL], G[NL], A[NL];
 #pragma unroll
-    for (int j = 0; j < NL; ++j) {
-        const int l = a.ls[j];
-        QkOut<T> o;
-        o.result = K[j] * T(0.5);
-        o.resabs = A[j] * T(0.5);
-        o.resasc = asc[j] * T(0.5);
-        o.abserr = qk_rescale_error((K[j] - G[j]) * T(0.5), o.resabs, o.resasc);
-        // QUADPACK's acceptance test of the first panel (gsl qag.c)
-        const T tolerance = (T)a.epsrel * fabs(o.result);
-        const T round_off = T(50) * qk_eps<T>() * o.resabs;
-        const bool roundoff_fail = o.abserr <= round_off && o.abserr > tolerance;
-        const bool ok = (o.abserr <= tolerance && o.abserr != o.resasc) || o.abserr == T(0);
-        if (!finite) {
-            cg_flag(err, CG_ERR_NONFINITE);
-            out[item * NL + j] = cg_nan<double>();
-        } else if (ok || roundoff_fail) {
-            const double res = (double)(T(2 * l + 1) * o.result);
-            if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
-            out[item * NL + j] = res;
-        } else {
-            const int slot = atomicAdd(retry_count, 1);
-            if (slot < a.retry_cap)
-                retry[slot] = make_int2((int)item, j);
-            else
-                cg_flag(err, CG_ERR_QAG_LIMIT);
+    for (int j = 0; j < NL; ++j) K[j] = Kc[j] = G[j] = A[j] = 0.f;
+    const float half_r = 0.5f * r;
+    const float span = tab1[(LY::ROWS - 1) * LY::R1] * half_r; // largest mu
+    const bool inside = (chim - span >= chi_lo) && (chim + span <= chi_hi);
+    const bool finite = inside && isfinite(I00) && isfinite(I02) && isfinite(I04);
+    if (inside) {
+        const float A2 = 2.f * chim * chim, Br = 0.5f * r * r, r2 = r * r;
+        const float e00 = I00 * (1.f / 15.f), e02 = I02 * (1.f / 21.f), e04 = I04 * (1.f / 35.f);
+        const float e00x2 = 2.f * e00, e0d = e00 - e02;
+        const float K1 = (I00 - 2.f * I02) * (1.f / 3.f);
+#pragma unroll 1
+        for (int k = 0; k < LY::ROWS; ++k) {
+            float rec[LY::R1];
+            lds_rec<LY::R1>(tab1 + k * LY::R1, rec);
+            const float mu = rec[0], mu2 = rec[1], omm = rec[2];
+            const float chi1 = fmaf(-mu, half_r, chim), chi2 = fmaf(mu, half_r, chim);
+            float G1, F1, G2, F2;
+            chi_cell(ct, chi1, G1, F1);
+            chi_cell(ct, chi2, G2, F2);
+            const float D = fmaf(-mu2, Br, A2); // 2 chi1 chi2
+            const float inv_D = __fdividef(1.f, D);
+            const float sv = r2 * omm * inv_D;
+            const float c = 1.f - sv;
+            float v = 0.f;
+            if (CONTRIB & COFFE_GPU_DEN) v = G1 * G2 * I00;
+            if (CONTRIB & COFFE_GPU_RSD) {
+                const float g2c = fmaf(rec[3], e04, fmaf(-rec[6], e02, e00x2));
+                const float g1c = fmaf(rec[4], e04, rec[7] * e02);
+                const float g0c = fmaf(rec[5], e04, e0d);
+                v = fmaf(F1 * F2, fmaf(fmaf(g2c, c, g1c), c, g0c), v);
+            }
+            if ((CONTRIB & COFFE_GPU_DEN) && (CONTRIB & COFFE_GPU_RSD)) {
+                const float gf = G1 * F2, fg = F1 * G2;
+                const float g = (1.f + c) * omm * inv_D;
+                v = fmaf(gf + fg, K1, v);
+                v = fmaf(g * I02, fmaf(gf, chi1 * chi1, fg * (chi2 * chi2)), v);
+            }
+            xs[k * bd + tid] = v;
+            const float av = fabsf(v);
+#pragma unroll
+            for (int j = 0; j < NL; ++j) { // Kahan-compensated Kronrod sum
+                const float yk = rec[8 + j] * v - Kc[j];
+                const float tk = K[j] + yk;
+                Kc[j] = (tk - K[j]) - yk;
+                K[j] = tk;
+                G[j] = fmaf(rec[8 + NL + j], v, G[j]);
+                A[j] = fmaf(rec[8 + 2 * NL + j], av, A[j]);
+            }
         }
     }
+    float asc[NL];
+#pragma unroll
+    for (int j = 0; j < NL; ++j) asc[j] = 0.f;
+    if (inside) {
+#pragma unroll 1
+        for (int k = 0; k < LY::ROWS; ++k) {
+            float rec[LY::R2];
+            lds_rec<LY::R2>(tab2 + k * LY::R2, rec);
+            const float v = xs[k * bd + tid];
+#pragma unroll
+            for (int j = 0; j < NL; ++j) asc[j] = fmaf(rec[0], fabsf(fmaf(v, rec[1 + j], -0.5f * K[j])), asc[j]);
+        }
+    }
+    first_panel_out<NL, float>(a, item, finite, K, G, A, asc, out, retry_count, retry, err);
+}
+
+__global__ void chitab_kernel(Spl64 z_of_chi, Spl64 D1, Spl64 f, double lo, double hi, int cells,
+                              float4 *__restrict__ rec)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x; // record k: cell k - 1
+    if (k >= cells + 2) return;
+    const int i = min(max(k - 1, 0), cells - 1);
+    const double h = (hi - lo) / cells;
+    const double xa = lo + i * h, xb = i == cells - 1 ? hi : fmin(lo + (i + 1) * h, hi);
+    const double za = spl_eval(z_of_chi, xa), zb = spl_eval(z_of_chi, xb);
+    const double ga = spl_eval(D1, za), gb = spl_eval(D1, zb);
+    const double fa = spl_eval(f, za) * ga, fb = spl_eval(f, zb) * gb;
+    const double sh = (double)(k - 1 - i); // -1 / +1 in the guards: the edge cell's line
+    rec[k] = make_float4((float)(0.5 * (ga + gb) + sh * (gb - ga)), (float)(gb - ga),
+                         (float)(0.5 * (fa + fb) + sh * (fb - fa)), (float)(fb - fa));
 }
 
 // ------------------------------------------------------- adaptive retries
@@ -603,6 +806,91 @@ __global__ void __launch_bounds__(32 * MP_RETRY_WARPS)
     }
 }
 
+// The cached node table of (multipole list, precision, layout), uploaded on
+// first use: layout 0 / 1 = NodeLayout without / with the mirror rule,
+// 2 = FastLayout.  *dev receives its device address.
+template <typename Build>
+int node_slot(coffe_gpu_ctx *ctx, int n_l, const int *ls, int prec_tag, int layout, Build build,
+              const void **dev)
+{
+    for (auto &sl : ctx->mp_node_slots) {
+        bool same = sl.buf.p && sl.nl == n_l && sl.prec == prec_tag && sl.mirror == layout;
+        for (int j = 0; same && j < n_l; ++j) same = sl.ls[j] == ls[j];
+        if (same) {
+            *dev = sl.buf.p;
+            return COFFE_GPU_OK;
+        }
+    }
+    coffe_gpu_ctx::NodeSlot *slot = &ctx->mp_node_slots[ctx->mp_node_next];
+    ctx->mp_node_next = (ctx->mp_node_next + 1) % coffe_gpu_ctx::CG_NODE_SLOTS;
+    std::vector<unsigned char> bytes;
+    build(bytes);
+    slot->nl = 0; // invalid until the upload below has finished
+    int st = cg_ensure(ctx, slot->buf, bytes.size());
+    if (st) return st;
+    CG_CUDA(ctx, cudaMemcpyAsync(slot->buf.p, bytes.data(), bytes.size(), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream)); // bytes is a host temporary
+    slot->nl = n_l;
+    slot->prec = prec_tag;
+    slot->mirror = layout;
+    for (int j = 0; j < n_l; ++j) slot->ls[j] = ls[j];
+    *dev = slot->buf.p;
+    return COFFE_GPU_OK;
+}
+
+// mp_fast_kernel for a validated mixed call with unit biases, even
+// multipoles (at most four) and no only-cross switch, then the retries
+int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<float, Spl32> &bg,
+                const Spl32 &chi_of_z, const float *tab_x, const float *tab_y,
+                const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
+                const double *sep, long long total, double *out)
+{
+    int *d_count = (int *)ctx->mp_retry.p;
+    int2 *d_retry = (int2 *)((char *)ctx->mp_retry.p + 256);
+    CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
+    const void *dn = nullptr;
+    int st = node_slot(ctx, a.n_l, a.ls, COFFE_GPU_MIXED, 2,
+                       [&](std::vector<unsigned char> &bytes) {
+                           std::vector<float> tab;
+                           build_node_table_fast(a.n_l, a.ls, tab);
+                           bytes.assign((const unsigned char *)tab.data(),
+                                        (const unsigned char *)(tab.data() + tab.size()));
+                       },
+                       &dn);
+    if (st) return st;
+    const double inv_h = ctx->chi_cells / (ctx->chi_hi - ctx->chi_lo);
+    const ChiTab ct{(const float4 *)ctx->chitab32.p, (float)inv_h,
+                    (float)(-ctx->chi_lo * inv_h - 0.5), (float)ctx->chi_cells};
+    const long long blocks = (total + MP_LANE_THREADS - 1) / MP_LANE_THREADS;
+    const int contrib = a.contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD);
+#define MP_FAST(NLV, CV)                                                                          \
+    if (a.n_l == NLV && contrib == CV) {                                                          \
+        const size_t smem = sizeof(float) * (FastLayout<NLV>::COUNT +                             \
+                                             FastLayout<NLV>::ROWS * MP_LANE_THREADS);            \
+        CG_CUDA(ctx, cudaFuncSetAttribute(mp_fast_kernel<NLV, CV>,                                \
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,            \
+                                          (int)smem));                                            \
+        mp_fast_kernel<NLV, CV><<<(unsigned)blocks, MP_LANE_THREADS, smem, ctx->stream>>>(        \
+            a, ct, bg.z_of_chi.x0, bg.z_of_chi.xn, chi_of_z, tab_x, tab_y, req_spectrum,          \
+            req_z_mean, req_offset, sep, total, (const float *)dn, out, d_count, d_retry,         \
+            ctx->d_err);                                                                          \
+    }
+#define MP_FAST_NL(NLV) MP_FAST(NLV, 1) MP_FAST(NLV, 2) MP_FAST(NLV, 3)
+    MP_FAST_NL(1)
+    MP_FAST_NL(2)
+    MP_FAST_NL(3)
+    MP_FAST_NL(4)
+#undef MP_FAST_NL
+#undef MP_FAST
+    if ((st = cg_after_launch(ctx, "mp_fast_kernel"))) return st;
+    mp_retry_kernel<float, Spl32, float><<<ctx->sm_count * 2, 32 * MP_RETRY_WARPS, 0,
+                                           ctx->stream>>>(a, bg, chi_of_z, tab_x, tab_y,
+                                                          req_spectrum, req_z_mean, req_offset,
+                                                          sep, out, d_count, d_retry, ctx->d_err);
+    return cg_after_launch(ctx, "mp_retry_kernel");
+}
+
 template <typename T, typename S, typename TT>
 int launch(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S &chi_of_z,
            const TT *tab_x, const TT *tab_y, const int *req_spectrum, const double *req_z_mean,
@@ -618,33 +906,21 @@ int launch(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S &chi
     for (int j = 0; j < a.n_l; ++j) mirror = mirror && (a.ls[j] % 2 == 0);
     // node table of these multipoles: one cached table per (l list,
     // precision, layout), built on first use
-    const int prec_tag = sizeof(T) == 8 ? COFFE_GPU_FP64 : COFFE_GPU_MIXED;
-    coffe_gpu_ctx::NodeSlot *slot = nullptr;
-    for (auto &sl : ctx->mp_node_slots) {
-        bool same = sl.buf.p && sl.nl == a.n_l && sl.prec == prec_tag && sl.mirror == (int)mirror;
-        for (int j = 0; same && j < a.n_l; ++j) same = sl.ls[j] == a.ls[j];
-        if (same) {
-            slot = &sl;
-            break;
-        }
-    }
-    if (!slot) {
-        slot = &ctx->mp_node_slots[ctx->mp_node_next];
-        ctx->mp_node_next = (ctx->mp_node_next + 1) % coffe_gpu_ctx::CG_NODE_SLOTS;
-        std::vector<T> tab;
-        build_node_table<T>(a.n_l, a.ls, tab, mirror);
-        slot->nl = 0; // invalid until the upload below has finished
-        int st0 = cg_ensure(ctx, slot->buf, sizeof(T) * tab.size());
+    const T *d_nodes = nullptr;
+    {
+        const void *dn = nullptr;
+        int st0 = node_slot(ctx, a.n_l, a.ls, sizeof(T) == 8 ? COFFE_GPU_FP64 : COFFE_GPU_MIXED,
+                            (int)mirror,
+                            [&](std::vector<unsigned char> &bytes) {
+                                std::vector<T> tab;
+                                build_node_table<T>(a.n_l, a.ls, tab, mirror);
+                                bytes.assign((const unsigned char *)tab.data(),
+                                             (const unsigned char *)(tab.data() + tab.size()));
+                            },
+                            &dn);
         if (st0) return st0;
-        CG_CUDA(ctx, cudaMemcpyAsync(slot->buf.p, tab.data(), sizeof(T) * tab.size(),
-                                     cudaMemcpyHostToDevice, ctx->stream));
-        CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream)); // tab is a host temporary
-        slot->nl = a.n_l;
-        slot->prec = prec_tag;
-        slot->mirror = (int)mirror;
-        for (int j = 0; j < a.n_l; ++j) slot->ls[j] = a.ls[j];
+        d_nodes = (const T *)dn;
     }
-    const T *d_nodes = (const T *)slot->buf.p;
     const long long blocks = (total + MP_LANE_THREADS - 1) / MP_LANE_THREADS;
 #define MP_LAUNCH_MIR(NLV, MIR)                                                                  \
     {                                                                                            \
@@ -712,6 +988,20 @@ int multipoles_prepare_background(coffe_gpu_ctx *ctx)
     CG_CUDA(ctx, cudaMemcpyAsync(z.data(), ctx->bg_nodes.p, sizeof(double) * n,
                                  cudaMemcpyDeviceToHost, ctx->stream));
     CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    {
+        // mixed-path chi table over the z(chi) spline's knots
+        ctx->chi_cells = 0;
+        const SplineBuf &zc = ctx->bg[BG_Z_OF_CHI];
+        int st = cg_ensure(ctx, ctx->chitab32, sizeof(float4) * (MP_CHI_CELLS + 2));
+        if (st) return st;
+        chitab_kernel<<<(MP_CHI_CELLS + 2 + 255) / 256, 256, 0, ctx->stream>>>(
+            zc.v64(), ctx->bg[BG_D1].v64(), ctx->bg[BG_F].v64(), zc.x0, zc.xn, MP_CHI_CELLS,
+            (float4 *)ctx->chitab32.p);
+        if ((st = cg_after_launch(ctx, "chitab_kernel"))) return st;
+        ctx->chi_cells = MP_CHI_CELLS;
+        ctx->chi_lo = zc.x0;
+        ctx->chi_hi = zc.xn;
+    }
     const double dz = (z[n - 1] - z[0]) / (n - 1);
     bool uni = dz > 0;
     for (int i = 0; i < n && uni; ++i)
@@ -834,6 +1124,13 @@ static int multipoles_nonintegrated(coffe_gpu_ctx *ctx, const MpArgs &a, int pre
         bg.dz = (float)ctx->dz;
         bg.inv_dz = (float)(1.0 / ctx->dz);
         bg.nz = ctx->bg_bins;
+        bool fast = ctx->chi_cells > 0 && a.n_l <= 4 && !ctx->bias_set[0] && !ctx->bias_set[1] &&
+                    !(a.contrib & COFFE_GPU_ONLY_CROSS);
+        for (int j = 0; j < a.n_l; ++j) fast = fast && a.ls[j] % 2 == 0;
+        if (fast)
+            return launch_fast(ctx, a, bg, ctx->bg[BG_CHI_OF_Z].v32(),
+                               (const float *)ctx->tab_x32.p, (const float *)ctx->tab_y.p,
+                               req_spectrum, req_z_mean, req_offset, sep, total, out);
         return launch<float, Spl32, float>(ctx, a, bg, ctx->bg[BG_CHI_OF_Z].v32(),
                                            (const float *)ctx->tab_x32.p,
                                            (const float *)ctx->tab_y.p, req_spectrum, req_z_mean,

@@ -5,7 +5,9 @@ Tolerances (stated per test):
   * FP64 path: 1e-10 relative (the benchmark spec), with a floor of 1e-3 of the largest
     |value| of the same multipole / 1e-8 of the local table envelope so that
     zero crossings do not turn rounding into infinite relative error;
-  * mixed path: 1e-4 relative with the same floors;
+  * mixed path: 1e-4 relative with the same floors; multipoles that vanish
+    in the flat-sky limit (odd l, l >= 6, density-only l >= 2) to a few FP32
+    ulps of the monopole (see _mixed_err);
   * golden vectors: the reference's own tolerances (integrals rtol 1e-4,
     multipoles rtol 5e-4, np.isclose semantics).
 """
@@ -226,6 +228,95 @@ def test_multipoles_batch_mixed(gpu_ctx, small_batch, small_batch_ref):
                np.maximum(np.abs(small_batch_ref), _per_l_floor(small_batch_ref, b, 1e-3)))
     print("mixed max rel error:", e)
     assert e < 1e-4, e
+
+
+FP32_RES = 4 * 2.0 ** -23  # a few FP32 ulps
+
+
+def _rel_fp64(got, ref, ls):
+    """FP64 error: 1e-10 relative with a floor of 1e-3 of the largest |value|
+    of the multipole; for odd l (rounding noise when the tracers are equal)
+    and l >= 6, of the largest |value| of the whole output."""
+    floor = 1e-3 * np.abs(ref).max(axis=0, keepdims=True)
+    small = np.array([(l % 2 == 1) or l >= 6 for l in ls])[None, :]
+    floor = np.where(small, 1e-3 * np.abs(ref).max(), floor)
+    return np.max(np.abs(got - ref) / np.maximum(np.abs(ref), floor))
+
+
+def _mixed_err(got, ref, ls, mono, contrib=3):
+    """Mixed-path error, as a fraction of its bound (pass: < 1).
+    Multipoles of the size of the monopole: 1e-4 relative with a floor of 1e-3
+    of the multipole's largest |value|.  Multipoles that vanish in the
+    flat-sky limit -- odd l (zero for equal tracers), l >= 6, and every l >= 2
+    of the density term alone (a wide-angle effect of order (r / chi)^2, ~1e-6
+    of the monopole at 10 Mpc/h) -- are known only to the FP32 resolution of
+    the integrand: |error| <= 4 * 2^-23 of the monopole's largest |value|."""
+    small = np.array([(l % 2 == 1) or l >= 6 or (contrib == 1 and l >= 2) for l in ls])
+    floor = 1e-3 * np.abs(ref).max(axis=0, keepdims=True)
+    rel = np.abs(got - ref) / np.maximum(np.abs(ref), floor) / 1e-4
+    absm = np.abs(got - ref) / (FP32_RES * np.abs(mono).max())
+    return max(rel[:, ~small].max(initial=0.0), absm[:, small].max(initial=0.0))
+
+
+@pytest.mark.parametrize("contrib", [1, 2, 3])
+@pytest.mark.parametrize("ls", [(0,), (2, 4), (0, 2, 4, 6), (0, 1, 2, 3)])
+def test_multipoles_mixed_variants(gpu_ctx, oracle, bg031, cfg1, contrib, ls):
+    """Mixed path against the oracle for each contribution mask and several
+    multipole lists: even lists of up to four run the unit-bias kernel, the
+    odd list the general one."""
+    k, pk = cfg1["k"], cfg1["pk"]
+    gpu_ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+    gpu_ctx.integrals_init(k, pk[None, :], [(0, 0), (0, 2), (0, 4)], N=4096, precision="mixed",
+                           small_r=False)
+    sep = cfg1["sep"][::7]
+    z = 0.8
+    got = gpu_ctx.multipoles([0], [z], [0, len(sep)], sep, ls, contrib=contrib, precision="mixed")
+    m = oracle_model(oracle, bg031, k, pk, 4096)
+    ref = np.stack([m.multipoles_batch(contrib, np.full(len(sep), z), sep, np.full(len(sep), l))
+                    for l in ls], axis=1)
+    mono = m.multipoles_batch(contrib, np.full(len(sep), z), sep, np.zeros(len(sep)))
+    e = _mixed_err(got, ref, ls, mono, contrib)
+    print(contrib, ls, "mixed error / bound", e)
+    assert e < 1, e
+
+
+@pytest.mark.parametrize("equal", [False, True])
+def test_multipoles_with_galaxy_bias(oracle, bg031, cfg1, equal):
+    """z-dependent galaxy biases of both tracers (different ones give odd
+    multipoles), FP64 at 1e-10 and mixed at 1e-4 against the oracle."""
+    k, pk = cfg1["k"], cfg1["pk"]
+    zb = np.linspace(0.0, 3.0, 31)
+    b1 = 1.2 + 0.3 * zb
+    b2 = b1 if equal else 1.6 + 0.1 * zb ** 2
+    m = oracle_model(oracle, bg031, k, pk, 4096)
+    m.set_bias(0, zb, b1)
+    m.set_bias(1, zb, b2)
+    sep = cfg1["sep"][::9]
+    ls = (0, 1, 2, 3, 4)
+    z = 1.1
+    ref = np.stack([m.multipoles_batch(3, np.full(len(sep), z), sep, np.full(len(sep), l))
+                    for l in ls], axis=1)
+    from coffe_gb300.api import Context
+
+    ctx = Context(0)  # biases stay set for the context's lifetime
+    try:
+        ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+        ctx.set_bias(0, zb, b1)
+        ctx.set_bias(1, zb, b2)
+        for prec in ("fp64", "mixed"):
+            ctx.integrals_init(k, pk[None, :], [(0, 0), (0, 2), (0, 4)], N=4096,
+                               precision=prec, small_r=False)
+            got = ctx.multipoles([0], [z], [0, len(sep)], sep, ls, precision=prec)
+            if prec == "fp64":
+                e = _rel_fp64(got, ref, ls)
+                print("equal" if equal else "different", "fp64 max rel error", e)
+                assert e < 1e-10, e
+            else:
+                e = _mixed_err(got, ref, ls, ref[:, 0])
+                print("equal" if equal else "different", "mixed error / bound", e)
+                assert e < 1, e
+    finally:
+        ctx.close()
 
 
 def test_multipoles_golden_through_gpu(gpu_ctx, golden, class_pk, ref_bg):
