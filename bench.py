@@ -39,10 +39,14 @@ METRIC = "multipole evals/s at <=1e-4 rel err vs FP64: batched mixed vs plain FP
 UNIT = "evals/s"
 TERMS = ((0, 0), (0, 2), (0, 4))
 N_FFT = 4096
-# algorithmic FLOP of one multipole-quadrature node (xi + three P_l + GK61 sums,
-# FMA = 2; counted from multipoles.cu) and per (request, separation) extras
-FLOP_PER_NODE = 170
-FLOP_PER_PAIR_EXTRA = 130
+# FLOP of one multipole-quadrature node of the mixed kernel (mp_fast_kernel<3,3>,
+# counted from multipoles.cu, FMA = 2): chi1/chi2 4, two chi-table cells 18,
+# D, 1/D, s, c 6, density 2, RSD polynomial 16, density-RSD 16, Kronrod
+# (Kahan) / Gauss / |f| sums 27, second-pass resasc sums 12
+FLOP_PER_NODE = 101
+# per (request, separation): chi(z_mean) 8, three Akima table lookups 141,
+# per-pair constants 14, QUADPACK acceptance test of three multipoles 57
+FLOP_PER_PAIR_EXTRA = 220
 # nodes evaluated per (request, separation): the integrand is even in mu for the
 # benchmark's equal tracers and even multipoles, so the kernel evaluates the 31
 # GK61 nodes with mu >= 0 (the other 30 are their mirror images)
@@ -69,6 +73,8 @@ def parse():
     p.add_argument("--no-extras", action="store_true",
                    help="skip the lensing / covariance / gradient workload timings")
     p.add_argument("--no-clocks", action="store_true")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="keep the default launch configuration instead of timing candidates")
     p.add_argument("--kernel-only", choices=["mixed", "fp64", "tables-mixed", "tables-fp64"],
                    default=None,
                    help="profiling aid: run only the multipole kernel (mixed/fp64) or only the "
@@ -347,6 +353,11 @@ def ours(args, rank, world, local_rank):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    # launch shapes: the first build and multipole call of each shape time the
+    # candidate configurations (benchmark mode), later calls and the captured
+    # graph reuse the choice
+    if not args.no_autotune and not args.kernel_only:
+        ctx.set_autotune(True)
     # build the per-grid tables once (synchronous), then warm up
     for prec in ("mixed", "fp64"):
         ctx.integrals_init_device(batch.k, pk_d, TERMS, N=N_FFT, precision=prec, sync=True)
@@ -410,6 +421,7 @@ def ours(args, rank, world, local_rank):
     with ClockSampler(local_rank, enabled=not args.no_clocks and rank == 0) as clk:
         dev_mixed, wall_mixed, launches = timed("mixed", args.steps)
     clocks = clk.summary()
+    tuning = ctx.tuning()
     k64 = args.fp64_steps or max(3, args.steps // 50)
     for _ in range(2):
         step("fp64")
@@ -520,6 +532,7 @@ def ours(args, rank, world, local_rank):
                    "separations": n_sep, "evals_per_step": n_evals,
                    "l2": "flushed between timed steps (256 MiB write outside the events)",
                    "cuda_graph": bool(graphs), "graph_output_equals_direct": graph_equal,
+                   "launch_config": tuning, "autotuned": not args.no_autotune,
                    "parallelism": f"replicas x{world}"},
         "fp64": {"value": fp64_value, "unit": UNIT, "steps": k64,
                  "ms_per_step": 1e3 * dev_fp64 / k64},
@@ -527,7 +540,7 @@ def ours(args, rank, world, local_rank):
         "max_rel_err_mixed_vs_fp64": err,
         "adaptive_retries": retries,
         "gpu_launches": int(launches),
-        "roofline": {"kernel": "mp_lane_kernel<3, float> (mixed multipole quadrature)",
+        "roofline": {"kernel": "mp_fast_kernel<3, 3> (mixed multipole quadrature, unit biases)",
                      "bound": "fp32", "achieved": achieved,
                      "peak": sgemm, "unit": "TFLOP/s", "frac": achieved / sgemm,
                      "peak_source": "measured cuBLAS SGEMM 8192^3 (FP32 CUDA cores, TF32 off) "

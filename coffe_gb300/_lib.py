@@ -59,6 +59,9 @@ EXPORTS = (
     "coffe_gpu_multipoles_adjoint",
     "coffe_gpu_covariance_integrals",
     "coffe_gpu_covariance_multipoles",
+    "coffe_gpu_set_autotune",
+    "coffe_gpu_get_tuning",
+    "coffe_gpu_set_tuning",
     "coffe_gpu_launch_count",
 )
 
@@ -71,6 +74,18 @@ class Cosmology(C.Structure):
         ("Omega0_de", C.c_double),
         ("h", C.c_double),
         ("bins", C.c_int),
+    ]
+
+
+class Tuning(C.Structure):
+    """coffe_gpu_tuning_t: launch shapes of the table stage and the mixed
+    multipole kernel."""
+    _fields_ = [
+        ("fft_threads", C.c_int),
+        ("fft_radix", C.c_int),
+        ("fft_swizzle", C.c_int),
+        ("spline_group", C.c_int),
+        ("lane_threads", C.c_int),
     ]
 
 
@@ -142,6 +157,9 @@ def load(build_if_missing: bool = True):
                                                   _ip, C.c_int, _dp, _dp]
     L.coffe_gpu_multipoles_retries.argtypes = [_p]
     L.coffe_gpu_multipoles_retries.restype = C.c_longlong
+    L.coffe_gpu_set_autotune.argtypes = [_p, C.c_int]
+    L.coffe_gpu_get_tuning.argtypes = [_p, C.POINTER(Tuning)]
+    L.coffe_gpu_set_tuning.argtypes = [_p, C.POINTER(Tuning)]
     L.coffe_gpu_launch_count.argtypes = [_p]
     L.coffe_gpu_launch_count.restype = C.c_longlong
     _lib = L

@@ -99,6 +99,31 @@ class Context:
     def launch_count(self) -> int:
         return int(self._L.coffe_gpu_launch_count(self._ctx))
 
+    # ------------------------------------------------------------- tuning
+    def set_autotune(self, enable: bool = True):
+        """Benchmark mode: the first table build and mixed multipole call of
+        each shape time every candidate launch configuration and keep the
+        fastest (calls under stream capture never time)."""
+        self._check(self._L.coffe_gpu_set_autotune(self._ctx, int(bool(enable))), "set_autotune")
+
+    def tuning(self) -> dict:
+        """Configuration used by the most recent table build and mixed
+        multipole call."""
+        t = _lib.Tuning()
+        self._check(self._L.coffe_gpu_get_tuning(self._ctx, C.byref(t)), "get_tuning")
+        return {name: getattr(t, name) for name, _ in _lib.Tuning._fields_}
+
+    def set_tuning(self, **cfg):
+        """Default configuration (keys of :meth:`tuning`; missing keys keep their
+        current value); forgets the configurations chosen by autotuning."""
+        cur = self.tuning()
+        unknown = set(cfg) - set(cur)
+        if unknown:
+            raise ValueError(f"unknown tuning keys {sorted(unknown)}")
+        cur.update(cfg)
+        t = _lib.Tuning(**{k: int(v) for k, v in cur.items()})
+        self._check(self._L.coffe_gpu_set_tuning(self._ctx, C.byref(t)), "set_tuning")
+
     def last_retries(self) -> int:
         """(separation, l) outputs of the last multipoles call that needed the
         adaptive bisection after the first GK61 panel."""

@@ -284,6 +284,36 @@ int coffe_gpu_set_bias(coffe_gpu_ctx_t *ctx, int which, const double *z, const d
     return cg_check_device_errors(ctx, "set_bias");
 }
 
+int coffe_gpu_set_autotune(coffe_gpu_ctx_t *ctx, int enable)
+{
+    if (!ctx) return COFFE_GPU_EINVAL;
+    ctx->autotune = enable != 0;
+    return COFFE_GPU_OK;
+}
+
+int coffe_gpu_get_tuning(const coffe_gpu_ctx_t *ctx, coffe_gpu_tuning_t *out)
+{
+    if (!ctx || !out) return COFFE_GPU_EINVAL;
+    *out = ctx->last_tuning;
+    return COFFE_GPU_OK;
+}
+
+int coffe_gpu_set_tuning(coffe_gpu_ctx_t *ctx, const coffe_gpu_tuning_t *t)
+{
+    if (!ctx || !t) return COFFE_GPU_EINVAL;
+    const int ft = t->fft_threads, lt = t->lane_threads, g = t->spline_group;
+    if (!(ft == 128 || ft == 256 || ft == 512 || ft == 1024) ||
+        !(t->fft_radix == 2 || t->fft_radix == 4) || !(t->fft_swizzle == 0 || t->fft_swizzle == 1) ||
+        !(g == 2 || g == 4 || g == 8) || !(lt == 64 || lt == 128 || lt == 256)) {
+        cg_set_error(ctx, "set_tuning: fft_threads 128/256/512/1024, fft_radix 2/4, fft_swizzle "
+                          "0/1, spline_group 2/4/8, lane_threads 64/128/256");
+        return COFFE_GPU_EINVAL;
+    }
+    ctx->tuning = *t;
+    ctx->tune_cache.clear();
+    return COFFE_GPU_OK;
+}
+
 size_t coffe_gpu_integral_table_len(size_t N) { return N + CG_N_SMALL_R + 1; }
 
 int coffe_gpu_integrals_init(coffe_gpu_ctx_t *ctx, const double *k, const double *pk,

@@ -5,6 +5,8 @@
 #include <stdarg.h>
 #include <stdio.h>
 
+#include <array>
+#include <map>
 #include <vector>
 
 #include "spline.cuh"
@@ -52,6 +54,12 @@ struct coffe_gpu_ctx {
     // ---- integral tables
     bool int_ready = false;
     int n_spectra = 0, n_terms = 0, int_precision = 0;
+
+    // ---- launch shapes (coffe_gpu_set_tuning / benchmark-mode autotuning)
+    coffe_gpu_tuning_t tuning = {512, 4, 1, 8, 128}; // default configuration
+    coffe_gpu_tuning_t last_tuning = {512, 4, 1, 8, 128};
+    bool autotune = false;
+    std::map<std::array<long long, 6>, coffe_gpu_tuning_t> tune_cache; // shape -> choice
     size_t N = 0, nk = 0;
     double kmin = 0, kmax = 0;
     bool int_small_r = false; // r = 0 and sub-Mpc entries filled
@@ -149,6 +157,56 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
 int integrals_eval(coffe_gpu_ctx *ctx, int spectrum, int term, const double *r, size_t nq,
                    double *out);
 int multipoles_prepare_background(coffe_gpu_ctx *ctx);
+
+// Configuration for one launch shape: the chosen one if the shape was tuned,
+// else (benchmark mode, stream not capturing) the fastest of `cands` timed
+// with `run` on the stream, else the default.  run(cfg) enqueues the work.
+template <typename Run>
+int cg_tuned(coffe_gpu_ctx *ctx, const std::array<long long, 6> &key,
+             const std::vector<coffe_gpu_tuning_t> &cands, Run run, coffe_gpu_tuning_t *out)
+{
+    auto it = ctx->tune_cache.find(key);
+    if (it != ctx->tune_cache.end()) {
+        *out = it->second;
+        return 0;
+    }
+    *out = ctx->tuning;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (!ctx->autotune || cands.size() < 2 ||
+        cudaStreamIsCapturing(ctx->stream, &cap) != cudaSuccess ||
+        cap != cudaStreamCaptureStatusNone)
+        return 0;
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess) return COFFE_GPU_ECUDA;
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return COFFE_GPU_ECUDA;
+    }
+    float best = 3.0e38f;
+    int st = 0;
+    for (const coffe_gpu_tuning_t &c : cands) {
+        if ((st = run(c))) break; // warm-up of this configuration
+        float t = 3.0e38f;
+        for (int rep = 0; rep < 2 && !st; ++rep) {
+            cudaEventRecord(e0, ctx->stream);
+            st = run(c);
+            cudaEventRecord(e1, ctx->stream);
+            if (cudaEventSynchronize(e1) != cudaSuccess) st = COFFE_GPU_ECUDA;
+            float ms = 0.f;
+            if (!st && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms < t) t = ms;
+        }
+        if (st) break;
+        if (t < best) {
+            best = t;
+            *out = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) return st;
+    ctx->tune_cache[key] = *out;
+    return 0;
+}
 int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, int n_req,
                    const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
                    const double *sep, int n_l, const int *l, double *out, long long total);

@@ -62,25 +62,33 @@ __device__ __forceinline__ double df_to_double(dfl x) { return (double)x.hi + (d
 // The same split with integer operations only (a double-to-float conversion
 // runs on the FP64 pipe, 1/64 of the FP32 rate): hi = the leading 24
 // significant bits rounded half up, lo = the remainder kept to 22 bits, so
-// |hi + lo - d| <= 2^-46 |d| and |lo| <= ulp(hi) / 2.  Magnitudes outside
-// [2^-80, 2^127), zeros and non-finite values take df_from_double.
+// |hi + lo - d| <= 2^-46 |d| and |lo| <= ulp(hi) / 2 for 2^-80 <= |d| < 2^128
+// (hi rounds to infinity as a float conversion does).  Outside that range
+// lo = 0 and hi is what a float keeps: the same leading bits down to 2^-126,
+// zero below, infinity above, NaN for NaN.
 __device__ __forceinline__ dfl df_from_double_bits(double d)
 {
     const unsigned long long u = (unsigned long long)__double_as_longlong(d);
     const unsigned top = (unsigned)(u >> 32);
-    const int E = (int)((top >> 20) & 0x7ffu) - 1023;
-    if (E < -80 || E > 126) return df_from_double(d);
+    const int e = (int)((top >> 20) & 0x7ffu);
+    const int E = e - 1023;
     const unsigned long long mant = u & 0xFFFFFFFFFFFFFull;
     const unsigned rbit = (unsigned)(mant >> 28) & 1u;
     const unsigned sign = top & 0x80000000u;
     // exponent and top 23 fraction bits; a rounding carry moves into the exponent
-    const unsigned hb = ((unsigned)(E + 127) << 23) + (unsigned)(mant >> 29) + rbit;
+    const int Ec = E < -126 ? -126 : (E > 127 ? 127 : E);
+    const unsigned hb = ((unsigned)(Ec + 127) << 23) + (unsigned)(mant >> 29) + rbit;
     // remainder in units of 2^(E - 52), in (-2^28, 2^28]; floor to units of 2^(E - 46)
     const int rem = ((int)(mant & 0x1FFFFFFFull) - (int)(rbit << 29)) >> 6;
     // |rem| <= 2^22: exact as a float through the 1.5 * 2^23 offset
     const float x = __int_as_float(0x4B400000 + rem) - 12582912.f;
-    const float lo = x * __int_as_float((E - 46 + 127) << 23);
-    return dfl{__int_as_float((int)(hb | sign)), __int_as_float(__float_as_int(lo) ^ (int)sign)};
+    const int Es = E < -80 ? -80 : (E > 127 ? 127 : E);
+    float lo = x * __int_as_float((Es - 46 + 127) << 23);
+    unsigned hi = hb;
+    if (E < -126) hi = 0u;                                        // zero, subnormal double
+    if (E > 127) hi = e == 2047 && mant ? 0x7FC00000u : 0x7F800000u; // NaN / overflow
+    if (E < -80 || E > 127) lo = 0.f;
+    return dfl{__int_as_float((int)(hi | sign)), __int_as_float(__float_as_int(lo) ^ (int)sign)};
 }
 
 // complex double-float, stored as float4 (re.hi, re.lo, im.hi, im.lo)

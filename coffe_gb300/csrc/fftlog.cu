@@ -316,11 +316,11 @@ __global__ void cspline_c_kernel(const double *__restrict__ x, const double *__r
 // memory, the band stored by diagonal so that its loads coalesce.
 #define CS_BAND 12
 #define CS_TILE 256
-#define CS_SPB 8 // spectra per block: each thread keeps its band row in registers
 #define CS_HALO (CS_TILE + 2 * CS_BAND + 2)
 // One pass per (tile of knots, group of CS_SPB spectra): reads the FP64
 // spectra once, writes them as double-float pairs for the FFT input
 // (integer split, no FP64 work) and the float spline coefficients.
+template <int CS_SPB> // spectra per block: each thread keeps its band row in registers
 __global__ void __launch_bounds__(CS_TILE)
     cspline_band_kernel(const double *__restrict__ pk, const float *__restrict__ band_t,
                         const float *__restrict__ fac32, int nk, int n_spectra,
@@ -535,20 +535,59 @@ __global__ void fftlog_inverse_kernel(GridPar g, const double2 *__restrict__ spe
 
 // ---- mixed path: the same transforms in double-float on the FP32 pipes
 
-// DIT FFT of M = 2^logM double-float complex points (bit-reversed input):
-// pairs of radix-2 stages fused into radix-4 butterflies in registers (three
-// twiddle products per four points instead of four, half the shared-memory
-// passes), after one twiddle-free radix-2 stage when logM is odd.
-// tw[j] = exp(-2 pi i j / (2M)), j <= M; sign = -1 forward, +1 backward.
+// Shared-memory layout of the double-float transforms: element i at
+// i ^ f(i >> 3), f taking values below 8, so each aligned group of eight
+// 16-byte elements (one 128-byte bank row) is permuted within itself.  f
+// spreads the patterns that otherwise fall on one bank: the bit-reversed
+// scatter (eight consecutive k differ in the three top index bits; the shift
+// sh = logM - 6 brings them down), the stride-two radix-2 stage and the
+// half = 2 radix-4 stage.  SWZ = false is the plain layout (needs M >= 8 for
+// the swizzle).
+template <bool SWZ> __device__ __forceinline__ int fft_slot(int i, int sh)
+{
+    if (!SWZ) return i;
+    const int x = i >> 3;
+    const int f = ((x & 1) * 3) | ((x & 2) << 1);
+    return i ^ ((f ^ (x >> sh)) & 7);
+}
+
+// DIT FFT of M = 2^logM double-float complex points (bit-reversed input).
+// RADIX 4: pairs of radix-2 stages fused into radix-4 butterflies in
+// registers (three twiddle products per four points instead of four, half the
+// shared-memory passes), after one twiddle-free radix-2 stage when logM is
+// odd.  RADIX 2: one stage per pass.  tw[j] = exp(-2 pi i j / (2M)), j <= M;
+// sign = -1 forward, +1 backward.
+template <int RADIX, bool SWZ>
 __device__ void smem_fft_df(float4 *buf, int logM, const float4 *__restrict__ tw, int sign)
 {
     const int M = 1 << logM;
+    const int sh = logM > 6 ? logM - 6 : 0;
+    if (RADIX == 2) {
+        for (int st = 1; st <= logM; ++st) {
+            const int half = 1 << (st - 1);
+            const int stride = M >> (st - 1);
+            for (int b = threadIdx.x; b < M / 2; b += blockDim.x) {
+                const int pos = b & (half - 1);
+                const int i0 = ((b >> (st - 1)) << st) + pos;
+                const int p0 = fft_slot<SWZ>(i0, sh), p1 = fft_slot<SWZ>(i0 + half, sh);
+                dfc w = dfc_load(tw[pos * stride]);
+                if (sign > 0) w.im = df_neg(w.im);
+                const dfc u = dfc_load(buf[p0]);
+                const dfc t = dfc_mul(w, dfc_load(buf[p1]));
+                buf[p0] = dfc_pack(dfc_add(u, t));
+                buf[p1] = dfc_pack(dfc_sub(u, t));
+            }
+            __syncthreads();
+        }
+        return;
+    }
     int st = 1;
     if (logM & 1) {
         for (int b = threadIdx.x; b < M / 2; b += blockDim.x) {
-            const dfc u = dfc_load(buf[2 * b]), v = dfc_load(buf[2 * b + 1]);
-            buf[2 * b] = dfc_pack(dfc_add(u, v));
-            buf[2 * b + 1] = dfc_pack(dfc_sub(u, v));
+            const int p0 = fft_slot<SWZ>(2 * b, sh), p1 = fft_slot<SWZ>(2 * b + 1, sh);
+            const dfc u = dfc_load(buf[p0]), v = dfc_load(buf[p1]);
+            buf[p0] = dfc_pack(dfc_add(u, v));
+            buf[p1] = dfc_pack(dfc_sub(u, v));
         }
         __syncthreads();
         st = 2;
@@ -561,10 +600,12 @@ __device__ void smem_fft_df(float4 *buf, int logM, const float4 *__restrict__ tw
         for (int b = threadIdx.x; b < M / 4; b += blockDim.x) {
             const int pos = b & (half - 1);
             const int i0 = ((b >> (st - 1)) << (st + 1)) + pos;
-            const dfc x0 = dfc_load(buf[i0]);
-            dfc x1 = dfc_load(buf[i0 + half]);
-            dfc x2 = dfc_load(buf[i0 + 2 * half]);
-            dfc x3 = dfc_load(buf[i0 + 3 * half]);
+            const int p0 = fft_slot<SWZ>(i0, sh), p1 = fft_slot<SWZ>(i0 + half, sh);
+            const int p2 = fft_slot<SWZ>(i0 + 2 * half, sh), p3 = fft_slot<SWZ>(i0 + 3 * half, sh);
+            const dfc x0 = dfc_load(buf[p0]);
+            dfc x1 = dfc_load(buf[p1]);
+            dfc x2 = dfc_load(buf[p2]);
+            dfc x3 = dfc_load(buf[p3]);
             if (half > 1) { // pos = 0 when half = 1: all twiddles are one
                 const int j = pos * step, j3 = 3 * j;
                 dfc w1 = dfc_load(tw[2 * j]), w2 = dfc_load(tw[j]);
@@ -582,10 +623,10 @@ __device__ void smem_fft_df(float4 *buf, int logM, const float4 *__restrict__ tw
             const dfc t2 = dfc_add(x2, x3), t3 = dfc_sub(x2, x3);
             // w_{4 half}^half = -i forward, +i backward
             const dfc r = sign < 0 ? dfc{t3.im, df_neg(t3.re)} : dfc{df_neg(t3.im), t3.re};
-            buf[i0] = dfc_pack(dfc_add(t0, t2));
-            buf[i0 + half] = dfc_pack(dfc_add(t1, r));
-            buf[i0 + 2 * half] = dfc_pack(dfc_sub(t0, t2));
-            buf[i0 + 3 * half] = dfc_pack(dfc_sub(t1, r));
+            buf[p0] = dfc_pack(dfc_add(t0, t2));
+            buf[p1] = dfc_pack(dfc_add(t1, r));
+            buf[p2] = dfc_pack(dfc_sub(t0, t2));
+            buf[p3] = dfc_pack(dfc_sub(t1, r));
         }
         __syncthreads();
     }
@@ -614,6 +655,7 @@ __device__ __forceinline__ dfl sample_input_df(const float2 *__restrict__ y,
     return df_mul(df_add(secant, dfl{corr, 0.f}), dfl{q.x, q.y});
 }
 
+template <int RADIX, bool SWZ>
 __global__ void fftlog_forward_df_kernel(GridPar g, const float2 *__restrict__ pkdf,
                                          const float *__restrict__ cc32,
                                          const int *__restrict__ idx,
@@ -630,22 +672,23 @@ __global__ void fftlog_forward_df_kernel(GridPar g, const float2 *__restrict__ p
     const int s = blockIdx.x, qi = blockIdx.y;
     const int N = g.N, M = N / 2;
     const int logM = 31 - __clz(M);
+    const int sh = logM > 6 ? logM - 6 : 0;
     const float2 *y = pkdf + (size_t)s * g.nk;
     const float *c = cc32 + (size_t)s * g.nk;
     bool bad = false;
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
         const dfl d = sample_input_df(y, c, idx, tdf, sf32, qfac_df + (size_t)qi * N, i);
         if (!isfinite(d.hi)) bad = true;
-        const int jj = __brev((unsigned)(i >> 1)) >> (32 - logM);
+        const int jj = fft_slot<SWZ>(__brev((unsigned)(i >> 1)) >> (32 - logM), sh);
         buf2[2 * jj + (i & 1)] = make_float2(d.hi, d.lo);
     }
     if (bad) cg_flag(err, CG_ERR_NONFINITE);
     __syncthreads();
-    smem_fft_df(buf, logM, twdf, -1);
+    smem_fft_df<RADIX, SWZ>(buf, logM, twdf, -1);
     float4 *out = spec + ((size_t)s * n_q + qi) * (M + 1);
     for (int k = threadIdx.x; k <= M; k += blockDim.x) {
-        const dfc zk = dfc_load(buf[k & (M - 1)]);
-        const dfc zm = dfc_conj(dfc_load(buf[(M - k) & (M - 1)]));
+        const dfc zk = dfc_load(buf[fft_slot<SWZ>(k & (M - 1), sh)]);
+        const dfc zm = dfc_conj(dfc_load(buf[fft_slot<SWZ>((M - k) & (M - 1), sh)]));
         const dfc e = dfc_add(zk, zm);                  // 2 E
         const dfc dd = dfc_sub(zk, zm);                 // 2 i O
         const dfc o = dfc{dd.im, df_neg(dd.re)};        // 2 O = -i (2 i O)
@@ -666,6 +709,7 @@ __device__ __forceinline__ dfc c2r_pre(dfc xa, dfc xb, float4 w)
     return dfc{df_sub(fe.re, fo.im), df_add(fe.im, fo.re)};
 }
 
+template <int RADIX, bool SWZ>
 __global__ void fftlog_inverse_df_kernel(GridPar g, const float4 *__restrict__ spec,
                                          const int *__restrict__ term_q, int n_q, int n_terms,
                                          const float4 *__restrict__ mcoef_df,
@@ -678,6 +722,7 @@ __global__ void fftlog_inverse_df_kernel(GridPar g, const float4 *__restrict__ s
     const int s = blockIdx.x, t = blockIdx.y;
     const int N = g.N, M = N / 2;
     const int logM = 31 - __clz(M);
+    const int sh = logM > 6 ? logM - 6 : 0;
     const float4 *in = spec + ((size_t)s * n_q + term_q[t]) * (M + 1);
     const float4 *mc = mcoef_df + (size_t)t * (M + 1);
     // z_k = Fe_k + i Fo_k from X_k and conj(X_{M-k}), X = spectrum x kernel;
@@ -690,18 +735,20 @@ __global__ void fftlog_inverse_df_kernel(GridPar g, const float4 *__restrict__ s
             xa.im = dfl{0.f, 0.f};
             xb.im = dfl{0.f, 0.f};
         }
-        buf[__brev((unsigned)k) >> (32 - logM)] = dfc_pack(c2r_pre(xa, xb, twdf[k]));
+        buf[fft_slot<SWZ>(__brev((unsigned)k) >> (32 - logM), sh)] =
+            dfc_pack(c2r_pre(xa, xb, twdf[k]));
         if (k > 0 && k < M / 2)
-            buf[__brev((unsigned)km) >> (32 - logM)] = dfc_pack(c2r_pre(xb, xa, twdf[km]));
+            buf[fft_slot<SWZ>(__brev((unsigned)km) >> (32 - logM), sh)] =
+                dfc_pack(c2r_pre(xb, xa, twdf[km]));
     }
     __syncthreads();
-    smem_fft_df(buf, logM, twdf, +1);
+    smem_fft_df<RADIX, SWZ>(buf, logM, twdf, +1);
     const size_t len = (size_t)N + CG_N_SMALL_R + 1;
     float *o = tab + ((size_t)s * n_terms + t) * len + CG_N_SMALL_R + 1;
     const float2 *pf = postf_df + (size_t)t * N;
     bool bad = false;
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        const float4 z = buf[i >> 1];
+        const float4 z = buf[fft_slot<SWZ>(i >> 1, sh)];
         const dfl u = (i & 1) ? dfl{z.z, z.w} : dfl{z.x, z.y};
         const float2 p = pf[i];
         const dfl r = df_mul(u, dfl{p.x, p.y});
@@ -1071,54 +1118,99 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         ctx->grid_terms = terms_key;
     }
     // per spectrum: natural-spline coefficients, forward FFTs, inverse FFTs
-    if (mixed) {
-        if ((st = cg_ensure(ctx, ctx->pk_df, sizeof(float2) * nk * n_spectra))) return st;
-        cspline_band_kernel<<<dim3(((int)nk - 2 + CS_TILE - 1) / CS_TILE,
-                                   (n_spectra + CS_SPB - 1) / CS_SPB),
-                              CS_TILE, 0, ctx->stream>>>(
-            d_pk, (const float *)ctx->csband.p, (const float *)ctx->csfac32.p, (int)nk, n_spectra,
-            (float2 *)ctx->pk_df.p, (float *)ctx->csc.p);
-        if ((st = cg_after_launch(ctx, "cspline_band_kernel"))) return st;
-    } else {
+    if (mixed && (st = cg_ensure(ctx, ctx->pk_df, sizeof(float2) * nk * n_spectra))) return st;
+    const size_t smem = sizeof(double2) * M; // == sizeof(float4) * M
+    const dim3 gf(n_spectra, n_q), gi(n_spectra, n_terms);
+    auto stage = [&](const coffe_gpu_tuning_t &tu) -> int {
+        int s2;
+        if (mixed) {
+            const dim3 gb(((int)nk - 2 + CS_TILE - 1) / CS_TILE,
+                          (n_spectra + tu.spline_group - 1) / tu.spline_group);
+#define CS_LAUNCH(G)                                                                              \
+    cspline_band_kernel<G><<<gb, CS_TILE, 0, ctx->stream>>>(                                      \
+        d_pk, (const float *)ctx->csband.p, (const float *)ctx->csfac32.p, (int)nk, n_spectra,    \
+        (float2 *)ctx->pk_df.p, (float *)ctx->csc.p)
+            if (tu.spline_group == 2)
+                CS_LAUNCH(2);
+            else if (tu.spline_group == 4)
+                CS_LAUNCH(4);
+            else
+                CS_LAUNCH(8);
+#undef CS_LAUNCH
+            if ((s2 = cg_after_launch(ctx, "cspline_band_kernel"))) return s2;
+#define DF_LAUNCH(R, W)                                                                           \
+    {                                                                                             \
+        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_forward_df_kernel<R, W>,                         \
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_df_kernel<R, W>,                         \
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+        fftlog_forward_df_kernel<R, W><<<gf, tu.fft_threads, smem, ctx->stream>>>(                \
+            g, (const float2 *)ctx->pk_df.p, (const float *)ctx->csc.p,                           \
+            (const int *)ctx->samp_idx.p, (const float2 *)ctx->samp_tdf.p,                        \
+            (const float4 *)ctx->samp_f32.p, (const float2 *)ctx->qfac_df.p, wdf,                 \
+            (const float4 *)ctx->twid32.p, n_q, (float4 *)ctx->spec.p, ctx->d_err);               \
+        if ((s2 = cg_after_launch(ctx, "fftlog_forward_df_kernel"))) return s2;                   \
+        fftlog_inverse_df_kernel<R, W><<<gi, tu.fft_threads, smem, ctx->stream>>>(                \
+            g, (const float4 *)ctx->spec.p, d_meta->tq, n_q, n_terms, mdf, pdf,                   \
+            (const float4 *)ctx->twid32.p, (float *)ctx->tab_y.p, ctx->d_err);                    \
+        if ((s2 = cg_after_launch(ctx, "fftlog_inverse_df_kernel"))) return s2;                   \
+    }
+            const bool swz = tu.fft_swizzle && M >= 64;
+            if (tu.fft_radix == 2) {
+                if (swz) DF_LAUNCH(2, true) else DF_LAUNCH(2, false)
+            } else {
+                if (swz) DF_LAUNCH(4, true) else DF_LAUNCH(4, false)
+            }
+#undef DF_LAUNCH
+            return COFFE_GPU_OK;
+        }
         cspline_c_kernel<<<(n_spectra + 3) / 4, 128, 0, ctx->stream>>>(
             (const double *)ctx->kgrid.p, d_pk, (const double *)ctx->csfac.p, (int)nk, n_spectra,
             (double *)ctx->csc.p);
-        if ((st = cg_after_launch(ctx, "cspline_c_kernel"))) return st;
-    }
-    const int fft_threads = 512;
-    const size_t smem = sizeof(double2) * M; // == sizeof(float4) * M
-    dim3 gf(n_spectra, n_q), gi(n_spectra, n_terms);
-    if (mixed) {
-        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_forward_df_kernel,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_df_kernel,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        fftlog_forward_df_kernel<<<gf, fft_threads, smem, ctx->stream>>>(
-            g, (const float2 *)ctx->pk_df.p, (const float *)ctx->csc.p,
-            (const int *)ctx->samp_idx.p, (const float2 *)ctx->samp_tdf.p,
-            (const float4 *)ctx->samp_f32.p, (const float2 *)ctx->qfac_df.p, wdf,
-            (const float4 *)ctx->twid32.p, n_q, (float4 *)ctx->spec.p, ctx->d_err);
-        if ((st = cg_after_launch(ctx, "fftlog_forward_df_kernel"))) return st;
-        fftlog_inverse_df_kernel<<<gi, fft_threads, smem, ctx->stream>>>(
-            g, (const float4 *)ctx->spec.p, d_meta->tq, n_q, n_terms, mdf, pdf,
-            (const float4 *)ctx->twid32.p, (float *)ctx->tab_y.p, ctx->d_err);
-        if ((st = cg_after_launch(ctx, "fftlog_inverse_df_kernel"))) return st;
-    } else {
+        if ((s2 = cg_after_launch(ctx, "cspline_c_kernel"))) return s2;
         CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_forward_kernel,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_kernel,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        fftlog_forward_kernel<<<gf, fft_threads, smem, ctx->stream>>>(
+        fftlog_forward_kernel<<<gf, tu.fft_threads, smem, ctx->stream>>>(
             g, (const double *)ctx->kgrid.p, d_pk, (const double *)ctx->csc.p,
             (const double *)ctx->csfac.p, (const int *)ctx->samp_idx.p,
             (const double *)ctx->samp_dx.p, (const double *)ctx->qfac.p, modew,
             (const double2 *)ctx->twid.p, n_q, (double2 *)ctx->spec.p, ctx->d_err);
-        if ((st = cg_after_launch(ctx, "fftlog_forward_kernel"))) return st;
-        fftlog_inverse_kernel<<<gi, fft_threads, smem, ctx->stream>>>(
+        if ((s2 = cg_after_launch(ctx, "fftlog_forward_kernel"))) return s2;
+        fftlog_inverse_kernel<<<gi, tu.fft_threads, smem, ctx->stream>>>(
             g, (const double2 *)ctx->spec.p, d_meta->tq, n_q, n_terms, mcoef,
             (const double *)ctx->postf.p, (const double2 *)ctx->twid.p, (double *)ctx->tab_y.p,
             ctx->d_err);
-        if ((st = cg_after_launch(ctx, "fftlog_inverse_kernel"))) return st;
+        return cg_after_launch(ctx, "fftlog_inverse_kernel");
+    };
+    // candidate launch shapes of this table stage
+    std::vector<coffe_gpu_tuning_t> cands;
+    for (int ft : {128, 256, 512})
+        for (int rad : {2, 4})
+            for (int sw : {0, 1})
+                for (int grp : {2, 4, 8}) {
+                    coffe_gpu_tuning_t c = ctx->tuning;
+                    c.fft_threads = ft;
+                    if (mixed) {
+                        if (sw && M < 64) continue;
+                        c.fft_radix = rad;
+                        c.fft_swizzle = sw;
+                        c.spline_group = grp;
+                    } else if (rad != 2 || sw || grp != 2) {
+                        continue; // the FP64 transforms have only the thread count
+                    }
+                    cands.push_back(c);
+                }
+    coffe_gpu_tuning_t tu;
+    const std::array<long long, 6> key{1, (long long)N, n_spectra, n_terms, n_q, mixed ? 1 : 0};
+    if ((st = cg_tuned(ctx, key, cands, stage, &tu))) return st;
+    if ((st = stage(tu))) return st;
+    ctx->last_tuning.fft_threads = tu.fft_threads;
+    if (mixed) {
+        ctx->last_tuning.fft_radix = tu.fft_radix;
+        ctx->last_tuning.fft_swizzle = tu.fft_swizzle;
+        ctx->last_tuning.spline_group = tu.spline_group;
     }
     // r = 0 and sub-Mpc entries
     const long tables = (long)n_spectra * n_terms;

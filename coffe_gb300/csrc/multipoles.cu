@@ -656,8 +656,9 @@ template <int NL> struct FastLayout {
     static constexpr int COUNT = ROWS * (R1 + R2);
 };
 
+#define MP_FAST_MAX_THREADS 256
 template <int NL, int CONTRIB>
-__global__ void __launch_bounds__(MP_LANE_THREADS)
+__global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
     mp_fast_kernel(MpArgs a, ChiTab ct, float chi_lo, float chi_hi, Spl32 chi_of_z,
                    const float *__restrict__ tab_x, const float *__restrict__ tab_y,
                    const int *__restrict__ req_spectrum, const double *__restrict__ req_z_mean,
@@ -848,7 +849,6 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<float, Spl32> &bg,
 {
     int *d_count = (int *)ctx->mp_retry.p;
     int2 *d_retry = (int2 *)((char *)ctx->mp_retry.p + 256);
-    CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
     const void *dn = nullptr;
     int st = node_slot(ctx, a.n_l, a.ls, COFFE_GPU_MIXED, 2,
                        [&](std::vector<unsigned char> &bytes) {
@@ -862,33 +862,51 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<float, Spl32> &bg,
     const double inv_h = ctx->chi_cells / (ctx->chi_hi - ctx->chi_lo);
     const ChiTab ct{(const float4 *)ctx->chitab32.p, (float)inv_h,
                     (float)(-ctx->chi_lo * inv_h - 0.5), (float)ctx->chi_cells};
-    const long long blocks = (total + MP_LANE_THREADS - 1) / MP_LANE_THREADS;
     const int contrib = a.contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD);
+    // first panel (with lt threads per block) and the adaptive retries
+    auto run = [&](const coffe_gpu_tuning_t &tu) -> int {
+        const int lt = tu.lane_threads;
+        const long long blocks = (total + lt - 1) / lt;
+        CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
 #define MP_FAST(NLV, CV)                                                                          \
     if (a.n_l == NLV && contrib == CV) {                                                          \
-        const size_t smem = sizeof(float) * (FastLayout<NLV>::COUNT +                             \
-                                             FastLayout<NLV>::ROWS * MP_LANE_THREADS);            \
+        const size_t smem = sizeof(float) * (FastLayout<NLV>::COUNT + FastLayout<NLV>::ROWS * lt); \
         CG_CUDA(ctx, cudaFuncSetAttribute(mp_fast_kernel<NLV, CV>,                                \
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,            \
                                           (int)smem));                                            \
-        mp_fast_kernel<NLV, CV><<<(unsigned)blocks, MP_LANE_THREADS, smem, ctx->stream>>>(        \
+        mp_fast_kernel<NLV, CV><<<(unsigned)blocks, lt, smem, ctx->stream>>>(                     \
             a, ct, bg.z_of_chi.x0, bg.z_of_chi.xn, chi_of_z, tab_x, tab_y, req_spectrum,          \
             req_z_mean, req_offset, sep, total, (const float *)dn, out, d_count, d_retry,         \
             ctx->d_err);                                                                          \
     }
 #define MP_FAST_NL(NLV) MP_FAST(NLV, 1) MP_FAST(NLV, 2) MP_FAST(NLV, 3)
-    MP_FAST_NL(1)
-    MP_FAST_NL(2)
-    MP_FAST_NL(3)
-    MP_FAST_NL(4)
+        MP_FAST_NL(1)
+        MP_FAST_NL(2)
+        MP_FAST_NL(3)
+        MP_FAST_NL(4)
 #undef MP_FAST_NL
 #undef MP_FAST
-    if ((st = cg_after_launch(ctx, "mp_fast_kernel"))) return st;
-    mp_retry_kernel<float, Spl32, float><<<ctx->sm_count * 2, 32 * MP_RETRY_WARPS, 0,
-                                           ctx->stream>>>(a, bg, chi_of_z, tab_x, tab_y,
-                                                          req_spectrum, req_z_mean, req_offset,
-                                                          sep, out, d_count, d_retry, ctx->d_err);
-    return cg_after_launch(ctx, "mp_retry_kernel");
+        int s2 = cg_after_launch(ctx, "mp_fast_kernel");
+        if (s2) return s2;
+        mp_retry_kernel<float, Spl32, float><<<ctx->sm_count * 2, 32 * MP_RETRY_WARPS, 0,
+                                               ctx->stream>>>(a, bg, chi_of_z, tab_x, tab_y,
+                                                              req_spectrum, req_z_mean, req_offset,
+                                                              sep, out, d_count, d_retry, ctx->d_err);
+        return cg_after_launch(ctx, "mp_retry_kernel");
+    };
+    std::vector<coffe_gpu_tuning_t> cands;
+    for (int lt : {64, 128, 256}) {
+        coffe_gpu_tuning_t c = ctx->tuning;
+        c.lane_threads = lt;
+        cands.push_back(c);
+    }
+    coffe_gpu_tuning_t tu;
+    long long bucket = 0;
+    while ((1ll << bucket) < total) ++bucket;
+    const std::array<long long, 6> key{2, a.n_l, contrib, bucket, 0, 0};
+    if ((st = cg_tuned(ctx, key, cands, run, &tu))) return st;
+    ctx->last_tuning.lane_threads = tu.lane_threads;
+    return run(tu);
 }
 
 template <typename T, typename S, typename TT>

@@ -272,6 +272,35 @@ int coffe_gpu_multipoles_noalloc(coffe_gpu_ctx_t *ctx, int contrib, int precisio
    No counterpart in the reference (its QAG keeps this count internal). */
 long long coffe_gpu_multipoles_retries(coffe_gpu_ctx_t *ctx);
 
+/* ------------------------------------------------------------------ tuning */
+
+/* No counterpart in the reference (FFTW plans its own transforms; the rest is
+   plain C): launch shapes of the GPU kernels.  A configuration is used by the
+   table stage of coffe_gpu_integrals_init (the per-spectrum spline pass and
+   the FFTLog transforms) and by the mixed-precision multipole kernel for unit
+   biases.  Every choice gives the same results except fft_radix, which changes
+   the rounding of the double-float transforms (by ~1e-14 relative). */
+typedef struct {
+    int fft_threads;  /* threads per block of the FFTLog transforms: 128, 256, 512 or 1024 */
+    int fft_radix;    /* 2 or 4: stages of the mixed-precision (double-float) transforms */
+    int fft_swizzle;  /* 0 or 1: XOR-swizzled shared-memory layout of those transforms */
+    int spline_group; /* 2, 4 or 8 spectra per block of the mixed-precision spline pass */
+    int lane_threads; /* 64, 128 or 256 threads per block of the mixed multipole kernel */
+} coffe_gpu_tuning_t;
+
+/* enable != 0 switches on benchmark mode: the first table build and the first
+   mixed multipole call of each shape (FFT size, spectra, terms and precision;
+   number of multipoles, contributions and batch size to the next power of
+   two) time every candidate configuration on the call's own inputs, keep the
+   fastest for that shape and finish with it; later calls of the shape reuse
+   it.  Calls made while the stream is being captured never time: they use the
+   shape's chosen configuration, else the default. */
+int coffe_gpu_set_autotune(coffe_gpu_ctx_t *ctx, int enable);
+/* the configuration the most recent table build and mixed multipole call used */
+int coffe_gpu_get_tuning(const coffe_gpu_ctx_t *ctx, coffe_gpu_tuning_t *out);
+/* sets the default configuration (validated) and forgets the chosen ones */
+int coffe_gpu_set_tuning(coffe_gpu_ctx_t *ctx, const coffe_gpu_tuning_t *t);
+
 /* ------------------------------------------------------------- derivatives */
 
 /* No counterpart in the reference (which has no derivatives): the den/rsd

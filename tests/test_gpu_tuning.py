@@ -1,0 +1,118 @@
+"""Launch-shape tuning: every configuration of the table stage and of the
+mixed multipole kernel gives the default configuration's results (bit for bit
+except the FFT radix, which changes the double-float rounding), and benchmark
+mode picks a configuration per shape and reuses it."""
+import numpy as np
+import pytest
+
+from conftest import H
+
+pytestmark = pytest.mark.gpu
+
+TERMS = [(0, 0), (0, 2), (0, 4)]
+
+
+@pytest.fixture(scope="module")
+def setup():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from coffe_gb300 import workloads
+    from coffe_gb300.api import Context
+
+    b = workloads.subset(workloads.cfg3(n_spectra=4), 4)
+    ctx = Context(0)
+    ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+    yield ctx, b
+    ctx.close()
+
+
+DEFAULT = dict(fft_threads=512, fft_radix=4, fft_swizzle=1, spline_group=8, lane_threads=128)
+
+
+def _tables(ctx, b, precision, **cfg):
+    ctx.set_tuning(**{**DEFAULT, **cfg})
+    ctx.integrals_init(b.k, b.pk, TERMS, N=4096, precision=precision, small_r=False)
+    return np.stack([ctx.integral_table(s, n, l)[1] for s in range(b.pk.shape[0])
+                     for n, l in TERMS])
+
+
+def _multipoles(ctx, b):
+    return ctx.multipoles(b.req_spectrum, b.req_z_mean, b.req_offset, b.sep, b.ls,
+                          precision="mixed")
+
+
+def test_table_configurations_agree(setup):
+    ctx, b = setup
+    ref = _tables(ctx, b, "mixed")
+    fin = np.isfinite(ref)
+    scale = np.abs(np.where(fin, ref, 0)).max(axis=1, keepdims=True)
+    for ft in (128, 256, 512):
+        for rad in (2, 4):
+            for sw in (0, 1):
+                for grp in (2, 4, 8):
+                    got = _tables(ctx, b, "mixed", fft_threads=ft, fft_radix=rad,
+                                  fft_swizzle=sw, spline_group=grp)
+                    assert np.array_equal(np.isfinite(got), fin)
+                    if rad == DEFAULT["fft_radix"]:
+                        assert np.array_equal(got[fin], ref[fin]), (ft, rad, sw, grp)
+                    else:
+                        # float tables from double-float transforms rounded differently
+                        e = np.max(np.abs(got - ref)[fin] / np.broadcast_to(scale, ref.shape)[fin])
+                        assert e < 1e-7, (ft, rad, sw, grp, e)
+    ref64 = _tables(ctx, b, "fp64")
+    for ft in (128, 256):
+        got = _tables(ctx, b, "fp64", fft_threads=ft)
+        assert np.array_equal(got, ref64, equal_nan=True), ft
+
+
+def test_lane_configurations_agree(setup):
+    ctx, b = setup
+    _tables(ctx, b, "mixed")
+    ref = _multipoles(ctx, b)
+    for lt in (64, 256):
+        ctx.set_tuning(**{**DEFAULT, "lane_threads": lt})
+        got = _multipoles(ctx, b)
+        assert ctx.tuning()["lane_threads"] == lt
+        assert np.array_equal(got, ref), lt
+
+
+def test_autotune_chooses_and_reuses(setup):
+    ctx, b = setup
+    _tables(ctx, b, "mixed")
+    ref = _multipoles(ctx, b)
+    ctx.set_tuning(**DEFAULT)  # forgets earlier choices
+    ctx.set_autotune(True)
+    try:
+        l0 = ctx.launch_count()
+        ctx.integrals_init(b.k, b.pk, TERMS, N=4096, precision="mixed", small_r=False)
+        got = _multipoles(ctx, b)
+        tuned = ctx.launch_count() - l0
+        cfg = ctx.tuning()
+        l0 = ctx.launch_count()
+        ctx.integrals_init(b.k, b.pk, TERMS, N=4096, precision="mixed", small_r=False)
+        again = _multipoles(ctx, b)
+        plain = ctx.launch_count() - l0
+    finally:
+        ctx.set_autotune(False)
+    print("chosen", cfg, "launches while tuning", tuned, "after", plain)
+    assert cfg["fft_threads"] in (128, 256, 512) and cfg["fft_radix"] in (2, 4)
+    assert cfg["spline_group"] in (2, 4, 8) and cfg["lane_threads"] in (64, 128, 256)
+    assert tuned > 10 * plain  # candidates were timed once, then reused
+    assert ctx.tuning() == cfg
+    assert np.array_equal(again, got)
+    floor = 1e-3 * np.abs(ref).max(axis=0, keepdims=True)
+    assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), floor)) < 1e-5
+
+
+def test_set_tuning_rejects_bad_values(setup):
+    from coffe_gb300.api import CoffeGpuError
+
+    ctx, _ = setup
+    for bad in (dict(fft_threads=384), dict(fft_radix=8), dict(fft_swizzle=2),
+                dict(spline_group=3), dict(lane_threads=32)):
+        with pytest.raises(CoffeGpuError):
+            ctx.set_tuning(**{**DEFAULT, **bad})
+    with pytest.raises(ValueError):
+        ctx.set_tuning(warp_size=32)
+    ctx.set_tuning(**DEFAULT)
