@@ -86,6 +86,7 @@ class Tuning(C.Structure):
         ("fft_swizzle", C.c_int),
         ("spline_group", C.c_int),
         ("lane_threads", C.c_int),
+        ("lane_unroll", C.c_int),
     ]
 
 

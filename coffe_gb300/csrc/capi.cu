@@ -304,9 +304,10 @@ int coffe_gpu_set_tuning(coffe_gpu_ctx_t *ctx, const coffe_gpu_tuning_t *t)
     const int ft = t->fft_threads, lt = t->lane_threads, g = t->spline_group;
     if (!(ft == 128 || ft == 256 || ft == 512 || ft == 1024) ||
         !(t->fft_radix == 2 || t->fft_radix == 4) || !(t->fft_swizzle == 0 || t->fft_swizzle == 1) ||
-        !(g == 2 || g == 4 || g == 8) || !(lt == 64 || lt == 128 || lt == 256)) {
+        !(g == 2 || g == 4 || g == 8) || !(lt == 64 || lt == 128 || lt == 256) ||
+        !(t->lane_unroll == 1 || t->lane_unroll == 2)) {
         cg_set_error(ctx, "set_tuning: fft_threads 128/256/512/1024, fft_radix 2/4, fft_swizzle "
-                          "0/1, spline_group 2/4/8, lane_threads 64/128/256");
+                          "0/1, spline_group 2/4/8, lane_threads 64/128/256, lane_unroll 1/2");
         return COFFE_GPU_EINVAL;
     }
     ctx->tuning = *t;

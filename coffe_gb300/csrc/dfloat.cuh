@@ -100,10 +100,35 @@ __device__ __forceinline__ dfc dfc_load(const float4 v) { return dfc{{v.x, v.y},
 __device__ __forceinline__ float4 dfc_pack(dfc a) { return make_float4(a.re.hi, a.re.lo, a.im.hi, a.im.lo); }
 __device__ __forceinline__ dfc dfc_add(dfc a, dfc b) { return dfc{df_add(a.re, b.re), df_add(a.im, b.im)}; }
 __device__ __forceinline__ dfc dfc_sub(dfc a, dfc b) { return dfc{df_sub(a.re, b.re), df_sub(a.im, b.im)}; }
+// Unnormalised intermediates for chains that end in a normalising df_add:
+// the product x y as p + e with p = fl(x.hi y.hi) and e its error plus the
+// cross terms (|e| may exceed ulp(p)/2), and the sum x + y as the exact
+// two-sum of the high parts with the low parts added to its error.
+__device__ __forceinline__ dfl df_mul_raw(dfl x, dfl y)
+{
+    const float p = x.hi * y.hi;
+    const float e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, fmaf(x.hi, y.hi, -p)));
+    return dfl{p, e};
+}
+__device__ __forceinline__ dfl df_add_raw(dfl x, dfl y)
+{
+    const dfl s = df_two_sum(x.hi, y.hi);
+    return dfl{s.hi, s.lo + (x.lo + y.lo)};
+}
+__device__ __forceinline__ dfc dfc_add_raw(dfc a, dfc b)
+{
+    return dfc{df_add_raw(a.re, b.re), df_add_raw(a.im, b.im)};
+}
+__device__ __forceinline__ dfc dfc_sub_raw(dfc a, dfc b)
+{
+    return dfc{df_add_raw(a.re, df_neg(b.re)), df_add_raw(a.im, df_neg(b.im))};
+}
+
+// complex product: each component one normalising sum of two raw products
 __device__ __forceinline__ dfc dfc_mul(dfc a, dfc b)
 {
-    return dfc{df_sub(df_mul(a.re, b.re), df_mul(a.im, b.im)),
-               df_add(df_mul(a.re, b.im), df_mul(a.im, b.re))};
+    return dfc{df_add(df_mul_raw(a.re, b.re), df_neg(df_mul_raw(a.im, b.im))),
+               df_add(df_mul_raw(a.re, b.im), df_mul_raw(a.im, b.re))};
 }
 __device__ __forceinline__ dfc dfc_conj(dfc a) { return dfc{a.re, df_neg(a.im)}; }
 __device__ __forceinline__ dfc dfc_neg(dfc a) { return dfc{df_neg(a.re), df_neg(a.im)}; }

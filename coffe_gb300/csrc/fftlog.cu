@@ -619,8 +619,9 @@ __device__ void smem_fft_df(float4 *buf, int logM, const float4 *__restrict__ tw
                 x2 = dfc_mul(x2, w2);
                 x3 = dfc_mul(x3, w3);
             }
-            const dfc t0 = dfc_add(x0, x1), t1 = dfc_sub(x0, x1);
-            const dfc t2 = dfc_add(x2, x3), t3 = dfc_sub(x2, x3);
+            // t0..t3 stay unnormalised: each feeds only the normalising sums below
+            const dfc t0 = dfc_add_raw(x0, x1), t1 = dfc_sub_raw(x0, x1);
+            const dfc t2 = dfc_add_raw(x2, x3), t3 = dfc_sub_raw(x2, x3);
             // w_{4 half}^half = -i forward, +i backward
             const dfc r = sign < 0 ? dfc{t3.im, df_neg(t3.re)} : dfc{df_neg(t3.im), t3.re};
             buf[p0] = dfc_pack(dfc_add(t0, t2));

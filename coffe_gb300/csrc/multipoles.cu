@@ -324,7 +324,7 @@ template <typename T, typename S> struct MpIntegrand {
 // Akima lookup of an I_l^n table: knots tab_x (r = 0, 42 sub-Mpc points, then
 // r0 (kmax/kmin)^(i/N)), values y; the interval is found as a binary search
 // would (an O(1) guess on the log grid, then a local correction).
-template <typename T>
+template <typename T, bool FAST = false>
 __device__ __forceinline__ T table_lookup(const T *__restrict__ x, const T *__restrict__ y, int n,
                                           T inv_dlog, T r)
 {
@@ -348,7 +348,7 @@ __device__ __forceinline__ T table_lookup(const T *__restrict__ x, const T *__re
         }
         i = lo;
     }
-    return akima_eval_at<T>(x, y, n, i, r);
+    return akima_eval_at<T, FAST>(x, y, n, i, r);
 }
 
 struct MpArgs {
@@ -657,7 +657,7 @@ template <int NL> struct FastLayout {
 };
 
 #define MP_FAST_MAX_THREADS 256
-template <int NL, int CONTRIB>
+template <int NL, int CONTRIB, int UNROLL>
 __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
     mp_fast_kernel(MpArgs a, ChiTab ct, float chi_lo, float chi_hi, Spl32 chi_of_z,
                    const float *__restrict__ tab_x, const float *__restrict__ tab_y,
@@ -681,9 +681,10 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
     const float chim = spl_eval(chi_of_z, (float)req_z_mean[q]);
     const float *y0 = tab_y + ((size_t)s * a.n_terms) * a.tab_len;
     const float idl = (float)a.inv_dlog;
-    const float I00 = table_lookup<float>(tab_x, y0 + (size_t)a.t00 * a.tab_len, a.tab_len, idl, r);
-    const float I02 = table_lookup<float>(tab_x, y0 + (size_t)a.t02 * a.tab_len, a.tab_len, idl, r);
-    const float I04 = table_lookup<float>(tab_x, y0 + (size_t)a.t04 * a.tab_len, a.tab_len, idl, r);
+    const int tl = a.tab_len;
+    const float I00 = table_lookup<float, true>(tab_x, y0 + (size_t)a.t00 * tl, tl, idl, r);
+    const float I02 = table_lookup<float, true>(tab_x, y0 + (size_t)a.t02 * tl, tl, idl, r);
+    const float I04 = table_lookup<float, true>(tab_x, y0 + (size_t)a.t04 * tl, tl, idl, r);
     const int bd = blockDim.x, tid = threadIdx.x;
     float K[NL], Kc[NL], G[NL], A[NL];
 #pragma unroll
@@ -697,7 +698,7 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
         const float e00 = I00 * (1.f / 15.f), e02 = I02 * (1.f / 21.f), e04 = I04 * (1.f / 35.f);
         const float e00x2 = 2.f * e00, e0d = e00 - e02;
         const float K1 = (I00 - 2.f * I02) * (1.f / 3.f);
-#pragma unroll 1
+#pragma unroll UNROLL
         for (int k = 0; k < LY::ROWS; ++k) {
             float rec[LY::R1];
             lds_rec<LY::R1>(tab1 + k * LY::R1, rec);
@@ -868,16 +869,23 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<float, Spl32> &bg,
         const int lt = tu.lane_threads;
         const long long blocks = (total + lt - 1) / lt;
         CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
-#define MP_FAST(NLV, CV)                                                                          \
-    if (a.n_l == NLV && contrib == CV) {                                                          \
+#define MP_FAST_U(NLV, CV, UV)                                                                    \
+    {                                                                                             \
         const size_t smem = sizeof(float) * (FastLayout<NLV>::COUNT + FastLayout<NLV>::ROWS * lt); \
-        CG_CUDA(ctx, cudaFuncSetAttribute(mp_fast_kernel<NLV, CV>,                                \
+        CG_CUDA(ctx, cudaFuncSetAttribute(mp_fast_kernel<NLV, CV, UV>,                            \
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,            \
                                           (int)smem));                                            \
-        mp_fast_kernel<NLV, CV><<<(unsigned)blocks, lt, smem, ctx->stream>>>(                     \
+        mp_fast_kernel<NLV, CV, UV><<<(unsigned)blocks, lt, smem, ctx->stream>>>(                 \
             a, ct, bg.z_of_chi.x0, bg.z_of_chi.xn, chi_of_z, tab_x, tab_y, req_spectrum,          \
             req_z_mean, req_offset, sep, total, (const float *)dn, out, d_count, d_retry,         \
             ctx->d_err);                                                                          \
+    }
+#define MP_FAST(NLV, CV)                                                                          \
+    if (a.n_l == NLV && contrib == CV) {                                                          \
+        if (tu.lane_unroll == 2)                                                                  \
+            MP_FAST_U(NLV, CV, 2)                                                                 \
+        else                                                                                      \
+            MP_FAST_U(NLV, CV, 1)                                                                 \
     }
 #define MP_FAST_NL(NLV) MP_FAST(NLV, 1) MP_FAST(NLV, 2) MP_FAST(NLV, 3)
         MP_FAST_NL(1)
@@ -886,6 +894,7 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<float, Spl32> &bg,
         MP_FAST_NL(4)
 #undef MP_FAST_NL
 #undef MP_FAST
+#undef MP_FAST_U
         int s2 = cg_after_launch(ctx, "mp_fast_kernel");
         if (s2) return s2;
         mp_retry_kernel<float, Spl32, float><<<ctx->sm_count * 2, 32 * MP_RETRY_WARPS, 0,
@@ -895,17 +904,20 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<float, Spl32> &bg,
         return cg_after_launch(ctx, "mp_retry_kernel");
     };
     std::vector<coffe_gpu_tuning_t> cands;
-    for (int lt : {64, 128, 256}) {
-        coffe_gpu_tuning_t c = ctx->tuning;
-        c.lane_threads = lt;
-        cands.push_back(c);
-    }
+    for (int lt : {64, 128, 256})
+        for (int un : {1, 2}) {
+            coffe_gpu_tuning_t c = ctx->tuning;
+            c.lane_threads = lt;
+            c.lane_unroll = un;
+            cands.push_back(c);
+        }
     coffe_gpu_tuning_t tu;
     long long bucket = 0;
     while ((1ll << bucket) < total) ++bucket;
     const std::array<long long, 6> key{2, a.n_l, contrib, bucket, 0, 0};
     if ((st = cg_tuned(ctx, key, cands, run, &tu))) return st;
     ctx->last_tuning.lane_threads = tu.lane_threads;
+    ctx->last_tuning.lane_unroll = tu.lane_unroll;
     return run(tu);
 }
 

@@ -68,21 +68,29 @@ __device__ __forceinline__ typename SplTraits<S>::T spl_eval(const S &s, typenam
 // gsl_interp_akima.  Used both to build coefficient records and to evaluate
 // tables on the fly (the I_l^n tables are evaluated a few times per output,
 // so their records are never stored).
-template <typename T>
+// a / b: IEEE division, or (FAST, float) the approximate __fdividef (2 ulp;
+// positive knot spacings and |b| < 2^126 here)
+template <typename T, bool FAST> __device__ __forceinline__ T akima_div(T a, T b) { return a / b; }
+template <> __device__ __forceinline__ float akima_div<float, true>(float a, float b)
+{
+    return __fdividef(a, b);
+}
+
+template <typename T, bool FAST = false>
 __device__ __forceinline__ T akima_secant(const T *x, const T *y, int n, int k)
 {
-    if (k >= 0 && k <= n - 2) return (y[k + 1] - y[k]) / (x[k + 1] - x[k]);
-    const T m0 = (y[1] - y[0]) / (x[1] - x[0]);
-    const T m1 = (y[2] - y[1]) / (x[2] - x[1]);
-    const T ma = (y[n - 1] - y[n - 2]) / (x[n - 1] - x[n - 2]);
-    const T mb = (y[n - 2] - y[n - 3]) / (x[n - 2] - x[n - 3]);
+    if (k >= 0 && k <= n - 2) return akima_div<T, FAST>(y[k + 1] - y[k], x[k + 1] - x[k]);
+    const T m0 = akima_div<T, FAST>(y[1] - y[0], x[1] - x[0]);
+    const T m1 = akima_div<T, FAST>(y[2] - y[1], x[2] - x[1]);
+    const T ma = akima_div<T, FAST>(y[n - 1] - y[n - 2], x[n - 1] - x[n - 2]);
+    const T mb = akima_div<T, FAST>(y[n - 2] - y[n - 3], x[n - 2] - x[n - 3]);
     if (k == -1) return T(2) * m0 - m1;
     if (k == -2) return T(3) * m0 - T(2) * m1;
     if (k == n - 1) return T(2) * ma - mb;
     return T(3) * ma - T(2) * mb; // k == n
 }
 
-template <typename T>
+template <typename T, bool FAST = false>
 __device__ __forceinline__ T akima_node_slope(T mm2, T mm1, T m0, T mp1)
 {
     // slope at knot i from m_{i-2}, m_{i-1}, m_i, m_{i+1}
@@ -90,33 +98,33 @@ __device__ __forceinline__ T akima_node_slope(T mm2, T mm1, T m0, T mp1)
     const T w2 = fabs(mm1 - mm2);
     const T ne = w1 + w2;
     if (ne == T(0)) return T(0.5) * (mm1 + m0);
-    return (w1 * mm1 + w2 * m0) / ne;
+    return akima_div<T, FAST>(w1 * mm1 + w2 * m0, ne);
 }
 
 // Coefficients (b, c, d) of interval i, 0 <= i <= n-2.
-template <typename T>
+template <typename T, bool FAST = false>
 __device__ __forceinline__ void akima_interval(const T *x, const T *y, int n, int i, T &b, T &c,
                                                T &d)
 {
-    const T mm2 = akima_secant(x, y, n, i - 2);
-    const T mm1 = akima_secant(x, y, n, i - 1);
-    const T m0 = akima_secant(x, y, n, i);
-    const T mp1 = akima_secant(x, y, n, i + 1);
-    const T mp2 = akima_secant(x, y, n, i + 2);
-    const T t0 = akima_node_slope(mm2, mm1, m0, mp1);
-    const T t1 = akima_node_slope(mm1, m0, mp1, mp2);
+    const T mm2 = akima_secant<T, FAST>(x, y, n, i - 2);
+    const T mm1 = akima_secant<T, FAST>(x, y, n, i - 1);
+    const T m0 = akima_secant<T, FAST>(x, y, n, i);
+    const T mp1 = akima_secant<T, FAST>(x, y, n, i + 1);
+    const T mp2 = akima_secant<T, FAST>(x, y, n, i + 2);
+    const T t0 = akima_node_slope<T, FAST>(mm2, mm1, m0, mp1);
+    const T t1 = akima_node_slope<T, FAST>(mm1, m0, mp1, mp2);
     const T h = x[i + 1] - x[i];
     b = t0;
-    c = (T(3) * m0 - T(2) * t0 - t1) / h;
-    d = (t0 + t1 - T(2) * m0) / (h * h);
+    c = akima_div<T, FAST>(T(3) * m0 - T(2) * t0 - t1, h);
+    d = akima_div<T, FAST>(t0 + t1 - T(2) * m0, h * h);
 }
 
 // Akima evaluation straight from knots (x, y), interval found by the caller.
-template <typename T>
+template <typename T, bool FAST = false>
 __device__ __forceinline__ T akima_eval_at(const T *x, const T *y, int n, int i, T v)
 {
     T b, c, d;
-    akima_interval(x, y, n, i, b, c, d);
+    akima_interval<T, FAST>(x, y, n, i, b, c, d);
     const T dx = v - x[i];
     return y[i] + dx * (b + dx * (c + d * dx));
 }

@@ -286,6 +286,7 @@ typedef struct {
     int fft_swizzle;  /* 0 or 1: XOR-swizzled shared-memory layout of those transforms */
     int spline_group; /* 2, 4 or 8 spectra per block of the mixed-precision spline pass */
     int lane_threads; /* 64, 128 or 256 threads per block of the mixed multipole kernel */
+    int lane_unroll;  /* 1 or 2 quadrature nodes per step of that kernel's node loop */
 } coffe_gpu_tuning_t;
 
 /* enable != 0 switches on benchmark mode: the first table build and the first

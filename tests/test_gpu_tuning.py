@@ -1,7 +1,8 @@
 """Launch-shape tuning: every configuration of the table stage and of the
 mixed multipole kernel gives the default configuration's results (bit for bit
-except the FFT radix, which changes the double-float rounding), and benchmark
-mode picks a configuration per shape and reuses it."""
+except the FFT radix, which changes the double-float rounding, and the node-loop
+unrolling, which may contract a multiply-add differently), and benchmark mode
+picks a configuration per shape and reuses it."""
 import numpy as np
 import pytest
 
@@ -27,7 +28,8 @@ def setup():
     ctx.close()
 
 
-DEFAULT = dict(fft_threads=512, fft_radix=4, fft_swizzle=1, spline_group=8, lane_threads=128)
+DEFAULT = dict(fft_threads=512, fft_radix=4, fft_swizzle=0, spline_group=8, lane_threads=256,
+               lane_unroll=1)
 
 
 def _tables(ctx, b, precision, **cfg):
@@ -70,11 +72,19 @@ def test_lane_configurations_agree(setup):
     ctx, b = setup
     _tables(ctx, b, "mixed")
     ref = _multipoles(ctx, b)
-    for lt in (64, 256):
-        ctx.set_tuning(**{**DEFAULT, "lane_threads": lt})
-        got = _multipoles(ctx, b)
-        assert ctx.tuning()["lane_threads"] == lt
-        assert np.array_equal(got, ref), lt
+    floor = 1e-3 * np.abs(ref).max(axis=0, keepdims=True)
+    first = {}
+    for un in (1, 2):
+        for lt in (64, 128, 256):
+            ctx.set_tuning(**{**DEFAULT, "lane_threads": lt, "lane_unroll": un})
+            got = _multipoles(ctx, b)
+            assert ctx.tuning()["lane_threads"] == lt and ctx.tuning()["lane_unroll"] == un
+            # the block size never changes a result; the unrolled node loop may
+            # contract a multiply-add differently (float rounding)
+            first.setdefault(un, got)
+            assert np.array_equal(got, first[un]), (lt, un)
+            assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), floor)) < 1e-6, (lt, un)
+    assert np.array_equal(first[1], ref)
 
 
 def test_autotune_chooses_and_reuses(setup):
@@ -98,6 +108,7 @@ def test_autotune_chooses_and_reuses(setup):
     print("chosen", cfg, "launches while tuning", tuned, "after", plain)
     assert cfg["fft_threads"] in (128, 256, 512) and cfg["fft_radix"] in (2, 4)
     assert cfg["spline_group"] in (2, 4, 8) and cfg["lane_threads"] in (64, 128, 256)
+    assert cfg["lane_unroll"] in (1, 2)
     assert tuned > 10 * plain  # candidates were timed once, then reused
     assert ctx.tuning() == cfg
     assert np.array_equal(again, got)
@@ -110,7 +121,7 @@ def test_set_tuning_rejects_bad_values(setup):
 
     ctx, _ = setup
     for bad in (dict(fft_threads=384), dict(fft_radix=8), dict(fft_swizzle=2),
-                dict(spline_group=3), dict(lane_threads=32)):
+                dict(spline_group=3), dict(lane_threads=32), dict(lane_unroll=4)):
         with pytest.raises(CoffeGpuError):
             ctx.set_tuning(**{**DEFAULT, **bad})
     with pytest.raises(ValueError):
