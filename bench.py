@@ -75,6 +75,10 @@ def parse():
     p.add_argument("--no-clocks", action="store_true")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the default launch configuration instead of timing candidates")
+    p.add_argument("--launch-config", default=None,
+                   help="fixed launch configuration instead of autotuning, e.g. "
+                        "fft_threads=512,fft_radix=4,fft_swizzle=1,spline_group=8,"
+                        "lane_threads=128,lane_unroll=2 (for profiling runs)")
     p.add_argument("--kernel-only", choices=["mixed", "fp64", "tables-mixed", "tables-fp64"],
                    default=None,
                    help="profiling aid: run only the multipole kernel (mixed/fp64) or only the "
@@ -356,7 +360,10 @@ def ours(args, rank, world, local_rank):
     # launch shapes: the first build and multipole call of each shape time the
     # candidate configurations (benchmark mode), later calls and the captured
     # graph reuse the choice
-    if not args.no_autotune and not args.kernel_only:
+    if args.launch_config:
+        ctx.set_tuning(**{k: int(v) for k, v in
+                          (kv.split("=") for kv in args.launch_config.split(","))})
+    elif not args.no_autotune and not args.kernel_only:
         ctx.set_autotune(True)
     # build the per-grid tables once (synchronous), then warm up
     for prec in ("mixed", "fp64"):
@@ -532,7 +539,8 @@ def ours(args, rank, world, local_rank):
                    "separations": n_sep, "evals_per_step": n_evals,
                    "l2": "flushed between timed steps (256 MiB write outside the events)",
                    "cuda_graph": bool(graphs), "graph_output_equals_direct": graph_equal,
-                   "launch_config": tuning, "autotuned": not args.no_autotune,
+                   "launch_config": tuning,
+                   "autotuned": not (args.no_autotune or args.launch_config),
                    "parallelism": f"replicas x{world}"},
         "fp64": {"value": fp64_value, "unit": UNIT, "steps": k64,
                  "ms_per_step": 1e3 * dev_fp64 / k64},

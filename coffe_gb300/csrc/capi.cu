@@ -435,11 +435,6 @@ int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, doubl
     }
     const int64_t total = req_offset[n_req];
     if (total > 0 && (!sep || !out)) return COFFE_GPU_EINVAL;
-    for (int64_t i = 0; i < total; ++i)
-        if (!(sep[i] > 0)) {
-            cg_set_error(ctx, "multipoles: separations must be positive");
-            return COFFE_GPU_EINVAL;
-        }
     const size_t b_spec = sizeof(int) * n_req, b_z = sizeof(double) * n_req,
                  b_off = sizeof(int64_t) * (n_req + 1), b_sep = sizeof(double) * total,
                  b_out = sizeof(double) * total * n_l;
@@ -463,7 +458,17 @@ int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, doubl
     if (st) return st;
     if (total > 0)
         CG_CUDA(ctx, cudaMemcpyAsync(out, d_out, b_out, cudaMemcpyDeviceToHost, ctx->stream));
-    return cg_check_device_errors(ctx, "multipoles");
+    // the separations are checked on the host while the device works (a
+    // non-positive one cannot make a kernel read out of bounds: its lookups
+    // give NaN); a branch-free scan vectorises
+    unsigned char ok = 1;
+    for (int64_t i = 0; i < total; ++i) ok &= (unsigned char)(sep[i] > 0);
+    st = cg_check_device_errors(ctx, "multipoles"); // also clears the device flags
+    if (st != COFFE_GPU_ECUDA && !ok) {
+        cg_set_error(ctx, "multipoles: separations must be positive");
+        return COFFE_GPU_EINVAL;
+    }
+    return st;
 }
 
 int coffe_gpu_multipoles_scaled(coffe_gpu_ctx_t *ctx, int contrib, int n_req, int64_t n_sep,

@@ -91,6 +91,29 @@ __device__ __forceinline__ dfl df_from_double_bits(double d)
     return dfl{__int_as_float((int)(hi | sign)), __int_as_float(__float_as_int(lo) ^ (int)sign)};
 }
 
+// float of a double (the high part above) and the exact double of a float,
+// both with integer operations only
+__device__ __forceinline__ float f32_of_bits(double d) { return df_from_double_bits(d).hi; }
+__device__ __forceinline__ double f64_of_bits(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    unsigned long long bits;
+    if (e == 0xffu) // infinity / NaN
+        bits = sign | (0x7ffull << 52) | ((unsigned long long)m << 29);
+    else if (e != 0u) // normal
+        bits = sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+    else if (m == 0u) // zero
+        bits = sign;
+    else { // subnormal: m 2^-149 with the leading one of m at bit p
+        const int p = 31 - __clz((int)m);
+        bits = sign | ((unsigned long long)(p - 149 + 1023) << 52) |
+               ((unsigned long long)(m ^ (1u << p)) << (52 - p));
+    }
+    return __longlong_as_double((long long)bits);
+}
+
 // complex double-float, stored as float4 (re.hi, re.lo, im.hi, im.lo)
 struct dfc {
     dfl re, im;

@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "ctx.cuh"
+#include "dfloat.cuh"
 #include "qag.cuh"
 
 namespace {
@@ -489,8 +490,11 @@ template <int R> __device__ __forceinline__ void lds_rec(const double *p, double
 // First-panel results of one separation: QUADPACK's acceptance test of the
 // 61-point panel (gsl qag.c) per multipole; accepted values are written,
 // the others queued for the adaptive continuation.
+__device__ __forceinline__ double to_f64(double x) { return x; }
+__device__ __forceinline__ double to_f64(float x) { return f64_of_bits(x); }
+
 template <int NL, typename T>
-__device__ __forceinline__ void first_panel_out(const MpArgs &a, long long item, bool finite,
+__device__ __forceinline__ void first_panel_out(const MpArgs &a, T epsrel, long long item, bool finite,
                                                 const T (&K)[NL], const T (&G)[NL],
                                                 const T (&A)[NL], const T (&asc)[NL],
                                                 double *__restrict__ out,
@@ -505,7 +509,7 @@ __device__ __forceinline__ void first_panel_out(const MpArgs &a, long long item,
         o.resabs = A[j] * T(0.5);
         o.resasc = asc[j] * T(0.5);
         o.abserr = qk_rescale_error((K[j] - G[j]) * T(0.5), o.resabs, o.resasc);
-        const T tolerance = (T)a.epsrel * fabs(o.result);
+        const T tolerance = epsrel * fabs(o.result);
         const T round_off = T(50) * qk_eps<T>() * o.resabs;
         const bool roundoff_fail = o.abserr <= round_off && o.abserr > tolerance;
         const bool ok = (o.abserr <= tolerance && o.abserr != o.resasc) || o.abserr == T(0);
@@ -513,7 +517,7 @@ __device__ __forceinline__ void first_panel_out(const MpArgs &a, long long item,
             cg_flag(err, CG_ERR_NONFINITE);
             out[item * NL + j] = cg_nan<double>();
         } else if (ok || roundoff_fail) {
-            const double res = (double)(T(2 * l + 1) * o.result);
+            const double res = to_f64(T(2 * l + 1) * o.result);
             if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
             out[item * NL + j] = res;
         } else {
@@ -606,7 +610,7 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
             for (int j = 0; j < NL; ++j) asc[j] += rec[0] * fabs(v * rec[1 + j] - K[j] * T(0.5));
         }
     }
-    first_panel_out<NL, T>(a, item, finite, K, G, A, asc, out, retry_count, retry, err);
+    first_panel_out<NL, T>(a, (T)a.epsrel, item, finite, K, G, A, asc, out, retry_count, retry, err);
 }
 
 // ------------------------------------------- mixed path, equal unit biases
@@ -677,10 +681,11 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
     if (item >= total) return;
     const int q = find_request(req_offset, a.n_req, item);
     const int s = req_spectrum[q];
-    const float r = (float)sep[item];
-    const float chim = spl_eval(chi_of_z, (float)req_z_mean[q]);
+    // double -> float without the FP64 pipe (1/64 of the FP32 rate)
+    const float r = f32_of_bits(sep[item]);
+    const float chim = spl_eval(chi_of_z, f32_of_bits(req_z_mean[q]));
     const float *y0 = tab_y + ((size_t)s * a.n_terms) * a.tab_len;
-    const float idl = (float)a.inv_dlog;
+    const float idl = f32_of_bits(a.inv_dlog);
     const int tl = a.tab_len;
     const float I00 = table_lookup<float, true>(tab_x, y0 + (size_t)a.t00 * tl, tl, idl, r);
     const float I02 = table_lookup<float, true>(tab_x, y0 + (size_t)a.t02 * tl, tl, idl, r);
@@ -751,7 +756,8 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
             for (int j = 0; j < NL; ++j) asc[j] = fmaf(rec[0], fabsf(fmaf(v, rec[1 + j], -0.5f * K[j])), asc[j]);
         }
     }
-    first_panel_out<NL, float>(a, item, finite, K, G, A, asc, out, retry_count, retry, err);
+    first_panel_out<NL, float>(a, f32_of_bits(a.epsrel), item, finite, K, G, A, asc, out,
+                               retry_count, retry, err);
 }
 
 __global__ void chitab_kernel(Spl64 z_of_chi, Spl64 D1, Spl64 f, double lo, double hi, int cells,

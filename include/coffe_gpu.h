@@ -193,7 +193,9 @@ int coffe_gpu_integral_eval(coffe_gpu_ctx_t *ctx, int spectrum, int term, const 
    single-integrated lensing terms stay FP64: their RSD-lensing coefficients
    cancel terms of size chi^5).
    All arrays are host pointers unless arrays_on_device != 0, in which case
-   every array (including out) is a device pointer. */
+   every array (including out) is a device pointer.  With host arrays a
+   non-positive separation returns COFFE_GPU_EINVAL after the work has run
+   (the check overlaps it), so `out` is then unspecified. */
 int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, double epsrel,
                          int n_req, const int *req_spectrum, const double *req_z_mean,
                          const int64_t *req_offset, const double *sep, int n_l,

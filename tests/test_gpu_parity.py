@@ -416,4 +416,9 @@ def test_error_statuses(w, cfg1):
         with pytest.raises(CoffeGpuError) as e:  # precision mismatch with the tables
             ctx.multipoles([0], [1.0], [0, 1], [10.0], precision="mixed")
         assert e.value.status == -1
+        with pytest.raises(CoffeGpuError) as e:  # non-positive separation
+            ctx.multipoles([0], [1.0], [0, 3], [10.0, -5.0, 20.0])
+        assert e.value.status == -1 and "positive" in str(e.value)
+        ok = ctx.multipoles([0], [1.0], [0, 2], [10.0, 20.0])  # the context stays usable
+        assert np.isfinite(ok).all()
         assert ctx.launch_count() > 0
