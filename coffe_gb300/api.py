@@ -240,6 +240,24 @@ class Context:
                                                  _dptr(out), 0), "multipoles")
         return out[: len(sp)]
 
+    def corrfunc(self, req_spectrum, req_z_mean, req_offset, sep, mu,
+                 contrib=_lib.DEN | _lib.RSD, precision="fp64") -> np.ndarray:
+        """Correlation function at every (separation, mu) of the batched requests;
+        returns an array of shape (len(sep), len(mu)) (corrfunc.c:55-141)."""
+        rs = np.ascontiguousarray(req_spectrum, dtype=np.int32)
+        rz = _f64(req_z_mean)
+        ro = np.ascontiguousarray(req_offset, dtype=np.int64)
+        sp = _f64(sep)
+        mu = _f64(np.atleast_1d(mu))
+        if len(ro) != len(rs) + 1 or len(rz) != len(rs):
+            raise ValueError("req_offset needs len(req_spectrum) + 1 entries")
+        out = np.zeros((max(len(sp), 1), len(mu)))
+        self._check(self._L.coffe_gpu_corrfunc(self._ctx, int(contrib), _precision(precision),
+                                               len(rs), _iptr(rs), _dptr(rz), _lptr(ro),
+                                               _dptr(sp), len(mu), _dptr(mu), _dptr(out), 0),
+                    "corrfunc")
+        return out[: len(sp)]
+
     def integrals_init_device(self, k, pk_dev, terms=DEN_RSD_TERMS, N: int = 4096,
                               precision="fp64", small_r: bool = False, sync: bool = True):
         """Like :meth:`integrals_init` with P(k) already on the device (a CUDA
@@ -377,6 +395,19 @@ class Multipoles:
         return {"z": self.z, "r": self.r, "l": self.l, "value": self.value}
 
 
+@dataclass
+class Corrfunc:
+    """One correlation-function value (python/coffe/representation.py's Corrfunc record)."""
+
+    z: float
+    r: float
+    mu: float
+    value: float
+
+    def to_dict(self):
+        return {"z": self.z, "r": self.r, "mu": self.mu, "value": self.value}
+
+
 def _check_parameter(name, value, kind, lo, hi):
     """Range/type check with the reference's semantics (coffe.pyx:86-110)."""
     if not isinstance(value, kind) or isinstance(value, bool) and kind is not bool:
@@ -393,7 +424,8 @@ class Coffe:
     """
 
     def __init__(self, *, omega_m=0.3, omega_baryon=0.05, omega_gamma=9e-5, h=0.67,
-                 sep=None, l=(0, 2, 4), z_mean=(1.0,), has_density=True, has_rsd=False,
+                 sep=None, l=(0, 2, 4), mu=(0.5,), z_mean=(1.0,), has_density=True,
+                 has_rsd=False, has_lensing=False,
                  integrals_fftlog_sampling=4096, background_bins=10000,
                  integration_1d_prec=1e-5, precision="fp64", device=0):
         self._ctx = Context(device)
@@ -404,9 +436,12 @@ class Coffe:
         # default separations of coffe_parse_default_parameters (parser.c:836-838)
         self.sep = np.linspace(5, 305, 100, endpoint=False) if sep is None else np.asarray(sep, float)
         self.l = list(l)
+        # default mu of coffe_parse_default_parameters (parser.c:980-982)
+        self.mu = [float(m) for m in mu]
         self.z_mean = list(z_mean)
         self.has_density = bool(has_density)
         self.has_rsd = bool(has_rsd)
+        self.has_lensing = bool(has_lensing)
         self.integrals_fftlog_sampling = int(integrals_fftlog_sampling)
         self.background_bins = int(background_bins)
         self.integration_1d_prec = float(integration_1d_prec)
@@ -467,9 +502,10 @@ class Coffe:
 
     @property
     def _contrib(self) -> int:
-        c = (_lib.DEN if self.has_density else 0) | (_lib.RSD if self.has_rsd else 0)
+        c = ((_lib.DEN if self.has_density else 0) | (_lib.RSD if self.has_rsd else 0) |
+             (_lib.LEN if self.has_lensing else 0))
         if c == 0:
-            raise ValueError("no contributions selected (has_density / has_rsd)")
+            raise ValueError("no contributions selected (has_density / has_rsd / has_lensing)")
         return c
 
     # --------------------------------------------------------------- outputs
@@ -505,6 +541,32 @@ class Coffe:
             for il, ll in enumerate(self.l):
                 for js, r in enumerate(self.sep):
                     res.append(Multipoles(z=zm, r=float(r), l=ll, value=float(vals[iz * ns + js, il])))
+        return res
+
+    def compute_corrfunc(self, *, z: float, r: float, mu: float) -> float:
+        """The correlation function at (z_mean, r, mu) (coffe.pyx:3159-3240)."""
+        _check_parameter("z", z, (int, float), 0, 15)
+        _check_parameter("r", r, (int, float), 0, 1500)
+        _check_parameter("mu", mu, (int, float), -1, 1)
+        self._ensure()
+        out = self._ctx.corrfunc([0], [float(z)], [0, 1], [float(r)], [float(mu)], self._contrib,
+                                 self.precision)
+        return float(out[0, 0])
+
+    def compute_corrfunc_bulk(self) -> List[Corrfunc]:
+        """All (z_mean, mu, sep) points in the reference's order: z outer, mu,
+        then separation (corrfunc.c:78-86)."""
+        self._ensure()
+        nz, ns = len(self.z_mean), len(self.sep)
+        offs = np.arange(nz + 1, dtype=np.int64) * ns
+        sep = np.tile(self.sep, nz)
+        vals = self._ctx.corrfunc(np.zeros(nz, np.int32), self.z_mean, offs, sep, self.mu,
+                                  self._contrib, self.precision)
+        res = []
+        for iz, zm in enumerate(self.z_mean):
+            for im, m in enumerate(self.mu):
+                for js, r in enumerate(self.sep):
+                    res.append(Corrfunc(z=zm, r=float(r), mu=m, value=float(vals[iz * ns + js, im])))
         return res
 
     def close(self):

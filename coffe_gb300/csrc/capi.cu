@@ -147,7 +147,8 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
                       &ctx->samp_f32, &ctx->csfac32,
                       &ctx->lens_rule, &ctx->lens_rec, &ctx->lens_part,
                       &ctx->cov_buf,  &ctx->cov_out, &ctx->adj_buf, &ctx->csband,
-                      &ctx->samp_tdf, &ctx->qfac_df, &ctx->pk_df, &ctx->chitab32};
+                      &ctx->samp_tdf, &ctx->qfac_df, &ctx->pk_df, &ctx->chitab32,
+                      &ctx->cf_rule};
     spline_free(ctx->cov_pk);
     for (DevBuf *b : bufs) cg_release(*b);
     for (auto &slot : ctx->mp_node_slots) cg_release(slot.buf);
@@ -469,6 +470,90 @@ int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, doubl
         return COFFE_GPU_EINVAL;
     }
     return st;
+}
+
+int coffe_gpu_corrfunc(coffe_gpu_ctx_t *ctx, int contrib, int precision, int n_req,
+                       const int *req_spectrum, const double *req_z_mean,
+                       const int64_t *req_offset, const double *sep, int n_mu, const double *mu,
+                       double *out, int arrays_on_device)
+{
+    if (!ctx || !req_spectrum || !req_z_mean || !req_offset || !mu || n_req < 1 || n_mu < 1 ||
+        n_mu > 1024)
+        return COFFE_GPU_EINVAL;
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    int64_t total = 0;
+    if (arrays_on_device) {
+        CG_CUDA(ctx, cudaMemcpyAsync(&total, req_offset + n_req, sizeof(int64_t),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+        CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    } else {
+        if (!ctx->bg_ready || !ctx->int_ready) {
+            cg_set_error(ctx, "corrfunc: %s not initialised", ctx->bg_ready ? "integrals" : "background");
+            return COFFE_GPU_ESTATE;
+        }
+        if (req_offset[0] != 0) {
+            cg_set_error(ctx, "corrfunc: req_offset[0] must be 0");
+            return COFFE_GPU_EINVAL;
+        }
+        for (int q = 0; q < n_req; ++q) {
+            if (req_offset[q + 1] < req_offset[q]) {
+                cg_set_error(ctx, "corrfunc: req_offset must be non-decreasing");
+                return COFFE_GPU_EINVAL;
+            }
+            if (req_spectrum[q] < 0 || req_spectrum[q] >= ctx->n_spectra) {
+                cg_set_error(ctx, "corrfunc: request %d names spectrum %d of %d", q,
+                             req_spectrum[q], ctx->n_spectra);
+                return COFFE_GPU_EINVAL;
+            }
+            if (!(req_z_mean[q] >= 0)) {
+                cg_set_error(ctx, "corrfunc: request %d has a bad mean redshift", q);
+                return COFFE_GPU_EINVAL;
+            }
+        }
+        total = req_offset[n_req];
+        for (int64_t i = 0; i < total; ++i)
+            if (!(sep[i] > 0)) {
+                cg_set_error(ctx, "corrfunc: separations must be positive");
+                return COFFE_GPU_EINVAL;
+            }
+    }
+    if (total > 0 && (!sep || !out)) return COFFE_GPU_EINVAL;
+    // mu on the device (a host array in both modes), then the inputs
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t b_mu = sizeof(double) * n_mu;
+    size_t bytes = al(b_mu);
+    const size_t b_spec = sizeof(int) * n_req, b_z = sizeof(double) * n_req,
+                 b_off = sizeof(int64_t) * (n_req + 1), b_sep = sizeof(double) * total,
+                 b_out = sizeof(double) * total * n_mu;
+    if (!arrays_on_device) bytes += al(b_spec) + al(b_z) + al(b_off) + al(b_sep) + al(b_out);
+    int st = cg_ensure(ctx, ctx->req_buf, bytes);
+    if (st) return st;
+    char *base = (char *)ctx->req_buf.p;
+    double *d_mu = (double *)base;
+    CG_CUDA(ctx, cudaMemcpyAsync(d_mu, mu, b_mu, cudaMemcpyHostToDevice, ctx->stream));
+    if (arrays_on_device) {
+        st = corrfunc_run(ctx, contrib, precision, n_req, req_spectrum, req_z_mean, req_offset, sep,
+                          n_mu, d_mu, mu, out, total);
+        if (st) return st;
+        return cg_check_device_errors(ctx, "corrfunc");
+    }
+    base += al(b_mu);
+    int *d_spec = (int *)base;
+    double *d_z = (double *)(base + al(b_spec));
+    int64_t *d_off = (int64_t *)(base + al(b_spec) + al(b_z));
+    double *d_sep = (double *)(base + al(b_spec) + al(b_z) + al(b_off));
+    double *d_out = (double *)(base + al(b_spec) + al(b_z) + al(b_off) + al(b_sep));
+    CG_CUDA(ctx, cudaMemcpyAsync(d_spec, req_spectrum, b_spec, cudaMemcpyHostToDevice, ctx->stream));
+    CG_CUDA(ctx, cudaMemcpyAsync(d_z, req_z_mean, b_z, cudaMemcpyHostToDevice, ctx->stream));
+    CG_CUDA(ctx, cudaMemcpyAsync(d_off, req_offset, b_off, cudaMemcpyHostToDevice, ctx->stream));
+    if (total > 0)
+        CG_CUDA(ctx, cudaMemcpyAsync(d_sep, sep, b_sep, cudaMemcpyHostToDevice, ctx->stream));
+    st = corrfunc_run(ctx, contrib, precision, n_req, d_spec, d_z, d_off, d_sep, n_mu, d_mu, mu,
+                      d_out, total);
+    if (st) return st;
+    if (total > 0)
+        CG_CUDA(ctx, cudaMemcpyAsync(out, d_out, b_out, cudaMemcpyDeviceToHost, ctx->stream));
+    return cg_check_device_errors(ctx, "corrfunc");
 }
 
 int coffe_gpu_multipoles_scaled(coffe_gpu_ctx_t *ctx, int contrib, int n_req, int64_t n_sep,

@@ -44,6 +44,7 @@ struct coffe_gpu_ctx {
     DevBuf zrec64, zrec32;
     // mixed path: D1 and f D1 on a uniform chi grid (linear cells, two guard cells)
     DevBuf chitab32;
+    DevBuf cf_rule; // mu list + line rules of the last coffe_gpu_corrfunc call with lensing
     int chi_cells = 0;
     double chi_lo = 0, chi_hi = 0;
     SplineBuf bias[4];
@@ -215,6 +216,14 @@ int multipoles_adjoint_run(coffe_gpu_ctx *ctx, int contrib, int n_req, const int
                            long long total, int n_l, const int *l, const double *bias_scale,
                            const double *growth_scale, const double *grad_out, double *value_out,
                            double *grad_pk, double *grad_bias, double *grad_growth);
+int corrfunc_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,
+                 const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
+                 const double *sep, int n_mu, const double *mu, const double *mu_host,
+                 double *out, long long total);
+int corrfunc_lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,
+                         const int *req_spectrum, const double *req_z_mean,
+                         const int64_t *req_offset, const double *sep, int n_mu,
+                         const double *mu_host, double *out, long long total);
 int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, int n_req,
                 const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
                 const double *sep, int n_l, const int *l, double *out, long long total);

@@ -454,6 +454,20 @@ __global__ void lens_reduce_kernel(LensArgs a, const double *__restrict__ rule,
     out[(a.pair0 + pl) * a.n_l + j] += res;
 }
 
+// correlation function: out[pair][m] += single + double partials at mu_m
+__global__ void lens_cf_reduce_kernel(LensArgs a, const double *__restrict__ part_d,
+                                      const double *__restrict__ part_s, long long n_pairs,
+                                      double *__restrict__ out, int *err)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_pairs * a.n_mu) return;
+    double v = 0;
+    if (part_d) v += part_d[t];
+    if (part_s) v += part_s[t];
+    if (!isfinite(v)) cg_flag(err, CG_ERR_NONFINITE);
+    out[a.pair0 * a.n_mu + t] += v;
+}
+
 // n-point Gauss-Legendre nodes and weights on [-1, 1] (Newton on P_n from the
 // Tricomi initial guesses), nodes ascending
 void gauss_legendre(int n, double *x, double *w)
@@ -611,7 +625,7 @@ template <typename T, typename S, typename TT>
 int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const LensBgT<S> &gT,
                    const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
                    const double *sep, double *out, long long total, bool do_single,
-                   bool do_double)
+                   bool do_double, const double *rule, bool per_node)
 {
     typedef typename Rec4<TT>::type R;
     int st;
@@ -629,7 +643,6 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
         return st;
     double *part_d = (double *)ctx->lens_part.p;
     double *part_s = part_d + chunk * a.n_mu;
-    const double *rule = (const double *)ctx->lens_rule.p;
     for (long long p0 = 0; p0 < total; p0 += chunk) {
         const long long np = std::min(chunk, total - p0);
         a.pair0 = p0;
@@ -647,10 +660,18 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
                 ctx->d_err);
             if ((st = cg_after_launch(ctx, "lens_single_kernel"))) return st;
         }
-        const long long nt = np * a.n_l;
-        lens_reduce_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, ctx->stream>>>(
-            a, rule, do_double ? part_d : nullptr, single ? part_s : nullptr, np, out, ctx->d_err);
-        if ((st = cg_after_launch(ctx, "lens_reduce_kernel"))) return st;
+        if (per_node) {
+            const long long nt = np * a.n_mu;
+            lens_cf_reduce_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, ctx->stream>>>(
+                a, do_double ? part_d : nullptr, single ? part_s : nullptr, np, out, ctx->d_err);
+            if ((st = cg_after_launch(ctx, "lens_cf_reduce_kernel"))) return st;
+        } else {
+            const long long nt = np * a.n_l;
+            lens_reduce_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, ctx->stream>>>(
+                a, rule, do_double ? part_d : nullptr, single ? part_s : nullptr, np, out,
+                ctx->d_err);
+            if ((st = cg_after_launch(ctx, "lens_reduce_kernel"))) return st;
+        }
     }
     return COFFE_GPU_OK;
 }
@@ -760,6 +781,105 @@ static int flatsky_run(coffe_gpu_ctx *ctx, bool denlen, bool lenlen, double epsr
     return COFFE_GPU_OK;
 }
 
+// arguments of the lensing kernels for a validated call (n_mu mu nodes)
+static int lens_args(coffe_gpu_ctx *ctx, int contrib, int n_req, int n_l, const int *l, int n_mu,
+                     LensArgs *out)
+{
+    LensArgs a;
+    const int want[LENS_NT][2] = {{0, 0}, {0, 2}, {0, 4}, {1, 1}, {1, 3}, {2, 0}};
+    for (int t = 0; t < LENS_NT; ++t) {
+        a.term[t] = cg_find_term(ctx, want[t][0], want[t][1]);
+        if (a.term[t] < 0) {
+            cg_set_error(ctx, "lensing needs the integral (n=%d, l=%d)", want[t][0], want[t][1]);
+            return COFFE_GPU_ESTATE;
+        }
+    }
+    a.n_req = n_req;
+    a.n_l = n_l;
+    a.n_mu = n_mu;
+    a.n_x = ctx->lens_n_x;
+    a.nh = (a.n_x % 2 == 0) ? a.n_x / 2 : 0;
+    a.contrib = contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD | COFFE_GPU_LEN);
+    a.tab_len = (int)(ctx->N + CG_N_SMALL_R + 1);
+    a.n_terms = ctx->n_terms;
+    a.inv_dlog = (double)ctx->N / log(ctx->kmax / ctx->kmin);
+    a.Om = ctx->Omega0_m;
+    a.pref2 = pow(CG_H0 * ctx->h, 2);
+    a.pref4 = pow(CG_H0 * ctx->h, 4);
+    a.has_b1 = ctx->bias_set[0];
+    a.has_b2 = ctx->bias_set[1];
+    a.has_s1 = ctx->bias_set[2];
+    a.has_s2 = ctx->bias_set[3];
+    a.pair0 = 0;
+    a.n_items = 0;
+    for (int i = 0; i < 8; ++i) a.ls[i] = i < n_l ? l[i] : 0;
+    *out = a;
+    return COFFE_GPU_OK;
+}
+
+static LensBg64 lens_bg64(const coffe_gpu_ctx *ctx)
+{
+    LensBg64 g64;
+    g64.chi_of_z = ctx->bg[BG_CHI_OF_Z].v64();
+    g64.z_of_chi = ctx->bg[BG_Z_OF_CHI].v64();
+    g64.D1 = ctx->bg[BG_D1].v64();
+    g64.f = ctx->bg[BG_F].v64();
+    g64.a = ctx->bg[BG_A].v64();
+    g64.b1 = ctx->bias[0].v64();
+    g64.b2 = ctx->bias[1].v64();
+    g64.s1 = ctx->bias[2].v64();
+    g64.s2 = ctx->bias[3].v64();
+    return g64;
+}
+
+// Adds the lensing terms of the correlation function (corrfunc.c:55-141:
+// signal.c:584-605 single-integrated, 695-702 double-integrated, always the
+// full-sky forms) at the n_mu values mu_host to out[item * n_mu + m], with the
+// x line rules of coffe_gpu_set_lensing_rule.
+int corrfunc_lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,
+                         const int *req_spectrum, const double *req_z_mean,
+                         const int64_t *req_offset, const double *sep, int n_mu,
+                         const double *mu_host, double *out, long long total)
+{
+    if (!(contrib & COFFE_GPU_LEN) || total <= 0) return COFFE_GPU_OK;
+    if (!ctx->int_small_r) {
+        cg_set_error(ctx, "corrfunc: lensing needs the r = 0 and sub-Mpc table entries "
+                          "(integrals_init with COFFE_GPU_SMALL_R)");
+        return COFFE_GPU_ESTATE;
+    }
+    const bool only_cross = (contrib & COFFE_GPU_ONLY_CROSS) != 0;
+    const bool single = (contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD)) != 0;
+    const bool dbl = !only_cross;
+    if (!single && !dbl) return COFFE_GPU_OK;
+    int st;
+    LensArgs a;
+    const int l0 = 0;
+    if ((st = lens_args(ctx, contrib, n_req, 1, &l0, n_mu, &a))) return st;
+    // rule: mu[n_mu], (unused weights)[n_mu], x[n_x], w_x[n_x], x_h[nh], w_h[nh]
+    std::vector<double> r(2 * (size_t)a.n_mu + 2 * (size_t)a.n_x + 2 * (size_t)a.nh, 0.0);
+    for (int m = 0; m < n_mu; ++m) r[m] = mu_host[m];
+    gauss_legendre(a.n_x, r.data() + 2 * a.n_mu, r.data() + 2 * a.n_mu + a.n_x);
+    if (a.nh)
+        gauss_legendre(a.nh, r.data() + 2 * a.n_mu + 2 * a.n_x,
+                       r.data() + 2 * a.n_mu + 2 * a.n_x + a.nh);
+    if ((st = cg_ensure(ctx, ctx->cf_rule, sizeof(double) * r.size()))) return st;
+    CG_CUDA(ctx, cudaMemcpyAsync(ctx->cf_rule.p, r.data(), sizeof(double) * r.size(),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream)); // r is a host temporary
+    const double *rule = (const double *)ctx->cf_rule.p;
+    const LensBg64 g64 = lens_bg64(ctx);
+    if (precision == COFFE_GPU_MIXED) {
+        LensBgT<Spl32> gT{ctx->bg[BG_Z_OF_CHI].v32(), ctx->bg[BG_D1].v32(), ctx->bg[BG_A].v32()};
+        return lensing_launch<float, Spl32, float>(ctx, a, g64, gT, req_spectrum, req_z_mean,
+                                                   req_offset, sep, out, total, single, dbl, rule,
+                                                   true);
+    }
+    LensBgT<Spl64> gT{ctx->bg[BG_Z_OF_CHI].v64(), ctx->bg[BG_D1].v64(), ctx->bg[BG_A].v64()};
+    return lensing_launch<double, Spl64, double>(ctx, a, g64, gT, req_spectrum, req_z_mean,
+                                                 req_offset, sep, out, total, single, dbl, rule,
+                                                 true);
+}
+
 int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, int n_req,
                 const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
                 const double *sep, int n_l, const int *l, double *out, long long total)
@@ -784,34 +904,7 @@ int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, i
         return COFFE_GPU_ESTATE;
     }
     LensArgs a;
-    const int want[LENS_NT][2] = {{0, 0}, {0, 2}, {0, 4}, {1, 1}, {1, 3}, {2, 0}};
-    for (int t = 0; t < LENS_NT; ++t) {
-        a.term[t] = cg_find_term(ctx, want[t][0], want[t][1]);
-        if (a.term[t] < 0) {
-            cg_set_error(ctx, "multipoles: lensing needs the integral (n=%d, l=%d)", want[t][0],
-                         want[t][1]);
-            return COFFE_GPU_ESTATE;
-        }
-    }
-    a.n_req = n_req;
-    a.n_l = n_l;
-    a.n_mu = ctx->lens_n_mu;
-    a.n_x = ctx->lens_n_x;
-    a.nh = (a.n_x % 2 == 0) ? a.n_x / 2 : 0;
-    a.contrib = contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD | COFFE_GPU_LEN);
-    a.tab_len = (int)(ctx->N + CG_N_SMALL_R + 1);
-    a.n_terms = ctx->n_terms;
-    a.inv_dlog = (double)ctx->N / log(ctx->kmax / ctx->kmin);
-    a.Om = ctx->Omega0_m;
-    a.pref2 = pow(CG_H0 * ctx->h, 2);
-    a.pref4 = pow(CG_H0 * ctx->h, 4);
-    a.has_b1 = ctx->bias_set[0];
-    a.has_b2 = ctx->bias_set[1];
-    a.has_s1 = ctx->bias_set[2];
-    a.has_s2 = ctx->bias_set[3];
-    a.pair0 = 0;
-    a.n_items = 0;
-    for (int i = 0; i < 8; ++i) a.ls[i] = i < n_l ? l[i] : 0;
+    if ((st = lens_args(ctx, contrib, n_req, n_l, l, ctx->lens_n_mu, &a))) return st;
     // the Gauss-Legendre rule: mu[n_mu], w_mu[n_mu], x[n_x], w_x[n_x], x_h[nh], w_h[nh]
     if (ctx->lens_rule_mu != a.n_mu || ctx->lens_rule_x != a.n_x) {
         std::vector<double> r(2 * (size_t)a.n_mu + 2 * (size_t)a.n_x + 2 * (size_t)a.nh);
@@ -827,24 +920,17 @@ int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, i
         ctx->lens_rule_mu = a.n_mu;
         ctx->lens_rule_x = a.n_x;
     }
-    LensBg64 g64;
-    g64.chi_of_z = ctx->bg[BG_CHI_OF_Z].v64();
-    g64.z_of_chi = ctx->bg[BG_Z_OF_CHI].v64();
-    g64.D1 = ctx->bg[BG_D1].v64();
-    g64.f = ctx->bg[BG_F].v64();
-    g64.a = ctx->bg[BG_A].v64();
-    g64.b1 = ctx->bias[0].v64();
-    g64.b2 = ctx->bias[1].v64();
-    g64.s1 = ctx->bias[2].v64();
-    g64.s2 = ctx->bias[3].v64();
+    const LensBg64 g64 = lens_bg64(ctx);
     if (precision == COFFE_GPU_MIXED) {
         LensBgT<Spl32> gT{ctx->bg[BG_Z_OF_CHI].v32(), ctx->bg[BG_D1].v32(), ctx->bg[BG_A].v32()};
         return lensing_launch<float, Spl32, float>(ctx, a, g64, gT, req_spectrum, req_z_mean,
                                                    req_offset, sep, out, total, single_full,
-                                                   double_full);
+                                                   double_full, (const double *)ctx->lens_rule.p,
+                                                   false);
     }
     LensBgT<Spl64> gT{ctx->bg[BG_Z_OF_CHI].v64(), ctx->bg[BG_D1].v64(), ctx->bg[BG_A].v64()};
     return lensing_launch<double, Spl64, double>(ctx, a, g64, gT, req_spectrum, req_z_mean,
                                                  req_offset, sep, out, total, single_full,
-                                                 double_full);
+                                                 double_full, (const double *)ctx->lens_rule.p,
+                                                 false);
 }

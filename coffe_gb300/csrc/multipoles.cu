@@ -776,6 +776,30 @@ __global__ void chitab_kernel(Spl64 z_of_chi, Spl64 D1, Spl64 f, double lo, doub
                          (float)(0.5 * (fa + fb) + sh * (fb - fa)), (float)(fb - fa));
 }
 
+// ------------------------------------------------- correlation function
+// xi(z_mean, mu, r) of the nonintegrated den/rsd terms (corrfunc.c:55-141,
+// signal.c:511-518: functions_nonintegrated at the requested mu), one thread
+// per (separation, mu): out[item * n_mu + m].
+template <typename T, typename S, typename TT>
+__global__ void cf_nonint_kernel(MpArgs a, Bg<T, S> bg, S chi_of_z, const TT *__restrict__ tab_x,
+                                 const TT *__restrict__ tab_y, const int *__restrict__ req_spectrum,
+                                 const double *__restrict__ req_z_mean,
+                                 const int64_t *__restrict__ req_offset,
+                                 const double *__restrict__ sep, const double *__restrict__ mu,
+                                 int n_mu, long long total, double *__restrict__ out, int *err)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total * n_mu) return;
+    const long long item = t / n_mu;
+    const int m = (int)(t - item * n_mu);
+    const int q = find_request(req_offset, a.n_req, item);
+    const Xi<T, S> xi = make_xi<T, S, TT>(a, bg, chi_of_z, tab_x, tab_y, req_spectrum[q],
+                                         (T)req_z_mean[q], (T)sep[item]);
+    const double res = to_f64(xi((T)mu[m]));
+    if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
+    out[t] = res;
+}
+
 // ------------------------------------------------------- adaptive retries
 template <typename T, typename S, typename TT>
 __global__ void __launch_bounds__(32 * MP_RETRY_WARPS)
@@ -1190,6 +1214,110 @@ static int multipoles_nonintegrated(coffe_gpu_ctx *ctx, const MpArgs &a, int pre
                                          (const double *)ctx->tab_x.p,
                                          (const double *)ctx->tab_y.p, req_spectrum, req_z_mean,
                                          req_offset, sep, total, out);
+}
+
+// The correlation function of a call to coffe_gpu_corrfunc (all arrays on the
+// device except mu_host, the same n_mu values as mu): the nonintegrated
+// den/rsd terms, then the lensing terms added by corrfunc_lensing_run.
+int corrfunc_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,
+                 const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
+                 const double *sep, int n_mu, const double *mu, const double *mu_host,
+                 double *out, long long total)
+{
+    if (!ctx->bg_ready || !ctx->int_ready) {
+        cg_set_error(ctx, "corrfunc: %s not initialised", ctx->bg_ready ? "integrals" : "background");
+        return COFFE_GPU_ESTATE;
+    }
+    if (precision != ctx->int_precision) {
+        cg_set_error(ctx, "corrfunc: precision %d differs from the integrals' (%d)", precision,
+                     ctx->int_precision);
+        return COFFE_GPU_EINVAL;
+    }
+    if (!(contrib & 7) || (contrib & ~15)) {
+        cg_set_error(ctx, "corrfunc: contrib must select den, rsd and/or len (+ only-cross)");
+        return COFFE_GPU_EINVAL;
+    }
+    if (n_req < 1 || n_mu < 1 || n_mu > 1024) {
+        cg_set_error(ctx, "corrfunc: need n_req >= 1 and 1 <= n_mu <= 1024");
+        return COFFE_GPU_EINVAL;
+    }
+    for (int m = 0; m < n_mu; ++m)
+        if (!(mu_host[m] >= -1.0 && mu_host[m] <= 1.0)) {
+            cg_set_error(ctx, "corrfunc: mu must lie in [-1, 1]");
+            return COFFE_GPU_EINVAL;
+        }
+    if (total * n_mu > (long long)INT32_MAX * 32) {
+        cg_set_error(ctx, "corrfunc: too many (separation, mu) outputs in one call");
+        return COFFE_GPU_EINVAL;
+    }
+    if (total <= 0) return COFFE_GPU_OK;
+    int st;
+    if (contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD)) {
+        MpArgs a;
+        a.n_req = n_req;
+        a.n_l = 1;
+        a.contrib = contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD | COFFE_GPU_ONLY_CROSS);
+        a.t00 = cg_find_term(ctx, 0, 0);
+        a.t02 = cg_find_term(ctx, 0, 2);
+        a.t04 = cg_find_term(ctx, 0, 4);
+        if (a.t00 < 0 || a.t02 < 0 || a.t04 < 0) {
+            cg_set_error(ctx, "corrfunc: integrals (0,0), (0,2), (0,4) are required");
+            return COFFE_GPU_ESTATE;
+        }
+        a.n_terms = ctx->n_terms;
+        a.tab_len = (int)(ctx->N + CG_N_SMALL_R + 1);
+        a.inv_dlog = (double)ctx->N / log(ctx->kmax / ctx->kmin);
+        a.epsrel = 1e-5;
+        a.retry_cap = 0;
+        for (int i = 0; i < MP_MAX_L; ++i) a.ls[i] = 0;
+        const long long n_out = total * n_mu;
+        const unsigned blocks = (unsigned)((n_out + 255) / 256);
+        if (precision == COFFE_GPU_MIXED) {
+            Bg<float, Spl32> bg;
+            bg.z_of_chi = ctx->bg[BG_Z_OF_CHI].v32();
+            bg.f = ctx->bg[BG_F].v32();
+            bg.D1 = ctx->bg[BG_D1].v32();
+            bg.b1 = ctx->bias[0].v32();
+            bg.b2 = ctx->bias[1].v32();
+            bg.has_b1 = ctx->bias_set[0];
+            bg.has_b2 = ctx->bias_set[1];
+            bg.zrec = ctx->z_uniform ? (const ZRec<float> *)ctx->zrec32.p : nullptr;
+            bg.z0 = (float)ctx->z0;
+            bg.zn = (float)ctx->zn;
+            bg.dz = (float)ctx->dz;
+            bg.inv_dz = (float)(1.0 / ctx->dz);
+            bg.nz = ctx->bg_bins;
+            cf_nonint_kernel<float, Spl32, float><<<blocks, 256, 0, ctx->stream>>>(
+                a, bg, ctx->bg[BG_CHI_OF_Z].v32(), (const float *)ctx->tab_x32.p,
+                (const float *)ctx->tab_y.p, req_spectrum, req_z_mean, req_offset, sep, mu, n_mu,
+                total, out, ctx->d_err);
+        } else {
+            Bg<double, Spl64> bg;
+            bg.z_of_chi = ctx->bg[BG_Z_OF_CHI].v64();
+            bg.f = ctx->bg[BG_F].v64();
+            bg.D1 = ctx->bg[BG_D1].v64();
+            bg.b1 = ctx->bias[0].v64();
+            bg.b2 = ctx->bias[1].v64();
+            bg.has_b1 = ctx->bias_set[0];
+            bg.has_b2 = ctx->bias_set[1];
+            bg.zrec = ctx->z_uniform ? (const ZRec<double> *)ctx->zrec64.p : nullptr;
+            bg.z0 = ctx->z0;
+            bg.zn = ctx->zn;
+            bg.dz = ctx->dz;
+            bg.inv_dz = 1.0 / ctx->dz;
+            bg.nz = ctx->bg_bins;
+            cf_nonint_kernel<double, Spl64, double><<<blocks, 256, 0, ctx->stream>>>(
+                a, bg, ctx->bg[BG_CHI_OF_Z].v64(), (const double *)ctx->tab_x.p,
+                (const double *)ctx->tab_y.p, req_spectrum, req_z_mean, req_offset, sep, mu, n_mu,
+                total, out, ctx->d_err);
+        }
+        if ((st = cg_after_launch(ctx, "cf_nonint_kernel"))) return st;
+    } else {
+        CG_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(double) * (size_t)(total * n_mu), ctx->stream));
+    }
+    if (!(contrib & COFFE_GPU_LEN)) return COFFE_GPU_OK;
+    return corrfunc_lensing_run(ctx, contrib, precision, n_req, req_spectrum, req_z_mean,
+                                req_offset, sep, n_mu, mu_host, out, total);
 }
 
 // ============================================================================

@@ -268,6 +268,24 @@ int coffe_gpu_multipoles_noalloc(coffe_gpu_ctx_t *ctx, int contrib, int precisio
                                  const int64_t *req_offset, const double *sep, int n_l,
                                  const int *l, double *out);
 
+/* coffe_corrfunc_init (corrfunc.c:55-141) batched like coffe_gpu_multipoles:
+   for request q, its separation j and mu[m] (n_mu <= 1024 values in [-1, 1]),
+     out[(req_offset[q] + j) * n_mu + m] = xi(z_mean_q, mu_m, sep_j),
+   the nonintegrated den/rsd terms at mu (functions.c:89-771; signal.c:511-518)
+   plus, with COFFE_GPU_LEN, the single-integrated den/rsd x lensing line
+   integral and the double-integrated lensing-lensing plane at mu
+   (signal.c:584-605, 695-702: full-sky forms, the CORRFUNC branches have no
+   flat-sky ones), by the Gauss-Legendre line rules of
+   coffe_gpu_set_lensing_rule (n_x; the reference uses QAG and Cuhre).
+   COFFE_GPU_ONLY_CROSS drops the auto-correlations as in coffe_gpu_multipoles.
+   `mu` is a host array; the other arrays are host pointers unless
+   arrays_on_device != 0 (then all of them, out included, are device
+   pointers). */
+int coffe_gpu_corrfunc(coffe_gpu_ctx_t *ctx, int contrib, int precision, int n_req,
+                       const int *req_spectrum, const double *req_z_mean,
+                       const int64_t *req_offset, const double *sep, int n_mu, const double *mu,
+                       double *out, int arrays_on_device);
+
 /* Number of (separation, multipole) outputs of the last multipoles call on
    this context whose first GK61 panel missed the tolerance and went through
    the adaptive bisection (synchronises the context's stream); -1 if none ran.

@@ -147,6 +147,11 @@ double or_xi_double_integrated(const or_model_t *m, int contrib, double z_mean, 
    (double); out[j] for l = ls[j] */
 int or_multipoles_lensing_gl(const or_model_t *m, int contrib, double z_mean, double sep,
                              int n_l, const int *ls, size_t n_mu, size_t n_x, double *out);
+/* correlation function (corrfunc.c:55-141): nonintegrated + lensing at fixed mu */
+double or_corrfunc_gl(const or_model_t *m, int contrib, double z_mean, double mu, double sep,
+                      size_t n_x);
+int or_corrfunc_batch(const or_model_t *m, int contrib, const double *z_mean, const double *mu,
+                      const double *sep, size_t count, size_t n_x, double *out, int nthreads);
 int or_multipoles_lensing_batch(const or_model_t *m, int contrib, const double *z_mean,
                                 const double *sep, size_t count, int n_l, const int *ls,
                                 size_t n_mu, size_t n_x, double *out, int nthreads);

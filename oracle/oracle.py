@@ -110,6 +110,9 @@ def lib():
         L.or_covariance_multipoles.argtypes = [C.c_void_p, C.c_int, C.c_size_t, _dp, _dp, _dp,
                                                _dp, _dp, _dp, C.c_size_t, _ip, C.c_size_t, _dp,
                                                _dp, _dp, _dp]
+        L.or_corrfunc_batch.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_size_t,
+                                        C.c_size_t, _dp, C.c_int]
+        L.or_corrfunc_batch.restype = C.c_int
         L.or_multipoles_lensing_batch.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_size_t,
                                                   C.c_int, _ip, C.c_size_t, C.c_size_t, _dp,
                                                   C.c_int]
@@ -267,6 +270,18 @@ class Model:
 
     def xi_double(self, contrib, z_mean, mu, sep, x1, x2):
         return lib().or_xi_double_integrated(self._p, contrib, z_mean, mu, sep, x1, x2)
+
+    def corrfunc(self, contrib, z_mean, mu, sep, n_x=256, nthreads=0):
+        """Correlation function at (z_mean, mu, sep) points (broadcast): the
+        nonintegrated den/rsd terms plus, with len, the lensing integrals at mu
+        (split Gauss-Legendre lines of n_x nodes)."""
+        z, m, r = np.broadcast_arrays(np.asarray(z_mean, dtype=np.float64),
+                                      np.asarray(mu, dtype=np.float64),
+                                      np.asarray(sep, dtype=np.float64))
+        z, m, r = _f64(z.ravel()), _f64(m.ravel()), _f64(r.ravel())
+        out = np.zeros(len(r))
+        lib().or_corrfunc_batch(self._p, contrib, z, m, r, len(r), int(n_x), out, int(nthreads))
+        return out
 
     def multipoles_lensing(self, contrib, z_mean, sep, ls, n_mu, n_x, nthreads=0):
         """Lensing multipoles (single + double integrated terms) with product

@@ -181,3 +181,20 @@ def test_flatsky_lensing_multipoles_match_golden(golden, oracle, class_pk, ref_b
             d = golden[f"{name}_multipoles{l}"]
             v = np.array([fn(1.0, r / H, l) for r in d[:, 0]])
             assert np.allclose(v, d[:, 1], rtol=5e-4), (name, l, v / d[:, 1] - 1)
+
+
+CORRFUNC_MU = (0.0, 0.2, 0.5, 0.8, 0.95)
+
+
+@pytest.mark.parametrize("name,mask", [("den", 1), ("rsd", 2), ("std", 3), ("len", 4),
+                                       ("std_len", 7)])
+def test_corrfunc_matches_golden(golden, lens_model, name, mask):
+    """The correlation function (corrfunc.c:55-141) at z = 1 and the five mu of
+    the reference's test (test_coffe.py:235-268), at its rtol 5e-4: the
+    nonintegrated terms at mu, the lensing line and plane integrals by the
+    split Gauss-Legendre rule (256 nodes per line; the reference uses QAG and
+    Cuhre)."""
+    for i, mu in enumerate(CORRFUNC_MU):
+        d = golden[f"{name}_corrfunc{i}"]
+        got = lens_model.corrfunc(mask, 1.0, mu, d[:, 0] / H, n_x=256)
+        assert np.allclose(got, d[:, 1], rtol=5e-4), (name, mu, got / d[:, 1] - 1)
