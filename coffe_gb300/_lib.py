@@ -55,6 +55,7 @@ EXPORTS = (
     "coffe_gpu_multipoles_async",
     "coffe_gpu_multipoles_noalloc",
     "coffe_gpu_corrfunc",
+    "coffe_gpu_average_multipoles",
     "coffe_gpu_multipoles_retries",
     "coffe_gpu_multipoles_scaled",
     "coffe_gpu_multipoles_adjoint",
@@ -161,6 +162,9 @@ def load(build_if_missing: bool = True):
     L.coffe_gpu_multipoles_retries.restype = C.c_longlong
     L.coffe_gpu_corrfunc.argtypes = [_p, C.c_int, C.c_int, C.c_int, _ip, _dp, _lp, _dp,
                                      C.c_int, _dp, _dp, C.c_int]
+    L.coffe_gpu_average_multipoles.argtypes = [_p, C.c_int, C.c_int, C.c_double, C.c_int, _ip,
+                                               _dp, _dp, _lp, _dp, C.c_int, _ip, C.c_int, _dp,
+                                               C.c_int]
     L.coffe_gpu_set_autotune.argtypes = [_p, C.c_int]
     L.coffe_gpu_get_tuning.argtypes = [_p, C.POINTER(Tuning)]
     L.coffe_gpu_set_tuning.argtypes = [_p, C.POINTER(Tuning)]

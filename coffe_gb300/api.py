@@ -240,6 +240,25 @@ class Context:
                                                  _dptr(out), 0), "multipoles")
         return out[: len(sp)]
 
+    def average_multipoles(self, win_spectrum, z_min, z_max, win_offset, sep, ls=(0, 2, 4),
+                           contrib=_lib.DEN | _lib.RSD, precision="fp64", epsrel=1e-5,
+                           n_z: int = 32) -> np.ndarray:
+        """Redshift-averaged multipoles of the batched windows; returns an array
+        of shape (len(sep), len(ls)) (average_multipoles.c:69-156)."""
+        ws = np.ascontiguousarray(win_spectrum, dtype=np.int32)
+        a, b = _f64(z_min), _f64(z_max)
+        wo = np.ascontiguousarray(win_offset, dtype=np.int64)
+        sp = _f64(sep)
+        la = np.ascontiguousarray(ls, dtype=np.int32)
+        if len(wo) != len(ws) + 1 or len(a) != len(ws) or len(b) != len(ws):
+            raise ValueError("win_offset needs len(win_spectrum) + 1 entries")
+        out = np.zeros((max(len(sp), 1), len(la)))
+        self._check(self._L.coffe_gpu_average_multipoles(
+            self._ctx, int(contrib), _precision(precision), float(epsrel), len(ws), _iptr(ws),
+            _dptr(a), _dptr(b), _lptr(wo), _dptr(sp), len(la), _iptr(la), int(n_z), _dptr(out), 0),
+            "average_multipoles")
+        return out[: len(sp)]
+
     def corrfunc(self, req_spectrum, req_z_mean, req_offset, sep, mu,
                  contrib=_lib.DEN | _lib.RSD, precision="fp64") -> np.ndarray:
         """Correlation function at every (separation, mu) of the batched requests;
@@ -396,6 +415,22 @@ class Multipoles:
 
 
 @dataclass
+class AverageMultipoles:
+    """One redshift-averaged multipole (python/coffe/representation.py's
+    AverageMultipoles record)."""
+
+    z_min: float
+    z_max: float
+    r: float
+    l: int
+    value: float
+
+    def to_dict(self):
+        return {"z_min": self.z_min, "z_max": self.z_max, "r": self.r, "l": self.l,
+                "value": self.value}
+
+
+@dataclass
 class Corrfunc:
     """One correlation-function value (python/coffe/representation.py's Corrfunc record)."""
 
@@ -424,7 +459,8 @@ class Coffe:
     """
 
     def __init__(self, *, omega_m=0.3, omega_baryon=0.05, omega_gamma=9e-5, h=0.67,
-                 sep=None, l=(0, 2, 4), mu=(0.5,), z_mean=(1.0,), has_density=True,
+                 sep=None, l=(0, 2, 4), mu=(0.5,), z_mean=(1.0,), z_min=(0.9,),
+                 z_max=(1.1,), has_density=True,
                  has_rsd=False, has_lensing=False,
                  integrals_fftlog_sampling=4096, background_bins=10000,
                  integration_1d_prec=1e-5, precision="fp64", device=0):
@@ -439,6 +475,9 @@ class Coffe:
         # default mu of coffe_parse_default_parameters (parser.c:980-982)
         self.mu = [float(m) for m in mu]
         self.z_mean = list(z_mean)
+        # redshift windows of the averaged multipoles (parser.c defaults 0.9, 1.1)
+        self.z_min = [float(z) for z in z_min]
+        self.z_max = [float(z) for z in z_max]
         self.has_density = bool(has_density)
         self.has_rsd = bool(has_rsd)
         self.has_lensing = bool(has_lensing)
@@ -541,6 +580,40 @@ class Coffe:
             for il, ll in enumerate(self.l):
                 for js, r in enumerate(self.sep):
                     res.append(Multipoles(z=zm, r=float(r), l=ll, value=float(vals[iz * ns + js, il])))
+        return res
+
+    def compute_average_multipole(self, *, z_min: float, z_max: float, r: float, l: int) -> float:
+        """One redshift-averaged multipole (coffe.pyx's compute_average_multipoles_bulk
+        for a single point)."""
+        _check_parameter("z_min", z_min, (int, float), 0, 15)
+        _check_parameter("z_max", z_max, (int, float), 0, 15)
+        _check_parameter("r", r, (int, float), 0, 1500)
+        _check_parameter("l", l, int, 0, 10)
+        self._ensure()
+        out = self._ctx.average_multipoles([0], [float(z_min)], [float(z_max)], [0, 1],
+                                           [float(r)], [l], self._contrib, self.precision,
+                                           self.integration_1d_prec)
+        return float(out[0, 0])
+
+    def compute_average_multipoles_bulk(self) -> List[AverageMultipoles]:
+        """All (window, l, sep) points in the reference's order: window outer, l,
+        then separation (average_multipoles.c:96-106)."""
+        if len(self.z_min) != len(self.z_max):
+            raise ValueError("z_min and z_max must have the same length")
+        self._ensure()
+        nw, ns = len(self.z_min), len(self.sep)
+        offs = np.arange(nw + 1, dtype=np.int64) * ns
+        sep = np.tile(self.sep, nw)
+        vals = self._ctx.average_multipoles(np.zeros(nw, np.int32), self.z_min, self.z_max, offs,
+                                            sep, self.l, self._contrib, self.precision,
+                                            self.integration_1d_prec)
+        res = []
+        for iw in range(nw):
+            for il, ll in enumerate(self.l):
+                for js, r in enumerate(self.sep):
+                    res.append(AverageMultipoles(z_min=self.z_min[iw], z_max=self.z_max[iw],
+                                                 r=float(r), l=ll,
+                                                 value=float(vals[iw * ns + js, il])))
         return res
 
     def compute_corrfunc(self, *, z: float, r: float, mu: float) -> float:

@@ -148,7 +148,7 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
                       &ctx->lens_rule, &ctx->lens_rec, &ctx->lens_part,
                       &ctx->cov_buf,  &ctx->cov_out, &ctx->adj_buf, &ctx->csband,
                       &ctx->samp_tdf, &ctx->qfac_df, &ctx->pk_df, &ctx->chitab32,
-                      &ctx->cf_rule};
+                      &ctx->cf_rule, &ctx->avg_buf};
     spline_free(ctx->cov_pk);
     for (DevBuf *b : bufs) cg_release(*b);
     for (auto &slot : ctx->mp_node_slots) cg_release(slot.buf);
@@ -470,6 +470,85 @@ int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, doubl
         return COFFE_GPU_EINVAL;
     }
     return st;
+}
+
+int coffe_gpu_average_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision,
+                                 double epsrel, int n_win, const int *win_spectrum,
+                                 const double *z_min, const double *z_max,
+                                 const int64_t *win_offset, const double *sep, int n_l,
+                                 const int *l, int n_z, double *out, int arrays_on_device)
+{
+    if (!ctx || !win_spectrum || !z_min || !z_max || !win_offset || !l || n_win < 1 || n_l < 1)
+        return COFFE_GPU_EINVAL;
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (arrays_on_device) {
+        int64_t total = 0;
+        CG_CUDA(ctx, cudaMemcpyAsync(&total, win_offset + n_win, sizeof(int64_t),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+        CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        const int st = average_multipoles_run(ctx, contrib, precision, epsrel, n_win, win_spectrum,
+                                              z_min, z_max, win_offset, sep, n_l, l, n_z, out,
+                                              total);
+        if (st) return st;
+        return cg_check_device_errors(ctx, "average_multipoles");
+    }
+    if (!ctx->bg_ready || !ctx->int_ready) {
+        cg_set_error(ctx, "average_multipoles: %s not initialised",
+                     ctx->bg_ready ? "integrals" : "background");
+        return COFFE_GPU_ESTATE;
+    }
+    if (win_offset[0] != 0) {
+        cg_set_error(ctx, "average_multipoles: win_offset[0] must be 0");
+        return COFFE_GPU_EINVAL;
+    }
+    for (int q = 0; q < n_win; ++q) {
+        if (win_offset[q + 1] < win_offset[q]) {
+            cg_set_error(ctx, "average_multipoles: win_offset must be non-decreasing");
+            return COFFE_GPU_EINVAL;
+        }
+        if (win_spectrum[q] < 0 || win_spectrum[q] >= ctx->n_spectra) {
+            cg_set_error(ctx, "average_multipoles: window %d names spectrum %d of %d", q,
+                         win_spectrum[q], ctx->n_spectra);
+            return COFFE_GPU_EINVAL;
+        }
+        if (!(z_min[q] >= 0 && z_max[q] > z_min[q])) {
+            cg_set_error(ctx, "average_multipoles: window %d needs 0 <= z_min < z_max", q);
+            return COFFE_GPU_EINVAL;
+        }
+    }
+    const int64_t total = win_offset[n_win];
+    if (total > 0 && (!sep || !out)) return COFFE_GPU_EINVAL;
+    for (int64_t i = 0; i < total; ++i)
+        if (!(sep[i] > 0)) {
+            cg_set_error(ctx, "average_multipoles: separations must be positive");
+            return COFFE_GPU_EINVAL;
+        }
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t b_spec = sizeof(int) * n_win, b_z = sizeof(double) * n_win,
+                 b_off = sizeof(int64_t) * (n_win + 1), b_sep = sizeof(double) * total,
+                 b_out = sizeof(double) * total * n_l;
+    int st = cg_ensure(ctx, ctx->req_buf, al(b_spec) + 2 * al(b_z) + al(b_off) + al(b_sep) +
+                                              al(b_out));
+    if (st) return st;
+    char *base = (char *)ctx->req_buf.p;
+    int *d_spec = (int *)base;
+    double *d_zmin = (double *)(base + al(b_spec));
+    double *d_zmax = (double *)(base + al(b_spec) + al(b_z));
+    int64_t *d_off = (int64_t *)(base + al(b_spec) + 2 * al(b_z));
+    double *d_sep = (double *)(base + al(b_spec) + 2 * al(b_z) + al(b_off));
+    double *d_out = (double *)(base + al(b_spec) + 2 * al(b_z) + al(b_off) + al(b_sep));
+    CG_CUDA(ctx, cudaMemcpyAsync(d_spec, win_spectrum, b_spec, cudaMemcpyHostToDevice, ctx->stream));
+    CG_CUDA(ctx, cudaMemcpyAsync(d_zmin, z_min, b_z, cudaMemcpyHostToDevice, ctx->stream));
+    CG_CUDA(ctx, cudaMemcpyAsync(d_zmax, z_max, b_z, cudaMemcpyHostToDevice, ctx->stream));
+    CG_CUDA(ctx, cudaMemcpyAsync(d_off, win_offset, b_off, cudaMemcpyHostToDevice, ctx->stream));
+    if (total > 0)
+        CG_CUDA(ctx, cudaMemcpyAsync(d_sep, sep, b_sep, cudaMemcpyHostToDevice, ctx->stream));
+    st = average_multipoles_run(ctx, contrib, precision, epsrel, n_win, d_spec, d_zmin, d_zmax,
+                                d_off, d_sep, n_l, l, n_z, d_out, total);
+    if (st) return st;
+    if (total > 0)
+        CG_CUDA(ctx, cudaMemcpyAsync(out, d_out, b_out, cudaMemcpyDeviceToHost, ctx->stream));
+    return cg_check_device_errors(ctx, "average_multipoles");
 }
 
 int coffe_gpu_corrfunc(coffe_gpu_ctx_t *ctx, int contrib, int precision, int n_req,

@@ -45,6 +45,7 @@ struct coffe_gpu_ctx {
     // mixed path: D1 and f D1 on a uniform chi grid (linear cells, two guard cells)
     DevBuf chitab32;
     DevBuf cf_rule; // mu list + line rules of the last coffe_gpu_corrfunc call with lensing
+    DevBuf avg_buf; // expanded requests of coffe_gpu_average_multipoles
     int chi_cells = 0;
     double chi_lo = 0, chi_hi = 0;
     SplineBuf bias[4];
@@ -216,6 +217,12 @@ int multipoles_adjoint_run(coffe_gpu_ctx *ctx, int contrib, int n_req, const int
                            long long total, int n_l, const int *l, const double *bias_scale,
                            const double *growth_scale, const double *grad_out, double *value_out,
                            double *grad_pk, double *grad_bias, double *grad_growth);
+int average_multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel,
+                           int n_win, const int *win_spectrum, const double *z_min,
+                           const double *z_max, const int64_t *win_offset, const double *sep,
+                           int n_l, const int *l, int n_z, double *out, long long total);
+// n-point Gauss-Legendre nodes (ascending) and weights on [-1, 1]
+void gauss_legendre_nodes(int n, double *x, double *w);
 int corrfunc_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,
                  const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
                  const double *sep, int n_mu, const double *mu, const double *mu_host,

@@ -880,6 +880,8 @@ int corrfunc_lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_r
                                                  true);
 }
 
+void gauss_legendre_nodes(int n, double *x, double *w) { gauss_legendre(n, x, w); }
+
 int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, int n_req,
                 const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
                 const double *sep, int n_l, const int *l, double *out, long long total)

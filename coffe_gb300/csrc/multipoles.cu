@@ -800,6 +800,56 @@ __global__ void cf_nonint_kernel(MpArgs a, Bg<T, S> bg, S chi_of_z, const TT *__
     out[t] = res;
 }
 
+// ------------------------------------------ redshift-averaged multipoles
+// Expansion of every (window, separation) into n_z Gauss-Legendre redshift
+// nodes (average_multipoles.c:69-156; signal.c:241-310): node k of separation
+// item sits at z = z1 + (z2 - z1) v_k, z1 = z(chi(z_min) + r/2),
+// z2 = z(chi(z_max) - r/2), with weight (w_k / 2) H0 h / (conformal_H(z) (1 + z)).
+// The expanded entries are single-separation requests for multipoles_run.
+__global__ void avg_expand_kernel(Spl64 chi_of_z, Spl64 z_of_chi, Spl64 confH, double H0h,
+                                  const int *__restrict__ win_spectrum,
+                                  const double *__restrict__ z_min, const double *__restrict__ z_max,
+                                  const int64_t *__restrict__ win_offset, int n_win,
+                                  const double *__restrict__ sep, long long total,
+                                  const double *__restrict__ gl, int n_z,
+                                  int *__restrict__ e_spec, double *__restrict__ e_z,
+                                  int64_t *__restrict__ e_off, double *__restrict__ e_sep,
+                                  double *__restrict__ e_w)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total * n_z) return;
+    const long long item = e / n_z;
+    const int k = (int)(e - item * n_z);
+    const int q = find_request(win_offset, n_win, item);
+    const double r = sep[item];
+    const double z1 = spl_eval(z_of_chi, spl_eval(chi_of_z, z_min[q]) + 0.5 * r);
+    const double z2 = spl_eval(z_of_chi, spl_eval(chi_of_z, z_max[q]) - 0.5 * r);
+    const double v = 0.5 * (gl[k] + 1.0);
+    const double z = (z2 - z1) * v + z1;
+    e_spec[e] = win_spectrum[q];
+    e_z[e] = z;
+    e_sep[e] = r;
+    e_off[e] = e;
+    if (e == total * n_z - 1) e_off[e + 1] = e + 1;
+    e_w[e] = 0.5 * gl[n_z + k] * H0h / (spl_eval(confH, z) * (1.0 + z));
+}
+
+// out[item][j] = sum_k w[item, k] mp[(item, k)][j]
+__global__ void avg_reduce_kernel(const double *__restrict__ e_w, const double *__restrict__ e_out,
+                                  long long total, int n_z, int n_l, double *__restrict__ out,
+                                  int *err)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total * n_l) return;
+    const long long item = t / n_l;
+    const int j = (int)(t - item * n_l);
+    double acc = 0.0;
+    for (int k = 0; k < n_z; ++k)
+        acc += e_w[item * n_z + k] * e_out[(item * n_z + k) * n_l + j];
+    if (!isfinite(acc)) cg_flag(err, CG_ERR_NONFINITE);
+    out[t] = acc;
+}
+
 // ------------------------------------------------------- adaptive retries
 template <typename T, typename S, typename TT>
 __global__ void __launch_bounds__(32 * MP_RETRY_WARPS)
@@ -1214,6 +1264,68 @@ static int multipoles_nonintegrated(coffe_gpu_ctx *ctx, const MpArgs &a, int pre
                                          (const double *)ctx->tab_x.p,
                                          (const double *)ctx->tab_y.p, req_spectrum, req_z_mean,
                                          req_offset, sep, total, out);
+}
+
+// Redshift-averaged multipoles of a call to coffe_gpu_average_multipoles (all
+// arrays on the device except l): the multipoles at the n_z redshift nodes of
+// every (window, separation) by multipoles_run, then their weighted sums.
+int average_multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel,
+                           int n_win, const int *win_spectrum, const double *z_min,
+                           const double *z_max, const int64_t *win_offset, const double *sep,
+                           int n_l, const int *l, int n_z, double *out, long long total)
+{
+    if (!ctx->bg_ready) {
+        cg_set_error(ctx, "average_multipoles: background not initialised");
+        return COFFE_GPU_ESTATE;
+    }
+    if (n_z < 1 || n_z > 256 || n_l < 1 || n_l > MP_MAX_L || n_win < 1) {
+        cg_set_error(ctx, "average_multipoles: need 1 <= n_z <= 256, 1 <= n_l <= %d, n_win >= 1",
+                     MP_MAX_L);
+        return COFFE_GPU_EINVAL;
+    }
+    if (total <= 0) return COFFE_GPU_OK;
+    const long long E = total * n_z;
+    if (E > (long long)INT32_MAX) {
+        cg_set_error(ctx, "average_multipoles: too many (separation, redshift node) entries");
+        return COFFE_GPU_EINVAL;
+    }
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t b_gl = sizeof(double) * 2 * n_z, b_spec = sizeof(int) * E,
+                 b_z = sizeof(double) * E, b_off = sizeof(int64_t) * (E + 1),
+                 b_sep = sizeof(double) * E, b_w = sizeof(double) * E,
+                 b_out = sizeof(double) * E * n_l;
+    int st = cg_ensure(ctx, ctx->avg_buf, al(b_gl) + al(b_spec) + al(b_z) + al(b_off) +
+                                              al(b_sep) + al(b_w) + al(b_out));
+    if (st) return st;
+    char *p = (char *)ctx->avg_buf.p;
+    double *d_gl = (double *)p;
+    p += al(b_gl);
+    int *e_spec = (int *)p;
+    p += al(b_spec);
+    double *e_z = (double *)p;
+    p += al(b_z);
+    int64_t *e_off = (int64_t *)p;
+    p += al(b_off);
+    double *e_sep = (double *)p;
+    p += al(b_sep);
+    double *e_w = (double *)p;
+    p += al(b_w);
+    double *e_out = (double *)p;
+    std::vector<double> gl(2 * (size_t)n_z);
+    gauss_legendre_nodes(n_z, gl.data(), gl.data() + n_z);
+    CG_CUDA(ctx, cudaMemcpyAsync(d_gl, gl.data(), b_gl, cudaMemcpyHostToDevice, ctx->stream));
+    CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream)); // gl is a host temporary
+    avg_expand_kernel<<<(unsigned)((E + 255) / 256), 256, 0, ctx->stream>>>(
+        ctx->bg[BG_CHI_OF_Z].v64(), ctx->bg[BG_Z_OF_CHI].v64(), ctx->bg[BG_CONFH].v64(),
+        CG_H0 * ctx->h, win_spectrum, z_min, z_max, win_offset, n_win, sep, total, d_gl, n_z,
+        e_spec, e_z, e_off, e_sep, e_w);
+    if ((st = cg_after_launch(ctx, "avg_expand_kernel"))) return st;
+    if ((st = multipoles_run(ctx, contrib, precision, epsrel, (int)E, e_spec, e_z, e_off, e_sep,
+                             n_l, l, e_out, E)))
+        return st;
+    avg_reduce_kernel<<<(unsigned)((total * n_l + 255) / 256), 256, 0, ctx->stream>>>(
+        e_w, e_out, total, n_z, n_l, out, ctx->d_err);
+    return cg_after_launch(ctx, "avg_reduce_kernel");
 }
 
 // The correlation function of a call to coffe_gpu_corrfunc (all arrays on the

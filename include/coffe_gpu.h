@@ -268,6 +268,26 @@ int coffe_gpu_multipoles_noalloc(coffe_gpu_ctx_t *ctx, int contrib, int precisio
                                  const int64_t *req_offset, const double *sep, int n_l,
                                  const int *l, double *out);
 
+/* coffe_average_multipoles_init (average_multipoles.c:69-156) batched: window q
+   (spectrum win_spectrum[q], redshifts z_min[q] < z_max[q]) with separations
+   sep[win_offset[q] .. win_offset[q+1]-1]; for each separation r and multipole
+   l[i],
+     out[(win_offset[q] + j) * n_l + i] = (2l+1) int_0^1 dv0 int_0^1 dv1
+         xi(z(v0), mu = 2 v1 - 1, r) P_l(mu) H0 h / (conformal_H(z) (1 + z)),
+   z(v0) = z1 + (z2 - z1) v0, z1 = z(chi(z_min) + r/2), z2 = z(chi(z_max) - r/2)
+   (signal.c:241-310 and the AVERAGE_MULTIPOLES branches 543-551, 672-680,
+   755-763), with the contributions of `contrib` as coffe_gpu_multipoles.  The
+   reference integrates the cube with Cuhre; here n_z (<= 256) Gauss-Legendre
+   nodes in v0 and, per node, the multipole at z_mean = z(v0) as
+   coffe_gpu_multipoles computes it (adaptive GK61 in mu, epsrel; the lensing
+   rules of coffe_gpu_set_lensing_rule).  `l` is a host array; the others are
+   host pointers unless arrays_on_device != 0. */
+int coffe_gpu_average_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision,
+                                 double epsrel, int n_win, const int *win_spectrum,
+                                 const double *z_min, const double *z_max,
+                                 const int64_t *win_offset, const double *sep, int n_l,
+                                 const int *l, int n_z, double *out, int arrays_on_device);
+
 /* coffe_corrfunc_init (corrfunc.c:55-141) batched like coffe_gpu_multipoles:
    for request q, its separation j and mu[m] (n_mu <= 1024 values in [-1, 1]),
      out[(req_offset[q] + j) * n_mu + m] = xi(z_mean_q, mu_m, sep_j),

@@ -147,6 +147,13 @@ double or_xi_double_integrated(const or_model_t *m, int contrib, double z_mean, 
    (double); out[j] for l = ls[j] */
 int or_multipoles_lensing_gl(const or_model_t *m, int contrib, double z_mean, double sep,
                              int n_l, const int *ls, size_t n_mu, size_t n_x, double *out);
+/* redshift-averaged multipoles (average_multipoles.c:69-156) */
+double or_average_multipole(const or_model_t *m, int contrib, double z_min, double z_max,
+                            double sep, int l, size_t n_z, size_t n_mu, size_t n_x);
+int or_average_multipoles_batch(const or_model_t *m, int contrib, const double *z_min,
+                                const double *z_max, const double *sep, const int *l,
+                                size_t count, size_t n_z, size_t n_mu, size_t n_x, double *out,
+                                int nthreads);
 /* correlation function (corrfunc.c:55-141): nonintegrated + lensing at fixed mu */
 double or_corrfunc_gl(const or_model_t *m, int contrib, double z_mean, double mu, double sep,
                       size_t n_x);

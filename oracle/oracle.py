@@ -110,6 +110,10 @@ def lib():
         L.or_covariance_multipoles.argtypes = [C.c_void_p, C.c_int, C.c_size_t, _dp, _dp, _dp,
                                                _dp, _dp, _dp, C.c_size_t, _ip, C.c_size_t, _dp,
                                                _dp, _dp, _dp]
+        L.or_average_multipoles_batch.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _ip,
+                                                  C.c_size_t, C.c_size_t, C.c_size_t,
+                                                  C.c_size_t, _dp, C.c_int]
+        L.or_average_multipoles_batch.restype = C.c_int
         L.or_corrfunc_batch.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_size_t,
                                         C.c_size_t, _dp, C.c_int]
         L.or_corrfunc_batch.restype = C.c_int
@@ -270,6 +274,21 @@ class Model:
 
     def xi_double(self, contrib, z_mean, mu, sep, x1, x2):
         return lib().or_xi_double_integrated(self._p, contrib, z_mean, mu, sep, x1, x2)
+
+    def average_multipoles(self, contrib, z_min, z_max, sep, l, n_z=32, n_mu=64, n_x=128,
+                           nthreads=0):
+        """Redshift-averaged multipoles at (z_min, z_max, sep, l) points (broadcast):
+        n_z Gauss-Legendre nodes in the redshift direction, the multipole per node
+        (QAG in mu; with len the lensing rules n_mu x n_x)."""
+        a, b, r, ll = np.broadcast_arrays(np.asarray(z_min, dtype=np.float64),
+                                          np.asarray(z_max, dtype=np.float64),
+                                          np.asarray(sep, dtype=np.float64), np.asarray(l))
+        a, b, r = _f64(a.ravel()), _f64(b.ravel()), _f64(r.ravel())
+        ll = np.ascontiguousarray(ll.ravel(), dtype=np.int32)
+        out = np.zeros(len(r))
+        lib().or_average_multipoles_batch(self._p, contrib, a, b, r, ll, len(r), int(n_z),
+                                          int(n_mu), int(n_x), out, int(nthreads))
+        return out
 
     def corrfunc(self, contrib, z_mean, mu, sep, n_x=256, nthreads=0):
         """Correlation function at (z_mean, mu, sep) points (broadcast): the

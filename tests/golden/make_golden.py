@@ -34,6 +34,9 @@ def main(ref: Path):
                  "flatsky_density_lensing"):
         for l in (0, 2, 4):
             out[f"{name}_multipoles{l}"] = np.loadtxt(bench / f"benchmark_{name}_multipoles{l}.dat")
+    # redshift-averaged den+rsd multipoles, z in [0.9, 1.1]
+    for l in (0, 2, 4):
+        out[f"avg_multipoles{l}"] = np.loadtxt(bench / f"benchmark_avg_multipoles{l}.dat")
     # correlation function at z = 1, mu = 0, 0.2, 0.5, 0.8, 0.95 (index 0..4)
     for name in ("den", "rsd", "std", "len", "std_len"):
         for i in range(5):

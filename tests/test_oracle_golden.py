@@ -198,3 +198,14 @@ def test_corrfunc_matches_golden(golden, lens_model, name, mask):
         d = golden[f"{name}_corrfunc{i}"]
         got = lens_model.corrfunc(mask, 1.0, mu, d[:, 0] / H, n_x=256)
         assert np.allclose(got, d[:, 1], rtol=5e-4), (name, mu, got / d[:, 1] - 1)
+
+
+def test_average_multipoles_match_golden(golden, lens_model):
+    """Redshift-averaged den+rsd multipoles over z in [0.9, 1.1]
+    (average_multipoles.c:69-156; test_coffe.py:305-326) at rtol 5e-4: 16
+    Gauss-Legendre redshift nodes, the multipole per node by QAG (the
+    reference integrates the (z, mu) square with Cuhre)."""
+    for l in (0, 2, 4):
+        d = golden[f"avg_multipoles{l}"]
+        got = lens_model.average_multipoles(3, 0.9, 1.1, d[:, 0] / H, l, n_z=16)
+        assert np.allclose(got, d[:, 1], rtol=5e-4), (l, got / d[:, 1] - 1)
