@@ -61,6 +61,7 @@ EXPORTS = (
     "coffe_gpu_multipoles_adjoint",
     "coffe_gpu_covariance_integrals",
     "coffe_gpu_covariance_multipoles",
+    "coffe_gpu_average_covariance_multipoles",
     "coffe_gpu_set_autotune",
     "coffe_gpu_get_tuning",
     "coffe_gpu_set_tuning",
@@ -165,6 +166,8 @@ def load(build_if_missing: bool = True):
     L.coffe_gpu_average_multipoles.argtypes = [_p, C.c_int, C.c_int, C.c_double, C.c_int, _ip,
                                                _dp, _dp, _lp, _dp, C.c_int, _ip, C.c_int, _dp,
                                                C.c_int]
+    L.coffe_gpu_average_covariance_multipoles.argtypes = (
+        L.coffe_gpu_covariance_multipoles.argtypes)
     L.coffe_gpu_set_autotune.argtypes = [_p, C.c_int]
     L.coffe_gpu_get_tuning.argtypes = [_p, C.POINTER(Tuning)]
     L.coffe_gpu_set_tuning.argtypes = [_p, C.POINTER(Tuning)]

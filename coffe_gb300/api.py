@@ -388,6 +388,22 @@ class Context:
             "covariance_multipoles")
         return out
 
+    def average_covariance_multipoles(self, k, pk, N, z_min, z_max, fsky, density1, density2,
+                                      pixelsize, ls, sep, contrib=_lib.DEN | _lib.RSD) -> np.ndarray:
+        """Covariance of the redshift-averaged multipoles, shape (n_win, n_l,
+        n_sep, n_l, n_sep) in the reference's (window, l1, r1, l2, r2) order."""
+        k, pk, sep = _f64(k), _f64(pk), _f64(sep)
+        a = _f64(np.atleast_1d(z_min))
+        per_w = [_f64(np.broadcast_to(np.asarray(v, dtype=np.float64), a.shape))
+                 for v in (z_max, fsky, density1, density2, pixelsize)]
+        la = np.ascontiguousarray(ls, dtype=np.int32)
+        out = np.zeros((len(a), len(la), len(sep), len(la), len(sep)))
+        self._check(self._L.coffe_gpu_average_covariance_multipoles(
+            self._ctx, int(contrib), _dptr(k), _dptr(pk), len(k), int(N), len(a), _dptr(a),
+            *map(_dptr, per_w), len(la), _iptr(la), len(sep), _dptr(sep), _dptr(out)),
+            "average_covariance_multipoles")
+        return out
+
     def multipoles_device(self, req_spectrum, req_z_mean, req_offset, sep, ls, out,
                           contrib=_lib.DEN | _lib.RSD, precision="fp64", epsrel=1e-5):
         """Same as :meth:`multipoles` with CUDA tensors (int32, float64, int64,

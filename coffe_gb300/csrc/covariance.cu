@@ -320,18 +320,46 @@ struct CvZ {
     double V, b, f, D1, n1, n2, pix;
 };
 
-// per-z scalars: volume (covariance.c:796-810), bias, growth rate, D1
+#define CV_VOL_PANELS 16
+#define CV_VOL_NODES 16
+// per-z scalars: volume, bias, growth rate, D1.  averaged = 0: bins (z_mean,
+// deltaz) with the shell volume (covariance.c:796-810); averaged = 1: windows
+// (z_min, z_max) at z = (z_min + z_max)/2 with the effective volume
+// 4 pi fsky / int dz / (conformal_H chi^2 (1 + z)) / (H0 h)^2 (covariance.c:
+// 811-840, 150-162), the integral by CV_VOL_PANELS Gauss-Legendre panels of
+// CV_VOL_NODES nodes, uniform in ln z (the integrand rises as 1/chi^2).
 __global__ void cv_zscalars_kernel(int nz, Spl64 chi_of_z, Spl64 f, Spl64 D1, Spl64 bias,
-                                   int has_bias, int contrib, const double *__restrict__ zin,
-                                   CvZ *__restrict__ zs)
+                                   Spl64 confH, double H0h, int has_bias, int contrib,
+                                   int averaged, const double *__restrict__ zin,
+                                   const double *__restrict__ gl, CvZ *__restrict__ zs)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nz) return;
-    // zin: z, deltaz, fsky, density1, density2, pixelsize per z bin
-    const double z = zin[6 * k], dz = zin[6 * k + 1], fsky = zin[6 * k + 2];
-    const double c1 = spl_eval(chi_of_z, z - dz), c2 = spl_eval(chi_of_z, z + dz);
+    // zin per bin: (z_mean, deltaz) or (z_min, z_max), fsky, density1, density2, pixelsize
+    const double za = zin[6 * k], zb = zin[6 * k + 1], fsky = zin[6 * k + 2];
     CvZ o;
-    o.V = 4 * CG_PI * fsky * (pow(c2, 3) - pow(c1, 3)) / 3.;
+    double z;
+    if (averaged) {
+        z = 0.5 * (za + zb);
+        const double la = log(za), dl = (log(zb) - la) / CV_VOL_PANELS;
+        double vint = 0;
+        for (int p = 0; p < CV_VOL_PANELS; ++p) {
+            const double a = exp(la + p * dl), b = exp(la + (p + 1) * dl);
+            const double c = 0.5 * (a + b), h = 0.5 * (b - a);
+            double part = 0;
+            for (int i = 0; i < CV_VOL_NODES; ++i) {
+                const double zz = c + h * gl[i];
+                const double chi = spl_eval(chi_of_z, zz);
+                part += gl[CV_VOL_NODES + i] / (spl_eval(confH, zz) * chi * chi * (1 + zz));
+            }
+            vint += h * part;
+        }
+        o.V = 4 * CG_PI * fsky / vint / (H0h * H0h);
+    } else {
+        z = za;
+        const double c1 = spl_eval(chi_of_z, z - zb), c2 = spl_eval(chi_of_z, z + zb);
+        o.V = 4 * CG_PI * fsky * (pow(c2, 3) - pow(c1, 3)) / 3.;
+    }
     o.b = (contrib & COFFE_GPU_DEN) ? (has_bias ? spl_eval(bias, z) : 1.0) : 0.0;
     o.f = (contrib & COFFE_GPU_RSD) ? spl_eval(f, z) : 0.0;
     o.D1 = spl_eval(D1, z);
@@ -612,15 +640,16 @@ extern "C" int coffe_gpu_covariance_integrals(coffe_gpu_ctx_t *ctx, const double
     return cg_check_device_errors(ctx, "covariance_integrals");
 }
 
-extern "C" int coffe_gpu_covariance_multipoles(coffe_gpu_ctx_t *ctx, int contrib, const double *k,
-                                               const double *pk, size_t nk, size_t N, int n_z,
-                                               const double *z_mean, const double *deltaz,
-                                               const double *fsky, const double *density1,
-                                               const double *density2, const double *pixelsize,
-                                               int n_l, const int *l, int n_sep, const double *sep,
-                                               double *out)
+// shared by coffe_gpu_covariance_multipoles (averaged = 0: za = z_mean,
+// zb = deltaz) and coffe_gpu_average_covariance_multipoles (averaged = 1:
+// za = z_min, zb = z_max)
+static int covariance_impl(coffe_gpu_ctx_t *ctx, int contrib, const double *k, const double *pk,
+                           size_t nk, size_t N, int n_z, int averaged, const double *za,
+                           const double *zb, const double *fsky, const double *density1,
+                           const double *density2, const double *pixelsize, int n_l, const int *l,
+                           int n_sep, const double *sep, double *out)
 {
-    if (!ctx || !k || !pk || !z_mean || !deltaz || !fsky || !density1 || !density2 || !pixelsize ||
+    if (!ctx || !k || !pk || !za || !zb || !fsky || !density1 || !density2 || !pixelsize ||
         !l || !sep || !out || n_z < 1 || n_l < 1 || n_l > 16 || n_sep < 1)
         return COFFE_GPU_EINVAL;
     if (!ctx->bg_ready) {
@@ -631,12 +660,13 @@ extern "C" int coffe_gpu_covariance_multipoles(coffe_gpu_ctx_t *ctx, int contrib
         cg_set_error(ctx, "covariance: contrib must select den and/or rsd");
         return COFFE_GPU_EINVAL;
     }
-    for (int q = 0; q < n_z; ++q)
-        if (!(density1[q] > 0 && density2[q] > 0 && fsky[q] > 0 && pixelsize[q] > 0 &&
-              deltaz[q] >= 0 && z_mean[q] - deltaz[q] >= 0)) {
+    for (int q = 0; q < n_z; ++q) {
+        const bool zok = averaged ? (za[q] > 0 && zb[q] > za[q]) : (zb[q] >= 0 && za[q] - zb[q] >= 0);
+        if (!(density1[q] > 0 && density2[q] > 0 && fsky[q] > 0 && pixelsize[q] > 0 && zok)) {
             cg_set_error(ctx, "covariance: bad survey parameters in redshift bin %d", q);
             return COFFE_GPU_EINVAL;
         }
+    }
     for (int i = 0; i < n_l; ++i)
         if (l[i] < 0 || l[i] > 64) {
             cg_set_error(ctx, "covariance: l = %d out of range", l[i]);
@@ -662,13 +692,16 @@ extern "C" int coffe_gpu_covariance_multipoles(coffe_gpu_ctx_t *ctx, int contrib
                 for (int b = 0; b < 3; ++b)
                     LI[((size_t)i * n_l + j) * 9 + a * 3 + b] = legendre_integral(l[i], l[j], 2 * a, 2 * b);
     for (int q = 0; q < n_z; ++q) {
-        zin[6 * q] = z_mean[q];
-        zin[6 * q + 1] = deltaz[q];
+        zin[6 * q] = za[q];
+        zin[6 * q + 1] = zb[q];
         zin[6 * q + 2] = fsky[q];
         zin[6 * q + 3] = density1[q];
         zin[6 * q + 4] = density2[q];
         zin[6 * q + 5] = pixelsize[q];
     }
+    const size_t n_zin = zin.size();
+    zin.resize(n_zin + 2 * CV_VOL_NODES);
+    gauss_legendre_nodes(CV_VOL_NODES, zin.data() + n_zin, zin.data() + n_zin + CV_VOL_NODES);
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t b_raw = al(sizeof(double) * n_jobs * nss), b_ipk = al(sizeof(double) * n_l * n_l * nss),
                  b_li = al(sizeof(double) * LI.size()), b_zin = al(sizeof(double) * zin.size()),
@@ -700,7 +733,8 @@ extern "C" int coffe_gpu_covariance_multipoles(coffe_gpu_ctx_t *ctx, int contrib
     if ((st = cg_after_launch(ctx, "cv_scale_kernel"))) return st;
     cv_zscalars_kernel<<<(n_z + 127) / 128, 128, 0, ctx->stream>>>(
         n_z, ctx->bg[BG_CHI_OF_Z].v64(), ctx->bg[BG_F].v64(), ctx->bg[BG_D1].v64(),
-        ctx->bias[0].v64(), ctx->bias_set[0], contrib, d_zin, d_zs);
+        ctx->bias[0].v64(), ctx->bg[BG_CONFH].v64(), CG_H0 * ctx->h, ctx->bias_set[0], contrib,
+        averaged, d_zin, d_zin + n_zin, d_zs);
     if ((st = cg_after_launch(ctx, "cv_zscalars_kernel"))) return st;
     const long nout = (long)n_z * n_l * n_l * nss;
     cv_assemble_kernel<<<(unsigned)((nout + 255) / 256), 256, 0, ctx->stream>>>(
@@ -709,4 +743,26 @@ extern "C" int coffe_gpu_covariance_multipoles(coffe_gpu_ctx_t *ctx, int contrib
     CG_CUDA(ctx, cudaMemcpyAsync(out, d_out, sizeof(double) * nout, cudaMemcpyDeviceToHost, ctx->stream));
     CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return cg_check_device_errors(ctx, "covariance_multipoles");
+}
+
+extern "C" int coffe_gpu_covariance_multipoles(coffe_gpu_ctx_t *ctx, int contrib, const double *k,
+                                               const double *pk, size_t nk, size_t N, int n_z,
+                                               const double *z_mean, const double *deltaz,
+                                               const double *fsky, const double *density1,
+                                               const double *density2, const double *pixelsize,
+                                               int n_l, const int *l, int n_sep, const double *sep,
+                                               double *out)
+{
+    return covariance_impl(ctx, contrib, k, pk, nk, N, n_z, 0, z_mean, deltaz, fsky, density1,
+                           density2, pixelsize, n_l, l, n_sep, sep, out);
+}
+
+extern "C" int coffe_gpu_average_covariance_multipoles(
+    coffe_gpu_ctx_t *ctx, int contrib, const double *k, const double *pk, size_t nk, size_t N,
+    int n_win, const double *z_min, const double *z_max, const double *fsky,
+    const double *density1, const double *density2, const double *pixelsize, int n_l,
+    const int *l, int n_sep, const double *sep, double *out)
+{
+    return covariance_impl(ctx, contrib, k, pk, nk, N, n_win, 1, z_min, z_max, fsky, density1,
+                           density2, pixelsize, n_l, l, n_sep, sep, out);
 }

@@ -410,6 +410,21 @@ int coffe_gpu_covariance_multipoles(coffe_gpu_ctx_t *ctx, int contrib, const dou
                                     const double *density2, const double *pixelsize, int n_l,
                                     const int *l, int n_sep, const double *sep, double *out);
 
+/* The covariance of the redshift-averaged multipoles (coffe_covariance_init's
+   average branch, covariance.c:811-840): as coffe_gpu_covariance_multipoles
+   with redshift windows 0 < z_min[w] < z_max[w] in place of (z_mean, deltaz):
+   every window at z = (z_min + z_max)/2 with the effective volume
+   4 pi fsky / int_{z_min}^{z_max} dz / (conformal_H chi^2 (1 + z)) / (H0 h)^2
+   (covariance.c:150-162; the reference's QAG, here 16 Gauss-Legendre panels
+   uniform in ln z).  Output order (window, l1, r1, l2, r2).  Host arrays. */
+int coffe_gpu_average_covariance_multipoles(coffe_gpu_ctx_t *ctx, int contrib,
+                                            const double *k, const double *pk, size_t nk,
+                                            size_t N, int n_win, const double *z_min,
+                                            const double *z_max, const double *fsky,
+                                            const double *density1, const double *density2,
+                                            const double *pixelsize, int n_l, const int *l,
+                                            int n_sep, const double *sep, double *out);
+
 /* Kernel launches issued by this context since creation (for accounting). */
 long long coffe_gpu_launch_count(const coffe_gpu_ctx_t *ctx);
 

@@ -1896,12 +1896,50 @@ int or_covariance_multipoles(const or_model_t *mdl, int contrib, size_t nz, cons
                              const double *sep, const double *ipk, const double *ipk2,
                              double *out)
 {
+    double *V = (double *)malloc(sizeof(double) * nz);
+    if (!V)
+        return -1;
+    for (size_t zk = 0; zk < nz; ++zk) {
+        const double c1 = or_spline_eval(&mdl->chi_of_z, z_mean[zk] - deltaz[zk]);
+        const double c2 = or_spline_eval(&mdl->chi_of_z, z_mean[zk] + deltaz[zk]);
+        V[zk] = 4 * M_PI * fsky[zk] * (pow(c2, 3) - pow(c1, 3)) / 3.;
+    }
+    const int e = or_covariance_multipoles_v(mdl, contrib, nz, z_mean, V, density1, density2,
+                                             pixelsize, nl, ls, nsep, sep, ipk, ipk2, out);
+    free(V);
+    return e;
+}
+
+/* covariance_volume_integrand (covariance.c:150-162) */
+static double avg_volume_integrand(double z, void *vp)
+{
+    const or_model_t *m = (const or_model_t *)vp;
+    const double chi = or_spline_eval(&m->chi_of_z, z);
+    return 1. / or_spline_eval(&m->confH, z) / (chi * chi) / (1 + z);
+}
+
+/* Effective volume of a redshift window for the covariance of the averaged
+   multipoles (covariance.c:811-840): 4 pi fsky / int_{z_min}^{z_max} dz
+   / (conformal_H chi^2 (1 + z)) / (H0 h)^2, the integral by QAG at relative
+   tolerance 1e-5 (integration_1d_prec). */
+double or_average_covariance_volume(const or_model_t *m, double z_min, double z_max, double fsky)
+{
+    const double vint = or_qag61(avg_volume_integrand, (void *)m, z_min, z_max, 0.0, 1e-5,
+                                 OR_QAG_LIMIT, NULL, NULL);
+    return 4 * M_PI * fsky / vint / pow(OR_H0 * m->h, 2);
+}
+
+/* the assembly of covariance.c:842-1059 for bins at redshifts z[] with volumes V[] */
+int or_covariance_multipoles_v(const or_model_t *mdl, int contrib, size_t nz, const double *zbin,
+                               const double *Vbin, const double *density1, const double *density2,
+                               const double *pixelsize, size_t nl, const int *ls, size_t nsep,
+                               const double *sep, const double *ipk, const double *ipk2,
+                               double *out)
+{
     size_t idx = 0;
     for (size_t zk = 0; zk < nz; ++zk) {
-        const double z = z_mean[zk];
-        const double c1 = or_spline_eval(&mdl->chi_of_z, z - deltaz[zk]);
-        const double c2 = or_spline_eval(&mdl->chi_of_z, z + deltaz[zk]);
-        const double V = 4 * M_PI * fsky[zk] * (pow(c2, 3) - pow(c1, 3)) / 3.;
+        const double z = zbin[zk];
+        const double V = Vbin[zk];
         const double b = (contrib & OR_CONTRIB_DEN) ? bias_eval(mdl, 0, z, 1.0) : 0.0;
         const double f = (contrib & OR_CONTRIB_RSD) ? or_spline_eval(&mdl->f, z) : 0.0;
         const double D1 = or_spline_eval(&mdl->D1, z);

@@ -179,6 +179,14 @@ double or_covariance_integral(const double *k, const double *pk, size_t nk, int 
                               double r2, int l1, int l2, double kmin, double kmax, double epsrel,
                               int power_of_spline);
 /* multipole covariance assembly (covariance.c:786-1059), one population */
+/* the assembly for bins at redshifts zbin[] with volumes Vbin[] */
+int or_covariance_multipoles_v(const or_model_t *mdl, int contrib, size_t nz, const double *zbin,
+                               const double *Vbin, const double *density1, const double *density2,
+                               const double *pixelsize, size_t nl, const int *ls, size_t nsep,
+                               const double *sep, const double *ipk, const double *ipk2,
+                               double *out);
+/* effective volume of a redshift window, covariance of the averaged multipoles */
+double or_average_covariance_volume(const or_model_t *m, double z_min, double z_max, double fsky);
 int or_covariance_multipoles(const or_model_t *mdl, int contrib, size_t nz, const double *z_mean,
                              const double *deltaz, const double *fsky, const double *density1,
                              const double *density2, const double *pixelsize, size_t nl, const int *ls, size_t nsep,

@@ -110,6 +110,12 @@ def lib():
         L.or_covariance_multipoles.argtypes = [C.c_void_p, C.c_int, C.c_size_t, _dp, _dp, _dp,
                                                _dp, _dp, _dp, C.c_size_t, _ip, C.c_size_t, _dp,
                                                _dp, _dp, _dp]
+        L.or_covariance_multipoles_v.argtypes = [C.c_void_p, C.c_int, C.c_size_t, _dp, _dp, _dp,
+                                                 _dp, _dp, C.c_size_t, _ip, C.c_size_t, _dp,
+                                                 _dp, _dp, _dp]
+        L.or_average_covariance_volume.argtypes = [C.c_void_p, C.c_double, C.c_double,
+                                                   C.c_double]
+        L.or_average_covariance_volume.restype = C.c_double
         L.or_average_multipoles_batch.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _ip,
                                                   C.c_size_t, C.c_size_t, C.c_size_t,
                                                   C.c_size_t, _dp, C.c_int]
@@ -330,6 +336,27 @@ class Model:
         out = np.zeros(nz * nl * ns * nl * ns)
         lib().or_covariance_multipoles(self._p, contrib, nz, z, *arr, nl, la, ns, sep,
                                        _f64(ipk).ravel(), _f64(ipk2).ravel(), out)
+        return out.reshape(nz, nl, ns, nl, ns)
+
+
+    def average_covariance_multipoles(self, contrib, z_min, z_max, fsky, density, pixelsize, ls,
+                                      sep, ipk, ipk2, density2=None):
+        """Covariance of the redshift-averaged multipoles (window, l1, r1, l2, r2):
+        the bins at (z_min + z_max) / 2 with the windows' effective volumes
+        (covariance.c:811-840)."""
+        a, b = _f64(np.atleast_1d(z_min)), _f64(np.atleast_1d(z_max))
+        nz = len(a)
+        arr = [_f64(np.broadcast_to(np.asarray(x, dtype=np.float64), a.shape))
+               for x in (fsky, density, density if density2 is None else density2, pixelsize)]
+        zb = _f64((a + b) / 2)
+        V = _f64([lib().or_average_covariance_volume(self._p, a[i], b[i], arr[0][i])
+                  for i in range(nz)])
+        la = np.ascontiguousarray(ls, dtype=np.int32)
+        sep = _f64(sep)
+        nl, ns = len(la), len(sep)
+        out = np.zeros(nz * nl * ns * nl * ns)
+        lib().or_covariance_multipoles_v(self._p, contrib, nz, zb, V, arr[1], arr[2], arr[3], nl,
+                                         la, ns, sep, _f64(ipk).ravel(), _f64(ipk2).ravel(), out)
         return out.reshape(nz, nl, ns, nl, ns)
 
 

@@ -45,6 +45,8 @@ def main(ref: Path):
         for b in (0, 2, 4):
             out[f"multipoles_covariance_{a}{b}"] = np.loadtxt(
                 bench / f"benchmark_multipoles_covariance_{a}{b}.dat")
+            out[f"avg_multipoles_covariance_{a}{b}"] = np.loadtxt(
+                bench / f"benchmark_avg_multipoles_covariance_{a}{b}.dat")
     dst = Path(__file__).resolve().parent / "golden.npz"
     np.savez_compressed(dst, **out)
     print(dst, dst.stat().st_size, "bytes")

@@ -99,3 +99,60 @@ def test_covariance_rejects_bad_input(gpu_ctx, cfg5):
         gpu_ctx.covariance_integrals(c["k"], c["pk"], 1000, [(1, 0, 0)], c["sep"][:4])
     with pytest.raises(CoffeGpuError):
         gpu_ctx.covariance_integrals(c["k"], c["pk"], 1024, [(1, 0, 0)], [1e9])
+
+
+def test_average_covariance_multipoles_match_oracle(gpu_ctx, oracle, cfg5):
+    """Covariance of the redshift-averaged multipoles: windows at
+    (z_min + z_max)/2 with their effective volumes, against the oracle's
+    assembly (QAG volume) of the oracle's FFTLog integrals, 1e-10 of each
+    block's largest value."""
+    c, bg = cfg5
+    sep = c["sep"][::5][:16]
+    N, ls = 1024, c["ls"]
+    zmin, zmax = [0.5, 1.0, 0.3], [0.8, 1.5, 1.2]
+    gpu_ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+    got = gpu_ctx.average_covariance_multipoles(c["k"], c["pk"], N, zmin, zmax, 0.2, 1e-3 * H ** 3,
+                                                1e-3 * H ** 3, 50 / H, ls, sep)
+    nl, ns = len(ls), len(sep)
+    ipk = np.zeros((nl, nl, ns, ns))
+    ipk2 = np.zeros_like(ipk)
+    for i, l1 in enumerate(ls):
+        for j, l2 in enumerate(ls):
+            if j < i:
+                continue
+            f = (2 * l1 + 1) * (2 * l2 + 1) / np.pi ** 2
+            ipk[i, j] = oracle.covariance_fftlog(c["k"], c["pk"], 1, l1, l2, N, sep) * 2 * f
+            ipk2[i, j] = oracle.covariance_fftlog(c["k"], c["pk"], 2, l1, l2, N, sep) * f
+    for i in range(nl):
+        for j in range(i):
+            ipk[i, j] = ipk[j, i].T
+            ipk2[i, j] = ipk2[j, i].T
+    m = oracle.Model(bg, H, 0.31)
+    ref = m.average_covariance_multipoles(3, zmin, zmax, 0.2, 1e-3 * H ** 3, 50 / H, ls, sep,
+                                          ipk, ipk2)
+    e = _blockrel(np.moveaxis(got, 3, 2), np.moveaxis(ref, 3, 2))
+    print("average covariance max abs error / block max", e)
+    assert e < 1e-10, e
+
+
+def test_average_covariance_golden_through_gpu(gpu_ctx, golden):
+    """The reference's golden averaged covariance (direct quadrature, z in
+    [0.9, 1.1]) through the FFTLog path at N = 8192, to 1e-2 of each block's
+    largest value, as the plain covariance."""
+    k, pk = golden["pk_class"].T
+    k, pk = k * H, pk / H ** 3
+    sep = np.arange(50, 350, 50) / H
+    gpu_ctx.background_init(0.3, 0.05, 9e-5, H, 10000)
+    got = gpu_ctx.average_covariance_multipoles(k, pk, 8192, [0.9], [1.1], [0.2], [1e-3 * H ** 3],
+                                                [1e-3 * H ** 3], [50 / H], (0, 2, 4), sep)
+    for i, l1 in enumerate((0, 2, 4)):
+        for j, l2 in enumerate((0, 2, 4)):
+            d = golden[f"avg_multipoles_covariance_{l1}{l2}"][:, 2].reshape(6, 6)
+            e = np.abs(got[0, i, :, j, :] - d).max() / np.abs(d).max()
+            print(l1, l2, "max abs error / block max", e)
+            assert e < 1e-2, (l1, l2, e)
+    from coffe_gb300.api import CoffeGpuError
+
+    with pytest.raises(CoffeGpuError):  # z_max <= z_min
+        gpu_ctx.average_covariance_multipoles(k, pk, 1024, [1.1], [0.9], [0.2], [1e-3], [1e-3],
+                                              [50 / H], (0,), sep)

@@ -114,3 +114,22 @@ def test_covariance_fftlog_close_to_direct(golden, oracle, l1, l2):
                                                   power_of_spline=True)
                        for m in range(len(sep))] for n in range(len(sep))]) * np.pi / 2
         assert np.abs(f - q).max() < 3e-2 * np.abs(q).max(), (p, np.abs(f - q).max() / np.abs(q).max())
+
+
+def test_average_covariance_direct_matches_golden(golden, oracle, ref_bg):
+    """Covariance of the redshift-averaged multipoles (covariance.c:811-840:
+    the bin at (z_min + z_max) / 2 with the window's effective volume
+    4 pi fsky / int dz / (conformal_H chi^2 (1 + z)) / (H0 h)^2) at the
+    reference test's settings (test_coffe.py:433-470: z in [0.9, 1.1], the rest
+    as test_covariance_direct_matches_golden), standard integration method."""
+    k, pk, sep, ls = _golden_setup(golden)
+    m = oracle.Model(ref_bg, H, 0.3)
+    ipk, ipk2 = _direct_integrals(oracle, k, pk, sep, ls)
+    cov = m.average_covariance_multipoles(3, [0.9], [1.1], [0.2], [1e-3 * H ** 3], [50 / H], ls,
+                                          sep, ipk, ipk2)
+    for i, l1 in enumerate(ls):
+        for j, l2 in enumerate(ls):
+            d = golden[f"avg_multipoles_covariance_{l1}{l2}"]
+            assert np.allclose(d[:, 0] / H, np.repeat(sep, len(sep)))
+            assert np.allclose(cov[0, i, :, j, :].ravel(), d[:, 2], rtol=5e-4), (
+                l1, l2, cov[0, i, :, j, :].ravel() / d[:, 2] - 1)
