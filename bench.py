@@ -78,7 +78,7 @@ def parse():
     p.add_argument("--launch-config", default=None,
                    help="fixed launch configuration instead of autotuning, e.g. "
                         "fft_threads=512,fft_radix=4,fft_swizzle=1,spline_group=8,"
-                        "lane_threads=128,lane_unroll=2 (for profiling runs)")
+                        "lane_threads=128,lane_unroll=2,fft_threads_fwd=256 (profiling runs)")
     p.add_argument("--kernel-only", choices=["mixed", "fp64", "tables-mixed", "tables-fp64"],
                    default=None,
                    help="profiling aid: run only the multipole kernel (mixed/fp64) or only the "

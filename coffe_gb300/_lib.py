@@ -90,6 +90,7 @@ class Tuning(C.Structure):
         ("spline_group", C.c_int),
         ("lane_threads", C.c_int),
         ("lane_unroll", C.c_int),
+        ("fft_threads_fwd", C.c_int),
     ]
 
 

@@ -147,7 +147,7 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
                       &ctx->samp_f32, &ctx->csfac32,
                       &ctx->lens_rule, &ctx->lens_rec, &ctx->lens_part,
                       &ctx->cov_buf,  &ctx->cov_out, &ctx->adj_buf, &ctx->csband,
-                      &ctx->samp_tdf, &ctx->qfac_df, &ctx->pk_df, &ctx->chitab32,
+                      &ctx->samp_tdf, &ctx->qfac_df, &ctx->pk_df, &ctx->mp_bgfit,
                       &ctx->cf_rule, &ctx->avg_buf};
     spline_free(ctx->cov_pk);
     for (DevBuf *b : bufs) cg_release(*b);
@@ -303,12 +303,15 @@ int coffe_gpu_set_tuning(coffe_gpu_ctx_t *ctx, const coffe_gpu_tuning_t *t)
 {
     if (!ctx || !t) return COFFE_GPU_EINVAL;
     const int ft = t->fft_threads, lt = t->lane_threads, g = t->spline_group;
+    const int ff = t->fft_threads_fwd;
     if (!(ft == 128 || ft == 256 || ft == 512 || ft == 1024) ||
+        !(ff == 128 || ff == 256 || ff == 512 || ff == 1024) ||
         !(t->fft_radix == 2 || t->fft_radix == 4) || !(t->fft_swizzle == 0 || t->fft_swizzle == 1) ||
         !(g == 2 || g == 4 || g == 8) || !(lt == 64 || lt == 128 || lt == 256) ||
         !(t->lane_unroll == 1 || t->lane_unroll == 2)) {
-        cg_set_error(ctx, "set_tuning: fft_threads 128/256/512/1024, fft_radix 2/4, fft_swizzle "
-                          "0/1, spline_group 2/4/8, lane_threads 64/128/256, lane_unroll 1/2");
+        cg_set_error(ctx, "set_tuning: fft_threads(_fwd) 128/256/512/1024, fft_radix 2/4, "
+                          "fft_swizzle 0/1, spline_group 2/4/8, lane_threads 64/128/256, "
+                          "lane_unroll 1/2");
         return COFFE_GPU_EINVAL;
     }
     ctx->tuning = *t;

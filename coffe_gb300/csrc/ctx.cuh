@@ -42,12 +42,8 @@ struct coffe_gpu_ctx {
     bool z_uniform = false;
     double z0 = 0, zn = 0, dz = 0;
     DevBuf zrec64, zrec32;
-    // mixed path: D1 and f D1 on a uniform chi grid (linear cells, two guard cells)
-    DevBuf chitab32;
     DevBuf cf_rule; // mu list + line rules of the last coffe_gpu_corrfunc call with lensing
     DevBuf avg_buf; // expanded requests of coffe_gpu_average_multipoles
-    int chi_cells = 0;
-    double chi_lo = 0, chi_hi = 0;
     SplineBuf bias[4];
     bool bias_set[4] = {false, false, false, false};
     std::vector<double> bias_host[4]; // (z, value) samples as set, for symmetry checks
@@ -58,8 +54,8 @@ struct coffe_gpu_ctx {
     int n_spectra = 0, n_terms = 0, int_precision = 0;
 
     // ---- launch shapes (coffe_gpu_set_tuning / benchmark-mode autotuning)
-    coffe_gpu_tuning_t tuning = {512, 4, 0, 8, 256, 1}; // default configuration
-    coffe_gpu_tuning_t last_tuning = {512, 4, 0, 8, 256, 1};
+    coffe_gpu_tuning_t tuning = {512, 4, 1, 8, 128, 2, 512}; // default configuration
+    coffe_gpu_tuning_t last_tuning = {512, 4, 1, 8, 128, 2, 512};
     bool autotune = false;
     std::map<std::array<long long, 6>, coffe_gpu_tuning_t> tune_cache; // shape -> choice
     size_t N = 0, nk = 0;
@@ -102,6 +98,7 @@ struct coffe_gpu_ctx {
     // ---- multipole request staging (host-pointer calls) and retry list
     DevBuf req_buf;
     DevBuf mp_retry;
+    DevBuf mp_bgfit; // per-request background polynomials of the mixed fast kernel
     // first-panel node tables, one per (multipole list, precision, layout):
     // each is written once and never overwritten while fewer than
     // CG_NODE_SLOTS distinct tables are in use, so a captured launch that

@@ -1145,7 +1145,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
         CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_df_kernel<R, W>,                         \
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
-        fftlog_forward_df_kernel<R, W><<<gf, tu.fft_threads, smem, ctx->stream>>>(                \
+        fftlog_forward_df_kernel<R, W><<<gf, tu.fft_threads_fwd, smem, ctx->stream>>>(            \
             g, (const float2 *)ctx->pk_df.p, (const float *)ctx->csc.p,                           \
             (const int *)ctx->samp_idx.p, (const float2 *)ctx->samp_tdf.p,                        \
             (const float4 *)ctx->samp_f32.p, (const float2 *)ctx->qfac_df.p, wdf,                 \
@@ -1173,7 +1173,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_kernel,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        fftlog_forward_kernel<<<gf, tu.fft_threads, smem, ctx->stream>>>(
+        fftlog_forward_kernel<<<gf, tu.fft_threads_fwd, smem, ctx->stream>>>(
             g, (const double *)ctx->kgrid.p, d_pk, (const double *)ctx->csc.p,
             (const double *)ctx->csfac.p, (const int *)ctx->samp_idx.p,
             (const double *)ctx->samp_dx.p, (const double *)ctx->qfac.p, modew,
@@ -1187,12 +1187,14 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     };
     // candidate launch shapes of this table stage
     std::vector<coffe_gpu_tuning_t> cands;
+    for (int ff : {256, 512})
     for (int ft : {128, 256, 512})
         for (int rad : {2, 4})
             for (int sw : {0, 1})
                 for (int grp : {2, 4, 8}) {
                     coffe_gpu_tuning_t c = ctx->tuning;
                     c.fft_threads = ft;
+                    c.fft_threads_fwd = ff;
                     if (mixed) {
                         if (sw && M < 64) continue;
                         c.fft_radix = rad;
@@ -1208,6 +1210,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     if ((st = cg_tuned(ctx, key, cands, stage, &tu))) return st;
     if ((st = stage(tu))) return st;
     ctx->last_tuning.fft_threads = tu.fft_threads;
+    ctx->last_tuning.fft_threads_fwd = tu.fft_threads_fwd;
     if (mixed) {
         ctx->last_tuning.fft_radix = tu.fft_radix;
         ctx->last_tuning.fft_swizzle = tu.fft_swizzle;

@@ -619,9 +619,14 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
 // biases (so equal tracers and, with even multipoles, the 31-node mirror
 // rule), density and/or RSD without the only-cross switch.  Two changes
 // against mp_lane_kernel, both exact rearrangements up to float rounding:
-//  * background: D1 and f D1 read from one uniform-chi table of linear cells
-//    (16384 cells over the background's chi range: interpolation error
-//    ~h^2 y''/8, about 1e-8 relative), instead of z(chi) and then f(z), D1(z);
+//  * background: D1 and f D1 along the line of sight of a request as one
+//    degree-5 polynomial each in t = x / X around the request's mean distance
+//    (chi = chi_mean + x, |x| <= X = half its largest separation, clamped to
+//    the background's range), interpolated at six Chebyshev points from the
+//    float background splines by mp_bgfit_kernel; a node evaluates the even and
+//    odd parts in t^2 (both ends from one evaluation, no loads).  Error: the
+//    interpolation's ~(X/L)^6 of the background's scale L ~ Gpc (1e-8 at
+//    X = 190 Mpc) plus the splines' float rounding, ~1e-7 relative;
 //  * integrand: with G = D1 and F = f D1 at both ends, xi g1 g2 becomes
 //      G1 G2 I00 + F1 F2 R(c) + (G1 F2 + F1 G2)(I00 - 2 I02)/3
 //      + g I02 (G1 F2 chi1^2 + F1 G2 chi2^2),       g = (2 - s)(1 - mu^2)/D,
@@ -629,25 +634,98 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
 //           + (a2 c^2 + a1 c + a0) I04/35,
 //    where the mu-only coefficients a_i, b_i of the RSD polynomials (functions.c
 //    :129-134 as rewritten for Xi::combine) sit in the node table.
-#define MP_CHI_CELLS 16384
 
-// Uniform-chi cells: u = (chi - chi_lo)/h - 1/2 in [-1/2, cells - 1/2];
-// record 1 + round(u) holds (G, dG, F, dF) at the cell centre (record 0 and
-// cells + 1 are guards), t = u - round(u) in [-1/2, 1/2].
-struct ChiTab {
-    const float4 *rec;
-    float inv_h, off, umax;
+// Per-request background polynomials: G(chi_mean + X t) = ge(t^2) + t go(t^2),
+// F likewise, ge = (c0, c2, c4), go = (c1, c3, c5) in t; the fourth lanes hold
+// 1/X, chi_mean, X.
+struct BgFit {
+    float4 ge, go, fe, fo; // (c0,c2,c4,1/X) (c1,c3,c5,chi_mean) (d0,d2,d4,X) (d1,d3,d5,-)
 };
 
-__device__ __forceinline__ void chi_cell(const ChiTab &ct, float chi, float &G, float &F)
+// the Chebyshev points t_j = cos((2j + 1) pi / 12), j < 6, and the inverse of
+// their Vandermonde matrix (monomial coefficients from the six values), both
+// computed on the host in FP64
+struct FitInv {
+    float t[6];
+    float m[6][6];
+};
+
+// one warp per request (MP_FIT_WARPS per block): the largest separation, the
+// background at the six Chebyshev points (lanes 0-5, the float background
+// splines, as mp_lane_kernel reads them), then the coefficients (lanes 0-11:
+// D1 and f D1) as rows of the inverse Vandermonde
+#define MP_FIT_WARPS 4
+__global__ void __launch_bounds__(32 * MP_FIT_WARPS)
+    mp_bgfit_kernel(Spl32 chi_of_z, Spl32 z_of_chi, Spl32 D1, Spl32 f, int n_req, FitInv vinv,
+                    const double *__restrict__ req_z_mean, const int64_t *__restrict__ req_offset,
+                    const double *__restrict__ sep, BgFit *__restrict__ fit)
 {
-    const float big = 12582912.f; // 1.5 * 2^23: round-to-nearest integer for |u| < 2^22
-    const float u = fminf(fmaxf(fmaf(chi, ct.inv_h, ct.off), -1.f), ct.umax);
-    const float rb = __fadd_rn(u, big);
-    const float t = __fadd_rn(u, -__fadd_rn(rb, -big));
-    const float4 c = __ldg(ct.rec + 1 + (__float_as_int(rb) - 0x4B400000));
-    G = fmaf(t, c.y, c.x);
-    F = fmaf(t, c.w, c.z);
+    __shared__ float val[MP_FIT_WARPS][12];
+    __shared__ float cof[MP_FIT_WARPS][12];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int q = blockIdx.x * MP_FIT_WARPS + w;
+    if (q >= n_req) return; // whole warps leave together
+    float rmax = 0.f;
+    for (long long i = req_offset[q] + lane; i < req_offset[q + 1]; i += 32)
+        rmax = fmaxf(rmax, f32_of_bits(sep[i]));
+    for (int o = 16; o > 0; o >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    const float chim = spl_eval(chi_of_z, f32_of_bits(req_z_mean[q]));
+    float X = fminf(0.5f * rmax, fminf(chim - z_of_chi.x0, z_of_chi.xn - chim));
+    if (!(X > 1e-3f)) X = 1e-3f; // empty request or no room: its pairs are outside anyway
+    if (lane < 6) {
+        const float z = spl_eval(z_of_chi, fmaf(X, vinv.t[lane], chim));
+        const float g = spl_eval(D1, z);
+        val[w][lane] = g;
+        val[w][6 + lane] = spl_eval(f, z) * g;
+    }
+    __syncwarp();
+    if (lane < 12) {
+        const int c = lane % 6, off = lane < 6 ? 0 : 6;
+        float acc = 0.f;
+        for (int k = 0; k < 6; ++k) acc = fmaf(vinv.m[c][k], val[w][off + k], acc);
+        cof[w][lane] = acc;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        const float *c = cof[w];
+        BgFit o;
+        o.ge = make_float4(c[0], c[2], c[4], 1.f / X);
+        o.go = make_float4(c[1], c[3], c[5], chim);
+        o.fe = make_float4(c[6], c[8], c[10], X);
+        o.fo = make_float4(c[7], c[9], c[11], 0.f);
+        fit[q] = o;
+    }
+}
+
+// the inverse Vandermonde matrix of the six Chebyshev points (host, FP64)
+FitInv fit_inverse()
+{
+    FitInv r;
+    double V[6][12];
+    for (int j = 0; j < 6; ++j) {
+        const double t = cos((2 * j + 1) * CG_PI / 12.0);
+        double p = 1.0;
+        for (int c = 0; c < 6; ++c, p *= t) V[j][c] = p;
+        for (int c = 0; c < 6; ++c) V[j][6 + c] = (c == j) ? 1.0 : 0.0;
+    }
+    for (int c = 0; c < 6; ++c) { // Gauss-Jordan with partial pivoting
+        int piv = c;
+        for (int r2 = c + 1; r2 < 6; ++r2)
+            if (fabs(V[r2][c]) > fabs(V[piv][c])) piv = r2;
+        for (int k = 0; k < 12; ++k) std::swap(V[c][k], V[piv][k]);
+        const double d = V[c][c];
+        for (int k = 0; k < 12; ++k) V[c][k] /= d;
+        for (int r2 = 0; r2 < 6; ++r2)
+            if (r2 != c) {
+                const double m = V[r2][c];
+                for (int k = 0; k < 12; ++k) V[r2][k] -= m * V[c][k];
+            }
+    }
+    for (int j = 0; j < 6; ++j) {
+        r.t[j] = (float)cos((2 * j + 1) * CG_PI / 12.0);
+        for (int k = 0; k < 6; ++k) r.m[j][k] = (float)V[j][6 + k];
+    }
+    return r;
 }
 
 // node table of mp_fast_kernel, rows mu >= 0 ascending:
@@ -663,7 +741,7 @@ template <int NL> struct FastLayout {
 #define MP_FAST_MAX_THREADS 256
 template <int NL, int CONTRIB, int UNROLL>
 __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
-    mp_fast_kernel(MpArgs a, ChiTab ct, float chi_lo, float chi_hi, Spl32 chi_of_z,
+    mp_fast_kernel(MpArgs a, const BgFit *__restrict__ fit, float chi_lo, float chi_hi,
                    const float *__restrict__ tab_x, const float *__restrict__ tab_y,
                    const int *__restrict__ req_spectrum, const double *__restrict__ req_z_mean,
                    const int64_t *__restrict__ req_offset, const double *__restrict__ sep,
@@ -683,7 +761,8 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
     const int s = req_spectrum[q];
     // double -> float without the FP64 pipe (1/64 of the FP32 rate)
     const float r = f32_of_bits(sep[item]);
-    const float chim = spl_eval(chi_of_z, f32_of_bits(req_z_mean[q]));
+    const BgFit bf = fit[q];
+    const float chim = bf.go.w;
     const float *y0 = tab_y + ((size_t)s * a.n_terms) * a.tab_len;
     const float idl = f32_of_bits(a.inv_dlog);
     const int tl = a.tab_len;
@@ -703,15 +782,21 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
         const float e00 = I00 * (1.f / 15.f), e02 = I02 * (1.f / 21.f), e04 = I04 * (1.f / 35.f);
         const float e00x2 = 2.f * e00, e0d = e00 - e02;
         const float K1 = (I00 - 2.f * I02) * (1.f / 3.f);
+        const float rho = half_r * bf.ge.w; // t = mu rho in [-1, 1] for inside pairs
 #pragma unroll UNROLL
         for (int k = 0; k < LY::ROWS; ++k) {
             float rec[LY::R1];
             lds_rec<LY::R1>(tab1 + k * LY::R1, rec);
             const float mu = rec[0], mu2 = rec[1], omm = rec[2];
             const float chi1 = fmaf(-mu, half_r, chim), chi2 = fmaf(mu, half_r, chim);
-            float G1, F1, G2, F2;
-            chi_cell(ct, chi1, G1, F1);
-            chi_cell(ct, chi2, G2, F2);
+            // background at chi_mean -/+ mu r/2: even and odd parts in t
+            const float t = mu * rho, u = t * t;
+            const float gE = fmaf(fmaf(bf.ge.z, u, bf.ge.y), u, bf.ge.x);
+            const float gO = fmaf(fmaf(bf.go.z, u, bf.go.y), u, bf.go.x);
+            const float fE = fmaf(fmaf(bf.fe.z, u, bf.fe.y), u, bf.fe.x);
+            const float fO = fmaf(fmaf(bf.fo.z, u, bf.fo.y), u, bf.fo.x);
+            const float G1 = fmaf(-t, gO, gE), G2 = fmaf(t, gO, gE);
+            const float F1 = fmaf(-t, fO, fE), F2 = fmaf(t, fO, fE);
             const float D = fmaf(-mu2, Br, A2); // 2 chi1 chi2
             const float inv_D = __fdividef(1.f, D);
             const float sv = r2 * omm * inv_D;
@@ -758,22 +843,6 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
     }
     first_panel_out<NL, float>(a, f32_of_bits(a.epsrel), item, finite, K, G, A, asc, out,
                                retry_count, retry, err);
-}
-
-__global__ void chitab_kernel(Spl64 z_of_chi, Spl64 D1, Spl64 f, double lo, double hi, int cells,
-                              float4 *__restrict__ rec)
-{
-    const int k = blockIdx.x * blockDim.x + threadIdx.x; // record k: cell k - 1
-    if (k >= cells + 2) return;
-    const int i = min(max(k - 1, 0), cells - 1);
-    const double h = (hi - lo) / cells;
-    const double xa = lo + i * h, xb = i == cells - 1 ? hi : fmin(lo + (i + 1) * h, hi);
-    const double za = spl_eval(z_of_chi, xa), zb = spl_eval(z_of_chi, xb);
-    const double ga = spl_eval(D1, za), gb = spl_eval(D1, zb);
-    const double fa = spl_eval(f, za) * ga, fb = spl_eval(f, zb) * gb;
-    const double sh = (double)(k - 1 - i); // -1 / +1 in the guards: the edge cell's line
-    rec[k] = make_float4((float)(0.5 * (ga + gb) + sh * (gb - ga)), (float)(gb - ga),
-                         (float)(0.5 * (fa + fb) + sh * (fb - fa)), (float)(fb - fa));
 }
 
 // ------------------------------------------------- correlation function
@@ -940,15 +1009,21 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<float, Spl32> &bg,
                        },
                        &dn);
     if (st) return st;
-    const double inv_h = ctx->chi_cells / (ctx->chi_hi - ctx->chi_lo);
-    const ChiTab ct{(const float4 *)ctx->chitab32.p, (float)inv_h,
-                    (float)(-ctx->chi_lo * inv_h - 0.5), (float)ctx->chi_cells};
+    if ((st = cg_ensure(ctx, ctx->mp_bgfit, sizeof(BgFit) * (size_t)a.n_req))) return st;
+    BgFit *d_fit = (BgFit *)ctx->mp_bgfit.p;
+    static const FitInv vinv = fit_inverse();
     const int contrib = a.contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD);
     // first panel (with lt threads per block) and the adaptive retries
     auto run = [&](const coffe_gpu_tuning_t &tu) -> int {
         const int lt = tu.lane_threads;
         const long long blocks = (total + lt - 1) / lt;
         CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
+        mp_bgfit_kernel<<<(a.n_req + MP_FIT_WARPS - 1) / MP_FIT_WARPS, 32 * MP_FIT_WARPS, 0,
+                          ctx->stream>>>(ctx->bg[BG_CHI_OF_Z].v32(), ctx->bg[BG_Z_OF_CHI].v32(),
+                                         ctx->bg[BG_D1].v32(), ctx->bg[BG_F].v32(), a.n_req,
+                                         vinv, req_z_mean, req_offset, sep, d_fit);
+        int s1 = cg_after_launch(ctx, "mp_bgfit_kernel");
+        if (s1) return s1;
 #define MP_FAST_U(NLV, CV, UV)                                                                    \
     {                                                                                             \
         const size_t smem = sizeof(float) * (FastLayout<NLV>::COUNT + FastLayout<NLV>::ROWS * lt); \
@@ -956,7 +1031,7 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<float, Spl32> &bg,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,            \
                                           (int)smem));                                            \
         mp_fast_kernel<NLV, CV, UV><<<(unsigned)blocks, lt, smem, ctx->stream>>>(                 \
-            a, ct, bg.z_of_chi.x0, bg.z_of_chi.xn, chi_of_z, tab_x, tab_y, req_spectrum,          \
+            a, d_fit, bg.z_of_chi.x0, bg.z_of_chi.xn, tab_x, tab_y, req_spectrum,                 \
             req_z_mean, req_offset, sep, total, (const float *)dn, out, d_count, d_retry,         \
             ctx->d_err);                                                                          \
     }
@@ -1098,20 +1173,6 @@ int multipoles_prepare_background(coffe_gpu_ctx *ctx)
     CG_CUDA(ctx, cudaMemcpyAsync(z.data(), ctx->bg_nodes.p, sizeof(double) * n,
                                  cudaMemcpyDeviceToHost, ctx->stream));
     CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    {
-        // mixed-path chi table over the z(chi) spline's knots
-        ctx->chi_cells = 0;
-        const SplineBuf &zc = ctx->bg[BG_Z_OF_CHI];
-        int st = cg_ensure(ctx, ctx->chitab32, sizeof(float4) * (MP_CHI_CELLS + 2));
-        if (st) return st;
-        chitab_kernel<<<(MP_CHI_CELLS + 2 + 255) / 256, 256, 0, ctx->stream>>>(
-            zc.v64(), ctx->bg[BG_D1].v64(), ctx->bg[BG_F].v64(), zc.x0, zc.xn, MP_CHI_CELLS,
-            (float4 *)ctx->chitab32.p);
-        if ((st = cg_after_launch(ctx, "chitab_kernel"))) return st;
-        ctx->chi_cells = MP_CHI_CELLS;
-        ctx->chi_lo = zc.x0;
-        ctx->chi_hi = zc.xn;
-    }
     const double dz = (z[n - 1] - z[0]) / (n - 1);
     bool uni = dz > 0;
     for (int i = 0; i < n && uni; ++i)
@@ -1234,7 +1295,7 @@ static int multipoles_nonintegrated(coffe_gpu_ctx *ctx, const MpArgs &a, int pre
         bg.dz = (float)ctx->dz;
         bg.inv_dz = (float)(1.0 / ctx->dz);
         bg.nz = ctx->bg_bins;
-        bool fast = ctx->chi_cells > 0 && a.n_l <= 4 && !ctx->bias_set[0] && !ctx->bias_set[1] &&
+        bool fast = a.n_l <= 4 && !ctx->bias_set[0] && !ctx->bias_set[1] &&
                     !(a.contrib & COFFE_GPU_ONLY_CROSS);
         for (int j = 0; j < a.n_l; ++j) fast = fast && a.ls[j] % 2 == 0;
         if (fast)

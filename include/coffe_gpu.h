@@ -321,12 +321,13 @@ long long coffe_gpu_multipoles_retries(coffe_gpu_ctx_t *ctx);
    biases.  Every choice gives the same results except fft_radix, which changes
    the rounding of the double-float transforms (by ~1e-14 relative). */
 typedef struct {
-    int fft_threads;  /* threads per block of the FFTLog transforms: 128, 256, 512 or 1024 */
+    int fft_threads;  /* threads per block of the FFTLog inverse transforms: 128, 256, 512, 1024 */
     int fft_radix;    /* 2 or 4: stages of the mixed-precision (double-float) transforms */
     int fft_swizzle;  /* 0 or 1: XOR-swizzled shared-memory layout of those transforms */
     int spline_group; /* 2, 4 or 8 spectra per block of the mixed-precision spline pass */
     int lane_threads; /* 64, 128 or 256 threads per block of the mixed multipole kernel */
     int lane_unroll;  /* 1 or 2 quadrature nodes per step of that kernel's node loop */
+    int fft_threads_fwd; /* threads per block of the forward transforms: 128 .. 1024 */
 } coffe_gpu_tuning_t;
 
 /* enable != 0 switches on benchmark mode: the first table build and the first

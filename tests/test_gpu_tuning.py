@@ -29,7 +29,7 @@ def setup():
 
 
 DEFAULT = dict(fft_threads=512, fft_radix=4, fft_swizzle=0, spline_group=8, lane_threads=256,
-               lane_unroll=1)
+               lane_unroll=1, fft_threads_fwd=512)
 
 
 def _tables(ctx, b, precision, **cfg):
@@ -54,7 +54,8 @@ def test_table_configurations_agree(setup):
             for sw in (0, 1):
                 for grp in (2, 4, 8):
                     got = _tables(ctx, b, "mixed", fft_threads=ft, fft_radix=rad,
-                                  fft_swizzle=sw, spline_group=grp)
+                                  fft_swizzle=sw, spline_group=grp,
+                                  fft_threads_fwd=(256 if grp == 4 else 512))
                     assert np.array_equal(np.isfinite(got), fin)
                     if rad == DEFAULT["fft_radix"]:
                         assert np.array_equal(got[fin], ref[fin]), (ft, rad, sw, grp)
@@ -64,7 +65,7 @@ def test_table_configurations_agree(setup):
                         assert e < 1e-7, (ft, rad, sw, grp, e)
     ref64 = _tables(ctx, b, "fp64")
     for ft in (128, 256):
-        got = _tables(ctx, b, "fp64", fft_threads=ft)
+        got = _tables(ctx, b, "fp64", fft_threads=ft, fft_threads_fwd=ft)
         assert np.array_equal(got, ref64, equal_nan=True), ft
 
 
@@ -121,7 +122,8 @@ def test_set_tuning_rejects_bad_values(setup):
 
     ctx, _ = setup
     for bad in (dict(fft_threads=384), dict(fft_radix=8), dict(fft_swizzle=2),
-                dict(spline_group=3), dict(lane_threads=32), dict(lane_unroll=4)):
+                dict(spline_group=3), dict(lane_threads=32), dict(lane_unroll=4),
+                dict(fft_threads_fwd=100)):
         with pytest.raises(CoffeGpuError):
             ctx.set_tuning(**{**DEFAULT, **bad})
     with pytest.raises(ValueError):
