@@ -166,6 +166,20 @@ def cpu_eval(batch, n_spectra, nthreads):
     return b.n_evals, dt, out
 
 
+def reduce_over_ranks(torch, values, world, device):
+    """Each timing's maximum over the ranks: the slowest replica sets the job's time."""
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return t.tolist()
+
+
+def job_throughput(evals_per_rank, steps, world, seconds):
+    """Whole-job evaluations per second: every rank evaluates its own batch
+    (independent replicas, no exchange), all within `seconds`."""
+    return evals_per_rank * steps * world / seconds
+
+
 def reference_arm(args, rank, world):
     from coffe_gb300 import workloads
 
@@ -492,21 +506,18 @@ def ours(args, rank, world, local_rank):
         ctx.set_stream(stream.cuda_stream)
 
     # reduce over ranks (max time)
-    times = torch.tensor([dev_mixed, dev_fp64, kern_s], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
-    dev_mixed, dev_fp64, kern_s = times.tolist()
+    dev_mixed, dev_fp64, kern_s = reduce_over_ranks(torch, [dev_mixed, dev_fp64, kern_s], world,
+                                                    dev)
     if e2e is not None and world > 1:
-        t = torch.tensor([e2e["ms_per_step"]], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e["ms_per_step"] = float(t.item())
-        e2e["value"] = n_evals * world / (e2e["ms_per_step"] * 1e-3)
+        (ms,) = reduce_over_ranks(torch, [e2e["ms_per_step"]], world, dev)
+        e2e["ms_per_step"] = ms
+        e2e["value"] = job_throughput(n_evals, 1, world, ms * 1e-3)
     if rank != 0:
         ctx.close()
         return
 
-    value = n_evals * args.steps * world / dev_mixed
-    fp64_value = n_evals * k64 * world / dev_fp64
+    value = job_throughput(n_evals, args.steps, world, dev_mixed)
+    fp64_value = job_throughput(n_evals, k64, world, dev_fp64)
     sgemm = measure_gemm_peak(torch, torch.float32)
     achieved = flop_launch / kern_s / 1e12
     peaks = {}
