@@ -195,15 +195,69 @@ template <typename T> struct Acc {
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
+// Mixed path: the lensing kernel D1(z(lambda)) / a(z(lambda)) along each side's
+// line of sight, lambda = chi_i x, x in [0, 1], as a degree-9 polynomial in
+// t = 2x - 1, interpolated at ten Chebyshev points (float background splines;
+// the function's Chebyshev tail is at the splines' 5e-9 noise from degree 9
+// for z <= 2.5).  The monomial coefficients are formed in FP64 from the inverse
+// Vandermonde matrix of the points (host, FP64), so their cancellation is
+// exact before they are rounded to float.
+#define LENS_PDEG 9
+struct LensPoly {
+    float t[LENS_PDEG + 1];
+    double vinv[LENS_PDEG + 1][LENS_PDEG + 1];
+};
+
+LensPoly lens_poly_tables()
+{
+    const int n = LENS_PDEG + 1;
+    LensPoly r;
+    double V[LENS_PDEG + 1][2 * (LENS_PDEG + 1)];
+    for (int j = 0; j < n; ++j) {
+        const double t = cos((2 * j + 1) * CG_PI / (2.0 * n));
+        r.t[j] = (float)t;
+        double p = 1.0;
+        for (int c = 0; c < n; ++c, p *= t) V[j][c] = p;
+        for (int c = 0; c < n; ++c) V[j][n + c] = c == j ? 1.0 : 0.0;
+    }
+    for (int c = 0; c < n; ++c) { // Gauss-Jordan with partial pivoting
+        int piv = c;
+        for (int r2 = c + 1; r2 < n; ++r2)
+            if (fabs(V[r2][c]) > fabs(V[piv][c])) piv = r2;
+        for (int k = 0; k < 2 * n; ++k) std::swap(V[c][k], V[piv][k]);
+        const double d = V[c][c];
+        for (int k = 0; k < 2 * n; ++k) V[c][k] /= d;
+        for (int r2 = 0; r2 < n; ++r2)
+            if (r2 != c) {
+                const double m = V[r2][c];
+                for (int k = 0; k < 2 * n; ++k) V[r2][k] -= m * V[c][k];
+            }
+    }
+    for (int j = 0; j < n; ++j)
+        for (int k = 0; k < n; ++k) r.vinv[j][k] = V[j][n + k];
+    return r;
+}
+
+__device__ __forceinline__ float lens_horner(const float *c, float t)
+{
+    float v = c[LENS_PDEG];
+#pragma unroll
+    for (int k = LENS_PDEG - 1; k >= 0; --k) v = fmaf(v, t, c[k]);
+    return v;
+}
+
 template <typename T, typename S, typename TT>
 __global__ void __launch_bounds__(LENS_THREADS)
-    lens_double_kernel(LensArgs a, LensBg64 g64, LensBgT<S> gT, const TT *__restrict__ tab_x,
+    lens_double_kernel(LensArgs a, LensBg64 g64, LensBgT<S> gT, LensPoly poly,
+                       const TT *__restrict__ tab_x,
                        const typename Rec4<TT>::type *__restrict__ rec,
                        const int *__restrict__ req_spectrum, const double *__restrict__ req_z_mean,
                        const int64_t *__restrict__ req_offset, const double *__restrict__ sep,
                        const double *__restrict__ rule, double *__restrict__ part, int *err)
 {
     __shared__ double red[LENS_THREADS / 32];
+    __shared__ float gval[2][LENS_PDEG + 1];
+    __shared__ float gcoef[2][LENS_PDEG + 1];
     const long long item = blockIdx.x;
     const long long pair = a.pair0 + item / a.n_mu;
     const int im = (int)(item % a.n_mu);
@@ -219,13 +273,38 @@ __global__ void __launch_bounds__(LENS_THREADS)
     const T chi1 = (T)G.chi1, chi2 = (T)G.chi2, ss = (T)G.s, ct = (T)G.ct, c2m = (T)(-G.omc2);
     const T i11_0 = (T)lens_at_zero<TT>(recs, L11);
     const TT inv_dlog = (TT)a.inv_dlog;
+    constexpr bool F32 = sizeof(T) == 4;
+    // mixed path: float copies of the line rules follow the FP64 rule
+    const float *xf32 = reinterpret_cast<const float *>(xh + 2 * a.nh);
+    const float *wf32 = xf32 + a.n_x, *xh32 = wf32 + a.n_x, *wh32 = xh32 + a.nh;
+    if (F32) { // D1 / a along both lines of sight as polynomials in 2x - 1
+        if (threadIdx.x < 2 * (LENS_PDEG + 1)) {
+            const int side = threadIdx.x / (LENS_PDEG + 1), j = threadIdx.x % (LENS_PDEG + 1);
+            const float lam = (float)(side ? G.chi2 : G.chi1) * 0.5f * (poly.t[j] + 1.f);
+            const float zz = spl_eval(gT.z_of_chi, (T)lam);
+            gval[side][j] = (float)(spl_eval(gT.D1, zz) / spl_eval(gT.a, zz));
+        }
+        __syncthreads();
+        if (threadIdx.x < 2 * (LENS_PDEG + 1)) {
+            const int side = threadIdx.x / (LENS_PDEG + 1), j = threadIdx.x % (LENS_PDEG + 1);
+            double c = 0.0;
+            for (int k = 0; k <= LENS_PDEG; ++k) c += poly.vinv[j][k] * (double)gval[side][k];
+            gcoef[side][j] = (float)c;
+        }
+        __syncthreads();
+    }
     Acc<T> acc;
     for (int ia = threadIdx.x; ia < a.n_x; ia += blockDim.x) {
         const double x1d = 0.5 * (xf[ia] + 1.0);
         const T x1 = (T)x1d;
         const T l1 = chi1 * x1;
-        const T z1 = spl_eval(gT.z_of_chi, l1);
-        const T g1 = spl_eval(gT.D1, z1) / spl_eval(gT.a, z1) * (T(1) - x1);
+        T g1;
+        if (F32) {
+            g1 = (T)lens_horner(gcoef[0], (float)(2 * x1 - 1)) * (T(1) - x1);
+        } else {
+            const T z1 = spl_eval(gT.z_of_chi, l1);
+            g1 = spl_eval(gT.D1, z1) / spl_eval(gT.a, z1) * (T(1) - x1);
+        }
         const double xs = x1d * G.chi1 / G.chi2;
         const bool split = a.nh > 0 && xs > 0 && xs < 1;
         T line = T(0);
@@ -234,12 +313,22 @@ __global__ void __launch_bounds__(LENS_THREADS)
             const double c = 0.5 * (lo + hi), hw = 0.5 * (hi - lo);
             const int np = split ? a.nh : a.n_x;
             const double *gx = split ? xh : xf, *gw = split ? wh : wf;
+            const float *gx32 = split ? xh32 : xf32, *gw32 = split ? wh32 : wf32;
+            const float cf = (float)c, hwf = (float)hw;
             Acc<T> pa;
             for (int k = 0; k < np; ++k) {
-                const T x2 = (T)(c + hw * gx[k]);
+                T x2, g2, wk;
+                if (F32) {
+                    x2 = (T)fmaf(hwf, gx32[k], cf);
+                    g2 = (T)lens_horner(gcoef[1], (float)(2 * x2 - 1)) * (T(1) - x2);
+                    wk = (T)gw32[k];
+                } else {
+                    x2 = (T)(c + hw * gx[k]);
+                    const T z2 = spl_eval(gT.z_of_chi, chi2 * x2);
+                    g2 = spl_eval(gT.D1, z2) / spl_eval(gT.a, z2) * (T(1) - x2);
+                    wk = (T)gw[k];
+                }
                 const T l2 = chi2 * x2;
-                const T z2 = spl_eval(gT.z_of_chi, l2);
-                const T g2 = spl_eval(gT.D1, z2) / spl_eval(gT.a, z2) * (T(1) - x2);
                 const T ll = l1 * l2;
                 const T dl = l1 - l2;
                 const T r2 = dl * dl + T(2) * ll * ss;
@@ -248,18 +337,32 @@ __global__ void __launch_bounds__(LENS_THREADS)
                     T I[LENS_NT];
                     lens_tables<T, TT>(recs, tab_x, a.tab_len, inv_dlog, sqrt(r2), I);
                     // functions.c:3695-3775
-                    v = T(2) * c2m * ll * I[L00] / T(5) + T(4) * ct * I[L20] / T(3) +
-                        T(4) * ct * (r2 + T(6) * ct * ll) * I[L11] / T(15) +
-                        T(2) * c2m * ll * (T(2) * r2 + T(3) * ct * ll) * I[L02] / T(7) / r2 +
-                        T(2) * ct * (T(2) * r2 * r2 + T(12) * ct * r2 * ll + T(15) * c2m * ll * ll) *
-                            I[L13] / T(15) / r2 +
-                        c2m * ll * (T(6) * r2 * r2 + T(30) * ct * r2 * ll + T(35) * c2m * ll * ll) *
-                            I[L04] / T(35) / r2 / r2;
+                    if (F32) { // the same terms with reciprocals instead of divisions
+                        const T ir2 = T(1) / r2;
+                        const T ctll = ct * ll, c2ll = c2m * ll;
+                        v = c2ll * I[L00] * T(0.4) + ct * I[L20] * T(4.0 / 3.0) +
+                            ct * (r2 + T(6) * ctll) * I[L11] * T(4.0 / 15.0) +
+                            c2ll * (T(2) * r2 + T(3) * ctll) * I[L02] * (T(2.0 / 7.0) * ir2) +
+                            ct * (T(2) * r2 * r2 + T(12) * r2 * ctll + T(15) * c2ll * ll) * I[L13] *
+                                (T(2.0 / 15.0) * ir2) +
+                            c2ll * (T(6) * r2 * r2 + T(30) * r2 * ctll + T(35) * c2ll * ll) *
+                                I[L04] * (T(1.0 / 35.0) * ir2 * ir2);
+                    } else {
+                        v = T(2) * c2m * ll * I[L00] / T(5) + T(4) * ct * I[L20] / T(3) +
+                            T(4) * ct * (r2 + T(6) * ct * ll) * I[L11] / T(15) +
+                            T(2) * c2m * ll * (T(2) * r2 + T(3) * ct * ll) * I[L02] / T(7) / r2 +
+                            T(2) * ct *
+                                (T(2) * r2 * r2 + T(12) * ct * r2 * ll + T(15) * c2m * ll * ll) *
+                                I[L13] / T(15) / r2 +
+                            c2m * ll *
+                                (T(6) * r2 * r2 + T(30) * ct * r2 * ll + T(35) * c2m * ll * ll) *
+                                I[L04] / T(35) / r2 / r2;
+                    }
                 } else {
                     // functions.c:3801-3833
                     v = T(4) + T(24) * ll * i11_0 / T(15);
                 }
-                pa.add((T)gw[k] * g2 * v);
+                pa.add(wk * g2 * v);
             }
             line += (T)hw * (T)pa.value();
         }
@@ -643,14 +746,15 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
         return st;
     double *part_d = (double *)ctx->lens_part.p;
     double *part_s = part_d + chunk * a.n_mu;
+    static const LensPoly poly = lens_poly_tables();
     for (long long p0 = 0; p0 < total; p0 += chunk) {
         const long long np = std::min(chunk, total - p0);
         a.pair0 = p0;
         a.n_items = np * a.n_mu;
         if (do_double) {
             lens_double_kernel<T, S, TT><<<(unsigned)a.n_items, LENS_THREADS, 0, ctx->stream>>>(
-                a, g64, gT, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule, part_d,
-                ctx->d_err);
+                a, g64, gT, poly, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule,
+                part_d, ctx->d_err);
             if ((st = cg_after_launch(ctx, "lens_double_kernel"))) return st;
         }
         if (single) {
@@ -781,6 +885,16 @@ static int flatsky_run(coffe_gpu_ctx *ctx, bool denlen, bool lenlen, double epsr
     return COFFE_GPU_OK;
 }
 
+// float copies of the line rules (x, w_x, x_h, w_h) after the FP64 rule
+// mu[n_mu], w_mu[n_mu], x[n_x], w_x[n_x], x_h[nh], w_h[nh] (r has room)
+static void lens_rule_floats(const LensArgs &a, std::vector<double> &r)
+{
+    const size_t off = 2 * (size_t)a.n_mu + 2 * (size_t)a.n_x + 2 * (size_t)a.nh;
+    float *f = reinterpret_cast<float *>(r.data() + off);
+    for (size_t i = 0; i < 2 * (size_t)a.n_x + 2 * (size_t)a.nh; ++i)
+        f[i] = (float)r[2 * (size_t)a.n_mu + i];
+}
+
 // arguments of the lensing kernels for a validated call (n_mu mu nodes)
 static int lens_args(coffe_gpu_ctx *ctx, int contrib, int n_req, int n_l, const int *l, int n_mu,
                      LensArgs *out)
@@ -856,12 +970,13 @@ int corrfunc_lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_r
     const int l0 = 0;
     if ((st = lens_args(ctx, contrib, n_req, 1, &l0, n_mu, &a))) return st;
     // rule: mu[n_mu], (unused weights)[n_mu], x[n_x], w_x[n_x], x_h[nh], w_h[nh]
-    std::vector<double> r(2 * (size_t)a.n_mu + 2 * (size_t)a.n_x + 2 * (size_t)a.nh, 0.0);
+    std::vector<double> r(2 * (size_t)a.n_mu + 3 * (size_t)a.n_x + 3 * (size_t)a.nh, 0.0);
     for (int m = 0; m < n_mu; ++m) r[m] = mu_host[m];
     gauss_legendre(a.n_x, r.data() + 2 * a.n_mu, r.data() + 2 * a.n_mu + a.n_x);
     if (a.nh)
         gauss_legendre(a.nh, r.data() + 2 * a.n_mu + 2 * a.n_x,
                        r.data() + 2 * a.n_mu + 2 * a.n_x + a.nh);
+    lens_rule_floats(a, r);
     if ((st = cg_ensure(ctx, ctx->cf_rule, sizeof(double) * r.size()))) return st;
     CG_CUDA(ctx, cudaMemcpyAsync(ctx->cf_rule.p, r.data(), sizeof(double) * r.size(),
                                  cudaMemcpyHostToDevice, ctx->stream));
@@ -909,12 +1024,13 @@ int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, i
     if ((st = lens_args(ctx, contrib, n_req, n_l, l, ctx->lens_n_mu, &a))) return st;
     // the Gauss-Legendre rule: mu[n_mu], w_mu[n_mu], x[n_x], w_x[n_x], x_h[nh], w_h[nh]
     if (ctx->lens_rule_mu != a.n_mu || ctx->lens_rule_x != a.n_x) {
-        std::vector<double> r(2 * (size_t)a.n_mu + 2 * (size_t)a.n_x + 2 * (size_t)a.nh);
+        std::vector<double> r(2 * (size_t)a.n_mu + 3 * (size_t)a.n_x + 3 * (size_t)a.nh);
         gauss_legendre(a.n_mu, r.data(), r.data() + a.n_mu);
         gauss_legendre(a.n_x, r.data() + 2 * a.n_mu, r.data() + 2 * a.n_mu + a.n_x);
         if (a.nh)
             gauss_legendre(a.nh, r.data() + 2 * a.n_mu + 2 * a.n_x,
                            r.data() + 2 * a.n_mu + 2 * a.n_x + a.nh);
+        lens_rule_floats(a, r);
         if ((st = cg_ensure(ctx, ctx->lens_rule, sizeof(double) * r.size()))) return st;
         CG_CUDA(ctx, cudaMemcpyAsync(ctx->lens_rule.p, r.data(), sizeof(double) * r.size(),
                                      cudaMemcpyHostToDevice, ctx->stream));
