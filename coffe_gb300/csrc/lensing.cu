@@ -18,8 +18,9 @@
 // Work split (one launch each, per chunk of pairs):
 //   lens_double_kernel  one CTA per (pair, mu node): threads own x1 lines and
 //                       sweep their x2 line; one partial per (pair, mu);
-//   lens_single_kernel  one warp per (pair, mu node), FP64 on both paths (the
-//                       RSD-lensing coefficients cancel terms of size chi^5);
+//   lens_single_kernel  one warp per (pair, mu node), FP64 (lens_single32_kernel
+//                       on the mixed path: FP32 with the RSD-lensing
+//                       coefficients expanded so that they cancel nothing);
 //   lens_reduce_kernel  per (pair, l): the mu weights and P_l(mu), summed in a
 //                       fixed order, added to the nonintegrated multipole.
 // The six I_l^n tables the integrands read are evaluated through Akima
@@ -521,6 +522,153 @@ __global__ void __launch_bounds__(LENS_THREADS)
     }
 }
 
+// Mixed path of lens_single_kernel: the same integrand in FP32, Kahan sums per
+// lane.  The RSD-lensing polynomials Q and P are written in d = chi_i -
+// lambda_j and s, where every term has the size of the result, so they need no
+// FP64; d itself is formed from 1 - x and chi2 - chi1 = sep mu (d21 = chi2 (1 -
+// x) - sep mu, d12 = chi1 (1 - x) + sep mu), which keeps its relative precision
+// where lambda_j approaches chi_i.  D1 / a along both lines of sight is the
+// per-item degree-9 polynomial of lens_double_kernel.  The per-item background
+// values are FP64 lookups spread over the lanes (one per lane).
+template <typename S>
+__global__ void __launch_bounds__(LENS_THREADS)
+    lens_single32_kernel(LensArgs a, LensBg64 g, LensBgT<S> gT, LensPoly poly,
+                         const float *__restrict__ tab_x, const float4 *__restrict__ rec,
+                         const int *__restrict__ req_spectrum,
+                         const double *__restrict__ req_z_mean,
+                         const int64_t *__restrict__ req_offset, const double *__restrict__ sep,
+                         const double *__restrict__ rule, double *__restrict__ part, int *err)
+{
+    const long long item = (long long)blockIdx.x * (LENS_THREADS / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (item >= a.n_items) return; // whole warps leave together
+    const unsigned full = 0xffffffffu;
+    const long long pair = a.pair0 + item / a.n_mu;
+    const int im = (int)(item % a.n_mu);
+    const int q = lens_find_request(req_offset, a.n_req, pair);
+    const int s = req_spectrum[q];
+    const double mu = rule[im], r = sep[pair];
+    // geometry as lens_geom, with z(chi1) on even and z(chi2) on odd lanes
+    const double chi_mean = spl_eval(g.chi_of_z, req_z_mean[q]);
+    const double chi1 = chi_mean - r * mu / 2., chi2 = chi_mean + r * mu / 2.;
+    const double sd = r * r * (1 - mu * mu) / (2. * chi_mean * chi_mean - mu * mu * r * r / 2.);
+    const double zl = spl_eval(g.z_of_chi, (lane & 1) ? chi2 : chi1);
+    const double z1c = __shfl_sync(full, zl, 0), z2c = __shfl_sync(full, zl, 1);
+    // lanes 0-7: b1, b2, s1, s2, f(z1), f(z2), D1(z1), D1(z2)
+    const int k8 = lane & 7;
+    const bool set = k8 == 0 ? a.has_b1 : k8 == 1 ? a.has_b2 : k8 == 2 ? a.has_s1 :
+                     k8 == 3 ? a.has_s2 : true;
+    const Spl64 sp = k8 == 0 ? g.b1 : k8 == 1 ? g.b2 : k8 == 2 ? g.s1 : k8 == 3 ? g.s2 :
+                     k8 < 6 ? g.f : g.D1;
+    double bv = k8 < 2 ? 1.0 : 0.0;
+    if (set) bv = spl_eval(sp, (k8 & 1) ? z2c : z1c);
+    const double b1 = __shfl_sync(full, bv, 0), b2 = __shfl_sync(full, bv, 1);
+    const double s1 = __shfl_sync(full, bv, 2), s2 = __shfl_sync(full, bv, 3);
+    const double f1c = __shfl_sync(full, bv, 4), f2c = __shfl_sync(full, bv, 5);
+    const double D1z1c = __shfl_sync(full, bv, 6), D1z2c = __shfl_sync(full, bv, 7);
+    // D1 / a along both lines of sight: lanes 0-9 side 1 (chi1), 10-19 side 2
+    float gc1[LENS_PDEG + 1], gc2[LENS_PDEG + 1];
+    {
+        const int side = lane >= LENS_PDEG + 1, j = lane % (LENS_PDEG + 1);
+        float gv = 0.f;
+        if (lane < 2 * (LENS_PDEG + 1)) {
+            const float lam = (float)(side ? chi2 : chi1) * 0.5f * (poly.t[j] + 1.f);
+            const float zz = spl_eval(gT.z_of_chi, lam);
+            gv = spl_eval(gT.D1, zz) / spl_eval(gT.a, zz);
+        }
+        double c = 0.0;
+#pragma unroll
+        for (int k = 0; k <= LENS_PDEG; ++k)
+            c += poly.vinv[j][k] * (double)__shfl_sync(full, gv, side * (LENS_PDEG + 1) + k);
+        const float cf = (float)c;
+#pragma unroll
+        for (int k = 0; k <= LENS_PDEG; ++k) {
+            gc1[k] = __shfl_sync(full, cf, k);
+            gc2[k] = __shfl_sync(full, cf, LENS_PDEG + 1 + k);
+        }
+    }
+    const float4 *recs = rec + (size_t)s * (a.tab_len - 1) * LENS_NT;
+    const float inv_dlog = (float)a.inv_dlog;
+    const float I00_0 = lens_at_zero<float>(recs, L00), I11_0 = lens_at_zero<float>(recs, L11);
+    const float c1 = (float)chi1, c2 = (float)chi2, dchi = (float)(r * mu), ss = (float)sd;
+    const float ct = (float)(1 - sd), omc2 = (float)(sd * (2 - sd));
+    const float c2m1 = (float)(1 - 2 * sd * (2 - sd));
+    const bool den = a.contrib & COFFE_GPU_DEN, rsd = a.contrib & COFFE_GPU_RSD;
+    const bool wide = fabs(mu) < 0.999;
+    // functions.c:1708-1780 and 2174-2306 with the background factors folded
+    const double kc = a.pref2 * 1.5 * a.Om;
+    const float kd2 = (float)(-kc * b1 * (2 - 5 * s2) * D1z1c * chi1 * chi2);
+    const float kd1 = (float)(-kc * b2 * (2 - 5 * s1) * D1z2c * chi1 * chi2);
+    const float kr2 = (float)(kc * chi2 * f1c * (2 - 5 * s2) * D1z1c);
+    const float kr1 = (float)(kc * chi1 * f2c * (2 - 5 * s1) * D1z2c);
+    auto Q = [&](float ch, float d) {
+        return d * d * d * (8.f - 24.f * ss + 12.f * ss * ss) +
+               ch * d * d * (-2.f + 38.f * ss - 18.f * ss * ss - 6.f * ss * ss * ss) +
+               ch * ch * d * ss * (-22.f + 9.f * ss + 12.f * ss * ss) +
+               ch * ch * ch * ss * (2.f - 3.f * ss - 6.f * ss * ss);
+    };
+    auto P = [&](float ch, float d) {
+        const float d2 = d * d, d3 = d2 * d, d4 = d2 * d2, d5 = d4 * d;
+        const float ch2 = ch * ch, ch3 = ch2 * ch, ch4 = ch2 * ch2, ch5 = ch4 * ch;
+        const float s2 = ss * ss, s3 = s2 * ss;
+        return d5 * (4.f - 12.f * ss + 6.f * s2) + ch * d4 * (-8.f + 60.f * ss - 48.f * s2 + 6.f * s3) +
+               ch2 * d3 * ss * (-92.f + 114.f * ss - 20.f * s2 - s3) +
+               ch3 * d2 * ss * (48.f - 120.f * ss + 26.f * s2 + 3.f * s3) +
+               ch4 * d * s2 * (60.f - 16.f * ss - 3.f * s2) + ch5 * s2 * (-12.f + 4.f * ss + s2);
+    };
+    // one side: density and RSD parts times D1 / a, without the (1 - x) factor
+    auto side_val = [&](float ch, float la, float d, float r2, const float *I, float kd, float kr,
+                        float gl) {
+        float v = 0.f;
+        if (r2 != 0.f) {
+            const float ir2 = 1.f / r2;
+            if (den) v += kd * (2.f * ct * I[L11] - ch * la * omc2 * I[L02] * ir2);
+            if (rsd) {
+                v += kr * ((la - 6.f * ch * ct + 3.f * la * c2m1) * I[L00] * (1.f / 15.f) -
+                           Q(ch, d) * I[L02] * ir2 * (1.f / 21.f));
+                v += kr * (wide ? -P(ch, d) * I[L04] * ir2 * ir2 * (1.f / 35.f)
+                                : 4.f * (la + ch) * I[L04] * (1.f / 35.f));
+            }
+        } else {
+            if (den) v += kd * 2.f * I11_0;
+            if (rsd) v += kr * (-2.f * ch * I00_0 * (1.f / 15.f));
+        }
+        return v * gl;
+    };
+    const float *xf32 = reinterpret_cast<const float *>(rule + 2 * a.n_mu + 2 * a.n_x + 2 * a.nh);
+    const float *wf32 = xf32 + a.n_x, *xh32 = wf32 + a.n_x, *wh32 = xh32 + a.nh;
+    const double xs = fmin(chi1, chi2) * (1 - sd) / fmax(chi1, chi2);
+    const bool split = a.nh > 0 && xs > 0 && xs < 1;
+    double sum = 0;
+    for (int p = 0; p < (split ? 2 : 1); ++p) {
+        const double lo = (split && p) ? xs : 0.0, hi = (split && !p) ? xs : 1.0;
+        const float cf = (float)(0.5 * (lo + hi)), omcf = (float)(1 - 0.5 * (lo + hi));
+        const float hwf = (float)(0.5 * (hi - lo));
+        const int np = split ? a.nh : a.n_x;
+        const float *gx = split ? xh32 : xf32, *gw = split ? wh32 : wf32;
+        Acc<float> ps;
+        for (int k = lane; k < np; k += 32) {
+            const float x = fmaf(hwf, gx[k], cf), omx = fmaf(-hwf, gx[k], omcf);
+            const float t = 2.f * x - 1.f;
+            const float la1 = c1 * x, la2 = c2 * x;
+            const float d21 = fmaf(c2, omx, -dchi), d12 = fmaf(c1, omx, dchi);
+            const float r21 = d21 * d21 + 2.f * c1 * la2 * ss;
+            const float r22 = d12 * d12 + 2.f * c2 * la1 * ss;
+            float I1[LENS_NT], I2[LENS_NT];
+            lens_tables<float, float>(recs, tab_x, a.tab_len, inv_dlog, sqrtf(r21), I1);
+            lens_tables<float, float>(recs, tab_x, a.tab_len, inv_dlog, sqrtf(r22), I2);
+            const float v = side_val(c1, la2, d21, r21, I1, kd2, kr2, lens_horner(gc2, t)) +
+                            side_val(c2, la1, d12, r22, I2, kd1, kr1, lens_horner(gc1, t));
+            ps.add(gw[k] * omx * v);
+        }
+        sum += (double)hwf * warp_sum(ps.value());
+    }
+    if (lane == 0) {
+        if (!isfinite(sum)) cg_flag(err, CG_ERR_NONFINITE);
+        part[item] = sum;
+    }
+}
+
 __device__ __forceinline__ double lens_legendre(int l, double x)
 {
     if (l == 0) return 1.0;
@@ -759,9 +907,14 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
         }
         if (single) {
             const long long blocks = (a.n_items + LENS_THREADS / 32 - 1) / (LENS_THREADS / 32);
-            lens_single_kernel<TT><<<(unsigned)blocks, LENS_THREADS, 0, ctx->stream>>>(
-                a, g64, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule, part_s,
-                ctx->d_err);
+            if constexpr (sizeof(T) == 4)
+                lens_single32_kernel<S><<<(unsigned)blocks, LENS_THREADS, 0, ctx->stream>>>(
+                    a, g64, gT, poly, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule,
+                    part_s, ctx->d_err);
+            else
+                lens_single_kernel<TT><<<(unsigned)blocks, LENS_THREADS, 0, ctx->stream>>>(
+                    a, g64, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule, part_s,
+                    ctx->d_err);
             if ((st = cg_after_launch(ctx, "lens_single_kernel"))) return st;
         }
         if (per_node) {

@@ -90,6 +90,25 @@ def test_lensing_mixed_close_to_oracle(gpu_ctx, lens_setup):
     assert e < 1e-4, e
 
 
+@pytest.mark.parametrize("z,rule", [(1.5, (16, 32)), (0.4, (32, 64))])
+def test_lensing_single_integrated_mixed(gpu_ctx, lens_setup, z, rule):
+    """The single-integrated den/rsd x lensing term alone on the mixed path
+    (FP32 integrand): total minus nonintegrated minus lensing-lensing, against
+    the oracle's single term, at 5e-5 of the term's largest |value| per l."""
+    k, pk, m = lens_setup
+    sep = np.array([15.0, 60.0, 150.0, 350.0]) / H
+    ls = (0, 2, 4, 6)
+    for contrib in (DEN | LEN, RSD | LEN, DEN | RSD | LEN):
+        ref = (m.multipoles_lensing(contrib, z, sep, ls, *rule) -
+               m.multipoles_lensing(LEN, z, sep, ls, *rule))
+        got = (_gpu(gpu_ctx, k, pk, "mixed", sep, z, ls, contrib, rule) -
+               _gpu(gpu_ctx, k, pk, "mixed", sep, z, ls, contrib & 3, rule) -
+               _gpu(gpu_ctx, k, pk, "mixed", sep, z, ls, LEN, rule))
+        e = np.max(np.abs(got - ref) / np.abs(ref).max(axis=0, keepdims=True))
+        print(contrib, z, "single-integrated mixed error", e)
+        assert e < 5e-5, (contrib, z, e)
+
+
 def test_lensing_full_rule_matches_oracle(gpu_ctx, lens_setup):
     """The 128 mu x 256 x rule at two separations (8.4M len-len nodes each)."""
     k, pk, m = lens_setup
