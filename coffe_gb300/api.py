@@ -220,8 +220,9 @@ class Context:
                    contrib=_lib.DEN | _lib.RSD, precision="fp64", epsrel=1e-5,
                    out=None) -> np.ndarray:
         """Batched multipoles; returns an array of shape (len(sep), len(ls)).
-        ``out``: optional C-contiguous float64 array of that shape to fill (page-locked
-        host memory makes the device-to-host copy run at full link speed)."""
+        ``out``: optional C-contiguous float64 array of that shape to fill; in
+        page-locked host memory (e.g. a pinned torch tensor's ``.numpy()``) the
+        den/rsd kernels write it directly, with no device copy and download."""
         rs = np.ascontiguousarray(req_spectrum, dtype=np.int32)
         rz = _f64(req_z_mean)
         ro = np.ascontiguousarray(req_offset, dtype=np.int64)

@@ -2,6 +2,7 @@
 // staging, error mapping.  The numerical work lives in the other .cu files.
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "ctx.cuh"
@@ -53,6 +54,46 @@ int cg_after_launch(coffe_gpu_ctx *ctx, const char *what)
     return COFFE_GPU_OK;
 }
 
+// Flags CG_ERR_BADSEP if any of the n separations is not > 0 (NaN included):
+// the check of a host-array call, on the device copy (5 MB of separations
+// read at HBM speed instead of a serial host scan).
+__global__ void sep_check_kernel(const double *__restrict__ sep, long long n, int *err)
+{
+    bool bad = false;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        bad |= !(sep[i] > 0);
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) cg_flag(err, CG_ERR_BADSEP);
+}
+
+static int sep_check(coffe_gpu_ctx *ctx, const double *d_sep, long long n)
+{
+    if (n <= 0) return COFFE_GPU_OK;
+    if (ctx->sm_count <= 0)
+        CG_CUDA(ctx, cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount,
+                                            ctx->device));
+    const long long blocks = std::min<long long>((n + 255) / 256, 4LL * ctx->sm_count);
+    sep_check_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(d_sep, n, ctx->d_err);
+    return cg_after_launch(ctx, "sep_check_kernel");
+}
+
+// The device address of `bytes` of page-locked host memory at p when both its
+// first and last byte are mapped into this device's address space as one
+// range, else nullptr (pageable memory, or a range the check cannot vouch for).
+static void *mapped_device_pointer(const void *p, size_t bytes)
+{
+    cudaPointerAttributes a0, a1;
+    const char *last = (const char *)p + bytes - 1;
+    const bool ok = cudaPointerGetAttributes(&a0, p) == cudaSuccess &&
+                    a0.type == cudaMemoryTypeHost && a0.devicePointer &&
+                    cudaPointerGetAttributes(&a1, last) == cudaSuccess &&
+                    a1.type == cudaMemoryTypeHost && a1.devicePointer &&
+                    (const char *)a1.devicePointer - (const char *)a0.devicePointer ==
+                        last - (const char *)p;
+    cudaGetLastError(); // an unregistered pointer is an answer, not an error
+    return ok ? a0.devicePointer : nullptr;
+}
+
 int cg_check_device_errors(coffe_gpu_ctx *ctx, const char *where)
 {
     CG_CUDA(ctx, cudaMemcpyAsync(ctx->h_err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost,
@@ -62,6 +103,10 @@ int cg_check_device_errors(coffe_gpu_ctx *ctx, const char *where)
     if (!bits) return COFFE_GPU_OK;
     CG_CUDA(ctx, cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
     *ctx->h_err = 0;
+    if (bits & CG_ERR_BADSEP) { // before NONFINITE: such separations give NaN
+        cg_set_error(ctx, "%s: separations must be positive", where);
+        return COFFE_GPU_EINVAL;
+    }
     if (bits & CG_ERR_NONFINITE) {
         cg_set_error(ctx, "%s: non-finite value produced (device flags 0x%x)", where, bits);
         return COFFE_GPU_ENONFINITE;
@@ -439,9 +484,14 @@ int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, doubl
     }
     const int64_t total = req_offset[n_req];
     if (total > 0 && (!sep || !out)) return COFFE_GPU_EINVAL;
+    // a page-locked, mapped output is written by the kernels directly (no
+    // device copy and download; the den/rsd kernels store it in whole lines)
+    double *out_mapped = total > 0 && !(contrib & COFFE_GPU_LEN)
+                             ? (double *)mapped_device_pointer(out, sizeof(double) * total * n_l)
+                             : nullptr;
     const size_t b_spec = sizeof(int) * n_req, b_z = sizeof(double) * n_req,
                  b_off = sizeof(int64_t) * (n_req + 1), b_sep = sizeof(double) * total,
-                 b_out = sizeof(double) * total * n_l;
+                 b_out = out_mapped ? 0 : sizeof(double) * total * n_l;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t bytes = al(b_spec) + al(b_z) + al(b_off) + al(b_sep) + al(b_out);
     int st = cg_ensure(ctx, ctx->req_buf, bytes);
@@ -451,28 +501,28 @@ int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, doubl
     double *d_z = (double *)(base + al(b_spec));
     int64_t *d_off = (int64_t *)(base + al(b_spec) + al(b_z));
     double *d_sep = (double *)(base + al(b_spec) + al(b_z) + al(b_off));
-    double *d_out = (double *)(base + al(b_spec) + al(b_z) + al(b_off) + al(b_sep));
+    double *d_out = out_mapped ? out_mapped
+                               : (double *)(base + al(b_spec) + al(b_z) + al(b_off) + al(b_sep));
     CG_CUDA(ctx, cudaMemcpyAsync(d_spec, req_spectrum, b_spec, cudaMemcpyHostToDevice, ctx->stream));
     CG_CUDA(ctx, cudaMemcpyAsync(d_z, req_z_mean, b_z, cudaMemcpyHostToDevice, ctx->stream));
     CG_CUDA(ctx, cudaMemcpyAsync(d_off, req_offset, b_off, cudaMemcpyHostToDevice, ctx->stream));
     if (total > 0)
         CG_CUDA(ctx, cudaMemcpyAsync(d_sep, sep, b_sep, cudaMemcpyHostToDevice, ctx->stream));
+    // the separations are checked on the device copy, in stream order with the
+    // work (a non-positive one cannot make a kernel read out of bounds: its
+    // lookups give NaN); the flag surfaces as EINVAL after the work has run
+    if ((st = sep_check(ctx, d_sep, total))) return st;
+    ctx->out_host = out_mapped != nullptr;
     st = multipoles_run(ctx, contrib, precision, epsrel, n_req, d_spec, d_z, d_off, d_sep, n_l, l,
                         d_out, total);
-    if (st) return st;
-    if (total > 0)
-        CG_CUDA(ctx, cudaMemcpyAsync(out, d_out, b_out, cudaMemcpyDeviceToHost, ctx->stream));
-    // the separations are checked on the host while the device works (a
-    // non-positive one cannot make a kernel read out of bounds: its lookups
-    // give NaN); a branch-free scan vectorises
-    unsigned char ok = 1;
-    for (int64_t i = 0; i < total; ++i) ok &= (unsigned char)(sep[i] > 0);
-    st = cg_check_device_errors(ctx, "multipoles"); // also clears the device flags
-    if (st != COFFE_GPU_ECUDA && !ok) {
-        cg_set_error(ctx, "multipoles: separations must be positive");
-        return COFFE_GPU_EINVAL;
+    ctx->out_host = false;
+    if (st) {
+        cudaStreamSynchronize(ctx->stream); // no kernel may write `out` after return
+        return st;
     }
-    return st;
+    if (total > 0 && !out_mapped)
+        CG_CUDA(ctx, cudaMemcpyAsync(out, d_out, b_out, cudaMemcpyDeviceToHost, ctx->stream));
+    return cg_check_device_errors(ctx, "multipoles"); // also clears the device flags
 }
 
 int coffe_gpu_average_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision,

@@ -31,6 +31,10 @@ struct coffe_gpu_ctx {
     long long launches = 0; // kernels launched through this context
     int sm_count = 0;
     char last_error[512] = {0};
+    // the multipole output of the running call is page-locked host memory
+    // (mapped): the den/rsd kernels stage each block's results in shared
+    // memory and store them as whole lines
+    bool out_host = false;
 
     // ---- background
     int bg_bins = 0;

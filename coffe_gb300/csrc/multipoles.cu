@@ -360,6 +360,7 @@ struct MpArgs {
     double epsrel;
     long long retry_cap;
     int ls[MP_MAX_L];
+    int out_staged = 0; // out is mapped host memory: store whole lines (mp_fast_kernel)
 };
 
 // request of each separation: largest q with req_offset[q] <= item
@@ -494,12 +495,12 @@ __device__ __forceinline__ double to_f64(double x) { return x; }
 __device__ __forceinline__ double to_f64(float x) { return f64_of_bits(x); }
 
 template <int NL, typename T>
-__device__ __forceinline__ void first_panel_out(const MpArgs &a, T epsrel, long long item, bool finite,
-                                                const T (&K)[NL], const T (&G)[NL],
-                                                const T (&A)[NL], const T (&asc)[NL],
-                                                double *__restrict__ out,
-                                                int *__restrict__ retry_count,
-                                                int2 *__restrict__ retry, int *err)
+__device__ __forceinline__ void first_panel_value(const MpArgs &a, T epsrel, long long item,
+                                                  bool finite, const T (&K)[NL], const T (&G)[NL],
+                                                  const T (&A)[NL], const T (&asc)[NL],
+                                                  double (&res)[NL], bool (&have)[NL],
+                                                  int *__restrict__ retry_count,
+                                                  int2 *__restrict__ retry, int *err)
 {
 #pragma unroll
     for (int j = 0; j < NL; ++j) {
@@ -513,14 +514,16 @@ __device__ __forceinline__ void first_panel_out(const MpArgs &a, T epsrel, long 
         const T round_off = T(50) * qk_eps<T>() * o.resabs;
         const bool roundoff_fail = o.abserr <= round_off && o.abserr > tolerance;
         const bool ok = (o.abserr <= tolerance && o.abserr != o.resasc) || o.abserr == T(0);
+        have[j] = true;
         if (!finite) {
             cg_flag(err, CG_ERR_NONFINITE);
-            out[item * NL + j] = cg_nan<double>();
+            res[j] = cg_nan<double>();
         } else if (ok || roundoff_fail) {
-            const double res = to_f64(T(2 * l + 1) * o.result);
-            if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
-            out[item * NL + j] = res;
-        } else {
+            res[j] = to_f64(T(2 * l + 1) * o.result);
+            if (!isfinite(res[j])) cg_flag(err, CG_ERR_NONFINITE);
+        } else { // the retry kernel writes this entry
+            have[j] = false;
+            res[j] = cg_nan<double>();
             const int slot = atomicAdd(retry_count, 1);
             if (slot < a.retry_cap)
                 retry[slot] = make_int2((int)item, j);
@@ -528,6 +531,23 @@ __device__ __forceinline__ void first_panel_out(const MpArgs &a, T epsrel, long 
                 cg_flag(err, CG_ERR_QAG_LIMIT);
         }
     }
+}
+
+template <int NL, typename T>
+__device__ __forceinline__ void first_panel_out(const MpArgs &a, T epsrel, long long item, bool finite,
+                                                const T (&K)[NL], const T (&G)[NL],
+                                                const T (&A)[NL], const T (&asc)[NL],
+                                                double *__restrict__ out,
+                                                int *__restrict__ retry_count,
+                                                int2 *__restrict__ retry, int *err)
+{
+    double res[NL];
+    bool have[NL];
+    first_panel_value<NL, T>(a, epsrel, item, finite, K, G, A, asc, res, have, retry_count, retry,
+                             err);
+#pragma unroll
+    for (int j = 0; j < NL; ++j)
+        if (have[j]) out[item * NL + j] = res[j];
 }
 
 template <int NL, typename T, typename S, typename TT, bool MIRROR = false>
@@ -736,6 +756,9 @@ template <int NL> struct FastLayout {
     static constexpr int R2 = ((1 + NL) + 3) / 4 * 4;
     static constexpr int ROWS = 31;
     static constexpr int COUNT = ROWS * (R1 + R2);
+    // the integrand rows start 16-byte aligned and hold a block's NL double
+    // results when mp_fast_kernel stages its output
+    static_assert(COUNT % 4 == 0 && ROWS * sizeof(float) >= NL * sizeof(double), "layout");
 };
 
 #define MP_FAST_MAX_THREADS 256
@@ -755,12 +778,14 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
     float *xs = tab2 + LY::ROWS * LY::R2;             // [ROWS][blockDim.x] integrand values
     for (int i = threadIdx.x; i < LY::COUNT; i += blockDim.x) tab1[i] = nodes[i];
     __syncthreads();
-    const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (item >= total) return;
-    const int q = find_request(req_offset, a.n_req, item);
+    const long long item0 = (long long)blockIdx.x * blockDim.x;
+    const long long item = item0 + threadIdx.x;
+    if (item >= total && !a.out_staged) return; // the staged store needs every thread
+    const bool valid = item < total;
+    const int q = valid ? find_request(req_offset, a.n_req, item) : 0;
     const int s = req_spectrum[q];
     // double -> float without the FP64 pipe (1/64 of the FP32 rate)
-    const float r = f32_of_bits(sep[item]);
+    const float r = valid ? f32_of_bits(sep[item]) : 1.f;
     const BgFit bf = fit[q];
     const float chim = bf.go.w;
     const float *y0 = tab_y + ((size_t)s * a.n_terms) * a.tab_len;
@@ -775,7 +800,7 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
     for (int j = 0; j < NL; ++j) K[j] = Kc[j] = G[j] = A[j] = 0.f;
     const float half_r = 0.5f * r;
     const float span = tab1[(LY::ROWS - 1) * LY::R1] * half_r; // largest mu
-    const bool inside = (chim - span >= chi_lo) && (chim + span <= chi_hi);
+    const bool inside = valid && (chim - span >= chi_lo) && (chim + span <= chi_hi);
     const bool finite = inside && isfinite(I00) && isfinite(I02) && isfinite(I04);
     if (inside) {
         const float A2 = 2.f * chim * chim, Br = 0.5f * r * r, r2 = r * r;
@@ -841,8 +866,36 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
             for (int j = 0; j < NL; ++j) asc[j] = fmaf(rec[0], fabsf(fmaf(v, rec[1 + j], -0.5f * K[j])), asc[j]);
         }
     }
-    first_panel_out<NL, float>(a, f32_of_bits(a.epsrel), item, finite, K, G, A, asc, out,
-                               retry_count, retry, err);
+    if (!a.out_staged) {
+        first_panel_out<NL, float>(a, f32_of_bits(a.epsrel), item, finite, K, G, A, asc, out,
+                                   retry_count, retry, err);
+        return;
+    }
+    // out in page-locked host memory: the block's results go through shared
+    // memory (the xs rows, no longer read) and leave as consecutive 16-byte
+    // stores, whole lines over the host link instead of 8-byte pieces
+    double res[NL];
+    bool have[NL];
+    if (valid)
+        first_panel_value<NL, float>(a, f32_of_bits(a.epsrel), item, finite, K, G, A, asc, res,
+                                     have, retry_count, retry, err);
+    __syncthreads();
+    double *stage = reinterpret_cast<double *>(xs);
+    if (valid) {
+#pragma unroll
+        for (int j = 0; j < NL; ++j) stage[tid * NL + j] = res[j]; // retried: NaN until retried
+    }
+    __syncthreads();
+    const int n = (int)min((long long)bd, total - item0) * NL;
+    double *o = out + item0 * NL;
+    if ((reinterpret_cast<uintptr_t>(o) & 15) == 0) {
+        const double2 *s2 = reinterpret_cast<const double2 *>(stage);
+        double2 *o2 = reinterpret_cast<double2 *>(o);
+        for (int i = tid; i < n / 2; i += bd) o2[i] = s2[i];
+        if ((n & 1) && tid == 0) o[n - 1] = stage[n - 1];
+    } else {
+        for (int i = tid; i < n; i += bd) o[i] = stage[i];
+    }
 }
 
 // ------------------------------------------------- correlation function
@@ -1235,6 +1288,7 @@ int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel
     a.n_req = n_req;
     a.n_l = n_l;
     a.contrib = contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD | COFFE_GPU_ONLY_CROSS);
+    a.out_staged = ctx->out_host;
     a.t00 = cg_find_term(ctx, 0, 0);
     a.t02 = cg_find_term(ctx, 0, 2);
     a.t04 = cg_find_term(ctx, 0, 4);

@@ -189,13 +189,15 @@ int coffe_gpu_integral_eval(coffe_gpu_ctx_t *ctx, int spectrum, int term, const 
    Gauss-Legendre rule of coffe_gpu_set_lensing_rule.  They also need the
    integrals (1,1), (1,3), (2,0) and tables built with COFFE_GPU_SMALL_R.
    precision: COFFE_GPU_FP64 follows the reference in FP64; COFFE_GPU_MIXED
-   evaluates the integrand in FP32 with compensated FP32 sums (the
-   single-integrated lensing terms stay FP64: their RSD-lensing coefficients
-   cancel terms of size chi^5).
+   evaluates the integrand in FP32 with compensated FP32 sums.
    All arrays are host pointers unless arrays_on_device != 0, in which case
-   every array (including out) is a device pointer.  With host arrays a
+   every array (including out) is a device pointer.  With host arrays and
+   without lensing, an `out` in page-locked host memory mapped into the
+   device's address space (cudaHostAlloc / cudaHostRegister) is written by the
+   kernels directly, with no device copy and download.  With host arrays a
    non-positive separation returns COFFE_GPU_EINVAL after the work has run
-   (the check overlaps it), so `out` is then unspecified. */
+   (the check runs on the device copy, in stream order with the work), so
+   `out` is then unspecified. */
 int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, double epsrel,
                          int n_req, const int *req_spectrum, const double *req_z_mean,
                          const int64_t *req_offset, const double *sep, int n_l,
