@@ -43,6 +43,10 @@ enum { L00 = 0, L02, L04, L11, L13, L20 };
 
 struct LensArgs {
     int n_req, n_l, n_mu, n_x, nh, contrib;
+    // mu nodes evaluated: mu0 .. mu0 + n_mu_run - 1 of the rule, weighted by
+    // mu_w (the upper half twice when the terms are even in mu)
+    int mu0, n_mu_run;
+    double mu_w;
     int tab_len, n_terms;
     int term[LENS_NT];
     double inv_dlog; // N / ln(kmax/kmin), r0 = 1
@@ -260,8 +264,8 @@ __global__ void __launch_bounds__(LENS_THREADS)
     __shared__ float gval[2][LENS_PDEG + 1];
     __shared__ float gcoef[2][LENS_PDEG + 1];
     const long long item = blockIdx.x;
-    const long long pair = a.pair0 + item / a.n_mu;
-    const int im = (int)(item % a.n_mu);
+    const long long pair = a.pair0 + item / a.n_mu_run;
+    const int im = a.mu0 + (int)(item % a.n_mu_run);
     const int q = lens_find_request(req_offset, a.n_req, pair);
     const int s = req_spectrum[q];
     const double *xf = rule + 2 * a.n_mu, *wf = xf + a.n_x, *xh = wf + a.n_x, *wh = xh + a.nh;
@@ -488,8 +492,8 @@ __global__ void __launch_bounds__(LENS_THREADS)
     const long long item = (long long)blockIdx.x * (LENS_THREADS / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (item >= a.n_items) return;
-    const long long pair = a.pair0 + item / a.n_mu;
-    const int im = (int)(item % a.n_mu);
+    const long long pair = a.pair0 + item / a.n_mu_run;
+    const int im = a.mu0 + (int)(item % a.n_mu_run);
     const int q = lens_find_request(req_offset, a.n_req, pair);
     const int s = req_spectrum[q];
     const double *xf = rule + 2 * a.n_mu, *wf = xf + a.n_x, *xh = wf + a.n_x, *wh = xh + a.nh;
@@ -543,8 +547,8 @@ __global__ void __launch_bounds__(LENS_THREADS)
     const int lane = threadIdx.x & 31;
     if (item >= a.n_items) return; // whole warps leave together
     const unsigned full = 0xffffffffu;
-    const long long pair = a.pair0 + item / a.n_mu;
-    const int im = (int)(item % a.n_mu);
+    const long long pair = a.pair0 + item / a.n_mu_run;
+    const int im = a.mu0 + (int)(item % a.n_mu_run);
     const int q = lens_find_request(req_offset, a.n_req, pair);
     const int s = req_spectrum[q];
     const double mu = rule[im], r = sep[pair];
@@ -694,11 +698,12 @@ __global__ void lens_reduce_kernel(LensArgs a, const double *__restrict__ rule,
     const int j = (int)(t % a.n_l);
     const int l = a.ls[j];
     double sum = 0;
-    for (int im = 0; im < a.n_mu; ++im) {
+    for (int k = 0; k < a.n_mu_run; ++k) {
+        const int im = a.mu0 + k;
         double v = 0;
-        if (part_d) v += part_d[pl * a.n_mu + im];
-        if (part_s) v += part_s[pl * a.n_mu + im];
-        sum += 0.5 * rule[a.n_mu + im] * v * lens_legendre(l, rule[im]);
+        if (part_d) v += part_d[pl * a.n_mu_run + k];
+        if (part_s) v += part_s[pl * a.n_mu_run + k];
+        sum += a.mu_w * 0.5 * rule[a.n_mu + im] * v * lens_legendre(l, rule[im]);
     }
     const double res = (2 * l + 1) * sum;
     if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
@@ -711,12 +716,12 @@ __global__ void lens_cf_reduce_kernel(LensArgs a, const double *__restrict__ par
                                       double *__restrict__ out, int *err)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n_pairs * a.n_mu) return;
+    if (t >= n_pairs * a.n_mu_run) return;
     double v = 0;
     if (part_d) v += part_d[t];
     if (part_s) v += part_s[t];
     if (!isfinite(v)) cg_flag(err, CG_ERR_NONFINITE);
-    out[a.pair0 * a.n_mu + t] += v;
+    out[a.pair0 * a.n_mu_run + t] += v;
 }
 
 // n-point Gauss-Legendre nodes and weights on [-1, 1] (Newton on P_n from the
@@ -889,16 +894,16 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
     if ((st = cg_after_launch(ctx, "lens_records_kernel"))) return st;
     const bool single = do_single;
     // pairs per chunk: partials of at most 2^22 (pair, mu) items per kind
-    const long long chunk = std::max(1LL, std::min(total, (1LL << 22) / a.n_mu));
-    if ((st = cg_ensure(ctx, ctx->lens_part, sizeof(double) * 2 * (size_t)(chunk * a.n_mu))))
+    const long long chunk = std::max(1LL, std::min(total, (1LL << 22) / a.n_mu_run));
+    if ((st = cg_ensure(ctx, ctx->lens_part, sizeof(double) * 2 * (size_t)(chunk * a.n_mu_run))))
         return st;
     double *part_d = (double *)ctx->lens_part.p;
-    double *part_s = part_d + chunk * a.n_mu;
+    double *part_s = part_d + chunk * a.n_mu_run;
     static const LensPoly poly = lens_poly_tables();
     for (long long p0 = 0; p0 < total; p0 += chunk) {
         const long long np = std::min(chunk, total - p0);
         a.pair0 = p0;
-        a.n_items = np * a.n_mu;
+        a.n_items = np * a.n_mu_run;
         if (do_double) {
             lens_double_kernel<T, S, TT><<<(unsigned)a.n_items, LENS_THREADS, 0, ctx->stream>>>(
                 a, g64, gT, poly, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule,
@@ -918,7 +923,7 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
             if ((st = cg_after_launch(ctx, "lens_single_kernel"))) return st;
         }
         if (per_node) {
-            const long long nt = np * a.n_mu;
+            const long long nt = np * a.n_mu_run;
             lens_cf_reduce_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, ctx->stream>>>(
                 a, do_double ? part_d : nullptr, single ? part_s : nullptr, np, out, ctx->d_err);
             if ((st = cg_after_launch(ctx, "lens_cf_reduce_kernel"))) return st;
@@ -1064,6 +1069,9 @@ static int lens_args(coffe_gpu_ctx *ctx, int contrib, int n_req, int n_l, const 
     a.n_req = n_req;
     a.n_l = n_l;
     a.n_mu = n_mu;
+    a.mu0 = 0;
+    a.n_mu_run = n_mu;
+    a.mu_w = 1.0;
     a.n_x = ctx->lens_n_x;
     a.nh = (a.n_x % 2 == 0) ? a.n_x / 2 : 0;
     a.contrib = contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD | COFFE_GPU_LEN);
@@ -1175,6 +1183,22 @@ int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, i
     }
     LensArgs a;
     if ((st = lens_args(ctx, contrib, n_req, n_l, l, ctx->lens_n_mu, &a))) return st;
+    // mu -> -mu swaps chi1 and chi2, i.e. the roles of the two tracers: when
+    // they share their magnification bias (and, for density-lensing, their
+    // galaxy bias) both lensing terms are even in mu, so even multipoles need
+    // only the rule's nodes with mu > 0 (the rule is symmetric), counted twice
+    auto same_tracer = [&](int i, int j) {
+        return (!ctx->bias_set[i] && !ctx->bias_set[j]) ||
+               (ctx->bias_set[i] && ctx->bias_set[j] && ctx->bias_host[i] == ctx->bias_host[j]);
+    };
+    bool mirror = a.n_mu % 2 == 0 && same_tracer(2, 3) &&
+                  (!(single_full && (contrib & COFFE_GPU_DEN)) || same_tracer(0, 1));
+    for (int j = 0; j < n_l; ++j) mirror = mirror && l[j] % 2 == 0;
+    if (mirror) {
+        a.mu0 = a.n_mu / 2;
+        a.n_mu_run = a.n_mu / 2;
+        a.mu_w = 2.0;
+    }
     // the Gauss-Legendre rule: mu[n_mu], w_mu[n_mu], x[n_x], w_x[n_x], x_h[nh], w_h[nh]
     if (ctx->lens_rule_mu != a.n_mu || ctx->lens_rule_x != a.n_x) {
         std::vector<double> r(2 * (size_t)a.n_mu + 3 * (size_t)a.n_x + 3 * (size_t)a.nh);

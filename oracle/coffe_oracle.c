@@ -1358,6 +1358,26 @@ static double lens_line(double x0, double x1_, double xs, const or_line_rule_t *
     return acc;
 }
 
+/* tracers i and j (0/1 galaxy, 2/3 magnification bias) are the same function:
+   both unset, or both set from equal samples */
+static int same_tracer(const or_model_t *m, int i, int j)
+{
+    if (!m->have_bias[i] || !m->have_bias[j])
+        return !m->have_bias[i] && !m->have_bias[j];
+    const or_spline_t *a = &m->bias[i], *b = &m->bias[j];
+    return a->n == b->n && a->type == b->type &&
+           memcmp(a->x, b->x, sizeof(double) * a->n) == 0 &&
+           memcmp(a->y, b->y, sizeof(double) * a->n) == 0;
+}
+
+/* The lensing multipoles on the product rule.  mu -> -mu swaps chi1 and chi2,
+   i.e. the roles of the two tracers; when they share their magnification bias
+   (and, with density-lensing, their galaxy bias) both lensing terms are even
+   in mu, and even multipoles are summed over the rule's nodes with mu > 0
+   (the Gauss-Legendre rule is symmetric), each counted twice.  Quadrature
+   choice of this restatement (the reference uses Cuhre): the plane rule at a
+   node -mu is the one at mu with x1 and x2 exchanged, equal to it up to the
+   rule's own error. */
 int or_multipoles_lensing_gl(const or_model_t *m, int contrib, double z_mean, double sep,
                              int n_l, const int *ls, size_t n_mu, size_t n_x, double *out)
 {
@@ -1375,8 +1395,12 @@ int or_multipoles_lensing_gl(const or_model_t *m, int contrib, double z_mean, do
     const int single = (contrib & OR_CONTRIB_LEN) && (contrib & (OR_CONTRIB_DEN | OR_CONTRIB_RSD));
     const int dbl = (contrib & OR_CONTRIB_LEN) != 0;
     const or_line_rule_t R = {n_x, xf, wf, xh, wh};
-    for (size_t i = 0; i < n_mu; ++i) {
-        const double mu = xm[i], wmu = 0.5 * wm[i]; /* dv = dmu / 2 */
+    int mirror = n_mu % 2 == 0 && same_tracer(m, 2, 3) &&
+                 (!(single && (contrib & OR_CONTRIB_DEN)) || same_tracer(m, 0, 1));
+    for (int j = 0; j < n_l; ++j)
+        mirror = mirror && ls[j] % 2 == 0;
+    for (size_t i = mirror ? n_mu / 2 : 0; i < n_mu; ++i) {
+        const double mu = xm[i], wmu = (mirror ? 1.0 : 0.5) * wm[i]; /* dv = dmu / 2 */
         const or_lens_geom_t g = lens_geom(m, z_mean, mu, sep);
         double acc = 0.0;
         if (single) {
