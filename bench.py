@@ -79,10 +79,14 @@ def parse():
                    help="fixed launch configuration instead of autotuning, e.g. "
                         "fft_threads=512,fft_radix=4,fft_swizzle=1,spline_group=8,"
                         "lane_threads=128,lane_unroll=2,fft_threads_fwd=256 (profiling runs)")
-    p.add_argument("--kernel-only", choices=["mixed", "fp64", "tables-mixed", "tables-fp64"],
+    p.add_argument("--kernel-only",
+                   choices=["mixed", "fp64", "tables-mixed", "tables-fp64", "lensing-mixed"],
                    default=None,
-                   help="profiling aid: run only the multipole kernel (mixed/fp64) or only the "
-                        "FFTLog tables (tables-*) `steps` times")
+                   help="profiling aid: run only the multipole kernel (mixed/fp64), only the "
+                        "FFTLog tables (tables-*) or only the config-4 lensing multipoles "
+                        "(lensing-mixed, --lensing-seps separations) `steps` times")
+    p.add_argument("--lensing-seps", type=int, default=200,
+                   help="separations of the lensing-mixed profiling run (config 4 has 200)")
     return p.parse_args()
 
 
@@ -296,7 +300,10 @@ def extras(torch, ctx, stream):
         "mixed_ms": res["mixed"][0], "fp64_ms": res["fp64"][0],
         "mixed_evals_per_s": n4 / (res["mixed"][0] * 1e-3),
         "fp64_evals_per_s": n4 / (res["fp64"][0] * 1e-3),
-        "lensing_nodes_per_s_mixed": len(c4["sep"]) * 128 * 256 * 256 / (res["mixed"][0] * 1e-3),
+        "lensing_rule_nodes_per_s_mixed": len(c4["sep"]) * 128 * 256 * 256 / (res["mixed"][0] * 1e-3),
+        "mu_nodes_evaluated": 64,
+        "note": "equal tracers and even multipoles: the rule's 64 mu > 0 nodes are evaluated "
+                "and counted twice (the terms are even in mu)",
         "max_rel_err_mixed_vs_fp64": err}
     # covariance: 5 z bins x l = 0,2,4 x 128 x 128 separations, 2D FFTLog 2^11
     ctx.background_init(co.omega_m, co.omega_baryon, co.omega_gamma, co.h, 10000)
@@ -426,6 +433,25 @@ def ours(args, rank, world, local_rank):
         launches = graphs[prec][1] * k if prec in graphs else ctx.launch_count() - l0
         return dev_s, wall, launches
 
+    if args.kernel_only == "lensing-mixed":
+        # profiling aid: the config-4 lensing multipoles on the first separations
+        c4 = workloads.cfg4()
+        co = c4["cosmo"]
+        ctx.background_init(co.omega_m, co.omega_baryon, co.omega_gamma, co.h, 10000)
+        ctx.integrals_init(c4["k"], c4["pk"][None, :], c4["terms"], N=N_FFT, precision="mixed",
+                           small_r=True)
+        ctx.set_lensing_rule(*c4["rule"])
+        ns = max(1, min(args.lensing_seps, len(c4["sep"])))
+        dev = torch.device("cuda", torch.cuda.current_device())
+        sep = torch.tensor(c4["sep"][:ns], device=dev)
+        rs = torch.zeros(1, dtype=torch.int32, device=dev)
+        rz = torch.tensor([c4["z_mean"]], dtype=torch.float64, device=dev)
+        ro = torch.tensor([0, ns], dtype=torch.int64, device=dev)
+        o = torch.empty((ns, len(c4["ls"])), dtype=torch.float64, device=dev)
+        for _ in range(args.steps):
+            ctx.multipoles_async(rs, rz, ro, sep, ns, c4["ls"], o, contrib=7, precision="mixed")
+        ctx.synchronize()
+        return
     if args.kernel_only:
         # profiling aid: only one stage of one precision
         prec = args.kernel_only.split("-")[-1]
