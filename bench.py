@@ -251,7 +251,8 @@ def measure_gemm_peak(torch, dtype, n=8192, reps=5):
 def extras(torch, ctx, stream):
     """Device timings of the other workloads of the path (one GB300, CUDA events
     on the library's stream): den+RSD+lensing multipoles (128 mu x 256 x rule),
-    the 2D-FFTLog multipole covariance and the multipole gradient."""
+    the 2D-FFTLog multipole covariance, the multipole gradient and the divergent
+    integral with its renormalisation grid."""
     from coffe_gb300 import workloads
 
     out = {}
@@ -340,6 +341,26 @@ def extras(torch, ctx, stream):
         "workload": "d(multipoles)/d(P(k), bias scale, growth scale), den+RSD l=0,2,4, z=1, "
                     "100 separations, 4096 k nodes, FP64 adjoint",
         "ms_per_call": grad_ms}
+    # divergent I^4_0 and its 201 x 201 renormalisation grid (integrals.c:773-914)
+    # on the config-1 spectrum, chi in [0, chi(1.2)]
+    c1 = workloads.cfg1()
+    ctx.background_init(0.31, 0.05, 9e-5, 0.67, 10000)
+    bgd = ctx.background(with_H=False)
+    chi = np.arange(201) * np.interp(1.2, bgd["z"], bgd["chi"]) / 200
+    ctx.renormalization_grid(c1["k"], c1["pk"], chi[:4])
+    t0 = time.perf_counter()
+    grid = ctx.renormalization_grid(c1["k"], c1["pk"], chi)
+    t1 = time.perf_counter()
+    _, r1d, _ = ctx.divergent_integral(c1["k"], c1["pk"])
+    t2 = time.perf_counter()
+    out["divergent_i40"] = {
+        "workload": "r^4 I^4_0 and its r = 0 renormalisation on the 297 fixed separations; "
+                    "renormalisation grid 201 x 201 over chi in [0, chi(z=1.2)]; config-1 P(k), "
+                    "GK61 QAG at 1e-5 per value, FP64",
+        "grid_ms": (t1 - t0) * 1e3, "separations_ms": (t2 - t1) * 1e3,
+        "grid_values_per_s": grid.size / (t1 - t0),
+        "finite": bool(np.isfinite(grid).all() and np.isfinite(r1d).all()),
+        "note": "host API wall time (host arrays in, values out)"}
     return out
 
 

@@ -66,6 +66,9 @@ EXPORTS = (
     "coffe_gpu_get_tuning",
     "coffe_gpu_set_tuning",
     "coffe_gpu_launch_count",
+    "coffe_gpu_divergent_separations",
+    "coffe_gpu_divergent_integral",
+    "coffe_gpu_renormalization_grid",
 )
 
 
@@ -174,5 +177,11 @@ def load(build_if_missing: bool = True):
     L.coffe_gpu_set_tuning.argtypes = [_p, C.POINTER(Tuning)]
     L.coffe_gpu_launch_count.argtypes = [_p]
     L.coffe_gpu_launch_count.restype = C.c_longlong
+    L.coffe_gpu_divergent_separations.argtypes = [_dp, C.c_size_t]
+    L.coffe_gpu_divergent_separations.restype = C.c_size_t
+    L.coffe_gpu_divergent_integral.argtypes = [_p, _dp, _dp, C.c_size_t, C.c_double, C.c_double,
+                                               _dp, C.c_size_t, _dp, _dp]
+    L.coffe_gpu_renormalization_grid.argtypes = [_p, _dp, _dp, C.c_size_t, C.c_double,
+                                                 C.c_double, _dp, C.c_size_t, _dp, C.c_size_t, _dp]
     _lib = L
     return L

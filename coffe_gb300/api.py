@@ -260,6 +260,41 @@ class Context:
             "average_multipoles")
         return out[: len(sp)]
 
+    # ------------------------------------------------ divergent I^4_0 (integrals.c:773-914)
+    @staticmethod
+    def _k_range(k, kmin, kmax):
+        return (float(k[0]) if kmin is None else float(kmin),
+                float(k[-1]) if kmax is None else float(kmax))
+
+    def divergent_integral(self, k, pk, sep=None, kmin=None, kmax=None):
+        """The divergent integral at separations ``sep`` (Mpc, default the fixed
+        ones the reference splines it on): returns (sep, result, result0) with
+        result = r^4 I^4_0(r) and result0 = r^4 times its r = 0 renormalisation
+        integral, both over 2 pi^2 (integrals.c:797-826).  k in 1/Mpc, P in Mpc^3,
+        integrated over [kmin, kmax] (default the k range)."""
+        k, pk = _f64(k), _f64(pk)
+        sp = divergent_separations() if sep is None else _f64(np.atleast_1d(sep))
+        lo, hi = self._k_range(k, kmin, kmax)
+        res, res0 = np.zeros(len(sp)), np.zeros(len(sp))
+        self._check(self._L.coffe_gpu_divergent_integral(self._ctx, _dptr(k), _dptr(pk), len(k),
+                                                         lo, hi, _dptr(sp), len(sp), _dptr(res),
+                                                         _dptr(res0)), "divergent_integral")
+        return sp, res, res0
+
+    def renormalization_grid(self, k, pk, chi1, chi2=None, kmin=None, kmax=None) -> np.ndarray:
+        """out[b, a] = (1/2 pi^2) int P j0(k chi1[a]) j0(k chi2[b]) / k^2 dk over
+        [kmin, kmax] (integrals.c:424-444); chi2 defaults to chi1."""
+        k, pk = _f64(k), _f64(pk)
+        c1 = _f64(np.atleast_1d(chi1))
+        c2 = c1 if chi2 is None else _f64(np.atleast_1d(chi2))
+        lo, hi = self._k_range(k, kmin, kmax)
+        out = np.zeros((len(c2), len(c1)))
+        self._check(self._L.coffe_gpu_renormalization_grid(self._ctx, _dptr(k), _dptr(pk), len(k),
+                                                           lo, hi, _dptr(c1), len(c1), _dptr(c2),
+                                                           len(c2), _dptr(out)),
+                    "renormalization_grid")
+        return out
+
     def corrfunc(self, req_spectrum, req_z_mean, req_offset, sep, mu,
                  contrib=_lib.DEN | _lib.RSD, precision="fp64") -> np.ndarray:
         """Correlation function at every (separation, mu) of the batched requests;
@@ -458,6 +493,16 @@ class Corrfunc:
 
     def to_dict(self):
         return {"z": self.z, "r": self.r, "mu": self.mu, "value": self.value}
+
+
+def divergent_separations() -> np.ndarray:
+    """The fixed separations (Mpc) on which the reference splines the divergent
+    integral I^4_0 (integrals.c:76-103)."""
+    L = _lib.load()
+    n = L.coffe_gpu_divergent_separations(None, 0)
+    out = np.zeros(n)
+    L.coffe_gpu_divergent_separations(_dptr(out), n)
+    return out
 
 
 def _check_parameter(name, value, kind, lo, hi):

@@ -193,7 +193,7 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
                       &ctx->lens_rule, &ctx->lens_rec, &ctx->lens_part,
                       &ctx->cov_buf,  &ctx->cov_out, &ctx->adj_buf, &ctx->csband,
                       &ctx->samp_tdf, &ctx->qfac_df, &ctx->pk_df, &ctx->mp_bgfit,
-                      &ctx->cf_rule, &ctx->avg_buf};
+                      &ctx->cf_rule, &ctx->avg_buf, &ctx->div_buf};
     spline_free(ctx->cov_pk);
     for (DevBuf *b : bufs) cg_release(*b);
     for (auto &slot : ctx->mp_node_slots) cg_release(slot.buf);
@@ -328,6 +328,70 @@ int coffe_gpu_set_bias(coffe_gpu_ctx_t *ctx, int which, const double *z, const d
     ctx->bias_host[which].assign(z, z + n);
     ctx->bias_host[which].insert(ctx->bias_host[which].end(), value, value + n);
     return cg_check_device_errors(ctx, "set_bias");
+}
+
+// the fixed separations (Mpc) of the divergent integral's spline
+// (integrals.c:76-103): a table the spline's knots must reproduce
+static const double cg_div_sep[] = {
+    1e-06, 5e-06, 0.0001, 0.005, 0.01, 0.02, 0.05, 0.1, 0.2, 0.4,
+    0.8, 1., 1.5, 2., 3., 4., 5., 6., 7., 8.,
+    9., 10., 11., 12., 13., 14., 15., 16., 17., 18.,
+    19., 20., 21., 22., 23., 24., 25., 26., 27., 28.,
+    29., 30., 32., 34., 36., 38., 40., 42., 44., 46.,
+    48., 50., 52., 54., 56., 58., 60., 62., 64., 66.,
+    68., 70., 72., 74., 76., 78., 80., 81., 82., 83.,
+    84., 85., 86., 87., 88., 89., 90., 91., 92., 93.,
+    94., 95., 95.5, 96., 96.5, 97., 97.5, 98., 98.5, 99.,
+    99.5, 100., 100.5, 101., 101.5, 102., 102.5, 103., 103.5, 104.,
+    104.5, 105., 106., 107., 108., 109., 110., 112., 114., 116.,
+    118., 120., 124., 128., 132., 136., 140., 144., 148., 152.,
+    156., 160., 164., 168., 172., 176., 180., 185., 190., 195.,
+    200., 205., 210., 215., 220., 225., 230., 235., 240., 250.,
+    260., 270., 280., 290., 300., 320., 340., 360., 380., 400.,
+    420., 440., 460., 480., 500., 520., 540., 560., 580., 600.,
+    620., 640., 660., 680., 700., 750., 800., 850., 900., 950.,
+    1000., 1050., 1100., 1150., 1200., 1250., 1300., 1350., 1400., 1450.,
+    1500., 1550., 1600., 1650., 1700., 1750., 1800., 1850., 1900., 1950.,
+    2000., 2050., 2100., 2150., 2200., 2250., 2300., 2350., 2400., 2450.,
+    2500., 2550., 2600., 2650., 2700., 2750., 2800., 2850., 2900., 2950.,
+    3000., 3050., 3100., 3150., 3200., 3250., 3300., 3350., 3400., 3450.,
+    3500., 3550., 3600., 3650., 3700., 3750., 3800., 3850., 3900., 3950.,
+    4000., 4050., 4100., 4150., 4200., 4250., 4300., 4350., 4400., 4450.,
+    4500., 4550., 4600., 4650., 4700., 4750., 4800., 4850., 4900., 4950.,
+    5000., 5050., 5100., 5150., 5200., 5250., 5300., 5350., 5400., 5450.,
+    5500., 5550., 5600., 5650., 5700., 5750., 5800., 5850., 5900., 5950.,
+    6000., 6050., 6100., 6150., 6200., 6250., 6300., 6350., 6400., 6450.,
+    6500., 6550., 6600., 7000., 8000., 9000., 10000., 11000., 12000., 13000.,
+    14000., 15000., 16000., 17000., 18000., 19000., 20000.,
+};
+
+size_t coffe_gpu_divergent_separations(double *out, size_t cap)
+{
+    const size_t n = sizeof(cg_div_sep) / sizeof(cg_div_sep[0]);
+    for (size_t i = 0; out && i < n && i < cap; ++i) out[i] = cg_div_sep[i];
+    return n;
+}
+
+int coffe_gpu_divergent_integral(coffe_gpu_ctx_t *ctx, const double *k, const double *pk,
+                                 size_t nk, double kmin, double kmax, const double *sep,
+                                 size_t n_sep, double *result, double *result0)
+{
+    if (!ctx) return COFFE_GPU_EINVAL;
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    return divergent_run(ctx, k, pk, nk, kmin, kmax, sep, n_sep, nullptr, 0, result, result0);
+}
+
+int coffe_gpu_renormalization_grid(coffe_gpu_ctx_t *ctx, const double *k, const double *pk,
+                                   size_t nk, double kmin, double kmax, const double *chi1,
+                                   size_t n1, const double *chi2, size_t n2, double *out)
+{
+    if (!ctx) return COFFE_GPU_EINVAL;
+    if (!chi2) {
+        cg_set_error(ctx, "renormalization grid: chi2 is required");
+        return COFFE_GPU_EINVAL;
+    }
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    return divergent_run(ctx, k, pk, nk, kmin, kmax, chi1, n1, chi2, n2, out, nullptr);
 }
 
 int coffe_gpu_set_autotune(coffe_gpu_ctx_t *ctx, int enable)

@@ -134,6 +134,7 @@ struct coffe_gpu_ctx {
 
     // ---- multipole adjoint (adjoint.cu)
     DevBuf adj_buf; // table, spectrum and resampling cotangents
+    DevBuf div_buf; // k, P(k), separations and results of the divergent integral
 };
 
 void cg_set_error(coffe_gpu_ctx *ctx, const char *fmt, ...);
@@ -157,6 +158,9 @@ int bg_build_splines(coffe_gpu_ctx *ctx);
 int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n_spectra,
                     size_t nk, const int *n, const int *l, const int *half, int n_terms, size_t N,
                     int precision, unsigned flags);
+int divergent_run(coffe_gpu_ctx *ctx, const double *k, const double *pk, size_t nk, double kmin,
+                  double kmax, const double *r1, size_t n1, const double *r2, size_t n2,
+                  double *out_a, double *out_b);
 int integrals_eval(coffe_gpu_ctx *ctx, int spectrum, int term, const double *r, size_t nq,
                    double *out);
 int multipoles_prepare_background(coffe_gpu_ctx *ctx);

@@ -13,6 +13,7 @@
 // biases, tapers, M_{q,l}, prefactors, twiddles) is a per-grid table built
 // once; a spectrum costs one forward FFT per distinct q and one inverse FFT
 // per term.  One CTA holds one transform in shared memory (radix-2, in place).
+#include <cmath>
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -884,6 +885,72 @@ __global__ void __launch_bounds__(32 * SR_WARPS)
     }
 }
 
+// ---------------------------------------------- divergent I^4_0 (integrals.c:773-914)
+// The integrands of the divergent integral: P (1 - j0(kr)^2) / k^2 (its r = 0
+// renormalisation, integrals.c:390-404) and P j0(k chi1) j0(k chi2) / k^2 (the
+// renormalisation term, integrals.c:406-422); the integral itself is
+// BesselIntegrand with n = 4, l = 0.
+struct RenormIntegrand {
+    PkAkima pk;
+    double r1, r2;
+    bool zero; // the r = 0 form
+    __device__ double operator()(double k) const
+    {
+        const double j1 = sph_bessel(0, k * r1);
+        const double w = zero ? 1.0 - j1 * j1 : j1 * sph_bessel(0, k * r2);
+        return pk(k) * w / k / k;
+    }
+};
+
+// One warp per item, GK61 QAG at relative 1e-5 over [kmin, kmax] (the
+// reference's coffe_integrate_1d_prec_gsl).  grid == 0: items 0..n1-1 are
+// r^4 I^4_0(r1[i]) / 2 pi^2, items n1..2 n1-1 the r^4-scaled r = 0
+// renormalisation integral / 2 pi^2 (integrals.c:803-826), each with a
+// DIV_CAP-interval store in `scratch` (below r ~ 1e-4 Mpc the reference's
+// 1 - j0(kr)^2 is rounding noise and QAG bisects ~1000 times before it stops);
+// grid != 0: item b * n1 + a is the renormalisation term at (r1[a], r2[b]) /
+// 2 pi^2 (under 30 intervals: a shared-memory store).
+#define DIV_CAP 4096
+#define DIV_CHUNK 1024
+__global__ void __launch_bounds__(32 * SR_WARPS)
+    divergent_kernel(const double *__restrict__ kx, const double *__restrict__ pk, int nk,
+                     double kmin, double kmax, const double *__restrict__ r1,
+                     const double *__restrict__ r2, long n1, long item0, long n_items,
+                     int grid, double *__restrict__ scratch, double *__restrict__ out, int *err)
+{
+    __shared__ double sa[SR_WARPS][SR_CAP], sb[SR_WARPS][SR_CAP], sr[SR_WARPS][SR_CAP],
+        se[SR_WARPS][SR_CAP];
+    const int w = threadIdx.x >> 5;
+    const long item = item0 + (long)blockIdx.x * SR_WARPS + w;
+    if (item >= n_items) return;
+    PkAkima P{kx, pk, nk};
+    // launches of at most DIV_CHUNK items: the store of item sits at item - item0
+    double *g = scratch + (size_t)(item - item0) * 4 * DIV_CAP;
+    const QagStore<double> store =
+        grid ? QagStore<double>{sa[w], sb[w], sr[w], se[w], SR_CAP}
+             : QagStore<double>{g, g + DIV_CAP, g + 2 * DIV_CAP, g + 3 * DIV_CAP, DIV_CAP};
+    int status = 0;
+    double v;
+    if (grid) {
+        RenormIntegrand f{P, r1[item % n1], r2[item / n1], false};
+        v = qag61_warp<double>(f, kmin, kmax, 0.0, 1e-5, store, 50000, &status);
+    } else if (item < n1) {
+        const double r = r1[item];
+        BesselIntegrand f{P, r, 4, 0};
+        v = qag61_warp<double>(f, kmin, kmax, 0.0, 1e-5, store, 50000, &status) * pow(r, 4.0);
+    } else {
+        const double r = r1[item - n1];
+        RenormIntegrand f{P, r, 0.0, true};
+        v = qag61_warp<double>(f, kmin, kmax, 0.0, 1e-5, store, 50000, &status) * pow(r, 4.0);
+    }
+    v = v / 2. / CG_PI / CG_PI;
+    if ((threadIdx.x & 31) == 0) {
+        if (status == 1) cg_flag(err, CG_ERR_QAG_LIMIT);
+        if (!isfinite(v)) cg_flag(err, CG_ERR_NONFINITE);
+        out[item] = v;
+    }
+}
+
 template <typename TO> __global__ void fill_nan_kernel(TO *tab, size_t len, long count)
 {
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1304,4 +1371,72 @@ int integrals_eval(coffe_gpu_ctx *ctx, int spectrum, int term, const double *r, 
     }
     cudaFree(tmp.p);
     return st;
+}
+
+// The divergent integral on host separations r (all > 0) or, with r2, the
+// renormalisation grid over host chi1 x chi2 (all >= 0): P(k) = Akima of
+// (k, pk) on the host, integrated over [kmin, kmax] inside its range.
+int divergent_run(coffe_gpu_ctx *ctx, const double *k, const double *pk, size_t nk, double kmin,
+                  double kmax, const double *r1, size_t n1, const double *r2, size_t n2,
+                  double *out_a, double *out_b)
+{
+    if (!k || !pk || !r1 || nk < 5 || nk > (1u << 22) || n1 < 1 || (r2 && n2 < 1) ||
+        n1 > (r2 ? (1u << 24) : (1u << 16)) || n2 > (1u << 24) || !out_a || (!r2 && !out_b)) {
+        cg_set_error(ctx, "divergent integral: bad arguments");
+        return COFFE_GPU_EINVAL;
+    }
+    for (size_t i = 0; i < nk; ++i)
+        if (!(k[i] > 0) || (i > 0 && !(k[i] > k[i - 1])) || !std::isfinite(pk[i])) {
+            cg_set_error(ctx, "divergent integral: k must be positive and strictly increasing, "
+                              "P(k) finite");
+            return COFFE_GPU_EINVAL;
+        }
+    if (!(kmin >= k[0] && kmax <= k[nk - 1] && kmin < kmax)) {
+        cg_set_error(ctx, "divergent integral: need k[0] <= kmin < kmax <= k[nk-1]");
+        return COFFE_GPU_EINVAL;
+    }
+    for (size_t i = 0; i < n1; ++i)
+        if (!(r2 ? r1[i] >= 0 : r1[i] > 0) || !std::isfinite(r1[i])) {
+            cg_set_error(ctx, "divergent integral: separations must be %s",
+                         r2 ? "non-negative" : "positive");
+            return COFFE_GPU_EINVAL;
+        }
+    for (size_t i = 0; r2 && i < n2; ++i)
+        if (!(r2[i] >= 0) || !std::isfinite(r2[i])) {
+            cg_set_error(ctx, "divergent integral: separations must be non-negative");
+            return COFFE_GPU_EINVAL;
+        }
+    const long items = r2 ? (long)(n1 * n2) : 2 * (long)n1;
+    const size_t scratch = r2 ? 0 : (size_t)std::min<long>(items, DIV_CHUNK) * 4 * DIV_CAP;
+    const size_t bytes =
+        sizeof(double) * (2 * nk + n1 + (r2 ? n2 : 0) + (size_t)items + scratch);
+    int st = cg_ensure(ctx, ctx->div_buf, bytes);
+    if (st) return st;
+    double *d = (double *)ctx->div_buf.p;
+    double *dk = d, *dp = dk + nk, *d1 = dp + nk, *d2 = d1 + n1;
+    double *dout = d2 + (r2 ? n2 : 0), *dscr = dout + items;
+    CG_CUDA(ctx, cudaMemcpyAsync(dk, k, sizeof(double) * nk, cudaMemcpyHostToDevice, ctx->stream));
+    CG_CUDA(ctx, cudaMemcpyAsync(dp, pk, sizeof(double) * nk, cudaMemcpyHostToDevice, ctx->stream));
+    CG_CUDA(ctx, cudaMemcpyAsync(d1, r1, sizeof(double) * n1, cudaMemcpyHostToDevice, ctx->stream));
+    if (r2)
+        CG_CUDA(ctx, cudaMemcpyAsync(d2, r2, sizeof(double) * n2, cudaMemcpyHostToDevice,
+                                     ctx->stream));
+    const long chunk = r2 ? items : DIV_CHUNK;
+    for (long i0 = 0; i0 < items; i0 += chunk) {
+        const long n = std::min(chunk, items - i0);
+        divergent_kernel<<<(unsigned)((n + SR_WARPS - 1) / SR_WARPS), 32 * SR_WARPS, 0,
+                           ctx->stream>>>(dk, dp, (int)nk, kmin, kmax, d1, d2, (long)n1, i0,
+                                          items, r2 ? 1 : 0, dscr, dout, ctx->d_err);
+        if ((st = cg_after_launch(ctx, "divergent_kernel"))) return st;
+    }
+    if (r2) {
+        CG_CUDA(ctx, cudaMemcpyAsync(out_a, dout, sizeof(double) * items, cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+    } else {
+        CG_CUDA(ctx, cudaMemcpyAsync(out_a, dout, sizeof(double) * n1, cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+        CG_CUDA(ctx, cudaMemcpyAsync(out_b, dout + n1, sizeof(double) * n1,
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    return cg_check_device_errors(ctx, "divergent integral");
 }

@@ -335,6 +335,37 @@ typedef struct {
     int fft_threads_fwd; /* threads per block of the forward transforms: 128 .. 1024 */
 } coffe_gpu_tuning_t;
 
+/* ---- the divergent integral I^4_0 and its renormalisation (integrals.c:773-914),
+   which the reference builds when par->divergent is set (for the d2 and g1-g5
+   terms).  P(k): Akima spline of the host arrays (k, pk) (nk >= 5, k > 0
+   strictly increasing, P finite), integrated over [kmin, kmax] (inside the k
+   range; the reference's defaults are 1e-5 and 300 h/Mpc), GK61 QAG at relative
+   1e-5 per value, one warp per value on the device.  Units: k in 1/Mpc, P in
+   Mpc^3, separations in Mpc. */
+
+/* The fixed separations (Mpc) on which coffe_integrals_init splines I^4_0
+   (integrals.c:76-103): writes min(cap, count) of them to out (out may be NULL)
+   and returns their count (297). */
+size_t coffe_gpu_divergent_separations(double *out, size_t cap);
+
+/* At each separation sep[i] > 0 (integrals.c:797-826):
+     result[i]  = r^4 I^4_0(r) = (1/2 pi^2) int k^2 P(k) j0(kr) / (kr)^4 dk r^4,
+     result0[i] = (1/2 pi^2) r^4 int P(k) (1 - j0(kr)^2) / k^2 dk
+   (the reference applies the r^(n-l) = r^4 factor of integrals_integrate_function
+   to both; it then splines result0 with its first knot set to r = 0, value 0).
+   Host arrays. */
+int coffe_gpu_divergent_integral(coffe_gpu_ctx_t *ctx, const double *k, const double *pk,
+                                 size_t nk, double kmin, double kmax, const double *sep,
+                                 size_t n_sep, double *result, double *result0);
+
+/* The renormalisation term on a grid (integrals.c:424-444, 848-903):
+     out[b * n1 + a] = (1/2 pi^2) int P(k) j0(k chi1[a]) j0(k chi2[b]) / k^2 dk
+   for chi >= 0 (the reference's grid is chi_j = j chi_max / 200, j = 0..200, in
+   both directions, chi_max = chi(max z_mean + deltaz)).  Host arrays. */
+int coffe_gpu_renormalization_grid(coffe_gpu_ctx_t *ctx, const double *k, const double *pk,
+                                   size_t nk, double kmin, double kmax, const double *chi1,
+                                   size_t n1, const double *chi2, size_t n2, double *out);
+
 /* enable != 0 switches on benchmark mode: the first table build and the first
    mixed multipole call of each shape (FFT size, spectra, terms and precision;
    number of multipoles, contributions and batch size to the next power of

@@ -745,6 +745,129 @@ double or_integral_direct(const double *k, const double *pk, size_t nk, int n, i
     return v;
 }
 
+/* ------------------------------------------- divergent I^4_0 (integrals.c:773-914) */
+
+typedef struct {
+    const or_spline_t *pk;
+    double r1, r2;
+} or_renorm_par_t;
+
+static double renorm0_integrand(double k, void *vp)
+{
+    /* integrals.c:390-404: P (1 - j0(kr)^2) / k^2 */
+    const or_renorm_par_t *p = (const or_renorm_par_t *)vp;
+    const double j = or_sph_bessel(0, k * p->r1);
+    return or_spline_eval(p->pk, k) * (1. - j * j) / k / k;
+}
+
+static double renorm_integrand(double k, void *vp)
+{
+    /* integrals.c:406-422: P j0(k chi1) j0(k chi2) / k^2 */
+    const or_renorm_par_t *p = (const or_renorm_par_t *)vp;
+    return or_spline_eval(p->pk, k) * or_sph_bessel(0, k * p->r1) * or_sph_bessel(0, k * p->r2) /
+           k / k;
+}
+
+/* The fixed separations (Mpc) of the divergent integral's spline, independent of
+   the user's separations (integrals.c:76-103) */
+static const double or_div_sep[] = {
+    1e-06, 5e-06, 0.0001, 0.005, 0.01, 0.02, 0.05, 0.1, 0.2, 0.4,
+    0.8, 1., 1.5, 2., 3., 4., 5., 6., 7., 8.,
+    9., 10., 11., 12., 13., 14., 15., 16., 17., 18.,
+    19., 20., 21., 22., 23., 24., 25., 26., 27., 28.,
+    29., 30., 32., 34., 36., 38., 40., 42., 44., 46.,
+    48., 50., 52., 54., 56., 58., 60., 62., 64., 66.,
+    68., 70., 72., 74., 76., 78., 80., 81., 82., 83.,
+    84., 85., 86., 87., 88., 89., 90., 91., 92., 93.,
+    94., 95., 95.5, 96., 96.5, 97., 97.5, 98., 98.5, 99.,
+    99.5, 100., 100.5, 101., 101.5, 102., 102.5, 103., 103.5, 104.,
+    104.5, 105., 106., 107., 108., 109., 110., 112., 114., 116.,
+    118., 120., 124., 128., 132., 136., 140., 144., 148., 152.,
+    156., 160., 164., 168., 172., 176., 180., 185., 190., 195.,
+    200., 205., 210., 215., 220., 225., 230., 235., 240., 250.,
+    260., 270., 280., 290., 300., 320., 340., 360., 380., 400.,
+    420., 440., 460., 480., 500., 520., 540., 560., 580., 600.,
+    620., 640., 660., 680., 700., 750., 800., 850., 900., 950.,
+    1000., 1050., 1100., 1150., 1200., 1250., 1300., 1350., 1400., 1450.,
+    1500., 1550., 1600., 1650., 1700., 1750., 1800., 1850., 1900., 1950.,
+    2000., 2050., 2100., 2150., 2200., 2250., 2300., 2350., 2400., 2450.,
+    2500., 2550., 2600., 2650., 2700., 2750., 2800., 2850., 2900., 2950.,
+    3000., 3050., 3100., 3150., 3200., 3250., 3300., 3350., 3400., 3450.,
+    3500., 3550., 3600., 3650., 3700., 3750., 3800., 3850., 3900., 3950.,
+    4000., 4050., 4100., 4150., 4200., 4250., 4300., 4350., 4400., 4450.,
+    4500., 4550., 4600., 4650., 4700., 4750., 4800., 4850., 4900., 4950.,
+    5000., 5050., 5100., 5150., 5200., 5250., 5300., 5350., 5400., 5450.,
+    5500., 5550., 5600., 5650., 5700., 5750., 5800., 5850., 5900., 5950.,
+    6000., 6050., 6100., 6150., 6200., 6250., 6300., 6350., 6400., 6450.,
+    6500., 6550., 6600., 7000., 8000., 9000., 10000., 11000., 12000., 13000.,
+    14000., 15000., 16000., 17000., 18000., 19000., 20000.,
+};
+
+size_t or_divergent_separations(double *out, size_t cap)
+{
+    const size_t n = sizeof(or_div_sep) / sizeof(or_div_sep[0]);
+    for (size_t i = 0; i < n && i < cap; ++i)
+        out[i] = or_div_sep[i];
+    return n;
+}
+
+/* At each separation r_i: result = r^4 I^4_0(r) = (1/2pi^2) int k^2 P j0(kr)/(kr)^4 dk
+   r^4 (integrals_integrate_function with n = 4, l = 0, integrals.c:333-383), and
+   result0 = (1/2pi^2) r^4 int P (1 - j0(kr)^2)/k^2 dk (the same function applies its
+   r^(n - l) factor to the r = 0 renormalisation integrand, integrals.c:812-826);
+   GK61 QAG at relative 1e-5 over [kmin, kmax], Akima P(k).  status: or of the
+   QAG statuses. */
+int or_divergent_i40(const double *k, const double *pk, size_t nk, double kmin, double kmax,
+                     const double *r, size_t nr, double *result, double *result0, int nthreads)
+{
+    or_spline_t sp;
+    if (or_spline_init(&sp, k, pk, nk, OR_AKIMA) != 0)
+        return -1;
+#ifdef _OPENMP
+    if (nthreads <= 0)
+        nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+    for (long i = 0; i < (long)nr; ++i) {
+        result[i] = integrate_function(bessel_integrand, &sp, 4, 0, r[i], kmin, kmax);
+        or_renorm_par_t p = {&sp, r[i], 0.};
+        double v = or_qag61(renorm0_integrand, &p, kmin, kmax, 0, 1e-5, OR_QAG_LIMIT, NULL, NULL);
+        if (r[i] > 0)
+            v *= pow(r[i], 4.0);
+        result0[i] = v / 2. / M_PI / M_PI;
+    }
+    (void)nthreads;
+    or_spline_free(&sp);
+    return 0;
+}
+
+/* out[b * n1 + a] = (1/2pi^2) int P j0(k chi1[a]) j0(k chi2[b]) / k^2 dk, GK61 QAG
+   at relative 1e-5 (integrals_renormalization, integrals.c:424-444; the
+   reference fills result2d[k * (nbins + 1) + j] for chi_j, chi_k,
+   integrals.c:880-893) */
+int or_renormalization_grid(const double *k, const double *pk, size_t nk, double kmin,
+                            double kmax, const double *chi1, size_t n1, const double *chi2,
+                            size_t n2, double *out, int nthreads)
+{
+    or_spline_t sp;
+    if (or_spline_init(&sp, k, pk, nk, OR_AKIMA) != 0)
+        return -1;
+#ifdef _OPENMP
+    if (nthreads <= 0)
+        nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
+#endif
+    for (long t = 0; t < (long)(n1 * n2); ++t) {
+        const size_t a = (size_t)t % n1, b = (size_t)t / n1;
+        or_renorm_par_t p = {&sp, chi1[a], chi2[b]};
+        out[t] = or_qag61(renorm_integrand, &p, kmin, kmax, 0, 1e-5, OR_QAG_LIMIT, NULL, NULL) /
+                 2. / M_PI / M_PI;
+    }
+    (void)nthreads;
+    or_spline_free(&sp);
+    return 0;
+}
+
 int or_integral_table(const double *k, const double *pk, size_t nk, int n, int l,
                       size_t N, double kmin, double kmax, int with_small_r,
                       double *out_x, double *out_y)

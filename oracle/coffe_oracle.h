@@ -88,6 +88,18 @@ int or_integral_table(const double *k, const double *pk, size_t nk, int n, int l
    when n >= l (integrals.c:333-383), P(k) through the Akima spline */
 double or_integral_direct(const double *k, const double *pk, size_t nk, int n, int l,
                           double r, double kmin, double kmax);
+/* The fixed separations of the divergent integral (integrals.c:76-103): writes at
+   most cap of them to out, returns their count. */
+size_t or_divergent_separations(double *out, size_t cap);
+/* The divergent I^4_0 on separations r (integrals.c:773-845): result = r^4 I^4_0(r),
+   result0 = its r = 0 renormalisation integral times r^4, both / 2 pi^2. */
+int or_divergent_i40(const double *k, const double *pk, size_t nk, double kmin, double kmax,
+                     const double *r, size_t nr, double *result, double *result0, int nthreads);
+/* The renormalisation grid (integrals.c:424-444, 848-903):
+   out[b * n1 + a] = (1/2pi^2) int P j0(k chi1[a]) j0(k chi2[b]) / k^2 dk. */
+int or_renormalization_grid(const double *k, const double *pk, size_t nk, double kmin,
+                            double kmax, const double *chi1, size_t n1, const double *chi2,
+                            size_t n2, double *out, int nthreads);
 
 /* -------------------------------------------------------------- background */
 typedef struct {

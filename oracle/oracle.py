@@ -67,6 +67,12 @@ def lib():
         L.or_integral_direct.argtypes = [_dp, _dp, C.c_size_t, C.c_int, C.c_int, C.c_double,
                                          C.c_double, C.c_double]
         L.or_integral_direct.restype = C.c_double
+        L.or_divergent_i40.argtypes = [_dp, _dp, C.c_size_t, C.c_double, C.c_double, _dp,
+                                       C.c_size_t, _dp, _dp, C.c_int]
+        L.or_divergent_separations.argtypes = [_dp, C.c_size_t]
+        L.or_divergent_separations.restype = C.c_size_t
+        L.or_renormalization_grid.argtypes = [_dp, _dp, C.c_size_t, C.c_double, C.c_double, _dp,
+                                              C.c_size_t, _dp, C.c_size_t, _dp, C.c_int]
         L.or_background_nodes.argtypes = [C.POINTER(_Cosmo), C.c_size_t] + [_dp] * 9
         L.or_gauss_legendre.argtypes = [C.c_size_t, _dp, _dp]
         L.or_model_new.restype = C.c_void_p
@@ -209,6 +215,40 @@ def integral_direct(k, pk, n, l, r, kmin=None, kmax=None):
     kmin = float(k[0] if kmin is None else kmin)
     kmax = float(k[-1] if kmax is None else kmax)
     return lib().or_integral_direct(k, pk, len(k), n, l, float(r), kmin, kmax)
+
+
+def divergent_separations():
+    """The fixed separations (Mpc) of the divergent integral (integrals.c:76-103)."""
+    n = lib().or_divergent_separations(np.zeros(1), 0)
+    out = np.zeros(n)
+    lib().or_divergent_separations(out, n)
+    return out
+
+
+def divergent_i40(k, pk, r, kmin=None, kmax=None, nthreads=0):
+    """(r^4 I^4_0(r), r^4 x its r = 0 renormalisation integral), both / 2 pi^2, at
+    separations r (integrals.c:773-845)."""
+    k, pk, r = _f64(k), _f64(pk), _f64(np.atleast_1d(r))
+    kmin = float(k[0] if kmin is None else kmin)
+    kmax = float(k[-1] if kmax is None else kmax)
+    res, res0 = np.zeros(len(r)), np.zeros(len(r))
+    if lib().or_divergent_i40(k, pk, len(k), kmin, kmax, r, len(r), res, res0, nthreads) != 0:
+        raise ValueError("divergent integral failed")
+    return res, res0
+
+
+def renormalization_grid(k, pk, chi1, chi2, kmin=None, kmax=None, nthreads=0):
+    """out[b, a] = (1/2pi^2) int P j0(k chi1[a]) j0(k chi2[b]) / k^2 dk
+    (integrals.c:424-444)."""
+    k, pk = _f64(k), _f64(pk)
+    c1, c2 = _f64(np.atleast_1d(chi1)), _f64(np.atleast_1d(chi2))
+    kmin = float(k[0] if kmin is None else kmin)
+    kmax = float(k[-1] if kmax is None else kmax)
+    out = np.zeros((len(c2), len(c1)))
+    if lib().or_renormalization_grid(k, pk, len(k), kmin, kmax, c1, len(c1), c2, len(c2), out,
+                                     nthreads) != 0:
+        raise ValueError("renormalisation grid failed")
+    return out
 
 
 def background_nodes(omega_m=0.3, omega_baryon=0.05, omega_gamma=9e-5, h=0.67, bins=10000):

@@ -6,7 +6,8 @@ Run once where the reference tree is available:
 It writes golden.npz next to this script.  The integral tables (10001 rows
 each) are thinned to the rows the reference's Python test checks
 (1.5 < r < 20000 Mpc, tests/test_coffe.py:196-233), every 8th row; all other
-files are copied whole except the background (every 4th of its 10001 rows).  The values are the reference's published outputs,
+files are copied whole except the background (every 4th of its 10001 rows) and
+the renormalisation grid of the divergent integral (every 10th chi node).  The values are the reference's published outputs,
 not recomputed.
 """
 import sys
@@ -47,6 +48,11 @@ def main(ref: Path):
                 bench / f"benchmark_multipoles_covariance_{a}{b}.dat")
             out[f"avg_multipoles_covariance_{a}{b}"] = np.loadtxt(
                 bench / f"benchmark_avg_multipoles_covariance_{a}{b}.dat")
+    # the divergent I^4_0 (every row) and its renormalisation grid (every 10th
+    # of the 201 chi nodes in each direction: 21 x 21 of its 40401 rows)
+    out["integral8"] = np.loadtxt(bench / "benchmark_integral8.dat")
+    ren = np.loadtxt(bench / "benchmark_integral8_renormalization.dat").reshape(201, 201, 3)
+    out["integral8_renormalization"] = ren[::10, ::10].reshape(-1, 3)
     dst = Path(__file__).resolve().parent / "golden.npz"
     np.savez_compressed(dst, **out)
     print(dst, dst.stat().st_size, "bytes")

@@ -58,3 +58,14 @@ def test_library_loads_and_reports_errors_without_gpu(libpath):
     st = L.coffe_gpu_ctx_create(0, ctypes.byref(ctx))
     assert st == -2 and not ctx.value  # COFFE_GPU_ECUDA, no context, no fallback
     assert L.coffe_gpu_ctx_destroy(None) == 0
+
+
+def test_divergent_separations_equal_the_oracle(libpath, oracle):
+    """The library's copy of the reference's fixed separations of I^4_0
+    (integrals.c:76-103) is the oracle's, value for value (a host-only call)."""
+    import numpy as np
+
+    from coffe_gb300 import divergent_separations
+
+    got = divergent_separations()
+    assert len(got) == 297 and np.array_equal(got, oracle.divergent_separations())

@@ -209,3 +209,39 @@ def test_average_multipoles_match_golden(golden, lens_model):
         d = golden[f"avg_multipoles{l}"]
         got = lens_model.average_multipoles(3, 0.9, 1.1, d[:, 0] / H, l, n_z=16)
         assert np.allclose(got, d[:, 1], rtol=5e-4), (l, got / d[:, 1] - 1)
+
+
+# the reference's default k range, 1e-5 .. 300 h/Mpc (parser.c:840-841), in 1/Mpc
+DIV_KMIN, DIV_KMAX = 1e-5 * H, 300.0 * H
+
+
+def test_divergent_integral_matches_golden(golden, oracle, class_pk):
+    """r^4 I^4_0 (integrals.c:773-845) at the reference's golden separations
+    (benchmark_integral8.dat, tests/test_integrals.c:156-201): directly at each
+    separation to 1e-8, and through the Akima spline on the reference's fixed
+    separations at the test's 1e-3 (the rows inside that list's range)."""
+    k, pk = class_pk
+    d = golden["integral8"]
+    r = d[:, 0] / (COFFE_H0 * H)
+    scale = (COFFE_H0 * H) ** 4
+    res, _ = oracle.divergent_i40(k, pk, r, DIV_KMIN, DIV_KMAX)
+    assert np.allclose(res * scale, d[:, 1], rtol=1e-8)
+    seps = oracle.divergent_separations()
+    assert len(seps) == 297 and np.all(np.diff(seps) > 0)
+    res, _ = oracle.divergent_i40(k, pk, seps, DIV_KMIN, DIV_KMAX)
+    inside = r <= seps[-1]
+    val = oracle.spline_eval("akima", seps, res, r[inside])
+    assert np.allclose(val * scale, d[inside, 1], rtol=1e-3)
+
+
+def test_renormalization_grid_matches_golden(golden, oracle, class_pk):
+    """The renormalisation grid (integrals.c:424-444, 848-903) at every 10th of the
+    golden file's 201 x 201 chi nodes (benchmark_integral8_renormalization.dat,
+    tests/test_integrals.c:203-248, made with chi_max = chi(z = 1.1)) to 1e-5."""
+    k, pk = class_pk
+    ren = golden["integral8_renormalization"]
+    n = int(round(np.sqrt(len(ren))))
+    chi1 = ren[::n, 0] / (COFFE_H0 * H)
+    chi2 = ren[:n, 1] / (COFFE_H0 * H)
+    grid = oracle.renormalization_grid(k, pk, chi1, chi2, DIV_KMIN, DIV_KMAX)
+    assert np.allclose(grid.T * (COFFE_H0 * H) ** 4, ren[:, 2].reshape(n, n), rtol=1e-5)
