@@ -47,6 +47,9 @@ struct LensArgs {
     // mu_w (the upper half twice when the terms are even in mu)
     int mu0, n_mu_run;
     double mu_w;
+    // the terms are even in mu: an even multipole of a run over every node
+    // sums the mu > 0 half twice, as it does when only that half is evaluated
+    int sym;
     int tab_len, n_terms;
     int term[LENS_NT];
     double inv_dlog; // N / ln(kmax/kmin), r0 = 1
@@ -692,22 +695,32 @@ __global__ void lens_reduce_kernel(LensArgs a, const double *__restrict__ rule,
                                    const double *__restrict__ part_s, long long n_pairs,
                                    double *__restrict__ out, int *err)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n_pairs * a.n_l) return;
+    // one warp per (pair, l); lanes take the mu nodes from the first one the
+    // multipole sums (so a multipole's terms meet in the same lanes and order
+    // whether or not the mu < 0 half was evaluated)
+    const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (t >= n_pairs * a.n_l) return; // whole warps leave together
     const long long pl = t / a.n_l;
     const int j = (int)(t % a.n_l);
     const int l = a.ls[j];
+    const bool half = a.sym && l % 2 == 0 && a.n_mu_run == a.n_mu;
+    const int first = half ? a.n_mu / 2 : a.mu0, end = a.mu0 + a.n_mu_run;
+    const double w = (half ? 2.0 : a.mu_w) * 0.5;
     double sum = 0;
-    for (int k = 0; k < a.n_mu_run; ++k) {
-        const int im = a.mu0 + k;
+    for (int im = first + lane; im < end; im += 32) {
+        const int k = im - a.mu0;
         double v = 0;
         if (part_d) v += part_d[pl * a.n_mu_run + k];
         if (part_s) v += part_s[pl * a.n_mu_run + k];
-        sum += a.mu_w * 0.5 * rule[a.n_mu + im] * v * lens_legendre(l, rule[im]);
+        sum += w * rule[a.n_mu + im] * v * lens_legendre(l, rule[im]);
     }
-    const double res = (2 * l + 1) * sum;
-    if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
-    out[(a.pair0 + pl) * a.n_l + j] += res;
+    sum = warp_sum(sum);
+    if (lane == 0) {
+        const double res = (2 * l + 1) * sum;
+        if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
+        out[(a.pair0 + pl) * a.n_l + j] += res;
+    }
 }
 
 // correlation function: out[pair][m] += single + double partials at mu_m
@@ -929,7 +942,7 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
             if ((st = cg_after_launch(ctx, "lens_cf_reduce_kernel"))) return st;
         } else {
             const long long nt = np * a.n_l;
-            lens_reduce_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, ctx->stream>>>(
+            lens_reduce_kernel<<<(unsigned)((nt + 3) / 4), 128, 0, ctx->stream>>>(
                 a, rule, do_double ? part_d : nullptr, single ? part_s : nullptr, np, out,
                 ctx->d_err);
             if ((st = cg_after_launch(ctx, "lens_reduce_kernel"))) return st;
@@ -1072,6 +1085,7 @@ static int lens_args(coffe_gpu_ctx *ctx, int contrib, int n_req, int n_l, const 
     a.mu0 = 0;
     a.n_mu_run = n_mu;
     a.mu_w = 1.0;
+    a.sym = 0;
     a.n_x = ctx->lens_n_x;
     a.nh = (a.n_x % 2 == 0) ? a.n_x / 2 : 0;
     a.contrib = contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD | COFFE_GPU_LEN);
@@ -1185,14 +1199,16 @@ int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, i
     if ((st = lens_args(ctx, contrib, n_req, n_l, l, ctx->lens_n_mu, &a))) return st;
     // mu -> -mu swaps chi1 and chi2, i.e. the roles of the two tracers: when
     // they share their magnification bias (and, for density-lensing, their
-    // galaxy bias) both lensing terms are even in mu, so even multipoles need
-    // only the rule's nodes with mu > 0 (the rule is symmetric), counted twice
+    // galaxy bias) both lensing terms are even in mu, so each even multipole
+    // is summed over the rule's nodes with mu > 0 (the rule is symmetric),
+    // counted twice; odd multipoles over every node, which are then evaluated
     auto same_tracer = [&](int i, int j) {
         return (!ctx->bias_set[i] && !ctx->bias_set[j]) ||
                (ctx->bias_set[i] && ctx->bias_set[j] && ctx->bias_host[i] == ctx->bias_host[j]);
     };
-    bool mirror = a.n_mu % 2 == 0 && same_tracer(2, 3) &&
-                  (!(single_full && (contrib & COFFE_GPU_DEN)) || same_tracer(0, 1));
+    a.sym = a.n_mu % 2 == 0 && same_tracer(2, 3) &&
+            (!(single_full && (contrib & COFFE_GPU_DEN)) || same_tracer(0, 1));
+    bool mirror = a.sym;
     for (int j = 0; j < n_l; ++j) mirror = mirror && l[j] % 2 == 0;
     if (mirror) {
         a.mu0 = a.n_mu / 2;

@@ -225,10 +225,11 @@ int coffe_gpu_set_flatsky(coffe_gpu_ctx_t *ctx, int local_nonlocal, int nonlocal
    the line's integrand peak (n_x even).  The single-integrated den/rsd-lensing
    terms (functions.c:1486-2483) use n_mu x n_x nodes, lensing-lensing
    (functions.c:3460-3836) n_mu x n_x x n_x.  When both tracers share their
-   magnification bias (and, with density-lensing, their galaxy bias), all
-   multipoles are even and n_mu is even, the terms are even in mu (mu -> -mu
-   exchanges the tracers) and only the n_mu / 2 nodes with mu > 0 are
-   evaluated, each counted twice.  Defaults 128 and 256; 2 <= n_mu, n_x <= 4096. */
+   magnification bias (and, with density-lensing, their galaxy bias) and n_mu
+   is even, the terms are even in mu (mu -> -mu exchanges the tracers): each
+   even multipole sums the n_mu / 2 nodes with mu > 0, each counted twice, and
+   only those nodes are evaluated unless an odd multipole (which sums every
+   node) is requested too.  Defaults 128 and 256; 2 <= n_mu, n_x <= 4096. */
 int coffe_gpu_set_lensing_rule(coffe_gpu_ctx_t *ctx, int n_mu, int n_x);
 
 /* Stream-ordered variant of coffe_gpu_multipoles for device-resident

@@ -1496,11 +1496,12 @@ static int same_tracer(const or_model_t *m, int i, int j)
 /* The lensing multipoles on the product rule.  mu -> -mu swaps chi1 and chi2,
    i.e. the roles of the two tracers; when they share their magnification bias
    (and, with density-lensing, their galaxy bias) both lensing terms are even
-   in mu, and even multipoles are summed over the rule's nodes with mu > 0
-   (the Gauss-Legendre rule is symmetric), each counted twice.  Quadrature
-   choice of this restatement (the reference uses Cuhre): the plane rule at a
-   node -mu is the one at mu with x1 and x2 exchanged, equal to it up to the
-   rule's own error. */
+   in mu, and each even multipole is summed over the rule's nodes with mu > 0
+   (the Gauss-Legendre rule is symmetric), each counted twice, whatever else
+   the list holds; odd multipoles over every node (nodes mu < 0 are evaluated
+   only when an odd one is asked for).  Quadrature choice of this restatement
+   (the reference uses Cuhre): the plane rule at a node -mu is the one at mu
+   with x1 and x2 exchanged, equal to it up to the rule's own error. */
 int or_multipoles_lensing_gl(const or_model_t *m, int contrib, double z_mean, double sep,
                              int n_l, const int *ls, size_t n_mu, size_t n_x, double *out)
 {
@@ -1518,12 +1519,13 @@ int or_multipoles_lensing_gl(const or_model_t *m, int contrib, double z_mean, do
     const int single = (contrib & OR_CONTRIB_LEN) && (contrib & (OR_CONTRIB_DEN | OR_CONTRIB_RSD));
     const int dbl = (contrib & OR_CONTRIB_LEN) != 0;
     const or_line_rule_t R = {n_x, xf, wf, xh, wh};
-    int mirror = n_mu % 2 == 0 && same_tracer(m, 2, 3) &&
-                 (!(single && (contrib & OR_CONTRIB_DEN)) || same_tracer(m, 0, 1));
+    const int sym = n_mu % 2 == 0 && same_tracer(m, 2, 3) &&
+                    (!(single && (contrib & OR_CONTRIB_DEN)) || same_tracer(m, 0, 1));
+    int all_even = 1;
     for (int j = 0; j < n_l; ++j)
-        mirror = mirror && ls[j] % 2 == 0;
-    for (size_t i = mirror ? n_mu / 2 : 0; i < n_mu; ++i) {
-        const double mu = xm[i], wmu = (mirror ? 1.0 : 0.5) * wm[i]; /* dv = dmu / 2 */
+        all_even = all_even && ls[j] % 2 == 0;
+    for (size_t i = (sym && all_even) ? n_mu / 2 : 0; i < n_mu; ++i) {
+        const double mu = xm[i], wmu = 0.5 * wm[i]; /* dv = dmu / 2 */
         const or_lens_geom_t g = lens_geom(m, z_mean, mu, sep);
         double acc = 0.0;
         if (single) {
@@ -1536,7 +1538,13 @@ int or_multipoles_lensing_gl(const or_model_t *m, int contrib, double z_mean, do
                 const double xs = x1 * g.chi1 / g.chi2;
                 acc += 0.5 * wf[a] * lens_line(0, 1, xs, &R, 2, m, contrib, z_mean, mu, sep, x1);
             }
-        for (int j = 0; j < n_l; ++j) out[j] += wmu * acc * or_legendre(ls[j], mu);
+        for (int j = 0; j < n_l; ++j) {
+            /* even l of equal tracers: the mu > 0 half, twice; else every node */
+            const int half = sym && ls[j] % 2 == 0;
+            if (half && i < n_mu / 2)
+                continue;
+            out[j] += (half ? 2.0 : 1.0) * wmu * acc * or_legendre(ls[j], mu);
+        }
     }
     for (int j = 0; j < n_l; ++j) out[j] *= (2 * ls[j] + 1);
     free(xm); free(wm); free(xf); free(wf); free(xh); free(wh);

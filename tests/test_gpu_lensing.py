@@ -104,10 +104,11 @@ def test_lensing_mixed_close_to_oracle(gpu_ctx, lens_setup):
 @pytest.mark.parametrize("case", ["equal", "different_s", "different_b", "odd_l"])
 def test_lensing_tracer_symmetry(oracle, lens_tables, case):
     """The lensing terms are even in mu when both tracers share their biases,
-    and the rule's mu > 0 half is then counted twice (GPU and oracle alike);
-    with different magnification (or, for density-lensing, galaxy) biases, or
-    odd multipoles, every mu node is evaluated.  FP64 at 1e-10 against the
-    oracle in each case.  For equal tracers the mirrored sum differs from the
+    and each even multipole then sums the rule's mu > 0 half twice (GPU and
+    oracle alike), whatever else the list holds; with different magnification
+    (or, for density-lensing, galaxy) biases every multipole sums every node.
+    FP64 at 1e-10 against the oracle in each case; with odd multipoles in the
+    list the even ones equal those of an even-only list bit for bit.  For equal tracers the mirrored sum differs from the
     sum over every node of the same rule only by the rule's own error (the
     plane rule at -mu is the one at mu with x1 and x2 exchanged): on this
     16 x 32 rule 2.3e-3 of the largest l = 4 value, while both are 4.5e-2 away
@@ -145,6 +146,17 @@ def test_lensing_tracer_symmetry(oracle, lens_tables, case):
         e_odd = np.max(np.abs(got[:, ~even] - ref[:, ~even]), initial=0) / np.abs(ref).max()
         print(case, "fp64 max rel error", e, "odd", e_odd)
         assert e < 1e-10 and e_odd < 1e-10, (case, e, e_odd)
+        if case == "odd_l":  # the even multipoles do not depend on the list
+            # (the nonintegrated part's own rule does: 31 mirrored GK61 nodes for
+            # even-only lists, all 61 otherwise, so the totals agree to rounding)
+            only_even = ctx.multipoles([0], [1.2], [0, len(sep)], sep, (0, 2),
+                                       contrib=DEN | RSD | LEN)
+            assert np.allclose(got[:, [0, 2]], only_even, rtol=1e-12, atol=0)
+            lens_odd = ctx.multipoles([0], [1.2], [0, len(sep)], sep, ls, contrib=LEN)
+            lens_even = ctx.multipoles([0], [1.2], [0, len(sep)], sep, (0, 2), contrib=LEN)
+            assert np.array_equal(lens_odd[:, [0, 2]], lens_even)
+            assert np.array_equal(lens[:, [0, 2]],
+                                  m.multipoles_lensing(DEN | RSD | LEN, 1.2, sep, (0, 2), *rule))
         if case == "equal":
             m.set_bias(3, zb, s2 * (1 + 1e-15))  # other samples: no longer the same tracer
             full = m.multipoles_lensing(DEN | RSD | LEN, 1.2, sep, ls, *rule)
