@@ -1,7 +1,7 @@
 /*
  * coffe_oracle.c -- FP64 CPU restatement of COFFE's correlation-function hot
- * path.  TEST INFRASTRUCTURE ONLY: the checker for the GPU product, never part
- * of it.  See coffe_oracle.h for the contract and the reference citations.
+ * path.  TEST INFRASTRUCTURE ONLY: the oracle the tests compare the GPU product
+ * against, never part of it.  See coffe_oracle.h for the contract and the reference citations.
  *
  * Build: make -C oracle  (gcc -O2 -fopenmp -ffp-contract=off, shared library)
  */

@@ -1,8 +1,8 @@
 /*
  * coffe_oracle.h -- CPU restatement of the COFFE correlation-function hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU product
- * (coffe_gb300).  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle the tests compare the
+ * GPU product (coffe_gb300) against.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
  * baseline leg may load it; the product never links, imports or calls it.
  *
  * Every routine restates, in FP64 and in code written for this project, the
