@@ -54,3 +54,32 @@ def test_mapped_output_equals_copied_output():
     finally:
         ctx.close()
 
+
+
+def test_mapped_output_with_lensing_takes_the_copy_path(oracle):
+    """With lensing the results are accumulated over several kernels: a
+    page-locked output then goes through the device copy, and equals the
+    pageable-output call."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from coffe_gb300 import workloads
+    from coffe_gb300.api import Context
+
+    c = workloads.cfg1()
+    terms = [(0, 0), (0, 2), (0, 4), (1, 1), (1, 3), (2, 0)]
+    sep = np.array([20.0, 80.0, 200.0]) / 0.67
+    ctx = Context(0)
+    try:
+        ctx.background_init(0.31, 0.05, 9e-5, 0.67, 10000)
+        ctx.integrals_init(c["k"], c["pk"][None, :], terms, N=4096, precision="mixed",
+                           small_r=True)
+        ctx.set_lensing_rule(16, 32)
+        pinned = torch.zeros((len(sep), 3), dtype=torch.float64).pin_memory().numpy()
+        got = ctx.multipoles([0], [1.5], [0, len(sep)], sep, (0, 2, 4), contrib=7,
+                             precision="mixed", out=pinned)
+        ref = ctx.multipoles([0], [1.5], [0, len(sep)], sep, (0, 2, 4), contrib=7,
+                             precision="mixed")
+        assert np.isfinite(ref).all() and np.array_equal(got, ref)
+    finally:
+        ctx.close()
