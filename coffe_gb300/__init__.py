@@ -10,9 +10,9 @@ of ``include/coffe_gpu.h``; this package is its Python host side:
 
 There is no CPU fallback: without the library or a CUDA device the calls raise.
 """
-from .api import (DEFAULT_TERMS, DEN_RSD_TERMS, AverageMultipoles, Coffe, Context,  # noqa: F401
-                  Corrfunc, Multipoles, divergent_separations)
+from .api import (DEFAULT_TERMS, DEN_RSD_TERMS, AverageCovariance, AverageMultipoles,  # noqa: F401
+                  Coffe, Context, Corrfunc, Covariance, Multipoles, divergent_separations)
 from ._lib import CoffeGpuError  # noqa: F401
 
-__all__ = ["AverageMultipoles", "Coffe", "Context", "Corrfunc", "Multipoles", "CoffeGpuError", "DEFAULT_TERMS",
+__all__ = ["AverageCovariance", "AverageMultipoles", "Coffe", "Covariance", "Context", "Corrfunc", "Multipoles", "CoffeGpuError", "DEFAULT_TERMS",
            "DEN_RSD_TERMS", "divergent_separations"]

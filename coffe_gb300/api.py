@@ -495,6 +495,32 @@ class Corrfunc:
         return {"z": self.z, "r": self.r, "mu": self.mu, "value": self.value}
 
 
+@dataclass
+class Covariance:
+    """One covariance value (python/coffe/representation.py's Covariance record)."""
+
+    z: float
+    r1: float
+    r2: float
+    l1: int
+    l2: int
+    value: float
+
+
+@dataclass
+class AverageCovariance:
+    """One covariance value of the averaged multipoles (representation.py's
+    AverageCovariance record)."""
+
+    z_min: float
+    z_max: float
+    r1: float
+    r2: float
+    l1: int
+    l2: int
+    value: float
+
+
 def divergent_separations() -> np.ndarray:
     """The fixed separations (Mpc) on which the reference splines the divergent
     integral I^4_0 (integrals.c:76-103)."""
@@ -525,7 +551,9 @@ class Coffe:
                  z_max=(1.1,), has_density=True,
                  has_rsd=False, has_lensing=False,
                  integrals_fftlog_sampling=4096, background_bins=10000,
-                 integration_1d_prec=1e-5, precision="fp64", device=0):
+                 integration_1d_prec=1e-5, precision="fp64", deltaz=(0.2,),
+                 number_density1=(), number_density2=(), pixelsize=(10.0,), fsky=(1.0,),
+                 covariance_fftlog_sampling=8192, device=0):
         self._ctx = Context(device)
         self.omega_m = float(omega_m)
         self.omega_baryon = float(omega_baryon)
@@ -547,6 +575,15 @@ class Coffe:
         self.background_bins = int(background_bins)
         self.integration_1d_prec = float(integration_1d_prec)
         self.precision = precision
+        # covariance parameters, one value per z_mean (or per averaging window):
+        # half-width deltaz, number densities (1/Mpc^3), pixel size (Mpc), sky
+        # fraction (parser.c:934-939 defaults for pixelsize and fsky)
+        self.deltaz = [float(v) for v in deltaz]
+        self.number_density1 = [float(v) for v in number_density1]
+        self.number_density2 = [float(v) for v in number_density2]
+        self.pixelsize = [float(v) for v in pixelsize]
+        self.fsky = [float(v) for v in fsky]
+        self.covariance_fftlog_sampling = int(covariance_fftlog_sampling)
         self._k = None
         self._pk = None
         self._bg_ready = False
@@ -703,6 +740,58 @@ class Coffe:
                 for js, r in enumerate(self.sep):
                     res.append(Corrfunc(z=zm, r=float(r), mu=m, value=float(vals[iz * ns + js, im])))
         return res
+
+    def _covariance_contrib(self) -> int:
+        c = (_lib.DEN if self.has_density else 0) | (_lib.RSD if self.has_rsd else 0)
+        if c == 0:
+            raise ValueError("the covariance needs has_density and/or has_rsd")
+        return c
+
+    def compute_covariance_bulk(self) -> List["Covariance"]:
+        """Covariance of the multipoles for every z_mean, in the reference's
+        order: z outer, then l1, r1, l2, r2 (coffe.pyx:3428-3480,
+        covariance.c:1046-1059); the FFTLog method with covariance_fftlog_sampling
+        points."""
+        nz = len(self.z_mean)
+        if not all(len(v) == nz for v in (self.deltaz, self.number_density1,
+                                          self.number_density2, self.pixelsize, self.fsky)):
+            raise ValueError("Mismatching lengths for covariance parameters (`z_mean`, `deltaz`, "
+                             "`number_density1`, `number_density2`, `pixelsize`, `fsky`)")
+        if self._k is None:
+            raise ValueError("set_power_spectrum_linear first")
+        if not self._bg_ready:
+            self._background_init()
+        cov = self._ctx.covariance_multipoles(
+            self._k, self._pk, self.covariance_fftlog_sampling, self.z_mean, self.deltaz,
+            self.fsky, self.number_density1, self.number_density2, self.pixelsize, self.l,
+            self.sep, self._covariance_contrib())
+        return [Covariance(z=float(zm), r1=float(r1), r2=float(r2), l1=l1, l2=l2,
+                           value=float(cov[iz, i, a, j, b]))
+                for iz, zm in enumerate(self.z_mean)
+                for i, l1 in enumerate(self.l) for a, r1 in enumerate(self.sep)
+                for j, l2 in enumerate(self.l) for b, r2 in enumerate(self.sep)]
+
+    def compute_average_covariance_bulk(self) -> List["AverageCovariance"]:
+        """Covariance of the redshift-averaged multipoles for every window
+        (z_min, z_max), in the reference's order (coffe.pyx:3482-3537)."""
+        nw = len(self.z_min)
+        if not all(len(v) == nw for v in (self.z_max, self.number_density1,
+                                          self.number_density2, self.pixelsize, self.fsky)):
+            raise ValueError("Mismatching lengths for average covariance parameters (`z_min`, "
+                             "`z_max`, `number_density1`, `number_density2`, `pixelsize`, `fsky`)")
+        if self._k is None:
+            raise ValueError("set_power_spectrum_linear first")
+        if not self._bg_ready:
+            self._background_init()
+        cov = self._ctx.average_covariance_multipoles(
+            self._k, self._pk, self.covariance_fftlog_sampling, self.z_min, self.z_max,
+            self.fsky, self.number_density1, self.number_density2, self.pixelsize, self.l,
+            self.sep, self._covariance_contrib())
+        return [AverageCovariance(z_min=float(a_), z_max=float(b_), r1=float(r1), r2=float(r2),
+                                  l1=l1, l2=l2, value=float(cov[iw, i, a, j, b]))
+                for iw, (a_, b_) in enumerate(zip(self.z_min, self.z_max))
+                for i, l1 in enumerate(self.l) for a, r1 in enumerate(self.sep)
+                for j, l2 in enumerate(self.l) for b, r2 in enumerate(self.sep)]
 
     def close(self):
         self._ctx.close()

@@ -156,3 +156,35 @@ def test_average_covariance_golden_through_gpu(gpu_ctx, golden):
     with pytest.raises(CoffeGpuError):  # z_max <= z_min
         gpu_ctx.average_covariance_multipoles(k, pk, 1024, [1.1], [0.9], [0.2], [1e-3], [1e-3],
                                               [50 / H], (0,), sep)
+
+
+def test_coffe_mirror_covariance_bulk(golden):
+    """Coffe.compute_covariance_bulk / compute_average_covariance_bulk in the
+    reference's order (z or window outer, then l1, r1, l2, r2) against the
+    golden covariances at the tolerance of the Context tests above."""
+    from coffe_gb300.api import Coffe
+
+    k, pk = golden["pk_class"].T
+    sep = np.arange(50, 350, 50) / H
+    cosmo = Coffe(sep=sep, l=[0, 2, 4], z_mean=[1.0], deltaz=[0.1], z_min=[0.9], z_max=[1.1],
+                  number_density1=[1e-3 * H ** 3], number_density2=[1e-3 * H ** 3],
+                  pixelsize=[50 / H], fsky=[0.2], has_density=True, has_rsd=True)
+    try:
+        cosmo.set_power_spectrum_linear(k * H, pk / H ** 3)
+        for name, res in (("multipoles_covariance", cosmo.compute_covariance_bulk()),
+                          ("avg_multipoles_covariance", cosmo.compute_average_covariance_bulk())):
+            assert len(res) == 9 * 36
+            assert (res[0].l1, res[0].l2, res[0].r1, res[0].r2) == (0, 0, sep[0], sep[0])
+            assert (res[1].r1, res[1].r2) == (sep[0], sep[1])
+            assert (res[6].r1, res[6].l2) == (sep[0], 2)
+            vals = np.array([r.value for r in res]).reshape(3, 6, 3, 6)
+            for i, l1 in enumerate((0, 2, 4)):
+                for j, l2 in enumerate((0, 2, 4)):
+                    d = golden[f"{name}_{l1}{l2}"][:, 2].reshape(6, 6)
+                    e = np.abs(vals[i, :, j, :] - d).max() / np.abs(d).max()
+                    assert e < 1e-2, (name, l1, l2, e)
+        cosmo.number_density2 = []
+        with pytest.raises(ValueError):
+            cosmo.compute_covariance_bulk()
+    finally:
+        cosmo.close()
