@@ -166,6 +166,55 @@ __device__ __forceinline__ TT lens_at_zero(const typename Rec4<TT>::type *__rest
     return ldg_c4(recs + t).x;
 }
 
+// Mixed lensing-lensing integrand regrouped by powers of ll = lambda1 lambda2
+// (functions.c:3695-3775, checked equal symbolically):
+//   v = ct A + ll (c2m B + ct^2 C) + ll^2 c2m ct D / r^2 + ll^3 c2m^2 E / r^4,
+//   A = 4/3 I20 + 4/15 r^2 S, C = 8/5 S, S = I11 + I13,
+//   B = 2/5 I00 + 4/7 I02 + 6/35 I04, D = 6/7 (I02 + I04) + 2 I13, E = I04:
+// five functions of r, whose Akima records are the same combinations of the
+// six tables' records (the interpolant is linear in the records), stored
+// rec5[(s * (len - 1) + i) * 5 + u] for u = I20, S, B, D, E.
+#define LENS_NC 5
+__global__ void lens_combine_kernel(const float4 *__restrict__ rec, long long n_int,
+                                    float4 *__restrict__ rec5)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_int) return;
+    const float4 *p = rec + i * LENS_NT;
+    const float4 i00 = p[L00], i02 = p[L02], i04 = p[L04], i11 = p[L11], i13 = p[L13],
+                 i20 = p[L20];
+    auto lin = [](float a, float4 x, float b, float4 y, float c, float4 z) {
+        return make_float4(a * x.x + b * y.x + c * z.x, a * x.y + b * y.y + c * z.y,
+                           a * x.z + b * y.z + c * z.z, a * x.w + b * y.w + c * z.w);
+    };
+    float4 *q = rec5 + i * LENS_NC;
+    q[0] = i20;
+    q[1] = lin(1.f, i11, 1.f, i13, 0.f, i13);
+    q[2] = lin(0.4f, i00, 4.f / 7.f, i02, 6.f / 35.f, i04);
+    q[3] = lin(6.f / 7.f, i02, 6.f / 7.f, i04, 2.f, i13);
+    q[4] = i04;
+}
+
+// the five combined functions at r (NaN outside the tables)
+__device__ __forceinline__ void lens_tables5(const float4 *__restrict__ recs5,
+                                             const float *__restrict__ x, int n, float inv_dlog,
+                                             float r, float (&v)[LENS_NC])
+{
+    const int i = lens_interval<float>(x, n, inv_dlog, r);
+    if (i < 0) {
+#pragma unroll
+        for (int u = 0; u < LENS_NC; ++u) v[u] = cg_nan<float>();
+        return;
+    }
+    const float dx = r - __ldg(x + i);
+    const float4 *p = recs5 + (size_t)i * LENS_NC;
+#pragma unroll
+    for (int u = 0; u < LENS_NC; ++u) {
+        const float4 c = __ldg(p + u);
+        v[u] = c.x + dx * (c.y + dx * (c.z + c.w * dx));
+    }
+}
+
 // Geometry of one (pair, mu node), functions.c:1498-1509 / 3473-3481, with
 // cos(theta) = 1 - s, s = sep^2 (1 - mu^2) / (2 chi1 chi2) (no cancellation)
 struct LensGeom {
@@ -259,6 +308,7 @@ __global__ void __launch_bounds__(LENS_THREADS)
     lens_double_kernel(LensArgs a, LensBg64 g64, LensBgT<S> gT, LensPoly poly,
                        const TT *__restrict__ tab_x,
                        const typename Rec4<TT>::type *__restrict__ rec,
+                       const float4 *__restrict__ rec5,
                        const int *__restrict__ req_spectrum, const double *__restrict__ req_z_mean,
                        const int64_t *__restrict__ req_offset, const double *__restrict__ sep,
                        const double *__restrict__ rule, double *__restrict__ part, int *err)
@@ -278,6 +328,8 @@ __global__ void __launch_bounds__(LENS_THREADS)
     const double s2 = a.has_s2 ? spl_eval(g64.s2, G.z2c) : 0.0;
     const double pre = 9. * a.Om * a.Om * (2 - 5 * s1) * (2 - 5 * s2) / 4. * G.chi1 * G.chi2 * a.pref4;
     const typename Rec4<TT>::type *recs = rec + (size_t)s * (a.tab_len - 1) * LENS_NT;
+    const float4 *recs5 =
+        sizeof(T) == 4 ? rec5 + (size_t)s * (a.tab_len - 1) * LENS_NC : nullptr;
     const T chi1 = (T)G.chi1, chi2 = (T)G.chi2, ss = (T)G.s, ct = (T)G.ct, c2m = (T)(-G.omc2);
     const T i11_0 = (T)lens_at_zero<TT>(recs, L11);
     const TT inv_dlog = (TT)a.inv_dlog;
@@ -342,20 +394,20 @@ __global__ void __launch_bounds__(LENS_THREADS)
                 const T r2 = dl * dl + T(2) * ll * ss;
                 T v;
                 if (r2 > T(1e-20)) {
-                    T I[LENS_NT];
-                    lens_tables<T, TT>(recs, tab_x, a.tab_len, inv_dlog, sqrt(r2), I);
                     // functions.c:3695-3775
-                    if (F32) { // the same terms with reciprocals instead of divisions
+                    if (F32) { // regrouped in powers of ll over the five combined tables
+                        float Q[LENS_NC];
+                        lens_tables5(recs5, (const float *)tab_x, a.tab_len, (float)inv_dlog,
+                                     (float)sqrt(r2), Q);
                         const T ir2 = T(1) / r2;
-                        const T ctll = ct * ll, c2ll = c2m * ll;
-                        v = c2ll * I[L00] * T(0.4) + ct * I[L20] * T(4.0 / 3.0) +
-                            ct * (r2 + T(6) * ctll) * I[L11] * T(4.0 / 15.0) +
-                            c2ll * (T(2) * r2 + T(3) * ctll) * I[L02] * (T(2.0 / 7.0) * ir2) +
-                            ct * (T(2) * r2 * r2 + T(12) * r2 * ctll + T(15) * c2ll * ll) * I[L13] *
-                                (T(2.0 / 15.0) * ir2) +
-                            c2ll * (T(6) * r2 * r2 + T(30) * r2 * ctll + T(35) * c2ll * ll) *
-                                I[L04] * (T(1.0 / 35.0) * ir2 * ir2);
+                        const T lc = ll * c2m * ir2;
+                        const T vA = ct * fmaf(T(4.0 / 15.0) * r2, Q[1], T(4.0 / 3.0) * Q[0]);
+                        const T vB = fmaf(c2m, Q[2], ct * ct * T(8.0 / 5.0) * Q[1]);
+                        const T vD = fmaf(lc, Q[4], ct * Q[3]); // ll c2m E / r^2 + ct D
+                        v = vA + ll * fmaf(lc, vD, vB);
                     } else {
+                        T I[LENS_NT];
+                        lens_tables<T, TT>(recs, tab_x, a.tab_len, inv_dlog, sqrt(r2), I);
                         v = T(2) * c2m * ll * I[L00] / T(5) + T(4) * ct * I[L20] / T(3) +
                             T(4) * ct * (r2 + T(6) * ct * ll) * I[L11] / T(15) +
                             T(2) * c2m * ll * (T(2) * r2 + T(3) * ct * ll) * I[L02] / T(7) / r2 +
@@ -899,12 +951,22 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
     typedef typename Rec4<TT>::type R;
     int st;
     const TT *tab_x = (const TT *)(sizeof(TT) == 8 ? ctx->tab_x.p : ctx->tab_x32.p);
-    const long long n_rec = (long long)ctx->n_spectra * (a.tab_len - 1) * LENS_NT;
-    if ((st = cg_ensure(ctx, ctx->lens_rec, sizeof(R) * (size_t)n_rec))) return st;
+    const long long n_int = (long long)ctx->n_spectra * (a.tab_len - 1);
+    const long long n_rec = n_int * LENS_NT;
+    // float path: the five combined records follow the six tables' records
+    const size_t rec_bytes = sizeof(R) * (size_t)n_rec +
+                             (sizeof(T) == 4 ? sizeof(float4) * (size_t)n_int * LENS_NC : 0);
+    if ((st = cg_ensure(ctx, ctx->lens_rec, rec_bytes))) return st;
     R *rec = (R *)ctx->lens_rec.p;
+    float4 *rec5 = sizeof(T) == 4 ? (float4 *)(rec + n_rec) : nullptr;
     lens_records_kernel<TT><<<(unsigned)((n_rec + 255) / 256), 256, 0, ctx->stream>>>(
         a, tab_x, (const TT *)ctx->tab_y.p, ctx->n_spectra, rec);
     if ((st = cg_after_launch(ctx, "lens_records_kernel"))) return st;
+    if (rec5 && do_double) {
+        lens_combine_kernel<<<(unsigned)((n_int + 255) / 256), 256, 0, ctx->stream>>>(
+            (const float4 *)rec, n_int, rec5);
+        if ((st = cg_after_launch(ctx, "lens_combine_kernel"))) return st;
+    }
     const bool single = do_single;
     // pairs per chunk: partials of at most 2^22 (pair, mu) items per kind
     const long long chunk = std::max(1LL, std::min(total, (1LL << 22) / a.n_mu_run));
@@ -919,8 +981,8 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
         a.n_items = np * a.n_mu_run;
         if (do_double) {
             lens_double_kernel<T, S, TT><<<(unsigned)a.n_items, LENS_THREADS, 0, ctx->stream>>>(
-                a, g64, gT, poly, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule,
-                part_d, ctx->d_err);
+                a, g64, gT, poly, tab_x, rec, rec5, req_spectrum, req_z_mean, req_offset, sep,
+                rule, part_d, ctx->d_err);
             if ((st = cg_after_launch(ctx, "lens_double_kernel"))) return st;
         }
         if (single) {
