@@ -142,6 +142,68 @@ def test_all_bessel_integrals_2e14_fp64(gpu_ctx, oracle, w):
     print("worst FP64 table error (2^14, 30 terms):", worst)
 
 
+def _cfg2_errors(got, ref):
+    """Errors of one config-2 table on r in [1, 1e4] Mpc/h: (max abs error /
+    the table's scale, the relative error with a floor of 1e-3 of the scale --
+    the convention of the multipole metric --, and the relative error with a
+    floor of only 1e-6 of the local envelope).  The last is reported, not
+    asserted: the n = -1 tables fall by many decades over the range, and where
+    they are far below their scale even the FP64 FFTLog's rounding (1e-15 of
+    the scale) is a large fraction of the value."""
+    scale = np.abs(ref).max()
+    d = np.abs(got - ref)
+    a = np.abs(ref)
+    env = np.array([a[max(0, i - 64): i + 65].max() for i in range(len(a))])
+    return (d.max() / scale, np.max(d / np.maximum(a, 1e-3 * scale)),
+            np.max(d / np.maximum(a, 1e-6 * env)))
+
+
+def test_all_bessel_integrals_2e14_mixed(gpu_ctx, oracle, w):
+    """Config 2 in mixed precision (double-float transforms on the FP32 pipes,
+    FP64 Gamma-ratio coefficients, tables stored as float): every one of the 30
+    (n, l) tables at 2^14 points against the FP64 oracle on r in [1, 1e4] Mpc/h:
+    at most 2e-6 of the table's scale, and 1e-4 relative with a floor of 1e-3 of
+    the scale."""
+    c = w.cfg2()
+    k, pk, N = c["k"], c["pk"], c["N"]
+    gpu_ctx.integrals_init(k, pk[None, :], c["terms"], N=N, precision="mixed", small_r=False)
+    worst = np.zeros(3)
+    for n, l in c["terms"]:
+        gx, gy = gpu_ctx.integral_table(0, n, l)
+        ox, oy = oracle.integral_table(k, pk, n, l, N, with_small_r=False)
+        mask = (ox >= 1.0 / H) & (ox <= 1e4 / H)
+        mask[:43] = False
+        e = _cfg2_errors(gy[mask], oy[mask])
+        worst = np.maximum(worst, e)
+        print((n, l), "abs/scale %.3g  rel (floor 1e-3 scale) %.3g  rel (floor 1e-6 local) %.3g"
+              % e)
+        assert e[0] < 2e-6, ((n, l), e)
+        assert e[1] < 1e-4, ((n, l), e)
+    print("worst mixed table errors (2^14, 30 terms): abs/scale %.3g, rel %.3g, local %.3g"
+          % tuple(worst))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cfg2_resampled_on_log_r(gpu_ctx, oracle, w, precision):
+    """Config 2's output grid: every table resampled by its Akima spline
+    (coffe_gpu_integral_eval, the lookup of coffe_interp_spline) at 2^14
+    log-spaced r in [1, 1e4] Mpc/h, against the same spline of the oracle's table.
+    FP64: 1e-10 of the table's scale and 1e-10 relative with a floor of 1e-3 of
+    the scale; mixed: 2e-6 of the scale and 1e-4 relative (same floor)."""
+    c = w.cfg2()
+    k, pk, N, r = c["k"], c["pk"], c["N"], c["r_out"]
+    gpu_ctx.integrals_init(k, pk[None, :], c["terms"], N=N, precision=precision, small_r=False)
+    tol_scale, tol_rel = (1e-10, 1e-10) if precision == "fp64" else (2e-6, 1e-4)
+    for n, l in c["terms"]:
+        got = gpu_ctx.integral_eval(0, n, l, r)
+        ox, oy = oracle.integral_table(k, pk, n, l, N, with_small_r=False)
+        ref = oracle.spline_eval("akima", ox[43:], oy[43:], r)
+        e = _cfg2_errors(got, ref)
+        print(precision, (n, l), "abs/scale %.3g  rel (floor 1e-3 scale) %.3g  local %.3g" % e)
+        assert e[0] < tol_scale, ((n, l), e)
+        assert e[1] < tol_rel, ((n, l), e)
+
+
 def test_integrals_golden_through_gpu(gpu_ctx, golden, class_pk):
     k, pk = class_pk
     gpu_ctx.integrals_init(k, pk[None, :], TERMS8, N=16384, precision="fp64", small_r=True)
