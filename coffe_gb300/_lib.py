@@ -31,6 +31,9 @@ SMALL_R = 1
 PK_DEVICE = 2
 ASYNC = 4
 NOALLOC_MAX_OUTPUTS = 1048576
+PEAK_FP64 = 0
+PEAK_FP32 = 1
+PEAK_FP32X2 = 2
 
 # every symbol include/coffe_gpu.h declares
 EXPORTS = (
@@ -69,6 +72,7 @@ EXPORTS = (
     "coffe_gpu_divergent_separations",
     "coffe_gpu_divergent_integral",
     "coffe_gpu_renormalization_grid",
+    "coffe_gpu_measure_peak",
 )
 
 
@@ -183,5 +187,6 @@ def load(build_if_missing: bool = True):
                                                _dp, C.c_size_t, _dp, _dp]
     L.coffe_gpu_renormalization_grid.argtypes = [_p, _dp, _dp, C.c_size_t, C.c_double,
                                                  C.c_double, _dp, C.c_size_t, _dp, C.c_size_t, _dp]
+    L.coffe_gpu_measure_peak.argtypes = [_p, C.c_int, _dp]
     _lib = L
     return L

@@ -99,6 +99,15 @@ class Context:
     def launch_count(self) -> int:
         return int(self._L.coffe_gpu_launch_count(self._ctx))
 
+    def measure_peak(self, kind: str) -> float:
+        """Measured FLOP/s of this device for ``kind`` in "fp64", "fp32" or
+        "fp32x2" (packed pair FMA): the roofline denominators of the
+        compute-bound kernels."""
+        k = {"fp64": _lib.PEAK_FP64, "fp32": _lib.PEAK_FP32, "fp32x2": _lib.PEAK_FP32X2}[kind]
+        v = C.c_double()
+        self._check(self._L.coffe_gpu_measure_peak(self._ctx, k, C.byref(v)), "measure_peak")
+        return float(v.value)
+
     # ------------------------------------------------------------- tuning
     def set_autotune(self, enable: bool = True):
         """Benchmark mode: the first table build and mixed multipole call of
@@ -384,8 +393,8 @@ class Context:
         ``NOALLOC_MAX_OUTPUTS`` = n_sep * len(ls) outputs per call).  For callers
         whose device memory is all pooled up front, or who cannot have
         cudaMalloc/cudaFree stall the device mid-run.  Calls on one device share
-        that array: serialise them (one stream).  Make the first call on a device
-        before any stream capture; it resolves the array's address."""
+        that array: serialise them (one stream).  The context's creation loads
+        the array and the kernels, so the call itself allocates nothing."""
         P = lambda t, ty: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ty))
         la = np.ascontiguousarray(ls, dtype=np.int32)
         self._check(self._L.coffe_gpu_multipoles_noalloc(

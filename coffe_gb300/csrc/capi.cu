@@ -170,6 +170,10 @@ int coffe_gpu_ctx_create(int device, coffe_gpu_ctx_t **out)
         coffe_gpu_ctx_destroy(ctx);
         return COFFE_GPU_ECUDA;
     }
+    if (multipoles_noalloc_prepare(ctx) != COFFE_GPU_OK) {
+        coffe_gpu_ctx_destroy(ctx);
+        return COFFE_GPU_ECUDA;
+    }
     *out = ctx;
     return COFFE_GPU_OK;
 }
@@ -193,7 +197,7 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
                       &ctx->lens_rule, &ctx->lens_rec, &ctx->lens_part,
                       &ctx->cov_buf,  &ctx->cov_out, &ctx->adj_buf, &ctx->csband,
                       &ctx->samp_tdf, &ctx->qfac_df, &ctx->pk_df, &ctx->mp_bgfit,
-                      &ctx->cf_rule, &ctx->avg_buf, &ctx->div_buf};
+                      &ctx->cf_rule, &ctx->avg_buf, &ctx->div_buf, &ctx->peak_buf};
     spline_free(ctx->cov_pk);
     for (DevBuf *b : bufs) cg_release(*b);
     for (auto &slot : ctx->mp_node_slots) cg_release(slot.buf);

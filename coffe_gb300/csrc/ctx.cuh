@@ -135,6 +135,7 @@ struct coffe_gpu_ctx {
     // ---- multipole adjoint (adjoint.cu)
     DevBuf adj_buf; // table, spectrum and resampling cotangents
     DevBuf div_buf; // k, P(k), separations and results of the divergent integral
+    DevBuf peak_buf; // per-thread outputs of the peak-rate kernels (peaks.cu)
 };
 
 void cg_set_error(coffe_gpu_ctx *ctx, const char *fmt, ...);
@@ -164,6 +165,8 @@ int divergent_run(coffe_gpu_ctx *ctx, const double *k, const double *pk, size_t 
 int integrals_eval(coffe_gpu_ctx *ctx, int spectrum, int term, const double *r, size_t nq,
                    double *out);
 int multipoles_prepare_background(coffe_gpu_ctx *ctx);
+// loads the module and kernels of coffe_gpu_multipoles_noalloc (ctx creation)
+int multipoles_noalloc_prepare(coffe_gpu_ctx *ctx);
 
 // Configuration for one launch shape: the chosen one if the shape was tuned,
 // else (benchmark mode, stream not capturing) the fastest of `cands` timed

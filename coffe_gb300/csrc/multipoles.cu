@@ -1573,38 +1573,26 @@ namespace {
 #define MP_NOALLOC_LIST_OFFSET (256 + MP_NOALLOC_NODE_BYTES)
 #define MP_NOALLOC_BYTES \
     (MP_NOALLOC_LIST_OFFSET + sizeof(int2) * (size_t)COFFE_GPU_NOALLOC_MAX_OUTPUTS)
-#define MP_NOALLOC_MAX_DEVICES 64
 static_assert(sizeof(double) * NodeLayout<MP_MAX_L>::COUNT <= MP_NOALLOC_NODE_BYTES,
               "node table of the largest multipole list must fit the scratch slot");
 static_assert(MP_NOALLOC_LIST_OFFSET % 256 == 0, "retry list alignment");
 
 static __device__ __align__(256) unsigned char noalloc_scratch[MP_NOALLOC_BYTES];
 
-// device address of noalloc_scratch per device, resolved once per device
-std::mutex noalloc_mutex;
-unsigned char *noalloc_addr[MP_NOALLOC_MAX_DEVICES];
-
-// Looks up (first call on the device) or returns the scratch address for
-// ctx->device, which the caller has made current.
+// Device address of noalloc_scratch in the current context.  Looked up on
+// every call rather than cached, so a call after cudaDeviceReset or under
+// another context never reuses a stale address; once the module is loaded
+// (noalloc_prepare) the lookup allocates nothing.
 int noalloc_scratch_address(coffe_gpu_ctx *ctx, unsigned char **addr)
 {
-    if (ctx->device < 0 || ctx->device >= MP_NOALLOC_MAX_DEVICES) {
-        cg_set_error(ctx, "multipoles_noalloc: device %d beyond the %d supported", ctx->device,
-                     MP_NOALLOC_MAX_DEVICES);
-        return COFFE_GPU_EINVAL;
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        cg_set_error(ctx, "multipoles_noalloc: cannot resolve the scratch array on device %d: %s",
+                     ctx->device, cudaGetErrorString(e));
+        return COFFE_GPU_ECUDA;
     }
-    std::lock_guard<std::mutex> lock(noalloc_mutex);
-    if (!noalloc_addr[ctx->device]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            cg_set_error(ctx, "multipoles_noalloc: cannot resolve the scratch array on device %d: %s",
-                         ctx->device, cudaGetErrorString(e));
-            return COFFE_GPU_ECUDA;
-        }
-        noalloc_addr[ctx->device] = (unsigned char *)p;
-    }
-    *addr = noalloc_addr[ctx->device];
+    *addr = (unsigned char *)p;
     return COFFE_GPU_OK;
 }
 
@@ -1751,7 +1739,38 @@ int launch_noalloc(coffe_gpu_ctx *ctx, const MpArgs &a, const S &chi_of_z, const
     return cg_after_launch(ctx, "mp_retry_kernel");
 }
 
+// Loads every kernel launch_noalloc<T, S, TT> launches (lazy loading would
+// otherwise load them, allocating their code, at the first call).
+template <typename T, typename S, typename TT> int noalloc_load_kernels(coffe_gpu_ctx *ctx)
+{
+    cudaFuncAttributes fa;
+    CG_CUDA(ctx, cudaFuncGetAttributes(&fa, mp_node_table_kernel<T>));
+    CG_CUDA(ctx, cudaFuncGetAttributes(&fa, mp_lane_kernel<1, T, S, TT>));
+    CG_CUDA(ctx, cudaFuncGetAttributes(&fa, mp_lane_kernel<2, T, S, TT>));
+    CG_CUDA(ctx, cudaFuncGetAttributes(&fa, mp_lane_kernel<3, T, S, TT>));
+    CG_CUDA(ctx, cudaFuncGetAttributes(&fa, mp_lane_kernel<4, T, S, TT>));
+    CG_CUDA(ctx, cudaFuncGetAttributes(&fa, mp_lane_kernel<5, T, S, TT>));
+    CG_CUDA(ctx, cudaFuncGetAttributes(&fa, mp_lane_kernel<6, T, S, TT>));
+    CG_CUDA(ctx, cudaFuncGetAttributes(&fa, mp_lane_kernel<7, T, S, TT>));
+    CG_CUDA(ctx, cudaFuncGetAttributes(&fa, mp_lane_kernel<8, T, S, TT>));
+    CG_CUDA(ctx, cudaFuncGetAttributes(&fa, mp_retry_kernel<T, S, TT>));
+    return COFFE_GPU_OK;
+}
+
 } // namespace
+
+// Called by coffe_gpu_ctx_create with ctx->device current: loads this file's
+// module (which places noalloc_scratch in device memory) and the kernels of
+// coffe_gpu_multipoles_noalloc, so that the entry point itself never triggers
+// an allocation.
+int multipoles_noalloc_prepare(coffe_gpu_ctx *ctx)
+{
+    unsigned char *p = nullptr;
+    int st = noalloc_scratch_address(ctx, &p);
+    if (st) return st;
+    if ((st = noalloc_load_kernels<float, Spl32, float>(ctx))) return st;
+    return noalloc_load_kernels<double, Spl64, double>(ctx);
+}
 
 extern "C" int coffe_gpu_multipoles_noalloc(coffe_gpu_ctx_t *ctx, int contrib, int precision,
                                             double epsrel, int n_req, int64_t n_sep,

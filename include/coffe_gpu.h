@@ -257,9 +257,11 @@ int coffe_gpu_multipoles_async(coffe_gpu_ctx_t *ctx, int contrib, int precision,
    - Limit: n_sep * n_l <= COFFE_GPU_NOALLOC_MAX_OUTPUTS per call; larger calls
      return COFFE_GPU_EINVAL with the reason in coffe_gpu_last_error (split the
      requests into several calls).
-   - Set-up: the first call on each device looks up the array's device address
-     (with that device current) and may trigger the driver's lazy loading of the
-     library's kernels; make that first call before any stream capture.
+   - Set-up: coffe_gpu_ctx_create loads, on its device, the module that holds
+     the array (which places the array in device memory) and every kernel this
+     entry point launches, so once a context exists a call allocates nothing;
+     each call looks the array's address up again (cudaGetSymbolAddress, with
+     the context's device current), so no address outlives its context.
    - Concurrency: every call on one device uses the same array, so two calls on
      the same device whose work can overlap (different streams, contexts or host
      threads) race and corrupt each other's results; serialise them, e.g. on one
@@ -462,6 +464,17 @@ int coffe_gpu_average_covariance_multipoles(coffe_gpu_ctx_t *ctx, int contrib,
                                             const double *density1, const double *density2,
                                             const double *pixelsize, int n_l, const int *l,
                                             int n_sep, const double *sep, double *out);
+
+/* No counterpart in the reference: the measured arithmetic rate of this
+   context's device, the denominator of the compute-bound kernels' roofline
+   fractions.  kind: COFFE_GPU_PEAK_FP64 (fma.rn.f64), COFFE_GPU_PEAK_FP32
+   (fma.rn.f32) or COFFE_GPU_PEAK_FP32X2 (fma.rn.f32x2, two FP32 lanes per
+   instruction).  Independent FMA chains on every SM, best of three ~10 ms
+   launches timed with CUDA events; *flops_per_s counts an FMA as 2 FLOP. */
+#define COFFE_GPU_PEAK_FP64 0
+#define COFFE_GPU_PEAK_FP32 1
+#define COFFE_GPU_PEAK_FP32X2 2
+int coffe_gpu_measure_peak(coffe_gpu_ctx_t *ctx, int kind, double *flops_per_s);
 
 /* Kernel launches issued by this context since creation (for accounting). */
 long long coffe_gpu_launch_count(const coffe_gpu_ctx_t *ctx);

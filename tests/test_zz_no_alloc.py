@@ -105,3 +105,58 @@ def test_noalloc_rejects_calls_beyond_its_scratch(setup):
                                arrays["req_offset"], arrays["sep"], n_sep, (0, 2, 4), out)
     assert ei.value.status == -1
     assert "scratch limit" in str(ei.value)
+
+
+def test_noalloc_retry_path_and_odd_multipoles(setup):
+    """Odd multipoles and unequal tracer biases (no mirror rule on either entry
+    point) at a tolerance tight enough that first panels fail: the retry counter
+    and list in the fixed scratch carry real work, and the results still match."""
+    torch, ctx, b, arrays = setup
+    z = np.linspace(0.0, 5.0, 11)
+    ctx.set_bias(0, z, 1.0 + 0.4 * z)
+    ctx.set_bias(1, z, 1.3 + 0.1 * z)
+    try:
+        ctx.integrals_init(b.k, b.pk, [(0, 0), (0, 2), (0, 4)], N=4096, precision="fp64",
+                           small_r=False)
+        ls = (1, 2, 3)
+        for call in range(2):
+            got = _run_eps(torch, ctx, b, arrays, ls, 1e-10, noalloc=True)
+            ref = _run_eps(torch, ctx, b, arrays, ls, 1e-10, noalloc=False)
+            assert ctx.last_retries() > 0  # the tolerance sends pairs to the retry list
+            assert np.isfinite(got).all(), call
+            assert _rel_err(got, ref, b.req_offset) < 1e-10, call
+    finally:
+        one = np.ones(11)
+        ctx.set_bias(0, z, one)
+        ctx.set_bias(1, z, one)
+
+
+def _run_eps(torch, ctx, b, arrays, ls, epsrel, noalloc):
+    out = torch.full((len(b.sep), len(ls)), float("nan"), dtype=torch.float64, device="cuda:0")
+    call = ctx.multipoles_noalloc if noalloc else ctx.multipoles_async
+    torch.cuda.synchronize()
+    call(arrays["req_spectrum"], arrays["req_z_mean"], arrays["req_offset"], arrays["sep"],
+         len(b.sep), ls, out, precision="fp64", epsrel=epsrel)
+    ctx.synchronize()
+    return out.cpu().numpy()
+
+
+def test_noalloc_call_leaves_device_memory_unchanged(setup):
+    """The contract itself: with the inputs and the output already on the device,
+    a call on a multipole list and size this context has not seen before changes
+    the device's free memory by nothing."""
+    torch, ctx, b, arrays = setup
+    ctx.integrals_init(b.k, b.pk, [(0, 0), (0, 2), (0, 4)], N=4096, precision="mixed",
+                       small_r=False)
+    n = int(b.req_offset[2])  # the first two requests only: a new size
+    ls = (4, 2, 0, 6)
+    out = torch.full((n, len(ls)), float("nan"), dtype=torch.float64, device="cuda:0")
+    offs = arrays["req_offset"][:3].clone()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    ctx.multipoles_noalloc(arrays["req_spectrum"][:2], arrays["req_z_mean"][:2], offs,
+                           arrays["sep"], n, ls, out, precision="mixed")
+    ctx.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    assert torch.isfinite(out).all()
