@@ -30,6 +30,7 @@ ONLY_CROSS = 8
 SMALL_R = 1
 PK_DEVICE = 2
 ASYNC = 4
+TABLES_DF = 8
 NOALLOC_MAX_OUTPUTS = 1048576
 PEAK_FP64 = 0
 PEAK_FP32 = 1

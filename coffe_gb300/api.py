@@ -173,8 +173,10 @@ class Context:
 
     # ------------------------------------------------------------- integrals
     def integrals_init(self, k, pk, terms: Sequence[Tuple[int, int]] = DEFAULT_TERMS,
-                       N: int = 4096, precision="fp64", small_r: bool = True):
-        """FFTLog tables of I_l^n for each spectrum row of ``pk`` (shape (S, nk))."""
+                       N: int = 4096, precision="fp64", small_r: bool = True,
+                       tables_df: bool = False):
+        """FFTLog tables of I_l^n for each spectrum row of ``pk`` (shape (S, nk)).
+        ``tables_df`` (mixed precision): double-float inverse transforms too."""
         k = _f64(k)
         pk = _f64(np.atleast_2d(pk))
         if pk.shape[1] != len(k):
@@ -184,7 +186,7 @@ class Context:
         l = np.ascontiguousarray([t[1] for t in terms], dtype=np.int32)
         half = np.ascontiguousarray([t[2] if len(t) > 2 else 0 for t in terms], dtype=np.int32)
         prec = _precision(precision)
-        flags = _lib.SMALL_R if small_r else 0
+        flags = (_lib.SMALL_R if small_r else 0) | (_lib.TABLES_DF if tables_df else 0)
         self._check(self._L.coffe_gpu_integrals_init_ex(self._ctx, _dptr(k), _dptr(pk),
                                                         pk.shape[0], len(k), _iptr(n), _iptr(l),
                                                         _iptr(half), len(terms), int(N), prec,
@@ -323,7 +325,8 @@ class Context:
         return out[: len(sp)]
 
     def integrals_init_device(self, k, pk_dev, terms=DEN_RSD_TERMS, N: int = 4096,
-                              precision="fp64", small_r: bool = False, sync: bool = True):
+                              precision="fp64", small_r: bool = False, sync: bool = True,
+                              tables_df: bool = False):
         """Like :meth:`integrals_init` with P(k) already on the device (a CUDA
         float64 tensor of shape (S, nk)); ``sync=False`` only enqueues."""
         k = _f64(k)
@@ -332,7 +335,8 @@ class Context:
             raise ValueError("pk must have shape (n_spectra, len(k))")
         n = np.ascontiguousarray([t[0] for t in terms], dtype=np.int32)
         l = np.ascontiguousarray([t[1] for t in terms], dtype=np.int32)
-        flags = _lib.PK_DEVICE | (_lib.SMALL_R if small_r else 0) | (0 if sync else _lib.ASYNC)
+        flags = (_lib.PK_DEVICE | (_lib.SMALL_R if small_r else 0) | (0 if sync else _lib.ASYNC)
+                 | (_lib.TABLES_DF if tables_df else 0))
         pk_ptr = C.cast(C.c_void_p(pk_dev.data_ptr()), C.POINTER(C.c_double))
         self._check(self._L.coffe_gpu_integrals_init(self._ctx, _dptr(k), pk_ptr, S, nk, _iptr(n),
                                                      _iptr(l), len(terms), int(N),

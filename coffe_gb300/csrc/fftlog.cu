@@ -206,23 +206,35 @@ __global__ void twiddle_kernel(int N, double2 *__restrict__ tw, float4 *__restri
     twdf[j] = dfc_pack(dfc_from_double2(make_double2(c, -s)));
 }
 
-// double-float copies of the per-term tables used by the mixed path
+// Mixed-path copies of the per-grid tables: the mode taper in double-float
+// (forward transform); the Gamma-ratio kernel M_{q,l}(t_m), the output
+// prefactors and the twiddles rounded to float for the FP32 inverse transforms
+// (each rounded once from its FP64 value), and the kernel and prefactors in
+// double-float for the double-float inverse transforms (COFFE_GPU_TABLES_DF)
 __global__ void term_tables_df_kernel(int M, int N, int n_terms, const double2 *__restrict__ mcoef,
                                       const double *__restrict__ postf,
-                                      const double *__restrict__ modew, float4 *__restrict__ mdf,
-                                      float2 *__restrict__ pdf, float2 *__restrict__ wdf)
+                                      const double *__restrict__ modew,
+                                      const double2 *__restrict__ tw, float2 *__restrict__ wdf,
+                                      float2 *__restrict__ m32, float *__restrict__ p32,
+                                      float2 *__restrict__ tw32, float4 *__restrict__ mdf,
+                                      float2 *__restrict__ pdf)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int t = blockIdx.y;
     if (i <= M) {
-        mdf[(size_t)t * (M + 1) + i] = dfc_pack(dfc_from_double2(mcoef[(size_t)t * (M + 1) + i]));
+        const double2 m = mcoef[(size_t)t * (M + 1) + i];
+        m32[(size_t)t * (M + 1) + i] = make_float2((float)m.x, (float)m.y);
+        mdf[(size_t)t * (M + 1) + i] = dfc_pack(dfc_from_double2(m));
         if (t == 0) {
             const dfl v = df_from_double(modew[i]);
             wdf[i] = make_float2(v.hi, v.lo);
+            tw32[i] = make_float2((float)tw[i].x, (float)tw[i].y);
         }
     }
     if (i < N) {
-        const dfl v = df_from_double(postf[(size_t)t * N + i]);
+        const double pf = postf[(size_t)t * N + i];
+        p32[(size_t)t * N + i] = (float)pf;
+        const dfl v = df_from_double(pf);
         pdf[(size_t)t * N + i] = make_float2(v.hi, v.lo);
     }
 }
@@ -657,7 +669,15 @@ __device__ __forceinline__ dfl sample_input_df(const float2 *__restrict__ y,
     return df_mul(df_add(secant, dfl{corr, 0.f}), dfl{q.x, q.y});
 }
 
-template <int RADIX, bool SWZ>
+__device__ __forceinline__ void store_spec(float4 *p, dfc v) { *p = dfc_pack(v); }
+__device__ __forceinline__ void store_spec(float2 *p, dfc v)
+{
+    *p = make_float2(v.re.hi + v.re.lo, v.im.hi + v.im.lo);
+}
+
+// OUT = float4: the double-float half spectrum (double-float inverse
+// transforms); OUT = float2: rounded to float (FP32 inverse transforms)
+template <int RADIX, bool SWZ, typename OUT>
 __global__ void fftlog_forward_df_kernel(GridPar g, const float2 *__restrict__ pkdf,
                                          const float *__restrict__ cc32,
                                          const int *__restrict__ idx,
@@ -666,7 +686,7 @@ __global__ void fftlog_forward_df_kernel(GridPar g, const float2 *__restrict__ p
                                          const float2 *__restrict__ qfac_df,
                                          const float2 *__restrict__ modew_df,
                                          const float4 *__restrict__ twdf, int n_q,
-                                         float4 *__restrict__ spec, int *err)
+                                         OUT *__restrict__ spec, int *err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float4 *buf = reinterpret_cast<float4 *>(smem_raw);
@@ -687,7 +707,7 @@ __global__ void fftlog_forward_df_kernel(GridPar g, const float2 *__restrict__ p
     if (bad) cg_flag(err, CG_ERR_NONFINITE);
     __syncthreads();
     smem_fft_df<RADIX, SWZ>(buf, logM, twdf, -1);
-    float4 *out = spec + ((size_t)s * n_q + qi) * (M + 1);
+    OUT *out = spec + ((size_t)s * n_q + qi) * (M + 1);
     for (int k = threadIdx.x; k <= M; k += blockDim.x) {
         const dfc zk = dfc_load(buf[fft_slot<SWZ>(k & (M - 1), sh)]);
         const dfc zm = dfc_conj(dfc_load(buf[fft_slot<SWZ>((M - k) & (M - 1), sh)]));
@@ -697,10 +717,14 @@ __global__ void fftlog_forward_df_kernel(GridPar g, const float2 *__restrict__ p
         const dfc yk = dfc_add(e, dfc_mul(dfc_load(twdf[k]), o)); // 2 Y_k
         const float2 mw = modew_df[k];
         const dfl m = df_scale(dfl{mw.x, mw.y}, 0.5f);
-        out[k] = dfc_pack(dfc{df_mul(yk.re, m), df_neg(df_mul(yk.im, m))}); // conjugate
+        // conjugate; the double-float transform keeps the high modes' rounding
+        // noise (which the growing Gamma-ratio kernel amplifies) at FP64 level
+        store_spec(out + k, dfc{df_mul(yk.re, m), df_neg(df_mul(yk.im, m))});
     }
 }
 
+// ---- mixed path, double-float inverse transforms (COFFE_GPU_TABLES_DF):
+// tables to ~1e-7 of their scale instead of the FP32 transforms' ~1e-6
 // the half-length complex input of a real inverse transform:
 // Fe + i Fo, Fe = X_k + conj(X_{M-k}), Fo = (X_k - conj(X_{M-k})) conj(w_k)
 __device__ __forceinline__ dfc c2r_pre(dfc xa, dfc xb, float4 w)
@@ -755,6 +779,141 @@ __global__ void fftlog_inverse_df_kernel(GridPar g, const float4 *__restrict__ s
         const float2 p = pf[i];
         const dfl r = df_mul(u, dfl{p.x, p.y});
         const float v = r.hi + r.lo;
+        if (!isfinite(v)) bad = true;
+        o[i] = v;
+    }
+    if (bad) cg_flag(err, CG_ERR_NONFINITE);
+}
+
+// ---- mixed path, inverse transforms in FP32 (the default)
+//
+// The c2r transform of (forward spectrum x Gamma-ratio kernel) needs no more
+// than float precision: its rounding error stays ~1e-7 of the outputs' scale
+// (unlike the forward transform's, which the kernel's growth at high modes
+// amplifies), so it runs in plain FP32 on float twiddles, kernel and
+// prefactors rounded from their FP64 values.
+
+__device__ __forceinline__ float2 c32_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 c32_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 c32_mul(float2 a, float2 b)
+{
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 c32_conj(float2 a) { return make_float2(a.x, -a.y); }
+
+// Shared-memory layout of the FP32 transforms (8-byte elements, 16 per
+// 128-byte bank row): element i at i ^ f(i >> 4), f(x) = (x ^ 8x ^ (x >> 4))
+// mod 16, a permutation within each row that makes the bit-reversed scatter
+// and the butterfly strides conflict-free (two-way in one stage at most).
+template <bool SWZ> __device__ __forceinline__ int slot32(int i)
+{
+    if (!SWZ) return i;
+    const int x = i >> 4;
+    return i ^ ((x ^ (x << 3) ^ (x >> 4)) & 15);
+}
+
+// In-place DIT FFT of M = 2^logM complex floats (bit-reversed input): radix-4
+// butterflies, after one radix-2 stage when logM is odd; tw[j] = exp(-2 pi i
+// j / (2M)), j <= M; sign +1 (backward) conjugates the twiddles.
+template <bool SWZ>
+__device__ void smem_fft_f32(float2 *buf, int logM, const float2 *__restrict__ tw, int sign)
+{
+    const int M = 1 << logM;
+    int st = 1;
+    if (logM & 1) {
+        for (int b = threadIdx.x; b < M / 2; b += blockDim.x) {
+            const int p0 = slot32<SWZ>(2 * b), p1 = slot32<SWZ>(2 * b + 1);
+            const float2 u = buf[p0], v = buf[p1];
+            buf[p0] = c32_add(u, v);
+            buf[p1] = c32_sub(u, v);
+        }
+        __syncthreads();
+        st = 2;
+    }
+    for (; st < logM; st += 2) {
+        const int half = 1 << (st - 1);
+        const int step = M >> st;
+        for (int b = threadIdx.x; b < M / 4; b += blockDim.x) {
+            const int pos = b & (half - 1);
+            const int i0 = ((b >> (st - 1)) << (st + 1)) + pos;
+            const int p0 = slot32<SWZ>(i0), p1 = slot32<SWZ>(i0 + half);
+            const int p2 = slot32<SWZ>(i0 + 2 * half), p3 = slot32<SWZ>(i0 + 3 * half);
+            const float2 x0 = buf[p0];
+            float2 x1 = buf[p1], x2 = buf[p2], x3 = buf[p3];
+            if (half > 1) {
+                const int j = pos * step, j3 = 3 * j;
+                float2 w1 = tw[2 * j], w2 = tw[j];
+                float2 w3 = j3 <= M ? tw[j3] : make_float2(-tw[j3 - M].x, -tw[j3 - M].y);
+                if (sign > 0) {
+                    w1 = c32_conj(w1);
+                    w2 = c32_conj(w2);
+                    w3 = c32_conj(w3);
+                }
+                x1 = c32_mul(x1, w1);
+                x2 = c32_mul(x2, w2);
+                x3 = c32_mul(x3, w3);
+            }
+            const float2 t0 = c32_add(x0, x1), t1 = c32_sub(x0, x1);
+            const float2 t2 = c32_add(x2, x3), t3 = c32_sub(x2, x3);
+            // w_{4 half}^half = -i forward, +i backward
+            const float2 r = sign < 0 ? make_float2(t3.y, -t3.x) : make_float2(-t3.y, t3.x);
+            buf[p0] = c32_add(t0, t2);
+            buf[p1] = c32_add(t1, r);
+            buf[p2] = c32_sub(t0, t2);
+            buf[p3] = c32_sub(t1, r);
+        }
+        __syncthreads();
+    }
+}
+
+// the half-length complex input of a real inverse transform:
+// Fe + i Fo, Fe = X_k + conj(X_{M-k}), Fo = (X_k - conj(X_{M-k})) conj(w_k)
+__device__ __forceinline__ float2 c2r_pre32(float2 xa, float2 xb, float2 w)
+{
+    const float2 xbc = c32_conj(xb);
+    const float2 fe = c32_add(xa, xbc);
+    const float2 fo = c32_mul(c32_sub(xa, xbc), c32_conj(w));
+    return make_float2(fe.x - fo.y, fe.y + fo.x);
+}
+
+template <bool SWZ>
+__global__ void fftlog_inverse_f32_kernel(GridPar g, const float2 *__restrict__ spec,
+                                          const int *__restrict__ term_q, int n_q, int n_terms,
+                                          const float2 *__restrict__ mcoef32,
+                                          const float *__restrict__ postf32,
+                                          const float2 *__restrict__ tw32,
+                                          float *__restrict__ tab, int *err)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *buf = reinterpret_cast<float2 *>(smem_raw);
+    const int s = blockIdx.x, t = blockIdx.y;
+    const int N = g.N, M = N / 2;
+    const int logM = 31 - __clz(M);
+    const float2 *in = spec + ((size_t)s * n_q + term_q[t]) * (M + 1);
+    const float2 *mc = mcoef32 + (size_t)t * (M + 1);
+    // z_k = Fe_k + i Fo_k from X_k and conj(X_{M-k}), X = spectrum x kernel;
+    // one thread makes z_k and z_{M-k} from the same two products
+    for (int k = threadIdx.x; k <= M / 2; k += blockDim.x) {
+        const int km = M - k;
+        float2 xa = c32_mul(in[k], mc[k]);
+        float2 xb = c32_mul(in[km], mc[km]);
+        if (k == 0) {
+            xa.y = 0.f;
+            xb.y = 0.f;
+        }
+        buf[slot32<SWZ>(__brev((unsigned)k) >> (32 - logM))] = c2r_pre32(xa, xb, tw32[k]);
+        if (k > 0 && k < M / 2)
+            buf[slot32<SWZ>(__brev((unsigned)km) >> (32 - logM))] = c2r_pre32(xb, xa, tw32[km]);
+    }
+    __syncthreads();
+    smem_fft_f32<SWZ>(buf, logM, tw32, +1);
+    const size_t len = (size_t)N + CG_N_SMALL_R + 1;
+    float *o = tab + ((size_t)s * n_terms + t) * len + CG_N_SMALL_R + 1;
+    const float *pf = postf32 + (size_t)t * N;
+    bool bad = false;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const float2 z = buf[slot32<SWZ>(i >> 1)];
+        const float v = ((i & 1) ? z.y : z.x) * pf[i];
         if (!isfinite(v)) bad = true;
         o[i] = v;
     }
@@ -998,6 +1157,26 @@ bool same_grid(const coffe_gpu_ctx *ctx, const double *k, size_t nk, size_t N,
 
 } // namespace
 
+// Byte offsets of the mixed path's per-grid arrays in ctx->term_df, each
+// rounded up to 256 bytes (float4 accesses need 16-byte alignment, and
+// N/2 + 1 entries of 8 bytes are not a multiple of 16)
+struct TermDfLayout {
+    size_t wdf, tw32, m32, mdf, pdf, p32, total;
+};
+static TermDfLayout term_df_layout(int M, int N, int n_terms)
+{
+    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    TermDfLayout l;
+    l.wdf = 0;
+    l.tw32 = up(l.wdf + sizeof(float2) * (M + 1));
+    l.m32 = up(l.tw32 + sizeof(float2) * (M + 1));
+    l.mdf = up(l.m32 + sizeof(float2) * (size_t)(M + 1) * n_terms);
+    l.pdf = up(l.mdf + sizeof(float4) * (size_t)(M + 1) * n_terms);
+    l.p32 = up(l.pdf + sizeof(float2) * (size_t)N * n_terms);
+    l.total = up(l.p32 + sizeof(float) * (size_t)N * n_terms);
+    return l;
+}
+
 int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n_spectra,
                     size_t nk, const int *n, const int *l, const int *half, int n_terms, size_t N,
                     int precision, unsigned flags)
@@ -1038,6 +1217,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         }
     }
     const bool mixed = precision == COFFE_GPU_MIXED;
+    const bool tables_df = mixed && (flags & COFFE_GPU_TABLES_DF) != 0;
     const int M = (int)N / 2;
     const size_t len = N + CG_N_SMALL_R + 1;
     int st;
@@ -1102,9 +1282,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         if ((st = cg_ensure(ctx, ctx->postf, sizeof(double) * N * n_terms))) return st;
         if ((st = cg_ensure(ctx, ctx->twid, sizeof(double2) * (M + 1)))) return st;
         if ((st = cg_ensure(ctx, ctx->twid32, sizeof(float4) * (M + 1)))) return st;
-        if ((st = cg_ensure(ctx, ctx->term_df, (sizeof(float4) + sizeof(float2)) * (M + 1) *
-                                                   (size_t)n_terms +
-                                               sizeof(float2) * (size_t)N * n_terms)))
+        if ((st = cg_ensure(ctx, ctx->term_df, term_df_layout(M, (int)N, n_terms).total)))
             return st;
         if ((st = cg_ensure(ctx, ctx->tab_x, sizeof(double) * len))) return st;
         if ((st = cg_ensure(ctx, ctx->tab_x32, sizeof(float) * len))) return st;
@@ -1135,9 +1313,16 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
 
     double2 *mcoef = (double2 *)ctx->modec.p;
     double *modew = (double *)((char *)ctx->modec.p + sizeof(double2) * (M + 1) * n_terms);
-    float4 *mdf = (float4 *)ctx->term_df.p;
-    float2 *wdf = (float2 *)(mdf + (size_t)(M + 1) * n_terms);
-    float2 *pdf = wdf + (size_t)(M + 1) * n_terms;
+    // mixed path: mode taper (double-float), twiddles, kernel and prefactors
+    // (float, and double-float for COFFE_GPU_TABLES_DF)
+    const TermDfLayout lay = term_df_layout(M, (int)N, n_terms);
+    char *tdb = (char *)ctx->term_df.p;
+    float2 *wdf = (float2 *)(tdb + lay.wdf);
+    float2 *tw32 = (float2 *)(tdb + lay.tw32);
+    float2 *m32 = (float2 *)(tdb + lay.m32);
+    float4 *mdf = (float4 *)(tdb + lay.mdf);
+    float2 *pdf = (float2 *)(tdb + lay.pdf);
+    float *p32 = (float *)(tdb + lay.p32);
     if (!grid_cached) {
         CG_CUDA(ctx, cudaMemcpyAsync(ctx->kgrid.p, k, sizeof(double) * nk, cudaMemcpyHostToDevice,
                                      ctx->stream));
@@ -1177,7 +1362,8 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
             (int)N, (double2 *)ctx->twid.p, (float4 *)ctx->twid32.p);
         if ((st = cg_after_launch(ctx, "twiddle_kernel"))) return st;
         term_tables_df_kernel<<<tg, tb, 0, ctx->stream>>>(
-            M, (int)N, n_terms, mcoef, (const double *)ctx->postf.p, modew, mdf, pdf, wdf);
+            M, (int)N, n_terms, mcoef, (const double *)ctx->postf.p, modew,
+            (const double2 *)ctx->twid.p, wdf, m32, p32, tw32, mdf, pdf);
         if ((st = cg_after_launch(ctx, "term_tables_df_kernel"))) return st;
         if ((st = cg_check_device_errors(ctx, "FFTLog coefficient tables"))) return st;
         ctx->grid_N = N;
@@ -1188,6 +1374,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     // per spectrum: natural-spline coefficients, forward FFTs, inverse FFTs
     if (mixed && (st = cg_ensure(ctx, ctx->pk_df, sizeof(float2) * nk * n_spectra))) return st;
     const size_t smem = sizeof(double2) * M; // == sizeof(float4) * M
+    const size_t smem32 = sizeof(float2) * M;
     const dim3 gf(n_spectra, n_q), gi(n_spectra, n_terms);
     auto stage = [&](const coffe_gpu_tuning_t &tu) -> int {
         int s2;
@@ -1208,20 +1395,41 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
             if ((s2 = cg_after_launch(ctx, "cspline_band_kernel"))) return s2;
 #define DF_LAUNCH(R, W)                                                                           \
     {                                                                                             \
-        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_forward_df_kernel<R, W>,                         \
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
-        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_df_kernel<R, W>,                         \
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
-        fftlog_forward_df_kernel<R, W><<<gf, tu.fft_threads_fwd, smem, ctx->stream>>>(            \
-            g, (const float2 *)ctx->pk_df.p, (const float *)ctx->csc.p,                           \
-            (const int *)ctx->samp_idx.p, (const float2 *)ctx->samp_tdf.p,                        \
-            (const float4 *)ctx->samp_f32.p, (const float2 *)ctx->qfac_df.p, wdf,                 \
-            (const float4 *)ctx->twid32.p, n_q, (float4 *)ctx->spec.p, ctx->d_err);               \
-        if ((s2 = cg_after_launch(ctx, "fftlog_forward_df_kernel"))) return s2;                   \
-        fftlog_inverse_df_kernel<R, W><<<gi, tu.fft_threads, smem, ctx->stream>>>(                \
-            g, (const float4 *)ctx->spec.p, d_meta->tq, n_q, n_terms, mdf, pdf,                   \
-            (const float4 *)ctx->twid32.p, (float *)ctx->tab_y.p, ctx->d_err);                    \
-        if ((s2 = cg_after_launch(ctx, "fftlog_inverse_df_kernel"))) return s2;                   \
+        if (tables_df) {                                                                          \
+            CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_forward_df_kernel<R, W, float4>,             \
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,        \
+                                              (int)smem));                                        \
+            CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_df_kernel<R, W>,                     \
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,        \
+                                              (int)smem));                                        \
+            fftlog_forward_df_kernel<R, W, float4><<<gf, tu.fft_threads_fwd, smem, ctx->stream>>>( \
+                g, (const float2 *)ctx->pk_df.p, (const float *)ctx->csc.p,                       \
+                (const int *)ctx->samp_idx.p, (const float2 *)ctx->samp_tdf.p,                    \
+                (const float4 *)ctx->samp_f32.p, (const float2 *)ctx->qfac_df.p, wdf,             \
+                (const float4 *)ctx->twid32.p, n_q, (float4 *)ctx->spec.p, ctx->d_err);           \
+            if ((s2 = cg_after_launch(ctx, "fftlog_forward_df_kernel"))) return s2;               \
+            fftlog_inverse_df_kernel<R, W><<<gi, tu.fft_threads, smem, ctx->stream>>>(            \
+                g, (const float4 *)ctx->spec.p, d_meta->tq, n_q, n_terms, mdf, pdf,               \
+                (const float4 *)ctx->twid32.p, (float *)ctx->tab_y.p, ctx->d_err);                \
+            if ((s2 = cg_after_launch(ctx, "fftlog_inverse_df_kernel"))) return s2;               \
+        } else {                                                                                  \
+            CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_forward_df_kernel<R, W, float2>,             \
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,        \
+                                              (int)smem));                                        \
+            CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_f32_kernel<W>,                       \
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,        \
+                                              (int)smem32));                                      \
+            fftlog_forward_df_kernel<R, W, float2><<<gf, tu.fft_threads_fwd, smem, ctx->stream>>>( \
+                g, (const float2 *)ctx->pk_df.p, (const float *)ctx->csc.p,                       \
+                (const int *)ctx->samp_idx.p, (const float2 *)ctx->samp_tdf.p,                    \
+                (const float4 *)ctx->samp_f32.p, (const float2 *)ctx->qfac_df.p, wdf,             \
+                (const float4 *)ctx->twid32.p, n_q, (float2 *)ctx->spec.p, ctx->d_err);           \
+            if ((s2 = cg_after_launch(ctx, "fftlog_forward_df_kernel"))) return s2;               \
+            fftlog_inverse_f32_kernel<W><<<gi, tu.fft_threads, smem32, ctx->stream>>>(            \
+                g, (const float2 *)ctx->spec.p, d_meta->tq, n_q, n_terms, m32, p32, tw32,         \
+                (float *)ctx->tab_y.p, ctx->d_err);                                               \
+            if ((s2 = cg_after_launch(ctx, "fftlog_inverse_f32_kernel"))) return s2;              \
+        }                                                                                         \
     }
             const bool swz = tu.fft_swizzle && M >= 64;
             if (tu.fft_radix == 2) {
@@ -1273,7 +1481,8 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
                     cands.push_back(c);
                 }
     coffe_gpu_tuning_t tu;
-    const std::array<long long, 6> key{1, (long long)N, n_spectra, n_terms, n_q, mixed ? 1 : 0};
+    const std::array<long long, 6> key{1, (long long)N, n_spectra, n_terms, n_q,
+                                       mixed ? (tables_df ? 2 : 1) : 0};
     if ((st = cg_tuned(ctx, key, cands, stage, &tu))) return st;
     if ((st = stage(tu))) return st;
     ctx->last_tuning.fft_threads = tu.fft_threads;

@@ -131,8 +131,11 @@ size_t coffe_gpu_integral_table_len(size_t N);
    sub-Mpc points by GK61 QAG (integrals.c:524-562); without it those 43
    entries are NaN and tables serve lookups at r >= the third FFT node
    (1.01 Mpc at the default grids).
-   precision: COFFE_GPU_FP64 or COFFE_GPU_MIXED (FP32 FFT, FP64 Gamma-ratio
-   coefficients).  Tables stay on the device for coffe_gpu_multipoles. */
+   precision: COFFE_GPU_FP64 or COFFE_GPU_MIXED (FP64 Gamma-ratio coefficients;
+   the forward transform in double-float on the FP32 pipes, the inverse
+   transforms in FP32, tables stored as float: ~1e-6 of a table's scale, 1e-4
+   relative above 1e-3 of it).  Tables stay on the device for
+   coffe_gpu_multipoles. */
 #define COFFE_GPU_SMALL_R 1
 /* flags bit 1: `pk` is a device pointer (n_spectra * nk doubles). */
 #define COFFE_GPU_PK_DEVICE 2
@@ -141,6 +144,10 @@ size_t coffe_gpu_integral_table_len(size_t N);
    N) must be those of the previous call so that no per-grid table is rebuilt
    (otherwise the call synchronises once to build them). */
 #define COFFE_GPU_ASYNC 4
+/* flags bit 3, COFFE_GPU_MIXED only: the inverse transforms in double-float as
+   well (tables to ~1e-7 of their scale, the float storage; about twice the
+   time of the table stage). */
+#define COFFE_GPU_TABLES_DF 8
 int coffe_gpu_integrals_init(coffe_gpu_ctx_t *ctx, const double *k, const double *pk,
                              int n_spectra, size_t nk, const int *n, const int *l,
                              int n_terms, size_t N, int precision, unsigned flags);
