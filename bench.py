@@ -51,6 +51,23 @@ FLOP_PER_PAIR_EXTRA = 220
 # benchmark's equal tracers and even multipoles, so the kernel evaluates the 31
 # GK61 nodes with mu >= 0 (the other 30 are their mirror images)
 NODES = 31
+# the FP64 instantiation of the same kernel (COFFE_GPU_FP64_FASTALG) has no
+# Kahan compensation: 3 fewer operations per multipole and node
+FLOP_PER_NODE_FP64_FASTALG = FLOP_PER_NODE - 9
+# the FP64 parity kernel (mp_lane_kernel<3, double>): the reference algebra per
+# node with the background from spline records (z(chi) cursors, f/D1 records)
+FLOP_PER_NODE_LANE = 170
+PRECISIONS = ("mixed", "fp64", "fp64-fastalg")
+# FFTLog table stage, per transform of N = 4096 real points (FMA = 2):
+#   FFT 2.5 N log2 N, kernel multiply 6 (N/2 + 1), prefactor N (inverse);
+#   resampling ~10 N and the real-FFT post-pass ~10 N/2 (forward)
+FFT_FLOP = 2.5 * N_FFT * 12
+INV_FLOP = FFT_FLOP + 6 * (N_FFT // 2 + 1) + N_FFT
+FWD_FLOP = FFT_FLOP + 10 * N_FFT + 5 * N_FFT
+# HBM bytes per transform: the inverse reads the half spectrum (N/2+1 complex
+# float on the mixed path, double on the FP64 path) and writes the table
+# (float / double)
+INV_BYTES = {"mixed": 8 * (N_FFT // 2 + 1) + 4 * N_FFT, "fp64": 16 * (N_FFT // 2 + 1) + 8 * N_FFT}
 # DRAM bytes (read + write) per (request, separation) of the mixed multipole
 # kernel, from an ncu capture of the first 256 spectra of this batch (324,864
 # pairs, 5.90 MB read, 0 B written); traffic grows with the number of pairs
@@ -231,6 +248,50 @@ def rel_err_vs(ref, got, batch):
     return float(np.max(np.abs(got - ref) / np.maximum(np.abs(ref), np.maximum(floor, 1e-300))))
 
 
+def kernel_rooflines(kt, n_spectra, n_terms, n_pairs, peaks):
+    """Roofline entries of the step's kernels from their event-timed average
+    launch (kt[precision][kernel] in ms): achieved = algorithmic work per launch
+    / that time, against the measured peak of the resource that bounds it."""
+    hbm = peaks["hbm_gbs"]
+    rows = []
+
+    def add(prec, name, label, bound, work, unit, peak, note):
+        ms = kt.get(prec, {}).get(name)
+        if not ms:
+            return
+        achieved = work / (ms * 1e-3) / (1e9 if unit == "GB/s" else 1e12)
+        rows.append({"kernel": label, "precision": prec, "launch_ms": ms, "bound": bound,
+                     "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
+                     "work_per_launch": work, "note": note})
+
+    inv = n_spectra * n_terms
+    add("mixed", "mp_fast_kernel", "mp_fast_kernel<3,3,U,float>", "fp32",
+        n_pairs * (NODES * FLOP_PER_NODE + FLOP_PER_PAIR_EXTRA), "TFLOP/s", peaks["fp32"],
+        "FLOP per launch / event time; peak = measured fma.rn.f32 rate")
+    add("mixed", "fftlog_inverse_f32_kernel", "fftlog_inverse_f32_kernel (FP32 c2r)", "hbm",
+        inv * INV_BYTES["mixed"], "GB/s", hbm,
+        "bytes: half spectra in, float tables out; %.0f FLOP per transform, %.1f FLOP/B, "
+        "below the FP32 ridge" % (INV_FLOP, INV_FLOP / INV_BYTES["mixed"]))
+    add("mixed", "fftlog_forward_df_kernel", "fftlog_forward_df_kernel (double-float r2c)", "fp32",
+        n_spectra * FWD_FLOP, "TFLOP/s", peaks["fp32"],
+        "FP64-equivalent FLOP of the transform; each is ~10-20 FP32 operations in "
+        "double-float, so frac counts FP64-class work against the FP32 peak")
+    add("mixed", "cspline_band_kernel", "cspline_band_kernel (spline split + band)", "hbm",
+        n_spectra * 20 * N_FFT, "GB/s", hbm, "bytes: P(k) in (8 B), hi/lo pairs (8 B) and "
+        "float curvature (4 B) out per knot")
+    add("fp64", "mp_lane_kernel", "mp_lane_kernel<3,double> (FP64 parity path)", "fp64",
+        n_pairs * (NODES * FLOP_PER_NODE_LANE + FLOP_PER_PAIR_EXTRA), "TFLOP/s", peaks["fp64"],
+        "~170 FLOP per node (reference algebra, spline records); peak = measured fma.rn.f64")
+    add("fp64-fastalg", "mp_fast_kernel", "mp_fast_kernel<3,3,U,double> (FP64, mixed algorithm)",
+        "fp64", n_pairs * (NODES * FLOP_PER_NODE_FP64_FASTALG + FLOP_PER_PAIR_EXTRA), "TFLOP/s",
+        peaks["fp64"], "the mixed kernel's algorithm in FP64")
+    add("fp64", "fftlog_inverse_kernel", "fftlog_inverse_kernel (FP64 c2r)", "fp64",
+        inv * INV_FLOP, "TFLOP/s", peaks["fp64"], "FLOP per transform x transforms")
+    add("fp64", "fftlog_forward_kernel", "fftlog_forward_kernel (FP64 r2c)", "fp64",
+        n_spectra * FWD_FLOP, "TFLOP/s", peaks["fp64"], "FLOP per transform x transforms")
+    return rows
+
+
 def measure_gemm_peak(torch, dtype, n=8192, reps=5):
     a = torch.randn(n, n, device="cuda", dtype=dtype)
     b = torch.randn(n, n, device="cuda", dtype=dtype)
@@ -341,6 +402,7 @@ def extras(torch, ctx, stream):
         "workload": "d(multipoles)/d(P(k), bias scale, growth scale), den+RSD l=0,2,4, z=1, "
                     "100 separations, 4096 k nodes, FP64 adjoint",
         "ms_per_call": grad_ms}
+    out.update(config_baselines(torch, ctx, ev_time, out))
     # divergent I^4_0 and its 201 x 201 renormalisation grid (integrals.c:773-914)
     # on the config-1 spectrum, chi in [0, chi(1.2)]
     c1 = workloads.cfg1()
@@ -362,6 +424,194 @@ def extras(torch, ctx, stream):
         "finite": bool(np.isfinite(grid).all() and np.isfinite(r1d).all()),
         "note": "host API wall time (host arrays in, values out)"}
     return out
+
+
+def _pool_map(fn, items, nthreads):
+    """fn over items on nthreads host threads (the oracle's ctypes calls release
+    the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    with ThreadPoolExecutor(max_workers=nthreads) as ex:
+        return list(ex.map(fn, items))
+
+
+def _err_scale_floor(got, ref):
+    """(max abs error / max |ref|, relative error with a floor of 1e-3 max |ref|)"""
+    sc = np.abs(ref).max()
+    d = np.abs(got - ref)
+    return float(d.max() / sc), float(np.max(d / np.maximum(np.abs(ref), 1e-3 * sc)))
+
+
+def config_baselines(torch, ctx, ev_time, extras_so_far):
+    """The other configurations of the path, each with its GPU time, its error
+    against the FP64 oracle and the oracle timed on the host cores (OpenMP or a
+    thread pool over independent items, all cores): config 1 through the
+    Coffe mirror (cold and warm), config 2's 30 tables at 2^14, a sample of
+    config 4's separations, config 5's covariance."""
+    import oracle as orc
+    from coffe_gb300 import workloads
+    from coffe_gb300.api import Coffe
+
+    nth = os.cpu_count() or 1
+    dev = torch.device("cuda", torch.cuda.current_device())
+    res = {}
+    # ---- config 1: plain FP64 den+RSD, 100 separations, one z, l = 0, 2, 4
+    c1 = workloads.cfg1()
+    co = c1["cosmo"]
+    kw = dict(omega_m=co.omega_m, omega_baryon=co.omega_baryon, omega_gamma=co.omega_gamma,
+              h=co.h, sep=c1["sep"], l=list(c1["ls"]), z_mean=[c1["z_mean"]], has_density=True,
+              has_rsd=True, integrals_fftlog_sampling=N_FFT, deltaz=[0.1])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    cc = Coffe(**kw)
+    cc.set_power_spectrum_linear(c1["k"], c1["pk"])
+    mp = cc.compute_multipoles_bulk()
+    cold = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    cc.set_power_spectrum_linear(c1["k"], c1["pk"] * 1.0)  # new spectrum: tables rebuilt
+    mp = cc.compute_multipoles_bulk()
+    warm = time.perf_counter() - t0
+    got1 = np.array([m.value for m in mp]).reshape(len(c1["ls"]), len(c1["sep"]))
+    t0 = time.perf_counter()
+    bg = orc.background_nodes(co.omega_m, co.omega_baryon, co.omega_gamma, co.h, 10000)
+    m = orc.Model(bg, co.h, co.omega_m)
+    for n, l in TERMS:
+        m.set_integral(n, l, *orc.integral_table(c1["k"], c1["pk"], n, l, N_FFT,
+                                                 with_small_r=True))
+    ref1 = np.array([m.multipoles_batch(3, np.full(len(c1["sep"]), c1["z_mean"]), c1["sep"],
+                                        np.full(len(c1["sep"]), l), nthreads=nth)
+                     for l in c1["ls"]])
+    cpu1 = time.perf_counter() - t0
+    del cc
+    n1 = ref1.size
+    res["config1"] = {
+        "workload": "den+RSD multipoles l=0,2,4, z=1, 100 separations 10-200 Mpc/h, FP64, one "
+                    "spectrum of 4096 k (Coffe.compute_multipoles_bulk: background, FFTLog tables "
+                    "with the r=0 and sub-Mpc points, multipoles)",
+        "gpu_cold_ms": cold * 1e3, "gpu_warm_ms": warm * 1e3,
+        "gpu_warm_evals_per_s": n1 / warm,
+        "cpu_ms": cpu1 * 1e3, "cpu_evals_per_s": n1 / cpu1, "cpu_cores": nth, "cpu_kind": "port",
+        "max_rel_err_fp64_vs_oracle": _err_scale_floor(got1, ref1)[1],
+        "note": "host API wall time; cold includes the context, the device background and the "
+                "lazy module loads, warm rebuilds the tables for a new spectrum"}
+    # ---- config 2: all 30 I_l^n at 2^14, resampled on 2^14 log-spaced r
+    c2 = workloads.cfg2()
+    k2, terms2, N2, r2 = c2["k"], c2["terms"], c2["N"], c2["r_out"]
+    pk2 = torch.tensor(c2["pk"][None, :], device=dev)
+    t0 = time.perf_counter()
+    refs = _pool_map(lambda t: orc.integral_table(k2, c2["pk"], t[0], t[1], N2,
+                                                  with_small_r=False), terms2, nth)
+    cpu2 = time.perf_counter() - t0
+    mask = (refs[0][0] >= 1.0 / co.h) & (refs[0][0] <= 1e4 / co.h)
+    mask[:43] = False
+    ref_r = [orc.spline_eval("akima", x[43:], y[43:], r2) for x, y in refs]
+    res2 = {}
+    for key, prec, df in (("fp64", "fp64", False), ("mixed", "mixed", False),
+                          ("mixed_tables_df", "mixed", True)):
+        ctx.integrals_init_device(k2, pk2, terms2, N=N2, precision=prec, sync=True, tables_df=df)
+        ms = ev_time(lambda p=prec, d=df: ctx.integrals_init_device(
+            k2, pk2, terms2, N=N2, precision=p, sync=False, tables_df=d), 5)
+        ctx.synchronize()
+        e_tab, e_res = (0.0, 0.0), (0.0, 0.0)
+        t0 = time.perf_counter()
+        vals = [ctx.integral_eval(0, n, l, r2) for n, l in terms2]
+        rs_ms = (time.perf_counter() - t0) * 1e3
+        for i, (n, l) in enumerate(terms2):
+            y = ctx.integral_table(0, n, l)[1]
+            e_tab = tuple(max(a, b) for a, b in
+                          zip(e_tab, _err_scale_floor(y[mask], refs[i][1][mask])))
+            e_res = tuple(max(a, b) for a, b in zip(e_res, _err_scale_floor(vals[i], ref_r[i])))
+        res2[key] = {"tables_ms": ms, "resample_ms": rs_ms,
+                     "table_err_abs_over_scale": e_tab[0], "table_err_rel_floor": e_tab[1],
+                     "resampled_err_abs_over_scale": e_res[0], "resampled_err_rel_floor": e_res[1]}
+    res["config2"] = {
+        "workload": "30 tables I_l^n, l = 0..4, n = -1..4, BAO-modulated BBKS spectrum, FFTLog "
+                    "N = 2^14; resampled by their Akima splines at 2^14 log-spaced r in "
+                    "[1, 1e4] Mpc/h",
+        "gpu": res2, "cpu_ms": cpu2 * 1e3, "cpu_cores": nth, "cpu_kind": "port",
+        "error_convention": "worst over the 30 tables and r in [1, 1e4] Mpc/h against the FP64 "
+                            "oracle: max abs error / the table's max |value|, and the relative "
+                            "error with a floor of 1e-3 of that max",
+        "note": "tables_ms: CUDA events on the library's stream, tables of all 30 terms; "
+                "resample_ms: 30 host API calls (host r in, values out)"}
+    # ---- config 4: a sample of its separations on the host
+    c4 = workloads.cfg4()
+    sample = c4["sep"][::25]  # 8 of the 200 separations
+    bg4 = orc.background_nodes(co.omega_m, co.omega_baryon, co.omega_gamma, co.h, 10000)
+    m4 = orc.Model(bg4, co.h, co.omega_m)
+    for n, l in c4["terms"]:
+        m4.set_integral(n, l, *orc.integral_table(c4["k"], c4["pk"], n, l, N_FFT,
+                                                  with_small_r=True))
+    t0 = time.perf_counter()
+    lens = m4.multipoles_lensing(7, c4["z_mean"], sample, c4["ls"], *c4["rule"], nthreads=nth)
+    nonint = np.array([m4.multipoles_batch(3, np.full(len(sample), c4["z_mean"]), sample,
+                                           np.full(len(sample), l), nthreads=nth)
+                       for l in c4["ls"]]).T
+    cpu4 = time.perf_counter() - t0
+    ref4 = lens + nonint
+    ctx.background_init(co.omega_m, co.omega_baryon, co.omega_gamma, co.h, 10000)
+    err4 = {}
+    for prec in ("fp64", "mixed"):
+        ctx.integrals_init(c4["k"], c4["pk"][None, :], c4["terms"], N=N_FFT, precision=prec,
+                           small_r=True)
+        ctx.set_lensing_rule(*c4["rule"])
+        g4 = ctx.multipoles([0], [c4["z_mean"]], [0, len(sample)], sample, c4["ls"], contrib=7,
+                            precision=prec)
+        fl = 1e-3 * np.abs(ref4).max(axis=0)
+        fl[3] = 1e-3 * np.abs(ref4).max()  # l = 6: a fraction of the whole output
+        err4[prec] = float(np.max(np.abs(g4 - ref4) / np.maximum(np.abs(ref4), fl)))
+    c4x = extras_so_far.get("lensing_cfg4", {})
+    res["config4"] = {
+        "workload": "den+RSD+lensing l=0,2,4,6, z=1.5, 128 mu x 256 x Gauss-Legendre rule; "
+                    "host sample: 8 of the 200 separations",
+        "cpu_ms": cpu4 * 1e3, "cpu_evals_per_s": sample.size * len(c4["ls"]) / cpu4,
+        "cpu_cores": nth, "cpu_kind": "port",
+        "gpu_mixed_evals_per_s": c4x.get("mixed_evals_per_s"),
+        "gpu_fp64_evals_per_s": c4x.get("fp64_evals_per_s"),
+        "max_rel_err_vs_oracle": err4,
+        "error_convention": "relative, floor 1e-3 of each multipole's largest |value| (l = 6: "
+                            "of the output's)"}
+    # ---- config 5: covariance, all five bins, 128 x 128 separations, 2D FFTLog 2^11
+    gbg = ctx.background(with_H=False)
+    c5 = workloads.cfg5(lambda z: np.interp(z, gbg["z"], gbg["chi"]))
+    ls5, sep5, N5 = c5["ls"], c5["sep"], c5["N"]
+    nl, ns = len(ls5), len(sep5)
+    t0 = time.perf_counter()
+    jobs = [(p, i, j) for p in (1, 2) for i in range(nl) for j in range(i, nl)]
+    blocks = _pool_map(lambda jb: orc.covariance_fftlog(c5["k"], c5["pk"], jb[0], ls5[jb[1]],
+                                                        ls5[jb[2]], N5, sep5), jobs, nth)
+    ipk = np.zeros((nl, nl, ns, ns))
+    ipk2 = np.zeros_like(ipk)
+    for (p, i, j), blk in zip(jobs, blocks):
+        f = (2 * ls5[i] + 1) * (2 * ls5[j] + 1) / np.pi ** 2
+        if p == 1:
+            ipk[i, j] = blk * 2 * f
+        else:
+            ipk2[i, j] = blk * f
+    for i in range(nl):
+        for j in range(i):
+            ipk[i, j] = ipk[j, i].T
+            ipk2[i, j] = ipk2[j, i].T
+    bg5 = orc.background_nodes(co.omega_m, co.omega_baryon, co.omega_gamma, co.h, 10000)
+    ref5 = orc.Model(bg5, co.h, co.omega_m).covariance_multipoles(
+        3, c5["z_mean"], c5["deltaz"], c5["fsky"], c5["density"], c5["pixelsize"], ls5, sep5,
+        ipk, ipk2)
+    cpu5 = time.perf_counter() - t0
+    got5 = ctx.covariance_multipoles(c5["k"], c5["pk"], N5, c5["z_mean"], c5["deltaz"],
+                                     c5["fsky"], c5["density"], c5["density"], c5["pixelsize"],
+                                     ls5, sep5)
+    g = np.moveaxis(got5, 3, 2)
+    r = np.moveaxis(ref5, 3, 2)
+    err5 = float(np.max(np.abs(g - r) / np.abs(r).max(axis=(-1, -2), keepdims=True)))
+    res["config5"] = {
+        "workload": "multipole covariance l=0,2,4, 5 z bins, 128 x 128 separations, 2D FFTLog "
+                    "2^11 x 2^11 (12 transforms) + assembly, FP64",
+        "gpu_ms": extras_so_far.get("covariance_cfg5", {}).get("ms_per_call"),
+        "cpu_ms": cpu5 * 1e3, "cpu_cores": nth, "cpu_kind": "port",
+        "max_err_vs_oracle_of_block_max": err5,
+        "error_convention": "max |GPU - oracle| over each (z, l1, l2) block / the block's "
+                            "largest |value|"}
+    return res
 
 
 def ours(args, rank, world, local_rank):
@@ -387,11 +637,13 @@ def ours(args, rank, world, local_rank):
     ro_d = torch.from_numpy(batch.req_offset).to(dev)
     sep_d = torch.from_numpy(batch.sep).to(dev)
     outs = {p: torch.empty((n_sep, len(batch.ls)), dtype=torch.float64, device=dev)
-            for p in ("mixed", "fp64")}
+            for p in PRECISIONS}
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
 
     def step(prec):
-        ctx.integrals_init_device(batch.k, pk_d, TERMS, N=N_FFT, precision=prec, sync=False)
+        # fp64-fastalg: FP64 tables, the mixed path's multipole algorithm in FP64
+        tprec = "mixed" if prec == "mixed" else "fp64"
+        ctx.integrals_init_device(batch.k, pk_d, TERMS, N=N_FFT, precision=tprec, sync=False)
         ctx.multipoles_async(rs_d, rz_d, ro_d, sep_d, n_sep, batch.ls, outs[prec], precision=prec)
 
     def barrier():
@@ -418,7 +670,7 @@ def ours(args, rank, world, local_rank):
     # multipole quadrature and retries), replayed every timed step
     graphs = {}
     if not args.no_graph:
-        for prec in ("mixed", "fp64"):
+        for prec in PRECISIONS:
             try:
                 step(prec)
                 ctx.synchronize()
@@ -493,8 +745,10 @@ def ours(args, rank, world, local_rank):
     k64 = args.fp64_steps or max(3, args.steps // 50)
     for _ in range(2):
         step("fp64")
+        step("fp64-fastalg")
     ctx.synchronize()
     dev_fp64, wall_fp64, _ = timed("fp64", k64)
+    dev_fast64, _, _ = timed("fp64-fastalg", k64)
 
     # accuracy of the mixed path against the FP64 path on the full batch (the
     # FP64 path itself matches the CPU oracle to 1e-10 in the parity tests);
@@ -511,8 +765,23 @@ def ours(args, rank, world, local_rank):
         graph_equal = bool(torch.equal(replayed, outs["mixed"]))
     step("fp64")
     retries["fp64"] = ctx.last_retries()
+    step("fp64-fastalg")
+    retries["fp64-fastalg"] = ctx.last_retries()
     ctx.synchronize()
-    err = rel_err_vs(outs["fp64"].cpu().numpy(), outs["mixed"].cpu().numpy(), batch)
+    ref64 = outs["fp64"].cpu().numpy()
+    err = rel_err_vs(ref64, outs["mixed"].cpu().numpy(), batch)
+    err_fast64 = rel_err_vs(ref64, outs["fp64-fastalg"].cpu().numpy(), batch)
+
+    # per-kernel device times (CUDA events after every launch, direct launches)
+    kt = {}
+    for prec, reps in (("mixed", 10), ("fp64", 2), ("fp64-fastalg", 2)):
+        ctx.set_kernel_timing(True)
+        ctx.kernel_times(reset=True)
+        for _ in range(reps):
+            flush.zero_()
+            step(prec)
+        kt[prec] = {name: ms / n for name, (n, ms) in ctx.kernel_times(reset=True).items()}
+        ctx.set_kernel_timing(False)
 
     # dominant kernel: the mixed multipole kernel alone, CUDA events on our stream
     ctx.integrals_init_device(batch.k, pk_d, TERMS, N=N_FFT, precision="mixed", sync=True)
@@ -553,8 +822,8 @@ def ours(args, rank, world, local_rank):
         ctx.set_stream(stream.cuda_stream)
 
     # reduce over ranks (max time)
-    dev_mixed, dev_fp64, kern_s = reduce_over_ranks(torch, [dev_mixed, dev_fp64, kern_s], world,
-                                                    dev)
+    dev_mixed, dev_fp64, dev_fast64, kern_s = reduce_over_ranks(
+        torch, [dev_mixed, dev_fp64, dev_fast64, kern_s], world, dev)
     if e2e is not None and world > 1:
         (ms,) = reduce_over_ranks(torch, [e2e["ms_per_step"]], world, dev)
         e2e["ms_per_step"] = ms
@@ -565,7 +834,11 @@ def ours(args, rank, world, local_rank):
 
     value = job_throughput(n_evals, args.steps, world, dev_mixed)
     fp64_value = job_throughput(n_evals, k64, world, dev_fp64)
+    fast64_value = job_throughput(n_evals, k64, world, dev_fast64)
     sgemm = measure_gemm_peak(torch, torch.float32)
+    peak32 = ctx.measure_peak("fp32") / 1e12
+    peak64 = ctx.measure_peak("fp64") / 1e12
+    peak32x2 = ctx.measure_peak("fp32x2") / 1e12
     achieved = flop_launch / kern_s / 1e12
     peaks = {}
     try:
@@ -601,22 +874,43 @@ def ours(args, rank, world, local_rank):
                    "autotuned": not (args.no_autotune or args.launch_config),
                    "parallelism": f"replicas x{world}"},
         "fp64": {"value": fp64_value, "unit": UNIT, "steps": k64,
-                 "ms_per_step": 1e3 * dev_fp64 / k64},
-        "mixed_over_fp64": value / fp64_value,
+                 "ms_per_step": 1e3 * dev_fp64 / k64,
+                 "algorithm": "reference algebra per node (the 1e-10 parity path)"},
+        "fp64_fastalg": {"value": fast64_value, "unit": UNIT, "steps": k64,
+                         "ms_per_step": 1e3 * dev_fast64 / k64,
+                         "algorithm": "the mixed path's algorithm in FP64 (FP64 tables and "
+                                      "transforms; per-request background polynomials, "
+                                      "regrouped integrand)",
+                         "max_rel_err_vs_fp64": err_fast64},
+        "mixed_over_fp64": value / fast64_value,
+        "mixed_over_fp64_note": "matched algorithms: the mixed step against the same "
+                                "algorithms in FP64 (fp64_fastalg); against the parity "
+                                "path's reference algebra see mixed_over_fp64_parity_path",
+        "mixed_over_fp64_parity_path": value / fp64_value,
         "max_rel_err_mixed_vs_fp64": err,
         "adaptive_retries": retries,
         "gpu_launches": int(launches),
+        "measured_peaks": {"fp32_fma_tflops": peak32, "fp32x2_fma_tflops": peak32x2,
+                           "fp64_fma_tflops": peak64, "sgemm_tflops": sgemm,
+                           "hbm_gbs": peaks.get("hbm_gbs"),
+                           "source": "FMA-chain kernels of coffe_gpu_measure_peak and cuBLAS "
+                                     "SGEMM 8192^3 (TF32 off) in this run; HBM from "
+                                     "MEASURED_PEAKS.json"},
         "roofline": {"kernel": "mp_fast_kernel<3, 3> (mixed multipole quadrature, unit biases)",
                      "bound": "fp32", "achieved": achieved,
-                     "peak": sgemm, "unit": "TFLOP/s", "frac": achieved / sgemm,
-                     "peak_source": "measured cuBLAS SGEMM 8192^3 (FP32 CUDA cores, TF32 off) "
-                                    "in this run; the kernel is FP32-pipe bound, neither HBM "
-                                    "nor tensor",
+                     "peak": peak32, "unit": "TFLOP/s", "frac": achieved / peak32,
+                     "peak_source": "measured fma.rn.f32 rate of this GPU in this run "
+                                    "(coffe_gpu_measure_peak); the kernel is FP32-issue bound, "
+                                    "neither HBM nor tensor",
                      "flop_per_launch": flop_launch, "launch_ms": kern_s * 1e3,
                      "traffic": n_sep * DRAM_BYTES_PER_PAIR,
                      "traffic_unit": "bytes per launch (ncu dram read+write of a 256-spectrum "
                                      "capture, scaled by pairs)",
                      "hbm_peak_gbs": peaks.get("hbm_gbs")},
+        "rooflines": kernel_rooflines(kt, args.n_spectra, len(TERMS), n_sep,
+                                      {"fp32": peak32, "fp64": peak64,
+                                       "hbm_gbs": peaks.get("hbm_gbs") or 6755.5}),
+        "kernel_ms": kt,
         "clocks": clocks,
         "e2e": e2e,
         "cpu_baseline": cpu,

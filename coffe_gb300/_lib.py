@@ -18,11 +18,11 @@ STATUS = {
     -4: "COFFE_GPU_ENONFINITE",
     -5: "COFFE_GPU_ESTATE",
     -6: "COFFE_GPU_ELIMIT",
-    -7: "COFFE_GPU_ETIMEOUT",
 }
 
 FP64 = 0
 MIXED = 1
+FP64_FASTALG = 2
 DEN = 1
 RSD = 2
 LEN = 4
@@ -74,6 +74,9 @@ EXPORTS = (
     "coffe_gpu_divergent_integral",
     "coffe_gpu_renormalization_grid",
     "coffe_gpu_measure_peak",
+    "coffe_gpu_set_kernel_timing",
+    "coffe_gpu_kernel_times",
+    "coffe_gpu_debug_fail_alloc",
 )
 
 
@@ -189,5 +192,9 @@ def load(build_if_missing: bool = True):
     L.coffe_gpu_renormalization_grid.argtypes = [_p, _dp, _dp, C.c_size_t, C.c_double,
                                                  C.c_double, _dp, C.c_size_t, _dp, C.c_size_t, _dp]
     L.coffe_gpu_measure_peak.argtypes = [_p, C.c_int, _dp]
+    L.coffe_gpu_set_kernel_timing.argtypes = [_p, C.c_int]
+    L.coffe_gpu_kernel_times.argtypes = [_p, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong),
+                                         _dp, C.c_int, C.c_int]
+    L.coffe_gpu_debug_fail_alloc.argtypes = [_p, C.c_int]
     _lib = L
     return L

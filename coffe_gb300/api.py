@@ -44,6 +44,8 @@ def _precision(p) -> int:
         return _lib.FP64
     if p in (1, "mixed", "fp32"):
         return _lib.MIXED
+    if p in (2, "fp64-fastalg"):
+        return _lib.FP64_FASTALG
     raise ValueError(f"unknown precision {p!r} (use 'fp64' or 'mixed')")
 
 
@@ -98,6 +100,27 @@ class Context:
 
     def launch_count(self) -> int:
         return int(self._L.coffe_gpu_launch_count(self._ctx))
+
+    def set_kernel_timing(self, enable: bool = True):
+        """Per-kernel CUDA-event timing of this context's launches (see
+        :meth:`kernel_times`)."""
+        self._check(self._L.coffe_gpu_set_kernel_timing(self._ctx, int(bool(enable))),
+                    "set_kernel_timing")
+
+    def kernel_times(self, reset: bool = True) -> dict:
+        """{kernel name: (launches, total ms)} recorded since the last reset."""
+        cap = 64
+        names = (C.c_char_p * cap)()
+        launches = (C.c_longlong * cap)()
+        ms = (C.c_double * cap)()
+        n = self._L.coffe_gpu_kernel_times(self._ctx, names, launches, ms, cap, int(bool(reset)))
+        if n < 0:
+            self._check(n, "kernel_times")
+        return {names[i].decode(): (int(launches[i]), float(ms[i])) for i in range(min(n, cap))}
+
+    def debug_fail_alloc(self, nth: int):
+        """Make the nth device allocation from now fail (ENOMEM); 0 disarms."""
+        self._check(self._L.coffe_gpu_debug_fail_alloc(self._ctx, int(nth)), "debug_fail_alloc")
 
     def measure_peak(self, kind: str) -> float:
         """Measured FLOP/s of this device for ``kind`` in "fp64", "fp32" or

@@ -27,6 +27,12 @@ int cg_ensure(coffe_gpu_ctx *ctx, DevBuf &b, size_t bytes)
     b.p = nullptr;
     b.bytes = 0;
     if (bytes == 0) return COFFE_GPU_OK;
+    // injected failure (coffe_gpu_debug_fail_alloc): this allocation fails as
+    // an exhausted device would make it fail, without calling cudaMalloc
+    if (ctx->fail_alloc_in > 0 && --ctx->fail_alloc_in == 0) {
+        cg_set_error(ctx, "cudaMalloc of %zu bytes failed (injected)", bytes);
+        return COFFE_GPU_ENOMEM;
+    }
     if (cudaMalloc(&b.p, bytes) != cudaSuccess) {
         cudaGetLastError();
         cg_set_error(ctx, "cudaMalloc of %zu bytes failed", bytes);
@@ -43,6 +49,43 @@ void cg_release(DevBuf &b)
     b.bytes = 0;
 }
 
+// Kernel timing mode (coffe_gpu_set_kernel_timing): an event recorded on the
+// stream after every launch (and one at the start of each table or multipole
+// call); the interval between consecutive events of a call is charged to the
+// kernel launched between them.  Nothing is recorded while the stream is
+// being captured.
+static bool cg_timing_active(coffe_gpu_ctx *ctx)
+{
+    if (!ctx->timing) return false;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(ctx->stream, &cap) == cudaSuccess &&
+           cap == cudaStreamCaptureStatusNone;
+}
+
+static void cg_timing_record(coffe_gpu_ctx *ctx, const char *what)
+{
+    if (ctx->timing_marks.size() >= 4096) return; // read them with coffe_gpu_kernel_times
+    const size_t i = ctx->timing_marks.size();
+    if (i == ctx->timing_events.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        ctx->timing_events.push_back(e);
+    }
+    if (cudaEventRecord(ctx->timing_events[i], ctx->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    ctx->timing_marks.push_back(what);
+}
+
+void cg_timing_begin(coffe_gpu_ctx *ctx)
+{
+    if (cg_timing_active(ctx)) cg_timing_record(ctx, nullptr);
+}
+
 int cg_after_launch(coffe_gpu_ctx *ctx, const char *what)
 {
     ctx->launches++;
@@ -51,6 +94,7 @@ int cg_after_launch(coffe_gpu_ctx *ctx, const char *what)
         cg_set_error(ctx, "launch of %s failed: %s", what, cudaGetErrorString(e));
         return COFFE_GPU_ECUDA;
     }
+    if (cg_timing_active(ctx) && !ctx->timing_marks.empty()) cg_timing_record(ctx, what);
     return COFFE_GPU_OK;
 }
 
@@ -120,10 +164,6 @@ int cg_check_device_errors(coffe_gpu_ctx *ctx, const char *where)
                      bits);
         return COFFE_GPU_EINVAL;
     }
-    if (bits & CG_ERR_TIMEOUT) {
-        cg_set_error(ctx, "%s: a bounded device wait timed out", where);
-        return COFFE_GPU_ETIMEOUT;
-    }
     cg_set_error(ctx, "%s: device error flags 0x%x", where, bits);
     return COFFE_GPU_EINVAL;
 }
@@ -140,7 +180,6 @@ const char *coffe_gpu_strerror(int status)
     case COFFE_GPU_ENONFINITE: return "non-finite value in a result";
     case COFFE_GPU_ESTATE: return "missing prerequisite (background or integrals)";
     case COFFE_GPU_ELIMIT: return "adaptive quadrature subinterval limit reached";
-    case COFFE_GPU_ETIMEOUT: return "device-side wait timed out";
     default: return "unknown status";
     }
 }
@@ -201,6 +240,7 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
     spline_free(ctx->cov_pk);
     for (DevBuf *b : bufs) cg_release(*b);
     for (auto &slot : ctx->mp_node_slots) cg_release(slot.buf);
+    for (cudaEvent_t ev : ctx->timing_events) cudaEventDestroy(ev);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -224,6 +264,56 @@ int coffe_gpu_set_stream(coffe_gpu_ctx_t *ctx, void *stream)
 {
     if (!ctx) return COFFE_GPU_EINVAL;
     ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return COFFE_GPU_OK;
+}
+
+int coffe_gpu_set_kernel_timing(coffe_gpu_ctx_t *ctx, int enable)
+{
+    if (!ctx) return COFFE_GPU_EINVAL;
+    ctx->timing = enable != 0;
+    return COFFE_GPU_OK;
+}
+
+int coffe_gpu_kernel_times(coffe_gpu_ctx_t *ctx, const char **names, long long *launches,
+                           double *total_ms, int cap, int reset)
+{
+    if (!ctx || cap < 0 || (cap > 0 && (!names || !launches || !total_ms)))
+        return COFFE_GPU_EINVAL;
+    CG_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (!ctx->timing_marks.empty()) {
+        CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (size_t i = 1; i < ctx->timing_marks.size(); ++i) {
+            const char *what = ctx->timing_marks[i];
+            if (!what) continue; // the start of a call
+            float ms = 0.f;
+            CG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->timing_events[i - 1],
+                                              ctx->timing_events[i]));
+            auto &acc = ctx->timing_totals[what];
+            acc.first += 1;
+            acc.second += ms;
+        }
+        ctx->timing_marks.clear();
+    }
+    // the names handed out live in a snapshot that the next call replaces
+    ctx->timing_names.clear();
+    for (const auto &kv : ctx->timing_totals) ctx->timing_names.push_back(kv.first);
+    int n = 0;
+    for (const auto &kv : ctx->timing_totals) {
+        if (n < cap) {
+            names[n] = ctx->timing_names[n].c_str();
+            launches[n] = kv.second.first;
+            total_ms[n] = kv.second.second;
+        }
+        ++n;
+    }
+    if (reset) ctx->timing_totals.clear();
+    return n;
+}
+
+int coffe_gpu_debug_fail_alloc(coffe_gpu_ctx_t *ctx, int nth)
+{
+    if (!ctx || nth < 0) return COFFE_GPU_EINVAL;
+    ctx->fail_alloc_in = nth;
     return COFFE_GPU_OK;
 }
 

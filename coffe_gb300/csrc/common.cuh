@@ -20,7 +20,6 @@ enum cg_err_bits {
     CG_ERR_NONFINITE = 1,
     CG_ERR_QAG_LIMIT = 2,
     CG_ERR_BOUNDS = 4,
-    CG_ERR_TIMEOUT = 8,
     CG_ERR_BADSEP = 16 // a separation of a host-array call is not > 0
 };
 

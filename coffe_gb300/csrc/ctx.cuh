@@ -7,6 +7,7 @@
 
 #include <array>
 #include <map>
+#include <string>
 #include <vector>
 
 #include "spline.cuh"
@@ -29,6 +30,13 @@ struct coffe_gpu_ctx {
     int *d_err = nullptr;   // device error bits (cg_err_bits)
     int *h_err = nullptr;   // pinned mirror
     long long launches = 0; // kernels launched through this context
+    int fail_alloc_in = 0;  // > 0: that many allocations from now, the last fails
+    // kernel timing mode: events after each launch, totals per kernel name
+    bool timing = false;
+    std::vector<cudaEvent_t> timing_events;
+    std::vector<const char *> timing_marks; // nullptr: the start of a call
+    std::map<std::string, std::pair<long long, double>> timing_totals;
+    std::vector<std::string> timing_names; // names of the last coffe_gpu_kernel_times
     int sm_count = 0;
     char last_error[512] = {0};
     // the multipole output of the running call is page-locked host memory
@@ -150,8 +158,10 @@ int cg_ensure(coffe_gpu_ctx *ctx, DevBuf &b, size_t bytes);
 void cg_release(DevBuf &b);
 // Reads and clears the device error bits; maps them to a status.
 int cg_check_device_errors(coffe_gpu_ctx *ctx, const char *where);
-// Checks the last launch; counts it.
+// Checks the last launch; counts it (and in timing mode records an event).
 int cg_after_launch(coffe_gpu_ctx *ctx, const char *what);
+// Timing mode: marks the start of a table or multipole call.
+void cg_timing_begin(coffe_gpu_ctx *ctx);
 
 // module entry points (host code)
 int bg_init_device(coffe_gpu_ctx *ctx, const coffe_gpu_cosmology_t *c);

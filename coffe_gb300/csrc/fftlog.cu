@@ -1216,6 +1216,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
             return COFFE_GPU_EINVAL;
         }
     }
+    cg_timing_begin(ctx);
     const bool mixed = precision == COFFE_GPU_MIXED;
     const bool tables_df = mixed && (flags & COFFE_GPU_TABLES_DF) != 0;
     const int M = (int)N / 2;

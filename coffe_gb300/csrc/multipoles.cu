@@ -112,34 +112,34 @@ const PanelTables<double> &panel_tables()
     return t64;
 }
 
-// The node table of mp_fast_kernel (layout FastLayout<NL>, float): the mirror
+// The node table of mp_fast_kernel (layout FastLayout<NL>, in T): the mirror
 // rule's rows mu >= 0 ascending with the mu-only RSD coefficients
-void build_node_table_fast(int NL, const int *ls, std::vector<float> &out)
+template <typename T> void build_node_table_fast(int NL, const int *ls, std::vector<T> &out)
 {
     const PanelTables<double> &P = panel_tables();
     const int R1 = ((8 + 3 * NL) + 3) / 4 * 4, R2 = ((1 + NL) + 3) / 4 * 4;
-    out.assign((size_t)31 * (R1 + R2), 0.f);
+    out.assign((size_t)31 * (R1 + R2), T(0));
     for (int k = 0; k < 31; ++k) {
         const int sl = P.order[30 + k];
         const double mult = sl == 60 ? 1.0 : 2.0;
         const double mu = P.mu_sorted[30 + k], mu2 = mu * mu, omm = 1.0 - mu2;
-        float *r = out.data() + (size_t)k * R1;
-        r[0] = (float)mu;
-        r[1] = (float)mu2;
-        r[2] = (float)omm;
-        r[3] = (float)(0.75 * omm * omm + 4.0 * mu2 * omm + 12.0 * mu2 * mu2);  // a2
-        r[4] = (float)(-2.5 * omm * omm - 20.0 * mu2 * omm);                   // a1
-        r[5] = (float)(4.75 * omm * omm - 8.0 * mu2 * omm - 4.0 * mu2 * mu2);  // a0
-        r[6] = (float)(11.0 - 9.0 * omm);                                      // b2
-        r[7] = (float)(9.0 * omm);                                             // -b1
+        T *r = out.data() + (size_t)k * R1;
+        r[0] = (T)mu;
+        r[1] = (T)mu2;
+        r[2] = (T)omm;
+        r[3] = (T)(0.75 * omm * omm + 4.0 * mu2 * omm + 12.0 * mu2 * mu2);  // a2
+        r[4] = (T)(-2.5 * omm * omm - 20.0 * mu2 * omm);                   // a1
+        r[5] = (T)(4.75 * omm * omm - 8.0 * mu2 * omm - 4.0 * mu2 * mu2);  // a0
+        r[6] = (T)(11.0 - 9.0 * omm);                                      // b2
+        r[7] = (T)(9.0 * omm);                                             // -b1
         for (int j = 0; j < NL; ++j) {
-            r[8 + j] = (float)(mult * P.wkP[ls[j]][sl]);
-            r[8 + NL + j] = (float)(mult * P.wgP[ls[j]][sl]);
-            r[8 + 2 * NL + j] = (float)(mult * P.wkA[ls[j]][sl]);
+            r[8 + j] = (T)(mult * P.wkP[ls[j]][sl]);
+            r[8 + NL + j] = (T)(mult * P.wgP[ls[j]][sl]);
+            r[8 + 2 * NL + j] = (T)(mult * P.wkA[ls[j]][sl]);
         }
-        float *r2 = out.data() + (size_t)31 * R1 + (size_t)k * R2;
-        r2[0] = (float)(mult * P.wk[sl]);
-        for (int j = 0; j < NL; ++j) r2[1 + j] = (float)P.Pl[ls[j]][sl];
+        T *r2 = out.data() + (size_t)31 * R1 + (size_t)k * R2;
+        r2[0] = (T)(mult * P.wk[sl]);
+        for (int j = 0; j < NL; ++j) r2[1 + j] = (T)P.Pl[ls[j]][sl];
     }
 }
 
@@ -658,16 +658,36 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
 // Per-request background polynomials: G(chi_mean + X t) = ge(t^2) + t go(t^2),
 // F likewise, ge = (c0, c2, c4), go = (c1, c3, c5) in t; the fourth lanes hold
 // 1/X, chi_mean, X.
-struct BgFit {
+template <typename T> struct BgFitT;
+template <> struct BgFitT<float> {
     float4 ge, go, fe, fo; // (c0,c2,c4,1/X) (c1,c3,c5,chi_mean) (d0,d2,d4,X) (d1,d3,d5,-)
 };
+template <> struct BgFitT<double> {
+    double4_32a ge, go, fe, fo;
+};
+
+template <typename T> __device__ __forceinline__ T from_f64(double x);
+// double -> float without the FP64 pipe (1/64 of the FP32 rate)
+template <> __device__ __forceinline__ float from_f64<float>(double x) { return f32_of_bits(x); }
+template <> __device__ __forceinline__ double from_f64<double>(double x) { return x; }
+
+__device__ __forceinline__ float4 mk4(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
+__device__ __forceinline__ double4_32a mk4(double a, double b, double c, double d)
+{
+    double4_32a v;
+    v.x = a;
+    v.y = b;
+    v.z = c;
+    v.w = d;
+    return v;
+}
 
 // the Chebyshev points t_j = cos((2j + 1) pi / 12), j < 6, and the inverse of
 // their Vandermonde matrix (monomial coefficients from the six values), both
 // computed on the host in FP64
-struct FitInv {
-    float t[6];
-    float m[6][6];
+template <typename T> struct FitInvT {
+    T t[6];
+    T m[6][6];
 };
 
 // one warp per request (MP_FIT_WARPS per block): the largest separation, the
@@ -675,52 +695,53 @@ struct FitInv {
 // splines, as mp_lane_kernel reads them), then the coefficients (lanes 0-11:
 // D1 and f D1) as rows of the inverse Vandermonde
 #define MP_FIT_WARPS 4
+template <typename T, typename S>
 __global__ void __launch_bounds__(32 * MP_FIT_WARPS)
-    mp_bgfit_kernel(Spl32 chi_of_z, Spl32 z_of_chi, Spl32 D1, Spl32 f, int n_req, FitInv vinv,
+    mp_bgfit_kernel(S chi_of_z, S z_of_chi, S D1, S f, int n_req, FitInvT<T> vinv,
                     const double *__restrict__ req_z_mean, const int64_t *__restrict__ req_offset,
-                    const double *__restrict__ sep, BgFit *__restrict__ fit)
+                    const double *__restrict__ sep, BgFitT<T> *__restrict__ fit)
 {
-    __shared__ float val[MP_FIT_WARPS][12];
-    __shared__ float cof[MP_FIT_WARPS][12];
+    __shared__ T val[MP_FIT_WARPS][12];
+    __shared__ T cof[MP_FIT_WARPS][12];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int q = blockIdx.x * MP_FIT_WARPS + w;
     if (q >= n_req) return; // whole warps leave together
-    float rmax = 0.f;
+    T rmax = T(0);
     for (long long i = req_offset[q] + lane; i < req_offset[q + 1]; i += 32)
-        rmax = fmaxf(rmax, f32_of_bits(sep[i]));
-    for (int o = 16; o > 0; o >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-    const float chim = spl_eval(chi_of_z, f32_of_bits(req_z_mean[q]));
-    float X = fminf(0.5f * rmax, fminf(chim - z_of_chi.x0, z_of_chi.xn - chim));
-    if (!(X > 1e-3f)) X = 1e-3f; // empty request or no room: its pairs are outside anyway
+        rmax = fmax(rmax, from_f64<T>(sep[i]));
+    for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    const T chim = spl_eval(chi_of_z, from_f64<T>(req_z_mean[q]));
+    T X = fmin(T(0.5) * rmax, fmin(chim - z_of_chi.x0, z_of_chi.xn - chim));
+    if (!(X > T(1e-3))) X = T(1e-3); // empty request or no room: its pairs are outside anyway
     if (lane < 6) {
-        const float z = spl_eval(z_of_chi, fmaf(X, vinv.t[lane], chim));
-        const float g = spl_eval(D1, z);
+        const T z = spl_eval(z_of_chi, fma(X, vinv.t[lane], chim));
+        const T g = spl_eval(D1, z);
         val[w][lane] = g;
         val[w][6 + lane] = spl_eval(f, z) * g;
     }
     __syncwarp();
     if (lane < 12) {
         const int c = lane % 6, off = lane < 6 ? 0 : 6;
-        float acc = 0.f;
-        for (int k = 0; k < 6; ++k) acc = fmaf(vinv.m[c][k], val[w][off + k], acc);
+        T acc = T(0);
+        for (int k = 0; k < 6; ++k) acc = fma(vinv.m[c][k], val[w][off + k], acc);
         cof[w][lane] = acc;
     }
     __syncwarp();
     if (lane == 0) {
-        const float *c = cof[w];
-        BgFit o;
-        o.ge = make_float4(c[0], c[2], c[4], 1.f / X);
-        o.go = make_float4(c[1], c[3], c[5], chim);
-        o.fe = make_float4(c[6], c[8], c[10], X);
-        o.fo = make_float4(c[7], c[9], c[11], 0.f);
+        const T *c = cof[w];
+        BgFitT<T> o;
+        o.ge = mk4(c[0], c[2], c[4], T(1) / X);
+        o.go = mk4(c[1], c[3], c[5], chim);
+        o.fe = mk4(c[6], c[8], c[10], X);
+        o.fo = mk4(c[7], c[9], c[11], T(0));
         fit[q] = o;
     }
 }
 
 // the inverse Vandermonde matrix of the six Chebyshev points (host, FP64)
-FitInv fit_inverse()
+template <typename T> FitInvT<T> fit_inverse()
 {
-    FitInv r;
+    FitInvT<T> r;
     double V[6][12];
     for (int j = 0; j < 6; ++j) {
         const double t = cos((2 * j + 1) * CG_PI / 12.0);
@@ -742,8 +763,8 @@ FitInv fit_inverse()
             }
     }
     for (int j = 0; j < 6; ++j) {
-        r.t[j] = (float)cos((2 * j + 1) * CG_PI / 12.0);
-        for (int k = 0; k < 6; ++k) r.m[j][k] = (float)V[j][6 + k];
+        r.t[j] = (T)cos((2 * j + 1) * CG_PI / 12.0);
+        for (int k = 0; k < 6; ++k) r.m[j][k] = (T)V[j][6 + k];
     }
     return r;
 }
@@ -762,20 +783,45 @@ template <int NL> struct FastLayout {
 };
 
 #define MP_FAST_MAX_THREADS 256
-template <int NL, int CONTRIB, int UNROLL>
+
+// 1/x: the MUFU reciprocal (2 ulp) on the float path, IEEE division in double
+__device__ __forceinline__ float fast_rcp(float x) { return __fdividef(1.f, x); }
+__device__ __forceinline__ double fast_rcp(double x) { return 1.0 / x; }
+
+// Compensated (Kahan) Kronrod sum on the float path; plain sums in double
+template <typename T> struct KSum;
+template <> struct KSum<float> {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float y)
+    {
+        const float yk = y - c;
+        const float t = s + yk;
+        c = (t - s) - yk;
+        s = t;
+    }
+};
+template <> struct KSum<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double y) { s += y; }
+};
+
+// T = float: the mixed path.  T = double: the same algorithm (background
+// polynomials, regrouped integrand) in FP64, the precision-only baseline of
+// the mixed path (COFFE_GPU_FP64_FASTALG).
+template <int NL, int CONTRIB, int UNROLL, typename T>
 __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
-    mp_fast_kernel(MpArgs a, const BgFit *__restrict__ fit, float chi_lo, float chi_hi,
-                   const float *__restrict__ tab_x, const float *__restrict__ tab_y,
+    mp_fast_kernel(MpArgs a, const BgFitT<T> *__restrict__ fit, T chi_lo, T chi_hi,
+                   const T *__restrict__ tab_x, const T *__restrict__ tab_y,
                    const int *__restrict__ req_spectrum, const double *__restrict__ req_z_mean,
                    const int64_t *__restrict__ req_offset, const double *__restrict__ sep,
-                   long long total, const float *__restrict__ nodes, double *__restrict__ out,
+                   long long total, const T *__restrict__ nodes, double *__restrict__ out,
                    int *__restrict__ retry_count, int2 *__restrict__ retry, int *err)
 {
     typedef FastLayout<NL> LY;
     extern __shared__ __align__(16) unsigned char mp_smem[];
-    float *tab1 = reinterpret_cast<float *>(mp_smem); // [ROWS][R1]
-    float *tab2 = tab1 + LY::ROWS * LY::R1;           // [ROWS][R2]
-    float *xs = tab2 + LY::ROWS * LY::R2;             // [ROWS][blockDim.x] integrand values
+    T *tab1 = reinterpret_cast<T *>(mp_smem); // [ROWS][R1]
+    T *tab2 = tab1 + LY::ROWS * LY::R1;       // [ROWS][R2]
+    T *xs = tab2 + LY::ROWS * LY::R2;         // [ROWS][blockDim.x] integrand values
     for (int i = threadIdx.x; i < LY::COUNT; i += blockDim.x) tab1[i] = nodes[i];
     __syncthreads();
     const long long item0 = (long long)blockIdx.x * blockDim.x;
@@ -784,91 +830,92 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
     const bool valid = item < total;
     const int q = valid ? find_request(req_offset, a.n_req, item) : 0;
     const int s = req_spectrum[q];
-    // double -> float without the FP64 pipe (1/64 of the FP32 rate)
-    const float r = valid ? f32_of_bits(sep[item]) : 1.f;
-    const BgFit bf = fit[q];
-    const float chim = bf.go.w;
-    const float *y0 = tab_y + ((size_t)s * a.n_terms) * a.tab_len;
-    const float idl = f32_of_bits(a.inv_dlog);
+    const T r = valid ? from_f64<T>(sep[item]) : T(1);
+    const BgFitT<T> bf = fit[q];
+    const T chim = bf.go.w;
+    const T *y0 = tab_y + ((size_t)s * a.n_terms) * a.tab_len;
+    const T idl = from_f64<T>(a.inv_dlog);
     const int tl = a.tab_len;
-    const float I00 = table_lookup<float, true>(tab_x, y0 + (size_t)a.t00 * tl, tl, idl, r);
-    const float I02 = table_lookup<float, true>(tab_x, y0 + (size_t)a.t02 * tl, tl, idl, r);
-    const float I04 = table_lookup<float, true>(tab_x, y0 + (size_t)a.t04 * tl, tl, idl, r);
+    const T I00 = table_lookup<T, true>(tab_x, y0 + (size_t)a.t00 * tl, tl, idl, r);
+    const T I02 = table_lookup<T, true>(tab_x, y0 + (size_t)a.t02 * tl, tl, idl, r);
+    const T I04 = table_lookup<T, true>(tab_x, y0 + (size_t)a.t04 * tl, tl, idl, r);
     const int bd = blockDim.x, tid = threadIdx.x;
-    float K[NL], Kc[NL], G[NL], A[NL];
+    KSum<T> K[NL];
+    T G[NL], A[NL];
 #pragma unroll
-    for (int j = 0; j < NL; ++j) K[j] = Kc[j] = G[j] = A[j] = 0.f;
-    const float half_r = 0.5f * r;
-    const float span = tab1[(LY::ROWS - 1) * LY::R1] * half_r; // largest mu
+    for (int j = 0; j < NL; ++j) G[j] = A[j] = T(0);
+    const T half_r = T(0.5) * r;
+    const T span = tab1[(LY::ROWS - 1) * LY::R1] * half_r; // largest mu
     const bool inside = valid && (chim - span >= chi_lo) && (chim + span <= chi_hi);
     const bool finite = inside && isfinite(I00) && isfinite(I02) && isfinite(I04);
     if (inside) {
-        const float A2 = 2.f * chim * chim, Br = 0.5f * r * r, r2 = r * r;
-        const float e00 = I00 * (1.f / 15.f), e02 = I02 * (1.f / 21.f), e04 = I04 * (1.f / 35.f);
-        const float e00x2 = 2.f * e00, e0d = e00 - e02;
-        const float K1 = (I00 - 2.f * I02) * (1.f / 3.f);
-        const float rho = half_r * bf.ge.w; // t = mu rho in [-1, 1] for inside pairs
+        const T A2 = T(2) * chim * chim, Br = T(0.5) * r * r, r2 = r * r;
+        const T e00 = I00 * T(1.0 / 15.0), e02 = I02 * T(1.0 / 21.0), e04 = I04 * T(1.0 / 35.0);
+        const T e00x2 = T(2) * e00, e0d = e00 - e02;
+        const T K1 = (I00 - T(2) * I02) * T(1.0 / 3.0);
+        const T rho = half_r * bf.ge.w; // t = mu rho in [-1, 1] for inside pairs
 #pragma unroll UNROLL
         for (int k = 0; k < LY::ROWS; ++k) {
-            float rec[LY::R1];
+            T rec[LY::R1];
             lds_rec<LY::R1>(tab1 + k * LY::R1, rec);
-            const float mu = rec[0], mu2 = rec[1], omm = rec[2];
-            const float chi1 = fmaf(-mu, half_r, chim), chi2 = fmaf(mu, half_r, chim);
+            const T mu = rec[0], mu2 = rec[1], omm = rec[2];
+            const T chi1 = fma(-mu, half_r, chim), chi2 = fma(mu, half_r, chim);
             // background at chi_mean -/+ mu r/2: even and odd parts in t
-            const float t = mu * rho, u = t * t;
-            const float gE = fmaf(fmaf(bf.ge.z, u, bf.ge.y), u, bf.ge.x);
-            const float gO = fmaf(fmaf(bf.go.z, u, bf.go.y), u, bf.go.x);
-            const float fE = fmaf(fmaf(bf.fe.z, u, bf.fe.y), u, bf.fe.x);
-            const float fO = fmaf(fmaf(bf.fo.z, u, bf.fo.y), u, bf.fo.x);
-            const float G1 = fmaf(-t, gO, gE), G2 = fmaf(t, gO, gE);
-            const float F1 = fmaf(-t, fO, fE), F2 = fmaf(t, fO, fE);
-            const float D = fmaf(-mu2, Br, A2); // 2 chi1 chi2
-            const float inv_D = __fdividef(1.f, D);
-            const float sv = r2 * omm * inv_D;
-            const float c = 1.f - sv;
-            float v = 0.f;
+            const T t = mu * rho, u = t * t;
+            const T gE = fma(fma(bf.ge.z, u, bf.ge.y), u, bf.ge.x);
+            const T gO = fma(fma(bf.go.z, u, bf.go.y), u, bf.go.x);
+            const T fE = fma(fma(bf.fe.z, u, bf.fe.y), u, bf.fe.x);
+            const T fO = fma(fma(bf.fo.z, u, bf.fo.y), u, bf.fo.x);
+            const T G1 = fma(-t, gO, gE), G2 = fma(t, gO, gE);
+            const T F1 = fma(-t, fO, fE), F2 = fma(t, fO, fE);
+            const T D = fma(-mu2, Br, A2); // 2 chi1 chi2
+            const T inv_D = fast_rcp(D);
+            const T sv = r2 * omm * inv_D;
+            const T c = T(1) - sv;
+            T v = T(0);
             if (CONTRIB & COFFE_GPU_DEN) v = G1 * G2 * I00;
             if (CONTRIB & COFFE_GPU_RSD) {
-                const float g2c = fmaf(rec[3], e04, fmaf(-rec[6], e02, e00x2));
-                const float g1c = fmaf(rec[4], e04, rec[7] * e02);
-                const float g0c = fmaf(rec[5], e04, e0d);
-                v = fmaf(F1 * F2, fmaf(fmaf(g2c, c, g1c), c, g0c), v);
+                const T g2c = fma(rec[3], e04, fma(-rec[6], e02, e00x2));
+                const T g1c = fma(rec[4], e04, rec[7] * e02);
+                const T g0c = fma(rec[5], e04, e0d);
+                v = fma(F1 * F2, fma(fma(g2c, c, g1c), c, g0c), v);
             }
             if ((CONTRIB & COFFE_GPU_DEN) && (CONTRIB & COFFE_GPU_RSD)) {
-                const float gf = G1 * F2, fg = F1 * G2;
-                const float g = (1.f + c) * omm * inv_D;
-                v = fmaf(gf + fg, K1, v);
-                v = fmaf(g * I02, fmaf(gf, chi1 * chi1, fg * (chi2 * chi2)), v);
+                const T gf = G1 * F2, fg = F1 * G2;
+                const T g = (T(1) + c) * omm * inv_D;
+                v = fma(gf + fg, K1, v);
+                v = fma(g * I02, fma(gf, chi1 * chi1, fg * (chi2 * chi2)), v);
             }
             xs[k * bd + tid] = v;
-            const float av = fabsf(v);
+            const T av = fabs(v);
 #pragma unroll
-            for (int j = 0; j < NL; ++j) { // Kahan-compensated Kronrod sum
-                const float yk = rec[8 + j] * v - Kc[j];
-                const float tk = K[j] + yk;
-                Kc[j] = (tk - K[j]) - yk;
-                K[j] = tk;
-                G[j] = fmaf(rec[8 + NL + j], v, G[j]);
-                A[j] = fmaf(rec[8 + 2 * NL + j], av, A[j]);
+            for (int j = 0; j < NL; ++j) {
+                K[j].add(rec[8 + j] * v);
+                G[j] = fma(rec[8 + NL + j], v, G[j]);
+                A[j] = fma(rec[8 + 2 * NL + j], av, A[j]);
             }
         }
     }
-    float asc[NL];
+    T Ks[NL], asc[NL];
 #pragma unroll
-    for (int j = 0; j < NL; ++j) asc[j] = 0.f;
+    for (int j = 0; j < NL; ++j) {
+        Ks[j] = K[j].s;
+        asc[j] = T(0);
+    }
     if (inside) {
 #pragma unroll 1
         for (int k = 0; k < LY::ROWS; ++k) {
-            float rec[LY::R2];
+            T rec[LY::R2];
             lds_rec<LY::R2>(tab2 + k * LY::R2, rec);
-            const float v = xs[k * bd + tid];
+            const T v = xs[k * bd + tid];
 #pragma unroll
-            for (int j = 0; j < NL; ++j) asc[j] = fmaf(rec[0], fabsf(fmaf(v, rec[1 + j], -0.5f * K[j])), asc[j]);
+            for (int j = 0; j < NL; ++j)
+                asc[j] = fma(rec[0], fabs(fma(v, rec[1 + j], T(-0.5) * Ks[j])), asc[j]);
         }
     }
     if (!a.out_staged) {
-        first_panel_out<NL, float>(a, f32_of_bits(a.epsrel), item, finite, K, G, A, asc, out,
-                                   retry_count, retry, err);
+        first_panel_out<NL, T>(a, from_f64<T>(a.epsrel), item, finite, Ks, G, A, asc, out,
+                               retry_count, retry, err);
         return;
     }
     // out in page-locked host memory: the block's results go through shared
@@ -877,8 +924,8 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
     double res[NL];
     bool have[NL];
     if (valid)
-        first_panel_value<NL, float>(a, f32_of_bits(a.epsrel), item, finite, K, G, A, asc, res,
-                                     have, retry_count, retry, err);
+        first_panel_value<NL, T>(a, from_f64<T>(a.epsrel), item, finite, Ks, G, A, asc, res,
+                                 have, retry_count, retry, err);
     __syncthreads();
     double *stage = reinterpret_cast<double *>(xs);
     if (valid) {
@@ -1043,50 +1090,50 @@ int node_slot(coffe_gpu_ctx *ctx, int n_l, const int *ls, int prec_tag, int layo
     return COFFE_GPU_OK;
 }
 
-// mp_fast_kernel for a validated mixed call with unit biases, even
-// multipoles (at most four) and no only-cross switch, then the retries
-int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<float, Spl32> &bg,
-                const Spl32 &chi_of_z, const float *tab_x, const float *tab_y,
-                const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
-                const double *sep, long long total, double *out)
+// mp_fast_kernel for a validated call with unit biases, even multipoles (at
+// most four) and no only-cross switch, then the retries: T = float for the
+// mixed path, double for its FP64 baseline (COFFE_GPU_FP64_FASTALG)
+template <typename T, typename S>
+int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S &chi_of_z,
+                const T *tab_x, const T *tab_y, const int *req_spectrum, const double *req_z_mean,
+                const int64_t *req_offset, const double *sep, long long total, double *out)
 {
     int *d_count = (int *)ctx->mp_retry.p;
     int2 *d_retry = (int2 *)((char *)ctx->mp_retry.p + 256);
     const void *dn = nullptr;
-    int st = node_slot(ctx, a.n_l, a.ls, COFFE_GPU_MIXED, 2,
+    const int prec_tag = sizeof(T) == sizeof(float) ? COFFE_GPU_MIXED : COFFE_GPU_FP64_FASTALG;
+    int st = node_slot(ctx, a.n_l, a.ls, prec_tag, 2,
                        [&](std::vector<unsigned char> &bytes) {
-                           std::vector<float> tab;
-                           build_node_table_fast(a.n_l, a.ls, tab);
+                           std::vector<T> tab;
+                           build_node_table_fast<T>(a.n_l, a.ls, tab);
                            bytes.assign((const unsigned char *)tab.data(),
                                         (const unsigned char *)(tab.data() + tab.size()));
                        },
                        &dn);
     if (st) return st;
-    if ((st = cg_ensure(ctx, ctx->mp_bgfit, sizeof(BgFit) * (size_t)a.n_req))) return st;
-    BgFit *d_fit = (BgFit *)ctx->mp_bgfit.p;
-    static const FitInv vinv = fit_inverse();
+    if ((st = cg_ensure(ctx, ctx->mp_bgfit, sizeof(BgFitT<T>) * (size_t)a.n_req))) return st;
+    BgFitT<T> *d_fit = (BgFitT<T> *)ctx->mp_bgfit.p;
+    static const FitInvT<T> vinv = fit_inverse<T>();
     const int contrib = a.contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD);
     // first panel (with lt threads per block) and the adaptive retries
     auto run = [&](const coffe_gpu_tuning_t &tu) -> int {
         const int lt = tu.lane_threads;
         const long long blocks = (total + lt - 1) / lt;
         CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
-        mp_bgfit_kernel<<<(a.n_req + MP_FIT_WARPS - 1) / MP_FIT_WARPS, 32 * MP_FIT_WARPS, 0,
-                          ctx->stream>>>(ctx->bg[BG_CHI_OF_Z].v32(), ctx->bg[BG_Z_OF_CHI].v32(),
-                                         ctx->bg[BG_D1].v32(), ctx->bg[BG_F].v32(), a.n_req,
-                                         vinv, req_z_mean, req_offset, sep, d_fit);
+        mp_bgfit_kernel<T, S><<<(a.n_req + MP_FIT_WARPS - 1) / MP_FIT_WARPS, 32 * MP_FIT_WARPS, 0,
+                                ctx->stream>>>(chi_of_z, bg.z_of_chi, bg.D1, bg.f, a.n_req, vinv,
+                                               req_z_mean, req_offset, sep, d_fit);
         int s1 = cg_after_launch(ctx, "mp_bgfit_kernel");
         if (s1) return s1;
 #define MP_FAST_U(NLV, CV, UV)                                                                    \
     {                                                                                             \
-        const size_t smem = sizeof(float) * (FastLayout<NLV>::COUNT + FastLayout<NLV>::ROWS * lt); \
-        CG_CUDA(ctx, cudaFuncSetAttribute(mp_fast_kernel<NLV, CV, UV>,                            \
+        const size_t smem = sizeof(T) * (FastLayout<NLV>::COUNT + FastLayout<NLV>::ROWS * lt);    \
+        CG_CUDA(ctx, cudaFuncSetAttribute(mp_fast_kernel<NLV, CV, UV, T>,                         \
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,            \
                                           (int)smem));                                            \
-        mp_fast_kernel<NLV, CV, UV><<<(unsigned)blocks, lt, smem, ctx->stream>>>(                 \
-            a, d_fit, bg.z_of_chi.x0, bg.z_of_chi.xn, tab_x, tab_y, req_spectrum,                 \
-            req_z_mean, req_offset, sep, total, (const float *)dn, out, d_count, d_retry,         \
-            ctx->d_err);                                                                          \
+        mp_fast_kernel<NLV, CV, UV, T><<<(unsigned)blocks, lt, smem, ctx->stream>>>(              \
+            a, d_fit, bg.z_of_chi.x0, bg.z_of_chi.xn, tab_x, tab_y, req_spectrum, req_z_mean,     \
+            req_offset, sep, total, (const T *)dn, out, d_count, d_retry, ctx->d_err);            \
     }
 #define MP_FAST(NLV, CV)                                                                          \
     if (a.n_l == NLV && contrib == CV) {                                                          \
@@ -1105,10 +1152,9 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<float, Spl32> &bg,
 #undef MP_FAST_U
         int s2 = cg_after_launch(ctx, "mp_fast_kernel");
         if (s2) return s2;
-        mp_retry_kernel<float, Spl32, float><<<ctx->sm_count * 2, 32 * MP_RETRY_WARPS, 0,
-                                               ctx->stream>>>(a, bg, chi_of_z, tab_x, tab_y,
-                                                              req_spectrum, req_z_mean, req_offset,
-                                                              sep, out, d_count, d_retry, ctx->d_err);
+        mp_retry_kernel<T, S, T><<<ctx->sm_count * 2, 32 * MP_RETRY_WARPS, 0, ctx->stream>>>(
+            a, bg, chi_of_z, tab_x, tab_y, req_spectrum, req_z_mean, req_offset, sep, out,
+            d_count, d_retry, ctx->d_err);
         return cg_after_launch(ctx, "mp_retry_kernel");
     };
     std::vector<coffe_gpu_tuning_t> cands;
@@ -1122,7 +1168,7 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<float, Spl32> &bg,
     coffe_gpu_tuning_t tu;
     long long bucket = 0;
     while ((1ll << bucket) < total) ++bucket;
-    const std::array<long long, 6> key{2, a.n_l, contrib, bucket, 0, 0};
+    const std::array<long long, 6> key{2, a.n_l, contrib, bucket, prec_tag, 0};
     if ((st = cg_tuned(ctx, key, cands, run, &tu))) return st;
     ctx->last_tuning.lane_threads = tu.lane_threads;
     ctx->last_tuning.lane_unroll = tu.lane_unroll;
@@ -1267,7 +1313,8 @@ int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel
         cg_set_error(ctx, "multipoles: need 1 <= n_l <= %d and n_req >= 1", MP_MAX_L);
         return COFFE_GPU_EINVAL;
     }
-    if (precision != ctx->int_precision) {
+    if (precision != ctx->int_precision &&
+        !(precision == COFFE_GPU_FP64_FASTALG && ctx->int_precision == COFFE_GPU_FP64)) {
         cg_set_error(ctx, "multipoles: precision %d differs from the integrals' (%d)", precision,
                      ctx->int_precision);
         return COFFE_GPU_EINVAL;
@@ -1313,6 +1360,7 @@ int multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel
     if (ctx->sm_count <= 0)
         CG_CUDA(ctx, cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount,
                                             ctx->device));
+    cg_timing_begin(ctx);
     if (!(contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD))) {
         // lensing only: no nonintegrated terms (signal.c:472-520 returns 0)
         CG_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(double) * (size_t)total * n_l, ctx->stream));
@@ -1353,9 +1401,10 @@ static int multipoles_nonintegrated(coffe_gpu_ctx *ctx, const MpArgs &a, int pre
                     !(a.contrib & COFFE_GPU_ONLY_CROSS);
         for (int j = 0; j < a.n_l; ++j) fast = fast && a.ls[j] % 2 == 0;
         if (fast)
-            return launch_fast(ctx, a, bg, ctx->bg[BG_CHI_OF_Z].v32(),
-                               (const float *)ctx->tab_x32.p, (const float *)ctx->tab_y.p,
-                               req_spectrum, req_z_mean, req_offset, sep, total, out);
+            return launch_fast<float, Spl32>(ctx, a, bg, ctx->bg[BG_CHI_OF_Z].v32(),
+                                             (const float *)ctx->tab_x32.p,
+                                             (const float *)ctx->tab_y.p, req_spectrum,
+                                             req_z_mean, req_offset, sep, total, out);
         return launch<float, Spl32, float>(ctx, a, bg, ctx->bg[BG_CHI_OF_Z].v32(),
                                            (const float *)ctx->tab_x32.p,
                                            (const float *)ctx->tab_y.p, req_spectrum, req_z_mean,
@@ -1375,6 +1424,16 @@ static int multipoles_nonintegrated(coffe_gpu_ctx *ctx, const MpArgs &a, int pre
     bg.dz = ctx->dz;
     bg.inv_dz = 1.0 / ctx->dz;
     bg.nz = ctx->bg_bins;
+    if (precision == COFFE_GPU_FP64_FASTALG) {
+        bool fast = a.n_l <= 4 && !ctx->bias_set[0] && !ctx->bias_set[1] &&
+                    !(a.contrib & COFFE_GPU_ONLY_CROSS);
+        for (int j = 0; j < a.n_l; ++j) fast = fast && a.ls[j] % 2 == 0;
+        if (fast)
+            return launch_fast<double, Spl64>(ctx, a, bg, ctx->bg[BG_CHI_OF_Z].v64(),
+                                              (const double *)ctx->tab_x.p,
+                                              (const double *)ctx->tab_y.p, req_spectrum,
+                                              req_z_mean, req_offset, sep, total, out);
+    }
     return launch<double, Spl64, double>(ctx, a, bg, ctx->bg[BG_CHI_OF_Z].v64(),
                                          (const double *)ctx->tab_x.p,
                                          (const double *)ctx->tab_y.p, req_spectrum, req_z_mean,

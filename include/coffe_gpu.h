@@ -37,15 +37,21 @@ enum coffe_gpu_status {
     COFFE_GPU_ENOMEM = -3,     /* device allocation failed */
     COFFE_GPU_ENONFINITE = -4, /* a kernel produced NaN/Inf (reference would exit) */
     COFFE_GPU_ESTATE = -5,     /* a prerequisite (background, integrals) is missing */
-    COFFE_GPU_ELIMIT = -6,     /* adaptive quadrature ran out of subintervals */
-    COFFE_GPU_ETIMEOUT = -7    /* a bounded device-side wait gave up */
+    COFFE_GPU_ELIMIT = -6      /* adaptive quadrature ran out of subintervals */
 };
 
 /* Precision of a computation. */
 enum coffe_gpu_precision {
-    COFFE_GPU_FP64 = 0, /* plain FP64 everywhere: the parity path */
-    COFFE_GPU_MIXED = 1 /* FP32 FFT/spline/integrand arithmetic with compensated
-                           sums; FP64 Gamma-ratio coefficients and background */
+    COFFE_GPU_FP64 = 0,        /* plain FP64 everywhere: the parity path */
+    COFFE_GPU_MIXED = 1,       /* FP32 FFT/spline/integrand arithmetic with compensated
+                                  sums; FP64 Gamma-ratio coefficients and background */
+    COFFE_GPU_FP64_FASTALG = 2 /* coffe_gpu_multipoles only, on FP64 tables: FP64
+                                  arithmetic through the mixed path's algorithm for
+                                  unit biases and even multipoles (per-request
+                                  background polynomials, regrouped integrand;
+                                  ~1e-8 from the parity path), the precision-only
+                                  baseline of COFFE_GPU_MIXED.  Other calls take the
+                                  FP64 path. */
 };
 
 /* Contributions to the 2-point function (the den, rsd, len flags of
@@ -482,6 +488,31 @@ int coffe_gpu_average_covariance_multipoles(coffe_gpu_ctx_t *ctx, int contrib,
 #define COFFE_GPU_PEAK_FP32 1
 #define COFFE_GPU_PEAK_FP32X2 2
 int coffe_gpu_measure_peak(coffe_gpu_ctx_t *ctx, int kind, double *flops_per_s);
+
+/* No counterpart in the reference (its only timing is the clock() prints of
+   its verbose mode): per-kernel device time.  enable != 0 records a CUDA event
+   on the context's stream after every kernel launch, and one at the start of
+   each table (coffe_gpu_integrals_init*) and multipole call; the interval
+   between consecutive events of a call is charged to the kernel launched in
+   it (a copy or memset enqueued before a kernel is charged to that kernel).
+   Calls made while the stream is being captured record nothing.  Costs a few
+   microseconds per launch; off by default. */
+int coffe_gpu_set_kernel_timing(coffe_gpu_ctx_t *ctx, int enable);
+/* Synchronises the stream and accumulates the recorded intervals, then writes
+   up to `cap` entries: kernel name (valid until the next call of this
+   function on the context or its destruction), launches and total
+   milliseconds.  Returns the number of distinct kernels timed since the last
+   reset (may exceed cap) or a negative status; reset != 0 clears the totals
+   after writing them. */
+int coffe_gpu_kernel_times(coffe_gpu_ctx_t *ctx, const char **names, long long *launches,
+                           double *total_ms, int cap, int reset);
+
+/* No counterpart in the reference: failure injection for tests.  The nth
+   device allocation this context makes from now on fails as an exhausted
+   device would make it fail (COFFE_GPU_ENOMEM from the call that needed it),
+   without calling cudaMalloc; nth = 0 disarms.  Allocations are made on first
+   use and when a call needs larger buffers than any before it. */
+int coffe_gpu_debug_fail_alloc(coffe_gpu_ctx_t *ctx, int nth);
 
 /* Kernel launches issued by this context since creation (for accounting). */
 long long coffe_gpu_launch_count(const coffe_gpu_ctx_t *ctx);
