@@ -3,11 +3,18 @@
 //
 // Node i sits at z_i = 15 i / (bins - 1).  chi(z_i) is the GK61 QAG integral of
 // 1/E(z) (background.c:485-502) computed by one warp per node; D1 and f come
-// from the growth ODE (background.c:196-211, 430-481) integrated from
-// a = 0.05, (D, D') = (0.05, 1) up to a_i independently for every node, as the
-// reference does, with classical RK4 steps of at most 1e-3 in a.  The ODE's
-// x(z) = Om/(1-Om) (1+z)^3 is read through the same linear interpolation on
-// 16385 points in [0, 100] as the reference's xint spline (background.c:337-412).
+// from the growth ODE (background.c:196-211, 430-481) from a = 0.05,
+// (D, D') = (0.05, 1): one trajectory of 950 classical RK4 steps of 1e-3 in a
+// up to a = 1, integrated on the host (a sequential recurrence of ~10^4
+// operations), then read at every node by cubic Hermite interpolation between
+// the two steps around a_i, with the ODE's own derivatives (error ~h^4/384 of
+// the fourth derivative, far below the RK4 error).  The reference integrates
+// every node separately with GSL's adaptive rk2; both agree with it to its
+// tolerance.  The ODE's x(z) = Om/(1-Om) (1+z)^3 is read through the same
+// linear interpolation on 16385 points in [0, 100] as the reference's xint
+// spline (background.c:337-412).
+#include <vector>
+
 #include "ctx.cuh"
 #include "qag.cuh"
 
@@ -15,13 +22,16 @@ namespace {
 
 #define BG_XINT_BINS 16384
 #define BG_XINT_ZMAX 100.0
-#define BG_ODE_HMAX 1e-3
 
 struct BgPar {
     double om, og, ode, h;
 };
 
-__device__ __forceinline__ double xint_lin(const BgPar &p, double z)
+#define BG_ODE_A0 0.05
+#define BG_ODE_STEPS 950 // (1 - 0.05) / 1e-3
+
+// x(z) through the linear interpolation of the reference's xint spline
+double xint_lin(const BgPar &p, double z)
 {
     const double dz = BG_XINT_ZMAX / BG_XINT_BINS;
     const double ratio = p.om / (1.0 - p.om);
@@ -35,8 +45,7 @@ __device__ __forceinline__ double xint_lin(const BgPar &p, double z)
     return x0 + (z - z0) * ((x1 - x0) / (z1 - z0));
 }
 
-__device__ __forceinline__ void growth_rhs(const BgPar &p, double a, double y0, double y1,
-                                           double &f0, double &f1)
+void growth_rhs(const BgPar &p, double a, double y0, double y1, double &f0, double &f1)
 {
     const double z = 1. / a - 1;
     const double w = -1.0;
@@ -45,7 +54,33 @@ __device__ __forceinline__ void growth_rhs(const BgPar &p, double a, double y0, 
     f1 = -3. / 2 * (1 - w / (1 + x)) * y1 / a + 3. / 2 * x / (1 + x) * y0 / (a * a);
 }
 
-__global__ void bg_nodes_kernel(BgPar p, int bins, double *__restrict__ nodes)
+// the growth trajectory at a_s = a0 + s h, s = 0..BG_ODE_STEPS: (D, D', and
+// their derivatives from the ODE) per step point, host side
+void growth_trajectory(const BgPar &p, std::vector<double4_32a> &tr)
+{
+    const double h = (1.0 - BG_ODE_A0) / BG_ODE_STEPS;
+    tr.resize(BG_ODE_STEPS + 1);
+    double y0 = 0.05, y1 = 1.0;
+    for (int s = 0; s <= BG_ODE_STEPS; ++s) {
+        const double a = BG_ODE_A0 + h * (double)s;
+        double k10, k11;
+        growth_rhs(p, a, y0, y1, k10, k11);
+        tr[s].x = y0;
+        tr[s].y = y1;
+        tr[s].z = k10;
+        tr[s].w = k11;
+        if (s == BG_ODE_STEPS) break;
+        double k20, k21, k30, k31, k40, k41;
+        growth_rhs(p, a + 0.5 * h, y0 + 0.5 * h * k10, y1 + 0.5 * h * k11, k20, k21);
+        growth_rhs(p, a + 0.5 * h, y0 + 0.5 * h * k20, y1 + 0.5 * h * k21, k30, k31);
+        growth_rhs(p, a + h, y0 + h * k30, y1 + h * k31, k40, k41);
+        y0 += h / 6.0 * (k10 + 2.0 * k20 + 2.0 * k30 + k40);
+        y1 += h / 6.0 * (k11 + 2.0 * k21 + 2.0 * k31 + k41);
+    }
+}
+
+__global__ void bg_nodes_kernel(BgPar p, int bins, const double4_32a *__restrict__ tr,
+                                double *__restrict__ nodes)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= bins) return;
@@ -53,23 +88,17 @@ __global__ void bg_nodes_kernel(BgPar p, int bins, double *__restrict__ nodes)
            *cH_ = nodes + 5 * bins, *H_ = nodes + 6 * bins, *cHp_ = nodes + 7 * bins;
     const double zi = 15. * i / (double)(bins - 1);
     const double ai = 1. / (1. + zi);
-    // growth ODE, RK4 from a = 0.05
-    const double a0 = 0.05;
-    double y0 = 0.05, y1 = 1.0;
-    if (ai > a0) {
-        const long nstep = (long)ceil((ai - a0) / BG_ODE_HMAX);
-        const double hh = (ai - a0) / (double)nstep;
-        for (long s = 0; s < nstep; ++s) {
-            const double a = a0 + hh * (double)s;
-            double k10, k11, k20, k21, k30, k31, k40, k41;
-            growth_rhs(p, a, y0, y1, k10, k11);
-            growth_rhs(p, a + 0.5 * hh, y0 + 0.5 * hh * k10, y1 + 0.5 * hh * k11, k20, k21);
-            growth_rhs(p, a + 0.5 * hh, y0 + 0.5 * hh * k20, y1 + 0.5 * hh * k21, k30, k31);
-            growth_rhs(p, a + hh, y0 + hh * k30, y1 + hh * k31, k40, k41);
-            y0 += hh / 6.0 * (k10 + 2.0 * k20 + 2.0 * k30 + k40);
-            y1 += hh / 6.0 * (k11 + 2.0 * k21 + 2.0 * k31 + k41);
-        }
-    }
+    // cubic Hermite interpolation of the trajectory between the steps around ai
+    const double h = (1.0 - BG_ODE_A0) / BG_ODE_STEPS;
+    int s = (int)floor((ai - BG_ODE_A0) / h);
+    s = s < 0 ? 0 : (s > BG_ODE_STEPS - 1 ? BG_ODE_STEPS - 1 : s);
+    const double t = (ai - (BG_ODE_A0 + h * (double)s)) / h;
+    const double4_32a u = tr[s], v = tr[s + 1];
+    const double t2 = t * t, t3 = t2 * t;
+    const double h00 = 2 * t3 - 3 * t2 + 1, h10 = t3 - 2 * t2 + t, h01 = -2 * t3 + 3 * t2,
+                 h11 = t3 - t2;
+    const double y0 = h00 * u.x + h10 * h * u.z + h01 * v.x + h11 * h * v.z;
+    const double y1 = h00 * u.y + h10 * h * u.w + h01 * v.y + h11 * h * v.w;
     const double Hi = sqrt(p.om * pow(1 + zi, 3) + p.og * pow(1 + zi, 4) + p.ode * 1.0) * p.h * CG_H0;
     z_[i] = zi;
     a_[i] = ai;
@@ -146,7 +175,14 @@ int bg_init_device(coffe_gpu_ctx *ctx, const coffe_gpu_cosmology_t *c)
     if (st) return st;
     BgPar p{c->Omega0_cdm + c->Omega0_baryon, c->Omega0_gamma, c->Omega0_de, c->h};
     double *nodes = (double *)ctx->bg_nodes.p;
-    bg_nodes_kernel<<<(bins + 127) / 128, 128, 0, ctx->stream>>>(p, bins, nodes);
+    growth_trajectory(p, ctx->bg_traj_host);
+    if ((st = cg_ensure(ctx, ctx->bg_traj, sizeof(double4_32a) * ctx->bg_traj_host.size())))
+        return st;
+    CG_CUDA(ctx, cudaMemcpyAsync(ctx->bg_traj.p, ctx->bg_traj_host.data(),
+                                 sizeof(double4_32a) * ctx->bg_traj_host.size(),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    bg_nodes_kernel<<<(bins + 127) / 128, 128, 0, ctx->stream>>>(
+        p, bins, (const double4_32a *)ctx->bg_traj.p, nodes);
     if ((st = cg_after_launch(ctx, "bg_nodes_kernel"))) return st;
     bg_chi_kernel<<<(bins + BG_WARPS - 1) / BG_WARPS, 32 * BG_WARPS, 0, ctx->stream>>>(
         p, bins, nodes, ctx->d_err);

@@ -236,7 +236,8 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
                       &ctx->lens_rule, &ctx->lens_rec, &ctx->lens_part,
                       &ctx->cov_buf,  &ctx->cov_out, &ctx->adj_buf, &ctx->csband,
                       &ctx->samp_tdf, &ctx->qfac_df, &ctx->pk_df, &ctx->mp_bgfit,
-                      &ctx->cf_rule, &ctx->avg_buf, &ctx->div_buf, &ctx->peak_buf};
+                      &ctx->cf_rule, &ctx->avg_buf, &ctx->div_buf, &ctx->peak_buf,
+                      &ctx->bg_traj};
     spline_free(ctx->cov_pk);
     for (DevBuf *b : bufs) cg_release(*b);
     for (auto &slot : ctx->mp_node_slots) cg_release(slot.buf);

@@ -49,6 +49,8 @@ struct coffe_gpu_ctx {
     bool bg_ready = false, bg_has_H = false;
     double Omega0_m = 0.3, h = 0.67;
     DevBuf bg_nodes; // bins * 8 doubles: z, chi, D1, f, a, confH, H, confHp
+    DevBuf bg_traj;  // growth ODE trajectory (D, D', and derivatives) per RK4 step
+    std::vector<double4_32a> bg_traj_host;
     SplineBuf bg[BG_NFN];
     // fused f / D1 coefficient records on a uniform z grid (multipoles.cu)
     bool z_uniform = false;
@@ -89,6 +91,9 @@ struct coffe_gpu_ctx {
     DevBuf samp_f32;  // N float4 (dx, h, 1/h, -) for the mixed path
     DevBuf csfac32;   // 4 * nk floats: spline factors for the mixed path
     DevBuf csband;    // 25 x (nk - 2) floats: band of the inverse spline matrix, by diagonal
+    // host copies of the per-grid spline factors and band (sources of the uploads)
+    std::vector<double> grid_fac_host;
+    std::vector<float> grid_fac32_host, grid_band_host;
     DevBuf samp_tdf;  // N float2: double-float dx / h of each FFT node (mixed path)
     DevBuf qfac_df;   // n_q * N float2: double-float windowed bias (mixed path)
     DevBuf pk_df;     // n_spectra * nk float2: double-float input spectra (mixed path)

@@ -70,15 +70,17 @@ struct GridPar {
 
 // --------------------------------------------------------------- per grid
 
-// Factors of the natural-spline tridiagonal system on the shared k grid (one
-// thread, once per grid): fac = [1/diag'_i (eliminated diagonal), w_i
-// (elimination multipliers), g_i = 1/h_i], each nk long.
-__global__ void csfac_kernel(const double *__restrict__ x, int nk, double *__restrict__ fac,
-                             float *__restrict__ fac32)
+// Factors of the natural-spline tridiagonal system on the shared k grid (host,
+// once per grid; O(nk) sequential work that the host does in microseconds):
+// fac = [1/diag'_i (eliminated diagonal), w_i (elimination multipliers),
+// g_i = 1/h_i], each nk long; fac32 = their float copies and h_i for the
+// mixed path: [1/diag', w, 1/h, h].
+void csfac_host(const double *x, int nk, std::vector<double> &fac, std::vector<float> &fac32)
 {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
     const int m = nk - 2;
-    double *invd = fac, *w = fac + nk, *g = fac + 2 * nk;
+    fac.assign((size_t)3 * nk, 0.0);
+    fac32.assign((size_t)4 * nk, 0.f);
+    double *invd = fac.data(), *w = fac.data() + nk, *g = fac.data() + 2 * nk;
     for (int i = 0; i + 1 < nk; ++i) g[i] = 1.0 / (x[i + 1] - x[i]);
     double dprev = 0.0;
     w[0] = 0.0;
@@ -93,7 +95,6 @@ __global__ void csfac_kernel(const double *__restrict__ x, int nk, double *__res
         invd[i] = 1.0 / d;
         dprev = d;
     }
-    // float copies for the mixed path: [1/diag', w, 1/h, h]
     for (int i = 0; i < nk; ++i) {
         fac32[i] = i < m ? (float)invd[i] : 0.f;
         fac32[nk + i] = i < m ? (float)w[i] : 0.f;
@@ -812,20 +813,28 @@ template <bool SWZ> __device__ __forceinline__ int slot32(int i)
     return i ^ ((x ^ (x << 3) ^ (x >> 4)) & 15);
 }
 
-// In-place DIT FFT of M = 2^logM complex floats (bit-reversed input): radix-4
-// butterflies, after one radix-2 stage when logM is odd; tw[j] = exp(-2 pi i
-// j / (2M)), j <= M; sign +1 (backward) conjugates the twiddles.
-template <bool SWZ>
-__device__ void smem_fft_f32(float2 *buf, int logM, const float2 *__restrict__ tw, int sign)
+// In-place DIT FFTs of `nact` <= G sequences of M = 2^logM complex floats
+// (bit-reversed input) at buf + j M: radix-4 butterflies, after one radix-2
+// stage when logM is odd; tw[j] = exp(-2 pi i j / (2M)), j <= M; sign +1
+// (backward) conjugates the twiddles.  The G transforms share each twiddle
+// load and give every thread G independent butterflies between barriers.
+template <bool SWZ, int G>
+__device__ void smem_fft_f32(float2 *buf, int logM, int nact, const float2 *__restrict__ tw,
+                             int sign)
 {
     const int M = 1 << logM;
     int st = 1;
     if (logM & 1) {
         for (int b = threadIdx.x; b < M / 2; b += blockDim.x) {
             const int p0 = slot32<SWZ>(2 * b), p1 = slot32<SWZ>(2 * b + 1);
-            const float2 u = buf[p0], v = buf[p1];
-            buf[p0] = c32_add(u, v);
-            buf[p1] = c32_sub(u, v);
+#pragma unroll
+            for (int j = 0; j < G; ++j) {
+                if (j >= nact) break;
+                float2 *bj = buf + j * M;
+                const float2 u = bj[p0], v = bj[p1];
+                bj[p0] = c32_add(u, v);
+                bj[p1] = c32_sub(u, v);
+            }
         }
         __syncthreads();
         st = 2;
@@ -838,29 +847,38 @@ __device__ void smem_fft_f32(float2 *buf, int logM, const float2 *__restrict__ t
             const int i0 = ((b >> (st - 1)) << (st + 1)) + pos;
             const int p0 = slot32<SWZ>(i0), p1 = slot32<SWZ>(i0 + half);
             const int p2 = slot32<SWZ>(i0 + 2 * half), p3 = slot32<SWZ>(i0 + 3 * half);
-            const float2 x0 = buf[p0];
-            float2 x1 = buf[p1], x2 = buf[p2], x3 = buf[p3];
+            float2 w1 = make_float2(1.f, 0.f), w2 = w1, w3 = w1;
             if (half > 1) {
-                const int j = pos * step, j3 = 3 * j;
-                float2 w1 = tw[2 * j], w2 = tw[j];
-                float2 w3 = j3 <= M ? tw[j3] : make_float2(-tw[j3 - M].x, -tw[j3 - M].y);
+                const int jj = pos * step, j3 = 3 * jj;
+                w1 = tw[2 * jj];
+                w2 = tw[jj];
+                w3 = j3 <= M ? tw[j3] : make_float2(-tw[j3 - M].x, -tw[j3 - M].y);
                 if (sign > 0) {
                     w1 = c32_conj(w1);
                     w2 = c32_conj(w2);
                     w3 = c32_conj(w3);
                 }
-                x1 = c32_mul(x1, w1);
-                x2 = c32_mul(x2, w2);
-                x3 = c32_mul(x3, w3);
             }
-            const float2 t0 = c32_add(x0, x1), t1 = c32_sub(x0, x1);
-            const float2 t2 = c32_add(x2, x3), t3 = c32_sub(x2, x3);
-            // w_{4 half}^half = -i forward, +i backward
-            const float2 r = sign < 0 ? make_float2(t3.y, -t3.x) : make_float2(-t3.y, t3.x);
-            buf[p0] = c32_add(t0, t2);
-            buf[p1] = c32_add(t1, r);
-            buf[p2] = c32_sub(t0, t2);
-            buf[p3] = c32_sub(t1, r);
+#pragma unroll
+            for (int j = 0; j < G; ++j) {
+                if (j >= nact) break;
+                float2 *bj = buf + j * M;
+                const float2 x0 = bj[p0];
+                float2 x1 = bj[p1], x2 = bj[p2], x3 = bj[p3];
+                if (half > 1) {
+                    x1 = c32_mul(x1, w1);
+                    x2 = c32_mul(x2, w2);
+                    x3 = c32_mul(x3, w3);
+                }
+                const float2 t0 = c32_add(x0, x1), t1 = c32_sub(x0, x1);
+                const float2 t2 = c32_add(x2, x3), t3 = c32_sub(x2, x3);
+                // w_{4 half}^half = -i forward, +i backward
+                const float2 r = sign < 0 ? make_float2(t3.y, -t3.x) : make_float2(-t3.y, t3.x);
+                bj[p0] = c32_add(t0, t2);
+                bj[p1] = c32_add(t1, r);
+                bj[p2] = c32_sub(t0, t2);
+                bj[p3] = c32_sub(t1, r);
+            }
         }
         __syncthreads();
     }
@@ -876,46 +894,69 @@ __device__ __forceinline__ float2 c2r_pre32(float2 xa, float2 xb, float2 w)
     return make_float2(fe.x - fo.y, fe.y + fo.x);
 }
 
-template <bool SWZ>
+// Up to G inverse transforms of one spectrum that share their forward half
+// spectrum (terms with the same q): block (s, g) makes the tables of the
+// terms group[g] = (q, t0, t1, t2) (-1: unused) of spectrum s.  The half
+// spectrum is read once for the G products with the terms' kernels.
+// fill_small != 0 also writes NaN into the 43 entries before the FFTLog part
+// (r = 0 and the sub-Mpc points, not computed).
+template <bool SWZ, int G>
 __global__ void fftlog_inverse_f32_kernel(GridPar g, const float2 *__restrict__ spec,
-                                          const int *__restrict__ term_q, int n_q, int n_terms,
+                                          const int4 *__restrict__ groups, int n_q, int n_terms,
                                           const float2 *__restrict__ mcoef32,
                                           const float *__restrict__ postf32,
                                           const float2 *__restrict__ tw32,
-                                          float *__restrict__ tab, int *err)
+                                          float *__restrict__ tab, int fill_small, int *err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *buf = reinterpret_cast<float2 *>(smem_raw);
-    const int s = blockIdx.x, t = blockIdx.y;
+    const int s = blockIdx.x;
+    const int4 gr = groups[blockIdx.y];
+    const int ts[3] = {gr.y, gr.z, gr.w};
+    const int nact = ts[0] < 0 ? 0 : (ts[1] < 0 ? 1 : (ts[2] < 0 ? 2 : 3));
     const int N = g.N, M = N / 2;
     const int logM = 31 - __clz(M);
-    const float2 *in = spec + ((size_t)s * n_q + term_q[t]) * (M + 1);
-    const float2 *mc = mcoef32 + (size_t)t * (M + 1);
+    const float2 *in = spec + ((size_t)s * n_q + gr.x) * (M + 1);
     // z_k = Fe_k + i Fo_k from X_k and conj(X_{M-k}), X = spectrum x kernel;
-    // one thread makes z_k and z_{M-k} from the same two products
+    // one thread makes z_k and z_{M-k} of every term from the same two loads
     for (int k = threadIdx.x; k <= M / 2; k += blockDim.x) {
         const int km = M - k;
-        float2 xa = c32_mul(in[k], mc[k]);
-        float2 xb = c32_mul(in[km], mc[km]);
-        if (k == 0) {
-            xa.y = 0.f;
-            xb.y = 0.f;
+        const float2 ik = in[k], ikm = in[km], wk = tw32[k], wkm = tw32[km];
+        const int pk = slot32<SWZ>(__brev((unsigned)k) >> (32 - logM));
+        const int pkm = slot32<SWZ>(__brev((unsigned)km) >> (32 - logM));
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+            if (j >= nact) break;
+            const float2 *mc = mcoef32 + (size_t)ts[j] * (M + 1);
+            float2 xa = c32_mul(ik, mc[k]);
+            float2 xb = c32_mul(ikm, mc[km]);
+            if (k == 0) {
+                xa.y = 0.f;
+                xb.y = 0.f;
+            }
+            buf[j * M + pk] = c2r_pre32(xa, xb, wk);
+            if (k > 0 && k < M / 2) buf[j * M + pkm] = c2r_pre32(xb, xa, wkm);
         }
-        buf[slot32<SWZ>(__brev((unsigned)k) >> (32 - logM))] = c2r_pre32(xa, xb, tw32[k]);
-        if (k > 0 && k < M / 2)
-            buf[slot32<SWZ>(__brev((unsigned)km) >> (32 - logM))] = c2r_pre32(xb, xa, tw32[km]);
     }
     __syncthreads();
-    smem_fft_f32<SWZ>(buf, logM, tw32, +1);
+    smem_fft_f32<SWZ, G>(buf, logM, nact, tw32, +1);
     const size_t len = (size_t)N + CG_N_SMALL_R + 1;
-    float *o = tab + ((size_t)s * n_terms + t) * len + CG_N_SMALL_R + 1;
-    const float *pf = postf32 + (size_t)t * N;
     bool bad = false;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        const float2 z = buf[slot32<SWZ>(i >> 1)];
-        const float v = ((i & 1) ? z.y : z.x) * pf[i];
-        if (!isfinite(v)) bad = true;
-        o[i] = v;
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+        if (j >= nact) break;
+        float *o = tab + ((size_t)s * n_terms + ts[j]) * len + CG_N_SMALL_R + 1;
+        const float *pf = postf32 + (size_t)ts[j] * N;
+        const float2 *bj = buf + j * M;
+        if (fill_small && threadIdx.x <= CG_N_SMALL_R)
+            o[(int)threadIdx.x - CG_N_SMALL_R - 1] = cg_nan<float>();
+#pragma unroll 4
+        for (int i = threadIdx.x; i < N; i += blockDim.x) {
+            const float2 z = bj[slot32<SWZ>(i >> 1)];
+            const float v = ((i & 1) ? z.y : z.x) * pf[i];
+            if (!isfinite(v)) bad = true;
+            o[i] = v;
+        }
     }
     if (bad) cg_flag(err, CG_ERR_NONFINITE);
 }
@@ -1292,7 +1333,24 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     struct TermMeta {
         double q[CG_MAX_TERMS], l[CG_MAX_TERMS], n[CG_MAX_TERMS], qv[CG_MAX_TERMS];
         int tq[CG_MAX_TERMS], tn[CG_MAX_TERMS], tl[CG_MAX_TERMS];
+        int4 grp[CG_MAX_TERMS]; // FP32 inverse transforms: (q, up to 3 terms of that q)
     } meta;
+    // terms sharing a forward spectrum go through the FP32 inverse kernel
+    // together, inv_g of them per block (one per block when three do not fit
+    // the shared memory twice over)
+    const int inv_g = 3 * sizeof(float2) * (size_t)M <= 112 * 1024 ? 3 : 1;
+    int n_grp = 0;
+    for (int q = 0; q < (int)qvals.size(); ++q) {
+        int cur[3] = {-1, -1, -1}, nc = 0;
+        for (int t = 0; t <= n_terms; ++t) {
+            if (t < n_terms && term_q[t] == q) cur[nc++] = t;
+            if (nc == inv_g || (t == n_terms && nc > 0)) {
+                meta.grp[n_grp++] = make_int4(q, cur[0], cur[1], cur[2]);
+                cur[0] = cur[1] = cur[2] = -1;
+                nc = 0;
+            }
+        }
+    }
     for (int t = 0; t < n_terms; ++t) {
         meta.q[t] = tq[t];
         meta.l[t] = tl[t];
@@ -1336,17 +1394,22 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
                                      ctx->stream));
         CG_CUDA(ctx, cudaMemcpyAsync(ctx->tab_x32.p, hx32, sizeof(hx32), cudaMemcpyHostToDevice,
                                      ctx->stream));
-        csfac_kernel<<<1, 1, 0, ctx->stream>>>((const double *)ctx->kgrid.p, (int)nk,
-                                               (double *)ctx->csfac.p, (float *)ctx->csfac32.p);
-        if ((st = cg_after_launch(ctx, "csfac_kernel"))) return st;
-        {
-            std::vector<float> band;
-            cspline_band_host(std::vector<double>(k, k + nk), band);
-            if ((st = cg_ensure(ctx, ctx->csband, sizeof(float) * band.size()))) return st;
-            CG_CUDA(ctx, cudaMemcpyAsync(ctx->csband.p, band.data(), sizeof(float) * band.size(),
-                                         cudaMemcpyHostToDevice, ctx->stream));
-            CG_CUDA(ctx, cudaStreamSynchronize(ctx->stream)); // band is a host temporary
-        }
+        // spline factors and the band of the inverse spline matrix, computed
+        // on the host; the host arrays live in the context, so the copies need
+        // no synchronisation for their sake
+        csfac_host(k, (int)nk, ctx->grid_fac_host, ctx->grid_fac32_host);
+        cspline_band_host(std::vector<double>(k, k + nk), ctx->grid_band_host);
+        if ((st = cg_ensure(ctx, ctx->csband, sizeof(float) * ctx->grid_band_host.size())))
+            return st;
+        CG_CUDA(ctx, cudaMemcpyAsync(ctx->csfac.p, ctx->grid_fac_host.data(),
+                                     sizeof(double) * ctx->grid_fac_host.size(),
+                                     cudaMemcpyHostToDevice, ctx->stream));
+        CG_CUDA(ctx, cudaMemcpyAsync(ctx->csfac32.p, ctx->grid_fac32_host.data(),
+                                     sizeof(float) * ctx->grid_fac32_host.size(),
+                                     cudaMemcpyHostToDevice, ctx->stream));
+        CG_CUDA(ctx, cudaMemcpyAsync(ctx->csband.p, ctx->grid_band_host.data(),
+                                     sizeof(float) * ctx->grid_band_host.size(),
+                                     cudaMemcpyHostToDevice, ctx->stream));
         const int tb = 256;
         sampling_kernel<<<((int)N + tb) / tb, tb, 0, ctx->stream>>>(
             g, (const double *)ctx->kgrid.p, (int *)ctx->samp_idx.p, (double *)ctx->samp_dx.p,
@@ -1375,8 +1438,10 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     // per spectrum: natural-spline coefficients, forward FFTs, inverse FFTs
     if (mixed && (st = cg_ensure(ctx, ctx->pk_df, sizeof(float2) * nk * n_spectra))) return st;
     const size_t smem = sizeof(double2) * M; // == sizeof(float4) * M
-    const size_t smem32 = sizeof(float2) * M;
-    const dim3 gf(n_spectra, n_q), gi(n_spectra, n_terms);
+    const size_t smem32 = sizeof(float2) * M * (size_t)inv_g;
+    const dim3 gf(n_spectra, n_q), gi(n_spectra, n_terms), gg(n_spectra, n_grp);
+    // the FP32 inverse kernel fills the 43 uncomputed entries itself
+    const int fill_small = (flags & COFFE_GPU_SMALL_R) ? 0 : 1;
     auto stage = [&](const coffe_gpu_tuning_t &tu) -> int {
         int s2;
         if (mixed) {
@@ -1417,18 +1482,28 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
             CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_forward_df_kernel<R, W, float2>,             \
                                               cudaFuncAttributeMaxDynamicSharedMemorySize,        \
                                               (int)smem));                                        \
-            CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_f32_kernel<W>,                       \
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize,        \
-                                              (int)smem32));                                      \
+            if (inv_g == 3)                                                                       \
+                CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_f32_kernel<W, 3>,                \
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                                                  (int)smem32));                                  \
+            else                                                                                  \
+                CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_inverse_f32_kernel<W, 1>,                \
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                                                  (int)smem32));                                  \
             fftlog_forward_df_kernel<R, W, float2><<<gf, tu.fft_threads_fwd, smem, ctx->stream>>>( \
                 g, (const float2 *)ctx->pk_df.p, (const float *)ctx->csc.p,                       \
                 (const int *)ctx->samp_idx.p, (const float2 *)ctx->samp_tdf.p,                    \
                 (const float4 *)ctx->samp_f32.p, (const float2 *)ctx->qfac_df.p, wdf,             \
                 (const float4 *)ctx->twid32.p, n_q, (float2 *)ctx->spec.p, ctx->d_err);           \
             if ((s2 = cg_after_launch(ctx, "fftlog_forward_df_kernel"))) return s2;               \
-            fftlog_inverse_f32_kernel<W><<<gi, tu.fft_threads, smem32, ctx->stream>>>(            \
-                g, (const float2 *)ctx->spec.p, d_meta->tq, n_q, n_terms, m32, p32, tw32,         \
-                (float *)ctx->tab_y.p, ctx->d_err);                                               \
+            if (inv_g == 3)                                                                       \
+                fftlog_inverse_f32_kernel<W, 3><<<gg, tu.fft_threads, smem32, ctx->stream>>>(     \
+                    g, (const float2 *)ctx->spec.p, d_meta->grp, n_q, n_terms, m32, p32, tw32,    \
+                    (float *)ctx->tab_y.p, fill_small, ctx->d_err);                               \
+            else                                                                                  \
+                fftlog_inverse_f32_kernel<W, 1><<<gg, tu.fft_threads, smem32, ctx->stream>>>(     \
+                    g, (const float2 *)ctx->spec.p, d_meta->grp, n_q, n_terms, m32, p32, tw32,    \
+                    (float *)ctx->tab_y.p, fill_small, ctx->d_err);                               \
             if ((s2 = cg_after_launch(ctx, "fftlog_inverse_f32_kernel"))) return s2;              \
         }                                                                                         \
     }
@@ -1509,7 +1584,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
                 n_terms, d_meta->tn, d_meta->tl, (const double *)ctx->tab_x.p, len,
                 (double *)ctx->tab_y.p, ctx->d_err);
         if ((st = cg_after_launch(ctx, "small_r_kernel"))) return st;
-    } else {
+    } else if (!mixed || tables_df) {
         const long items = tables * (CG_N_SMALL_R + 1);
         if (mixed)
             fill_nan_kernel<float><<<(int)((items + 255) / 256), 256, 0, ctx->stream>>>(

@@ -16,7 +16,13 @@
 #include <omp.h>
 #endif
 
-#include "gk61_table.h"
+/* the 61-point Gauss-Kronrod rule, generated from its definition at 60 digits
+   by coffe_gb300/csrc/gen_gk61.py (one table for the library and the oracle;
+   the oracle is pinned against the reference's golden vectors independently) */
+#include "../coffe_gb300/csrc/gk61_table.h"
+static const double OR_GK61_XGK[31] = CG_GK61_XGK_INIT;
+static const double OR_GK61_WGK[31] = CG_GK61_WGK_INIT;
+static const double OR_GK61_WG[15] = CG_GK61_WG_INIT;
 
 #ifndef M_PI
 #define M_PI 3.14159265358979323846
@@ -910,7 +916,6 @@ int or_integral_table(const double *k, const double *pk, size_t nk, int n, int l
 
 #define OR_XINT_BINS 16384
 #define OR_XINT_ZMAX 100.0
-#define OR_ODE_HMAX 1e-3
 
 typedef struct {
     double om; /* Omega0_cdm + Omega0_baryon */
@@ -944,19 +949,29 @@ static void growth_rhs(const or_bgpar_t *p, double a, const double y[2], double 
     f[1] = -3. / 2 * (1 - w / (1 + x)) * y[1] / a + 3. / 2 * x / (1 + x) * y[0] / (a * a);
 }
 
-static void growth_integrate(const or_bgpar_t *p, double a_end, double y[2])
+/* The growth ODE from a = 0.05, (D, D') = (0.05, 1) (background.c:430-481):
+   one trajectory of OR_ODE_STEPS classical RK4 steps of 1e-3 in a up to a = 1,
+   stored as (D, D', dD/da, dD'/da) per step point, and read at each node by
+   cubic Hermite interpolation between the two steps around it.  (The
+   reference integrates every node separately with GSL's adaptive rk2; this
+   restatement agrees with it to that solver's tolerance.) */
+#define OR_ODE_A0 0.05
+#define OR_ODE_STEPS 950
+
+static void growth_trajectory(const or_bgpar_t *p, double (*tr)[4])
 {
-    const double a0 = 0.05;
-    y[0] = 0.05;
-    y[1] = 1.0;
-    if (!(a_end > a0))
-        return;
-    const size_t nstep = (size_t)ceil((a_end - a0) / OR_ODE_HMAX);
-    const double h = (a_end - a0) / (double)nstep;
-    for (size_t s = 0; s < nstep; ++s) {
-        const double a = a0 + h * (double)s;
+    const double h = (1.0 - OR_ODE_A0) / OR_ODE_STEPS;
+    double y[2] = {0.05, 1.0};
+    for (int s = 0; s <= OR_ODE_STEPS; ++s) {
+        const double a = OR_ODE_A0 + h * (double)s;
         double k1[2], k2[2], k3[2], k4[2], t[2];
         growth_rhs(p, a, y, k1);
+        tr[s][0] = y[0];
+        tr[s][1] = y[1];
+        tr[s][2] = k1[0];
+        tr[s][3] = k1[1];
+        if (s == OR_ODE_STEPS)
+            break;
         t[0] = y[0] + 0.5 * h * k1[0];
         t[1] = y[1] + 0.5 * h * k1[1];
         growth_rhs(p, a + 0.5 * h, t, k2);
@@ -969,6 +984,23 @@ static void growth_integrate(const or_bgpar_t *p, double a_end, double y[2])
         y[0] += h / 6.0 * (k1[0] + 2.0 * k2[0] + 2.0 * k3[0] + k4[0]);
         y[1] += h / 6.0 * (k1[1] + 2.0 * k2[1] + 2.0 * k3[1] + k4[1]);
     }
+}
+
+static void growth_at(double (*tr)[4], double ai, double y[2])
+{
+    const double h = (1.0 - OR_ODE_A0) / OR_ODE_STEPS;
+    int s = (int)floor((ai - OR_ODE_A0) / h);
+    if (s < 0)
+        s = 0;
+    if (s > OR_ODE_STEPS - 1)
+        s = OR_ODE_STEPS - 1;
+    const double t = (ai - (OR_ODE_A0 + h * (double)s)) / h;
+    const double t2 = t * t, t3 = t2 * t;
+    const double h00 = 2 * t3 - 3 * t2 + 1, h10 = t3 - 2 * t2 + t, h01 = -2 * t3 + 3 * t2,
+                 h11 = t3 - t2;
+    for (int c = 0; c < 2; ++c)
+        y[c] = h00 * tr[s][c] + h10 * h * tr[s][2 + c] + h01 * tr[s + 1][c] +
+               h11 * h * tr[s + 1][2 + c];
 }
 
 static double comoving_integrand(double z, void *vp)
@@ -990,13 +1022,15 @@ int or_background_nodes(const or_cosmo_t *c, size_t bins, double *z, double *a,
     p.ode = c->Omega0_de;
     double *Dtmp = (double *)malloc(sizeof(double) * bins);
     double *ftmp = (double *)malloc(sizeof(double) * bins);
+    double(*tr)[4] = (double(*)[4])malloc(sizeof(double) * 4 * (OR_ODE_STEPS + 1));
+    growth_trajectory(&p, tr);
 #pragma omp parallel for schedule(dynamic, 16)
     for (long li = 0; li < (long)bins; ++li) {
         const size_t i = (size_t)li;
         const double zi = 15. * i / (double)(bins - 1);
         const double ai = 1. / (1. + zi);
         double y[2];
-        growth_integrate(&p, ai, y);
+        growth_at(tr, ai, y);
         Dtmp[i] = y[0];
         ftmp[i] = y[1] * ai / y[0];
         const double Hi =
@@ -1028,6 +1062,7 @@ int or_background_nodes(const or_cosmo_t *c, size_t bins, double *z, double *a,
     }
     free(Dtmp);
     free(ftmp);
+    free(tr);
     return 0;
 }
 

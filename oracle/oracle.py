@@ -30,7 +30,7 @@ def build(force: bool = False) -> Path:
     """Compile the oracle with its Makefile (gcc + OpenMP)."""
     if force or not _LIB_PATH.exists() or any(
         (_HERE / f).stat().st_mtime > _LIB_PATH.stat().st_mtime
-        for f in ("coffe_oracle.c", "coffe_oracle.h", "gk61_table.h")
+        for f in ("coffe_oracle.c", "coffe_oracle.h", "../coffe_gb300/csrc/gk61_table.h")
     ):
         subprocess.run(["make", "-C", str(_HERE)], check=True, capture_output=True)
     return _LIB_PATH

@@ -82,9 +82,11 @@ def test_oracle_gk61_nodes():
     import importlib.util
     from pathlib import Path
 
-    src = (Path(__file__).resolve().parent.parent / "oracle" / "gk61_table.h").read_text()
-    vals = [float(t.strip().rstrip(",")) for t in src.split("{")[1].split("}")[0].split()
-            if t.strip().rstrip(",")]
+    src = (Path(__file__).resolve().parent.parent / "coffe_gb300" / "csrc" /
+           "gk61_table.h").read_text()
+    body = src.split("CG_GK61_XGK_INIT {")[1].split("}")[0]
+    vals = [float(t.strip().rstrip(",").rstrip("\\").strip().rstrip(","))
+            for t in body.replace("\\", " ").split() if t.strip().rstrip(",")]
     assert abs(vals[0] - 0.999484410050490637571325895705811) < 1e-16
 
 
