@@ -614,6 +614,45 @@ def config_baselines(torch, ctx, ev_time, extras_so_far):
     return res
 
 
+def gradient_batch(torch, ctx, stream, batch, pk_d, rs_d, rz_d, ro_d, sep_d, n_sep):
+    """The differentiable den+RSD multipoles of the whole batch (FP64 tables,
+    first-panel values) and their reverse-mode derivative with respect to all
+    512 spectra and every request's bias and growth scales: CUDA events on the
+    library's stream, best of three."""
+    dev = pk_d.device
+    ctx.integrals_init_device(batch.k, pk_d, TERMS, N=N_FFT, precision="fp64", sync=True)
+    out = torch.empty((n_sep, len(batch.ls)), dtype=torch.float64, device=dev)
+    G = torch.ones_like(out)
+    gpk = torch.empty_like(pk_d)
+    nq = len(batch.req_spectrum)
+    gb = torch.empty(nq, dtype=torch.float64, device=dev)
+    gf = torch.empty_like(gb)
+
+    def best(fn):
+        fn()
+        torch.cuda.synchronize()
+        t = None
+        for _ in range(3):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            fn()
+            e.record(stream)
+            e.synchronize()
+            t = s.elapsed_time(e) if t is None else min(t, s.elapsed_time(e))
+        return t
+
+    fwd = best(lambda: ctx.multipoles_scaled(rs_d, rz_d, ro_d, sep_d, n_sep, batch.ls, out))
+    rejected = ctx.last_retries()
+    adj = best(lambda: ctx.multipoles_adjoint(rs_d, rz_d, ro_d, sep_d, n_sep, batch.ls, G, gpk,
+                                              gb, gf))
+    return {"workload": "d(multipoles)/d(P(k) of 512 spectra, bias and growth scale of 3072 "
+                        "requests), den+RSD l=0,2,4, the config-3 batch (646,853 separations), "
+                        "FP64 adjoint; forward = the differentiable first-panel values",
+            "forward_ms": fwd, "adjoint_ms": adj, "outputs": n_sep * len(batch.ls),
+            "first_panels_rejected": rejected,
+            "finite": bool(torch.isfinite(gpk).all().item())}
+
+
 def ours(args, rank, world, local_rank):
     import torch
 
@@ -859,6 +898,8 @@ def ours(args, rank, world, local_rank):
     extra = None
     if not args.no_extras:
         extra = extras(torch, ctx, stream)
+        extra["gradient_cfg3"] = gradient_batch(torch, ctx, stream, batch, pk_d, rs_d, rz_d,
+                                                ro_d, sep_d, n_sep)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_mixed / args.steps,

@@ -10,7 +10,11 @@ reference, which has no derivatives).
 ``pk`` is a CUDA float64 tensor (n_spectra, nk) on the k grid ``k`` (1/Mpc);
 the request tensors follow :meth:`Context.multipoles_async`.  The value is the
 first-GK61-panel multipole (coffe_gpu_multipoles_scaled), equal to the
-adaptive result wherever the first panel meets the tolerance.
+adaptive result wherever the first panel meets the tolerance.  Where QUADPACK
+would reject a first panel (and refine it adaptively), the differentiable
+value is not the adaptive one: the forward raises :class:`FirstPanelRejected`
+unless ``allow_rejected=True`` (the value and gradient then stay the first
+panel's for those outputs).
 """
 from __future__ import annotations
 
@@ -20,9 +24,15 @@ from . import _lib
 from .api import DEN_RSD_TERMS, Context
 
 
+class FirstPanelRejected(RuntimeError):
+    """Some outputs' first GK61 panel misses the quadrature tolerance: the
+    adaptive multipole differs from the differentiable (first-panel) value."""
+
+
 class _Spec:
-    def __init__(self, engine: Context, k, req, ls, contrib, N):
+    def __init__(self, engine: Context, k, req, ls, contrib, N, allow_rejected=False):
         self.engine, self.k, self.req, self.ls, self.contrib, self.N = engine, k, req, ls, contrib, N
+        self.allow_rejected = allow_rejected
 
 
 class MultipolesFunction(torch.autograd.Function):
@@ -40,6 +50,12 @@ class MultipolesFunction(torch.autograd.Function):
                             bias_scale=bias_scale.detach().contiguous(),
                             growth_scale=growth_scale.detach().contiguous(),
                             contrib=spec.contrib)
+        rejected = e.last_retries()
+        if rejected > 0 and not spec.allow_rejected:
+            raise FirstPanelRejected(
+                f"{rejected} outputs' first GK61 panel misses the 1e-5 tolerance: their adaptive "
+                "multipole differs from the differentiable first-panel value (pass "
+                "allow_rejected=True to differentiate the first panel anyway)")
         fctx.spec = spec
         fctx.save_for_backward(pk, bias_scale, growth_scale)
         return out
@@ -66,7 +82,8 @@ class MultipolesFunction(torch.autograd.Function):
 
 
 def multipoles(engine: Context, k, pk, req_spectrum, req_z_mean, req_offset, sep, ls=(0, 2, 4),
-               bias_scale=None, growth_scale=None, contrib=_lib.DEN | _lib.RSD, N: int = 4096):
+               bias_scale=None, growth_scale=None, contrib=_lib.DEN | _lib.RSD, N: int = 4096,
+               allow_rejected: bool = False):
     """Differentiable batched den/RSD multipoles, shape (len(sep), len(ls))."""
     n_req = req_spectrum.numel()
     dev = pk.device
@@ -74,5 +91,6 @@ def multipoles(engine: Context, k, pk, req_spectrum, req_z_mean, req_offset, sep
         bias_scale = torch.ones(n_req, dtype=torch.float64, device=dev)
     if growth_scale is None:
         growth_scale = torch.ones(n_req, dtype=torch.float64, device=dev)
-    spec = _Spec(engine, k, (req_spectrum, req_z_mean, req_offset, sep), tuple(ls), contrib, N)
+    spec = _Spec(engine, k, (req_spectrum, req_z_mean, req_offset, sep), tuple(ls), contrib, N,
+                 allow_rejected)
     return MultipolesFunction.apply(pk, bias_scale, growth_scale, spec)

@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(ADJ_THREADS)
                     const double *__restrict__ bias_scale, const double *__restrict__ growth_scale,
                     const double *__restrict__ grad_out, double *__restrict__ value_out,
                     double *__restrict__ gY, double *__restrict__ g_bias,
-                    double *__restrict__ g_growth, int *err)
+                    double *__restrict__ g_growth, int *__restrict__ rejected, int *err)
 {
     const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (item >= total) return;
@@ -198,9 +198,14 @@ __global__ void __launch_bounds__(ADJ_THREADS)
         for (int j = 0; j < ADJ_MAX_L; ++j) J[k][j] = 0.0;
     const double chi_mean = spl_eval(bg.chi_of_z, zm);
     const bool den = a.contrib & COFFE_GPU_DEN, rsd = a.contrib & COFFE_GPU_RSD;
+    const double bb = beta * beta, bf = beta * alpha, ff = alpha * alpha;
+    // forward call: the integrand at each node for QUADPACK's acceptance test
+    // of this first panel (sums per multipole: Kronrod, Gauss, |f|)
+    double xiv[61], wkv[61], Kq[ADJ_MAX_L], Gq[ADJ_MAX_L], Aq[ADJ_MAX_L];
+    for (int j = 0; j < ADJ_MAX_L; ++j) Kq[j] = Gq[j] = Aq[j] = 0.0;
     for (int node = 0; node < 61; ++node) {
         const int p = node >> 1;
-        double x, wk;
+        double x, wk, wg = 0.0;
         if (node == 60) {
             x = 0.5;
             wk = cg_gk_wgk[30];
@@ -209,6 +214,7 @@ __global__ void __launch_bounds__(ADJ_THREADS)
             const double absc = 0.5 * cg_gk_xgk[g];
             x = (node & 1) ? 0.5 + absc : 0.5 - absc;
             wk = cg_gk_wgk[g];
+            wg = p < 15 ? cg_gk_wg[p] : 0.0;
         }
         const double mu = 2 * x - 1;
         const double chi1 = chi_mean - r * mu * 0.5, chi2 = chi_mean + r * mu * 0.5;
@@ -239,8 +245,47 @@ __global__ void __launch_bounds__(ADJ_THREADS)
             const double wp = wk * adj_legendre(a.ls[j], mu) * D;
             for (int k = 0; k < NKIND; ++k) J[k][j] += wp * co[k];
         }
+        if (value_out) {
+            const double xi = D * (I[0].v * (bb * co[K00BB] + bf * co[K00BF] + ff * co[K00FF]) +
+                                   I[1].v * (bf * co[K02BF] + ff * co[K02FF]) +
+                                   I[2].v * ff * co[K04FF]);
+            xiv[node] = xi;
+            wkv[node] = wk;
+            for (int j = 0; j < a.n_l; ++j) {
+                const double v = adj_legendre(a.ls[j], mu) * xi;
+                Kq[j] += wk * v;
+                Gq[j] += wg * v;
+                Aq[j] += wk * fabs(v);
+            }
+        }
     }
-    const double bb = beta * beta, bf = beta * alpha, ff = alpha * alpha;
+    if (value_out && rejected) {
+        // QUADPACK's test of the first panel (gsl qag.c) at the default
+        // relative tolerance 1e-5: outputs it rejects would go through the
+        // adaptive continuation in coffe_gpu_multipoles, so their first-panel
+        // value is counted for the caller
+        int nrej = 0;
+        for (int j = 0; j < a.n_l; ++j) {
+            double asc = 0.0;
+            for (int node = 0; node < 61; ++node) {
+                const int p = node >> 1;
+                double mu = 0.0;
+                if (node != 60) {
+                    const int g = p < 15 ? 2 * p + 1 : 2 * (p - 15);
+                    mu = (node & 1) ? cg_gk_xgk[g] : -cg_gk_xgk[g];
+                }
+                asc += wkv[node] * fabs(adj_legendre(a.ls[j], mu) * xiv[node] - 0.5 * Kq[j]);
+            }
+            const double result = 0.5 * Kq[j], resabs = 0.5 * Aq[j], resasc = 0.5 * asc;
+            const double abserr = qk_rescale_error(0.5 * (Kq[j] - Gq[j]), resabs, resasc);
+            const double tolerance = 1e-5 * fabs(result);
+            const double round_off = 50 * qk_eps<double>() * resabs;
+            const bool roundoff_fail = abserr <= round_off && abserr > tolerance;
+            const bool ok = (abserr <= tolerance && abserr != resasc) || abserr == 0.0;
+            if (!(ok || roundoff_fail)) ++nrej;
+        }
+        if (nrej) atomicAdd(rejected, nrej);
+    }
     double gI[3] = {0, 0, 0}, gb = 0, gg = 0;
     for (int j = 0; j < a.n_l; ++j) {
         const double sc = (2 * a.ls[j] + 1) * 0.5;
@@ -489,10 +534,18 @@ int multipoles_adjoint_run(coffe_gpu_ctx *ctx, int contrib, int n_req, const int
     }
     AdjBg bg{ctx->bg[BG_CHI_OF_Z].v64(), ctx->bg[BG_Z_OF_CHI].v64(), ctx->bg[BG_F].v64(),
              ctx->bg[BG_D1].v64(),       ctx->bias[0].v64(),        ctx->bias[1].v64()};
+    // forward calls count the outputs whose first panel QUADPACK would reject
+    // in the retry counter (coffe_gpu_multipoles_retries reads it)
+    int *rejected = nullptr;
+    if (value_out) {
+        if ((st = cg_ensure(ctx, ctx->mp_retry, 256))) return st;
+        rejected = (int *)ctx->mp_retry.p;
+        CG_CUDA(ctx, cudaMemsetAsync(rejected, 0, sizeof(int), ctx->stream));
+    }
     adj_pair_kernel<<<(unsigned)((total + ADJ_THREADS - 1) / ADJ_THREADS), ADJ_THREADS, 0, ctx->stream>>>(
         a, bg, (const double *)ctx->tab_x.p, (const double *)ctx->tab_y.p, req_spectrum, req_z_mean,
         req_offset, sep, total, bias_scale, growth_scale, grad_out, value_out, gY, grad_bias,
-        grad_growth, ctx->d_err);
+        grad_growth, rejected, ctx->d_err);
     if ((st = cg_after_launch(ctx, "adj_pair_kernel"))) return st;
     if (!grad_out || !grad_pk) return COFFE_GPU_OK;
     const double2 *mcoef = (const double2 *)ctx->modec.p;

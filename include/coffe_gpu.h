@@ -329,7 +329,8 @@ int coffe_gpu_corrfunc(coffe_gpu_ctx_t *ctx, int contrib, int precision, int n_r
 
 /* Number of (separation, multipole) outputs of the last multipoles call on
    this context whose first GK61 panel missed the tolerance and went through
-   the adaptive bisection (synchronises the context's stream); -1 if none ran.
+   the adaptive bisection (after coffe_gpu_multipoles_scaled: whose first
+   panel the test rejects; synchronises the context's stream); -1 if none ran.
    No counterpart in the reference (its QAG keeps this count internal). */
 long long coffe_gpu_multipoles_retries(coffe_gpu_ctx_t *ctx);
 
@@ -407,7 +408,11 @@ int coffe_gpu_set_tuning(coffe_gpu_ctx_t *ctx, const coffe_gpu_tuning_t *t);
    integrals (0,0), (0,2), (0,4)); separations >= the third FFTLog node above
    1 Mpc (the Akima stencil must stay on the FFTLog part of the tables).
    Every array is a device pointer except `l` (host, n_l entries); out as
-   coffe_gpu_multipoles: out[(req_offset[q] + j) * n_l + i]. */
+   coffe_gpu_multipoles: out[(req_offset[q] + j) * n_l + i].  The call applies
+   QUADPACK's acceptance test to each first panel (relative tolerance 1e-5,
+   the reference's default integration_1d_prec) and counts the outputs it
+   rejects -- there the adaptive result differs from this value -- in the
+   counter coffe_gpu_multipoles_retries reads. */
 int coffe_gpu_multipoles_scaled(coffe_gpu_ctx_t *ctx, int contrib, int n_req, int64_t n_sep,
                                 const int *req_spectrum, const double *req_z_mean,
                                 const int64_t *req_offset, const double *sep, int n_l,

@@ -168,3 +168,51 @@ def test_batched_gradients_per_spectrum(setup):
         print("spectrum", s, fd, ad)
         assert abs(fd - ad) <= 1e-6 * abs(fd)
     assert g_b.shape == (len(b.req_spectrum),) and np.all(np.isfinite(g_b)) and np.all(np.isfinite(g_f))
+
+
+def test_rejected_first_panels_are_counted_and_raise(setup):
+    """At a separation where the monopole crosses zero, QUADPACK rejects the
+    first panel (its tolerance, 1e-5 of a vanishing value, is below the
+    round-off floor): the differentiable forward counts that output as the
+    adaptive forward does, and the autograd surface refuses to differentiate a
+    value that is not the adaptive one unless told to."""
+    torch, ctx, c, req, pk = setup
+    from coffe_gb300.autograd import FirstPanelRejected, multipoles
+
+    ctx.integrals_init(c["k"], c["pk"][None, :], [(0, 0), (0, 2), (0, 4)], N=4096,
+                       precision="fp64", small_r=False)
+
+    def mono(r):
+        return ctx.multipoles([0], [1.0], [0, len(r)], r, (0,), precision="fp64")[:, 0]
+
+    r = np.linspace(60, 140, 161) / H
+    v = mono(r)
+    i = np.where(np.sign(v[:-1]) != np.sign(v[1:]))[0][0]
+    a, b = r[i], r[i + 1]
+    fa = v[i]
+    for _ in range(60):  # bisection to the double-precision zero crossing
+        m = 0.5 * (a + b)
+        fm = mono(np.array([m]))[0]
+        if np.sign(fm) == np.sign(fa):
+            a, fa = m, fm
+        else:
+            b = m
+    seps = np.array([a, 100 / H, b])
+    ctx.multipoles([0], [1.0], [0, 3], seps, (0, 2, 4), precision="fp64")
+    n_adaptive = ctx.last_retries()
+    assert n_adaptive >= 1
+    dev = "cuda:0"
+    rq = (torch.tensor([0], dtype=torch.int32, device=dev),
+          torch.tensor([1.0], dtype=torch.float64, device=dev),
+          torch.tensor([0, 3], dtype=torch.int64, device=dev),
+          torch.tensor(seps, dtype=torch.float64, device=dev))
+    out = torch.empty((3, 3), dtype=torch.float64, device=dev)
+    ctx.integrals_init_device(c["k"], pk, N=4096, precision="fp64")
+    ctx.multipoles_scaled(*rq, 3, (0, 2, 4), out)
+    assert ctx.last_retries() == n_adaptive
+    p = pk.clone().requires_grad_(True)
+    with pytest.raises(FirstPanelRejected):
+        multipoles(ctx, c["k"], p, *rq, (0, 2, 4))
+    mp = multipoles(ctx, c["k"], p, *rq, (0, 2, 4), allow_rejected=True)
+    mp.sum().backward()
+    assert torch.isfinite(p.grad).all()
