@@ -102,6 +102,8 @@ class Tuning(C.Structure):
         ("lane_threads", C.c_int),
         ("lane_unroll", C.c_int),
         ("fft_threads_fwd", C.c_int),
+        ("lane_pack", C.c_int),
+        ("fft_fused", C.c_int),
     ]
 
 

@@ -512,10 +512,11 @@ int coffe_gpu_set_tuning(coffe_gpu_ctx_t *ctx, const coffe_gpu_tuning_t *t)
         !(ff == 128 || ff == 256 || ff == 512 || ff == 1024) ||
         !(t->fft_radix == 2 || t->fft_radix == 4) || !(t->fft_swizzle == 0 || t->fft_swizzle == 1) ||
         !(g == 2 || g == 4 || g == 8) || !(lt == 64 || lt == 128 || lt == 256) ||
-        !(t->lane_unroll == 1 || t->lane_unroll == 2)) {
+        !(t->lane_unroll == 1 || t->lane_unroll == 2) ||
+        !(t->lane_pack == 1 || t->lane_pack == 2) || !(t->fft_fused == 0 || t->fft_fused == 1)) {
         cg_set_error(ctx, "set_tuning: fft_threads(_fwd) 128/256/512/1024, fft_radix 2/4, "
                           "fft_swizzle 0/1, spline_group 2/4/8, lane_threads 64/128/256, "
-                          "lane_unroll 1/2");
+                          "lane_unroll 1/2, lane_pack 1/2, fft_fused 0/1");
         return COFFE_GPU_EINVAL;
     }
     ctx->tuning = *t;

@@ -68,8 +68,8 @@ struct coffe_gpu_ctx {
     int n_spectra = 0, n_terms = 0, int_precision = 0;
 
     // ---- launch shapes (coffe_gpu_set_tuning / benchmark-mode autotuning)
-    coffe_gpu_tuning_t tuning = {512, 4, 1, 8, 128, 2, 512}; // default configuration
-    coffe_gpu_tuning_t last_tuning = {512, 4, 1, 8, 128, 2, 512};
+    coffe_gpu_tuning_t tuning = {512, 4, 1, 8, 128, 2, 512, 1, 1}; // default configuration
+    coffe_gpu_tuning_t last_tuning = {512, 4, 1, 8, 128, 2, 512, 1, 1};
     bool autotune = false;
     std::map<std::array<long long, 6>, coffe_gpu_tuning_t> tune_cache; // shape -> choice
     size_t N = 0, nk = 0;

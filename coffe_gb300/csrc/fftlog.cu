@@ -961,6 +961,171 @@ __global__ void fftlog_inverse_f32_kernel(GridPar g, const float2 *__restrict__ 
     if (bad) cg_flag(err, CG_ERR_NONFINITE);
 }
 
+// ---- mixed path, the whole table stage of one spectrum in one block
+//
+// The three kernels above (spline band product, double-float forward
+// transform, FP32 inverse transforms) each wait on global memory between
+// short bursts of work (their top stall: loads from L2/HBM), and pass their
+// results through global memory.  Here one block per (spectrum, q) keeps
+// everything in shared memory: the spectrum's double-float knots, its spline
+// coefficients, the forward transform, the half spectrum and the inverse
+// transforms of every term of that q, writing only the tables.  Same
+// arithmetic as the separate kernels, so the same results.
+//
+// Shared memory (bytes; nk >= N/2 + 1 is required):
+//   phase 1: knots (hi, lo) [0, 8 nk) | spline c [FUS_C, +4 nk) |
+//            forward buffer [FUS_F, +16 M) (the spline right-hand sides
+//            live there before the sampling)
+//   phase 2: half spectrum [0, 8 (M + 1)) | inverse buffers [FUS_I, +8 G M)
+struct FusedLayout {
+    size_t c, f, i, total;
+};
+__host__ __device__ inline FusedLayout fused_layout(int nk, int M, int G)
+{
+    auto up = [](size_t x) { return (x + 15) & ~(size_t)15; };
+    FusedLayout l;
+    l.c = up(sizeof(float2) * (size_t)nk);
+    l.f = up(l.c + sizeof(float) * (size_t)nk);
+    l.i = up(sizeof(float2) * (size_t)(M + 1));
+    const size_t t1 = l.f + sizeof(float4) * (size_t)M;
+    const size_t t2 = l.i + sizeof(float2) * (size_t)M * G;
+    l.total = t1 > t2 ? t1 : t2;
+    return l;
+}
+
+#define FUSED_THREADS 512
+template <int RADIX, bool SWZ, int G>
+__global__ void __launch_bounds__(FUSED_THREADS)
+    fftlog_tables_fused_kernel(GridPar g, const double *__restrict__ pk,
+                               const float *__restrict__ band_t, const float *__restrict__ fac32,
+                               const int *__restrict__ idx, const float2 *__restrict__ tdf,
+                               const float4 *__restrict__ sf32, const float2 *__restrict__ qfac_df,
+                               const float2 *__restrict__ modew_df,
+                               const float4 *__restrict__ twdf, const int4 *__restrict__ groups,
+                               int n_grp, int n_terms, const float2 *__restrict__ mcoef32,
+                               const float *__restrict__ postf32, const float2 *__restrict__ tw32,
+                               float *__restrict__ tab, int fill_small, int *err)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int s = blockIdx.x, qi = blockIdx.y;
+    const int N = g.N, M = N / 2, nk = g.nk, m = nk - 2;
+    const int logM = 31 - __clz(M);
+    const int sh = logM > 6 ? logM - 6 : 0;
+    const FusedLayout L = fused_layout(nk, M, G);
+    float2 *ydf = reinterpret_cast<float2 *>(smem_raw);
+    float *cs = reinterpret_cast<float *>(smem_raw + L.c);
+    float4 *fbuf = reinterpret_cast<float4 *>(smem_raw + L.f);
+    float2 *fbuf2 = reinterpret_cast<float2 *>(smem_raw + L.f);
+    float *rhs = reinterpret_cast<float *>(smem_raw + L.f);
+    const int tid = threadIdx.x, bd = blockDim.x;
+    // knots as (hi, lo) pairs, split with integer operations
+    const double *p = pk + (size_t)s * nk;
+    for (int i = tid; i < nk; i += bd) {
+        const dfl d = df_from_double_bits(p[i]);
+        ydf[i] = make_float2(d.hi, d.lo);
+    }
+    __syncthreads();
+    // natural-spline right-hand sides (float, from the high parts), padded by
+    // CS_BAND zeros on both sides
+    const float *gi = fac32 + 2 * nk;
+    for (int t = tid; t < m + 2 * CS_BAND; t += bd) {
+        const int j = t - CS_BAND;
+        float v = 0.f;
+        if (j >= 0 && j < m) {
+            const float ya = ydf[j].x, yb = ydf[j + 1].x, yc = ydf[j + 2].x;
+            v = 3.f * ((yc - yb) * __ldg(gi + j + 1) - (yb - ya) * __ldg(gi + j));
+        }
+        rhs[t] = v;
+    }
+    __syncthreads();
+    // spline coefficients: the band of the inverse spline matrix times the
+    // right-hand sides (cspline_band_kernel's product)
+    for (int i = tid; i < m; i += bd) {
+        float acc = 0.f;
+#pragma unroll
+        for (int d = 0; d <= 2 * CS_BAND; ++d)
+            acc = fmaf(__ldg(band_t + (size_t)d * m + i), rhs[i + d], acc);
+        cs[i + 1] = acc;
+    }
+    if (tid == 0) {
+        cs[0] = 0.f;
+        cs[nk - 1] = 0.f;
+    }
+    __syncthreads();
+    // forward transform input (double-float sampling), bit-reversed
+    bool bad = false;
+    for (int i = tid; i < N; i += bd) {
+        const dfl d = sample_input_df(ydf, cs, idx, tdf, sf32, qfac_df + (size_t)qi * N, i);
+        if (!isfinite(d.hi)) bad = true;
+        const int jj = fft_slot<SWZ>(__brev((unsigned)(i >> 1)) >> (32 - logM), sh);
+        fbuf2[2 * jj + (i & 1)] = make_float2(d.hi, d.lo);
+    }
+    __syncthreads();
+    smem_fft_df<RADIX, SWZ>(fbuf, logM, twdf, -1);
+    // half spectrum, rounded to float (phase 2 starts: the knots are dead)
+    float2 *spec = reinterpret_cast<float2 *>(smem_raw);
+    for (int k = tid; k <= M; k += bd) {
+        const dfc zk = dfc_load(fbuf[fft_slot<SWZ>(k & (M - 1), sh)]);
+        const dfc zm = dfc_conj(dfc_load(fbuf[fft_slot<SWZ>((M - k) & (M - 1), sh)]));
+        const dfc e = dfc_add(zk, zm);
+        const dfc dd = dfc_sub(zk, zm);
+        const dfc o = dfc{dd.im, df_neg(dd.re)};
+        const dfc yk = dfc_add(e, dfc_mul(dfc_load(twdf[k]), o));
+        const float2 mw = modew_df[k];
+        const dfl mm = df_scale(dfl{mw.x, mw.y}, 0.5f);
+        const dfl re = df_mul(yk.re, mm), im = df_mul(yk.im, mm);
+        spec[k] = make_float2(re.hi + re.lo, -(im.hi + im.lo));
+    }
+    __syncthreads();
+    // the inverse transforms of this q's terms, G at a time
+    float2 *buf = reinterpret_cast<float2 *>(smem_raw + L.i);
+    const size_t len = (size_t)N + CG_N_SMALL_R + 1;
+    for (int gi2 = 0; gi2 < n_grp; ++gi2) {
+        const int4 gr = groups[gi2];
+        if (gr.x != qi) continue;
+        const int ts[3] = {gr.y, gr.z, gr.w};
+        const int nact = ts[0] < 0 ? 0 : (ts[1] < 0 ? 1 : (ts[2] < 0 ? 2 : 3));
+        for (int k = tid; k <= M / 2; k += bd) {
+            const int km = M - k;
+            const float2 ik = spec[k], ikm = spec[km], wk = tw32[k], wkm = tw32[km];
+            const int pk0 = slot32<SWZ>(__brev((unsigned)k) >> (32 - logM));
+            const int pkm = slot32<SWZ>(__brev((unsigned)km) >> (32 - logM));
+#pragma unroll
+            for (int j = 0; j < G; ++j) {
+                if (j >= nact) break;
+                const float2 *mc = mcoef32 + (size_t)ts[j] * (M + 1);
+                float2 xa = c32_mul(ik, mc[k]);
+                float2 xb = c32_mul(ikm, mc[km]);
+                if (k == 0) {
+                    xa.y = 0.f;
+                    xb.y = 0.f;
+                }
+                buf[j * M + pk0] = c2r_pre32(xa, xb, wk);
+                if (k > 0 && k < M / 2) buf[j * M + pkm] = c2r_pre32(xb, xa, wkm);
+            }
+        }
+        __syncthreads();
+        smem_fft_f32<SWZ, G>(buf, logM, nact, tw32, +1);
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+            if (j >= nact) break;
+            float *o = tab + ((size_t)s * n_terms + ts[j]) * len + CG_N_SMALL_R + 1;
+            const float *pf = postf32 + (size_t)ts[j] * N;
+            const float2 *bj = buf + j * M;
+            if (fill_small && tid <= CG_N_SMALL_R) o[tid - CG_N_SMALL_R - 1] = cg_nan<float>();
+#pragma unroll 4
+            for (int i = tid; i < N; i += bd) {
+                const float2 z = bj[slot32<SWZ>(i >> 1)];
+                const float v = ((i & 1) ? z.y : z.x) * pf[i];
+                if (!isfinite(v)) bad = true;
+                o[i] = v;
+            }
+        }
+        __syncthreads(); // the buffers are refilled by the next group
+    }
+    if (bad) cg_flag(err, CG_ERR_NONFINITE);
+}
+
 // ------------------------------------------------- r = 0 and sub-Mpc points
 
 // j_l(x): ascending series below max(1, l + 1), upward recurrence above
@@ -1442,8 +1607,44 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     const dim3 gf(n_spectra, n_q), gi(n_spectra, n_terms), gg(n_spectra, n_grp);
     // the FP32 inverse kernel fills the 43 uncomputed entries itself
     const int fill_small = (flags & COFFE_GPU_SMALL_R) ? 0 : 1;
+    // the fused mixed table kernel: one block per (spectrum, q), everything in
+    // shared memory, where that fits
+    const FusedLayout fl = fused_layout((int)nk, M, inv_g);
+    const bool fused_ok = mixed && !tables_df && nk >= (size_t)M + 1 && nk <= 8192 &&
+                          N <= 8192 && fl.total <= 200 * 1024;
     auto stage = [&](const coffe_gpu_tuning_t &tu) -> int {
         int s2;
+        if (fused_ok && tu.fft_fused) {
+#define FUSED_LAUNCH(R, W, G)                                                                     \
+    {                                                                                             \
+        CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_tables_fused_kernel<R, W, G>,                    \
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,            \
+                                          (int)fl.total));                                        \
+        fftlog_tables_fused_kernel<R, W, G><<<gf, FUSED_THREADS, fl.total, ctx->stream>>>(        \
+            g, d_pk, (const float *)ctx->csband.p, (const float *)ctx->csfac32.p,                 \
+            (const int *)ctx->samp_idx.p, (const float2 *)ctx->samp_tdf.p,                        \
+            (const float4 *)ctx->samp_f32.p, (const float2 *)ctx->qfac_df.p, wdf,                 \
+            (const float4 *)ctx->twid32.p, d_meta->grp, n_grp, n_terms, m32, p32, tw32,           \
+            (float *)ctx->tab_y.p, fill_small, ctx->d_err);                                       \
+        if ((s2 = cg_after_launch(ctx, "fftlog_tables_fused_kernel"))) return s2;                 \
+    }
+            const bool swz = tu.fft_swizzle && M >= 64;
+            if (inv_g == 3) {
+                if (tu.fft_radix == 2) {
+                    if (swz) FUSED_LAUNCH(2, true, 3) else FUSED_LAUNCH(2, false, 3)
+                } else {
+                    if (swz) FUSED_LAUNCH(4, true, 3) else FUSED_LAUNCH(4, false, 3)
+                }
+            } else {
+                if (tu.fft_radix == 2) {
+                    if (swz) FUSED_LAUNCH(2, true, 1) else FUSED_LAUNCH(2, false, 1)
+                } else {
+                    if (swz) FUSED_LAUNCH(4, true, 1) else FUSED_LAUNCH(4, false, 1)
+                }
+            }
+#undef FUSED_LAUNCH
+            return COFFE_GPU_OK;
+        }
         if (mixed) {
             const dim3 gb(((int)nk - 2 + CS_TILE - 1) / CS_TILE,
                           (n_spectra + tu.spline_group - 1) / tu.spline_group);
@@ -1538,6 +1739,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     };
     // candidate launch shapes of this table stage
     std::vector<coffe_gpu_tuning_t> cands;
+    for (int fu : {0, 1})
     for (int ff : {256, 512})
     for (int ft : {128, 256, 512})
         for (int rad : {2, 4})
@@ -1546,6 +1748,9 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
                     coffe_gpu_tuning_t c = ctx->tuning;
                     c.fft_threads = ft;
                     c.fft_threads_fwd = ff;
+                    c.fft_fused = fu;
+                    // the fused kernel has fixed block shapes and no spline grouping
+                    if (fu && (!fused_ok || ft != 256 || ff != 512 || grp != 8)) continue;
                     if (mixed) {
                         if (sw && M < 64) continue;
                         c.fft_radix = rad;
@@ -1567,6 +1772,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         ctx->last_tuning.fft_radix = tu.fft_radix;
         ctx->last_tuning.fft_swizzle = tu.fft_swizzle;
         ctx->last_tuning.spline_group = tu.spline_group;
+        ctx->last_tuning.fft_fused = fused_ok && tu.fft_fused;
     }
     // r = 0 and sub-Mpc entries
     const long tables = (long)n_spectra * n_terms;

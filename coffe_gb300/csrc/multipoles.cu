@@ -29,6 +29,7 @@
 
 #include "ctx.cuh"
 #include "dfloat.cuh"
+#include "f32x2.cuh"
 #include "qag.cuh"
 
 namespace {
@@ -140,6 +141,42 @@ template <typename T> void build_node_table_fast(int NL, const int *ls, std::vec
         T *r2 = out.data() + (size_t)31 * R1 + (size_t)k * R2;
         r2[0] = (T)(mult * P.wk[sl]);
         for (int j = 0; j < NL; ++j) r2[1 + j] = (T)P.Pl[ls[j]][sl];
+    }
+}
+
+// The node table of mp_fast2_kernel (layout Fast2Layout<NL>): every constant of
+// the rows mu >= 0 stored twice, as the packed pair (c, c) both lanes of a
+// packed FP32 operation use; pass-1 pairs mu, -mu, -mu^2, 1 - mu^2, a2, a1, a0,
+// -b2, -b1, wk P_l (NL), wg P_l (NL), wk |P_l| (NL); pass-2 pairs wk, P_l (NL)
+void build_node_table_fast2(int NL, const int *ls, std::vector<float> &out)
+{
+    const PanelTables<double> &P = panel_tables();
+    const int F1 = (2 * (9 + 3 * NL) + 3) / 4 * 4, F2 = (2 * (1 + NL) + 3) / 4 * 4;
+    out.assign((size_t)31 * (F1 + F2), 0.f);
+    for (int k = 0; k < 31; ++k) {
+        const int sl = P.order[30 + k];
+        const double mult = sl == 60 ? 1.0 : 2.0;
+        const double mu = P.mu_sorted[30 + k], mu2 = mu * mu, omm = 1.0 - mu2;
+        double c[9 + 3 * MP_MAX_L];
+        c[0] = mu;
+        c[1] = -mu;
+        c[2] = -mu2;
+        c[3] = omm;
+        c[4] = 0.75 * omm * omm + 4.0 * mu2 * omm + 12.0 * mu2 * mu2; // a2
+        c[5] = -2.5 * omm * omm - 20.0 * mu2 * omm;                   // a1
+        c[6] = 4.75 * omm * omm - 8.0 * mu2 * omm - 4.0 * mu2 * mu2;  // a0
+        c[7] = -(11.0 - 9.0 * omm);                                   // -b2
+        c[8] = 9.0 * omm;                                             // -b1
+        for (int j = 0; j < NL; ++j) {
+            c[9 + j] = mult * P.wkP[ls[j]][sl];
+            c[9 + NL + j] = mult * P.wgP[ls[j]][sl];
+            c[9 + 2 * NL + j] = mult * P.wkA[ls[j]][sl];
+        }
+        float *r = out.data() + (size_t)k * F1;
+        for (int i = 0; i < 9 + 3 * NL; ++i) r[2 * i] = r[2 * i + 1] = (float)c[i];
+        float *r2 = out.data() + (size_t)31 * F1 + (size_t)k * F2;
+        r2[0] = r2[1] = (float)(mult * P.wk[sl]);
+        for (int j = 0; j < NL; ++j) r2[2 + 2 * j] = r2[3 + 2 * j] = (float)P.Pl[ls[j]][sl];
     }
 }
 
@@ -945,6 +982,226 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
     }
 }
 
+// ---------------------------------- mixed path, two separations per thread
+//
+// mp_fast_kernel's algorithm (float) with every per-node operation on packed
+// FP32 pairs: each thread evaluates two (request, separation) pairs, lane lo
+// the separation item0 + tid and lane hi item0 + blockDim + tid, so one
+// fma/add/mul.rn.f32x2 issue serves both.  The kernel is bound by instruction
+// issue, not by the FMA pipe, so halving the FP32 instructions is the lever.
+// The results are those of the one-pair kernel up to float rounding order.
+template <int NL> struct Fast2Layout {
+    static constexpr int P1 = 9 + 3 * NL;  // packed constants of pass 1
+    static constexpr int P2 = 1 + NL;      // and of pass 2
+    static constexpr int F1 = (2 * P1 + 3) / 4 * 4;
+    static constexpr int F2 = (2 * P2 + 3) / 4 * 4;
+    static constexpr int ROWS = 31;
+    static constexpr int COUNT = ROWS * (F1 + F2); // floats
+    // the rows of integrand pairs (8 bytes per thread and node) hold the
+    // block's 2 blockDim x NL double results when the output is staged
+    static_assert(COUNT % 4 == 0 && ROWS * 8 >= 2 * NL * 8, "layout");
+};
+
+// row of packed pairs from shared memory (16-byte loads)
+template <int F> __device__ __forceinline__ void lds_pairs(const float *p, f2 (&r)[F / 2])
+{
+#pragma unroll
+    for (int i = 0; i < F / 4; ++i) {
+        const ulonglong2 v = reinterpret_cast<const ulonglong2 *>(p)[i];
+        r[2 * i].v = v.x;
+        r[2 * i + 1].v = v.y;
+    }
+}
+
+template <int NL, int CONTRIB, int UNROLL>
+__global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
+    mp_fast2_kernel(MpArgs a, const BgFitT<float> *__restrict__ fit, float chi_lo, float chi_hi,
+                    const float *__restrict__ tab_x, const float *__restrict__ tab_y,
+                    const int *__restrict__ req_spectrum, const double *__restrict__ req_z_mean,
+                    const int64_t *__restrict__ req_offset, const double *__restrict__ sep,
+                    long long total, const float *__restrict__ nodes, double *__restrict__ out,
+                    int *__restrict__ retry_count, int2 *__restrict__ retry, int *err)
+{
+    typedef Fast2Layout<NL> LY;
+    extern __shared__ __align__(16) unsigned char mp_smem[];
+    float *tab1 = reinterpret_cast<float *>(mp_smem); // [ROWS][F1]
+    float *tab2 = tab1 + LY::ROWS * LY::F1;           // [ROWS][F2]
+    f2 *xs = reinterpret_cast<f2 *>(tab2 + LY::ROWS * LY::F2); // [ROWS][blockDim.x]
+    for (int i = threadIdx.x; i < LY::COUNT; i += blockDim.x) tab1[i] = nodes[i];
+    __syncthreads();
+    const int bd = blockDim.x, tid = threadIdx.x;
+    const long long item0 = (long long)blockIdx.x * 2 * bd;
+    const long long it[2] = {item0 + tid, item0 + bd + tid};
+    if (it[0] >= total && !a.out_staged) return; // the staged store needs every thread
+    const float idl = f32_of_bits(a.inv_dlog);
+    const int tl = a.tab_len;
+    const float mu_max = tab1[(LY::ROWS - 1) * LY::F1]; // largest mu
+    // per lane: the separation, its request's background polynomials and the
+    // three table values
+    float r[2], chim[2], rho[2], I00[2], I02[2], I04[2];
+    float4 ge[2], go[2], fe[2], fo[2];
+    bool valid[2], inside[2], finite[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        valid[h] = it[h] < total;
+        const int q = valid[h] ? find_request(req_offset, a.n_req, it[h]) : 0;
+        const int s = req_spectrum[q];
+        r[h] = valid[h] ? f32_of_bits(sep[it[h]]) : 1.f;
+        const BgFitT<float> bf = fit[q];
+        ge[h] = bf.ge;
+        go[h] = bf.go;
+        fe[h] = bf.fe;
+        fo[h] = bf.fo;
+        chim[h] = bf.go.w;
+        rho[h] = 0.5f * r[h] * bf.ge.w;
+        const float *y0 = tab_y + ((size_t)s * a.n_terms) * tl;
+        I00[h] = table_lookup<float, true>(tab_x, y0 + (size_t)a.t00 * tl, tl, idl, r[h]);
+        I02[h] = table_lookup<float, true>(tab_x, y0 + (size_t)a.t02 * tl, tl, idl, r[h]);
+        I04[h] = table_lookup<float, true>(tab_x, y0 + (size_t)a.t04 * tl, tl, idl, r[h]);
+        const float span = mu_max * 0.5f * r[h];
+        inside[h] = valid[h] && (chim[h] - span >= chi_lo) && (chim[h] + span <= chi_hi);
+        finite[h] = inside[h] && isfinite(I00[h]) && isfinite(I02[h]) && isfinite(I04[h]);
+    }
+    f2 K[NL], nKc[NL], G[NL], A[NL];
+#pragma unroll
+    for (int j = 0; j < NL; ++j) K[j] = nKc[j] = G[j] = A[j] = f2_dup(0.f);
+    const bool any = inside[0] || inside[1];
+    if (any) {
+        const f2 hr = f2_pack(0.5f * r[0], 0.5f * r[1]);
+        const f2 cm = f2_pack(chim[0], chim[1]);
+        const f2 A2 = f2_pack(2.f * chim[0] * chim[0], 2.f * chim[1] * chim[1]);
+        const f2 Br = f2_pack(0.5f * r[0] * r[0], 0.5f * r[1] * r[1]);
+        const f2 r2 = f2_pack(r[0] * r[0], r[1] * r[1]);
+        const f2 rh = f2_pack(rho[0], rho[1]);
+        const f2 gex = f2_pack(ge[0].x, ge[1].x), gey = f2_pack(ge[0].y, ge[1].y),
+                 gez = f2_pack(ge[0].z, ge[1].z);
+        const f2 gox = f2_pack(go[0].x, go[1].x), goy = f2_pack(go[0].y, go[1].y),
+                 goz = f2_pack(go[0].z, go[1].z);
+        const f2 fex = f2_pack(fe[0].x, fe[1].x), fey = f2_pack(fe[0].y, fe[1].y),
+                 fez = f2_pack(fe[0].z, fe[1].z);
+        const f2 fox = f2_pack(fo[0].x, fo[1].x), foy = f2_pack(fo[0].y, fo[1].y),
+                 foz = f2_pack(fo[0].z, fo[1].z);
+        const f2 i00 = f2_pack(I00[0], I00[1]), i02 = f2_pack(I02[0], I02[1]);
+        const f2 e00 = f2_mul(i00, f2_dup(1.f / 15.f)), e02 = f2_mul(i02, f2_dup(1.f / 21.f)),
+                 e04 = f2_pack(I04[0] * (1.f / 35.f), I04[1] * (1.f / 35.f));
+        const f2 e00x2 = f2_add(e00, e00), e0d = f2_sub(e00, e02);
+        const f2 K1 = f2_mul(f2_sub(i00, f2_add(i02, i02)), f2_dup(1.f / 3.f));
+        const f2 one = f2_dup(1.f);
+#pragma unroll UNROLL
+        for (int k = 0; k < LY::ROWS; ++k) {
+            f2 c[LY::F1 / 2];
+            lds_pairs<LY::F1>(tab1 + k * LY::F1, c);
+            const f2 mu = c[0], nmu = c[1], nmu2 = c[2], omm = c[3];
+            const f2 chi1 = f2_fma(nmu, hr, cm), chi2 = f2_fma(mu, hr, cm);
+            // background at chi_mean -/+ mu r/2: even and odd parts in t
+            const f2 t = f2_mul(mu, rh), tn = f2_mul(nmu, rh), u = f2_mul(t, t);
+            const f2 gE = f2_fma(f2_fma(gez, u, gey), u, gex);
+            const f2 gO = f2_fma(f2_fma(goz, u, goy), u, gox);
+            const f2 fE = f2_fma(f2_fma(fez, u, fey), u, fex);
+            const f2 fO = f2_fma(f2_fma(foz, u, foy), u, fox);
+            const f2 G1 = f2_fma(tn, gO, gE), G2 = f2_fma(t, gO, gE);
+            const f2 F1 = f2_fma(tn, fO, fE), F2 = f2_fma(t, fO, fE);
+            const f2 D = f2_fma(nmu2, Br, A2); // 2 chi1 chi2
+            const f2 inv_D = f2_rcp(D);
+            const f2 sv = f2_mul(f2_mul(r2, omm), inv_D);
+            const f2 cc = f2_sub(one, sv);
+            f2 v = f2_dup(0.f);
+            if (CONTRIB & COFFE_GPU_DEN) v = f2_mul(f2_mul(G1, G2), i00);
+            if (CONTRIB & COFFE_GPU_RSD) {
+                const f2 g2c = f2_fma(c[4], e04, f2_fma(c[7], e02, e00x2));
+                const f2 g1c = f2_fma(c[5], e04, f2_mul(c[8], e02));
+                const f2 g0c = f2_fma(c[6], e04, e0d);
+                v = f2_fma(f2_mul(F1, F2), f2_fma(f2_fma(g2c, cc, g1c), cc, g0c), v);
+            }
+            if ((CONTRIB & COFFE_GPU_DEN) && (CONTRIB & COFFE_GPU_RSD)) {
+                const f2 gf = f2_mul(G1, F2), fg = f2_mul(F1, G2);
+                const f2 g = f2_mul(f2_mul(f2_add(one, cc), omm), inv_D);
+                v = f2_fma(f2_add(gf, fg), K1, v);
+                v = f2_fma(f2_mul(g, i02),
+                           f2_fma(gf, f2_mul(chi1, chi1), f2_mul(fg, f2_mul(chi2, chi2))), v);
+            }
+            xs[k * bd + tid] = v;
+            const f2 av = f2_abs(v);
+#pragma unroll
+            for (int j = 0; j < NL; ++j) { // Kahan-compensated Kronrod sum, -c kept
+                const f2 yk = f2_fma(c[9 + j], v, nKc[j]);
+                const f2 tk = f2_add(K[j], yk);
+                nKc[j] = f2_sub(yk, f2_sub(tk, K[j]));
+                K[j] = tk;
+                G[j] = f2_fma(c[9 + NL + j], v, G[j]);
+                A[j] = f2_fma(c[9 + 2 * NL + j], av, A[j]);
+            }
+        }
+    }
+    f2 asc[NL], nhK[NL];
+#pragma unroll
+    for (int j = 0; j < NL; ++j) {
+        asc[j] = f2_dup(0.f);
+        nhK[j] = f2_mul(K[j], f2_dup(-0.5f));
+    }
+    if (any) {
+#pragma unroll 1
+        for (int k = 0; k < LY::ROWS; ++k) {
+            f2 c[LY::F2 / 2];
+            lds_pairs<LY::F2>(tab2 + k * LY::F2, c);
+            const f2 v = xs[k * bd + tid];
+#pragma unroll
+            for (int j = 0; j < NL; ++j)
+                asc[j] = f2_fma(c[0], f2_abs(f2_fma(v, c[1 + j], nhK[j])), asc[j]);
+        }
+    }
+    float Kl[2][NL], Gl[2][NL], Al[2][NL], Sl[2][NL];
+#pragma unroll
+    for (int j = 0; j < NL; ++j) {
+        Kl[0][j] = f2_lo(K[j]);
+        Kl[1][j] = f2_hi(K[j]);
+        Gl[0][j] = f2_lo(G[j]);
+        Gl[1][j] = f2_hi(G[j]);
+        Al[0][j] = f2_lo(A[j]);
+        Al[1][j] = f2_hi(A[j]);
+        Sl[0][j] = f2_lo(asc[j]);
+        Sl[1][j] = f2_hi(asc[j]);
+    }
+    const float eps = f32_of_bits(a.epsrel);
+    if (!a.out_staged) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            if (valid[h])
+                first_panel_out<NL, float>(a, eps, it[h], finite[h], Kl[h], Gl[h], Al[h], Sl[h],
+                                           out, retry_count, retry, err);
+        return;
+    }
+    // out in page-locked host memory: the block's 2 blockDim results go
+    // through shared memory (the integrand rows, no longer read) and leave as
+    // consecutive 16-byte stores
+    double res[2][NL];
+    bool have[2][NL];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        if (valid[h])
+            first_panel_value<NL, float>(a, eps, it[h], finite[h], Kl[h], Gl[h], Al[h], Sl[h],
+                                         res[h], have[h], retry_count, retry, err);
+    __syncthreads();
+    double *stage = reinterpret_cast<double *>(xs);
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        if (valid[h]) {
+#pragma unroll
+            for (int j = 0; j < NL; ++j) stage[(h * bd + tid) * NL + j] = res[h][j];
+        }
+    __syncthreads();
+    const int n = (int)min((long long)(2 * bd), total - item0) * NL;
+    double *o = out + item0 * NL;
+    if ((reinterpret_cast<uintptr_t>(o) & 15) == 0) {
+        const double2 *s2 = reinterpret_cast<const double2 *>(stage);
+        double2 *o2 = reinterpret_cast<double2 *>(o);
+        for (int i = tid; i < n / 2; i += bd) o2[i] = s2[i];
+        if ((n & 1) && tid == 0) o[n - 1] = stage[n - 1];
+    } else {
+        for (int i = tid; i < n; i += bd) o[i] = stage[i];
+    }
+}
+
 // ------------------------------------------------- correlation function
 // xi(z_mean, mu, r) of the nonintegrated den/rsd terms (corrfunc.c:55-141,
 // signal.c:511-518: functions_nonintegrated at the requested mu), one thread
@@ -1059,7 +1316,8 @@ __global__ void __launch_bounds__(32 * MP_RETRY_WARPS)
 
 // The cached node table of (multipole list, precision, layout), uploaded on
 // first use: layout 0 / 1 = NodeLayout without / with the mirror rule,
-// 2 = FastLayout.  *dev receives its device address.
+// 2 = FastLayout, 3 = Fast2Layout (packed pairs).  *dev receives its device
+// address.
 template <typename Build>
 int node_slot(coffe_gpu_ctx *ctx, int n_l, const int *ls, int prec_tag, int layout, Build build,
               const void **dev)
@@ -1116,9 +1374,23 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S
     static const FitInvT<T> vinv = fit_inverse<T>();
     const int contrib = a.contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD);
     // first panel (with lt threads per block) and the adaptive retries
+    // the packed two-separation kernel (float only) and its node table
+    const bool can_pack = sizeof(T) == sizeof(float);
+    const void *dn2 = nullptr;
+    if (can_pack &&
+        (st = node_slot(ctx, a.n_l, a.ls, COFFE_GPU_MIXED, 3,
+                        [&](std::vector<unsigned char> &bytes) {
+                            std::vector<float> tab;
+                            build_node_table_fast2(a.n_l, a.ls, tab);
+                            bytes.assign((const unsigned char *)tab.data(),
+                                         (const unsigned char *)(tab.data() + tab.size()));
+                        },
+                        &dn2)))
+        return st;
     auto run = [&](const coffe_gpu_tuning_t &tu) -> int {
         const int lt = tu.lane_threads;
-        const long long blocks = (total + lt - 1) / lt;
+        const bool pack = can_pack && tu.lane_pack == 2;
+        const long long blocks = (total + (pack ? 2 : 1) * lt - 1) / ((pack ? 2 : 1) * lt);
         CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
         mp_bgfit_kernel<T, S><<<(a.n_req + MP_FIT_WARPS - 1) / MP_FIT_WARPS, 32 * MP_FIT_WARPS, 0,
                                 ctx->stream>>>(chi_of_z, bg.z_of_chi, bg.D1, bg.f, a.n_req, vinv,
@@ -1126,7 +1398,17 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S
         int s1 = cg_after_launch(ctx, "mp_bgfit_kernel");
         if (s1) return s1;
 #define MP_FAST_U(NLV, CV, UV)                                                                    \
-    {                                                                                             \
+    if (pack) {                                                                                   \
+        const size_t smem = sizeof(float) * Fast2Layout<NLV>::COUNT +                             \
+                            sizeof(f2) * Fast2Layout<NLV>::ROWS * lt;                             \
+        CG_CUDA(ctx, cudaFuncSetAttribute(mp_fast2_kernel<NLV, CV, UV>,                           \
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,            \
+                                          (int)smem));                                            \
+        mp_fast2_kernel<NLV, CV, UV><<<(unsigned)blocks, lt, smem, ctx->stream>>>(                \
+            a, (const BgFitT<float> *)d_fit, (float)bg.z_of_chi.x0, (float)bg.z_of_chi.xn,        \
+            (const float *)tab_x, (const float *)tab_y, req_spectrum, req_z_mean, req_offset,     \
+            sep, total, (const float *)dn2, out, d_count, d_retry, ctx->d_err);                   \
+    } else {                                                                                      \
         const size_t smem = sizeof(T) * (FastLayout<NLV>::COUNT + FastLayout<NLV>::ROWS * lt);    \
         CG_CUDA(ctx, cudaFuncSetAttribute(mp_fast_kernel<NLV, CV, UV, T>,                         \
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,            \
@@ -1158,13 +1440,16 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S
         return cg_after_launch(ctx, "mp_retry_kernel");
     };
     std::vector<coffe_gpu_tuning_t> cands;
-    for (int lt : {64, 128, 256})
-        for (int un : {1, 2}) {
-            coffe_gpu_tuning_t c = ctx->tuning;
-            c.lane_threads = lt;
-            c.lane_unroll = un;
-            cands.push_back(c);
-        }
+    for (int pk : {1, 2})
+        for (int lt : {64, 128, 256})
+            for (int un : {1, 2}) {
+                if (pk == 2 && !can_pack) continue;
+                coffe_gpu_tuning_t c = ctx->tuning;
+                c.lane_threads = lt;
+                c.lane_unroll = un;
+                c.lane_pack = pk;
+                cands.push_back(c);
+            }
     coffe_gpu_tuning_t tu;
     long long bucket = 0;
     while ((1ll << bucket) < total) ++bucket;
@@ -1172,6 +1457,7 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S
     if ((st = cg_tuned(ctx, key, cands, run, &tu))) return st;
     ctx->last_tuning.lane_threads = tu.lane_threads;
     ctx->last_tuning.lane_unroll = tu.lane_unroll;
+    ctx->last_tuning.lane_pack = can_pack ? tu.lane_pack : 1;
     return run(tu);
 }
 

@@ -350,6 +350,11 @@ typedef struct {
     int lane_threads; /* 64, 128 or 256 threads per block of the mixed multipole kernel */
     int lane_unroll;  /* 1 or 2 quadrature nodes per step of that kernel's node loop */
     int fft_threads_fwd; /* threads per block of the forward transforms: 128 .. 1024 */
+    int lane_pack;    /* 1 or 2 separations per thread of that kernel (2: both evaluated
+                         at once with packed FP32 pair instructions) */
+    int fft_fused;    /* 1: the mixed table stage as one kernel per (spectrum, q), all in
+                         shared memory (where it fits: FFT size <= 8192, the k grid no
+                         shorter than N/2 + 1 and no longer than 8192); 0: three kernels */
 } coffe_gpu_tuning_t;
 
 /* ---- the divergent integral I^4_0 and its renormalisation (integrals.c:773-914),

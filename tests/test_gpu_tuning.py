@@ -29,7 +29,7 @@ def setup():
 
 
 DEFAULT = dict(fft_threads=512, fft_radix=4, fft_swizzle=0, spline_group=8, lane_threads=256,
-               lane_unroll=1, fft_threads_fwd=512)
+               lane_unroll=1, fft_threads_fwd=512, lane_pack=1, fft_fused=0)
 
 
 def _tables(ctx, b, precision, **cfg):
@@ -69,23 +69,42 @@ def test_table_configurations_agree(setup):
         assert np.array_equal(got, ref64, equal_nan=True), ft
 
 
+def test_fused_table_stage_matches_three_kernels(setup):
+    """The one-kernel-per-spectrum mixed table stage runs the same arithmetic as
+    the three separate kernels: the tables agree to float rounding."""
+    ctx, b = setup
+    sep = _tables(ctx, b, "mixed", fft_fused=0)
+    fused = _tables(ctx, b, "mixed", fft_fused=1)
+    assert ctx.tuning()["fft_fused"] == 1
+    fin = np.isfinite(sep)
+    assert np.array_equal(fin, np.isfinite(fused))
+    scale = np.nanmax(np.abs(sep), axis=1, keepdims=True)
+    e = np.max(np.abs(fused - sep)[fin] / np.broadcast_to(scale, sep.shape)[fin])
+    print("fused vs three kernels, max |difference| / table scale:", e)
+    assert e < 1e-7, e
+
+
 def test_lane_configurations_agree(setup):
     ctx, b = setup
     _tables(ctx, b, "mixed")
     ref = _multipoles(ctx, b)
     floor = 1e-3 * np.abs(ref).max(axis=0, keepdims=True)
     first = {}
-    for un in (1, 2):
-        for lt in (64, 128, 256):
-            ctx.set_tuning(**{**DEFAULT, "lane_threads": lt, "lane_unroll": un})
-            got = _multipoles(ctx, b)
-            assert ctx.tuning()["lane_threads"] == lt and ctx.tuning()["lane_unroll"] == un
-            # the block size never changes a result; the unrolled node loop may
-            # contract a multiply-add differently (float rounding)
-            first.setdefault(un, got)
-            assert np.array_equal(got, first[un]), (lt, un)
-            assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), floor)) < 1e-6, (lt, un)
-    assert np.array_equal(first[1], ref)
+    for pk in (1, 2):
+        for un in (1, 2):
+            for lt in (64, 128, 256):
+                ctx.set_tuning(**{**DEFAULT, "lane_threads": lt, "lane_unroll": un,
+                                  "lane_pack": pk})
+                got = _multipoles(ctx, b)
+                cfg = ctx.tuning()
+                assert (cfg["lane_threads"], cfg["lane_unroll"], cfg["lane_pack"]) == (lt, un, pk)
+                # the block size never changes a result; the unrolled node loop
+                # and the packed pair kernel may round differently (float)
+                first.setdefault((pk, un), got)
+                assert np.array_equal(got, first[(pk, un)]), (lt, un, pk)
+                e = np.max(np.abs(got - ref) / np.maximum(np.abs(ref), floor))
+                assert e < 1e-6, (lt, un, pk, e)
+    assert np.array_equal(first[(1, 1)], ref)
 
 
 def test_autotune_chooses_and_reuses(setup):
@@ -109,7 +128,7 @@ def test_autotune_chooses_and_reuses(setup):
     print("chosen", cfg, "launches while tuning", tuned, "after", plain)
     assert cfg["fft_threads"] in (128, 256, 512) and cfg["fft_radix"] in (2, 4)
     assert cfg["spline_group"] in (2, 4, 8) and cfg["lane_threads"] in (64, 128, 256)
-    assert cfg["lane_unroll"] in (1, 2)
+    assert cfg["lane_unroll"] in (1, 2) and cfg["lane_pack"] in (1, 2)
     assert tuned > 10 * plain  # candidates were timed once, then reused
     assert ctx.tuning() == cfg
     assert np.array_equal(again, got)
@@ -123,7 +142,7 @@ def test_set_tuning_rejects_bad_values(setup):
     ctx, _ = setup
     for bad in (dict(fft_threads=384), dict(fft_radix=8), dict(fft_swizzle=2),
                 dict(spline_group=3), dict(lane_threads=32), dict(lane_unroll=4),
-                dict(fft_threads_fwd=100)):
+                dict(fft_threads_fwd=100), dict(lane_pack=3), dict(fft_fused=2)):
         with pytest.raises(CoffeGpuError):
             ctx.set_tuning(**{**DEFAULT, **bad})
     with pytest.raises(ValueError):
