@@ -36,7 +36,9 @@ def test_kernel_timing_names_the_launched_kernels(fresh_ctx):
     ctx.multipoles(b.req_spectrum, b.req_z_mean, b.req_offset, b.sep, b.ls, precision="mixed")
     t = ctx.kernel_times()
     print(t)
-    for name in ("fftlog_forward_df_kernel", "fftlog_inverse_f32_kernel", "mp_fast_kernel"):
+    tables = (("fftlog_tables_fused_kernel",) if ctx.tuning()["fft_fused"] else
+              ("fftlog_forward_df_kernel", "fftlog_inverse_f32_kernel"))
+    for name in tables + ("mp_fast_kernel",):
         assert name in t, (name, sorted(t))
         assert t[name][0] >= 1 and t[name][1] > 0
     assert ctx.kernel_times() == {}  # reset by the previous read
