@@ -40,7 +40,8 @@ UNIT = "evals/s"
 TERMS = ((0, 0), (0, 2), (0, 4))
 N_FFT = 4096
 # FLOP of one multipole-quadrature node of the mixed kernel (mp_fast_kernel<3,3>,
-# counted from multipoles.cu, FMA = 2): chi1/chi2 4, two chi-table cells 18,
+# counted from multipoles.cu, FMA = 2): chi1/chi2 4, D1 and f D1 at both ends
+# from the per-request degree-5 polynomials 18,
 # D, 1/D, s, c 6, density 2, RSD polynomial 16, density-RSD 16, Kronrod
 # (Kahan) / Gauss / |f| sums 27, second-pass resasc sums 12
 FLOP_PER_NODE = 101
@@ -342,15 +343,29 @@ def extras(torch, ctx, stream):
     rz = torch.tensor([c4["z_mean"]], dtype=torch.float64, device=dev)
     ro = torch.tensor([0, len(c4["sep"])], dtype=torch.int64, device=dev)
     res = {}
-    for prec, reps in (("mixed", 3), ("fp64", 1)):
-        ctx.integrals_init(c4["k"], c4["pk"][None, :], c4["terms"], N=N_FFT, precision=prec,
-                           small_r=True)
+    for prec, reps in (("mixed", 3), ("fp64", 1), ("fp64-fastalg", 1)):
+        ctx.integrals_init(c4["k"], c4["pk"][None, :], c4["terms"], N=N_FFT,
+                           precision="mixed" if prec == "mixed" else "fp64", small_r=True)
         ctx.set_lensing_rule(*c4["rule"])
         o = torch.empty((len(c4["sep"]), 4), dtype=torch.float64, device=dev)
         ms = ev_time(lambda: ctx.multipoles_async(rs, rz, ro, sep, len(c4["sep"]), c4["ls"], o,
                                                   contrib=7, precision=prec), reps)
         ctx.synchronize()
         res[prec] = (ms, o.cpu().numpy())
+    # the gradient of the same call with respect to P(k) and the bias / growth
+    # scales (FP64 adjoint through the lensing integrands, tables and sub-Mpc
+    # QAG entries; den/RSD on their first GK61 panel)
+    pk4 = torch.tensor(c4["pk"][None, :], device=dev)
+    ctx.integrals_init_device(c4["k"], pk4, c4["terms"], N=N_FFT, precision="fp64",
+                              small_r=True)
+    ov = torch.empty((len(c4["sep"]), 4), dtype=torch.float64, device=dev)
+    G4, gpk4 = torch.ones_like(ov), torch.empty_like(pk4)
+    gb4, gf4 = (torch.empty(1, dtype=torch.float64, device=dev) for _ in range(2))
+    grad_fwd = ev_time(lambda: ctx.multipoles_scaled(rs, rz, ro, sep, len(c4["sep"]), c4["ls"],
+                                                     ov, contrib=7), 1)
+    grad_adj = ev_time(lambda: ctx.multipoles_adjoint(rs, rz, ro, sep, len(c4["sep"]), c4["ls"],
+                                                      G4, gpk4, gb4, gf4, contrib=7), 1)
+    ctx.synchronize()
     fl = 1e-3 * np.abs(res["fp64"][1]).max(0)
     fl[3] = 1e-3 * np.abs(res["fp64"][1]).max()  # l = 6: see the lensing tests
     err = float(np.max(np.abs(res["mixed"][1] - res["fp64"][1]) /
@@ -360,13 +375,25 @@ def extras(torch, ctx, stream):
         "workload": "den+RSD+lensing multipoles l=0,2,4,6, z=1.5, 200 separations 20-300 "
                     "Mpc/h, Gauss-Legendre 128 mu x 256 x (split), FFTLog N=4096",
         "mixed_ms": res["mixed"][0], "fp64_ms": res["fp64"][0],
+        "fp64_fastalg_ms": res["fp64-fastalg"][0],
+        "mixed_over_fp64": res["fp64"][0] / res["mixed"][0],
+        "mixed_over_fp64_matched": res["fp64-fastalg"][0] / res["mixed"][0],
+        "matched_note": "fp64_fastalg = the mixed path's algorithm (line-of-sight "
+                        "polynomials, five combined plane records, fast den/RSD kernel) in FP64",
         "mixed_evals_per_s": n4 / (res["mixed"][0] * 1e-3),
         "fp64_evals_per_s": n4 / (res["fp64"][0] * 1e-3),
         "lensing_rule_nodes_per_s_mixed": len(c4["sep"]) * 128 * 256 * 256 / (res["mixed"][0] * 1e-3),
         "mu_nodes_evaluated": 64,
         "note": "equal tracers and even multipoles: the rule's 64 mu > 0 nodes are evaluated "
                 "and counted twice (the terms are even in mu)",
-        "max_rel_err_mixed_vs_fp64": err}
+        "max_rel_err_mixed_vs_fp64": err,
+        "gradient": {"forward_ms": grad_fwd, "adjoint_ms": grad_adj,
+                     "finite": bool(torch.isfinite(gpk4).all().item()),
+                     "note": "d(multipoles)/d(P(k), bias scale, growth scale) of this call "
+                             "(den+RSD first panel + lensing), FP64"},
+        "max_rel_err_fp64_fastalg_vs_fp64": float(np.max(
+            np.abs(res["fp64-fastalg"][1] - res["fp64"][1]) /
+            np.maximum(np.abs(res["fp64"][1]), fl)))}
     # covariance: 5 z bins x l = 0,2,4 x 128 x 128 separations, 2D FFTLog 2^11
     ctx.background_init(co.omega_m, co.omega_baryon, co.omega_gamma, co.h, 10000)
     bg = ctx.background(with_H=False)

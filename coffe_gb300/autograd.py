@@ -1,7 +1,7 @@
-"""PyTorch autograd surface of the den/RSD multipoles: derivatives with respect
-to the input power spectra and to per-request galaxy-bias and growth-rate
-scales, computed by the library's adjoint kernels (no counterpart in the
-reference, which has no derivatives).
+"""PyTorch autograd surface of the den/RSD (+ lensing) multipoles: derivatives
+with respect to the input power spectra and to per-request galaxy-bias and
+growth-rate scales, computed by the library's adjoint kernels (no counterpart
+in the reference, which has no derivatives).
 
     mp = multipoles(ctx, k, pk, req_spectrum, req_z_mean, req_offset, sep, ls,
                     bias_scale, growth_scale)
@@ -14,7 +14,10 @@ adaptive result wherever the first panel meets the tolerance.  Where QUADPACK
 would reject a first panel (and refine it adaptively), the differentiable
 value is not the adaptive one: the forward raises :class:`FirstPanelRejected`
 unless ``allow_rejected=True`` (the value and gradient then stay the first
-panel's for those outputs).
+panel's for those outputs).  With ``contrib`` including lensing (4), the
+full-sky lensing terms on the context's Gauss-Legendre rule
+(:meth:`Context.set_lensing_rule`) are added and differentiated too (the
+tables then include the six lensing integrals and their sub-Mpc entries).
 """
 from __future__ import annotations
 
@@ -22,6 +25,8 @@ import torch
 
 from . import _lib
 from .api import DEN_RSD_TERMS, Context
+
+LENS_TERMS = ((0, 0), (0, 2), (0, 4), (1, 1), (1, 3), (2, 0))
 
 
 class FirstPanelRejected(RuntimeError):
@@ -34,6 +39,13 @@ class _Spec:
         self.engine, self.k, self.req, self.ls, self.contrib, self.N = engine, k, req, ls, contrib, N
         self.allow_rejected = allow_rejected
 
+    def tables(self, pk):
+        """FP64 tables of this spectrum batch for the call's contributions."""
+        lens = bool(self.contrib & _lib.LEN)
+        self.engine.integrals_init_device(self.k, pk.detach().contiguous(),
+                                          LENS_TERMS if lens else DEN_RSD_TERMS, N=self.N,
+                                          precision="fp64", small_r=lens, sync=True)
+
 
 class MultipolesFunction(torch.autograd.Function):
     """(pk, bias_scale, growth_scale) -> multipoles (n_sep, n_l)."""
@@ -43,8 +55,7 @@ class MultipolesFunction(torch.autograd.Function):
         e = spec.engine
         rs, rz, ro, sep = spec.req
         torch.cuda.synchronize()
-        e.integrals_init_device(spec.k, pk.detach().contiguous(), DEN_RSD_TERMS, N=spec.N,
-                                precision="fp64", small_r=False, sync=True)
+        spec.tables(pk)
         out = torch.empty((sep.numel(), len(spec.ls)), dtype=torch.float64, device=pk.device)
         e.multipoles_scaled(rs, rz, ro, sep, sep.numel(), spec.ls, out,
                             bias_scale=bias_scale.detach().contiguous(),
@@ -68,8 +79,7 @@ class MultipolesFunction(torch.autograd.Function):
         rs, rz, ro, sep = spec.req
         torch.cuda.synchronize()
         # the tables of this forward's spectra (another forward may have run since)
-        e.integrals_init_device(spec.k, pk.detach().contiguous(), DEN_RSD_TERMS, N=spec.N,
-                                precision="fp64", small_r=False, sync=True)
+        spec.tables(pk)
         g_pk = torch.empty_like(pk, dtype=torch.float64)
         g_b = torch.empty_like(bias_scale, dtype=torch.float64)
         g_f = torch.empty_like(growth_scale, dtype=torch.float64)
@@ -84,7 +94,7 @@ class MultipolesFunction(torch.autograd.Function):
 def multipoles(engine: Context, k, pk, req_spectrum, req_z_mean, req_offset, sep, ls=(0, 2, 4),
                bias_scale=None, growth_scale=None, contrib=_lib.DEN | _lib.RSD, N: int = 4096,
                allow_rejected: bool = False):
-    """Differentiable batched den/RSD multipoles, shape (len(sep), len(ls))."""
+    """Differentiable batched den/RSD (+ lensing) multipoles, shape (len(sep), len(ls))."""
     n_req = req_spectrum.numel()
     dev = pk.device
     if bias_scale is None:

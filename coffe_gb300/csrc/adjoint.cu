@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "ctx.cuh"
+#include "dual6.cuh"
 #include "fft.cuh"
 #include "qag.cuh"
 
@@ -35,10 +36,12 @@ namespace {
 #define ADJ_THREADS 128
 enum { K00BB = 0, K00BF, K00FF, K02BF, K02FF, K04FF, NKIND };
 
+#define ADJ_MAX_T 6
 struct AdjArgs {
     int n_req, n_l, contrib, n_terms, tab_len, N, nk, n_q;
-    int t[3];        // table index of I00, I02, I04
-    int tq[3];       // bias-exponent index of each of the three tables
+    int n_at;                // differentiated tables: 3 (den/RSD), 6 (with lensing)
+    int t[ADJ_MAX_T];        // table index of I00, I02, I04 (and I11, I13, I20)
+    int tq[ADJ_MAX_T];       // bias-exponent index of each table
     double inv_dlog; // N / ln(kmax/kmin)
     int has_b1, has_b2;
     int ls[ADJ_MAX_L];
@@ -72,85 +75,6 @@ __device__ __forceinline__ double adj_legendre(int l, double x)
         p1 = p2;
     }
     return p1;
-}
-
-// value and gradient with respect to the six stencil values y_{i-2..i+3}
-struct D6 {
-    double v, g[6];
-};
-__device__ __forceinline__ D6 d6_const(double v)
-{
-    D6 r;
-    r.v = v;
-    for (int k = 0; k < 6; ++k) r.g[k] = 0.0;
-    return r;
-}
-__device__ __forceinline__ D6 operator+(const D6 &a, const D6 &b)
-{
-    D6 r;
-    r.v = a.v + b.v;
-    for (int k = 0; k < 6; ++k) r.g[k] = a.g[k] + b.g[k];
-    return r;
-}
-__device__ __forceinline__ D6 operator-(const D6 &a, const D6 &b)
-{
-    D6 r;
-    r.v = a.v - b.v;
-    for (int k = 0; k < 6; ++k) r.g[k] = a.g[k] - b.g[k];
-    return r;
-}
-__device__ __forceinline__ D6 operator*(const D6 &a, const D6 &b)
-{
-    D6 r;
-    r.v = a.v * b.v;
-    for (int k = 0; k < 6; ++k) r.g[k] = a.g[k] * b.v + a.v * b.g[k];
-    return r;
-}
-__device__ __forceinline__ D6 operator*(double s, const D6 &a)
-{
-    D6 r;
-    r.v = s * a.v;
-    for (int k = 0; k < 6; ++k) r.g[k] = s * a.g[k];
-    return r;
-}
-__device__ __forceinline__ D6 operator/(const D6 &a, const D6 &b)
-{
-    D6 r;
-    r.v = a.v / b.v;
-    for (int k = 0; k < 6; ++k) r.g[k] = (a.g[k] - r.v * b.g[k]) / b.v;
-    return r;
-}
-__device__ __forceinline__ D6 d6_abs(const D6 &a)
-{
-    return a.v < 0 ? -1.0 * a : a;
-}
-
-// Akima value at v in interval i (x_i <= v < x_{i+1}) from the interior
-// stencil y_{i-2..i+3}, with its partials (spline.cuh's akima_eval_at, same
-// operation order for the value)
-__device__ D6 akima_d6(const double *__restrict__ x, const double *__restrict__ y, int i, double v)
-{
-    D6 yy[6];
-    for (int k = 0; k < 6; ++k) {
-        yy[k] = d6_const(y[i - 2 + k]);
-        yy[k].g[k] = 1.0;
-    }
-    D6 m[5]; // m_{i-2} .. m_{i+2}
-    for (int k = 0; k < 5; ++k) m[k] = (yy[k + 1] - yy[k]) / d6_const(x[i - 1 + k] - x[i - 2 + k]);
-    auto slope = [](const D6 &mm2, const D6 &mm1, const D6 &m0, const D6 &mp1) {
-        const D6 w1 = d6_abs(mp1 - m0), w2 = d6_abs(mm1 - mm2);
-        const D6 ne = w1 + w2;
-        if (ne.v == 0.0) return 0.5 * (mm1 + m0);
-        return (w1 * mm1 + w2 * m0) / ne;
-    };
-    const D6 t0 = slope(m[0], m[1], m[2], m[3]);
-    const D6 t1 = slope(m[1], m[2], m[3], m[4]);
-    const double h = x[i + 1] - x[i];
-    const D6 b = t0;
-    const D6 c = (3.0 * m[2] - 2.0 * t0 - t1) / d6_const(h);
-    const D6 d = (t0 + t1 - 2.0 * m[2]) / d6_const(h * h);
-    const D6 dx = d6_const(v - x[i]);
-    return yy[2] + dx * (b + dx * (c + d * dx));
 }
 
 // per (request, separation): J integrals over the first GK61 panel, the three
@@ -191,7 +115,7 @@ __global__ void __launch_bounds__(ADJ_THREADS)
     }
     const double *y0 = tab_y + (size_t)s * a.n_terms * n;
     D6 I[3];
-    for (int t = 0; t < 3; ++t) I[t] = akima_d6(tab_x, y0 + (size_t)a.t[t] * n, i, r);
+    for (int t = 0; t < 3; ++t) I[t] = akima_eval_d6(tab_x, y0 + (size_t)a.t[t] * n, n, i, r);
     // J integrals: first GK61 panel on [0, 1], mu = 2x - 1
     double J[NKIND][ADJ_MAX_L];
     for (int k = 0; k < NKIND; ++k)
@@ -313,7 +237,7 @@ __global__ void __launch_bounds__(ADJ_THREADS)
     if (g_bias) atomicAdd(g_bias + q, gb);
     if (g_growth) atomicAdd(g_growth + q, gg);
     for (int t = 0; t < 3; ++t) {
-        double *dst = gY + ((size_t)s * 3 + t) * n + (i - 2);
+        double *dst = gY + ((size_t)s * a.n_at + t) * n + (i - 2);
         for (int k = 0; k < 6; ++k) atomicAdd(dst + k, gI[t] * I[t].g[k]);
     }
 }
@@ -332,7 +256,7 @@ __global__ void adj_r2c_kernel(AdjArgs a, const double *__restrict__ gY,
     const int N = a.N, M = N / 2;
     const int logM = 31 - __clz(M);
     const int term = a.t[t];
-    const double *g = gY + ((size_t)s * 3 + t) * a.tab_len + CG_N_SMALL_R + 1;
+    const double *g = gY + ((size_t)s * a.n_at + t) * a.tab_len + CG_N_SMALL_R + 1;
     const double *pf = postf + (size_t)term * N;
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
         const double v = g[i] * pf[i];
@@ -345,7 +269,7 @@ __global__ void adj_r2c_kernel(AdjArgs a, const double *__restrict__ gY,
     __syncthreads();
     smem_fft<double2>(buf, logM, tw, -1);
     const double2 *mc = mcoef + (size_t)term * (M + 1);
-    double2 *out = gU + ((size_t)s * 3 + t) * (M + 1);
+    double2 *out = gU + ((size_t)s * a.n_at + t) * (M + 1);
     for (int k = threadIdx.x; k <= M; k += blockDim.x) {
         const double2 zk = buf[k & (M - 1)];
         const double2 zm = buf[(M - k) & (M - 1)];
@@ -379,9 +303,9 @@ __global__ void adj_c2r_kernel(AdjArgs a, const double2 *__restrict__ gU,
     const int logM = 31 - __clz(M);
     auto H = [&](int k) {
         double2 h = make_double2(0.0, 0.0);
-        for (int t = 0; t < 3; ++t)
+        for (int t = 0; t < a.n_at; ++t)
             if (a.tq[t] == qi) {
-                const double2 u = gU[((size_t)s * 3 + t) * (M + 1) + k];
+                const double2 u = gU[((size_t)s * a.n_at + t) * (M + 1) + k];
                 h.x += u.x;
                 h.y += u.y;
             }
@@ -477,10 +401,12 @@ int multipoles_adjoint_run(coffe_gpu_ctx *ctx, int contrib, int n_req, const int
         cg_set_error(ctx, "multipoles adjoint: needs FP64 integral tables");
         return COFFE_GPU_EINVAL;
     }
-    if (!(contrib & 3) || (contrib & ~3)) {
-        cg_set_error(ctx, "multipoles adjoint: contrib must select den and/or rsd");
+    if (!(contrib & 7) || (contrib & ~7)) {
+        cg_set_error(ctx, "multipoles adjoint: contrib must select den, rsd and/or len");
         return COFFE_GPU_EINVAL;
     }
+    const bool len = (contrib & COFFE_GPU_LEN) != 0;
+    const bool nonint = (contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD)) != 0;
     if (n_l < 1 || n_l > ADJ_MAX_L || n_req < 1) {
         cg_set_error(ctx, "multipoles adjoint: need 1 <= n_l <= %d, n_req >= 1", ADJ_MAX_L);
         return COFFE_GPU_EINVAL;
@@ -488,7 +414,7 @@ int multipoles_adjoint_run(coffe_gpu_ctx *ctx, int contrib, int n_req, const int
     AdjArgs a;
     a.n_req = n_req;
     a.n_l = n_l;
-    a.contrib = contrib;
+    a.contrib = contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD);
     a.n_terms = ctx->n_terms;
     a.tab_len = (int)(ctx->N + CG_N_SMALL_R + 1);
     a.N = (int)ctx->N;
@@ -497,15 +423,20 @@ int multipoles_adjoint_run(coffe_gpu_ctx *ctx, int contrib, int n_req, const int
     a.inv_dlog = (double)ctx->N / log(ctx->kmax / ctx->kmin);
     a.has_b1 = ctx->bias_set[0];
     a.has_b2 = ctx->bias_set[1];
-    const int want[3] = {0, 2, 4};
-    for (int t = 0; t < 3; ++t) {
-        a.t[t] = cg_find_term(ctx, 0, want[t]);
+    // the tables differentiated, in the lensing kernels' order (the den/RSD
+    // integrand reads the first three)
+    const int want[ADJ_MAX_T][2] = {{0, 0}, {0, 2}, {0, 4}, {1, 1}, {1, 3}, {2, 0}};
+    a.n_at = len ? 6 : 3;
+    for (int t = 0; t < a.n_at; ++t) {
+        a.t[t] = cg_find_term(ctx, want[t][0], want[t][1]);
         if (a.t[t] < 0) {
-            cg_set_error(ctx, "multipoles adjoint: integrals (0,0), (0,2), (0,4) are required");
+            cg_set_error(ctx, "multipoles adjoint: the integral (n=%d, l=%d) is required",
+                         want[t][0], want[t][1]);
             return COFFE_GPU_ESTATE;
         }
         a.tq[t] = ctx->term_q[a.t[t]];
     }
+    for (int t = a.n_at; t < ADJ_MAX_T; ++t) a.t[t] = a.tq[t] = -1;
     for (int j = 0; j < ADJ_MAX_L; ++j) a.ls[j] = j < n_l ? l[j] : 0;
     for (int j = 0; j < n_l; ++j)
         if (l[j] < 0 || l[j] > 32) {
@@ -517,8 +448,8 @@ int multipoles_adjoint_run(coffe_gpu_ctx *ctx, int contrib, int n_req, const int
     // each sub-buffer starts on a 256-byte boundary (gU holds 16-byte double2;
     // the table length N + 43 is odd, so gY's byte size is not a multiple of 16)
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    const size_t b_gY = al(sizeof(double) * (size_t)S * 3 * a.tab_len),
-                 b_gU = al(sizeof(double2) * (size_t)S * 3 * (M + 1)),
+    const size_t b_gY = al(sizeof(double) * (size_t)S * a.n_at * a.tab_len),
+                 b_gU = al(sizeof(double2) * (size_t)S * a.n_at * (M + 1)),
                  b_Sb = al(sizeof(double) * (size_t)S * a.n_q * N),
                  b_cb = al(sizeof(double) * (size_t)S * a.nk);
     int st;
@@ -542,18 +473,31 @@ int multipoles_adjoint_run(coffe_gpu_ctx *ctx, int contrib, int n_req, const int
         rejected = (int *)ctx->mp_retry.p;
         CG_CUDA(ctx, cudaMemsetAsync(rejected, 0, sizeof(int), ctx->stream));
     }
-    adj_pair_kernel<<<(unsigned)((total + ADJ_THREADS - 1) / ADJ_THREADS), ADJ_THREADS, 0, ctx->stream>>>(
-        a, bg, (const double *)ctx->tab_x.p, (const double *)ctx->tab_y.p, req_spectrum, req_z_mean,
-        req_offset, sep, total, bias_scale, growth_scale, grad_out, value_out, gY, grad_bias,
-        grad_growth, rejected, ctx->d_err);
-    if ((st = cg_after_launch(ctx, "adj_pair_kernel"))) return st;
+    if (nonint) {
+        adj_pair_kernel<<<(unsigned)((total + ADJ_THREADS - 1) / ADJ_THREADS), ADJ_THREADS, 0,
+                          ctx->stream>>>(
+            a, bg, (const double *)ctx->tab_x.p, (const double *)ctx->tab_y.p, req_spectrum,
+            req_z_mean, req_offset, sep, total, bias_scale, growth_scale, grad_out, value_out, gY,
+            grad_bias, grad_growth, rejected, ctx->d_err);
+        if ((st = cg_after_launch(ctx, "adj_pair_kernel"))) return st;
+    } else if (value_out) {
+        CG_CUDA(ctx, cudaMemsetAsync(value_out, 0, sizeof(double) * (size_t)total * n_l,
+                                     ctx->stream));
+    }
+    // the lensing terms: their values added to value_out, their table cotangents to gY
+    if (len && (st = lensing_adjoint_run(ctx, contrib, n_req, req_spectrum, req_z_mean,
+                                         req_offset, sep, total, n_l, l, bias_scale,
+                                         growth_scale, grad_out, value_out, gY, a.n_at,
+                                         grad_out ? grad_bias : nullptr,
+                                         grad_out ? grad_growth : nullptr)))
+        return st;
     if (!grad_out || !grad_pk) return COFFE_GPU_OK;
     const double2 *mcoef = (const double2 *)ctx->modec.p;
     const double *modew = (const double *)((const char *)ctx->modec.p + sizeof(double2) * (M + 1) * ctx->n_terms);
     const size_t smem = sizeof(double2) * M;
     CG_CUDA(ctx, cudaFuncSetAttribute(adj_r2c_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CG_CUDA(ctx, cudaFuncSetAttribute(adj_c2r_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    adj_r2c_kernel<<<dim3(S, 3), 512, smem, ctx->stream>>>(a, gY, (const double *)ctx->postf.p, mcoef,
+    adj_r2c_kernel<<<dim3(S, a.n_at), 512, smem, ctx->stream>>>(a, gY, (const double *)ctx->postf.p, mcoef,
                                                            modew, (const double2 *)ctx->twid.p, gU);
     if ((st = cg_after_launch(ctx, "adj_r2c_kernel"))) return st;
     adj_c2r_kernel<<<dim3(S, a.n_q), 512, smem, ctx->stream>>>(a, gU, (const double *)ctx->qfac.p,
@@ -562,5 +506,9 @@ int multipoles_adjoint_run(coffe_gpu_ctx *ctx, int contrib, int n_req, const int
     adj_spline_kernel<<<(S + 63) / 64, 64, 0, ctx->stream>>>(
         a, (const double *)ctx->kgrid.p, (const double *)ctx->csfac.p, (const int *)ctx->samp_idx.p,
         (const double *)ctx->samp_dx.p, Sbar, cbar, grad_pk, S);
-    return cg_after_launch(ctx, "adj_spline_kernel");
+    if ((st = cg_after_launch(ctx, "adj_spline_kernel"))) return st;
+    // the lensing lookups reach the r = 0 and sub-Mpc entries (their own QAG
+    // integrals of P(k)); adj_spline_kernel has set grad_pk, these add to it
+    if (len) return small_r_adjoint_run(ctx, gY, a.n_at, a.t, grad_pk);
+    return COFFE_GPU_OK;
 }

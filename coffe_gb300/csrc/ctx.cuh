@@ -244,6 +244,15 @@ int average_multipoles_run(coffe_gpu_ctx *ctx, int contrib, int precision, doubl
                            int n_win, const int *win_spectrum, const double *z_min,
                            const double *z_max, const int64_t *win_offset, const double *sep,
                            int n_l, const int *l, int n_z, double *out, long long total);
+int lensing_adjoint_run(coffe_gpu_ctx *ctx, int contrib, int n_req, const int *req_spectrum,
+                        const double *req_z_mean, const int64_t *req_offset, const double *sep,
+                        long long total, int n_l, const int *l, const double *bias_scale,
+                        const double *growth_scale, const double *grad_out, double *value_out,
+                        double *gY, int n_at, double *grad_bias, double *grad_growth);
+// adjoint of the r = 0 and sub-Mpc table entries: gY's first CG_N_SMALL_R + 1
+// entries of each of the n_at tables (term index term[t]) into grad_pk (added)
+int small_r_adjoint_run(coffe_gpu_ctx *ctx, const double *gY, int n_at, const int *term,
+                        double *grad_pk);
 // n-point Gauss-Legendre nodes (ascending) and weights on [-1, 1]
 void gauss_legendre_nodes(int n, double *x, double *w);
 int corrfunc_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_req,

@@ -21,6 +21,7 @@
 #include "cplx.cuh"
 #include "ctx.cuh"
 #include "dfloat.cuh"
+#include "dual6.cuh"
 #include "fft.cuh"
 #include "qag.cuh"
 
@@ -1250,6 +1251,91 @@ __global__ void __launch_bounds__(32 * SR_WARPS)
     }
 }
 
+// (n, l) of the tables whose sub-Mpc entries an adjoint call differentiates
+struct SmallRTerms {
+    int n[8], l[8];
+};
+
+// Adjoint of small_r_kernel for one (spectrum, table t, point j): the table
+// cotangent gY[(s * n_at + t) * len + j] carried into dL/dP(k).  With the
+// final QAG partition of the entry fixed (recomputed here as small_r_kernel
+// found it; it changes only where an error estimate crosses a threshold), the
+// entry is sum over the partition's GK61 nodes of weight x kernel(k) x P(k), P
+// the Akima spline of the input spectrum: the node cotangents go to the
+// spline's knots through its exact partials.
+__global__ void __launch_bounds__(32 * SR_WARPS)
+    small_r_adjoint_kernel(const double *__restrict__ kx, const double *__restrict__ pk, int nk,
+                           int n_spectra, int n_at, SmallRTerms tm,
+                           const double *__restrict__ tab_x, size_t len,
+                           const double *__restrict__ gY, double *__restrict__ gpk, int *err)
+{
+    __shared__ double sa[SR_WARPS][SR_CAP], sb[SR_WARPS][SR_CAP], sr[SR_WARPS][SR_CAP],
+        se[SR_WARPS][SR_CAP];
+    const int w = threadIdx.x >> 5;
+    const long item = (long)blockIdx.x * SR_WARPS + w;
+    const long total = (long)n_spectra * n_at * (CG_N_SMALL_R + 1);
+    if (item >= total) return;
+    const int j = (int)(item % (CG_N_SMALL_R + 1));
+    const long st_ = item / (CG_N_SMALL_R + 1);
+    const int t = (int)(st_ % n_at);
+    const int s = (int)(st_ / n_at);
+    const double cot = gY[((size_t)s * n_at + t) * len + j];
+    const int n = tm.n[t], l = tm.l[t];
+    if (cot == 0.0 || l < 0 || (j == 0 && n < l)) return; // whole warps leave together
+    const double *ps = pk + (size_t)s * nk;
+    PkAkima P{kx, ps, nk};
+    QagStore<double> store{sa[w], sb[w], sr[w], se[w], SR_CAP};
+    int status = 0, nf = 1;
+    const double kmin = kx[0], kmax = kx[nk - 1];
+    const double r = tab_x[j];
+    double scale;
+    if (j == 0) {
+        PrefactorIntegrand f{P, n, l};
+        qag61_warp<double>(f, kmin, kmax, 0.0, 1e-5, store, 50000, &status, &nf);
+        const double coeff = sqrt(CG_PI / 2.) / pow(2.0, l + 0.5) / tgamma(l + 1.5);
+        scale = coeff / 2. / CG_PI / CG_PI;
+    } else {
+        BesselIntegrand f{P, r, n, l};
+        qag61_warp<double>(f, kmin, kmax, 0.0, 1e-5, store, 50000, &status, &nf);
+        scale = (n >= l ? pow(r, (double)(n - l)) : 1.0) / 2. / CG_PI / CG_PI;
+    }
+    if (status == 1 && (threadIdx.x & 31) == 0) cg_flag(err, CG_ERR_QAG_LIMIT);
+    // the integrand without P(k)
+    auto kernel = [&](double k) {
+        if (j == 0) return pow(k, 2.0 + l - n);
+        return k * k * sph_bessel(l, k * r) / pow(k * r, (double)n);
+    };
+    // one GK61 node at k with weight wgt (the Kronrod result is
+    // half_length x sum wgk f)
+    auto scatter = [&](double k, double wgt) {
+        int lo = 0, hi = nk - 1;
+        while (hi > lo + 1) {
+            const int mid = (lo + hi) / 2;
+            if (kx[mid] > k)
+                hi = mid;
+            else
+                lo = mid;
+        }
+        const D6 v = akima_eval_d6(kx, ps, nk, lo, k);
+        const double g = cot * scale * wgt * kernel(k);
+        double *dst = gpk + (size_t)s * nk + d6_base(nk, lo);
+        for (int q = 0; q < 6; ++q)
+            if (v.g[q] != 0.0) atomicAdd(dst + q, g * v.g[q]);
+    };
+    const GkLane<double> gl = gk_lane<double>();
+    for (int p = 0; p < nf; ++p) {
+        const double a = nf == 1 ? kmin : store.a[p], b = nf == 1 ? kmax : store.b[p];
+        const double center = 0.5 * (a + b), half = 0.5 * (b - a);
+        if (gl.centre) {
+            scatter(center, half * gl.wk);
+        } else if (gl.active) {
+            const double absc = half * gl.x;
+            scatter(center - absc, half * gl.wk);
+            scatter(center + absc, half * gl.wk);
+        }
+    }
+}
+
 // ---------------------------------------------- divergent I^4_0 (integrals.c:773-914)
 // The integrands of the divergent integral: P (1 - j0(kr)^2) / k^2 (its r = 0
 // renormalisation, integrals.c:390-404) and P j0(k chi1) j0(k chi2) / k^2 (the
@@ -1468,7 +1554,9 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     const bool grid_cached = same_grid(ctx, k, nk, N, terms_key);
     // device buffers
     const bool pk_on_device = (flags & COFFE_GPU_PK_DEVICE) != 0;
-    if (!pk_on_device && (st = cg_ensure(ctx, ctx->pk, sizeof(double) * nk * n_spectra))) return st;
+    if ((!pk_on_device || (flags & COFFE_GPU_SMALL_R)) &&
+        (st = cg_ensure(ctx, ctx->pk, sizeof(double) * nk * n_spectra)))
+        return st;
     if ((st = cg_ensure(ctx, ctx->csc, sizeof(double) * nk * n_spectra))) return st;
     if ((st = cg_ensure(ctx, ctx->spec, sizeof(double2) * (M + 1) * (size_t)n_spectra * n_q)))
         return st;
@@ -1534,6 +1622,9 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     if (!pk_on_device)
         CG_CUDA(ctx, cudaMemcpyAsync(ctx->pk.p, pk, sizeof(double) * nk * n_spectra,
                                      cudaMemcpyHostToDevice, ctx->stream));
+    else if (flags & COFFE_GPU_SMALL_R) // kept for the adjoint of the sub-Mpc entries
+        CG_CUDA(ctx, cudaMemcpyAsync(ctx->pk.p, pk, sizeof(double) * nk * n_spectra,
+                                     cudaMemcpyDeviceToDevice, ctx->stream));
 
     double2 *mcoef = (double2 *)ctx->modec.p;
     double *modew = (double *)((char *)ctx->modec.p + sizeof(double2) * (M + 1) * n_terms);
@@ -1930,4 +2021,24 @@ int divergent_run(coffe_gpu_ctx *ctx, const double *k, const double *pk, size_t 
                                      cudaMemcpyDeviceToHost, ctx->stream));
     }
     return cg_check_device_errors(ctx, "divergent integral");
+}
+
+// gY: table cotangents [n_spectra][n_at][N + CG_N_SMALL_R + 1]; adds the part
+// of dL/dP that flows through the r = 0 and sub-Mpc entries to grad_pk
+int small_r_adjoint_run(coffe_gpu_ctx *ctx, const double *gY, int n_at, const int *term,
+                        double *grad_pk)
+{
+    if (n_at > 8) return COFFE_GPU_EINVAL;
+    SmallRTerms tm;
+    for (int t = 0; t < 8; ++t) {
+        tm.n[t] = t < n_at ? ctx->term_n[term[t]] : 0;
+        tm.l[t] = t < n_at ? (ctx->term_half[term[t]] ? -1 : ctx->term_l[term[t]]) : -1;
+    }
+    const long items = (long)ctx->n_spectra * n_at * (CG_N_SMALL_R + 1);
+    const int blocks = (int)((items + SR_WARPS - 1) / SR_WARPS);
+    small_r_adjoint_kernel<<<blocks, 32 * SR_WARPS, 0, ctx->stream>>>(
+        (const double *)ctx->kgrid.p, (const double *)ctx->pk.p, (int)ctx->nk, ctx->n_spectra,
+        n_at, tm, (const double *)ctx->tab_x.p, ctx->N + CG_N_SMALL_R + 1, gY, grad_pk,
+        ctx->d_err);
+    return cg_after_launch(ctx, "small_r_adjoint_kernel");
 }

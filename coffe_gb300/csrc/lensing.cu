@@ -18,7 +18,7 @@
 // Work split (one launch each, per chunk of pairs):
 //   lens_double_kernel  one CTA per (pair, mu node): threads own x1 lines and
 //                       sweep their x2 line; one partial per (pair, mu);
-//   lens_single_kernel  one warp per (pair, mu node), FP64 (lens_single32_kernel
+//   lens_single_kernel  one warp per (pair, mu node), FP64 (lens_single_fast_kernel
 //                       on the mixed path: FP32 with the RSD-lensing
 //                       coefficients expanded so that they cancel nothing);
 //   lens_reduce_kernel  per (pair, l): the mu weights and P_l(mu), summed in a
@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "ctx.cuh"
+#include "dual6.cuh"
 #include "qag.cuh"
 
 namespace {
@@ -175,45 +176,55 @@ __device__ __forceinline__ TT lens_at_zero(const typename Rec4<TT>::type *__rest
 // six tables' records (the interpolant is linear in the records), stored
 // rec5[(s * (len - 1) + i) * 5 + u] for u = I20, S, B, D, E.
 #define LENS_NC 5
-__global__ void lens_combine_kernel(const float4 *__restrict__ rec, long long n_int,
-                                    float4 *__restrict__ rec5)
+template <typename R>
+__global__ void lens_combine_kernel(const R *__restrict__ rec, long long n_int,
+                                    R *__restrict__ rec5)
 {
+    typedef decltype(R::x) E;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_int) return;
-    const float4 *p = rec + i * LENS_NT;
-    const float4 i00 = p[L00], i02 = p[L02], i04 = p[L04], i11 = p[L11], i13 = p[L13],
-                 i20 = p[L20];
-    auto lin = [](float a, float4 x, float b, float4 y, float c, float4 z) {
-        return make_float4(a * x.x + b * y.x + c * z.x, a * x.y + b * y.y + c * z.y,
-                           a * x.z + b * y.z + c * z.z, a * x.w + b * y.w + c * z.w);
+    const R *p = rec + i * LENS_NT;
+    const R i00 = p[L00], i02 = p[L02], i04 = p[L04], i11 = p[L11], i13 = p[L13], i20 = p[L20];
+    auto lin = [](E a, R x, E b, R y, E c, R z) {
+        R o;
+        o.x = a * x.x + b * y.x + c * z.x;
+        o.y = a * x.y + b * y.y + c * z.y;
+        o.z = a * x.z + b * y.z + c * z.z;
+        o.w = a * x.w + b * y.w + c * z.w;
+        return o;
     };
-    float4 *q = rec5 + i * LENS_NC;
+    R *q = rec5 + i * LENS_NC;
     q[0] = i20;
-    q[1] = lin(1.f, i11, 1.f, i13, 0.f, i13);
-    q[2] = lin(0.4f, i00, 4.f / 7.f, i02, 6.f / 35.f, i04);
-    q[3] = lin(6.f / 7.f, i02, 6.f / 7.f, i04, 2.f, i13);
+    q[1] = lin(E(1), i11, E(1), i13, E(0), i13);
+    q[2] = lin(E(0.4), i00, E(4) / E(7), i02, E(6) / E(35), i04);
+    q[3] = lin(E(6) / E(7), i02, E(6) / E(7), i04, E(2), i13);
     q[4] = i04;
 }
 
 // the five combined functions at r (NaN outside the tables)
-__device__ __forceinline__ void lens_tables5(const float4 *__restrict__ recs5,
-                                             const float *__restrict__ x, int n, float inv_dlog,
-                                             float r, float (&v)[LENS_NC])
+template <typename T, typename TT>
+__device__ __forceinline__ void lens_tables5(const typename Rec4<TT>::type *__restrict__ recs5,
+                                             const TT *__restrict__ x, int n, TT inv_dlog, T r,
+                                             T (&v)[LENS_NC])
 {
-    const int i = lens_interval<float>(x, n, inv_dlog, r);
+    const int i = lens_interval<TT>(x, n, inv_dlog, (TT)r);
     if (i < 0) {
 #pragma unroll
-        for (int u = 0; u < LENS_NC; ++u) v[u] = cg_nan<float>();
+        for (int u = 0; u < LENS_NC; ++u) v[u] = cg_nan<T>();
         return;
     }
-    const float dx = r - __ldg(x + i);
-    const float4 *p = recs5 + (size_t)i * LENS_NC;
+    const T dx = r - (T)__ldg(x + i);
+    const typename Rec4<TT>::type *p = recs5 + (size_t)i * LENS_NC;
 #pragma unroll
     for (int u = 0; u < LENS_NC; ++u) {
-        const float4 c = __ldg(p + u);
-        v[u] = c.x + dx * (c.y + dx * (c.z + c.w * dx));
+        const typename Rec4<TT>::type c = ldg_c4(p + u);
+        v[u] = (T)c.x + dx * ((T)c.y + dx * ((T)c.z + (T)c.w * dx));
     }
 }
+
+// a b + c with one rounding, in the working precision
+__device__ __forceinline__ float lens_fma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double lens_fma(double a, double b, double c) { return fma(a, b, c); }
 
 // Geometry of one (pair, mu node), functions.c:1498-1509 / 3473-3481, with
 // cos(theta) = 1 - s, s = sep^2 (1 - mu^2) / (2 chi1 chi2) (no cancellation)
@@ -262,6 +273,7 @@ template <typename T> struct Acc {
 #define LENS_PDEG 9
 struct LensPoly {
     float t[LENS_PDEG + 1];
+    double td[LENS_PDEG + 1];
     double vinv[LENS_PDEG + 1][LENS_PDEG + 1];
 };
 
@@ -273,6 +285,7 @@ LensPoly lens_poly_tables()
     for (int j = 0; j < n; ++j) {
         const double t = cos((2 * j + 1) * CG_PI / (2.0 * n));
         r.t[j] = (float)t;
+        r.td[j] = t;
         double p = 1.0;
         for (int c = 0; c < n; ++c, p *= t) V[j][c] = p;
         for (int c = 0; c < n; ++c) V[j][n + c] = c == j ? 1.0 : 0.0;
@@ -295,27 +308,43 @@ LensPoly lens_poly_tables()
     return r;
 }
 
-__device__ __forceinline__ float lens_horner(const float *c, float t)
+template <typename T> __device__ __forceinline__ T lens_horner(const T *c, T t)
 {
-    float v = c[LENS_PDEG];
+    T v = c[LENS_PDEG];
 #pragma unroll
-    for (int k = LENS_PDEG - 1; k >= 0; --k) v = fmaf(v, t, c[k]);
+    for (int k = LENS_PDEG - 1; k >= 0; --k) v = lens_fma(v, t, c[k]);
     return v;
 }
+// the Chebyshev point t_j of the polynomial fits in the working precision
+template <typename T> __device__ __forceinline__ T lens_cheb(const LensPoly &p, int j);
+template <> __device__ __forceinline__ float lens_cheb<float>(const LensPoly &p, int j)
+{
+    return p.t[j];
+}
+template <> __device__ __forceinline__ double lens_cheb<double>(const LensPoly &p, int j)
+{
+    return p.td[j];
+}
 
-template <typename T, typename S, typename TT>
+// FAST selects the algorithm of the mixed path (D1 / a along both lines of
+// sight as degree-9 polynomials, the integrand regrouped over the five
+// combined records); with T = double it is that algorithm in FP64, the
+// matched-algorithm baseline of the mixed path.  FAST = false: the reference's
+// six-table form with spline lookups per node (the FP64 parity path).
+template <typename T, typename S, typename TT, bool FAST>
 __global__ void __launch_bounds__(LENS_THREADS)
     lens_double_kernel(LensArgs a, LensBg64 g64, LensBgT<S> gT, LensPoly poly,
                        const TT *__restrict__ tab_x,
                        const typename Rec4<TT>::type *__restrict__ rec,
-                       const float4 *__restrict__ rec5,
+                       const typename Rec4<TT>::type *__restrict__ rec5,
                        const int *__restrict__ req_spectrum, const double *__restrict__ req_z_mean,
                        const int64_t *__restrict__ req_offset, const double *__restrict__ sep,
                        const double *__restrict__ rule, double *__restrict__ part, int *err)
 {
+    static_assert(FAST || sizeof(T) == 8, "the FP32 plane kernel has only the fast algorithm");
     __shared__ double red[LENS_THREADS / 32];
-    __shared__ float gval[2][LENS_PDEG + 1];
-    __shared__ float gcoef[2][LENS_PDEG + 1];
+    __shared__ T gval[2][LENS_PDEG + 1];
+    __shared__ T gcoef[2][LENS_PDEG + 1];
     const long long item = blockIdx.x;
     const long long pair = a.pair0 + item / a.n_mu_run;
     const int im = a.mu0 + (int)(item % a.n_mu_run);
@@ -328,8 +357,8 @@ __global__ void __launch_bounds__(LENS_THREADS)
     const double s2 = a.has_s2 ? spl_eval(g64.s2, G.z2c) : 0.0;
     const double pre = 9. * a.Om * a.Om * (2 - 5 * s1) * (2 - 5 * s2) / 4. * G.chi1 * G.chi2 * a.pref4;
     const typename Rec4<TT>::type *recs = rec + (size_t)s * (a.tab_len - 1) * LENS_NT;
-    const float4 *recs5 =
-        sizeof(T) == 4 ? rec5 + (size_t)s * (a.tab_len - 1) * LENS_NC : nullptr;
+    const typename Rec4<TT>::type *recs5 =
+        FAST ? rec5 + (size_t)s * (a.tab_len - 1) * LENS_NC : nullptr;
     const T chi1 = (T)G.chi1, chi2 = (T)G.chi2, ss = (T)G.s, ct = (T)G.ct, c2m = (T)(-G.omc2);
     const T i11_0 = (T)lens_at_zero<TT>(recs, L11);
     const TT inv_dlog = (TT)a.inv_dlog;
@@ -337,19 +366,19 @@ __global__ void __launch_bounds__(LENS_THREADS)
     // mixed path: float copies of the line rules follow the FP64 rule
     const float *xf32 = reinterpret_cast<const float *>(xh + 2 * a.nh);
     const float *wf32 = xf32 + a.n_x, *xh32 = wf32 + a.n_x, *wh32 = xh32 + a.nh;
-    if (F32) { // D1 / a along both lines of sight as polynomials in 2x - 1
+    if (FAST) { // D1 / a along both lines of sight as polynomials in 2x - 1
         if (threadIdx.x < 2 * (LENS_PDEG + 1)) {
             const int side = threadIdx.x / (LENS_PDEG + 1), j = threadIdx.x % (LENS_PDEG + 1);
-            const float lam = (float)(side ? G.chi2 : G.chi1) * 0.5f * (poly.t[j] + 1.f);
-            const float zz = spl_eval(gT.z_of_chi, (T)lam);
-            gval[side][j] = (float)(spl_eval(gT.D1, zz) / spl_eval(gT.a, zz));
+            const T lam = (T)(side ? G.chi2 : G.chi1) * T(0.5) * (lens_cheb<T>(poly, j) + T(1));
+            const T zz = spl_eval(gT.z_of_chi, lam);
+            gval[side][j] = (T)(spl_eval(gT.D1, zz) / spl_eval(gT.a, zz));
         }
         __syncthreads();
         if (threadIdx.x < 2 * (LENS_PDEG + 1)) {
             const int side = threadIdx.x / (LENS_PDEG + 1), j = threadIdx.x % (LENS_PDEG + 1);
             double c = 0.0;
             for (int k = 0; k <= LENS_PDEG; ++k) c += poly.vinv[j][k] * (double)gval[side][k];
-            gcoef[side][j] = (float)c;
+            gcoef[side][j] = (T)c;
         }
         __syncthreads();
     }
@@ -359,8 +388,8 @@ __global__ void __launch_bounds__(LENS_THREADS)
         const T x1 = (T)x1d;
         const T l1 = chi1 * x1;
         T g1;
-        if (F32) {
-            g1 = (T)lens_horner(gcoef[0], (float)(2 * x1 - 1)) * (T(1) - x1);
+        if (FAST) {
+            g1 = lens_horner(gcoef[0], (T)(2 * x1 - 1)) * (T(1) - x1);
         } else {
             const T z1 = spl_eval(gT.z_of_chi, l1);
             g1 = spl_eval(gT.D1, z1) / spl_eval(gT.a, z1) * (T(1) - x1);
@@ -377,16 +406,20 @@ __global__ void __launch_bounds__(LENS_THREADS)
             const float cf = (float)c, hwf = (float)hw;
             Acc<T> pa;
             for (int k = 0; k < np; ++k) {
-                T x2, g2, wk;
+                T x2, wk;
                 if (F32) {
                     x2 = (T)fmaf(hwf, gx32[k], cf);
-                    g2 = (T)lens_horner(gcoef[1], (float)(2 * x2 - 1)) * (T(1) - x2);
                     wk = (T)gw32[k];
                 } else {
                     x2 = (T)(c + hw * gx[k]);
+                    wk = (T)gw[k];
+                }
+                T g2;
+                if (FAST) {
+                    g2 = lens_horner(gcoef[1], (T)(2 * x2 - 1)) * (T(1) - x2);
+                } else {
                     const T z2 = spl_eval(gT.z_of_chi, chi2 * x2);
                     g2 = spl_eval(gT.D1, z2) / spl_eval(gT.a, z2) * (T(1) - x2);
-                    wk = (T)gw[k];
                 }
                 const T l2 = chi2 * x2;
                 const T ll = l1 * l2;
@@ -395,16 +428,16 @@ __global__ void __launch_bounds__(LENS_THREADS)
                 T v;
                 if (r2 > T(1e-20)) {
                     // functions.c:3695-3775
-                    if (F32) { // regrouped in powers of ll over the five combined tables
-                        float Q[LENS_NC];
-                        lens_tables5(recs5, (const float *)tab_x, a.tab_len, (float)inv_dlog,
-                                     (float)sqrt(r2), Q);
+                    if (FAST) { // regrouped in powers of ll over the five combined tables
+                        T Q[LENS_NC];
+                        lens_tables5<T, TT>(recs5, tab_x, a.tab_len, inv_dlog, (T)sqrt(r2), Q);
                         const T ir2 = T(1) / r2;
                         const T lc = ll * c2m * ir2;
-                        const T vA = ct * fmaf(T(4.0 / 15.0) * r2, Q[1], T(4.0 / 3.0) * Q[0]);
-                        const T vB = fmaf(c2m, Q[2], ct * ct * T(8.0 / 5.0) * Q[1]);
-                        const T vD = fmaf(lc, Q[4], ct * Q[3]); // ll c2m E / r^2 + ct D
-                        v = vA + ll * fmaf(lc, vD, vB);
+                        const T vA =
+                            ct * lens_fma(T(4.0 / 15.0) * r2, Q[1], T(4.0 / 3.0) * Q[0]);
+                        const T vB = lens_fma(c2m, Q[2], ct * ct * T(8.0 / 5.0) * Q[1]);
+                        const T vD = lens_fma(lc, Q[4], ct * Q[3]); // ll c2m E / r^2 + ct D
+                        v = vA + ll * lens_fma(lc, vD, vB);
                     } else {
                         T I[LENS_NT];
                         lens_tables<T, TT>(recs, tab_x, a.tab_len, inv_dlog, sqrt(r2), I);
@@ -588,15 +621,19 @@ __global__ void __launch_bounds__(LENS_THREADS)
 // x) - sep mu, d12 = chi1 (1 - x) + sep mu), which keeps its relative precision
 // where lambda_j approaches chi_i.  D1 / a along both lines of sight is the
 // per-item degree-9 polynomial of lens_double_kernel.  The per-item background
-// values are FP64 lookups spread over the lanes (one per lane).
-template <typename S>
+// values are FP64 lookups spread over the lanes (one per lane).  With T =
+// double (tables and line rules in FP64) it is the same algorithm in FP64, the
+// matched-algorithm baseline of the mixed path.
+template <typename T, typename S, typename TT>
 __global__ void __launch_bounds__(LENS_THREADS)
-    lens_single32_kernel(LensArgs a, LensBg64 g, LensBgT<S> gT, LensPoly poly,
-                         const float *__restrict__ tab_x, const float4 *__restrict__ rec,
-                         const int *__restrict__ req_spectrum,
-                         const double *__restrict__ req_z_mean,
-                         const int64_t *__restrict__ req_offset, const double *__restrict__ sep,
-                         const double *__restrict__ rule, double *__restrict__ part, int *err)
+    lens_single_fast_kernel(LensArgs a, LensBg64 g, LensBgT<S> gT, LensPoly poly,
+                            const TT *__restrict__ tab_x,
+                            const typename Rec4<TT>::type *__restrict__ rec,
+                            const int *__restrict__ req_spectrum,
+                            const double *__restrict__ req_z_mean,
+                            const int64_t *__restrict__ req_offset,
+                            const double *__restrict__ sep, const double *__restrict__ rule,
+                            double *__restrict__ part, int *err)
 {
     const long long item = (long long)blockIdx.x * (LENS_THREADS / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
@@ -626,74 +663,77 @@ __global__ void __launch_bounds__(LENS_THREADS)
     const double f1c = __shfl_sync(full, bv, 4), f2c = __shfl_sync(full, bv, 5);
     const double D1z1c = __shfl_sync(full, bv, 6), D1z2c = __shfl_sync(full, bv, 7);
     // D1 / a along both lines of sight: lanes 0-9 side 1 (chi1), 10-19 side 2
-    float gc1[LENS_PDEG + 1], gc2[LENS_PDEG + 1];
+    T gc1[LENS_PDEG + 1], gc2[LENS_PDEG + 1];
     {
         const int side = lane >= LENS_PDEG + 1, j = lane % (LENS_PDEG + 1);
-        float gv = 0.f;
+        T gv = T(0);
         if (lane < 2 * (LENS_PDEG + 1)) {
-            const float lam = (float)(side ? chi2 : chi1) * 0.5f * (poly.t[j] + 1.f);
-            const float zz = spl_eval(gT.z_of_chi, lam);
+            const T lam = (T)(side ? chi2 : chi1) * T(0.5) * (lens_cheb<T>(poly, j) + T(1));
+            const T zz = spl_eval(gT.z_of_chi, lam);
             gv = spl_eval(gT.D1, zz) / spl_eval(gT.a, zz);
         }
         double c = 0.0;
 #pragma unroll
         for (int k = 0; k <= LENS_PDEG; ++k)
             c += poly.vinv[j][k] * (double)__shfl_sync(full, gv, side * (LENS_PDEG + 1) + k);
-        const float cf = (float)c;
+        const T cf = (T)c;
 #pragma unroll
         for (int k = 0; k <= LENS_PDEG; ++k) {
             gc1[k] = __shfl_sync(full, cf, k);
             gc2[k] = __shfl_sync(full, cf, LENS_PDEG + 1 + k);
         }
     }
-    const float4 *recs = rec + (size_t)s * (a.tab_len - 1) * LENS_NT;
-    const float inv_dlog = (float)a.inv_dlog;
-    const float I00_0 = lens_at_zero<float>(recs, L00), I11_0 = lens_at_zero<float>(recs, L11);
-    const float c1 = (float)chi1, c2 = (float)chi2, dchi = (float)(r * mu), ss = (float)sd;
-    const float ct = (float)(1 - sd), omc2 = (float)(sd * (2 - sd));
-    const float c2m1 = (float)(1 - 2 * sd * (2 - sd));
+    const typename Rec4<TT>::type *recs = rec + (size_t)s * (a.tab_len - 1) * LENS_NT;
+    const TT inv_dlog = (TT)a.inv_dlog;
+    const T I00_0 = (T)lens_at_zero<TT>(recs, L00), I11_0 = (T)lens_at_zero<TT>(recs, L11);
+    const T c1 = (T)chi1, c2 = (T)chi2, dchi = (T)(r * mu), ss = (T)sd;
+    const T ct = (T)(1 - sd), omc2 = (T)(sd * (2 - sd));
+    const T c2m1 = (T)(1 - 2 * sd * (2 - sd));
     const bool den = a.contrib & COFFE_GPU_DEN, rsd = a.contrib & COFFE_GPU_RSD;
     const bool wide = fabs(mu) < 0.999;
     // functions.c:1708-1780 and 2174-2306 with the background factors folded
     const double kc = a.pref2 * 1.5 * a.Om;
-    const float kd2 = (float)(-kc * b1 * (2 - 5 * s2) * D1z1c * chi1 * chi2);
-    const float kd1 = (float)(-kc * b2 * (2 - 5 * s1) * D1z2c * chi1 * chi2);
-    const float kr2 = (float)(kc * chi2 * f1c * (2 - 5 * s2) * D1z1c);
-    const float kr1 = (float)(kc * chi1 * f2c * (2 - 5 * s1) * D1z2c);
-    auto Q = [&](float ch, float d) {
-        return d * d * d * (8.f - 24.f * ss + 12.f * ss * ss) +
-               ch * d * d * (-2.f + 38.f * ss - 18.f * ss * ss - 6.f * ss * ss * ss) +
-               ch * ch * d * ss * (-22.f + 9.f * ss + 12.f * ss * ss) +
-               ch * ch * ch * ss * (2.f - 3.f * ss - 6.f * ss * ss);
+    const T kd2 = (T)(-kc * b1 * (2 - 5 * s2) * D1z1c * chi1 * chi2);
+    const T kd1 = (T)(-kc * b2 * (2 - 5 * s1) * D1z2c * chi1 * chi2);
+    const T kr2 = (T)(kc * chi2 * f1c * (2 - 5 * s2) * D1z1c);
+    const T kr1 = (T)(kc * chi1 * f2c * (2 - 5 * s1) * D1z2c);
+    auto Q = [&](T ch, T d) {
+        return d * d * d * (T(8) - T(24) * ss + T(12) * ss * ss) +
+               ch * d * d * (T(-2) + T(38) * ss - T(18) * ss * ss - T(6) * ss * ss * ss) +
+               ch * ch * d * ss * (T(-22) + T(9) * ss + T(12) * ss * ss) +
+               ch * ch * ch * ss * (T(2) - T(3) * ss - T(6) * ss * ss);
     };
-    auto P = [&](float ch, float d) {
-        const float d2 = d * d, d3 = d2 * d, d4 = d2 * d2, d5 = d4 * d;
-        const float ch2 = ch * ch, ch3 = ch2 * ch, ch4 = ch2 * ch2, ch5 = ch4 * ch;
-        const float s2 = ss * ss, s3 = s2 * ss;
-        return d5 * (4.f - 12.f * ss + 6.f * s2) + ch * d4 * (-8.f + 60.f * ss - 48.f * s2 + 6.f * s3) +
-               ch2 * d3 * ss * (-92.f + 114.f * ss - 20.f * s2 - s3) +
-               ch3 * d2 * ss * (48.f - 120.f * ss + 26.f * s2 + 3.f * s3) +
-               ch4 * d * s2 * (60.f - 16.f * ss - 3.f * s2) + ch5 * s2 * (-12.f + 4.f * ss + s2);
+    auto P = [&](T ch, T d) {
+        const T d2 = d * d, d3 = d2 * d, d4 = d2 * d2, d5 = d4 * d;
+        const T ch2 = ch * ch, ch3 = ch2 * ch, ch4 = ch2 * ch2, ch5 = ch4 * ch;
+        const T s2 = ss * ss, s3 = s2 * ss;
+        return d5 * (T(4) - T(12) * ss + T(6) * s2) +
+               ch * d4 * (T(-8) + T(60) * ss - T(48) * s2 + T(6) * s3) +
+               ch2 * d3 * ss * (T(-92) + T(114) * ss - T(20) * s2 - s3) +
+               ch3 * d2 * ss * (T(48) - T(120) * ss + T(26) * s2 + T(3) * s3) +
+               ch4 * d * s2 * (T(60) - T(16) * ss - T(3) * s2) +
+               ch5 * s2 * (T(-12) + T(4) * ss + s2);
     };
     // one side: density and RSD parts times D1 / a, without the (1 - x) factor
-    auto side_val = [&](float ch, float la, float d, float r2, const float *I, float kd, float kr,
-                        float gl) {
-        float v = 0.f;
-        if (r2 != 0.f) {
-            const float ir2 = 1.f / r2;
-            if (den) v += kd * (2.f * ct * I[L11] - ch * la * omc2 * I[L02] * ir2);
+    auto side_val = [&](T ch, T la, T d, T r2, const T *I, T kd, T kr, T gl) {
+        T v = T(0);
+        if (r2 != T(0)) {
+            const T ir2 = T(1) / r2;
+            if (den) v += kd * (T(2) * ct * I[L11] - ch * la * omc2 * I[L02] * ir2);
             if (rsd) {
-                v += kr * ((la - 6.f * ch * ct + 3.f * la * c2m1) * I[L00] * (1.f / 15.f) -
-                           Q(ch, d) * I[L02] * ir2 * (1.f / 21.f));
-                v += kr * (wide ? -P(ch, d) * I[L04] * ir2 * ir2 * (1.f / 35.f)
-                                : 4.f * (la + ch) * I[L04] * (1.f / 35.f));
+                v += kr * ((la - T(6) * ch * ct + T(3) * la * c2m1) * I[L00] * (T(1) / T(15)) -
+                           Q(ch, d) * I[L02] * ir2 * (T(1) / T(21)));
+                v += kr * (wide ? -P(ch, d) * I[L04] * ir2 * ir2 * (T(1) / T(35))
+                                : T(4) * (la + ch) * I[L04] * (T(1) / T(35)));
             }
         } else {
-            if (den) v += kd * 2.f * I11_0;
-            if (rsd) v += kr * (-2.f * ch * I00_0 * (1.f / 15.f));
+            if (den) v += kd * T(2) * I11_0;
+            if (rsd) v += kr * (T(-2) * ch * I00_0 * (T(1) / T(15)));
         }
         return v * gl;
     };
+    constexpr bool F32 = sizeof(T) == 4;
+    const double *xf = rule + 2 * a.n_mu, *wf = xf + a.n_x, *xh = wf + a.n_x, *wh = xh + a.nh;
     const float *xf32 = reinterpret_cast<const float *>(rule + 2 * a.n_mu + 2 * a.n_x + 2 * a.nh);
     const float *wf32 = xf32 + a.n_x, *xh32 = wf32 + a.n_x, *wh32 = xh32 + a.nh;
     const double xs = fmin(chi1, chi2) * (1 - sd) / fmax(chi1, chi2);
@@ -701,24 +741,27 @@ __global__ void __launch_bounds__(LENS_THREADS)
     double sum = 0;
     for (int p = 0; p < (split ? 2 : 1); ++p) {
         const double lo = (split && p) ? xs : 0.0, hi = (split && !p) ? xs : 1.0;
-        const float cf = (float)(0.5 * (lo + hi)), omcf = (float)(1 - 0.5 * (lo + hi));
-        const float hwf = (float)(0.5 * (hi - lo));
+        const T cf = (T)(0.5 * (lo + hi)), omcf = (T)(1 - 0.5 * (lo + hi));
+        const T hwf = (T)(0.5 * (hi - lo));
         const int np = split ? a.nh : a.n_x;
-        const float *gx = split ? xh32 : xf32, *gw = split ? wh32 : wf32;
-        Acc<float> ps;
+        const float *gx32 = split ? xh32 : xf32, *gw32 = split ? wh32 : wf32;
+        const double *gx64 = split ? xh : xf, *gw64 = split ? wh : wf;
+        Acc<T> ps;
         for (int k = lane; k < np; k += 32) {
-            const float x = fmaf(hwf, gx[k], cf), omx = fmaf(-hwf, gx[k], omcf);
-            const float t = 2.f * x - 1.f;
-            const float la1 = c1 * x, la2 = c2 * x;
-            const float d21 = fmaf(c2, omx, -dchi), d12 = fmaf(c1, omx, dchi);
-            const float r21 = d21 * d21 + 2.f * c1 * la2 * ss;
-            const float r22 = d12 * d12 + 2.f * c2 * la1 * ss;
-            float I1[LENS_NT], I2[LENS_NT];
-            lens_tables<float, float>(recs, tab_x, a.tab_len, inv_dlog, sqrtf(r21), I1);
-            lens_tables<float, float>(recs, tab_x, a.tab_len, inv_dlog, sqrtf(r22), I2);
-            const float v = side_val(c1, la2, d21, r21, I1, kd2, kr2, lens_horner(gc2, t)) +
-                            side_val(c2, la1, d12, r22, I2, kd1, kr1, lens_horner(gc1, t));
-            ps.add(gw[k] * omx * v);
+            const T gxk = F32 ? (T)gx32[k] : (T)gx64[k];
+            const T gwk = F32 ? (T)gw32[k] : (T)gw64[k];
+            const T x = lens_fma(hwf, gxk, cf), omx = lens_fma(-hwf, gxk, omcf);
+            const T t = T(2) * x - T(1);
+            const T la1 = c1 * x, la2 = c2 * x;
+            const T d21 = lens_fma(c2, omx, -dchi), d12 = lens_fma(c1, omx, dchi);
+            const T r21 = d21 * d21 + T(2) * c1 * la2 * ss;
+            const T r22 = d12 * d12 + T(2) * c2 * la1 * ss;
+            T I1[LENS_NT], I2[LENS_NT];
+            lens_tables<T, TT>(recs, tab_x, a.tab_len, inv_dlog, sqrt(r21), I1);
+            lens_tables<T, TT>(recs, tab_x, a.tab_len, inv_dlog, sqrt(r22), I2);
+            const T v = side_val(c1, la2, d21, r21, I1, kd2, kr2, lens_horner(gc2, t)) +
+                        side_val(c2, la1, d12, r22, I2, kd1, kr1, lens_horner(gc1, t));
+            ps.add(gwk * omx * v);
         }
         sum += (double)hwf * warp_sum(ps.value());
     }
@@ -942,7 +985,7 @@ double host_fact(int n)
     return r;
 }
 
-template <typename T, typename S, typename TT>
+template <typename T, typename S, typename TT, bool FAST>
 int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const LensBgT<S> &gT,
                    const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
                    const double *sep, double *out, long long total, bool do_single,
@@ -953,18 +996,17 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
     const TT *tab_x = (const TT *)(sizeof(TT) == 8 ? ctx->tab_x.p : ctx->tab_x32.p);
     const long long n_int = (long long)ctx->n_spectra * (a.tab_len - 1);
     const long long n_rec = n_int * LENS_NT;
-    // float path: the five combined records follow the six tables' records
-    const size_t rec_bytes = sizeof(R) * (size_t)n_rec +
-                             (sizeof(T) == 4 ? sizeof(float4) * (size_t)n_int * LENS_NC : 0);
+    // fast algorithm: the five combined records follow the six tables' records
+    const size_t rec_bytes = sizeof(R) * (size_t)(n_rec + (FAST ? n_int * LENS_NC : 0));
     if ((st = cg_ensure(ctx, ctx->lens_rec, rec_bytes))) return st;
     R *rec = (R *)ctx->lens_rec.p;
-    float4 *rec5 = sizeof(T) == 4 ? (float4 *)(rec + n_rec) : nullptr;
+    R *rec5 = FAST ? rec + n_rec : nullptr;
     lens_records_kernel<TT><<<(unsigned)((n_rec + 255) / 256), 256, 0, ctx->stream>>>(
         a, tab_x, (const TT *)ctx->tab_y.p, ctx->n_spectra, rec);
     if ((st = cg_after_launch(ctx, "lens_records_kernel"))) return st;
-    if (rec5 && do_double) {
-        lens_combine_kernel<<<(unsigned)((n_int + 255) / 256), 256, 0, ctx->stream>>>(
-            (const float4 *)rec, n_int, rec5);
+    if (FAST && do_double) {
+        lens_combine_kernel<R><<<(unsigned)((n_int + 255) / 256), 256, 0, ctx->stream>>>(
+            rec, n_int, rec5);
         if ((st = cg_after_launch(ctx, "lens_combine_kernel"))) return st;
     }
     const bool single = do_single;
@@ -980,17 +1022,19 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
         a.pair0 = p0;
         a.n_items = np * a.n_mu_run;
         if (do_double) {
-            lens_double_kernel<T, S, TT><<<(unsigned)a.n_items, LENS_THREADS, 0, ctx->stream>>>(
+            lens_double_kernel<T, S, TT, FAST>
+                <<<(unsigned)a.n_items, LENS_THREADS, 0, ctx->stream>>>(
                 a, g64, gT, poly, tab_x, rec, rec5, req_spectrum, req_z_mean, req_offset, sep,
                 rule, part_d, ctx->d_err);
             if ((st = cg_after_launch(ctx, "lens_double_kernel"))) return st;
         }
         if (single) {
             const long long blocks = (a.n_items + LENS_THREADS / 32 - 1) / (LENS_THREADS / 32);
-            if constexpr (sizeof(T) == 4)
-                lens_single32_kernel<S><<<(unsigned)blocks, LENS_THREADS, 0, ctx->stream>>>(
-                    a, g64, gT, poly, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule,
-                    part_s, ctx->d_err);
+            if constexpr (FAST)
+                lens_single_fast_kernel<T, S, TT>
+                    <<<(unsigned)blocks, LENS_THREADS, 0, ctx->stream>>>(
+                        a, g64, gT, poly, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep,
+                        rule, part_s, ctx->d_err);
             else
                 lens_single_kernel<TT><<<(unsigned)blocks, LENS_THREADS, 0, ctx->stream>>>(
                     a, g64, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule, part_s,
@@ -1011,6 +1055,380 @@ int lensing_launch(coffe_gpu_ctx *ctx, LensArgs a, const LensBg64 &g64, const Le
         }
     }
     return COFFE_GPU_OK;
+}
+
+// ----------------------------------------------------------------- adjoint
+// Reverse mode of the full-sky lensing multipoles in FP64 (the parity path's
+// six-table integrands, the same rules, mu symmetry and weights).  The
+// integrands are linear in the table values; a table value at r in interval i
+// is y_i + b dx + c dx^2 + d dx^3 of that interval's Akima record, so the
+// cotangent of the records is accumulated as the four moments
+// gR[((s * LENS_NT + t) * (len - 1) + i) * 4 + p] = sum g dx^p over the
+// lookups, and adj_lens_records_kernel carries it to the table knots.
+
+// cotangent of each (pair, mu node) partial of this chunk: the weight with
+// which lens_reduce_kernel adds the partial to each multipole, times grad_out
+__global__ void adj_lens_gpm_kernel(LensArgs a, const double *__restrict__ rule,
+                                    const double *__restrict__ grad_out, long long n_pairs,
+                                    double *__restrict__ gpm)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_pairs * a.n_mu_run) return;
+    const long long pl = t / a.n_mu_run;
+    const int im = a.mu0 + (int)(t % a.n_mu_run);
+    double g = 0.0;
+    for (int j = 0; j < a.n_l; ++j) {
+        const int l = a.ls[j];
+        const bool half = a.sym && l % 2 == 0 && a.n_mu_run == a.n_mu;
+        const int first = half ? a.n_mu / 2 : a.mu0;
+        if (im < first) continue;
+        const double w = (half ? 2.0 : a.mu_w) * 0.5;
+        g += grad_out[(a.pair0 + pl) * a.n_l + j] * (2 * l + 1) * w * rule[a.n_mu + im] *
+             lens_legendre(l, rule[im]);
+    }
+    gpm[t] = g;
+}
+
+__device__ __forceinline__ void adj_rec_add(double *gR, long long at, double g, double dx)
+{
+    if (g == 0.0) return;
+    const double g1 = g * dx, g2 = g1 * dx;
+    atomicAdd(gR + at, g);
+    atomicAdd(gR + at + 1, g1);
+    atomicAdd(gR + at + 2, g2);
+    atomicAdd(gR + at + 3, g2 * dx);
+}
+
+// table value at r from the FP64 records; interval and offset for the moments
+__device__ __forceinline__ double adj_table_at(const double4_32a *__restrict__ recs, int i, int t,
+                                               double dx)
+{
+    const double4_32a c = ldg_c4(recs + (size_t)i * LENS_NT + t);
+    return c.x + dx * (c.y + dx * (c.z + c.w * dx));
+}
+
+// lensing-lensing partial of one (pair, mu node) (lens_double_kernel's FP64
+// form) and, with gpm, the record cotangents of its lookups
+__global__ void __launch_bounds__(LENS_THREADS)
+    adj_lens_double_kernel(LensArgs a, LensBg64 g64, LensBgT<Spl64> gT,
+                           const double *__restrict__ tab_x, const double4_32a *__restrict__ rec,
+                           const int *__restrict__ req_spectrum,
+                           const double *__restrict__ req_z_mean,
+                           const int64_t *__restrict__ req_offset, const double *__restrict__ sep,
+                           const double *__restrict__ rule, const double *__restrict__ gpm,
+                           double *__restrict__ part, double *__restrict__ gR, int *err)
+{
+    __shared__ double red[LENS_THREADS / 32];
+    const long long item = blockIdx.x;
+    const long long pair = a.pair0 + item / a.n_mu_run;
+    const int im = a.mu0 + (int)(item % a.n_mu_run);
+    const int q = lens_find_request(req_offset, a.n_req, pair);
+    const int s = req_spectrum[q];
+    const double *xf = rule + 2 * a.n_mu, *wf = xf + a.n_x, *xh = wf + a.n_x, *wh = xh + a.nh;
+    const LensGeom G = lens_geom(g64, req_z_mean[q], rule[im], sep[pair]);
+    const double s1 = a.has_s1 ? spl_eval(g64.s1, G.z1c) : 0.0;
+    const double s2 = a.has_s2 ? spl_eval(g64.s2, G.z2c) : 0.0;
+    const double pre = 9. * a.Om * a.Om * (2 - 5 * s1) * (2 - 5 * s2) / 4. * G.chi1 * G.chi2 * a.pref4;
+    const int ni = a.tab_len - 1;
+    const double4_32a *recs = rec + (size_t)s * ni * LENS_NT;
+    double *gRs = gR ? gR + (size_t)s * LENS_NT * ni * 4 : nullptr;
+    const double chi1 = G.chi1, chi2 = G.chi2, ss = G.s, ct = G.ct, c2m = -G.omc2;
+    const double i11_0 = lens_at_zero<double>(recs, L11);
+    const double gp = gpm ? gpm[item] * pre : 0.0;
+    Acc<double> acc;
+    for (int ia = threadIdx.x; ia < a.n_x; ia += blockDim.x) {
+        const double x1 = 0.5 * (xf[ia] + 1.0);
+        const double l1 = chi1 * x1;
+        const double z1 = spl_eval(gT.z_of_chi, l1);
+        const double g1 = spl_eval(gT.D1, z1) / spl_eval(gT.a, z1) * (1 - x1);
+        const double xs = x1 * G.chi1 / G.chi2;
+        const bool split = a.nh > 0 && xs > 0 && xs < 1;
+        double line = 0.0;
+        for (int p = 0; p < (split ? 2 : 1); ++p) {
+            const double lo = (split && p) ? xs : 0.0, hi = (split && !p) ? xs : 1.0;
+            const double c = 0.5 * (lo + hi), hw = 0.5 * (hi - lo);
+            const int np = split ? a.nh : a.n_x;
+            const double *gx = split ? xh : xf, *gw = split ? wh : wf;
+            const double gl = gp * 0.5 * wf[ia] * g1 * hw;
+            Acc<double> pa;
+            for (int k = 0; k < np; ++k) {
+                const double x2 = c + hw * gx[k], wk = gw[k];
+                const double z2 = spl_eval(gT.z_of_chi, chi2 * x2);
+                const double g2 = spl_eval(gT.D1, z2) / spl_eval(gT.a, z2) * (1 - x2);
+                const double l2 = chi2 * x2;
+                const double ll = l1 * l2;
+                const double dl = l1 - l2;
+                const double r2 = dl * dl + 2 * ll * ss;
+                const double gn = gl * wk * g2; // cotangent of v at this node
+                double v;
+                if (r2 > 1e-20) {
+                    // functions.c:3695-3775 as a linear form in the six tables
+                    double cof[LENS_NT];
+                    cof[L00] = 2 * c2m * ll / 5;
+                    cof[L20] = 4 * ct / 3;
+                    cof[L11] = 4 * ct * (r2 + 6 * ct * ll) / 15;
+                    cof[L02] = 2 * c2m * ll * (2 * r2 + 3 * ct * ll) / 7 / r2;
+                    cof[L13] = 2 * ct * (2 * r2 * r2 + 12 * ct * r2 * ll + 15 * c2m * ll * ll) / 15 / r2;
+                    cof[L04] = c2m * ll * (6 * r2 * r2 + 30 * ct * r2 * ll + 35 * c2m * ll * ll) / 35 /
+                               r2 / r2;
+                    const double r = sqrt(r2);
+                    const int i = lens_interval<double>(tab_x, a.tab_len, a.inv_dlog, r);
+                    if (i < 0) {
+                        v = cg_nan<double>();
+                    } else {
+                        const double dx = r - tab_x[i];
+                        v = 0.0;
+#pragma unroll
+                        for (int t = 0; t < LENS_NT; ++t) v += cof[t] * adj_table_at(recs, i, t, dx);
+                        if (gRs)
+#pragma unroll
+                            for (int t = 0; t < LENS_NT; ++t)
+                                adj_rec_add(gRs, ((long long)t * ni + i) * 4, gn * cof[t], dx);
+                    }
+                } else {
+                    // functions.c:3801-3833
+                    v = 4 + 24 * ll * i11_0 / 15;
+                    if (gRs && gn != 0.0)
+                        atomicAdd(gRs + (long long)L11 * ni * 4, gn * 24 * ll / 15);
+                }
+                pa.add(wk * g2 * v);
+            }
+            line += hw * pa.value();
+        }
+        acc.add(0.5 * wf[ia] * g1 * line);
+    }
+    double tot = warp_sum(acc.value());
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = tot;
+    __syncthreads();
+    if (threadIdx.x == 0 && part) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        const double res = pre * t;
+        if (!isfinite(res)) cg_flag(err, CG_ERR_NONFINITE);
+        part[item] = res;
+    }
+}
+
+// The single-integrated den and RSD parts at (mu, x) (lens_single_xi) as
+// linear forms in the six tables at r21 (c1), at r22 (c2) and in I11(0),
+// I00(0)
+struct AdjSingleCoef {
+    double den1[LENS_NT], den2[LENS_NT], rsd1[LENS_NT], rsd2[LENS_NT];
+    double den_i11_0, rsd_i00_0;
+};
+
+__device__ void adj_single_coef(const LensArgs &a, const LensGeom &G, double x, double lambda1,
+                                double lambda2, double r21, double r22, double b1, double b2,
+                                double s1, double s2, double f1c, double f2c, double D1z1c,
+                                double D1z2c, double ga1, double ga2, double mu,
+                                AdjSingleCoef &k)
+{
+    // ga1 = D1 / a at lambda1, ga2 at lambda2
+    for (int t = 0; t < LENS_NT; ++t) k.den1[t] = k.den2[t] = k.rsd1[t] = k.rsd2[t] = 0.0;
+    k.den_i11_0 = k.rsd_i00_0 = 0.0;
+    const double chi1 = G.chi1, chi2 = G.chi2, ct = G.ct, omc2 = G.omc2;
+    if (a.contrib & COFFE_GPU_DEN) {
+        const double K1 = a.pref2 * (-3 * a.Om / 2.) * b1 * (2 - 5 * s2) * D1z1c * (1 - x) * ga2;
+        const double K2 = a.pref2 * (-3 * a.Om / 2.) * b2 * (2 - 5 * s1) * D1z2c * (1 - x) * ga1;
+        if (r21 != 0.0) {
+            k.den1[L11] = K1 * chi2 * 2 * chi1 * ct;
+            k.den1[L02] = -K1 * chi2 * chi1 * chi1 * lambda2 * omc2 / r21;
+        } else {
+            k.den_i11_0 += K1 * chi2 * 2 * chi1;
+        }
+        if (r22 != 0.0) {
+            k.den2[L11] = K2 * chi1 * 2 * chi2 * ct;
+            k.den2[L02] = -K2 * chi1 * chi2 * chi2 * lambda1 * omc2 / r22;
+        } else {
+            k.den_i11_0 += K2 * chi1 * 2 * chi2;
+        }
+    }
+    if (a.contrib & COFFE_GPU_RSD) {
+        const double c2m1 = 2 * ct * ct - 1;
+        const double ss = G.s;
+        auto Q = [&](double ch, double d) {
+            return d * d * d * (8 - 24 * ss + 12 * ss * ss) +
+                   ch * d * d * (-2 + 38 * ss - 18 * ss * ss - 6 * ss * ss * ss) +
+                   ch * ch * d * ss * (-22 + 9 * ss + 12 * ss * ss) +
+                   ch * ch * ch * ss * (2 - 3 * ss - 6 * ss * ss);
+        };
+        auto P = [&](double ch, double d) {
+            const double d2 = d * d, d3 = d2 * d, d4 = d2 * d2, d5 = d4 * d;
+            const double ch2 = ch * ch, ch3 = ch2 * ch, ch4 = ch2 * ch2, ch5 = ch4 * ch;
+            const double sq = ss * ss, s3 = sq * ss;
+            return d5 * (4 - 12 * ss + 6 * sq) + ch * d4 * (-8 + 60 * ss - 48 * sq + 6 * s3) +
+                   ch2 * d3 * ss * (-92 + 114 * ss - 20 * sq - s3) +
+                   ch3 * d2 * ss * (48 - 120 * ss + 26 * sq + 3 * s3) +
+                   ch4 * d * sq * (60 - 16 * ss - 3 * sq) + ch5 * sq * (-12 + 4 * ss + sq);
+        };
+        // A: I00 and I02 parts, B: I04 part of one side (functions.c:2174-2183, 2298-2306)
+        auto addA = [&](double *co, double w, double ch, double la, double r2) {
+            co[L00] += w * (la - 6 * ch * ct + 3 * la * c2m1) / 15.;
+            co[L02] += -w * Q(ch, ch - la) / r2 / 21.;
+        };
+        auto addB = [&](double *co, double w, double ch, double la, double r2) {
+            co[L04] += -w * P(ch, ch - la) / r2 / r2 / 35.;
+        };
+        const double w2 = chi2 * f1c * (2 - 5 * s2) * D1z1c * ga2;
+        const double w1 = chi1 * f2c * (2 - 5 * s1) * D1z2c * ga1;
+        const double c = a.pref2 * 3 * a.Om / 2.;
+        const double e2 = c * w2 * (1 - x), e1 = c * w1 * (1 - x);
+        if (r21 != 0 && r22 != 0) {
+            addA(k.rsd1, e2, chi1, lambda2, r21);
+            addA(k.rsd2, e1, chi2, lambda1, r22);
+            if (fabs(mu) < 0.999) {
+                addB(k.rsd1, e2, chi1, lambda2, r21);
+                addB(k.rsd2, e1, chi2, lambda1, r22);
+            } else {
+                k.rsd1[L04] += e2 * 4. * (lambda2 + chi1) / 35.;
+                k.rsd2[L04] += e1 * 4. * (lambda1 + chi2) / 35.;
+            }
+        } else if (r21 == 0 && r22 != 0) {
+            k.rsd_i00_0 += c * w2 * (1 - chi1 / chi2) * (-2 * chi1 / 15.);
+            addA(k.rsd2, e1, chi2, lambda1, r22);
+            addB(k.rsd2, e1, chi2, lambda1, r22);
+        } else if (r21 != 0 && r22 == 0) {
+            addA(k.rsd1, e2, chi1, lambda2, r21);
+            addB(k.rsd1, e2, chi1, lambda2, r21);
+            k.rsd_i00_0 += c * w1 * (1 - chi2 / chi1) * (-2 * chi2 / 15.);
+        } else {
+            k.rsd_i00_0 += c * w2 * (1 - chi1 / chi2) * (-2 * chi1 / 15.) +
+                           c * w1 * (1 - chi2 / chi1) * (-2 * chi2 / 15.);
+        }
+    }
+}
+
+// single-integrated partial of one (pair, mu node) with the per-request bias
+// (den) and growth (RSD) scales, one warp (lens_single_kernel); with gpm the
+// record cotangents and the bias / growth-scale cotangents
+__global__ void __launch_bounds__(LENS_THREADS)
+    adj_lens_single_kernel(LensArgs a, LensBg64 g, const double *__restrict__ tab_x,
+                           const double4_32a *__restrict__ rec,
+                           const int *__restrict__ req_spectrum,
+                           const double *__restrict__ req_z_mean,
+                           const int64_t *__restrict__ req_offset, const double *__restrict__ sep,
+                           const double *__restrict__ rule, const double *__restrict__ bias_scale,
+                           const double *__restrict__ growth_scale,
+                           const double *__restrict__ gpm, double *__restrict__ part,
+                           double *__restrict__ gR, double *__restrict__ g_bias,
+                           double *__restrict__ g_growth, int *err)
+{
+    const long long item = (long long)blockIdx.x * (LENS_THREADS / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (item >= a.n_items) return;
+    const long long pair = a.pair0 + item / a.n_mu_run;
+    const int im = a.mu0 + (int)(item % a.n_mu_run);
+    const int q = lens_find_request(req_offset, a.n_req, pair);
+    const int s = req_spectrum[q];
+    const double beta = bias_scale ? bias_scale[q] : 1.0;
+    const double alpha = growth_scale ? growth_scale[q] : 1.0;
+    const double *xf = rule + 2 * a.n_mu, *wf = xf + a.n_x, *xh = wf + a.n_x, *wh = xh + a.nh;
+    const double mu = rule[im];
+    const LensGeom G = lens_geom(g, req_z_mean[q], mu, sep[pair]);
+    const double b1 = a.has_b1 ? spl_eval(g.b1, G.z1c) : 1.0;
+    const double b2 = a.has_b2 ? spl_eval(g.b2, G.z2c) : 1.0;
+    const double s1 = a.has_s1 ? spl_eval(g.s1, G.z1c) : 0.0;
+    const double s2 = a.has_s2 ? spl_eval(g.s2, G.z2c) : 0.0;
+    const double f1c = spl_eval(g.f, G.z1c), f2c = spl_eval(g.f, G.z2c);
+    const double D1z1c = spl_eval(g.D1, G.z1c), D1z2c = spl_eval(g.D1, G.z2c);
+    const int ni = a.tab_len - 1;
+    const double4_32a *recs = rec + (size_t)s * ni * LENS_NT;
+    double *gRs = gR ? gR + (size_t)s * LENS_NT * ni * 4 : nullptr;
+    const double I00_0 = lens_at_zero<double>(recs, L00), I11_0 = lens_at_zero<double>(recs, L11);
+    const double gi = gpm ? gpm[item] : 0.0;
+    const double xs = fmin(G.chi1, G.chi2) * G.ct / fmax(G.chi1, G.chi2);
+    const bool split = a.nh > 0 && xs > 0 && xs < 1;
+    double den_sum = 0, rsd_sum = 0;
+    for (int p = 0; p < (split ? 2 : 1); ++p) {
+        const double lo = (split && p) ? xs : 0.0, hi = (split && !p) ? xs : 1.0;
+        const double c = 0.5 * (lo + hi), hw = 0.5 * (hi - lo);
+        const int np = split ? a.nh : a.n_x;
+        const double *gx = split ? xh : xf, *gw = split ? wh : wf;
+        double pd = 0, pr = 0;
+        for (int k = lane; k < np; k += 32) {
+            const double x = c + hw * gx[k];
+            const double lambda1 = G.chi1 * x, lambda2 = G.chi2 * x;
+            double r21 = (lambda2 - G.chi1) * (lambda2 - G.chi1) + 2 * G.chi1 * lambda2 * G.s;
+            double r22 = (lambda1 - G.chi2) * (lambda1 - G.chi2) + 2 * G.chi2 * lambda1 * G.s;
+            if (r21 < 0) r21 = 0;
+            if (r22 < 0) r22 = 0;
+            const double z1 = spl_eval(g.z_of_chi, lambda1), z2 = spl_eval(g.z_of_chi, lambda2);
+            const double ga1 = spl_eval(g.D1, z1) / spl_eval(g.a, z1);
+            const double ga2 = spl_eval(g.D1, z2) / spl_eval(g.a, z2);
+            AdjSingleCoef K;
+            adj_single_coef(a, G, x, lambda1, lambda2, r21, r22, b1, b2, s1, s2, f1c, f2c, D1z1c,
+                            D1z2c, ga1, ga2, mu, K);
+            const double ra = sqrt(r21), rb = sqrt(r22);
+            const int ia = lens_interval<double>(tab_x, a.tab_len, a.inv_dlog, ra);
+            const int ib = lens_interval<double>(tab_x, a.tab_len, a.inv_dlog, rb);
+            double vd = K.den_i11_0 * I11_0, vr = K.rsd_i00_0 * I00_0;
+            if (ia < 0 || ib < 0) {
+                vd = vr = cg_nan<double>();
+            } else {
+                const double dxa = ra - tab_x[ia], dxb = rb - tab_x[ib];
+#pragma unroll
+                for (int t = 0; t < LENS_NT; ++t) {
+                    const double Ia = adj_table_at(recs, ia, t, dxa);
+                    const double Ib = adj_table_at(recs, ib, t, dxb);
+                    vd += K.den1[t] * Ia + K.den2[t] * Ib;
+                    vr += K.rsd1[t] * Ia + K.rsd2[t] * Ib;
+                }
+                if (gRs) {
+                    const double gn = gi * hw * gw[k];
+#pragma unroll
+                    for (int t = 0; t < LENS_NT; ++t) {
+                        adj_rec_add(gRs, ((long long)t * ni + ia) * 4,
+                                    gn * (beta * K.den1[t] + alpha * K.rsd1[t]), dxa);
+                        adj_rec_add(gRs, ((long long)t * ni + ib) * 4,
+                                    gn * (beta * K.den2[t] + alpha * K.rsd2[t]), dxb);
+                    }
+                    if (K.den_i11_0 != 0.0)
+                        atomicAdd(gRs + (long long)L11 * ni * 4, gn * beta * K.den_i11_0);
+                    if (K.rsd_i00_0 != 0.0)
+                        atomicAdd(gRs + (long long)L00 * ni * 4, gn * alpha * K.rsd_i00_0);
+                }
+            }
+            pd += gw[k] * vd;
+            pr += gw[k] * vr;
+        }
+        den_sum += hw * warp_sum(pd);
+        rsd_sum += hw * warp_sum(pr);
+    }
+    if (lane == 0) {
+        const double v = beta * den_sum + alpha * rsd_sum;
+        if (!isfinite(v)) cg_flag(err, CG_ERR_NONFINITE);
+        if (part) part[item] = v;
+        if (gpm) {
+            if (g_bias && den_sum != 0.0) atomicAdd(g_bias + q, gi * den_sum);
+            if (g_growth && rsd_sum != 0.0) atomicAdd(g_growth + q, gi * rsd_sum);
+        }
+    }
+}
+
+// record cotangents -> table-knot cotangents gY[(s * n_at + t) * len + j]
+// through the Akima coefficients of each interval (lens_records_kernel)
+__global__ void adj_lens_records_kernel(LensArgs a, const double *__restrict__ tab_x,
+                                        const double *__restrict__ tab_y, int n_spectra,
+                                        const double *__restrict__ gR, double *__restrict__ gY,
+                                        int n_at)
+{
+    const int len = a.tab_len, ni = len - 1;
+    const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= (long long)n_spectra * LENS_NT * ni) return;
+    const double *g = gR + item * 4;
+    if (g[0] == 0.0 && g[1] == 0.0 && g[2] == 0.0 && g[3] == 0.0) return;
+    const int i = (int)(item % ni);
+    const long long st = item / ni;
+    const int t = (int)(st % LENS_NT);
+    const int s = (int)(st / LENS_NT);
+    const double *y = tab_y + ((size_t)s * a.n_terms + a.term[t]) * len;
+    D6 r[4];
+    akima_record_d6(tab_x, y, len, i, r);
+    double *dst = gY + ((size_t)s * n_at + t) * len + d6_base(len, i);
+    for (int k = 0; k < 6; ++k) {
+        const double v = g[0] * r[0].g[k] + g[1] * r[1].g[k] + g[2] * r[2].g[k] + g[3] * r[3].g[k];
+        if (v != 0.0) atomicAdd(dst + k, v);
+    }
 }
 
 } // namespace
@@ -1222,41 +1640,25 @@ int corrfunc_lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, int n_r
     const LensBg64 g64 = lens_bg64(ctx);
     if (precision == COFFE_GPU_MIXED) {
         LensBgT<Spl32> gT{ctx->bg[BG_Z_OF_CHI].v32(), ctx->bg[BG_D1].v32(), ctx->bg[BG_A].v32()};
-        return lensing_launch<float, Spl32, float>(ctx, a, g64, gT, req_spectrum, req_z_mean,
-                                                   req_offset, sep, out, total, single, dbl, rule,
-                                                   true);
+        return lensing_launch<float, Spl32, float, true>(ctx, a, g64, gT, req_spectrum,
+                                                         req_z_mean, req_offset, sep, out, total,
+                                                         single, dbl, rule, true);
     }
     LensBgT<Spl64> gT{ctx->bg[BG_Z_OF_CHI].v64(), ctx->bg[BG_D1].v64(), ctx->bg[BG_A].v64()};
-    return lensing_launch<double, Spl64, double>(ctx, a, g64, gT, req_spectrum, req_z_mean,
-                                                 req_offset, sep, out, total, single, dbl, rule,
-                                                 true);
+    return lensing_launch<double, Spl64, double, false>(ctx, a, g64, gT, req_spectrum,
+                                                        req_z_mean, req_offset, sep, out, total,
+                                                        single, dbl, rule, true);
 }
 
 void gauss_legendre_nodes(int n, double *x, double *w) { gauss_legendre(n, x, w); }
 
-int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, int n_req,
-                const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
-                const double *sep, int n_l, const int *l, double *out, long long total)
+// LensArgs of a validated multipole call with the full-sky single-integrated
+// term (single_full) or not, the mu symmetry applied, and the Gauss-Legendre
+// rule on the device (ctx->lens_rule)
+static int lens_prepare(coffe_gpu_ctx *ctx, int contrib, int n_req, int n_l, const int *l,
+                        bool single_full, LensArgs *out)
 {
-    if (!(contrib & COFFE_GPU_LEN) || total <= 0) return COFFE_GPU_OK;
-    // which forms of the single- and double-integrated terms (signal.c:607-754)
-    const bool only_cross = (contrib & COFFE_GPU_ONLY_CROSS) != 0;
-    const bool want_single = (contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD)) != 0;
-    const bool single_full = want_single && !ctx->flat_local_nonlocal;
-    const bool single_flat = want_single && ctx->flat_local_nonlocal && (contrib & COFFE_GPU_DEN);
-    const bool double_full = !only_cross && !ctx->flat_nonlocal;
-    const bool double_flat = !only_cross && ctx->flat_nonlocal;
     int st;
-    if (single_flat || double_flat)
-        if ((st = flatsky_run(ctx, single_flat, double_flat, epsrel, n_req, req_spectrum,
-                              req_z_mean, req_offset, sep, n_l, l, out, total)))
-            return st;
-    if (!single_full && !double_full) return COFFE_GPU_OK;
-    if (!ctx->int_small_r) {
-        cg_set_error(ctx, "multipoles: lensing needs the r = 0 and sub-Mpc table entries "
-                          "(integrals_init with COFFE_GPU_SMALL_R)");
-        return COFFE_GPU_ESTATE;
-    }
     LensArgs a;
     if ((st = lens_args(ctx, contrib, n_req, n_l, l, ctx->lens_n_mu, &a))) return st;
     // mu -> -mu swaps chi1 and chi2, i.e. the roles of the two tracers: when
@@ -1293,17 +1695,135 @@ int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, i
         ctx->lens_rule_mu = a.n_mu;
         ctx->lens_rule_x = a.n_x;
     }
+    *out = a;
+    return COFFE_GPU_OK;
+}
+
+int lensing_run(coffe_gpu_ctx *ctx, int contrib, int precision, double epsrel, int n_req,
+                const int *req_spectrum, const double *req_z_mean, const int64_t *req_offset,
+                const double *sep, int n_l, const int *l, double *out, long long total)
+{
+    if (!(contrib & COFFE_GPU_LEN) || total <= 0) return COFFE_GPU_OK;
+    // which forms of the single- and double-integrated terms (signal.c:607-754)
+    const bool only_cross = (contrib & COFFE_GPU_ONLY_CROSS) != 0;
+    const bool want_single = (contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD)) != 0;
+    const bool single_full = want_single && !ctx->flat_local_nonlocal;
+    const bool single_flat = want_single && ctx->flat_local_nonlocal && (contrib & COFFE_GPU_DEN);
+    const bool double_full = !only_cross && !ctx->flat_nonlocal;
+    const bool double_flat = !only_cross && ctx->flat_nonlocal;
+    int st;
+    if (single_flat || double_flat)
+        if ((st = flatsky_run(ctx, single_flat, double_flat, epsrel, n_req, req_spectrum,
+                              req_z_mean, req_offset, sep, n_l, l, out, total)))
+            return st;
+    if (!single_full && !double_full) return COFFE_GPU_OK;
+    if (!ctx->int_small_r) {
+        cg_set_error(ctx, "multipoles: lensing needs the r = 0 and sub-Mpc table entries "
+                          "(integrals_init with COFFE_GPU_SMALL_R)");
+        return COFFE_GPU_ESTATE;
+    }
+    LensArgs a;
+    if ((st = lens_prepare(ctx, contrib, n_req, n_l, l, single_full, &a))) return st;
     const LensBg64 g64 = lens_bg64(ctx);
     if (precision == COFFE_GPU_MIXED) {
         LensBgT<Spl32> gT{ctx->bg[BG_Z_OF_CHI].v32(), ctx->bg[BG_D1].v32(), ctx->bg[BG_A].v32()};
-        return lensing_launch<float, Spl32, float>(ctx, a, g64, gT, req_spectrum, req_z_mean,
-                                                   req_offset, sep, out, total, single_full,
-                                                   double_full, (const double *)ctx->lens_rule.p,
-                                                   false);
+        return lensing_launch<float, Spl32, float, true>(
+            ctx, a, g64, gT, req_spectrum, req_z_mean, req_offset, sep, out, total, single_full,
+            double_full, (const double *)ctx->lens_rule.p, false);
     }
     LensBgT<Spl64> gT{ctx->bg[BG_Z_OF_CHI].v64(), ctx->bg[BG_D1].v64(), ctx->bg[BG_A].v64()};
-    return lensing_launch<double, Spl64, double>(ctx, a, g64, gT, req_spectrum, req_z_mean,
-                                                 req_offset, sep, out, total, single_full,
-                                                 double_full, (const double *)ctx->lens_rule.p,
-                                                 false);
+    // COFFE_GPU_FP64_FASTALG: the mixed path's lensing algorithm in FP64
+    if (precision == COFFE_GPU_FP64_FASTALG)
+        return lensing_launch<double, Spl64, double, true>(
+            ctx, a, g64, gT, req_spectrum, req_z_mean, req_offset, sep, out, total, single_full,
+            double_full, (const double *)ctx->lens_rule.p, false);
+    return lensing_launch<double, Spl64, double, false>(
+        ctx, a, g64, gT, req_spectrum, req_z_mean, req_offset, sep, out, total, single_full,
+        double_full, (const double *)ctx->lens_rule.p, false);
+}
+
+// Reverse mode of the full-sky lensing terms of coffe_gpu_multipoles (FP64
+// tables with the sub-Mpc entries): value_out (when not NULL) += the lensing
+// multipoles with the den-lensing part scaled by bias_scale[q] and the
+// RSD-lensing part by growth_scale[q]; with grad_out, the table cotangents
+// are added to gY[(s * n_at + t) * tab_len + j] for t in the order of the six
+// lensing tables (I00, I02, I04, I11, I13, I20) and the scale cotangents to
+// grad_bias / grad_growth.
+int lensing_adjoint_run(coffe_gpu_ctx *ctx, int contrib, int n_req, const int *req_spectrum,
+                        const double *req_z_mean, const int64_t *req_offset, const double *sep,
+                        long long total, int n_l, const int *l, const double *bias_scale,
+                        const double *growth_scale, const double *grad_out, double *value_out,
+                        double *gY, int n_at, double *grad_bias, double *grad_growth)
+{
+    if (!(contrib & COFFE_GPU_LEN) || total <= 0) return COFFE_GPU_OK;
+    if (ctx->flat_local_nonlocal || ctx->flat_nonlocal) {
+        cg_set_error(ctx, "multipoles adjoint: the lensing terms are differentiated in their "
+                          "full-sky form only (coffe_gpu_set_flatsky(ctx, 0, 0))");
+        return COFFE_GPU_EINVAL;
+    }
+    if (!ctx->int_small_r) {
+        cg_set_error(ctx, "multipoles adjoint: lensing needs the r = 0 and sub-Mpc table "
+                          "entries (integrals_init with COFFE_GPU_SMALL_R)");
+        return COFFE_GPU_ESTATE;
+    }
+    const bool single = (contrib & (COFFE_GPU_DEN | COFFE_GPU_RSD)) != 0;
+    int st;
+    LensArgs a;
+    if ((st = lens_prepare(ctx, contrib, n_req, n_l, l, single, &a))) return st;
+    const double *rule = (const double *)ctx->lens_rule.p;
+    const LensBg64 g64 = lens_bg64(ctx);
+    LensBgT<Spl64> gT{ctx->bg[BG_Z_OF_CHI].v64(), ctx->bg[BG_D1].v64(), ctx->bg[BG_A].v64()};
+    const double *tab_x = (const double *)ctx->tab_x.p;
+    const int ni = a.tab_len - 1;
+    const long long n_int = (long long)ctx->n_spectra * ni;
+    const long long n_rec = n_int * LENS_NT;
+    // the FP64 records, then (with grad_out) the record cotangents
+    const size_t b_rec = (sizeof(double4_32a) * (size_t)n_rec + 255) & ~(size_t)255;
+    const size_t b_gR = grad_out ? sizeof(double) * 4 * (size_t)n_rec : 0;
+    if ((st = cg_ensure(ctx, ctx->lens_rec, b_rec + b_gR))) return st;
+    double4_32a *rec = (double4_32a *)ctx->lens_rec.p;
+    double *gR = grad_out ? (double *)((char *)ctx->lens_rec.p + b_rec) : nullptr;
+    lens_records_kernel<double><<<(unsigned)((n_rec + 255) / 256), 256, 0, ctx->stream>>>(
+        a, tab_x, (const double *)ctx->tab_y.p, ctx->n_spectra, rec);
+    if ((st = cg_after_launch(ctx, "lens_records_kernel"))) return st;
+    if (gR) CG_CUDA(ctx, cudaMemsetAsync(gR, 0, b_gR, ctx->stream));
+    // pairs per chunk: at most 2^22 (pair, mu) items
+    const long long chunk = std::max(1LL, std::min(total, (1LL << 22) / a.n_mu_run));
+    const size_t per = (size_t)(chunk * a.n_mu_run);
+    if ((st = cg_ensure(ctx, ctx->lens_part, sizeof(double) * 3 * per))) return st;
+    double *part_d = (double *)ctx->lens_part.p;
+    double *part_s = part_d + per;
+    double *gpm = grad_out ? part_s + per : nullptr;
+    for (long long p0 = 0; p0 < total; p0 += chunk) {
+        const long long np = std::min(chunk, total - p0);
+        a.pair0 = p0;
+        a.n_items = np * a.n_mu_run;
+        if (gpm) {
+            adj_lens_gpm_kernel<<<(unsigned)((a.n_items + 127) / 128), 128, 0, ctx->stream>>>(
+                a, rule, grad_out, np, gpm);
+            if ((st = cg_after_launch(ctx, "adj_lens_gpm_kernel"))) return st;
+        }
+        adj_lens_double_kernel<<<(unsigned)a.n_items, LENS_THREADS, 0, ctx->stream>>>(
+            a, g64, gT, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule, gpm,
+            value_out ? part_d : nullptr, gR, ctx->d_err);
+        if ((st = cg_after_launch(ctx, "adj_lens_double_kernel"))) return st;
+        if (single) {
+            const long long blocks = (a.n_items + LENS_THREADS / 32 - 1) / (LENS_THREADS / 32);
+            adj_lens_single_kernel<<<(unsigned)blocks, LENS_THREADS, 0, ctx->stream>>>(
+                a, g64, tab_x, rec, req_spectrum, req_z_mean, req_offset, sep, rule, bias_scale,
+                growth_scale, gpm, value_out ? part_s : nullptr, gR, grad_bias, grad_growth,
+                ctx->d_err);
+            if ((st = cg_after_launch(ctx, "adj_lens_single_kernel"))) return st;
+        }
+        if (value_out) {
+            const long long nt = np * a.n_l;
+            lens_reduce_kernel<<<(unsigned)((nt + 3) / 4), 128, 0, ctx->stream>>>(
+                a, rule, part_d, single ? part_s : nullptr, np, value_out, ctx->d_err);
+            if ((st = cg_after_launch(ctx, "lens_reduce_kernel"))) return st;
+        }
+    }
+    if (!gR) return COFFE_GPU_OK;
+    adj_lens_records_kernel<<<(unsigned)((n_rec + 255) / 256), 256, 0, ctx->stream>>>(
+        a, tab_x, (const double *)ctx->tab_y.p, ctx->n_spectra, gR, gY, n_at);
+    return cg_after_launch(ctx, "adj_lens_records_kernel");
 }

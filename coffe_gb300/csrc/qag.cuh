@@ -147,15 +147,21 @@ __device__ __forceinline__ bool qag_too_small(double a1, double a2, double b2)
 
 // Adaptive continuation after a first panel `p0` over [a, b] (gsl qag.c
 // semantics).  Returns the integral; *status: 0 ok, 1 limit reached,
-// 2 round-off, 3 bad integrand behaviour.  `F` evaluates one point.
+// 2 round-off, 3 bad integrand behaviour.  `F` evaluates one point.  When
+// n_final is given it receives the number of intervals of the final
+// partition: 1 when the first panel is the result ([a, b]; the store is not
+// written), else the intervals s.a[0..n) / s.b[0..n) whose results sum up to
+// the returned integral.
 template <typename T, class F>
 __device__ T qag_continue(const F &f, const GkLane<T> &g, T a, T b, QkOut<T> p0, T epsabs,
-                          T epsrel, const QagStore<T> &s, int limit, int *status)
+                          T epsrel, const QagStore<T> &s, int limit, int *status,
+                          int *n_final = nullptr)
 {
     const int lane = threadIdx.x & 31;
     T tolerance = fmax(epsabs, epsrel * fabs(p0.result));
     const T round_off = T(50) * qk_eps<T>() * p0.resabs;
     *status = 0;
+    if (n_final) *n_final = 1;
     if (p0.abserr <= round_off && p0.abserr > tolerance) {
         *status = 2;
         return p0.result;
@@ -212,6 +218,7 @@ __device__ T qag_continue(const F &f, const GkLane<T> &g, T a, T b, QkOut<T> p0,
         size++;
         iteration++;
     } while (iteration < lim && !error_type && errsum > tolerance);
+    if (n_final) *n_final = size;
     if (error_type)
         *status = error_type;
     else if (errsum > tolerance)
@@ -226,9 +233,10 @@ __device__ T qag_continue(const F &f, const GkLane<T> &g, T a, T b, QkOut<T> p0,
 // Full QAG: first panel then the adaptive loop.
 template <typename T, class F>
 __device__ __forceinline__ T qag61_warp(const F &f, T a, T b, T epsabs, T epsrel,
-                                        const QagStore<T> &s, int limit, int *status)
+                                        const QagStore<T> &s, int limit, int *status,
+                                        int *n_final = nullptr)
 {
     const GkLane<T> g = gk_lane<T>();
     const QkOut<T> p0 = qk61_warp(f, g, a, b);
-    return qag_continue(f, g, a, b, p0, epsabs, epsrel, s, limit, status);
+    return qag_continue(f, g, a, b, p0, epsabs, epsrel, s, limit, status, n_final);
 }

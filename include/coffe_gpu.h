@@ -46,12 +46,15 @@ enum coffe_gpu_precision {
     COFFE_GPU_MIXED = 1,       /* FP32 FFT/spline/integrand arithmetic with compensated
                                   sums; FP64 Gamma-ratio coefficients and background */
     COFFE_GPU_FP64_FASTALG = 2 /* coffe_gpu_multipoles only, on FP64 tables: FP64
-                                  arithmetic through the mixed path's algorithm for
-                                  unit biases and even multipoles (per-request
-                                  background polynomials, regrouped integrand;
-                                  ~1e-8 from the parity path), the precision-only
-                                  baseline of COFFE_GPU_MIXED.  Other calls take the
-                                  FP64 path. */
+                                  arithmetic through the mixed path's algorithm, the
+                                  precision-only baseline of COFFE_GPU_MIXED (~1e-8
+                                  from the parity path).  Den/RSD terms with unit
+                                  biases and even multipoles: per-request background
+                                  polynomials, regrouped integrand; lensing terms:
+                                  D1/a polynomials along the lines of sight, the
+                                  plane integrand over five combined table records.
+                                  Other den/RSD cases and other calls take the FP64
+                                  path. */
 };
 
 /* Contributions to the 2-point function (the den, rsd, len flags of
@@ -417,7 +420,13 @@ int coffe_gpu_set_tuning(coffe_gpu_ctx_t *ctx, const coffe_gpu_tuning_t *t);
    QUADPACK's acceptance test to each first panel (relative tolerance 1e-5,
    the reference's default integration_1d_prec) and counts the outputs it
    rejects -- there the adaptive result differs from this value -- in the
-   counter coffe_gpu_multipoles_retries reads. */
+   counter coffe_gpu_multipoles_retries reads.
+   contrib may add COFFE_GPU_LEN: the full-sky lensing terms on the
+   Gauss-Legendre rule of coffe_gpu_set_lensing_rule, as coffe_gpu_multipoles
+   computes them in FP64 (same mu symmetry and weights; the den-lensing part
+   scaled by bias_scale, the RSD-lensing part by growth_scale); the tables
+   then need (1,1), (1,3), (2,0) too and COFFE_GPU_SMALL_R, and the flat-sky
+   switches of coffe_gpu_set_flatsky must be off. */
 int coffe_gpu_multipoles_scaled(coffe_gpu_ctx_t *ctx, int contrib, int n_req, int64_t n_sep,
                                 const int *req_spectrum, const double *req_z_mean,
                                 const int64_t *req_offset, const double *sep, int n_l,
@@ -428,8 +437,11 @@ int coffe_gpu_multipoles_scaled(coffe_gpu_ctx_t *ctx, int contrib, int n_req, in
    layout as out), writes grad_pk[s * nk + i] = sum grad_out * d out / d P_s(k_i)
    for every spectrum of the last coffe_gpu_integrals_init (through the
    natural-spline resampling, the FFTLog transform and the Akima interpolation
-   of the tables, twofast.c:362-483), and, when not NULL, grad_bias_scale[q] and
-   grad_growth_scale[q].  Device pointers except `l`. */
+   of the tables, twofast.c:362-483; with COFFE_GPU_LEN also through the
+   lensing integrands and the QAG integrals of the r = 0 and sub-Mpc table
+   entries, integrals.c:524-562, on their final partition), and, when not
+   NULL, grad_bias_scale[q] and grad_growth_scale[q].  Device pointers except
+   `l`. */
 int coffe_gpu_multipoles_adjoint(coffe_gpu_ctx_t *ctx, int contrib, int n_req, int64_t n_sep,
                                  const int *req_spectrum, const double *req_z_mean,
                                  const int64_t *req_offset, const double *sep, int n_l,

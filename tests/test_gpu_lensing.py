@@ -81,6 +81,36 @@ def test_lensing_fp64_matches_oracle(gpu_ctx, lens_setup, contrib):
     assert e < 1e-10, e
 
 
+@pytest.mark.parametrize("contrib", [LEN, DEN | RSD | LEN])
+def test_lensing_fp64_fastalg_matches_oracle(gpu_ctx, lens_setup, contrib):
+    """The mixed path's lensing algorithm in FP64 (degree-9 D1/a polynomials along
+    the lines of sight, the plane integrand over the five combined records): the
+    matched-algorithm baseline of the mixed path, within the polynomials' ~1e-8
+    of the oracle's spline lookups."""
+    k, pk, m = lens_setup
+    sep = np.array([20.0, 55.0, 120.0, 300.0]) / H
+    ls = (0, 2, 4, 6)
+    rule = (16, 32)
+    gpu_ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+    gpu_ctx.integrals_init(k, pk[None, :], LENS_TERMS, N=4096, precision="fp64", small_r=True)
+    gpu_ctx.set_lensing_rule(*rule)
+    got = gpu_ctx.multipoles([0], [1.5], [0, len(sep)], sep, ls, contrib=contrib,
+                             precision="fp64-fastalg")
+    ref = m.multipoles_lensing(contrib, 1.5, sep, ls, *rule)
+    if contrib & (DEN | RSD):
+        for j, l in enumerate(ls):
+            ref[:, j] += [m.multipole(contrib & 3, 1.5, r, l) for r in sep]
+    # with den+RSD the l = 6 floor of the mixed tests: the degree-5 background
+    # polynomials of the den/RSD part (~1e-8 of the monopole) are not resolved
+    # against that multipole's own (wide-angle) scale
+    e = _rel_mixed(got, ref, ls) if contrib & (DEN | RSD) else _rel(got, ref)
+    print("contrib", contrib, "fp64-fastalg max rel error", e)
+    assert e < 1e-6, e
+    par = gpu_ctx.multipoles([0], [1.5], [0, len(sep)], sep, ls, contrib=contrib,
+                             precision="fp64")
+    assert not np.array_equal(got, par)  # the other algorithm ran
+
+
 def test_lensing_mixed_close_to_oracle(gpu_ctx, lens_setup):
     k, pk, m = lens_setup
     sep = np.array([20.0, 55.0, 120.0, 300.0]) / H
