@@ -168,6 +168,32 @@ int cg_check_device_errors(coffe_gpu_ctx *ctx, const char *where)
     return COFFE_GPU_EINVAL;
 }
 
+namespace {
+// reads 16-byte words of buf; the sum only keeps the loads alive
+__global__ void l2_read_kernel(const uint4 *__restrict__ buf, size_t n, unsigned *sink)
+{
+    unsigned acc = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const uint4 v = buf[i];
+        acc ^= v.x ^ v.y ^ v.z ^ v.w;
+    }
+    if (acc == 0x9e3779b9u) atomicAdd(sink, 1u); // practically never taken
+}
+} // namespace
+
+int cg_l2_evict(coffe_gpu_ctx *ctx, void *buf, size_t bytes, int value)
+{
+    CG_CUDA(ctx, cudaMemsetAsync(buf, value, bytes, ctx->stream));
+    if (ctx->sm_count <= 0)
+        CG_CUDA(ctx, cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount,
+                                            ctx->device));
+    l2_read_kernel<<<ctx->sm_count * 4, 512, 0, ctx->stream>>>((const uint4 *)buf, bytes / 16,
+                                                               (unsigned *)buf);
+    CG_CUDA(ctx, cudaGetLastError());
+    return COFFE_GPU_OK;
+}
+
 extern "C" {
 
 const char *coffe_gpu_strerror(int status)

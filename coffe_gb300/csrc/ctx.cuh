@@ -183,12 +183,22 @@ int multipoles_prepare_background(coffe_gpu_ctx *ctx);
 // loads the module and kernels of coffe_gpu_multipoles_noalloc (ctx creation)
 int multipoles_noalloc_prepare(coffe_gpu_ctx *ctx);
 
+// Evicts the L2 cache on the context's stream: writes `bytes` (>= twice the L2)
+// at buf, then reads them back, so that the lines left in L2 are clean and the
+// work timed next neither finds its inputs there nor pays for writing the
+// eviction's dirty lines back.
+int cg_l2_evict(coffe_gpu_ctx *ctx, void *buf, size_t bytes, int value);
+
 // Configuration for one launch shape: the chosen one if the shape was tuned,
 // else (benchmark mode, stream not capturing) the fastest of `cands` timed
 // with `run` on the stream, else the default.  run(cfg) enqueues the work.
+// cold: the work's inputs arrive from outside (new spectra): every timed run
+// starts with the L2 cache evicted (cg_l2_evict), as it does in use, where the
+// candidates rank differently than on L2-resident inputs.
 template <typename Run>
 int cg_tuned(coffe_gpu_ctx *ctx, const std::array<long long, 6> &key,
-             const std::vector<coffe_gpu_tuning_t> &cands, Run run, coffe_gpu_tuning_t *out)
+             const std::vector<coffe_gpu_tuning_t> &cands, Run run, coffe_gpu_tuning_t *out,
+             bool cold = false)
 {
     auto it = ctx->tune_cache.find(key);
     if (it != ctx->tune_cache.end()) {
@@ -207,12 +217,23 @@ int cg_tuned(coffe_gpu_ctx *ctx, const std::array<long long, 6> &key,
         cudaEventDestroy(e0);
         return COFFE_GPU_ECUDA;
     }
+    void *flush = nullptr;
+    size_t flush_bytes = 0;
+    if (cold) {
+        int l2 = 0;
+        if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device) == cudaSuccess &&
+            l2 > 0 && cudaMalloc(&flush, 2 * (size_t)l2) == cudaSuccess)
+            flush_bytes = 2 * (size_t)l2;
+        else
+            flush = nullptr; // no room: time on warm inputs
+    }
     float best = 3.0e38f;
     int st = 0;
     for (const coffe_gpu_tuning_t &c : cands) {
         if ((st = run(c))) break; // warm-up of this configuration
         float t = 3.0e38f;
         for (int rep = 0; rep < 2 && !st; ++rep) {
+            if (flush && (st = cg_l2_evict(ctx, flush, flush_bytes, rep))) break;
             cudaEventRecord(e0, ctx->stream);
             st = run(c);
             cudaEventRecord(e1, ctx->stream);
@@ -228,6 +249,10 @@ int cg_tuned(coffe_gpu_ctx *ctx, const std::array<long long, 6> &key,
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (flush) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(flush);
+    }
     if (st) return st;
     ctx->tune_cache[key] = *out;
     return 0;

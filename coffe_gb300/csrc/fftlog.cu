@@ -1855,7 +1855,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     coffe_gpu_tuning_t tu;
     const std::array<long long, 6> key{1, (long long)N, n_spectra, n_terms, n_q,
                                        mixed ? (tables_df ? 2 : 1) : 0};
-    if ((st = cg_tuned(ctx, key, cands, stage, &tu))) return st;
+    if ((st = cg_tuned(ctx, key, cands, stage, &tu, /*cold=*/true))) return st;
     if ((st = stage(tu))) return st;
     ctx->last_tuning.fft_threads = tu.fft_threads;
     ctx->last_tuning.fft_threads_fwd = tu.fft_threads_fwd;
