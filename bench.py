@@ -885,7 +885,11 @@ def ours(args, rank, world, local_rank):
         barrier()
         t0 = time.perf_counter()
         for _ in range(ke):
-            ctx.integrals_init(batch.k, h_pk, TERMS, N=N_FFT, precision="mixed", small_r=False)
+            # the tables are enqueued (the call returns once P(k) is on the device) and
+            # the multipole call uploads its requests while they are being made; it
+            # returns when the results are in h_out and reports any device error
+            ctx.integrals_init(batch.k, h_pk, TERMS, N=N_FFT, precision="mixed", small_r=False,
+                               sync=False)
             res = ctx.multipoles(h_rs, h_rz, h_ro, h_sep, batch.ls, precision="mixed", out=h_out)
         barrier()
         te = time.perf_counter() - t0

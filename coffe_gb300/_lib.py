@@ -152,13 +152,15 @@ def load(build_if_missing: bool = True):
     L.coffe_gpu_integral_table_len.restype = C.c_size_t
     L.coffe_gpu_integrals_init.argtypes = [_p, _dp, _dp, C.c_int, C.c_size_t, _ip, _ip, C.c_int,
                                            C.c_size_t, C.c_int, C.c_uint]
-    L.coffe_gpu_integrals_init_ex.argtypes = [_p, _dp, _dp, C.c_int, C.c_size_t, _ip, _ip, _ip,
+    # the per-step entry points take raw addresses (void *): numpy's
+    # .ctypes.data_as costs ~3 us per array, a noticeable share of a call
+    L.coffe_gpu_integrals_init_ex.argtypes = [_p, _p, _p, C.c_int, C.c_size_t, _p, _p, _p,
                                               C.c_int, C.c_size_t, C.c_int, C.c_uint]
     L.coffe_gpu_set_flatsky.argtypes = [_p, C.c_int, C.c_int]
     L.coffe_gpu_integral_get.argtypes = [_p, C.c_int, C.c_int, _dp, _dp]
     L.coffe_gpu_integral_eval.argtypes = [_p, C.c_int, C.c_int, _dp, C.c_size_t, _dp]
-    L.coffe_gpu_multipoles.argtypes = [_p, C.c_int, C.c_int, C.c_double, C.c_int, _ip, _dp, _lp,
-                                       _dp, C.c_int, _ip, _dp, C.c_int]
+    L.coffe_gpu_multipoles.argtypes = [_p, C.c_int, C.c_int, C.c_double, C.c_int, _p, _p, _p,
+                                       _p, C.c_int, _p, _p, C.c_int]
     L.coffe_gpu_multipoles_async.argtypes = [_p, C.c_int, C.c_int, C.c_double, C.c_int,
                                              C.c_int64, _ip, _dp, _lp, _dp, C.c_int, _ip, _dp]
     L.coffe_gpu_set_lensing_rule.argtypes = [_p, C.c_int, C.c_int]

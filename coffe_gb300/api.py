@@ -35,6 +35,11 @@ def _lptr(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_int64))
 
 
+def _addr(a: np.ndarray) -> int:
+    """Address of a numpy array's data (for the void * arguments)."""
+    return a.__array_interface__["data"][0]
+
+
 def _f64(a) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.float64)
 
@@ -197,9 +202,13 @@ class Context:
     # ------------------------------------------------------------- integrals
     def integrals_init(self, k, pk, terms: Sequence[Tuple[int, int]] = DEFAULT_TERMS,
                        N: int = 4096, precision="fp64", small_r: bool = True,
-                       tables_df: bool = False):
+                       tables_df: bool = False, sync: bool = True):
         """FFTLog tables of I_l^n for each spectrum row of ``pk`` (shape (S, nk)).
-        ``tables_df`` (mixed precision): double-float inverse transforms too."""
+        ``tables_df`` (mixed precision): double-float inverse transforms too.
+        ``sync=False``: return once ``pk`` has been copied to the device, with
+        the tables still being made (COFFE_GPU_ASYNC); their device-side errors
+        surface at the next call that checks (:meth:`multipoles`,
+        :meth:`synchronize`)."""
         k = _f64(k)
         pk = _f64(np.atleast_2d(pk))
         if pk.shape[1] != len(k):
@@ -209,10 +218,11 @@ class Context:
         l = np.ascontiguousarray([t[1] for t in terms], dtype=np.int32)
         half = np.ascontiguousarray([t[2] if len(t) > 2 else 0 for t in terms], dtype=np.int32)
         prec = _precision(precision)
-        flags = (_lib.SMALL_R if small_r else 0) | (_lib.TABLES_DF if tables_df else 0)
-        self._check(self._L.coffe_gpu_integrals_init_ex(self._ctx, _dptr(k), _dptr(pk),
-                                                        pk.shape[0], len(k), _iptr(n), _iptr(l),
-                                                        _iptr(half), len(terms), int(N), prec,
+        flags = ((_lib.SMALL_R if small_r else 0) | (_lib.TABLES_DF if tables_df else 0)
+                 | (0 if sync else _lib.ASYNC))
+        self._check(self._L.coffe_gpu_integrals_init_ex(self._ctx, _addr(k), _addr(pk),
+                                                        pk.shape[0], len(k), _addr(n), _addr(l),
+                                                        _addr(half), len(terms), int(N), prec,
                                                         flags), "integrals_init")
         self.N = int(N)
         self.terms = tuple((int(t[0]), int(t[1])) + ((1,) if len(t) > 2 and t[2] else ())
@@ -270,9 +280,9 @@ class Context:
               out.shape[0] < max(len(sp), 1) or out.shape[1] != len(la)):
             raise ValueError("out must be a C-contiguous float64 array of shape (len(sep), len(ls))")
         self._check(self._L.coffe_gpu_multipoles(self._ctx, int(contrib), _precision(precision),
-                                                 float(epsrel), len(rs), _iptr(rs), _dptr(rz),
-                                                 _lptr(ro), _dptr(sp), len(la), _iptr(la),
-                                                 _dptr(out), 0), "multipoles")
+                                                 float(epsrel), len(rs), _addr(rs), _addr(rz),
+                                                 _addr(ro), _addr(sp), len(la), _addr(la),
+                                                 _addr(out), 0), "multipoles")
         return out[: len(sp)]
 
     def average_multipoles(self, win_spectrum, z_min, z_max, win_offset, sep, ls=(0, 2, 4),
@@ -480,11 +490,10 @@ class Context:
                           contrib=_lib.DEN | _lib.RSD, precision="fp64", epsrel=1e-5):
         """Same as :meth:`multipoles` with CUDA tensors (int32, float64, int64,
         float64, int32, float64 out of shape (len(sep), len(ls))); no copies."""
-        P = lambda t, ty: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ty))
         self._check(self._L.coffe_gpu_multipoles(
             self._ctx, int(contrib), _precision(precision), float(epsrel), int(req_spectrum.numel()),
-            P(req_spectrum, C.c_int), P(req_z_mean, C.c_double), P(req_offset, C.c_int64),
-            P(sep, C.c_double), int(ls.numel()), P(ls, C.c_int), P(out, C.c_double), 1),
+            req_spectrum.data_ptr(), req_z_mean.data_ptr(), req_offset.data_ptr(),
+            sep.data_ptr(), int(ls.numel()), ls.data_ptr(), out.data_ptr(), 1),
             "multipoles")
 
 

@@ -182,6 +182,15 @@ __global__ void l2_read_kernel(const uint4 *__restrict__ buf, size_t n, unsigned
 }
 } // namespace
 
+int cg_copy_stream(coffe_gpu_ctx *ctx)
+{
+    if (!ctx->copy_stream)
+        CG_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t &e : ctx->copy_ev)
+        if (!e) CG_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return COFFE_GPU_OK;
+}
+
 int cg_l2_evict(coffe_gpu_ctx *ctx, void *buf, size_t bytes, int value)
 {
     CG_CUDA(ctx, cudaMemsetAsync(buf, value, bytes, ctx->stream));
@@ -270,6 +279,9 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
     for (cudaEvent_t ev : ctx->timing_events) cudaEventDestroy(ev);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
+    for (cudaEvent_t e : ctx->copy_ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
     return COFFE_GPU_OK;
@@ -573,7 +585,12 @@ int coffe_gpu_integrals_init_ex(coffe_gpu_ctx_t *ctx, const double *k, const dou
         ctx->int_ready = false;
         return st;
     }
-    if (flags & COFFE_GPU_ASYNC) return COFFE_GPU_OK;
+    if (flags & COFFE_GPU_ASYNC) {
+        // host P(k): returns once it has been copied, so the caller may reuse it
+        if (!(flags & COFFE_GPU_PK_DEVICE) && ctx->copy_ev[2])
+            CG_CUDA(ctx, cudaEventSynchronize(ctx->copy_ev[2]));
+        return COFFE_GPU_OK;
+    }
     const int st2 = cg_check_device_errors(ctx, "integrals_init");
     if (st2) ctx->int_ready = false;
     return st2;
@@ -689,11 +706,17 @@ int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, doubl
     double *d_sep = (double *)(base + al(b_spec) + al(b_z) + al(b_off));
     double *d_out = out_mapped ? out_mapped
                                : (double *)(base + al(b_spec) + al(b_z) + al(b_off) + al(b_sep));
-    CG_CUDA(ctx, cudaMemcpyAsync(d_spec, req_spectrum, b_spec, cudaMemcpyHostToDevice, ctx->stream));
-    CG_CUDA(ctx, cudaMemcpyAsync(d_z, req_z_mean, b_z, cudaMemcpyHostToDevice, ctx->stream));
-    CG_CUDA(ctx, cudaMemcpyAsync(d_off, req_offset, b_off, cudaMemcpyHostToDevice, ctx->stream));
-    if (total > 0)
-        CG_CUDA(ctx, cudaMemcpyAsync(d_sep, sep, b_sep, cudaMemcpyHostToDevice, ctx->stream));
+    // the uploads go through the copy stream, so that they overlap work still
+    // running on the context's stream (the tables of an ASYNC integrals_init);
+    // the request buffer is free: every host-array call ends synchronised
+    if ((st = cg_copy_stream(ctx))) return st;
+    cudaStream_t up = ctx->copy_stream;
+    CG_CUDA(ctx, cudaMemcpyAsync(d_spec, req_spectrum, b_spec, cudaMemcpyHostToDevice, up));
+    CG_CUDA(ctx, cudaMemcpyAsync(d_z, req_z_mean, b_z, cudaMemcpyHostToDevice, up));
+    CG_CUDA(ctx, cudaMemcpyAsync(d_off, req_offset, b_off, cudaMemcpyHostToDevice, up));
+    if (total > 0) CG_CUDA(ctx, cudaMemcpyAsync(d_sep, sep, b_sep, cudaMemcpyHostToDevice, up));
+    CG_CUDA(ctx, cudaEventRecord(ctx->copy_ev[0], up));
+    CG_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[0], 0));
     // the separations are checked on the device copy, in stream order with the
     // work (a non-positive one cannot make a kernel read out of bounds: its
     // lookups give NaN); the flag surfaces as EINVAL after the work has run
@@ -861,11 +884,17 @@ int coffe_gpu_corrfunc(coffe_gpu_ctx_t *ctx, int contrib, int precision, int n_r
     int64_t *d_off = (int64_t *)(base + al(b_spec) + al(b_z));
     double *d_sep = (double *)(base + al(b_spec) + al(b_z) + al(b_off));
     double *d_out = (double *)(base + al(b_spec) + al(b_z) + al(b_off) + al(b_sep));
-    CG_CUDA(ctx, cudaMemcpyAsync(d_spec, req_spectrum, b_spec, cudaMemcpyHostToDevice, ctx->stream));
-    CG_CUDA(ctx, cudaMemcpyAsync(d_z, req_z_mean, b_z, cudaMemcpyHostToDevice, ctx->stream));
-    CG_CUDA(ctx, cudaMemcpyAsync(d_off, req_offset, b_off, cudaMemcpyHostToDevice, ctx->stream));
-    if (total > 0)
-        CG_CUDA(ctx, cudaMemcpyAsync(d_sep, sep, b_sep, cudaMemcpyHostToDevice, ctx->stream));
+    // the uploads go through the copy stream, so that they overlap work still
+    // running on the context's stream (the tables of an ASYNC integrals_init);
+    // the request buffer is free: every host-array call ends synchronised
+    if ((st = cg_copy_stream(ctx))) return st;
+    cudaStream_t up = ctx->copy_stream;
+    CG_CUDA(ctx, cudaMemcpyAsync(d_spec, req_spectrum, b_spec, cudaMemcpyHostToDevice, up));
+    CG_CUDA(ctx, cudaMemcpyAsync(d_z, req_z_mean, b_z, cudaMemcpyHostToDevice, up));
+    CG_CUDA(ctx, cudaMemcpyAsync(d_off, req_offset, b_off, cudaMemcpyHostToDevice, up));
+    if (total > 0) CG_CUDA(ctx, cudaMemcpyAsync(d_sep, sep, b_sep, cudaMemcpyHostToDevice, up));
+    CG_CUDA(ctx, cudaEventRecord(ctx->copy_ev[0], up));
+    CG_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[0], 0));
     st = corrfunc_run(ctx, contrib, precision, n_req, d_spec, d_z, d_off, d_sep, n_mu, d_mu, mu,
                       d_out, total);
     if (st) return st;

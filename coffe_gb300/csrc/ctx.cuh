@@ -27,6 +27,10 @@ struct coffe_gpu_ctx {
     int device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
+    // uploads that overlap work on `stream` (created on first use) and the
+    // events that order them
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_ev[3] = {nullptr, nullptr, nullptr};
     int *d_err = nullptr;   // device error bits (cg_err_bits)
     int *h_err = nullptr;   // pinned mirror
     long long launches = 0; // kernels launched through this context
@@ -188,6 +192,8 @@ int multipoles_noalloc_prepare(coffe_gpu_ctx *ctx);
 // work timed next neither finds its inputs there nor pays for writing the
 // eviction's dirty lines back.
 int cg_l2_evict(coffe_gpu_ctx *ctx, void *buf, size_t bytes, int value);
+// creates ctx->copy_stream and ctx->copy_ev on first use
+int cg_copy_stream(coffe_gpu_ctx *ctx);
 
 // Configuration for one launch shape: the chosen one if the shape was tuned,
 // else (benchmark mode, stream not capturing) the fastest of `cands` timed

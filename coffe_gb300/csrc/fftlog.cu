@@ -1619,10 +1619,8 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         CG_CUDA(ctx, cudaMemcpyAsync(d_meta, &meta, sizeof(TermMeta), cudaMemcpyHostToDevice,
                                      ctx->stream));
     const double *d_pk = pk_on_device ? pk : (const double *)ctx->pk.p;
-    if (!pk_on_device)
-        CG_CUDA(ctx, cudaMemcpyAsync(ctx->pk.p, pk, sizeof(double) * nk * n_spectra,
-                                     cudaMemcpyHostToDevice, ctx->stream));
-    else if (flags & COFFE_GPU_SMALL_R) // kept for the adjoint of the sub-Mpc entries
+    // (host P(k) is uploaded below, once the launch configuration is known)
+    if (pk_on_device && (flags & COFFE_GPU_SMALL_R)) // kept for the adjoint of the sub-Mpc entries
         CG_CUDA(ctx, cudaMemcpyAsync(ctx->pk.p, pk, sizeof(double) * nk * n_spectra,
                                      cudaMemcpyDeviceToDevice, ctx->stream));
 
@@ -1703,39 +1701,51 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     const FusedLayout fl = fused_layout((int)nk, M, inv_g);
     const bool fused_ok = mixed && !tables_df && nk >= (size_t)M + 1 && nk <= 8192 &&
                           N <= 8192 && fl.total <= 200 * 1024;
-    auto stage = [&](const coffe_gpu_tuning_t &tu) -> int {
+    // the fused kernel over spectra [s0, s0 + ns), P(k) of spectrum s0 at pks
+    // (occ: only the kernel's resident blocks per SM, nothing launched)
+    auto launch_fused = [&](const coffe_gpu_tuning_t &tu, int s0, int ns, const double *pks,
+                            int *occ) -> int {
         int s2;
-        if (fused_ok && tu.fft_fused) {
+        const dim3 gfc(ns, n_q);
+        float *tab0 = (float *)ctx->tab_y.p + (size_t)s0 * n_terms * (N + CG_N_SMALL_R + 1);
 #define FUSED_LAUNCH(R, W, G)                                                                     \
     {                                                                                             \
         CG_CUDA(ctx, cudaFuncSetAttribute(fftlog_tables_fused_kernel<R, W, G>,                    \
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,            \
                                           (int)fl.total));                                        \
-        fftlog_tables_fused_kernel<R, W, G><<<gf, FUSED_THREADS, fl.total, ctx->stream>>>(        \
-            g, d_pk, (const float *)ctx->csband.p, (const float *)ctx->csfac32.p,                 \
+        if (occ) {                                                                                \
+            CG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(                           \
+                             occ, fftlog_tables_fused_kernel<R, W, G>, FUSED_THREADS, fl.total)); \
+            return COFFE_GPU_OK;                                                                  \
+        }                                                                                         \
+        fftlog_tables_fused_kernel<R, W, G><<<gfc, FUSED_THREADS, fl.total, ctx->stream>>>(       \
+            g, pks, (const float *)ctx->csband.p, (const float *)ctx->csfac32.p,                  \
             (const int *)ctx->samp_idx.p, (const float2 *)ctx->samp_tdf.p,                        \
             (const float4 *)ctx->samp_f32.p, (const float2 *)ctx->qfac_df.p, wdf,                 \
-            (const float4 *)ctx->twid32.p, d_meta->grp, n_grp, n_terms, m32, p32, tw32,           \
-            (float *)ctx->tab_y.p, fill_small, ctx->d_err);                                       \
+            (const float4 *)ctx->twid32.p, d_meta->grp, n_grp, n_terms, m32, p32, tw32, tab0,     \
+            fill_small, ctx->d_err);                                                              \
         if ((s2 = cg_after_launch(ctx, "fftlog_tables_fused_kernel"))) return s2;                 \
     }
-            const bool swz = tu.fft_swizzle && M >= 64;
-            if (inv_g == 3) {
-                if (tu.fft_radix == 2) {
-                    if (swz) FUSED_LAUNCH(2, true, 3) else FUSED_LAUNCH(2, false, 3)
-                } else {
-                    if (swz) FUSED_LAUNCH(4, true, 3) else FUSED_LAUNCH(4, false, 3)
-                }
+        const bool swz = tu.fft_swizzle && M >= 64;
+        if (inv_g == 3) {
+            if (tu.fft_radix == 2) {
+                if (swz) FUSED_LAUNCH(2, true, 3) else FUSED_LAUNCH(2, false, 3)
             } else {
-                if (tu.fft_radix == 2) {
-                    if (swz) FUSED_LAUNCH(2, true, 1) else FUSED_LAUNCH(2, false, 1)
-                } else {
-                    if (swz) FUSED_LAUNCH(4, true, 1) else FUSED_LAUNCH(4, false, 1)
-                }
+                if (swz) FUSED_LAUNCH(4, true, 3) else FUSED_LAUNCH(4, false, 3)
             }
-#undef FUSED_LAUNCH
-            return COFFE_GPU_OK;
+        } else {
+            if (tu.fft_radix == 2) {
+                if (swz) FUSED_LAUNCH(2, true, 1) else FUSED_LAUNCH(2, false, 1)
+            } else {
+                if (swz) FUSED_LAUNCH(4, true, 1) else FUSED_LAUNCH(4, false, 1)
+            }
         }
+#undef FUSED_LAUNCH
+        return COFFE_GPU_OK;
+    };
+    auto stage = [&](const coffe_gpu_tuning_t &tu) -> int {
+        int s2;
+        if (fused_ok && tu.fft_fused) return launch_fused(tu, 0, n_spectra, d_pk, nullptr);
         if (mixed) {
             const dim3 gb(((int)nk - 2 + CS_TILE - 1) / CS_TILE,
                           (n_spectra + tu.spline_group - 1) / tu.spline_group);
@@ -1852,11 +1862,61 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
                     }
                     cands.push_back(c);
                 }
-    coffe_gpu_tuning_t tu;
     const std::array<long long, 6> key{1, (long long)N, n_spectra, n_terms, n_q,
                                        mixed ? (tables_df ? 2 : 1) : 0};
-    if ((st = cg_tuned(ctx, key, cands, stage, &tu, /*cold=*/true))) return st;
-    if ((st = stage(tu))) return st;
+    coffe_gpu_tuning_t tu = ctx->tuning;
+    bool known = !ctx->autotune;
+    {
+        const auto it = ctx->tune_cache.find(key);
+        if (it != ctx->tune_cache.end()) {
+            tu = it->second;
+            known = true;
+        }
+    }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CG_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cap));
+    // host P(k) for the fused kernel with a known configuration: uploaded in
+    // two parts on the copy stream, so that the tables of the first wave of
+    // spectra (the blocks the device holds at once) are made while the rest
+    // is on its way
+    int first = n_spectra;
+    if (!pk_on_device && known && fused_ok && tu.fft_fused && !(flags & COFFE_GPU_SMALL_R) &&
+        cap == cudaStreamCaptureStatusNone) {
+        int occ = 0;
+        if ((st = launch_fused(tu, 0, 0, nullptr, &occ))) return st;
+        if (ctx->sm_count <= 0)
+            CG_CUDA(ctx, cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount,
+                                                ctx->device));
+        first = std::min(n_spectra, std::max(1, occ * ctx->sm_count / n_q));
+    }
+    if (first < n_spectra) {
+        if ((st = cg_copy_stream(ctx))) return st;
+        const size_t row = sizeof(double) * nk;
+        double *dst = (double *)ctx->pk.p;
+        CG_CUDA(ctx, cudaEventRecord(ctx->copy_ev[0], ctx->stream)); // earlier readers of ctx->pk
+        CG_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev[0], 0));
+        CG_CUDA(ctx, cudaMemcpyAsync(dst, pk, row * first, cudaMemcpyHostToDevice,
+                                     ctx->copy_stream));
+        CG_CUDA(ctx, cudaEventRecord(ctx->copy_ev[1], ctx->copy_stream));
+        CG_CUDA(ctx, cudaMemcpyAsync(dst + (size_t)first * nk, pk + (size_t)first * nk,
+                                     row * (n_spectra - first), cudaMemcpyHostToDevice,
+                                     ctx->copy_stream));
+        CG_CUDA(ctx, cudaEventRecord(ctx->copy_ev[2], ctx->copy_stream)); // P(k) consumed
+        CG_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[1], 0));
+        if ((st = launch_fused(tu, 0, first, dst, nullptr))) return st;
+        CG_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[2], 0));
+        if ((st = launch_fused(tu, first, n_spectra - first, dst + (size_t)first * nk, nullptr)))
+            return st;
+    } else {
+        if (!pk_on_device) {
+            CG_CUDA(ctx, cudaMemcpyAsync(ctx->pk.p, pk, sizeof(double) * nk * n_spectra,
+                                         cudaMemcpyHostToDevice, ctx->stream));
+            if ((st = cg_copy_stream(ctx))) return st;
+            CG_CUDA(ctx, cudaEventRecord(ctx->copy_ev[2], ctx->stream)); // P(k) consumed
+        }
+        if ((st = cg_tuned(ctx, key, cands, stage, &tu, /*cold=*/true))) return st;
+        if ((st = stage(tu))) return st;
+    }
     ctx->last_tuning.fft_threads = tu.fft_threads;
     ctx->last_tuning.fft_threads_fwd = tu.fft_threads_fwd;
     if (mixed) {

@@ -149,9 +149,13 @@ size_t coffe_gpu_integral_table_len(size_t N);
 /* flags bit 1: `pk` is a device pointer (n_spectra * nk doubles). */
 #define COFFE_GPU_PK_DEVICE 2
 /* flags bit 2: enqueue only -- no host synchronisation; device-side errors are
-   reported by the next coffe_gpu_synchronize.  The grid arguments (k, n, l,
-   N) must be those of the previous call so that no per-grid table is rebuilt
-   (otherwise the call synchronises once to build them). */
+   reported by the next call that checks them (coffe_gpu_synchronize, or a
+   host-array coffe_gpu_multipoles).  The grid arguments (k, n, l, N) must be
+   those of the previous call so that no per-grid table is rebuilt (otherwise
+   the call synchronises once to build them).  With host P(k) the call returns
+   once P(k) has been copied (the array may then be reused); the table kernels
+   may still be running, and a following host-array coffe_gpu_multipoles
+   uploads its requests meanwhile. */
 #define COFFE_GPU_ASYNC 4
 /* flags bit 3, COFFE_GPU_MIXED only: the inverse transforms in double-float as
    well (tables to ~1e-7 of their scale, the float storage; about twice the

@@ -148,3 +148,53 @@ def test_set_tuning_rejects_bad_values(setup):
     with pytest.raises(ValueError):
         ctx.set_tuning(warp_size=32)
     ctx.set_tuning(**DEFAULT)
+
+
+def test_pipelined_host_upload_matches_device_input():
+    """Host P(k) on the fused table path is uploaded in two parts that overlap
+    the tables of the first wave of spectra; the tables equal those made from a
+    device copy of the same spectra in one launch, bit for bit."""
+    torch = pytest.importorskip("torch")
+    from coffe_gb300 import workloads
+    from coffe_gb300.api import Context
+
+    b = workloads.cfg3(n_spectra=512)  # more spectra than the device holds blocks of
+    ctx = Context(0)
+    try:
+        ctx.background_init(0.31, 0.05, 9e-5, 0.67, 10000)
+        ctx.set_tuning(**{**DEFAULT, "fft_fused": 1, "fft_swizzle": 1})
+        pin = torch.from_numpy(np.ascontiguousarray(b.pk)).pin_memory()
+        ctx.integrals_init(b.k, pin.numpy(), TERMS, N=4096, precision="mixed", small_r=False)
+        host = np.stack([ctx.integral_table(s, n, l)[1] for s in (0, 303, 304, 305, 511)
+                         for n, l in TERMS])
+        ctx.integrals_init_device(b.k, pin.cuda(), TERMS, N=4096, precision="mixed")
+        dev = np.stack([ctx.integral_table(s, n, l)[1] for s in (0, 303, 304, 305, 511)
+                        for n, l in TERMS])
+        assert np.array_equal(host, dev, equal_nan=True)
+    finally:
+        ctx.close()
+
+
+def test_async_tables_then_host_multipoles_match_sync():
+    """integrals_init(sync=False) returns once P(k) is on the device; the
+    host-array multipole call that follows uploads its requests while the
+    tables are still being made: the results equal the synchronous sequence's."""
+    torch = pytest.importorskip("torch")
+    from coffe_gb300 import workloads
+    from coffe_gb300.api import Context
+
+    b = workloads.subset(workloads.cfg3(n_spectra=512), 512)
+    ctx = Context(0)
+    try:
+        ctx.background_init(0.31, 0.05, 9e-5, 0.67, 10000)
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+        h_pk, h_sep = pin(b.pk), pin(b.sep)
+        out = []
+        for sync in (True, False, False):
+            ctx.integrals_init(b.k, h_pk, TERMS, N=4096, precision="mixed", small_r=False,
+                               sync=sync)
+            out.append(ctx.multipoles(b.req_spectrum, b.req_z_mean, b.req_offset, h_sep, b.ls,
+                                      precision="mixed").copy())
+        assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])
+    finally:
+        ctx.close()
