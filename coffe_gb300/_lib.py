@@ -104,6 +104,7 @@ class Tuning(C.Structure):
         ("fft_threads_fwd", C.c_int),
         ("lane_pack", C.c_int),
         ("fft_fused", C.c_int),
+        ("lane_poly", C.c_int),
     ]
 
 

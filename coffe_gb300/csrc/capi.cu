@@ -110,14 +110,14 @@ __global__ void sep_check_kernel(const double *__restrict__ sep, long long n, in
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) cg_flag(err, CG_ERR_BADSEP);
 }
 
-static int sep_check(coffe_gpu_ctx *ctx, const double *d_sep, long long n)
+static int sep_check(coffe_gpu_ctx *ctx, const double *d_sep, long long n, cudaStream_t stream)
 {
     if (n <= 0) return COFFE_GPU_OK;
     if (ctx->sm_count <= 0)
         CG_CUDA(ctx, cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount,
                                             ctx->device));
     const long long blocks = std::min<long long>((n + 255) / 256, 4LL * ctx->sm_count);
-    sep_check_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(d_sep, n, ctx->d_err);
+    sep_check_kernel<<<(unsigned)blocks, 256, 0, stream>>>(d_sep, n, ctx->d_err);
     return cg_after_launch(ctx, "sep_check_kernel");
 }
 
@@ -551,10 +551,11 @@ int coffe_gpu_set_tuning(coffe_gpu_ctx_t *ctx, const coffe_gpu_tuning_t *t)
         !(t->fft_radix == 2 || t->fft_radix == 4) || !(t->fft_swizzle == 0 || t->fft_swizzle == 1) ||
         !(g == 2 || g == 4 || g == 8) || !(lt == 64 || lt == 128 || lt == 256) ||
         !(t->lane_unroll == 1 || t->lane_unroll == 2) ||
-        !(t->lane_pack == 1 || t->lane_pack == 2) || !(t->fft_fused == 0 || t->fft_fused == 1)) {
+        !(t->lane_pack == 1 || t->lane_pack == 2) || !(t->fft_fused == 0 || t->fft_fused == 1) ||
+        !(t->lane_poly == 0 || t->lane_poly == 1)) {
         cg_set_error(ctx, "set_tuning: fft_threads(_fwd) 128/256/512/1024, fft_radix 2/4, "
                           "fft_swizzle 0/1, spline_group 2/4/8, lane_threads 64/128/256, "
-                          "lane_unroll 1/2, lane_pack 1/2, fft_fused 0/1");
+                          "lane_unroll 1/2, lane_pack 1/2, fft_fused 0/1, lane_poly 0/1");
         return COFFE_GPU_EINVAL;
     }
     ctx->tuning = *t;
@@ -715,15 +716,19 @@ int coffe_gpu_multipoles(coffe_gpu_ctx_t *ctx, int contrib, int precision, doubl
     CG_CUDA(ctx, cudaMemcpyAsync(d_z, req_z_mean, b_z, cudaMemcpyHostToDevice, up));
     CG_CUDA(ctx, cudaMemcpyAsync(d_off, req_offset, b_off, cudaMemcpyHostToDevice, up));
     if (total > 0) CG_CUDA(ctx, cudaMemcpyAsync(d_sep, sep, b_sep, cudaMemcpyHostToDevice, up));
+    // the separations are checked on the device copy, after the uploads (a
+    // non-positive one cannot make a kernel read out of bounds: its lookups
+    // give NaN); the flag surfaces as EINVAL after the work has run
+    if ((st = sep_check(ctx, d_sep, total, up))) return st;
     CG_CUDA(ctx, cudaEventRecord(ctx->copy_ev[0], up));
     CG_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[0], 0));
-    // the separations are checked on the device copy, in stream order with the
-    // work (a non-positive one cannot make a kernel read out of bounds: its
-    // lookups give NaN); the flag surfaces as EINVAL after the work has run
-    if ((st = sep_check(ctx, d_sep, total))) return st;
     ctx->out_host = out_mapped != nullptr;
+    // work that needs only the requests may run on the upload stream (per-kernel
+    // timing keeps everything on one stream)
+    ctx->prep_stream = ctx->timing ? nullptr : up;
     st = multipoles_run(ctx, contrib, precision, epsrel, n_req, d_spec, d_z, d_off, d_sep, n_l, l,
                         d_out, total);
+    ctx->prep_stream = nullptr;
     ctx->out_host = false;
     if (st) {
         cudaStreamSynchronize(ctx->stream); // no kernel may write `out` after return

@@ -31,6 +31,9 @@ struct coffe_gpu_ctx {
     // events that order them
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_ev[3] = {nullptr, nullptr, nullptr};
+    // set by the host-array multipole call for the duration of its run: the
+    // stream its request uploads went to, for work that needs only them
+    cudaStream_t prep_stream = nullptr;
     int *d_err = nullptr;   // device error bits (cg_err_bits)
     int *h_err = nullptr;   // pinned mirror
     long long launches = 0; // kernels launched through this context
@@ -72,8 +75,8 @@ struct coffe_gpu_ctx {
     int n_spectra = 0, n_terms = 0, int_precision = 0;
 
     // ---- launch shapes (coffe_gpu_set_tuning / benchmark-mode autotuning)
-    coffe_gpu_tuning_t tuning = {512, 4, 1, 8, 128, 2, 512, 1, 1}; // default configuration
-    coffe_gpu_tuning_t last_tuning = {512, 4, 1, 8, 128, 2, 512, 1, 1};
+    coffe_gpu_tuning_t tuning = {512, 4, 1, 8, 128, 2, 512, 1, 1, 1}; // default configuration
+    coffe_gpu_tuning_t last_tuning = {512, 4, 1, 8, 128, 2, 512, 1, 1, 1};
     bool autotune = false;
     std::map<std::array<long long, 6>, coffe_gpu_tuning_t> tune_cache; // shape -> choice
     size_t N = 0, nk = 0;

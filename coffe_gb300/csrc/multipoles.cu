@@ -144,6 +144,79 @@ template <typename T> void build_node_table_fast(int NL, const int *ls, std::vec
     }
 }
 
+// ------------------------------------------ integrand as a polynomial in mu^2
+//
+// For the fast kernels' case (unit biases, even multipoles, equal tracers) the
+// den/RSD integrand at a node is a polynomial in w = mu^2 times powers of
+// 1/D, D = 2 chi1 chi2 = 2 chi^2 (1 - w r^2 / (4 chi^2)): the background
+// polynomials are polynomials in t^2 = rho^2 w (their odd parts pair up into
+// even products), the mu-only RSD coefficients are quadratics in w, and 1/D
+// is a geometric series in w r^2 / (4 chi^2) <= (r / 2 chi)^2 < 0.01 here.
+// mp_poly_kernel therefore forms, once per (request, separation), the
+// coefficients of the integrand in w up to MP_PJ (the 1/D series to MP_PS
+// terms; truncation < 1e-12 of the integrand over 5 <= r <= 375 Mpc,
+// chi >= 1300 Mpc), and the Kronrod and Gauss sums of the first panel
+// become dot products of those coefficients with the rule's moments
+// sum_k w_k P_l(mu_k) mu_k^(2j) (host, FP64).  Only QUADPACK's |f| and
+// |f - mean| sums still need the integrand at the 31 nodes: a Horner
+// evaluation each.
+#define MP_PJ 8
+#define MP_PS 4
+#define MP_FAST_MAX_L 4
+template <typename T> struct PolyMom {
+    T mk[MP_FAST_MAX_L][MP_PJ + 1]; // sum_k mult wk P_l mu_k^(2j)
+    T mg[MP_FAST_MAX_L][MP_PJ + 1]; // sum_k mult wg P_l mu_k^(2j)
+};
+template <typename T> PolyMom<T> poly_moments(int NL, const int *ls)
+{
+    const PanelTables<double> &P = panel_tables();
+    PolyMom<T> m;
+    for (int j = 0; j < NL; ++j) {
+        double sk[MP_PJ + 1] = {0}, sg[MP_PJ + 1] = {0};
+        for (int k = 0; k < 31; ++k) {
+            const int sl = P.order[30 + k];
+            const double mult = sl == 60 ? 1.0 : 2.0;
+            const double w = P.mu_sorted[30 + k] * P.mu_sorted[30 + k];
+            double wp = 1.0;
+            for (int e = 0; e <= MP_PJ; ++e, wp *= w) {
+                sk[e] += mult * P.wkP[ls[j]][sl] * wp;
+                sg[e] += mult * P.wgP[ls[j]][sl] * wp;
+            }
+        }
+        for (int e = 0; e <= MP_PJ; ++e) {
+            m.mk[j][e] = (T)sk[e];
+            m.mg[j][e] = (T)sg[e];
+        }
+    }
+    for (int j = NL; j < MP_FAST_MAX_L; ++j)
+        for (int e = 0; e <= MP_PJ; ++e) m.mk[j][e] = m.mg[j][e] = T(0);
+    return m;
+}
+// node rows of mp_poly_kernel: w = mu^2, mult wk, P_l (NL), mult wk |P_l| (NL)
+template <int NL> struct PolyLayout {
+    static constexpr int R = (2 + 2 * NL + 3) / 4 * 4;
+    static constexpr int ROWS = 31;
+    static constexpr int COUNT = ROWS * R;
+};
+template <typename T> void build_node_table_poly(int NL, const int *ls, std::vector<T> &out)
+{
+    const PanelTables<double> &P = panel_tables();
+    const int R = (2 + 2 * NL + 3) / 4 * 4;
+    out.assign((size_t)31 * R, T(0));
+    for (int k = 0; k < 31; ++k) {
+        const int sl = P.order[30 + k];
+        const double mult = sl == 60 ? 1.0 : 2.0;
+        const double mu = P.mu_sorted[30 + k];
+        T *r = out.data() + (size_t)k * R;
+        r[0] = (T)(mu * mu);
+        r[1] = (T)(mult * P.wk[sl]);
+        for (int j = 0; j < NL; ++j) {
+            r[2 + j] = (T)P.Pl[ls[j]][sl];
+            r[2 + NL + j] = (T)(mult * P.wkA[ls[j]][sl]);
+        }
+    }
+}
+
 // The node table of mp_fast2_kernel (layout Fast2Layout<NL>): every constant of
 // the rows mu >= 0 stored twice, as the packed pair (c, c) both lanes of a
 // packed FP32 operation use; pass-1 pairs mu, -mu, -mu^2, 1 - mu^2, a2, a1, a0,
@@ -982,6 +1055,224 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
     }
 }
 
+// o += a b, truncated to the NO lowest coefficients
+template <int NA, int NB, int NO, typename T>
+__device__ __forceinline__ void poly_fma(const T (&a)[NA], const T (&b)[NB], T (&o)[NO])
+{
+#pragma unroll
+    for (int i = 0; i < NA; ++i)
+#pragma unroll
+        for (int j = 0; j < NB; ++j)
+            if (i + j < NO) o[i + j] = fma(a[i], b[j], o[i + j]);
+}
+
+// The first-panel integrand of one (request, separation) as coefficients of
+// w = mu^2 (mp_fast_kernel's algebra, functions.c:129-362, 670-771, expanded):
+//   v = G1 G2 I00 + F1 F2 R(c) + (G1 F2 + F1 G2) K1 + g I02 (G1 F2 chi1^2 + F1 G2 chi2^2)
+// with G1 G2 = gE^2 - rho^2 w gO^2, F1 F2 = fE^2 - rho^2 w fO^2,
+// G1 F2 + F1 G2 = 2 A, A = gE fE - rho^2 w gO fO, and
+// G1 F2 chi1^2 + F1 G2 chi2^2 = 2 A (chi^2 + w r^2 / 4) - 2 rho r chi w B,
+// B = gE fO - gO fE; c = 1 - r^2 (1 - w) / D, g = (1 + c)(1 - w) / D.
+template <int CONTRIB, typename T>
+__device__ __forceinline__ void poly_integrand(const BgFitT<T> &bf, T chim, T r, T rho, T I00,
+                                               T I02, T I04, T (&v)[MP_PJ + 1])
+{
+    constexpr int N = MP_PJ + 1;
+#pragma unroll
+    for (int j = 0; j < N; ++j) v[j] = T(0);
+    const T p2 = rho * rho, p4 = p2 * p2;
+    const T gE[3] = {bf.ge.x, bf.ge.y * p2, bf.ge.z * p4};
+    const T gO[3] = {bf.go.x, bf.go.y * p2, bf.go.z * p4};
+    const T fE[3] = {bf.fe.x, bf.fe.y * p2, bf.fe.z * p4};
+    const T fO[3] = {bf.fo.x, bf.fo.y * p2, bf.fo.z * p4};
+    // a w-shifted product: o[j + 1] += s a[i] b[j - i]
+    auto shifted = [&](const T(&a)[3], const T(&b)[3], T sc, T(&o)[6]) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) o[i + j + 1] = fma(sc * a[i], b[j], o[i + j + 1]);
+    };
+    if (CONTRIB & COFFE_GPU_DEN) {
+        T GG[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+        poly_fma(gE, gE, GG);
+        shifted(gO, gO, -p2, GG);
+#pragma unroll
+        for (int j = 0; j < 6; ++j) v[j] = GG[j] * I00;
+    }
+    if (CONTRIB & COFFE_GPU_RSD) {
+        const T h = T(0.5) / (chim * chim), x = r * r * T(0.5) * h; // 1/(2 chi^2), r^2/(4 chi^2)
+        T iD[MP_PS + 1];
+        iD[0] = h;
+#pragma unroll
+        for (int n = 1; n <= MP_PS; ++n) iD[n] = iD[n - 1] * x;
+        // s = r^2 (1 - w) / D, c = 1 - s
+        T c[MP_PS + 2];
+        const T rr = r * r;
+        c[0] = T(1) - rr * iD[0];
+#pragma unroll
+        for (int n = 1; n <= MP_PS; ++n) c[n] = rr * (iD[n - 1] - iD[n]);
+        c[MP_PS + 1] = rr * iD[MP_PS];
+        T c2[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) c2[j] = T(0);
+        poly_fma(c, c, c2);
+        const T e00 = I00 * T(1.0 / 15.0), e02 = I02 * T(1.0 / 21.0), e04 = I04 * T(1.0 / 35.0);
+        // R(c) = g2c c^2 + g1c c + g0c with the quadratics in w of the node table
+        const T g2c[3] = {fma(T(0.75), e04, fma(T(-2), e02, T(2) * e00)),
+                          fma(T(2.5), e04, T(-9) * e02), T(8.75) * e04};
+        const T g1c[3] = {fma(T(-2.5), e04, T(9) * e02), fma(T(-15), e04, T(-9) * e02),
+                          T(17.5) * e04};
+        const T g0c[3] = {fma(T(4.75), e04, e00 - e02), T(-17.5) * e04, T(8.75) * e04};
+        T R[N] = {g0c[0], g0c[1], g0c[2]};
+#pragma unroll
+        for (int j = 3; j < N; ++j) R[j] = T(0);
+        poly_fma(g2c, c2, R);
+        poly_fma(g1c, c, R);
+        T FF[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+        poly_fma(fE, fE, FF);
+        shifted(fO, fO, -p2, FF);
+        poly_fma(FF, R, v);
+        if (CONTRIB & COFFE_GPU_DEN) {
+            T Am[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+            poly_fma(gE, fE, Am);
+            shifted(gO, fO, -p2, Am);
+            T Bm[5] = {T(0), T(0), T(0), T(0), T(0)};
+            poly_fma(gE, fO, Bm);
+            const T mgO[3] = {-gO[0], -gO[1], -gO[2]};
+            poly_fma(mgO, fE, Bm);
+            const T K1 = (I00 - T(2) * I02) * T(1.0 / 3.0);
+#pragma unroll
+            for (int j = 0; j < 6; ++j) v[j] = fma(T(2) * K1, Am[j], v[j]);
+            // Q = 2 A (chi^2 + w r^2/4) - 2 rho r chi w B
+            T Q[7];
+            const T cq0 = T(2) * chim * chim, cq1 = T(0.5) * rr, cb = T(-2) * rho * r * chim;
+            Q[0] = cq0 * Am[0];
+#pragma unroll
+            for (int j = 1; j < 6; ++j) Q[j] = fma(cq0, Am[j], fma(cq1, Am[j - 1], cb * Bm[j - 1]));
+            Q[6] = cq1 * Am[5];
+            // g = (2 - s)(1 - w) / D = (1 + c)(1 - w) / D
+            T om[MP_PS + 3];
+            const T cp0 = T(1) + c[0];
+            om[0] = cp0;
+#pragma unroll
+            for (int n = 1; n <= MP_PS + 1; ++n)
+                om[n] = c[n] - (n == 1 ? cp0 : c[n - 1]);
+            om[MP_PS + 2] = -c[MP_PS + 1];
+            T g[N];
+#pragma unroll
+            for (int j = 0; j < N; ++j) g[j] = T(0);
+            poly_fma(om, iD, g);
+#pragma unroll
+            for (int j = 0; j < N; ++j) g[j] *= I02;
+            poly_fma(g, Q, v);
+        }
+    }
+}
+
+// Mixed path (T = float) and its FP64 baseline (T = double), unit biases and
+// even multipoles: mp_fast_kernel's first panel with the integrand as the
+// polynomial of poly_integrand (Kronrod and Gauss sums as moments; the |f|
+// and |f - mean| sums from a Horner evaluation at each node).
+template <int NL, int CONTRIB, int UNROLL, typename T>
+__global__ void __launch_bounds__(MP_FAST_MAX_THREADS)
+    mp_poly_kernel(MpArgs a, const BgFitT<T> *__restrict__ fit, T chi_lo, T chi_hi,
+                   const T *__restrict__ tab_x, const T *__restrict__ tab_y,
+                   const int *__restrict__ req_spectrum, const double *__restrict__ req_z_mean,
+                   const int64_t *__restrict__ req_offset, const double *__restrict__ sep,
+                   long long total, const T *__restrict__ nodes, PolyMom<T> mom,
+                   double *__restrict__ out, int *__restrict__ retry_count,
+                   int2 *__restrict__ retry, int *err)
+{
+    typedef PolyLayout<NL> LY;
+    extern __shared__ __align__(16) unsigned char mp_smem[];
+    T *tab = reinterpret_cast<T *>(mp_smem);                           // [ROWS][R]
+    double *stage = reinterpret_cast<double *>(tab + LY::COUNT);      // [blockDim][NL]
+    for (int i = threadIdx.x; i < LY::COUNT; i += blockDim.x) tab[i] = nodes[i];
+    __syncthreads();
+    const long long item0 = (long long)blockIdx.x * blockDim.x;
+    const long long item = item0 + threadIdx.x;
+    if (item >= total && !a.out_staged) return; // the staged store needs every thread
+    const bool valid = item < total;
+    const int q = valid ? find_request(req_offset, a.n_req, item) : 0;
+    const int s = req_spectrum[q];
+    const T r = valid ? from_f64<T>(sep[item]) : T(1);
+    const BgFitT<T> bf = fit[q];
+    const T chim = bf.go.w;
+    const T *y0 = tab_y + ((size_t)s * a.n_terms) * a.tab_len;
+    const T idl = from_f64<T>(a.inv_dlog);
+    const int tl = a.tab_len;
+    const T I00 = table_lookup<T, true>(tab_x, y0 + (size_t)a.t00 * tl, tl, idl, r);
+    const T I02 = table_lookup<T, true>(tab_x, y0 + (size_t)a.t02 * tl, tl, idl, r);
+    const T I04 = table_lookup<T, true>(tab_x, y0 + (size_t)a.t04 * tl, tl, idl, r);
+    T K[NL], G[NL], A[NL], asc[NL];
+#pragma unroll
+    for (int j = 0; j < NL; ++j) K[j] = G[j] = A[j] = asc[j] = T(0);
+    const T half_r = T(0.5) * r;
+    const T span = half_r * sqrt(tab[(LY::ROWS - 1) * LY::R]); // largest mu
+    const bool inside = valid && (chim - span >= chi_lo) && (chim + span <= chi_hi);
+    const bool finite = inside && isfinite(I00) && isfinite(I02) && isfinite(I04);
+    if (inside) {
+        T v[MP_PJ + 1];
+        poly_integrand<CONTRIB, T>(bf, chim, r, half_r * bf.ge.w, I00, I02, I04, v);
+        T Kh[NL];
+#pragma unroll
+        for (int j = 0; j < NL; ++j) {
+            T k = T(0), g = T(0);
+#pragma unroll
+            for (int e = MP_PJ; e >= 0; --e) {
+                k = fma(v[e], mom.mk[j][e], k);
+                g = fma(v[e], mom.mg[j][e], g);
+            }
+            K[j] = k;
+            G[j] = g;
+            Kh[j] = T(-0.5) * k;
+        }
+#pragma unroll UNROLL
+        for (int n = 0; n < LY::ROWS; ++n) {
+            T rec[LY::R];
+            lds_rec<LY::R>(tab + n * LY::R, rec);
+            const T w = rec[0];
+            T f = v[MP_PJ];
+#pragma unroll
+            for (int e = MP_PJ - 1; e >= 0; --e) f = fma(f, w, v[e]);
+            const T af = fabs(f);
+#pragma unroll
+            for (int j = 0; j < NL; ++j) {
+                A[j] = fma(rec[2 + NL + j], af, A[j]);
+                asc[j] = fma(rec[1], fabs(fma(f, rec[2 + j], Kh[j])), asc[j]);
+            }
+        }
+    }
+    if (!a.out_staged) {
+        first_panel_out<NL, T>(a, from_f64<T>(a.epsrel), item, finite, K, G, A, asc, out,
+                               retry_count, retry, err);
+        return;
+    }
+    // out in page-locked host memory: staged in shared memory, stored as
+    // consecutive 16-byte words (mp_fast_kernel's epilogue)
+    double res[NL];
+    bool have[NL];
+    if (valid)
+        first_panel_value<NL, T>(a, from_f64<T>(a.epsrel), item, finite, K, G, A, asc, res, have,
+                                 retry_count, retry, err);
+    const int tid = threadIdx.x, bd = blockDim.x;
+    if (valid) {
+#pragma unroll
+        for (int j = 0; j < NL; ++j) stage[tid * NL + j] = res[j];
+    }
+    __syncthreads();
+    const int n = (int)min((long long)bd, total - item0) * NL;
+    double *o = out + item0 * NL;
+    if ((reinterpret_cast<uintptr_t>(o) & 15) == 0) {
+        const double2 *s2 = reinterpret_cast<const double2 *>(stage);
+        double2 *o2 = reinterpret_cast<double2 *>(o);
+        for (int i = tid; i < n / 2; i += bd) o2[i] = s2[i];
+        if ((n & 1) && tid == 0) o[n - 1] = stage[n - 1];
+    } else {
+        for (int i = tid; i < n; i += bd) o[i] = stage[i];
+    }
+}
+
 // ---------------------------------- mixed path, two separations per thread
 //
 // mp_fast_kernel's algorithm (float) with every per-node operation on packed
@@ -1387,18 +1678,47 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S
                         },
                         &dn2)))
         return st;
+    // the polynomial kernel's node rows and the rule's moments
+    const void *dnp = nullptr;
+    if ((st = node_slot(ctx, a.n_l, a.ls, prec_tag, 4,
+                        [&](std::vector<unsigned char> &bytes) {
+                            std::vector<T> tab;
+                            build_node_table_poly<T>(a.n_l, a.ls, tab);
+                            bytes.assign((const unsigned char *)tab.data(),
+                                         (const unsigned char *)(tab.data() + tab.size()));
+                        },
+                        &dnp)))
+        return st;
+    const PolyMom<T> mom = poly_moments<T>(a.n_l, a.ls);
+    // the per-request background polynomials (independent of the launch
+    // shape); on ctx->prep_stream when the caller gives one (its uploads of
+    // the requests run there), so that they overlap earlier work on the stream
+    {
+        cudaStream_t fs = ctx->prep_stream ? ctx->prep_stream : ctx->stream;
+        mp_bgfit_kernel<T, S><<<(a.n_req + MP_FIT_WARPS - 1) / MP_FIT_WARPS, 32 * MP_FIT_WARPS, 0,
+                                fs>>>(chi_of_z, bg.z_of_chi, bg.D1, bg.f, a.n_req, vinv,
+                                      req_z_mean, req_offset, sep, d_fit);
+        if ((st = cg_after_launch(ctx, "mp_bgfit_kernel"))) return st;
+        if (ctx->prep_stream) {
+            CG_CUDA(ctx, cudaEventRecord(ctx->copy_ev[1], fs));
+            CG_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[1], 0));
+        }
+    }
     auto run = [&](const coffe_gpu_tuning_t &tu) -> int {
         const int lt = tu.lane_threads;
-        const bool pack = can_pack && tu.lane_pack == 2;
+        const bool pack = can_pack && tu.lane_pack == 2 && !tu.lane_poly;
         const long long blocks = (total + (pack ? 2 : 1) * lt - 1) / ((pack ? 2 : 1) * lt);
         CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
-        mp_bgfit_kernel<T, S><<<(a.n_req + MP_FIT_WARPS - 1) / MP_FIT_WARPS, 32 * MP_FIT_WARPS, 0,
-                                ctx->stream>>>(chi_of_z, bg.z_of_chi, bg.D1, bg.f, a.n_req, vinv,
-                                               req_z_mean, req_offset, sep, d_fit);
-        int s1 = cg_after_launch(ctx, "mp_bgfit_kernel");
-        if (s1) return s1;
 #define MP_FAST_U(NLV, CV, UV)                                                                    \
-    if (pack) {                                                                                   \
+    if (tu.lane_poly) {                                                                           \
+        const size_t smem = sizeof(T) * PolyLayout<NLV>::COUNT + sizeof(double) * NLV * lt;       \
+        CG_CUDA(ctx, cudaFuncSetAttribute(mp_poly_kernel<NLV, CV, UV, T>,                         \
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,            \
+                                          (int)smem));                                            \
+        mp_poly_kernel<NLV, CV, UV, T><<<(unsigned)blocks, lt, smem, ctx->stream>>>(              \
+            a, d_fit, bg.z_of_chi.x0, bg.z_of_chi.xn, tab_x, tab_y, req_spectrum, req_z_mean,     \
+            req_offset, sep, total, (const T *)dnp, mom, out, d_count, d_retry, ctx->d_err);      \
+    } else if (pack) {                                                                            \
         const size_t smem = sizeof(float) * Fast2Layout<NLV>::COUNT +                             \
                             sizeof(f2) * Fast2Layout<NLV>::ROWS * lt;                             \
         CG_CUDA(ctx, cudaFuncSetAttribute(mp_fast2_kernel<NLV, CV, UV>,                           \
@@ -1432,7 +1752,7 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S
 #undef MP_FAST_NL
 #undef MP_FAST
 #undef MP_FAST_U
-        int s2 = cg_after_launch(ctx, "mp_fast_kernel");
+        int s2 = cg_after_launch(ctx, tu.lane_poly ? "mp_poly_kernel" : "mp_fast_kernel");
         if (s2) return s2;
         mp_retry_kernel<T, S, T><<<ctx->sm_count * 2, 32 * MP_RETRY_WARPS, 0, ctx->stream>>>(
             a, bg, chi_of_z, tab_x, tab_y, req_spectrum, req_z_mean, req_offset, sep, out,
@@ -1440,16 +1760,18 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S
         return cg_after_launch(ctx, "mp_retry_kernel");
     };
     std::vector<coffe_gpu_tuning_t> cands;
-    for (int pk : {1, 2})
-        for (int lt : {64, 128, 256})
-            for (int un : {1, 2}) {
-                if (pk == 2 && !can_pack) continue;
-                coffe_gpu_tuning_t c = ctx->tuning;
-                c.lane_threads = lt;
-                c.lane_unroll = un;
-                c.lane_pack = pk;
-                cands.push_back(c);
-            }
+    for (int po : {1, 0})
+        for (int pk : {1, 2})
+            for (int lt : {64, 128, 256})
+                for (int un : {1, 2}) {
+                    if (pk == 2 && (!can_pack || po)) continue;
+                    coffe_gpu_tuning_t c = ctx->tuning;
+                    c.lane_threads = lt;
+                    c.lane_unroll = un;
+                    c.lane_pack = pk;
+                    c.lane_poly = po;
+                    cands.push_back(c);
+                }
     coffe_gpu_tuning_t tu;
     long long bucket = 0;
     while ((1ll << bucket) < total) ++bucket;
@@ -1457,7 +1779,8 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S
     if ((st = cg_tuned(ctx, key, cands, run, &tu))) return st;
     ctx->last_tuning.lane_threads = tu.lane_threads;
     ctx->last_tuning.lane_unroll = tu.lane_unroll;
-    ctx->last_tuning.lane_pack = can_pack ? tu.lane_pack : 1;
+    ctx->last_tuning.lane_pack = can_pack && !tu.lane_poly ? tu.lane_pack : 1;
+    ctx->last_tuning.lane_poly = tu.lane_poly;
     return run(tu);
 }
 

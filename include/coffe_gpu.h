@@ -362,6 +362,10 @@ typedef struct {
     int fft_fused;    /* 1: the mixed table stage as one kernel per (spectrum, q), all in
                          shared memory (where it fits: FFT size <= 8192, the k grid no
                          shorter than N/2 + 1 and no longer than 8192); 0: three kernels */
+    int lane_poly;    /* 1: that kernel forms each separation's integrand as a polynomial
+                         in mu^2 once and takes the first-panel sums as its moments; 0:
+                         the integrand evaluated at every node (same results to float
+                         rounding) */
 } coffe_gpu_tuning_t;
 
 /* ---- the divergent integral I^4_0 and its renormalisation (integrals.c:773-914),

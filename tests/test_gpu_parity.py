@@ -303,32 +303,39 @@ def test_multipoles_batch_fp64(gpu_ctx, small_batch, small_batch_ref):
     assert e < 1e-10, e
 
 
-def test_multipoles_batch_mixed(gpu_ctx, small_batch, small_batch_ref):
+@pytest.mark.parametrize("poly", [1, 0])
+def test_multipoles_batch_mixed(gpu_ctx, small_batch, small_batch_ref, poly):
     b = small_batch
+    gpu_ctx.set_tuning(lane_poly=poly)
     gpu_ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
     gpu_ctx.integrals_init(b.k, b.pk, [(0, 0), (0, 2), (0, 4)], N=4096, precision="mixed",
                            small_r=False)
     got = _run_batch(gpu_ctx, b, "mixed")
+    gpu_ctx.set_tuning(lane_poly=1)
     e = np.max(np.abs(got - small_batch_ref) /
                np.maximum(np.abs(small_batch_ref), _per_l_floor(small_batch_ref, b, 1e-3)))
-    print("mixed max rel error:", e)
+    print("mixed max rel error (polynomial integrand %d):" % poly, e)
     assert e < 1e-4, e
 
 
-def test_multipoles_batch_fp64_fastalg(gpu_ctx, small_batch, small_batch_ref):
+@pytest.mark.parametrize("poly", [1, 0])
+def test_multipoles_batch_fp64_fastalg(gpu_ctx, small_batch, small_batch_ref, poly):
     """COFFE_GPU_FP64_FASTALG (the mixed path's algorithm in FP64, the
-    precision-only baseline of the mixed path) against the oracle: its only
-    approximation is the degree-5 background polynomial along each request's
-    line of sight, ~(X/L)^6 ~ 1e-8 relative; asserted at 1e-6 with the
-    per-request floor of the other batch tests."""
+    precision-only baseline of the mixed path) against the oracle: its
+    approximations are the degree-5 background polynomial along each request's
+    line of sight, ~(X/L)^6 ~ 1e-8 relative, and (polynomial integrand) the
+    truncated 1/D series, < 1e-12; asserted at 1e-6 with the per-request floor
+    of the other batch tests."""
     b = small_batch
+    gpu_ctx.set_tuning(lane_poly=poly)
     gpu_ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
     gpu_ctx.integrals_init(b.k, b.pk, [(0, 0), (0, 2), (0, 4)], N=4096, precision="fp64",
                            small_r=False)
     got = _run_batch(gpu_ctx, b, "fp64-fastalg")
+    gpu_ctx.set_tuning(lane_poly=1)
     e = np.max(np.abs(got - small_batch_ref) /
                np.maximum(np.abs(small_batch_ref), _per_l_floor(small_batch_ref, b, 1e-3)))
-    print("fp64-fastalg max rel error:", e)
+    print("fp64-fastalg max rel error (polynomial integrand %d):" % poly, e)
     assert e < 1e-6, e
 
 
