@@ -50,11 +50,16 @@ template <typename T> __device__ __forceinline__ T qk_eps();
 template <> __device__ __forceinline__ double qk_eps<double>() { return CG_DBL_EPS; }
 template <> __device__ __forceinline__ float qk_eps<float>() { return 1.1920928955078125e-07f; }
 
+// x^1.5: pow as QUADPACK writes it in FP64; x sqrt(x) in FP32 (the same
+// function to an ulp, a fraction of powf's instructions)
+__device__ __forceinline__ double qk_pow15(double x) { return pow(x, 1.5); }
+__device__ __forceinline__ float qk_pow15(float x) { return x * sqrtf(x); }
+
 template <typename T> __device__ __forceinline__ T qk_rescale_error(T err, T result_abs, T result_asc)
 {
     err = fabs(err);
     if (result_asc != T(0) && err != T(0)) {
-        const T scale = pow((T(200) * err / result_asc), T(1.5));
+        const T scale = qk_pow15(T(200) * err / result_asc);
         err = scale < T(1) ? result_asc * scale : result_asc;
     }
     if (result_abs > qk_tiny<T>()) {

@@ -38,7 +38,8 @@ def test_kernel_timing_names_the_launched_kernels(fresh_ctx):
     print(t)
     tables = (("fftlog_tables_fused_kernel",) if ctx.tuning()["fft_fused"] else
               ("fftlog_forward_df_kernel", "fftlog_inverse_f32_kernel"))
-    for name in tables + ("mp_fast_kernel",):
+    lanes = ("mp_poly_kernel",) if ctx.tuning()["lane_poly"] else ("mp_fast_kernel",)
+    for name in tables + lanes:
         assert name in t, (name, sorted(t))
         assert t[name][0] >= 1 and t[name][1] > 0
     assert ctx.kernel_times() == {}  # reset by the previous read
