@@ -330,6 +330,10 @@ __global__ void cspline_c_kernel(const double *__restrict__ x, const double *__r
 // ~(h/k)^2.  One thread per knot for CS_SPB spectra, rhs staged in shared
 // memory, the band stored by diagonal so that its loads coalesce.
 #define CS_BAND 12
+// row stride of the band: m rounded up to a multiple of 8 (zeros past m), so
+// that 8 consecutive coefficients of a row are two aligned float4
+__host__ __device__ inline int cs_band_stride(int m) { return (m + 7) & ~7; }
+
 #define CS_TILE 256
 #define CS_HALO (CS_TILE + 2 * CS_BAND + 2)
 // One pass per (tile of knots, group of CS_SPB spectra): reads the FP64
@@ -379,7 +383,8 @@ __global__ void __launch_bounds__(CS_TILE)
     if (i < m) {
         float bw[2 * CS_BAND + 1];
 #pragma unroll
-        for (int d = 0; d <= 2 * CS_BAND; ++d) bw[d] = __ldg(band_t + (size_t)d * m + i);
+        for (int d = 0; d <= 2 * CS_BAND; ++d)
+            bw[d] = __ldg(band_t + (size_t)d * cs_band_stride(m) + i);
         for (int q = 0; q < ns; ++q) {
             float acc = 0.f;
 #pragma unroll
@@ -400,7 +405,8 @@ __global__ void __launch_bounds__(CS_TILE)
 void cspline_band_host(const std::vector<double> &x, std::vector<float> &band)
 {
     const int nk = (int)x.size(), m = nk - 2, W = 3 * CS_BAND, B = 2 * CS_BAND + 1;
-    band.assign((size_t)m * B, 0.f);
+    const int ms = cs_band_stride(m);
+    band.assign((size_t)ms * B, 0.f);
     std::vector<double> dg(2 * W + 1), up(2 * W + 1), rhs(2 * W + 1);
     for (int j = 0; j < m; ++j) {
         const int lo = std::max(0, j - W), hi = std::min(m, j + W + 1), n = hi - lo;
@@ -420,7 +426,7 @@ void cspline_band_host(const std::vector<double> &x, std::vector<float> &band)
         for (int r = n - 2; r >= 0; --r) rhs[r] = (rhs[r] - up[r] * rhs[r + 1]) / dg[r];
         for (int d = -CS_BAND; d <= CS_BAND; ++d) {
             const int i = j + d;
-            if (i >= lo && i < hi) band[(size_t)(d + CS_BAND) * m + j] = (float)rhs[i - lo];
+            if (i >= lo && i < hi) band[(size_t)(d + CS_BAND) * ms + j] = (float)rhs[i - lo];
         }
     }
 }
@@ -996,7 +1002,7 @@ __host__ __device__ inline FusedLayout fused_layout(int nk, int M, int G)
 
 #define FUSED_THREADS 512
 template <int RADIX, bool SWZ, int G>
-__global__ void __launch_bounds__(FUSED_THREADS)
+__global__ void __launch_bounds__(FUSED_THREADS, 2)
     fftlog_tables_fused_kernel(GridPar g, const double *__restrict__ pk,
                                const float *__restrict__ band_t, const float *__restrict__ fac32,
                                const int *__restrict__ idx, const float2 *__restrict__ tdf,
@@ -1040,13 +1046,36 @@ __global__ void __launch_bounds__(FUSED_THREADS)
     }
     __syncthreads();
     // spline coefficients: the band of the inverse spline matrix times the
-    // right-hand sides (cspline_band_kernel's product)
-    for (int i = tid; i < m; i += bd) {
-        float acc = 0.f;
+    // right-hand sides (cspline_band_kernel's product), 8 consecutive rows per
+    // thread: their 32 right-hand sides in registers, the band rows as aligned
+    // float4 pairs (the band's row stride is a multiple of 8, zero-padded; the
+    // right-hand-side window of the last rows reads past m + 2 CS_BAND into the
+    // transform buffer, for rows past m, whose results are not kept)
+    {
+        const int ms = cs_band_stride(m);
+        for (int i0 = 8 * tid; i0 < m; i0 += 8 * bd) {
+            float win[8 + 2 * CS_BAND + 4];
 #pragma unroll
-        for (int d = 0; d <= 2 * CS_BAND; ++d)
-            acc = fmaf(__ldg(band_t + (size_t)d * m + i), rhs[i + d], acc);
-        cs[i + 1] = acc;
+            for (int k = 0; k < (8 + 2 * CS_BAND + 4) / 4; ++k) {
+                const float4 v = reinterpret_cast<const float4 *>(rhs + i0)[k];
+                win[4 * k] = v.x;
+                win[4 * k + 1] = v.y;
+                win[4 * k + 2] = v.z;
+                win[4 * k + 3] = v.w;
+            }
+            float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int d = 0; d <= 2 * CS_BAND; ++d) {
+                const float4 *bp = reinterpret_cast<const float4 *>(band_t + (size_t)d * ms + i0);
+                const float4 b0 = __ldg(bp), b1 = __ldg(bp + 1);
+                const float bw[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[j] = fmaf(bw[j], win[j + d], acc[j]);
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (i0 + j < m) cs[i0 + j + 1] = acc[j];
+        }
     }
     if (tid == 0) {
         cs[0] = 0.f;
