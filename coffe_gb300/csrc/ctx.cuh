@@ -101,6 +101,8 @@ struct coffe_gpu_ctx {
     // host copies of the per-grid spline factors and band (sources of the uploads)
     std::vector<double> grid_fac_host;
     std::vector<float> grid_fac32_host, grid_band_host;
+    int grid_band_ok = 0;         // the band factorises (geometric k grid)
+    float grid_band_tau[25] = {}; // its 2 CS_BAND + 1 constants
     DevBuf samp_tdf;  // N float2: double-float dx / h of each FFT node (mixed path)
     DevBuf qfac_df;   // n_q * N float2: double-float windowed bias (mixed path)
     DevBuf pk_df;     // n_spectra * nk float2: double-float input spectra (mixed path)

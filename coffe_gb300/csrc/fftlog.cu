@@ -431,6 +431,50 @@ void cspline_band_host(const std::vector<double> &x, std::vector<float> &band)
     }
 }
 
+// On a geometric k grid (h_j = h rho^j) the spline matrix is diag(h_i) times a
+// Toeplitz matrix, so away from the ends (rows CS_BAND .. m - CS_BAND - 1) its
+// inverse's band is tau_d g_{i+d}, g_j = 1 / h_j: 25 constants times one scale
+// per knot.  BandFac holds the constants when the band has that form to float
+// accuracy; the fused table kernel then multiplies the right-hand sides by g
+// once and needs no band rows but the 2 CS_BAND end rows (their coefficients
+// divided by g, appended to the band buffer).
+struct BandFac {
+    int ok;
+    float tau[2 * CS_BAND + 1];
+};
+BandFac cspline_band_factor(const std::vector<double> &x, const std::vector<float> &band,
+                            std::vector<float> &edge)
+{
+    BandFac f;
+    f.ok = 0;
+    const int nk = (int)x.size(), m = nk - 2, ms = cs_band_stride(m), B = 2 * CS_BAND + 1;
+    edge.assign((size_t)2 * CS_BAND * B, 0.f);
+    if (m < 4 * CS_BAND + 8) return f;
+    auto g = [&](int j) { return 1.0 / (x[j + 1] - x[j]); };
+    const int mid = m / 2;
+    double tau[2 * CS_BAND + 1];
+    for (int d = 0; d < B; ++d) tau[d] = band[(size_t)d * ms + mid] / g(mid + d - CS_BAND);
+    for (int i = CS_BAND; i < m - CS_BAND; ++i) {
+        double big = 0.0, err = 0.0;
+        for (int d = 0; d < B; ++d) {
+            const double b = band[(size_t)d * ms + i];
+            big = std::max(big, std::fabs(b));
+            err = std::max(err, std::fabs(b - tau[d] * g(i + d - CS_BAND)));
+        }
+        if (!(err <= 2e-7 * big)) return f;
+    }
+    for (int r = 0; r < 2 * CS_BAND; ++r) {
+        const int i = r < CS_BAND ? r : m - 2 * CS_BAND + r;
+        for (int d = 0; d < B; ++d) {
+            const int j = i + d - CS_BAND;
+            if (j >= 0 && j < m) edge[(size_t)r * B + d] = (float)(band[(size_t)d * ms + i] / g(j));
+        }
+    }
+    for (int d = 0; d < B; ++d) f.tau[d] = (float)tau[d];
+    f.ok = 1;
+    return f;
+}
+
 template <typename T> struct V2;
 template <> struct V2<double> { typedef double2 t; };
 template <> struct V2<float> { typedef float2 t; };
@@ -1004,7 +1048,8 @@ __host__ __device__ inline FusedLayout fused_layout(int nk, int M, int G)
 template <int RADIX, bool SWZ, int G>
 __global__ void __launch_bounds__(FUSED_THREADS, 2)
     fftlog_tables_fused_kernel(GridPar g, const double *__restrict__ pk,
-                               const float *__restrict__ band_t, const float *__restrict__ fac32,
+                               const float *__restrict__ band_t, BandFac bfac,
+                               const float *__restrict__ fac32,
                                const int *__restrict__ idx, const float2 *__restrict__ tdf,
                                const float4 *__restrict__ sf32, const float2 *__restrict__ qfac_df,
                                const float2 *__restrict__ modew_df,
@@ -1040,40 +1085,68 @@ __global__ void __launch_bounds__(FUSED_THREADS, 2)
         float v = 0.f;
         if (j >= 0 && j < m) {
             const float ya = ydf[j].x, yb = ydf[j + 1].x, yc = ydf[j + 2].x;
-            v = 3.f * ((yc - yb) * __ldg(gi + j + 1) - (yb - ya) * __ldg(gi + j));
+            const float gj = __ldg(gi + j);
+            v = 3.f * ((yc - yb) * __ldg(gi + j + 1) - (yb - ya) * gj);
+            if (bfac.ok) v *= gj; // the factorised band: g_j rhs_j
         }
         rhs[t] = v;
     }
     __syncthreads();
     // spline coefficients: the band of the inverse spline matrix times the
-    // right-hand sides (cspline_band_kernel's product), 8 consecutive rows per
-    // thread: their 32 right-hand sides in registers, the band rows as aligned
-    // float4 pairs (the band's row stride is a multiple of 8, zero-padded; the
-    // right-hand-side window of the last rows reads past m + 2 CS_BAND into the
-    // transform buffer, for rows past m, whose results are not kept)
+    // right-hand sides (cspline_band_kernel's product), BR consecutive rows per
+    // thread with their right-hand sides in registers: on a geometric grid
+    // (bfac.ok) the 2 CS_BAND + 1 constants of the factorised band and, for the
+    // 2 CS_BAND end rows, their own coefficients; otherwise the band rows as
+    // aligned float4 (row stride a multiple of 8, zero-padded).  The window of
+    // the last rows reads past m + 2 CS_BAND into the transform buffer, for
+    // rows past m, whose results are not kept.
     {
+        constexpr int BR = 4, BW = BR + 2 * CS_BAND; // rows per thread, window
         const int ms = cs_band_stride(m);
-        for (int i0 = 8 * tid; i0 < m; i0 += 8 * bd) {
-            float win[8 + 2 * CS_BAND + 4];
+        const float *edge = band_t + (size_t)(2 * CS_BAND + 1) * ms;
+        for (int i0 = BR * tid; i0 < m; i0 += BR * bd) {
+            float win[BW];
 #pragma unroll
-            for (int k = 0; k < (8 + 2 * CS_BAND + 4) / 4; ++k) {
+            for (int k = 0; k < BW / 4; ++k) {
                 const float4 v = reinterpret_cast<const float4 *>(rhs + i0)[k];
                 win[4 * k] = v.x;
                 win[4 * k + 1] = v.y;
                 win[4 * k + 2] = v.z;
                 win[4 * k + 3] = v.w;
             }
-            float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            float acc[BR];
 #pragma unroll
-            for (int d = 0; d <= 2 * CS_BAND; ++d) {
-                const float4 *bp = reinterpret_cast<const float4 *>(band_t + (size_t)d * ms + i0);
-                const float4 b0 = __ldg(bp), b1 = __ldg(bp + 1);
-                const float bw[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+            for (int j = 0; j < BR; ++j) acc[j] = 0.f;
+            if (!bfac.ok) {
 #pragma unroll
-                for (int j = 0; j < 8; ++j) acc[j] = fmaf(bw[j], win[j + d], acc[j]);
+                for (int d = 0; d <= 2 * CS_BAND; ++d) {
+                    const float4 b0 =
+                        __ldg(reinterpret_cast<const float4 *>(band_t + (size_t)d * ms + i0));
+                    const float bw[4] = {b0.x, b0.y, b0.z, b0.w};
+#pragma unroll
+                    for (int j = 0; j < BR; ++j) acc[j] = fmaf(bw[j], win[j + d], acc[j]);
+                }
+            } else if (i0 >= CS_BAND && i0 + BR <= m - CS_BAND) { // interior rows
+#pragma unroll
+                for (int d = 0; d <= 2 * CS_BAND; ++d)
+#pragma unroll
+                    for (int j = 0; j < BR; ++j) acc[j] = fmaf(bfac.tau[d], win[j + d], acc[j]);
+            } else { // rows near the ends: their own coefficients
+#pragma unroll
+                for (int j = 0; j < BR; ++j) {
+                    const int i = i0 + j;
+                    // (rows past m, not kept, take the constants: no loads past the end rows)
+                    const bool end = i < m && (i < CS_BAND || i >= m - CS_BAND);
+                    const float *e =
+                        edge + (size_t)(!end ? 0 : i < CS_BAND ? i : i - m + 2 * CS_BAND) *
+                                   (2 * CS_BAND + 1);
+#pragma unroll
+                    for (int d = 0; d <= 2 * CS_BAND; ++d)
+                        acc[j] = fmaf(end ? __ldg(e + d) : bfac.tau[d], win[j + d], acc[j]);
+                }
             }
 #pragma unroll
-            for (int j = 0; j < 8; ++j)
+            for (int j = 0; j < BR; ++j)
                 if (i0 + j < m) cs[i0 + j + 1] = acc[j];
         }
     }
@@ -1682,6 +1755,15 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
         // no synchronisation for their sake
         csfac_host(k, (int)nk, ctx->grid_fac_host, ctx->grid_fac32_host);
         cspline_band_host(std::vector<double>(k, k + nk), ctx->grid_band_host);
+        {
+            std::vector<float> edge;
+            const BandFac bfac =
+                cspline_band_factor(std::vector<double>(k, k + nk), ctx->grid_band_host, edge);
+            ctx->grid_band_ok = bfac.ok;
+            for (int d = 0; d <= 2 * CS_BAND; ++d) ctx->grid_band_tau[d] = bfac.tau[d];
+            // the end rows' coefficients follow the band rows
+            ctx->grid_band_host.insert(ctx->grid_band_host.end(), edge.begin(), edge.end());
+        }
         if ((st = cg_ensure(ctx, ctx->csband, sizeof(float) * ctx->grid_band_host.size())))
             return st;
         CG_CUDA(ctx, cudaMemcpyAsync(ctx->csfac.p, ctx->grid_fac_host.data(),
@@ -1730,6 +1812,9 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
     const FusedLayout fl = fused_layout((int)nk, M, inv_g);
     const bool fused_ok = mixed && !tables_df && nk >= (size_t)M + 1 && nk <= 8192 &&
                           N <= 8192 && fl.total <= 200 * 1024;
+    BandFac bfac;
+    bfac.ok = ctx->grid_band_ok;
+    for (int d = 0; d <= 2 * CS_BAND; ++d) bfac.tau[d] = ctx->grid_band_tau[d];
     // the fused kernel over spectra [s0, s0 + ns), P(k) of spectrum s0 at pks
     // (occ: only the kernel's resident blocks per SM, nothing launched)
     auto launch_fused = [&](const coffe_gpu_tuning_t &tu, int s0, int ns, const double *pks,
@@ -1748,7 +1833,7 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
             return COFFE_GPU_OK;                                                                  \
         }                                                                                         \
         fftlog_tables_fused_kernel<R, W, G><<<gfc, FUSED_THREADS, fl.total, ctx->stream>>>(       \
-            g, pks, (const float *)ctx->csband.p, (const float *)ctx->csfac32.p,                  \
+            g, pks, (const float *)ctx->csband.p, bfac, (const float *)ctx->csfac32.p,            \
             (const int *)ctx->samp_idx.p, (const float2 *)ctx->samp_tdf.p,                        \
             (const float4 *)ctx->samp_f32.p, (const float2 *)ctx->qfac_df.p, wdf,                 \
             (const float4 *)ctx->twid32.p, d_meta->grp, n_grp, n_terms, m32, p32, tw32, tab0,     \
