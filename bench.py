@@ -52,6 +52,21 @@ FLOP_PER_PAIR_EXTRA = 220
 # benchmark's equal tracers and even multipoles, so the kernel evaluates the 31
 # GK61 nodes with mu >= 0 (the other 30 are their mirror images)
 NODES = 31
+# FLOP of one (request, separation) of the polynomial-integrand kernel
+# (mp_poly_kernel<3,3>, counted from multipoles.cu, FMA = 2): the integrand's
+# coefficients in mu^2 662 (density 51, 1/D series and c 21, c^2 66, RSD
+# quadratics 24, R(c) 84, F1 F2 45, F1 F2 R 78, A 45, B 39, the K1 term 13, Q 32,
+# (1 + c)(1 - w) 7, g 73, g Q 84), the Kronrod and Gauss moment sums 111, the 31
+# nodes x 34 (Horner 16, QUADPACK's |f| and |f - mean| sums 18) and the per-pair
+# lookups and acceptance test 220
+FLOP_PER_PAIR_POLY = 662 + 111 + 31 * 34 + 220
+# bytes of the fused table kernel per spectrum (algorithmic): the FP64 spectrum
+# in (8 B per knot) and the float tables out (4 B x (N + 43) per term)
+TABLE_BYTES_PER_SPECTRUM = 8 * 4096 + 4 * (4096 + 43) * 3
+# its DRAM traffic per launch from the ncu capture of the full batch
+# (dram__bytes_read.sum + dram__bytes_write.sum: the spectra are read, the
+# tables stay in L2 during the kernel)
+TABLE_DRAM_BYTES_PER_LAUNCH = 17.163e6 + 512
 # the FP64 instantiation of the same kernel (COFFE_GPU_FP64_FASTALG) has no
 # Kahan compensation: 3 fewer operations per multipole and node
 FLOP_PER_NODE_FP64_FASTALG = FLOP_PER_NODE - 9
@@ -69,10 +84,6 @@ FWD_FLOP = FFT_FLOP + 10 * N_FFT + 5 * N_FFT
 # float on the mixed path, double on the FP64 path) and writes the table
 # (float / double)
 INV_BYTES = {"mixed": 8 * (N_FFT // 2 + 1) + 4 * N_FFT, "fp64": 16 * (N_FFT // 2 + 1) + 8 * N_FFT}
-# DRAM bytes (read + write) per (request, separation) of the mixed multipole
-# kernel, from an ncu capture of the first 256 spectra of this batch (324,864
-# pairs, 5.90 MB read, 0 B written); traffic grows with the number of pairs
-DRAM_BYTES_PER_PAIR = 5.897728e6 / 324864
 
 
 def parse():
@@ -266,6 +277,20 @@ def kernel_rooflines(kt, n_spectra, n_terms, n_pairs, peaks):
                      "work_per_launch": work, "note": note})
 
     inv = n_spectra * n_terms
+    add("mixed", "fftlog_tables_fused_kernel", "fftlog_tables_fused_kernel (table stage)", "hbm",
+        n_spectra * TABLE_BYTES_PER_SPECTRUM, "GB/s", hbm,
+        "bytes: FP64 spectra in, float tables out; latency-bound (2 blocks per SM, long "
+        "scoreboard on the per-grid tables), far from HBM")
+    add("mixed", "fftlog_tables_fused_kernel", "fftlog_tables_fused_kernel (table stage)",
+        "fp32", n_spectra * (FWD_FLOP + n_terms * INV_FLOP), "TFLOP/s", peaks["fp32"],
+        "FP64-equivalent FLOP of the forward and inverse transforms against the FP32 peak "
+        "(the forward is double-float, ~10-20 FP32 operations per FP64 one)")
+    add("mixed", "mp_poly_kernel", "mp_poly_kernel<3,3,U,float>", "fp32",
+        n_pairs * FLOP_PER_PAIR_POLY, "TFLOP/s", peaks["fp32"],
+        "its own FLOP per launch / event time; peak = measured fma.rn.f32 rate")
+    add("fp64-fastalg", "mp_poly_kernel", "mp_poly_kernel<3,3,U,double> (FP64, mixed algorithm)",
+        "fp64", n_pairs * FLOP_PER_PAIR_POLY, "TFLOP/s", peaks["fp64"],
+        "the mixed kernel's algorithm in FP64")
     add("mixed", "mp_fast_kernel", "mp_fast_kernel<3,3,U,float>", "fp32",
         n_pairs * (NODES * FLOP_PER_NODE + FLOP_PER_PAIR_EXTRA), "TFLOP/s", peaks["fp32"],
         "FLOP per launch / event time; peak = measured fma.rn.f32 rate")
@@ -869,7 +894,9 @@ def ours(args, rank, world, local_rank):
     e_ev.record(stream)
     e_ev.synchronize()
     kern_s = s_ev.elapsed_time(e_ev) * 1e-3 / nk_rep
-    flop_launch = n_sep * (NODES * FLOP_PER_NODE + FLOP_PER_PAIR_EXTRA)
+    poly = bool(ctx.tuning().get("lane_poly"))
+    flop_launch = n_sep * (FLOP_PER_PAIR_POLY if poly else
+                           NODES * FLOP_PER_NODE + FLOP_PER_PAIR_EXTRA)
 
     # end to end through the public API with pinned host buffers
     e2e = None
@@ -939,6 +966,23 @@ def ours(args, rank, world, local_rank):
         extra = extras(torch, ctx, stream)
         extra["gradient_cfg3"] = gradient_batch(torch, ctx, stream, batch, pk_d, rs_d, rz_d,
                                                 ro_d, sep_d, n_sep)
+    # the dominant kernel of the step: the table stage (the fused kernel when the
+    # tuner picks it), against HBM with its algorithmic bytes
+    hbm = peaks.get("hbm_gbs") or 6755.5
+    t_ms = kt.get("mixed", {}).get("fftlog_tables_fused_kernel")
+    table_roofline = None
+    if t_ms:
+        tb = args.n_spectra * TABLE_BYTES_PER_SPECTRUM
+        table_roofline = {
+            "kernel": "fftlog_tables_fused_kernel (spline band, double-float forward and FP32 "
+                      "inverse transforms of one spectrum per block)",
+            "bound": "hbm", "achieved": tb / (t_ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+            "frac": tb / (t_ms * 1e-3) / 1e9 / hbm, "launch_ms": t_ms,
+            "bytes_per_launch": tb,
+            "traffic": TABLE_DRAM_BYTES_PER_LAUNCH * args.n_spectra / 512,
+            "traffic_unit": "bytes per launch (ncu dram read+write of the 512-spectrum batch)",
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)",
+            "note": "latency-bound: 2 blocks per SM, long-scoreboard stalls on per-grid tables"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_mixed / args.steps,
@@ -960,8 +1004,9 @@ def ours(args, rank, world, local_rank):
         "fp64_fastalg": {"value": fast64_value, "unit": UNIT, "steps": k64,
                          "ms_per_step": 1e3 * dev_fast64 / k64,
                          "algorithm": "the mixed path's algorithm in FP64 (FP64 tables and "
-                                      "transforms; per-request background polynomials, "
-                                      "regrouped integrand)",
+                                      "transforms; per-request background polynomials, the "
+                                      "integrand as a polynomial in mu^2 when the tuner "
+                                      "picks it for both)",
                          "max_rel_err_vs_fp64": err_fast64},
         "mixed_over_fp64": value / fast64_value,
         "mixed_over_fp64_note": "matched algorithms: the mixed step against the same "
@@ -977,17 +1022,16 @@ def ours(args, rank, world, local_rank):
                            "source": "FMA-chain kernels of coffe_gpu_measure_peak and cuBLAS "
                                      "SGEMM 8192^3 (TF32 off) in this run; HBM from "
                                      "MEASURED_PEAKS.json"},
-        "roofline": {"kernel": "mp_fast_kernel<3, 3> (mixed multipole quadrature, unit biases)",
-                     "bound": "fp32", "achieved": achieved,
-                     "peak": peak32, "unit": "TFLOP/s", "frac": achieved / peak32,
-                     "peak_source": "measured fma.rn.f32 rate of this GPU in this run "
-                                    "(coffe_gpu_measure_peak); the kernel is FP32-issue bound, "
-                                    "neither HBM nor tensor",
-                     "flop_per_launch": flop_launch, "launch_ms": kern_s * 1e3,
-                     "traffic": n_sep * DRAM_BYTES_PER_PAIR,
-                     "traffic_unit": "bytes per launch (ncu dram read+write of a 256-spectrum "
-                                     "capture, scaled by pairs)",
-                     "hbm_peak_gbs": peaks.get("hbm_gbs")},
+        "roofline": table_roofline,
+        "roofline_multipoles": {
+            "kernel": ("mp_poly_kernel<3, 3>" if poly else "mp_fast_kernel<3, 3>") +
+                      " (mixed multipole quadrature, unit biases; the multipole call: "
+                      "background fit included)",
+            "bound": "fp32", "achieved": achieved,
+            "peak": peak32, "unit": "TFLOP/s", "frac": achieved / peak32,
+            "peak_source": "measured fma.rn.f32 rate of this GPU in this run "
+                           "(coffe_gpu_measure_peak); FP32-issue bound, neither HBM nor tensor",
+            "flop_per_launch": flop_launch, "launch_ms": kern_s * 1e3},
         "rooflines": kernel_rooflines(kt, args.n_spectra, len(TERMS), n_sep,
                                       {"fp32": peak32, "fp64": peak64,
                                        "hbm_gbs": peaks.get("hbm_gbs") or 6755.5}),
