@@ -1025,8 +1025,10 @@ __global__ void fftlog_inverse_f32_kernel(GridPar g, const float2 *__restrict__ 
 //
 // Shared memory (bytes; nk >= N/2 + 1 is required):
 //   phase 1: knots (hi, lo) [0, 8 nk) | spline c [FUS_C, +4 nk) |
-//            forward buffer [FUS_F, +16 M) (the spline right-hand sides
-//            live there before the sampling)
+//            forward buffer [FUS_F, +max(16 M, 4 (nk + 2 CS_BAND + 8))) (the
+//            spline right-hand sides, nk + 2 CS_BAND - 2 floats, live there
+//            before the sampling, and the band product's window reads up to
+//            3 floats past them)
 //   phase 2: half spectrum [0, 8 (M + 1)) | inverse buffers [FUS_I, +8 G M)
 struct FusedLayout {
     size_t c, f, i, total;
@@ -1038,7 +1040,9 @@ __host__ __device__ inline FusedLayout fused_layout(int nk, int M, int G)
     l.c = up(sizeof(float2) * (size_t)nk);
     l.f = up(l.c + sizeof(float) * (size_t)nk);
     l.i = up(sizeof(float2) * (size_t)(M + 1));
-    const size_t t1 = l.f + sizeof(float4) * (size_t)M;
+    const size_t fwd = sizeof(float4) * (size_t)M;
+    const size_t rhs = sizeof(float) * ((size_t)nk + 2 * CS_BAND + 8);
+    const size_t t1 = l.f + (fwd > rhs ? fwd : rhs);
     const size_t t2 = l.i + sizeof(float2) * (size_t)M * G;
     l.total = t1 > t2 ? t1 : t2;
     return l;
@@ -1098,8 +1102,9 @@ __global__ void __launch_bounds__(FUSED_THREADS, 2)
     // (bfac.ok) the 2 CS_BAND + 1 constants of the factorised band and, for the
     // 2 CS_BAND end rows, their own coefficients; otherwise the band rows as
     // aligned float4 (row stride a multiple of 8, zero-padded).  The window of
-    // the last rows reads past m + 2 CS_BAND into the transform buffer, for
-    // rows past m, whose results are not kept.
+    // the last rows reads up to 3 floats past the m + 2 CS_BAND right-hand
+    // sides (inside the region fused_layout reserves), for rows past m, whose
+    // results are not kept.
     {
         constexpr int BR = 4, BW = BR + 2 * CS_BAND; // rows per thread, window
         const int ms = cs_band_stride(m);

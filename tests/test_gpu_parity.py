@@ -99,17 +99,19 @@ def test_integral_tables_fp64_match_oracle(gpu_ctx, oracle, cfg1):
         assert e_small < 1e-9, ((n, l), e_small)
 
 
+@pytest.mark.parametrize("N", [4096, 2048, 8192])
 @pytest.mark.parametrize("tables_df", [False, True])
-def test_integral_tables_mixed_close_to_oracle(gpu_ctx, oracle, cfg1, tables_df):
+def test_integral_tables_mixed_close_to_oracle(gpu_ctx, oracle, cfg1, tables_df, N):
     """Mixed-precision tables of I_0^0, I_2^0, I_4^0 over the multipoles' range.
     FP32 inverse transforms (default): 1e-5 relative with a floor of 1e-3 of the
     range's largest |I| (their rounding is ~1e-7 of the outputs' scale, so the
     error stays near that fraction of the scale, also at zero crossings).
     Double-float inverse transforms: 1e-5 relative with a floor of 1e-6 of the
     local envelope (the float spline-curvature correction of the resampled
-    P(k) adds ~1e-6 near zero crossings)."""
+    P(k) adds ~1e-6 near zero crossings).  N = 2048 and 8192 run the forward
+    transform's two packed N/4-point halves with a radix-2 first stage (odd
+    log2(N/4)), N = 4096 without."""
     k, pk = cfg1["k"], cfg1["pk"]
-    N = 4096
     gpu_ctx.integrals_init(k, pk[None, :], [(0, 0), (0, 2), (0, 4)], N=N, precision="mixed",
                            small_r=False, tables_df=tables_df)
     for n, l in [(0, 0), (0, 2), (0, 4)]:
