@@ -128,6 +128,45 @@ def test_integral_tables_mixed_close_to_oracle(gpu_ctx, oracle, cfg1, tables_df,
         assert e < 1e-5, ((n, l), e)
 
 
+@pytest.mark.parametrize("fused", [1, 0])
+def test_integral_tables_mixed_irregular_grid(oracle, cfg1, fused):
+    """A k grid that is not geometric (log-spacing varying by +-15% along the
+    grid): the natural spline's band is applied as full rows instead of the
+    factorised form, in the fused table kernel (fused = 1) and in
+    cspline_band_kernel (fused = 0).  Tables of I_0^0, I_2^0, I_4^0 against the
+    oracle on the same grid, with the tolerance of the geometric case."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from coffe_gb300.api import Context
+
+    k0, pk0 = cfg1["k"], cfg1["pk"]
+    u = np.linspace(0.0, 1.0, len(k0))
+    lk = np.log(k0[0]) + np.log(k0[-1] / k0[0]) * (u + 0.15 * np.sin(10 * np.pi * u) / (10 * np.pi))
+    k = np.exp(lk)
+    k[0], k[-1] = k0[0], k0[-1]
+    pk = np.exp(np.interp(lk, np.log(k0), np.log(pk0)))
+    dl = np.diff(np.log(k))
+    assert np.all(dl > 0) and dl.max() / dl.min() > 1.3
+    N = 4096
+    ctx = Context(0)
+    try:
+        ctx.set_tuning(fft_fused=fused)
+        ctx.integrals_init(k, pk[None, :], [(0, 0), (0, 2), (0, 4)], N=N, precision="mixed",
+                           small_r=False)
+        assert ctx.tuning()["fft_fused"] == fused
+        for n, l in [(0, 0), (0, 2), (0, 4)]:
+            gx, gy = ctx.integral_table(0, n, l)
+            ox, oy = oracle.integral_table(k, pk, n, l, N, with_small_r=False)
+            mask = (ox >= 5 / H) & (ox <= 300 / H)
+            mask[:43] = False
+            e = rel_floor(gy[mask], oy[mask], 1e-3 * np.abs(oy[mask]).max())
+            print("irregular grid, fused", fused, (n, l), e)
+            assert e < 1e-5, ((n, l), e)
+    finally:
+        ctx.close()
+
+
 def test_all_bessel_integrals_2e14_fp64(gpu_ctx, oracle, w):
     """l = 0..4, n = -1..4 on 2^14 points, including the pairs whose Gamma-ratio
     reflection overflows at high frequency (kept as the reference computes them)."""
