@@ -147,6 +147,10 @@ int cg_check_device_errors(coffe_gpu_ctx *ctx, const char *where)
     if (!bits) return COFFE_GPU_OK;
     CG_CUDA(ctx, cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
     *ctx->h_err = 0;
+    if (bits & CG_ERR_WAIT) {
+        cg_set_error(ctx, "%s: an asynchronous copy into shared memory did not complete", where);
+        return COFFE_GPU_ECUDA;
+    }
     if (bits & CG_ERR_BADSEP) { // before NONFINITE: such separations give NaN
         cg_set_error(ctx, "%s: separations must be positive", where);
         return COFFE_GPU_EINVAL;

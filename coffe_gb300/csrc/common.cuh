@@ -20,7 +20,8 @@ enum cg_err_bits {
     CG_ERR_NONFINITE = 1,
     CG_ERR_QAG_LIMIT = 2,
     CG_ERR_BOUNDS = 4,
-    CG_ERR_BADSEP = 16 // a separation of a host-array call is not > 0
+    CG_ERR_BADSEP = 16, // a separation of a host-array call is not > 0
+    CG_ERR_WAIT = 32    // a bounded wait for an asynchronous copy gave up
 };
 
 __device__ __forceinline__ void cg_flag(int *err, int bit)

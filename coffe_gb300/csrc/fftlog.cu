@@ -18,6 +18,7 @@
 #include <cstring>
 #include <vector>
 
+#include "bulk.cuh"
 #include "cplx.cuh"
 #include "ctx.cuh"
 #include "dfloat.cuh"
@@ -1052,6 +1053,7 @@ __host__ __device__ inline FusedLayout fused_layout(int nk, int M, int G)
 template <int RADIX, bool SWZ, int G>
 __global__ void __launch_bounds__(FUSED_THREADS, 2)
     fftlog_tables_fused_kernel(GridPar g, const double *__restrict__ pk,
+                               const double *__restrict__ pk_end,
                                const float *__restrict__ band_t, BandFac bfac,
                                const float *__restrict__ fac32,
                                const int *__restrict__ idx, const float2 *__restrict__ tdf,
@@ -1074,11 +1076,38 @@ __global__ void __launch_bounds__(FUSED_THREADS, 2)
     float2 *fbuf2 = reinterpret_cast<float2 *>(smem_raw + L.f);
     float *rhs = reinterpret_cast<float *>(smem_raw + L.f);
     const int tid = threadIdx.x, bd = blockDim.x;
-    // knots as (hi, lo) pairs, split with integer operations
+    // knots as (hi, lo) pairs, split with integer operations.  The spectrum's
+    // FP64 row comes into shared memory by one bulk asynchronous copy (into the
+    // spline-coefficient and transform region, free until the band product;
+    // from the 16-byte boundary at or below the row to the one at or above its
+    // end), instead of nk / blockDim dependent rounds of loads from memory.
+    // A row whose rounded end would pass the end of the P(k) array (the last
+    // one, when that end is not 16-byte aligned) is read with plain loads.
     const double *p = pk + (size_t)s * nk;
-    for (int i = tid; i < nk; i += bd) {
-        const dfl d = df_from_double_bits(p[i]);
-        ydf[i] = make_float2(d.hi, d.lo);
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p), a0 = a & ~(uintptr_t)15;
+    const unsigned bytes = (unsigned)(((a - a0) + sizeof(double) * (size_t)nk + 15) & ~(size_t)15);
+    if (a0 + bytes <= reinterpret_cast<uintptr_t>(pk_end)) {
+        __shared__ __align__(8) unsigned long long kbar;
+        double *stage = reinterpret_cast<double *>(smem_raw + L.c);
+        if (tid == 0) bulk_begin(&kbar, stage, reinterpret_cast<const void *>(a0), bytes);
+        __syncthreads(); // the barrier is initialised before it is waited on
+        bool ok = bulk_wait(&kbar);
+        if (__syncthreads_or(!ok)) { // given up: wait once more for the copy, then leave
+            if (!ok) ok = bulk_wait(&kbar);
+            if (tid == 0) cg_flag(err, CG_ERR_WAIT);
+            __syncthreads();
+            return;
+        }
+        const double *row = stage + (a - a0) / sizeof(double);
+        for (int i = tid; i < nk; i += bd) {
+            const dfl d = df_from_double_bits(row[i]);
+            ydf[i] = make_float2(d.hi, d.lo);
+        }
+    } else {
+        for (int i = tid; i < nk; i += bd) {
+            const dfl d = df_from_double_bits(p[i]);
+            ydf[i] = make_float2(d.hi, d.lo);
+        }
     }
     __syncthreads();
     // natural-spline right-hand sides (float, from the high parts), padded by
@@ -1838,7 +1867,8 @@ int integrals_build(coffe_gpu_ctx *ctx, const double *k, const double *pk, int n
             return COFFE_GPU_OK;                                                                  \
         }                                                                                         \
         fftlog_tables_fused_kernel<R, W, G><<<gfc, FUSED_THREADS, fl.total, ctx->stream>>>(       \
-            g, pks, (const float *)ctx->csband.p, bfac, (const float *)ctx->csfac32.p,            \
+            g, pks, d_pk + nk * (size_t)n_spectra, (const float *)ctx->csband.p, bfac,            \
+            (const float *)ctx->csfac32.p,                                                        \
             (const int *)ctx->samp_idx.p, (const float2 *)ctx->samp_tdf.p,                        \
             (const float4 *)ctx->samp_f32.p, (const float2 *)ctx->qfac_df.p, wdf,                 \
             (const float4 *)ctx->twid32.p, d_meta->grp, n_grp, n_terms, m32, p32, tw32, tab0,     \
