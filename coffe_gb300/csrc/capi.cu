@@ -270,7 +270,7 @@ int coffe_gpu_ctx_destroy(coffe_gpu_ctx_t *ctx)
                       &ctx->kgrid,    &ctx->csc,    &ctx->csfac,   &ctx->samp_idx, &ctx->samp_dx,
                       &ctx->qfac,     &ctx->modec,  &ctx->postf,   &ctx->twid,   &ctx->twid32,
                       &ctx->spec,     &ctx->req_buf, &ctx->term_meta, &ctx->zrec64,
-                      &ctx->zrec32,   &ctx->mp_retry, &ctx->term_df,
+                      &ctx->zrec32,   &ctx->mp_retry, &ctx->term_df, &ctx->chi_tab64, &ctx->chi_tab32,
                       &ctx->samp_f32, &ctx->csfac32,
                       &ctx->lens_rule, &ctx->lens_rec, &ctx->lens_part,
                       &ctx->cov_buf,  &ctx->cov_out, &ctx->adj_buf, &ctx->csband,

@@ -63,6 +63,10 @@ struct coffe_gpu_ctx {
     bool z_uniform = false;
     double z0 = 0, zn = 0, dz = 0;
     DevBuf zrec64, zrec32;
+    // (D1, f D1) at CG_CHI_TAB uniform chi over the background's range, FP64
+    // and float, for the per-request background fits (linear interpolation)
+    DevBuf chi_tab64, chi_tab32;
+    double chi_t0 = 0, chi_tn = 0;
     DevBuf cf_rule; // mu list + line rules of the last coffe_gpu_corrfunc call with lensing
     DevBuf avg_buf; // expanded requests of coffe_gpu_average_multipoles
     SplineBuf bias[4];

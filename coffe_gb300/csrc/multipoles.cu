@@ -881,6 +881,36 @@ __device__ __forceinline__ double4_32a mk4(double a, double b, double c, double 
     return v;
 }
 
+// (D1, f D1) as functions of chi on a uniform grid of CG_CHI_TAB points over
+// the background's chi range (multipoles_prepare_background evaluates the FP64
+// splines there), read by linear interpolation: two independent loads where
+// the splines need a chain of three lookups (z of chi, then D1 and f of z).
+// Interpolation error ~ h^2 / 8 of the second derivative: ~5e-9 relative for
+// the growth factor's Gpc scale at h = range / 16383.
+#define CG_CHI_TAB 16384
+template <typename T> struct V2T;
+template <> struct V2T<double> { typedef double2 t; };
+template <> struct V2T<float> { typedef float2 t; };
+template <typename T> struct ChiTab {
+    const typename V2T<T>::t *rec;
+    T c0, cn, inv_dc;
+};
+template <typename T>
+__device__ __forceinline__ void chi_tab_eval(const ChiTab<T> &tb, T chi, T &g, T &fg)
+{
+    if (!(chi >= tb.c0 && chi <= tb.cn)) {
+        g = fg = cg_nan<T>();
+        return;
+    }
+    const T u = (chi - tb.c0) * tb.inv_dc;
+    int i = (int)u;
+    i = i > CG_CHI_TAB - 2 ? CG_CHI_TAB - 2 : i;
+    const T w = u - (T)i;
+    const typename V2T<T>::t p = tb.rec[i], q = tb.rec[i + 1];
+    g = fma(w, q.x - p.x, p.x);
+    fg = fma(w, q.y - p.y, p.y);
+}
+
 // the Chebyshev points t_j = cos((2j + 1) pi / 12), j < 6, and the inverse of
 // their Vandermonde matrix (monomial coefficients from the six values), both
 // computed on the host in FP64
@@ -896,7 +926,7 @@ template <typename T> struct FitInvT {
 #define MP_FIT_WARPS 4
 template <typename T, typename S>
 __global__ void __launch_bounds__(32 * MP_FIT_WARPS)
-    mp_bgfit_kernel(S chi_of_z, S z_of_chi, S D1, S f, int n_req, FitInvT<T> vinv,
+    mp_bgfit_kernel(S chi_of_z, ChiTab<T> tab, int n_req, FitInvT<T> vinv,
                     const double *__restrict__ req_z_mean, const int64_t *__restrict__ req_offset,
                     const double *__restrict__ sep, BgFitT<T> *__restrict__ fit)
 {
@@ -905,18 +935,34 @@ __global__ void __launch_bounds__(32 * MP_FIT_WARPS)
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int q = blockIdx.x * MP_FIT_WARPS + w;
     if (q >= n_req) return; // whole warps leave together
-    T rmax = T(0);
-    for (long long i = req_offset[q] + lane; i < req_offset[q + 1]; i += 32)
-        rmax = fmax(rmax, from_f64<T>(sep[i]));
-    for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    // a chain of dependent loads per warp: the separations are read eight per
+    // lane at a time (one round for requests of up to 256), chi(z_mean) while
+    // the first round is in flight, then (D1, f D1) at the six nodes from the
+    // uniform chi table
+    constexpr int U = 8;
+    const long long o1 = req_offset[q + 1];
+    long long i0 = req_offset[q] + lane;
+    double sv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) sv[u] = i0 + 32 * u < o1 ? sep[i0 + 32 * u] : 0.0;
     const T chim = spl_eval(chi_of_z, from_f64<T>(req_z_mean[q]));
-    T X = fmin(T(0.5) * rmax, fmin(chim - z_of_chi.x0, z_of_chi.xn - chim));
+    T rmax = T(0);
+    for (;;) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) rmax = fmax(rmax, from_f64<T>(sv[u]));
+        i0 += 32 * U;
+        if (i0 >= o1) break;
+#pragma unroll
+        for (int u = 0; u < U; ++u) sv[u] = i0 + 32 * u < o1 ? sep[i0 + 32 * u] : 0.0;
+    }
+    for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    T X = fmin(T(0.5) * rmax, fmin(chim - tab.c0, tab.cn - chim));
     if (!(X > T(1e-3))) X = T(1e-3); // empty request or no room: its pairs are outside anyway
     if (lane < 6) {
-        const T z = spl_eval(z_of_chi, fma(X, vinv.t[lane], chim));
-        const T g = spl_eval(D1, z);
+        T g, fg;
+        chi_tab_eval(tab, fma(X, vinv.t[lane], chim), g, fg);
         val[w][lane] = g;
-        val[w][6 + lane] = spl_eval(f, z) * g;
+        val[w][6 + lane] = fg;
     }
     __syncwarp();
     if (lane < 12) {
@@ -1789,9 +1835,15 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S
     // the requests run there), so that they overlap earlier work on the stream
     {
         cudaStream_t fs = ctx->prep_stream ? ctx->prep_stream : ctx->stream;
+        ChiTab<T> tab;
+        tab.rec = (const typename V2T<T>::t *)(sizeof(T) == sizeof(double) ? ctx->chi_tab64.p
+                                                                         : ctx->chi_tab32.p);
+        tab.c0 = (T)ctx->chi_t0;
+        tab.cn = (T)ctx->chi_tn;
+        tab.inv_dc = (T)((CG_CHI_TAB - 1) / (ctx->chi_tn - ctx->chi_t0));
         mp_bgfit_kernel<T, S><<<(a.n_req + MP_FIT_WARPS - 1) / MP_FIT_WARPS, 32 * MP_FIT_WARPS, 0,
-                                fs>>>(chi_of_z, bg.z_of_chi, bg.D1, bg.f, a.n_req, vinv,
-                                      req_z_mean, req_offset, sep, d_fit);
+                                fs>>>(chi_of_z, tab, a.n_req, vinv, req_z_mean, req_offset, sep,
+                                      d_fit);
         if ((st = cg_after_launch(ctx, "mp_bgfit_kernel"))) return st;
         if (ctx->prep_stream) {
             CG_CUDA(ctx, cudaEventRecord(ctx->copy_ev[1], fs));
@@ -1951,6 +2003,19 @@ int launch(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S &chi
     return cg_after_launch(ctx, "mp_retry_kernel");
 }
 
+// (D1, f D1) at chi_j = c0 + j (cn - c0) / (CG_CHI_TAB - 1) from the FP64 splines
+__global__ void chi_tab_kernel(Spl64 z_of_chi, Spl64 D1, Spl64 f, double c0, double cn,
+                               double2 *__restrict__ t64, float2 *__restrict__ t32)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= CG_CHI_TAB) return;
+    const double chi = j == CG_CHI_TAB - 1 ? cn : c0 + (cn - c0) * ((double)j / (CG_CHI_TAB - 1));
+    const double z = spl_eval(z_of_chi, chi);
+    const double g = spl_eval(D1, z), fg = spl_eval(f, z) * g;
+    t64[j] = make_double2(g, fg);
+    t32[j] = make_float2((float)g, (float)fg);
+}
+
 __global__ void zrec_kernel(const double4_32a *__restrict__ f64, const double4_32a *__restrict__ d64,
                             const float4 *__restrict__ f32, const float4 *__restrict__ d32, int n,
                             ZRec<double> *__restrict__ r64, ZRec<float> *__restrict__ r32)
@@ -1971,6 +2036,17 @@ int multipoles_prepare_background(coffe_gpu_ctx *ctx)
 {
     const int n = ctx->bg_bins;
     ctx->z_uniform = false;
+    {
+        const Spl64 zc = ctx->bg[BG_Z_OF_CHI].v64();
+        int st = cg_ensure(ctx, ctx->chi_tab64, sizeof(double2) * CG_CHI_TAB);
+        if (st || (st = cg_ensure(ctx, ctx->chi_tab32, sizeof(float2) * CG_CHI_TAB))) return st;
+        chi_tab_kernel<<<(CG_CHI_TAB + 255) / 256, 256, 0, ctx->stream>>>(
+            zc, ctx->bg[BG_D1].v64(), ctx->bg[BG_F].v64(), zc.x0, zc.xn,
+            (double2 *)ctx->chi_tab64.p, (float2 *)ctx->chi_tab32.p);
+        if ((st = cg_after_launch(ctx, "chi_tab_kernel"))) return st;
+        ctx->chi_t0 = zc.x0;
+        ctx->chi_tn = zc.xn;
+    }
     std::vector<double> z(n);
     CG_CUDA(ctx, cudaMemcpyAsync(z.data(), ctx->bg_nodes.p, sizeof(double) * n,
                                  cudaMemcpyDeviceToHost, ctx->stream));
