@@ -22,6 +22,7 @@
 #include "cplx.cuh"
 #include "ctx.cuh"
 #include "dfloat.cuh"
+#include "f32x2.cuh"
 #include "dual6.cuh"
 #include "fft.cuh"
 #include "qag.cuh"
@@ -854,6 +855,17 @@ __device__ __forceinline__ float2 c32_mul(float2 a, float2 b)
 }
 __device__ __forceinline__ float2 c32_conj(float2 a) { return make_float2(a.x, -a.y); }
 
+// (re, im) of a complex float as one packed f32x2 value: the butterflies'
+// complex additions as one add/sub.rn.f32x2 each (the same per-lane rounding as
+// two scalar ones, so the same results)
+__device__ __forceinline__ f2 c32_pk(float2 a) { return f2_pack(a.x, a.y); }
+__device__ __forceinline__ float2 c32_unpk(f2 a)
+{
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(a.v));
+    return r;
+}
+
 // Shared-memory layout of the FP32 transforms (8-byte elements, 16 per
 // 128-byte bank row): element i at i ^ f(i >> 4), f(x) = (x ^ 8x ^ (x >> 4))
 // mod 16, a permutation within each row that makes the bit-reversed scatter
@@ -883,9 +895,9 @@ __device__ void smem_fft_f32(float2 *buf, int logM, int nact, const float2 *__re
             for (int j = 0; j < G; ++j) {
                 if (j >= nact) break;
                 float2 *bj = buf + j * M;
-                const float2 u = bj[p0], v = bj[p1];
-                bj[p0] = c32_add(u, v);
-                bj[p1] = c32_sub(u, v);
+                const f2 u = c32_pk(bj[p0]), v = c32_pk(bj[p1]);
+                bj[p0] = c32_unpk(f2_add(u, v));
+                bj[p1] = c32_unpk(f2_sub(u, v));
             }
         }
         __syncthreads();
@@ -922,13 +934,14 @@ __device__ void smem_fft_f32(float2 *buf, int logM, int nact, const float2 *__re
                     x2 = c32_mul(x2, w2);
                     x3 = c32_mul(x3, w3);
                 }
-                const float2 t0 = c32_add(x0, x1), t1 = c32_sub(x0, x1);
-                const float2 t2 = c32_add(x2, x3), t3 = c32_sub(x2, x3);
-                // w_{4 half}^half = -i forward, +i backward
+                const f2 X0 = c32_pk(x0), X1 = c32_pk(x1), X2 = c32_pk(x2), X3 = c32_pk(x3);
+                const f2 t0 = f2_add(X0, X1), t2 = f2_add(X2, X3);
+                const float2 t1 = c32_unpk(f2_sub(X0, X1)), t3 = c32_unpk(f2_sub(X2, X3));
+                // w_{4 half}^half = -i forward, +i backward (a lane swap: scalar)
                 const float2 r = sign < 0 ? make_float2(t3.y, -t3.x) : make_float2(-t3.y, t3.x);
-                bj[p0] = c32_add(t0, t2);
+                bj[p0] = c32_unpk(f2_add(t0, t2));
                 bj[p1] = c32_add(t1, r);
-                bj[p2] = c32_sub(t0, t2);
+                bj[p2] = c32_unpk(f2_sub(t0, t2));
                 bj[p3] = c32_sub(t1, r);
             }
         }

@@ -84,6 +84,49 @@ def test_fused_table_stage_matches_three_kernels(setup):
     assert e < 1e-7, e
 
 
+def test_fused_bulk_copy_rows_match_plain_loads():
+    """The fused kernel copies each P(k) row into shared memory with one bulk
+    asynchronous copy from the 16-byte boundary at or below the row, and reads
+    a row whose rounded end would pass the P(k) array with plain loads.  With
+    an odd k-grid length (4095 knots) and three spectra the batch has an
+    aligned row, a row 8 bytes past a boundary and a last row read with plain
+    loads; a call with one spectrum always takes the plain loads.  The tables
+    are bit for bit those of one spectrum per call, for host and device P(k)."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from coffe_gb300 import workloads
+    from coffe_gb300.api import Context
+
+    b = workloads.subset(workloads.cfg3(n_spectra=4), 4)
+    ctx = Context(0)
+    try:
+        ctx.background_init(0.31, 0.05, 9e-5, H, 10000)
+        ctx.set_tuning(**{**DEFAULT, "fft_fused": 1, "fft_swizzle": 1})
+        for k, pk in ((b.k[:-1], b.pk[:3, :-1]), (b.k, b.pk[:3])):
+            k, pk = np.ascontiguousarray(k), np.ascontiguousarray(pk)
+
+            def tables(n_spec):
+                return np.stack([ctx.integral_table(s, n, l)[1] for s in range(n_spec)
+                                 for n, l in TERMS])
+
+            ctx.integrals_init(k, pk, TERMS, N=4096, precision="mixed", small_r=False)
+            assert ctx.tuning()["fft_fused"] == 1
+            batch = tables(3)
+            assert np.isfinite(batch[:, 43:]).all()
+            one = []
+            for s in range(3):
+                ctx.integrals_init(k, pk[s:s + 1], TERMS, N=4096, precision="mixed",
+                                   small_r=False)
+                one.append(tables(1))
+            assert np.array_equal(batch, np.concatenate(one), equal_nan=True), len(k)
+            ctx.integrals_init_device(k, torch.from_numpy(pk).cuda(), TERMS, N=4096,
+                                      precision="mixed")
+            assert np.array_equal(tables(3), batch, equal_nan=True), len(k)
+    finally:
+        ctx.close()
+
+
 def test_lane_configurations_agree(setup):
     ctx, b = setup
     _tables(ctx, b, "mixed")
