@@ -22,12 +22,14 @@ __device__ __forceinline__ float f2_lo(f2 a)
 {
     float lo, hi;
     asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
+    (void)hi;
     return lo;
 }
 __device__ __forceinline__ float f2_hi(f2 a)
 {
     float lo, hi;
     asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
+    (void)lo;
     return hi;
 }
 __device__ __forceinline__ f2 f2_add(f2 a, f2 b)

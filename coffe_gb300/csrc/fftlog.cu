@@ -1078,6 +1078,11 @@ __global__ void __launch_bounds__(FUSED_THREADS, 2)
                                float *__restrict__ tab, int fill_small, int *err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    // a kernel launched after this one with programmatic stream serialization
+    // (the per-request background fit, which does not read the tables) may
+    // start once every block of this grid has started, and waits for this
+    // grid's completion itself before it exits
+    asm volatile("griddepcontrol.launch_dependents;");
     const int s = blockIdx.x, qi = blockIdx.y;
     const int N = g.N, M = N / 2, nk = g.nk, m = nk - 2;
     const int logM = 31 - __clz(M);

@@ -934,53 +934,60 @@ __global__ void __launch_bounds__(32 * MP_FIT_WARPS)
     __shared__ T cof[MP_FIT_WARPS][12];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int q = blockIdx.x * MP_FIT_WARPS + w;
-    if (q >= n_req) return; // whole warps leave together
-    // a chain of dependent loads per warp: the separations are read eight per
-    // lane at a time (one round for requests of up to 256), chi(z_mean) while
-    // the first round is in flight, then (D1, f D1) at the six nodes from the
-    // uniform chi table
-    constexpr int U = 8;
-    const long long o1 = req_offset[q + 1];
-    long long i0 = req_offset[q] + lane;
-    double sv[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) sv[u] = i0 + 32 * u < o1 ? sep[i0 + 32 * u] : 0.0;
-    const T chim = spl_eval(chi_of_z, from_f64<T>(req_z_mean[q]));
-    T rmax = T(0);
-    for (;;) {
-#pragma unroll
-        for (int u = 0; u < U; ++u) rmax = fmax(rmax, from_f64<T>(sv[u]));
-        i0 += 32 * U;
-        if (i0 >= o1) break;
+    if (q < n_req) { // whole warps
+        // a chain of dependent loads per warp: the separations are read eight per
+        // lane at a time (one round for requests of up to 256), chi(z_mean) while
+        // the first round is in flight, then (D1, f D1) at the six nodes from the
+        // uniform chi table
+        constexpr int U = 8;
+        const long long o1 = req_offset[q + 1];
+        long long i0 = req_offset[q] + lane;
+        double sv[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) sv[u] = i0 + 32 * u < o1 ? sep[i0 + 32 * u] : 0.0;
+        const T chim = spl_eval(chi_of_z, from_f64<T>(req_z_mean[q]));
+        T rmax = T(0);
+        for (;;) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) rmax = fmax(rmax, from_f64<T>(sv[u]));
+            i0 += 32 * U;
+            if (i0 >= o1) break;
+#pragma unroll
+            for (int u = 0; u < U; ++u) sv[u] = i0 + 32 * u < o1 ? sep[i0 + 32 * u] : 0.0;
+        }
+        for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+        T X = fmin(T(0.5) * rmax, fmin(chim - tab.c0, tab.cn - chim));
+        if (!(X > T(1e-3))) X = T(1e-3); // empty request or no room: its pairs are outside anyway
+        if (lane < 6) {
+            T g, fg;
+            chi_tab_eval(tab, fma(X, vinv.t[lane], chim), g, fg);
+            val[w][lane] = g;
+            val[w][6 + lane] = fg;
+        }
+        __syncwarp();
+        if (lane < 12) {
+            const int c = lane % 6, off = lane < 6 ? 0 : 6;
+            T acc = T(0);
+            for (int k = 0; k < 6; ++k) acc = fma(vinv.m[c][k], val[w][off + k], acc);
+            cof[w][lane] = acc;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            const T *c = cof[w];
+            BgFitT<T> o;
+            o.ge = mk4(c[0], c[2], c[4], T(1) / X);
+            o.go = mk4(c[1], c[3], c[5], chim);
+            o.fe = mk4(c[6], c[8], c[10], X);
+            o.fo = mk4(c[7], c[9], c[11], T(0));
+            fit[q] = o;
+        }
     }
-    for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-    T X = fmin(T(0.5) * rmax, fmin(chim - tab.c0, tab.cn - chim));
-    if (!(X > T(1e-3))) X = T(1e-3); // empty request or no room: its pairs are outside anyway
-    if (lane < 6) {
-        T g, fg;
-        chi_tab_eval(tab, fma(X, vinv.t[lane], chim), g, fg);
-        val[w][lane] = g;
-        val[w][6 + lane] = fg;
-    }
-    __syncwarp();
-    if (lane < 12) {
-        const int c = lane % 6, off = lane < 6 ? 0 : 6;
-        T acc = T(0);
-        for (int k = 0; k < 6; ++k) acc = fma(vinv.m[c][k], val[w][off + k], acc);
-        cof[w][lane] = acc;
-    }
-    __syncwarp();
-    if (lane == 0) {
-        const T *c = cof[w];
-        BgFitT<T> o;
-        o.ge = mk4(c[0], c[2], c[4], T(1) / X);
-        o.go = mk4(c[1], c[3], c[5], chim);
-        o.fe = mk4(c[6], c[8], c[10], X);
-        o.fo = mk4(c[7], c[9], c[11], T(0));
-        fit[q] = o;
-    }
+    // Launched right after the table kernel (programmatic dependent launch),
+    // this grid may run while the table kernel's last blocks do; every thread
+    // waits here for that kernel to complete and its writes to be visible, so
+    // that work ordered after this grid sees the tables.  (Launched after
+    // anything else, the wait returns at once.)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
 // the inverse Vandermonde matrix of the six Chebyshev points (host, FP64)
@@ -1841,9 +1848,21 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S
         tab.c0 = (T)ctx->chi_t0;
         tab.cn = (T)ctx->chi_tn;
         tab.inv_dc = (T)((CG_CHI_TAB - 1) / (ctx->chi_tn - ctx->chi_t0));
-        mp_bgfit_kernel<T, S><<<(a.n_req + MP_FIT_WARPS - 1) / MP_FIT_WARPS, 32 * MP_FIT_WARPS, 0,
-                                fs>>>(chi_of_z, tab, a.n_req, vinv, req_z_mean, req_offset, sep,
-                                      d_fit);
+        // on the library's stream it may start while the preceding table kernel
+        // finishes (programmatic dependent launch: that kernel signals once all
+        // its blocks are resident, and this one waits for its completion before
+        // it exits)
+        cudaLaunchConfig_t lc = {};
+        lc.gridDim = dim3((a.n_req + MP_FIT_WARPS - 1) / MP_FIT_WARPS);
+        lc.blockDim = dim3(32 * MP_FIT_WARPS);
+        lc.stream = fs;
+        cudaLaunchAttribute la[1];
+        la[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        la[0].val.programmaticStreamSerializationAllowed = 1;
+        lc.attrs = la;
+        lc.numAttrs = fs == ctx->stream ? 1 : 0;
+        CG_CUDA(ctx, cudaLaunchKernelEx(&lc, mp_bgfit_kernel<T, S>, chi_of_z, tab, a.n_req, vinv,
+                                        req_z_mean, req_offset, sep, d_fit));
         if ((st = cg_after_launch(ctx, "mp_bgfit_kernel"))) return st;
         if (ctx->prep_stream) {
             CG_CUDA(ctx, cudaEventRecord(ctx->copy_ev[1], fs));
