@@ -18,20 +18,8 @@ __device__ __forceinline__ f2 f2_pack(float lo, float hi)
     return r;
 }
 __device__ __forceinline__ f2 f2_dup(float x) { return f2_pack(x, x); }
-__device__ __forceinline__ float f2_lo(f2 a)
-{
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
-    (void)hi;
-    return lo;
-}
-__device__ __forceinline__ float f2_hi(f2 a)
-{
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
-    (void)lo;
-    return hi;
-}
+__device__ __forceinline__ float f2_lo(f2 a) { return __uint_as_float((unsigned)(a.v & 0xFFFFFFFFull)); }
+__device__ __forceinline__ float f2_hi(f2 a) { return __uint_as_float((unsigned)(a.v >> 32)); }
 __device__ __forceinline__ f2 f2_add(f2 a, f2 b)
 {
     f2 r;

@@ -928,10 +928,18 @@ template <typename T, typename S>
 __global__ void __launch_bounds__(32 * MP_FIT_WARPS)
     mp_bgfit_kernel(S chi_of_z, ChiTab<T> tab, int n_req, FitInvT<T> vinv,
                     const double *__restrict__ req_z_mean, const int64_t *__restrict__ req_offset,
-                    const double *__restrict__ sep, BgFitT<T> *__restrict__ fit)
+                    const double *__restrict__ sep, BgFitT<T> *__restrict__ fit,
+                    int *__restrict__ retry_count)
 {
     __shared__ T val[MP_FIT_WARPS][12];
     __shared__ T cof[MP_FIT_WARPS][12];
+    // the multipole kernel launched after this one with programmatic stream
+    // serialization may start (its node-table prologue) once every block of
+    // this grid has started; it waits for this grid's completion before it
+    // reads the fits.  The retry counter of that kernel starts at zero here
+    // (the last kernel that read it completed before this grid began).
+    asm volatile("griddepcontrol.launch_dependents;");
+    if (retry_count && blockIdx.x == 0 && threadIdx.x == 0) *retry_count = 0;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int q = blockIdx.x * MP_FIT_WARPS + w;
     if (q < n_req) { // whole warps
@@ -1334,6 +1342,10 @@ __global__ void __launch_bounds__(MP_FAST_MAX_THREADS, sizeof(T) == sizeof(float
     T *tab = reinterpret_cast<T *>(mp_smem);                           // [ROWS][R]
     double *stage = reinterpret_cast<double *>(tab + LY::COUNT);      // [blockDim][NL]
     for (int i = threadIdx.x; i < LY::COUNT; i += blockDim.x) tab[i] = nodes[i];
+    // launched as a dependent of the background fit: the fits (and, through
+    // the fit's own wait, the tables) are complete and visible after this
+    // (otherwise it returns at once)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     __syncthreads();
     const long long item0 = (long long)blockIdx.x * blockDim.x;
     const long long item = item0 + threadIdx.x;
@@ -1862,27 +1874,47 @@ int launch_fast(coffe_gpu_ctx *ctx, const MpArgs &a, const Bg<T, S> &bg, const S
         lc.attrs = la;
         lc.numAttrs = fs == ctx->stream ? 1 : 0;
         CG_CUDA(ctx, cudaLaunchKernelEx(&lc, mp_bgfit_kernel<T, S>, chi_of_z, tab, a.n_req, vinv,
-                                        req_z_mean, req_offset, sep, d_fit));
+                                        req_z_mean, req_offset, sep, d_fit, d_count));
         if ((st = cg_after_launch(ctx, "mp_bgfit_kernel"))) return st;
         if (ctx->prep_stream) {
             CG_CUDA(ctx, cudaEventRecord(ctx->copy_ev[1], fs));
             CG_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[1], 0));
         }
     }
+    // the first launch after the fit finds the retry counter zeroed by it and,
+    // when the fit ran on this stream, follows it as a programmatic dependent
+    // launch (the polynomial kernel); later launches (the tuner's candidates)
+    // clear the counter themselves
+    bool after_fit = true;
+    const bool dependent = !ctx->prep_stream && !ctx->timing;
     auto run = [&](const coffe_gpu_tuning_t &tu) -> int {
         const int lt = tu.lane_threads;
         const bool pack = can_pack && tu.lane_pack == 2 && !tu.lane_poly;
         const long long blocks = (total + (pack ? 2 : 1) * lt - 1) / ((pack ? 2 : 1) * lt);
-        CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
+        const bool first = after_fit;
+        after_fit = false;
+        if (!first) CG_CUDA(ctx, cudaMemsetAsync(d_count, 0, sizeof(int), ctx->stream));
 #define MP_FAST_U(NLV, CV, UV)                                                                    \
     if (tu.lane_poly) {                                                                           \
         const size_t smem = sizeof(T) * PolyLayout<NLV>::COUNT + sizeof(double) * NLV * lt;       \
         CG_CUDA(ctx, cudaFuncSetAttribute(mp_poly_kernel<NLV, CV, UV, T>,                         \
                                           cudaFuncAttributeMaxDynamicSharedMemorySize,            \
                                           (int)smem));                                            \
-        mp_poly_kernel<NLV, CV, UV, T><<<(unsigned)blocks, lt, smem, ctx->stream>>>(              \
-            a, d_fit, bg.z_of_chi.x0, bg.z_of_chi.xn, tab_x, tab_y, req_spectrum, req_z_mean,     \
-            req_offset, sep, total, (const T *)dnp, mom, out, d_count, d_retry, ctx->d_err);      \
+        cudaLaunchConfig_t lc = {};                                                               \
+        lc.gridDim = dim3((unsigned)blocks);                                                      \
+        lc.blockDim = dim3(lt);                                                                   \
+        lc.dynamicSmemBytes = smem;                                                               \
+        lc.stream = ctx->stream;                                                                  \
+        cudaLaunchAttribute la[1];                                                                \
+        la[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;                            \
+        la[0].val.programmaticStreamSerializationAllowed = 1;                                     \
+        lc.attrs = la;                                                                            \
+        lc.numAttrs = first && dependent ? 1 : 0;                                                 \
+        CG_CUDA(ctx, cudaLaunchKernelEx(&lc, mp_poly_kernel<NLV, CV, UV, T>, a, d_fit,            \
+                                        (T)bg.z_of_chi.x0, (T)bg.z_of_chi.xn, tab_x, tab_y,       \
+                                        req_spectrum, req_z_mean, req_offset, sep, total,         \
+                                        (const T *)dnp, mom, out, d_count, d_retry,               \
+                                        ctx->d_err));                                             \
     } else if (pack) {                                                                            \
         const size_t smem = sizeof(float) * Fast2Layout<NLV>::COUNT +                             \
                             sizeof(f2) * Fast2Layout<NLV>::ROWS * lt;                             \
