@@ -625,7 +625,8 @@ template <bool SWZ> __device__ __forceinline__ int fft_slot(int i, int sh)
 // odd.  RADIX 2: one stage per pass.  tw[j] = exp(-2 pi i j / (2M)), j <= M;
 // sign = -1 forward, +1 backward.
 template <int RADIX, bool SWZ>
-__device__ void smem_fft_df(float4 *buf, int logM, const float4 *__restrict__ tw, int sign)
+__device__ void smem_fft_df(float4 *buf, int logM, const float4 *__restrict__ tw, int sign,
+                            bool first_done = false)
 {
     const int M = 1 << logM;
     const int sh = logM > 6 ? logM - 6 : 0;
@@ -649,14 +650,16 @@ __device__ void smem_fft_df(float4 *buf, int logM, const float4 *__restrict__ tw
         return;
     }
     int st = 1;
-    if (logM & 1) {
-        for (int b = threadIdx.x; b < M / 2; b += blockDim.x) {
-            const int p0 = fft_slot<SWZ>(2 * b, sh), p1 = fft_slot<SWZ>(2 * b + 1, sh);
-            const dfc u = dfc_load(buf[p0]), v = dfc_load(buf[p1]);
-            buf[p0] = dfc_pack(dfc_add(u, v));
-            buf[p1] = dfc_pack(dfc_sub(u, v));
+    if (logM & 1) { // (first_done: the caller wrote the input with this stage applied)
+        if (!first_done) {
+            for (int b = threadIdx.x; b < M / 2; b += blockDim.x) {
+                const int p0 = fft_slot<SWZ>(2 * b, sh), p1 = fft_slot<SWZ>(2 * b + 1, sh);
+                const dfc u = dfc_load(buf[p0]), v = dfc_load(buf[p1]);
+                buf[p0] = dfc_pack(dfc_add(u, v));
+                buf[p1] = dfc_pack(dfc_sub(u, v));
+            }
+            __syncthreads();
         }
-        __syncthreads();
         st = 2;
     }
     for (; st < logM; st += 2) {
@@ -723,6 +726,36 @@ __device__ __forceinline__ dfl sample_input_df(const float2 *__restrict__ y,
     return df_mul(df_add(secant, dfl{corr, 0.f}), dfl{q.x, q.y});
 }
 
+// The forward input written with the first (twiddle-free) radix-2 stage of
+// smem_fft_df<4> applied, for odd logM: the complex points c and c + M/2
+// (real samples 2c, 2c + 1, 2c + M, 2c + M + 1) occupy the neighbouring
+// bit-reversed slots brev(c) and brev(c) + 1, so one thread samples both and
+// stores their sum and difference, the stage's operations on the same values,
+// without a pass over shared memory.  Returns whether a sample was not finite.
+template <bool SWZ>
+__device__ __forceinline__ bool fill_forward_r2(float4 *buf, int logM, const float2 *y,
+                                                const float *c, const int *__restrict__ idx,
+                                                const float2 *__restrict__ tdf,
+                                                const float4 *__restrict__ sf,
+                                                const float2 *__restrict__ qf)
+{
+    const int M = 1 << logM, sh = logM > 6 ? logM - 6 : 0;
+    bool bad = false;
+    for (int q = threadIdx.x; q < M / 2; q += blockDim.x) {
+        const dfl a0 = sample_input_df(y, c, idx, tdf, sf, qf, 2 * q);
+        const dfl a1 = sample_input_df(y, c, idx, tdf, sf, qf, 2 * q + 1);
+        const dfl b0 = sample_input_df(y, c, idx, tdf, sf, qf, 2 * q + M);
+        const dfl b1 = sample_input_df(y, c, idx, tdf, sf, qf, 2 * q + M + 1);
+        if (!isfinite(a0.hi) || !isfinite(a1.hi) || !isfinite(b0.hi) || !isfinite(b1.hi))
+            bad = true;
+        const dfc u{a0, a1}, v{b0, b1};
+        const int j0 = (int)(__brev((unsigned)q) >> (32 - logM)); // even
+        buf[fft_slot<SWZ>(j0, sh)] = dfc_pack(dfc_add(u, v));
+        buf[fft_slot<SWZ>(j0 + 1, sh)] = dfc_pack(dfc_sub(u, v));
+    }
+    return bad;
+}
+
 __device__ __forceinline__ void store_spec(float4 *p, dfc v) { *p = dfc_pack(v); }
 __device__ __forceinline__ void store_spec(float2 *p, dfc v)
 {
@@ -751,16 +784,21 @@ __global__ void fftlog_forward_df_kernel(GridPar g, const float2 *__restrict__ p
     const int sh = logM > 6 ? logM - 6 : 0;
     const float2 *y = pkdf + (size_t)s * g.nk;
     const float *c = cc32 + (size_t)s * g.nk;
+    const bool r2 = RADIX == 4 && (logM & 1);
     bool bad = false;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        const dfl d = sample_input_df(y, c, idx, tdf, sf32, qfac_df + (size_t)qi * N, i);
-        if (!isfinite(d.hi)) bad = true;
-        const int jj = fft_slot<SWZ>(__brev((unsigned)(i >> 1)) >> (32 - logM), sh);
-        buf2[2 * jj + (i & 1)] = make_float2(d.hi, d.lo);
+    if (r2) {
+        bad = fill_forward_r2<SWZ>(buf, logM, y, c, idx, tdf, sf32, qfac_df + (size_t)qi * N);
+    } else {
+        for (int i = threadIdx.x; i < N; i += blockDim.x) {
+            const dfl d = sample_input_df(y, c, idx, tdf, sf32, qfac_df + (size_t)qi * N, i);
+            if (!isfinite(d.hi)) bad = true;
+            const int jj = fft_slot<SWZ>(__brev((unsigned)(i >> 1)) >> (32 - logM), sh);
+            buf2[2 * jj + (i & 1)] = make_float2(d.hi, d.lo);
+        }
     }
     if (bad) cg_flag(err, CG_ERR_NONFINITE);
     __syncthreads();
-    smem_fft_df<RADIX, SWZ>(buf, logM, twdf, -1);
+    smem_fft_df<RADIX, SWZ>(buf, logM, twdf, -1, r2);
     OUT *out = spec + ((size_t)s * n_q + qi) * (M + 1);
     for (int k = threadIdx.x; k <= M; k += blockDim.x) {
         const dfc zk = dfc_load(buf[fft_slot<SWZ>(k & (M - 1), sh)]);
@@ -1208,15 +1246,21 @@ __global__ void __launch_bounds__(FUSED_THREADS, 2)
     }
     __syncthreads();
     // forward transform input (double-float sampling), bit-reversed
+    const bool r2 = RADIX == 4 && (logM & 1);
     bool bad = false;
-    for (int i = tid; i < N; i += bd) {
-        const dfl d = sample_input_df(ydf, cs, idx, tdf, sf32, qfac_df + (size_t)qi * N, i);
-        if (!isfinite(d.hi)) bad = true;
-        const int jj = fft_slot<SWZ>(__brev((unsigned)(i >> 1)) >> (32 - logM), sh);
-        fbuf2[2 * jj + (i & 1)] = make_float2(d.hi, d.lo);
+    if (r2) {
+        bad = fill_forward_r2<SWZ>(fbuf, logM, ydf, cs, idx, tdf, sf32,
+                                   qfac_df + (size_t)qi * N);
+    } else {
+        for (int i = tid; i < N; i += bd) {
+            const dfl d = sample_input_df(ydf, cs, idx, tdf, sf32, qfac_df + (size_t)qi * N, i);
+            if (!isfinite(d.hi)) bad = true;
+            const int jj = fft_slot<SWZ>(__brev((unsigned)(i >> 1)) >> (32 - logM), sh);
+            fbuf2[2 * jj + (i & 1)] = make_float2(d.hi, d.lo);
+        }
     }
     __syncthreads();
-    smem_fft_df<RADIX, SWZ>(fbuf, logM, twdf, -1);
+    smem_fft_df<RADIX, SWZ>(fbuf, logM, twdf, -1, r2);
     // half spectrum, rounded to float (phase 2 starts: the knots are dead)
     float2 *spec = reinterpret_cast<float2 *>(smem_raw);
     for (int k = tid; k <= M; k += bd) {
