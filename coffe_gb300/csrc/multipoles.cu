@@ -841,11 +841,13 @@ __global__ void __launch_bounds__(MP_LANE_THREADS)
 //  * background: D1 and f D1 along the line of sight of a request as one
 //    degree-5 polynomial each in t = x / X around the request's mean distance
 //    (chi = chi_mean + x, |x| <= X = half its largest separation, clamped to
-//    the background's range), interpolated at six Chebyshev points from the
-//    float background splines by mp_bgfit_kernel; a node evaluates the even and
-//    odd parts in t^2 (both ends from one evaluation, no loads).  Error: the
-//    interpolation's ~(X/L)^6 of the background's scale L ~ Gpc (1e-8 at
-//    X = 190 Mpc) plus the splines' float rounding, ~1e-7 relative;
+//    the background's range), interpolated at six Chebyshev points by
+//    mp_bgfit_kernel from the uniform chi table of (D1, f D1) (ChiTab, filled
+//    from the FP64 splines); a node evaluates the even and odd parts in t^2
+//    (both ends from one evaluation, no loads).  Error: the interpolation's
+//    ~(X/L)^6 of the background's scale L ~ Gpc (1e-8 at X = 190 Mpc), the
+//    table's linear interpolation (~5e-9) and float rounding (~1e-7 relative
+//    in the float kernels);
 //  * integrand: with G = D1 and F = f D1 at both ends, xi g1 g2 becomes
 //      G1 G2 I00 + F1 F2 R(c) + (G1 F2 + F1 G2)(I00 - 2 I02)/3
 //      + g I02 (G1 F2 chi1^2 + F1 G2 chi2^2),       g = (2 - s)(1 - mu^2)/D,
